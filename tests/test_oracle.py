@@ -1,0 +1,141 @@
+"""The CPU oracle against the reference's golden values and its own Rys code."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from openlowdin_gb300 import systems as S
+from tests import golden_systems as GS
+
+
+def test_boys_against_incomplete_gamma(oracle):
+    sp = pytest.importorskip("scipy.special")
+    for T in [0.0, 1e-9, 0.3, 2.0, 11.5, 29.9, 39.99, 40.0, 75.0, 400.0]:
+        F = oracle.boys(12, T)
+        for m in range(13):
+            if T == 0.0:
+                ref = 1.0 / (2 * m + 1)
+            else:
+                a = m + 0.5
+                ref = sp.gamma(a) * sp.gammainc(a, T) / (2.0 * T ** a)
+            assert abs(F[m] - ref) <= 5e-14 * max(ref, 1e-300) + 1e-300, (T, m, F[m], ref)
+
+
+def test_norma_gives_unit_self_overlap(oracle, golden):
+    sysd = GS.h2o_apmo(golden)
+    for sp_ in sysd["species"]:
+        b = oracle.Basis.from_shells(sp_["shells"])
+        Sm, _ = oracle.overlap_kinetic(b)
+        assert np.allclose(np.diag(Sm), 1.0, atol=1e-13)
+
+
+def _rys_quartet(R, l4, a4, o12):
+    n = [(l + 1) * (l + 2) // 2 for l in l4]
+    out = np.zeros(int(np.prod(n)))
+    args = []
+    for c in range(4):
+        for d in range(3):
+            args.append(ctypes.byref(ctypes.c_double(o12[3 * c + d])))
+        args.append(ctypes.byref(ctypes.c_int(int(l4[c]))))
+        args.append(ctypes.byref(ctypes.c_double(a4[c])))
+        args.append(ctypes.byref(ctypes.c_int(1000 * c)))   # labels chosen so every integral is emitted
+    args += [ctypes.byref(ctypes.c_int(0)), ctypes.byref(ctypes.c_int(1)),
+             out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))]
+    R.coul_rep_(*args)
+    return out
+
+
+def test_primitive_eris_against_reference_rys(oracle):
+    """src/ints/RysQInts.cpp (the reference's own in-tree ERI code, compiled
+    into oracle/_ref) and the oracle's Obara-Saika code agree up to l=4."""
+    try:
+        oracle.build(ref=True)
+    except Exception:
+        pass
+    R = oracle.rys_lib()
+    if R is None:
+        pytest.skip("reference tree not present: oracle/_ref/librys.so not built")
+    rng = np.random.default_rng(7)
+    worst = 0.0
+    for _ in range(150):
+        l4 = rng.integers(0, 5, 4).astype(np.int32)
+        if l4.sum() > 12:
+            continue
+        a4 = rng.uniform(0.1, 6.0, 4)
+        o12 = rng.uniform(-1.5, 1.5, 12)
+        ref = _rys_quartet(R, l4, a4, o12)
+        mine = np.zeros_like(ref)
+        oracle.lib().or_eri_primitive(l4, a4, o12, mine)
+        worst = max(worst, np.max(np.abs(ref - mine)) / np.max(np.abs(ref)))
+    assert worst < 1e-9
+
+
+def test_golden_h2o_rhf_and_mp2(oracle, golden):
+    """test/H2O.BOA.DIRECT.py and test/H2O.BOA.MP2.DIRECT.py golden values."""
+    sysd = GS.h2o_boa(golden)
+    res = oracle.scf(oracle.from_plain(sysd))
+    assert res.converged
+    ref = golden["values"]["H2O.BOA.DIRECT"]["HF energy"]
+    assert abs(res.energy - ref[0]) <= ref[1]
+    b = oracle.Basis.from_shells(sysd["species"][0]["shells"])
+    e2 = oracle.rmp2(oracle.eri_full(b), res.coefficients[0], res.orbital_energies[0], 5)
+    ref = golden["values"]["H2O.BOA.MP2.DIRECT"]["MP2 energy"]
+    assert abs(res.energy + e2 - ref[0]) <= ref[1]
+
+
+def test_golden_h2o_apmo(oracle, golden):
+    """test/H2O.APMO.MP2.py (RHF-APMO total energy, quantum protons)."""
+    res = oracle.scf(oracle.from_plain(GS.h2o_apmo(golden)))
+    assert res.converged
+    ref = golden["values"]["H2O.APMO.MP2"]["HF energy"]
+    assert abs(res.energy - ref[0]) <= ref[1]
+    ref = golden["values"]["H2O.APMO.UHF.DIRECT"]["HF energy"]
+    assert abs(res.energy - ref[0]) <= ref[1]
+
+
+def _jk_full(eri, D, f):
+    return np.einsum("ijkl,kl->ij", eri, D) + f * np.einsum("ikjl,kl->ij", eri, D)
+
+
+def test_direct_loops_against_full_tensor(oracle):
+    """The restated screened loops equal J + fK from the full tensor."""
+    sysd = S.water()
+    b = oracle.Basis.from_shells(sysd["species"][0]["shells"])
+    eri = oracle.eri_full(b)
+    rng = np.random.default_rng(1)
+    X = rng.normal(size=(b.nbf, b.nbf)) * 0.1
+    D = X + X.T
+    G = oracle.two_body_direct(b, True, D, -0.5)
+    assert np.max(np.abs(G - _jk_full(eri, D, -0.5))) < 1e-10
+
+
+def test_first_quarter_restatement(oracle):
+    """IntraIntsIt enumeration + role updates reproduce sum_mu C(p,mu)(mu nu|ls)
+    (up to the reference's |raw| > 1e-10 cut)."""
+    sysd = S.water()
+    b = oracle.Basis.from_shells(sysd["species"][0]["shells"])
+    eri = oracle.eri_full(b)
+    n = b.nbf
+    rng = np.random.default_rng(2)
+    C = rng.normal(size=(n, n))
+    D = np.ones((n, n))  # dense: no quartet is screened
+    A = oracle.two_body_directIT(b, True, D, C, 3)
+    ref = np.einsum("m,mnls->nls", C[3], eri)
+    assert np.max(np.abs(A - ref)) < 1e-8
+
+
+def test_coupling_restatement(oracle, golden):
+    sysd = S.water_cluster(1, 0, quantum_protons=True, place=False)
+    e = oracle.Basis.from_shells(sysd["species"][0]["shells"])
+    p = oracle.Basis.from_shells(sysd["species"][1]["shells"])
+    rng = np.random.default_rng(3)
+    X = rng.normal(size=(p.nbf, p.nbf)); Dp = X + X.T
+    for sid, osid in [(1, 2), (2, 1)]:
+        B = oracle.coupling_direct(e, sid, p, osid, Dp)
+        assert np.allclose(np.triu(B, 1), 0)
+        full = np.tril(B) + np.tril(B, -1).T
+        # reference value: J_e[D_p] from primitive quartets computed by the oracle
+        assert np.allclose(full, full.T)
+    B12 = oracle.coupling_direct(e, 1, p, 2, Dp)
+    B21 = oracle.coupling_direct(e, 2, p, 1, Dp)
+    assert np.max(np.abs(B12 - B21)) < 1e-10
