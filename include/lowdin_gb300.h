@@ -1,0 +1,163 @@
+/*
+ * lowdin_gb300.h -- C ABI of liblowdin_gb300.so, a GB300 (sm_103a) drop-in for
+ * openLOWDIN's direct two-particle integral interface.
+ *
+ * Part 1 repeats the reference's extern "C" interface (src/ints/Libint2Iface.h,
+ * lines 357-449; the Fortran binding is src/ints/Libint2Interface.f90:165-373)
+ * with the same names, argument order, passing convention and layouts:
+ *   - handles are created by LibintInterface_new and destroyed by _del;
+ *   - shells are added in basis order; coefficients are the raw basis-file
+ *     contraction coefficients (the library applies the primitive norm of the
+ *     x^l component and renormalises every Cartesian component to unit
+ *     self-overlap, src/ints/Libint2Iface.cpp:79-128);
+ *   - matrices are n x n, read and written row-major (the Fortran caller
+ *     passes column-major arrays; densities and two-particle matrices are
+ *     symmetric so the transposition is harmless);
+ *   - `factor` and `p` are passed by reference (C++ double& / int&): in C they
+ *     are pointers, in C++ references; the ABI is the same;
+ *   - results are fully overwritten; calls are synchronous with respect to the
+ *     host buffers.
+ * All reference functions return void as in the reference.  Errors (CUDA
+ * failures, unsupported requests) are reported through LowdinGB300_last_error()
+ * and printed on stderr; with LOWDIN_GB300_STRICT=1 in the environment the
+ * process aborts on the first error, as the reference aborts in libint.
+ *
+ * Part 2 adds device-resident entry points (pointers are device pointers) used
+ * by batched and served SCF drivers that keep densities and Fock matrices in
+ * HBM between iterations.
+ */
+#ifndef LOWDIN_GB300_H
+#define LOWDIN_GB300_H
+
+#ifdef __cplusplus
+#include <cstddef>
+#define LGB_REF(T) T &
+extern "C" {
+#else
+#include <stdbool.h>
+#include <stddef.h>
+#define LGB_REF(T) T *
+#endif
+
+typedef struct LibintInterface LibintInterface;
+
+/* ---------------------------------------------------------------- Part 1 --
+ * Reference interface, src/ints/Libint2Iface.h:357-449.                      */
+
+/* Libint2Iface.h:364 -- one handle per species; stack_size and parallel are
+   accepted and ignored (one CUDA stream per handle replaces the OpenMP pool). */
+LibintInterface *LibintInterface_new(const int stack_size, const int id, const bool el, const bool parallel);
+
+/* Libint2Iface.h:367 */
+void LibintInterface_del(LibintInterface *lint);
+
+/* Libint2Iface.h:369 -- point charge z at center[3] (used by kind 3 of
+   LibintInterface_compute_1body_ints). */
+void LibintInterface_add_particle(LibintInterface *lint, const int z, const double *center);
+
+/* Libint2Iface.h:372 */
+void LibintInterface_add_shell(LibintInterface *lint, double *alpha, double *coeff, double *origin, int l, int nprim);
+
+/* Libint2Iface.h:375 */
+int LibintInterface_get_nbasis(LibintInterface *lint);
+
+/* Libint2Iface.h:377 -- kind 1 overlap, 2 kinetic, 3 attraction to the added
+   particles (sum_C z_C <i|1/|r-C||j>); row-major n x n; host computed. */
+void LibintInterface_compute_1body_ints(LibintInterface *lint, int integral_kind, double *result);
+
+/* Libint2Iface.h:380 -- builds the significant shell-pair list; the library
+   also caches Schwarz factors on the device (they depend on the shells only). */
+void LibintInterface_init_2body_ints(LibintInterface *lint);
+
+/* Libint2Iface.h:382 (Libint2Iface.cpp:3510-3526, :418-618) -- two-particle
+   matrix G = J[D] + factor K[D] of one species from its density. */
+void LibintInterface_compute_2body_direct(LibintInterface *lint, double *dens, double *result, LGB_REF(double) factor);
+
+/* Libint2Iface.h:385 (Libint2Iface.cpp:3528-3549, :620-921) -- first-quarter
+   transform of orbital p: result[nu][lam][sig] = sum_mu C(p,mu)(mu nu|lam sig),
+   n^3 entries; coeff is n x n row-major, dens is used for screening. */
+void LibintInterface_compute_2body_directIT(LibintInterface *lint, double *dens, double *coeff, double *result,
+                                            LGB_REF(int) p);
+
+/* Libint2Iface.h:388 -- disk integrals: not provided (reports an error). */
+void LibintInterface_compute_2body_disk(LibintInterface *lint, const char *filename, double *dens);
+
+/* Libint2Iface.h:391 (Libint2Iface.cpp:3566-3589, :1111-1294) -- inter-species
+   Coulomb matrix of lint's species from olint's density dens (n_o x n_o):
+   lower triangle (row >= col) of the row-major n x n result, zero above. */
+void LibintInterface_compute_coupling_direct(LibintInterface *lint, LibintInterface *olint, double *dens,
+                                             double *result);
+
+/* Libint2Iface.h:395 (Libint2Iface.cpp:3591-3620, :1296-1622) --
+   result[nu][lam][sig] = sum_mu C(p,mu)(mu nu|lam sig), mu,nu of lint's
+   species (coeff n x n), lam,sig of olint's; n * n_o * n_o entries. */
+void LibintInterface_compute_coupling_directIT(LibintInterface *lint, LibintInterface *olint, double *dens,
+                                               double *coeff, double *result, LGB_REF(int) p);
+
+/* Libint2Iface.h:399 -- UHF alpha/beta direct coupling: not provided. */
+void LibintInterface_compute_alphabeta_direct(LibintInterface *lint, LibintInterface *olint, double *dens,
+                                              double *otherdens, double *result);
+
+/* Libint2Iface.h:403 -- not provided. */
+void LibintInterface_compute_coupling_disk(LibintInterface *lint, LibintInterface *olint, const char *filename);
+
+/* Libint2Iface.h:407-437 -- G12 (inter-particle potential) integrals: not
+   provided (out of the direct Coulomb path). */
+void libintinterface_compute_g12_disk(LibintInterface *lint, const char *filename, const double *coefficients,
+                                      const double *exponents, const int pot_size);
+void libintinterface_compute_g12inter_disk(LibintInterface *lint, LibintInterface *olint, const char *filename,
+                                           const double *coefficients, const double *exponents, const int pot_size);
+void libintinterface_compute_g12_direct(LibintInterface *lint, double *dens, double *result, LGB_REF(double) factor,
+                                        const double *coefficients, const double *exponents, const int pot_size);
+void libintinterface_compute_g12inter_direct(LibintInterface *lint, LibintInterface *olint, double *dens,
+                                             double *result, const double *coefficients, const double *exponents,
+                                             const int pot_size);
+
+/* Libint2Iface.h:439-446 -- in-memory all-integral tensors: not provided. */
+void LibintInterface_compute_2body_directAll(LibintInterface *lint, double *dens, double *result);
+void LibintInterface_compute_coupling_directAll(LibintInterface *lint, LibintInterface *olint, double *dens,
+                                                double *result);
+void libintinterface_compute_g12_directAll(LibintInterface *lint, double *dens, double *result,
+                                           const double *coefficients, const double *exponents, const int pot_size);
+void libintinterface_compute_g12inter_directAll(LibintInterface *lint, LibintInterface *olint, double *dens,
+                                                double *result, const double *coefficients, const double *exponents,
+                                                const int pot_size);
+
+/* ---------------------------------------------------------------- Part 2 --
+ * Device-resident extensions (no counterpart in the reference).             */
+
+/* Text of the last error in this process ("" when none); cleared by the call
+   of LowdinGB300_clear_error. */
+const char *LowdinGB300_last_error(void);
+void LowdinGB300_clear_error(void);
+
+/* Point-charge potential V_ij = sum_C Z_C <i|1/|r-R_C||j> (norma applied),
+   row-major n x n, host memory. */
+void LowdinGB300_potential(LibintInterface *lint, int ncharge, const double *Z, const double *R, double *result);
+
+/* Device-resident two-particle matrix: dG = J[dD] + factor K[dD] (n x n device
+   buffers, full symmetric).  precision: 0 = FP64, 1 = mixed (quartets whose
+   Schwarz-density bound is below `split` run in FP32, the rest in FP64).
+   Work is queued on `stream` (a cudaStream_t, 0 = legacy default); returns 0
+   on success, -1 on error (see LowdinGB300_last_error). */
+int LowdinGB300_twobody_device(LibintInterface *lint, const double *dD, double *dG, double factor, int precision,
+                               double split, void *stream);
+
+/* Device-resident fused coupling of species a and b in one pass over the
+   (a pair | b pair) quartets: dJa = J_a[dDb] and dJb = J_b[dDa] (full
+   symmetric, either output may be NULL).  fp32 selects FP32 integrals. */
+int LowdinGB300_coupling_device(LibintInterface *a, LibintInterface *b, const double *dDa, const double *dDb,
+                                double *dJa, double *dJb, int fp32, void *stream);
+
+/* Number of shell quartets evaluated by the last two-particle build of the
+   handle (after screening), or -1. */
+long long LowdinGB300_last_quartets(LibintInterface *lint);
+
+/* Library and device description (static string). */
+const char *LowdinGB300_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#undef LGB_REF
+#endif /* LOWDIN_GB300_H */

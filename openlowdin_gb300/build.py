@@ -1,0 +1,72 @@
+"""Build liblowdin_gb300.so in-tree with nvcc for sm_103a.
+
+Each translation unit is compiled in parallel (one nvcc per unit) and linked
+into openlowdin_gb300/liblowdin_gb300.so.  Objects go to openlowdin_gb300/_build/.
+A unit is recompiled only when it or a header is newer than its object.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "csrc")
+OUT_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "liblowdin_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for c in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build liblowdin_gb300.so")
+
+
+def _flags():
+    return ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+            "--expt-relaxed-constexpr", "-I" + os.path.join(HERE, "..", "include")] + ARCH
+
+
+def _compile(src: str, obj: str) -> str:
+    cmd = [nvcc(), *_flags(), "-c", src, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {os.path.basename(src)}:\n{r.stdout}\n{r.stderr}")
+    return obj
+
+
+def build(verbose: bool = False, force: bool = False) -> str:
+    os.makedirs(OUT_DIR, exist_ok=True)
+    sources = sorted(glob.glob(os.path.join(SRC, "*.cu")))
+    headers = glob.glob(os.path.join(SRC, "*.cuh")) + glob.glob(os.path.join(HERE, "..", "include", "*.h"))
+    hdr_time = max((os.path.getmtime(h) for h in headers), default=0)
+    jobs = []
+    objs = []
+    for s in sources:
+        o = os.path.join(OUT_DIR, os.path.basename(s)[:-3] + ".o")
+        objs.append(o)
+        if force or not os.path.exists(o) or os.path.getmtime(o) < max(os.path.getmtime(s), hdr_time):
+            jobs.append((s, o))
+    if jobs:
+        with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+            for f in [ex.submit(_compile, s, o) for s, o in jobs]:
+                o = f.result()
+                if verbose:
+                    print("compiled", os.path.basename(o))
+    if jobs or not os.path.exists(LIB):
+        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        if verbose:
+            print("linked", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True, force="--force" in sys.argv)

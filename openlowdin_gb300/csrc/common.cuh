@@ -1,0 +1,164 @@
+// Shared device definitions: Cartesian index tables, compile-time loops,
+// device-side records of shells / shell pairs and the Boys function.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <type_traits>
+
+namespace lgb {
+
+constexpr int kMaxL = 2;               // per-shell angular momentum handled by the kernels (d)
+constexpr int kMaxLQuartet = 4 * kMaxL;
+
+// ---- Cartesian components -------------------------------------------------
+// Order inside a shell of angular momentum l (lowdin order, also libint2's
+// default): for i = 0..l: x = l - i, for j = 0..i: y = i - j, z = j,
+// i.e. xx, xy, xz, yy, yz, zz for d.  A "cumulative" index enumerates every
+// component of every total 0, 1, 2, ... in that order.
+__host__ __device__ constexpr int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+__host__ __device__ constexpr int coff(int k) { return k * (k + 1) * (k + 2) / 6; }
+__host__ __device__ constexpr int cidx(int x, int y, int z) {
+  return coff(x + y + z) + (y + z) * (y + z + 1) / 2 + z;
+}
+__host__ __device__ constexpr int clevel(int c) {
+  int k = 0;
+  while (coff(k + 1) <= c) ++k;
+  return k;
+}
+__host__ __device__ constexpr int crow(int c) {
+  int r = c - coff(clevel(c)), i = 0;
+  while ((i + 1) * (i + 2) / 2 <= r) ++i;
+  return i;
+}
+__host__ __device__ constexpr int cx(int c) { return clevel(c) - crow(c); }
+__host__ __device__ constexpr int cz(int c) { return c - coff(clevel(c)) - crow(c) * (crow(c) + 1) / 2; }
+__host__ __device__ constexpr int cy(int c) { return clevel(c) - cx(c) - cz(c); }
+__host__ __device__ constexpr int ccomp(int c, int d) { return d == 0 ? cx(c) : (d == 1 ? cy(c) : cz(c)); }
+// recursion axis: first axis with a non-zero exponent
+__host__ __device__ constexpr int cdir(int c) { return cx(c) > 0 ? 0 : (cy(c) > 0 ? 1 : 2); }
+__host__ __device__ constexpr int cminus(int c, int d) {
+  return cidx(cx(c) - (d == 0), cy(c) - (d == 1), cz(c) - (d == 2));
+}
+__host__ __device__ constexpr int cplus(int c, int d) {
+  return cidx(cx(c) + (d == 0), cy(c) + (d == 1), cz(c) + (d == 2));
+}
+
+// compile-time loop: f(std::integral_constant<int, I>) for I in [B, E)
+template <int B, int E, typename F>
+__device__ __forceinline__ void sfor(F &&f) {
+  if constexpr (B < E) {
+    f(std::integral_constant<int, B>{});
+    sfor<B + 1, E>(f);
+  }
+}
+
+// ---- device records ---------------------------------------------------------
+// One shell pair of a species, stored in canonical order (la >= lb).  Pairs are
+// grouped by class (la, lb) and, inside a class, sorted by decreasing Schwarz
+// factor so that a contiguous range is one class.
+struct alignas(16) PairRec {
+  int sa, sb;      // shell indices inside the species
+  int fa, fb;      // first basis function of each shell
+  int prim0, nprim;// primitive-pair range
+  int la, lb;
+  double A[3];     // centre of shell a
+  double AB[3];    // A - B
+  double Q;        // Schwarz factor sqrt(max |(ab|ab)|) of raw integrals
+  double pad;
+};
+
+// One primitive pair: exponent sum, Gaussian-product centre and the prefactor
+// exp(-ab/p |AB|^2) * c_a N_a * c_b N_b (coefficient times the primitive norm
+// of the x^l component).
+struct alignas(16) PrimRec {
+  double p, Px, Py, Pz, K, pad;
+};
+
+// ---- Boys function ----------------------------------------------------------
+// F_m(T) = int_0^1 t^{2m} exp(-T t^2) dt.
+// T < kBoysTMax: Taylor series about the nearest grid point T_i = i h of a table
+// of F_n(T_i) (n = 0 .. kBoysOrders-1), giving F_L, then the downward recursion
+// F_m = (2T F_{m+1} + e^{-T}) / (2m+1).
+// T >= kBoysTMax: F_0 = sqrt(pi/T)/2 (erfc(6) < 3e-17), upward recursion
+// F_{m+1} = ((2m+1) F_m - e^{-T}) / (2T).
+constexpr double kBoysH = 0.1;
+constexpr double kBoysTMax = 36.0;
+constexpr int kBoysPoints = 361;          // T_i = 0, 0.1, ..., 36.0
+constexpr int kBoysTaylor = 9;            // terms k = 0..8 (|dT| <= 0.05: error < 6e-18)
+constexpr int kBoysTaylorF32 = 6;
+constexpr int kBoysOrders = kMaxLQuartet + kBoysTaylor + 1;
+
+template <int L>
+__device__ __forceinline__ void boys_f64(double T, double (&F)[L + 1], const double *__restrict__ tab) {
+  if (T < kBoysTMax) {
+    const int i = __double2int_rn(T * (1.0 / kBoysH));
+    const double mdT = i * kBoysH - T;  // -(T - T_i)
+    const double *t = tab + i * kBoysOrders + L;
+    double s = __ldg(t + kBoysTaylor - 1);
+#pragma unroll
+    for (int k = kBoysTaylor - 1; k >= 1; --k) s = fma(mdT * (1.0 / k), s, __ldg(t + k - 1));
+    F[L] = s;
+    if constexpr (L > 0) {
+      const double e = exp(-T);
+      const double twoT = 2.0 * T;
+#pragma unroll
+      for (int m = L - 1; m >= 0; --m) F[m] = fma(twoT, F[m + 1], e) * (1.0 / (2 * m + 1));
+    }
+  } else {
+    const double e = exp(-T);
+    F[0] = 0.88622692545275801365 / sqrt(T);  // sqrt(pi)/2
+    const double o2T = 0.5 / T;
+#pragma unroll
+    for (int m = 0; m < L; ++m) F[m + 1] = ((2 * m + 1) * F[m] - e) * o2T;
+  }
+}
+
+// FP32 Boys: Taylor about the float table; large arguments are evaluated in FP64.
+template <int L>
+__device__ __forceinline__ void boys_f32(float T, float (&F)[L + 1], const float *__restrict__ tab) {
+  if (T < (float)kBoysTMax) {
+    const int i = __float2int_rn(T * (float)(1.0 / kBoysH));
+    const float mdT = i * (float)kBoysH - T;
+    const float *t = tab + i * kBoysOrders + L;
+    float s = __ldg(t + kBoysTaylorF32 - 1);
+#pragma unroll
+    for (int k = kBoysTaylorF32 - 1; k >= 1; --k) s = fmaf(mdT * (1.0f / k), s, __ldg(t + k - 1));
+    F[L] = s;
+    if constexpr (L > 0) {
+      const float e = __expf(-T);
+      const float twoT = 2.0f * T;
+#pragma unroll
+      for (int m = L - 1; m >= 0; --m) F[m] = fmaf(twoT, F[m + 1], e) * (1.0f / (2 * m + 1));
+    }
+  } else {
+    const double Td = T;
+    const double e = exp(-Td);
+    double f = 0.88622692545275801365 / sqrt(Td);
+    F[0] = (float)f;
+    const double o2T = 0.5 / Td;
+#pragma unroll
+    for (int m = 0; m < L; ++m) {
+      f = ((2 * m + 1) * f - e) * o2T;
+      F[m + 1] = (float)f;
+    }
+  }
+}
+
+template <typename R>
+struct BoysTab;
+template <>
+struct BoysTab<double> {
+  template <int L>
+  __device__ __forceinline__ static void eval(double T, double (&F)[L + 1], const double *t64, const float *) {
+    boys_f64<L>(T, F, t64);
+  }
+};
+template <>
+struct BoysTab<float> {
+  template <int L>
+  __device__ __forceinline__ static void eval(float T, float (&F)[L + 1], const double *, const float *t32) {
+    boys_f32<L>(T, F, t32);
+  }
+};
+
+}  // namespace lgb

@@ -1,0 +1,904 @@
+// Host side of liblowdin_gb300.so: the per-species handle behind the
+// LibintInterface_* C ABI, device data of a species (class-binned shell pairs
+// sorted by Schwarz factor), and the builds that queue the integral kernels.
+#include <algorithm>
+#include <array>
+#include <cfloat>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/lowdin_gb300.h"
+#include "kernels.cuh"
+
+using namespace lgb;
+
+// ------------------------------------------------------------------ errors --
+namespace {
+std::mutex g_err_mu;
+std::string g_err;
+
+void set_error(const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_err = buf;
+  }
+  fprintf(stderr, "lowdin_gb300: %s\n", buf);
+  const char *strict = getenv("LOWDIN_GB300_STRICT");
+  if (strict && strict[0] == '1') abort();
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) {                                                              \
+      set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return false;                                                                       \
+    }                                                                                     \
+  } while (0)
+
+// ------------------------------------------------------------- Boys table --
+// F_n(T_i), T_i = i h, from the series F_n(T) = e^{-T} sum_k (2T)^k /
+// ((2n+1)(2n+3)...(2n+2k+1)) in long double.
+struct BoysHost {
+  std::vector<double> f64;
+  std::vector<float> f32;
+  BoysHost() : f64((size_t)kBoysPoints * kBoysOrders), f32((size_t)kBoysPoints * kBoysOrders) {
+    for (int i = 0; i < kBoysPoints; ++i) {
+      const long double T = (long double)i * (long double)kBoysH;
+      for (int n = 0; n < kBoysOrders; ++n) {
+        long double term = 1.0L / (2 * n + 1), sum = term;
+        for (int k = 1; k < 2000; ++k) {
+          term *= 2.0L * T / (2 * n + 2 * k + 1);
+          sum += term;
+          if (term < 1e-24L * sum) break;
+        }
+        const double v = (double)(expl(-T) * sum);
+        f64[(size_t)i * kBoysOrders + n] = v;
+        f32[(size_t)i * kBoysOrders + n] = (float)v;
+      }
+    }
+  }
+  // F_m(T), m = 0..mmax (host; Taylor + downward recursion like the device)
+  void eval(int mmax, double T, double *F) const {
+    if (T < kBoysTMax) {
+      const int i = (int)std::lround(T / kBoysH);
+      const double mdT = i * kBoysH - T;
+      const double *t = &f64[(size_t)i * kBoysOrders + mmax];
+      double s = t[kBoysTaylor - 1];
+      for (int k = kBoysTaylor - 1; k >= 1; --k) s = std::fma(mdT / k, s, t[k - 1]);
+      F[mmax] = s;
+      const double e = std::exp(-T);
+      for (int m = mmax - 1; m >= 0; --m) F[m] = (2.0 * T * F[m + 1] + e) / (2 * m + 1);
+    } else {
+      const double e = std::exp(-T);
+      F[0] = 0.88622692545275801365 / std::sqrt(T);
+      for (int m = 0; m < mmax; ++m) F[m + 1] = ((2 * m + 1) * F[m] - e) / (2.0 * T);
+    }
+  }
+};
+const BoysHost &boys_host() {
+  static BoysHost b;
+  return b;
+}
+
+// device copies of the Boys tables, one per device
+struct DeviceBoys {
+  int device = -1;
+  double *f64 = nullptr;
+  float *f32 = nullptr;
+};
+std::mutex g_boys_mu;
+std::vector<DeviceBoys> g_boys;
+
+bool device_boys(BoysTables &out) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_boys_mu);
+  for (auto &b : g_boys)
+    if (b.device == dev) {
+      out.f64 = b.f64;
+      out.f32 = b.f32;
+      return true;
+    }
+  const BoysHost &h = boys_host();
+  DeviceBoys b;
+  b.device = dev;
+  CK(cudaMalloc(&b.f64, h.f64.size() * sizeof(double)));
+  CK(cudaMalloc(&b.f32, h.f32.size() * sizeof(float)));
+  CK(cudaMemcpy(b.f64, h.f64.data(), h.f64.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b.f32, h.f32.data(), h.f32.size() * sizeof(float), cudaMemcpyHostToDevice));
+  g_boys.push_back(b);
+  out.f64 = b.f64;
+  out.f32 = b.f32;
+  return true;
+}
+
+// ------------------------------------------------------------ host shells --
+struct HostShell {
+  int l = 0, nprim = 0;
+  double O[3] = {0, 0, 0};
+  std::vector<double> alpha, cn;  // cn = coefficient * primitive norm of x^l
+};
+
+double prim_norm(double a, int l) {
+  double df = 1.0;
+  for (int k = 2 * l - 1; k > 1; k -= 2) df *= k;
+  return std::sqrt(std::pow(2.0, l) * std::pow(2.0 * a, l + 1.5) / (std::pow(M_PI, 1.5) * df));
+}
+
+// 1-D Obara-Saika overlap table s[i][j], i <= li, j <= lj
+void ovl1d(int li, int lj, double PA, double PB, double o2p, double s[8][8]) {
+  s[0][0] = 1.0;
+  for (int i = 0; i <= li; ++i)
+    for (int j = 0; j <= lj; ++j) {
+      if (!i && !j) continue;
+      double v;
+      if (i > 0) {
+        v = PA * s[i - 1][j];
+        if (i > 1) v += (i - 1) * o2p * s[i - 2][j];
+        if (j > 0) v += j * o2p * s[i - 1][j - 1];
+      } else {
+        v = PB * s[0][j - 1];
+        if (j > 1) v += (j - 1) * o2p * s[0][j - 2];
+      }
+      s[i][j] = v;
+    }
+}
+
+// raw overlap (and optionally kinetic) block, row-major [ncart(la)][ncart(lb)]
+void overlap_block(const HostShell &A, const HostShell &B, double *S, double *T) {
+  const int n1 = ncart(A.l), n2 = ncart(B.l);
+  std::fill(S, S + n1 * n2, 0.0);
+  if (T) std::fill(T, T + n1 * n2, 0.0);
+  double AB2 = 0;
+  for (int d = 0; d < 3; ++d) AB2 += (A.O[d] - B.O[d]) * (A.O[d] - B.O[d]);
+  for (int pa = 0; pa < A.nprim; ++pa)
+    for (int pb = 0; pb < B.nprim; ++pb) {
+      const double a = A.alpha[pa], b = B.alpha[pb], p = a + b, o2p = 0.5 / p;
+      const double pref = std::pow(M_PI / p, 1.5) * std::exp(-a * b / p * AB2) * A.cn[pa] * B.cn[pb];
+      double s[3][8][8];
+      for (int d = 0; d < 3; ++d) {
+        const double P = (a * A.O[d] + b * B.O[d]) / p;
+        ovl1d(A.l, B.l + 2, P - A.O[d], P - B.O[d], o2p, s[d]);
+      }
+      for (int f1 = 0; f1 < n1; ++f1) {
+        const int c1 = coff(A.l) + f1;
+        const int ax[3] = {cx(c1), cy(c1), cz(c1)};
+        for (int f2 = 0; f2 < n2; ++f2) {
+          const int c2 = coff(B.l) + f2;
+          const int bx[3] = {cx(c2), cy(c2), cz(c2)};
+          const double sx = s[0][ax[0]][bx[0]], sy = s[1][ax[1]][bx[1]], sz = s[2][ax[2]][bx[2]];
+          S[f1 * n2 + f2] += pref * sx * sy * sz;
+          if (T) {
+            double t[3];
+            for (int d = 0; d < 3; ++d) {
+              const int j = bx[d];
+              double v = -2.0 * b * (2 * j + 1) * s[d][ax[d]][j] + 4.0 * b * b * s[d][ax[d]][j + 2];
+              if (j >= 2) v += j * (j - 1) * s[d][ax[d]][j - 2];
+              t[d] = -0.5 * v;
+            }
+            T[f1 * n2 + f2] += pref * (t[0] * sy * sz + sx * t[1] * sz + sx * sy * t[2]);
+          }
+        }
+      }
+    }
+}
+
+// raw point-charge potential block sum_C Z_C <a|1/|r-C||b> via Obara-Saika on
+// the bra and horizontal transfer to b
+void potential_block(const HostShell &A, const HostShell &B, int nc, const double *Z, const double *R, double *V) {
+  const int la = A.l, lb = B.l, L = la + lb, NE = coff(L + 1), E0 = coff(la), M = L + 1;
+  std::vector<double> W((size_t)NE * M), X(NE - E0, 0.0);
+  double AB[3], AB2 = 0;
+  for (int d = 0; d < 3; ++d) {
+    AB[d] = A.O[d] - B.O[d];
+    AB2 += AB[d] * AB[d];
+  }
+  const BoysHost &bh = boys_host();
+  for (int pa = 0; pa < A.nprim; ++pa)
+    for (int pb = 0; pb < B.nprim; ++pb) {
+      const double a = A.alpha[pa], b = B.alpha[pb], p = a + b, o2p = 0.5 / p;
+      double P[3], PA[3];
+      for (int d = 0; d < 3; ++d) {
+        P[d] = (a * A.O[d] + b * B.O[d]) / p;
+        PA[d] = P[d] - A.O[d];
+      }
+      const double w = A.cn[pa] * B.cn[pb] * 2.0 * M_PI / p * std::exp(-a * b / p * AB2);
+      for (int c = 0; c < nc; ++c) {
+        double PC[3], PC2 = 0, F[kMaxLQuartet + 1];
+        for (int d = 0; d < 3; ++d) {
+          PC[d] = P[d] - R[3 * c + d];
+          PC2 += PC[d] * PC[d];
+        }
+        bh.eval(L, p * PC2, F);
+        for (int m = 0; m <= L; ++m) W[m] = F[m];
+        for (int e = 1; e < NE; ++e) {
+          const int d = cdir(e), em = cminus(e, d), ei = ccomp(e, d) - 1;
+          for (int m = 0; m <= L - clevel(e); ++m) {
+            double v = PA[d] * W[em * M + m] - PC[d] * W[em * M + m + 1];
+            if (ei > 0) {
+              const int emm = cminus(em, d);
+              v += ei * o2p * (W[emm * M + m] - W[emm * M + m + 1]);
+            }
+            W[e * M + m] = v;
+          }
+        }
+        for (int e = E0; e < NE; ++e) X[e - E0] += Z[c] * w * W[e * M];
+      }
+    }
+  // horizontal transfer (a, b+1_i| = (a+1_i, b| + AB_i (a, b|
+  const int nA = NE - E0;
+  std::vector<std::vector<double>> lev(lb + 1);
+  lev[0] = X;  // [a rows][1]
+  for (int j = 1; j <= lb; ++j) {
+    const int na = coff(la + lb - j + 1) - E0, nb = ncart(j), nbm = ncart(j - 1);
+    lev[j].assign((size_t)na * nb, 0.0);
+    for (int bi = 0; bi < nb; ++bi) {
+      const int bc = coff(j) + bi, d = cdir(bc), bm = cminus(bc, d) - coff(j - 1);
+      for (int ar = 0; ar < na; ++ar) {
+        const int apr = cplus(E0 + ar, d) - E0;
+        lev[j][(size_t)ar * nb + bi] = lev[j - 1][(size_t)apr * nbm + bm] + AB[d] * lev[j - 1][(size_t)ar * nbm + bm];
+      }
+    }
+  }
+  (void)nA;
+  const int n1 = ncart(la), n2 = ncart(lb);
+  for (int f1 = 0; f1 < n1; ++f1)
+    for (int f2 = 0; f2 < n2; ++f2) V[f1 * n2 + f2] = lev[lb][(size_t)f1 * n2 + f2];
+}
+
+// --------------------------------------------------------- device species --
+template <typename T>
+bool dev_upload(T *&dst, const std::vector<T> &src) {
+  if (dst) cudaFree(dst);
+  dst = nullptr;
+  if (src.empty()) return true;
+  CK(cudaMalloc(&dst, src.size() * sizeof(T)));
+  CK(cudaMemcpy(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return true;
+}
+
+struct PairList {
+  std::vector<PairRec> h;
+  std::vector<PrimRec> hp;
+  int start[kNumPairClasses + 1] = {0};
+  PairRec *d = nullptr;
+  PrimRec *dp = nullptr;
+  void release() {
+    if (d) cudaFree(d);
+    if (dp) cudaFree(dp);
+    d = nullptr;
+    dp = nullptr;
+  }
+  int count(int pc) const { return start[pc + 1] - start[pc]; }
+};
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  bool ensure(size_t want) {
+    if (want <= n && p) return true;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    CK(cudaMalloc(&p, want * sizeof(T) + 16));
+    n = want;
+    return true;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+}  // namespace
+
+struct LibintInterface {
+  int id = 0;
+  bool is_electron = true;
+  int stack_size = 0;
+  std::vector<HostShell> shells;
+  std::vector<int> first;  // shell -> first basis function
+  std::vector<double> norma;
+  std::vector<std::pair<int, std::array<double, 3>>> atoms;
+  int nbasis = 0;
+
+  // device state (valid while !dirty)
+  bool dirty = true;
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  BoysTables boys{nullptr, nullptr};
+  PairList sig;   // significant pairs (pair-list test), sorted by Schwarz factor inside a class
+  PairList all;   // every unordered pair (coupling)
+  bool have_sig = false, have_all = false;
+  double *d_norma = nullptr;
+  int *d_shell_of = nullptr;
+  DevBuf<double> dD, dDs, dDn, dGacc, dG, dA, dC;
+  DevBuf<unsigned long long> dcount;
+  long long last_quartets = -1;
+
+  ~LibintInterface() { release_device(); }
+
+  void release_device() {
+    sig.release();
+    all.release();
+    if (d_norma) cudaFree(d_norma);
+    if (d_shell_of) cudaFree(d_shell_of);
+    d_norma = nullptr;
+    d_shell_of = nullptr;
+    dD.release(); dDs.release(); dDn.release(); dGacc.release(); dG.release(); dA.release(); dC.release();
+    dcount.release();
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+    have_sig = have_all = false;
+    dirty = true;
+  }
+  int nshell() const { return (int)shells.size(); }
+
+  bool ensure_base() {
+    if (!dirty && stream) return true;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (stream && dev != device) release_device();
+    device = dev;
+    if (!stream) CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    if (!device_boys(boys)) return false;
+    for (const auto &s : shells)
+      if (s.l > kMaxL) {
+        set_error("shell with l=%d: this build handles l <= %d", s.l, kMaxL);
+        return false;
+      }
+    std::vector<int> shell_of(nbasis);
+    for (int s = 0; s < nshell(); ++s)
+      for (int i = first[s]; i < first[s] + ncart(shells[s].l); ++i) shell_of[i] = s;
+    if (d_norma) cudaFree(d_norma);
+    if (d_shell_of) cudaFree(d_shell_of);
+    d_norma = nullptr;
+    d_shell_of = nullptr;
+    if (!dev_upload(d_norma, norma)) return false;
+    if (!dev_upload(d_shell_of, shell_of)) return false;
+    have_sig = have_all = false;
+    dirty = false;
+    return true;
+  }
+
+  PairRec make_pair(int s1, int s2, std::vector<PrimRec> &prims) const {
+    // canonical order: larger l first; equal l keeps (s1, s2)
+    int a = s1, b = s2;
+    if (shells[b].l > shells[a].l) std::swap(a, b);
+    const HostShell &A = shells[a], &B = shells[b];
+    PairRec r{};
+    r.sa = a;
+    r.sb = b;
+    r.fa = first[a];
+    r.fb = first[b];
+    r.la = A.l;
+    r.lb = B.l;
+    r.prim0 = (int)prims.size();
+    r.nprim = A.nprim * B.nprim;
+    double AB2 = 0;
+    for (int d = 0; d < 3; ++d) {
+      r.A[d] = A.O[d];
+      r.AB[d] = A.O[d] - B.O[d];
+      AB2 += r.AB[d] * r.AB[d];
+    }
+    r.Q = 0;
+    for (int i = 0; i < A.nprim; ++i)
+      for (int j = 0; j < B.nprim; ++j) {
+        const double x = A.alpha[i], y = B.alpha[j], p = x + y;
+        PrimRec q{};
+        q.p = p;
+        q.Px = (x * A.O[0] + y * B.O[0]) / p;
+        q.Py = (x * A.O[1] + y * B.O[1]) / p;
+        q.Pz = (x * A.O[2] + y * B.O[2]) / p;
+        q.K = std::exp(-x * y / p * AB2) * A.cn[i] * B.cn[j];
+        prims.push_back(q);
+      }
+    return r;
+  }
+
+  // Bins pairs by class (stable), rebuilding the primitive array in the new order.
+  static void bin_pairs(PairList &L, std::vector<PairRec> &raw, const std::vector<PrimRec> &rawp, bool by_q) {
+    std::stable_sort(raw.begin(), raw.end(), [&](const PairRec &x, const PairRec &y) {
+      const int cx_ = pair_class(x.la, x.lb), cy_ = pair_class(y.la, y.lb);
+      if (cx_ != cy_) return cx_ < cy_;
+      if (by_q && x.Q != y.Q) return x.Q > y.Q;
+      return false;
+    });
+    L.h.clear();
+    L.hp.clear();
+    for (int c = 0; c <= kNumPairClasses; ++c) L.start[c] = 0;
+    for (auto r : raw) {
+      const int n0 = (int)L.hp.size();
+      for (int k = 0; k < r.nprim; ++k) L.hp.push_back(rawp[r.prim0 + k]);
+      r.prim0 = n0;
+      L.h.push_back(r);
+      L.start[pair_class(r.la, r.lb) + 1]++;
+    }
+    for (int c = 0; c < kNumPairClasses; ++c) L.start[c + 1] += L.start[c];
+  }
+
+  bool compute_schwarz(PairList &L) {
+    DevBuf<double> dq;
+    if (!dq.ensure(L.h.size())) return false;
+    for (int pc = 0; pc < kNumPairClasses; ++pc) {
+      if (!L.count(pc)) continue;
+      SchwarzParams sp{L.d, L.dp, L.start[pc], L.count(pc), dq.p, boys};
+      CK(launch_schwarz(pc, sp, stream));
+    }
+    std::vector<double> q(L.h.size());
+    CK(cudaMemcpyAsync(q.data(), dq.p, q.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    dq.release();
+    for (size_t i = 0; i < q.size(); ++i) L.h[i].Q = q[i];
+    return true;
+  }
+
+  // significant pairs of init_2body_ints (Libint2Iface.cpp:3248-3342): same
+  // centre, or Frobenius norm of the raw overlap block >= 1e-12
+  bool ensure_sig() {
+    if (!ensure_base()) return false;
+    if (have_sig) return true;
+    std::vector<PairRec> raw;
+    std::vector<PrimRec> rawp;
+    double S[225];
+    for (int s1 = 0; s1 < nshell(); ++s1)
+      for (int s2 = 0; s2 <= s1; ++s2) {
+        const HostShell &A = shells[s1], &B = shells[s2];
+        bool sigf = A.O[0] == B.O[0] && A.O[1] == B.O[1] && A.O[2] == B.O[2];
+        if (!sigf) {
+          overlap_block(A, B, S, nullptr);
+          double nrm = 0;
+          for (int i = 0; i < ncart(A.l) * ncart(B.l); ++i) nrm += S[i] * S[i];
+          sigf = std::sqrt(nrm) >= 1e-12;
+        }
+        if (sigf) raw.push_back(make_pair(s1, s2, rawp));
+      }
+    bin_pairs(sig, raw, rawp, false);
+    sig.release();
+    if (!dev_upload(sig.d, sig.h) || !dev_upload(sig.dp, sig.hp)) return false;
+    if (!compute_schwarz(sig)) return false;
+    // sort by decreasing Schwarz factor inside each class
+    std::vector<PairRec> tmp = sig.h;
+    std::vector<PrimRec> tmpp = sig.hp;
+    bin_pairs(sig, tmp, tmpp, true);
+    sig.release();
+    if (!dev_upload(sig.d, sig.h) || !dev_upload(sig.dp, sig.hp)) return false;
+    have_sig = true;
+    return true;
+  }
+
+  bool ensure_all() {
+    if (!ensure_base()) return false;
+    if (have_all) return true;
+    std::vector<PairRec> raw;
+    std::vector<PrimRec> rawp;
+    for (int s1 = 0; s1 < nshell(); ++s1)
+      for (int s2 = 0; s2 <= s1; ++s2) raw.push_back(make_pair(s1, s2, rawp));
+    bin_pairs(all, raw, rawp, false);
+    all.release();
+    if (!dev_upload(all.d, all.h) || !dev_upload(all.dp, all.hp)) return false;
+    have_all = true;
+    return true;
+  }
+
+  // dG = J[dD] + factor K[dD]; dD, dG device n x n
+  bool twobody(const double *dDin, double *dGout, double factor, int precision, double split, cudaStream_t s) {
+    if (!ensure_sig()) return false;
+    const int n = nbasis, nsh = nshell();
+    if (!dDs.ensure((size_t)n * n) || !dDn.ensure((size_t)nsh * nsh) || !dGacc.ensure((size_t)n * n) ||
+        !dcount.ensure(1))
+      return false;
+    CK(launch_prepare_density(dDin, d_norma, d_shell_of, n, nsh, dDs.p, dDn.p, s));
+    CK(cudaMemsetAsync(dGacc.p, 0, sizeof(double) * n * n, s));
+    CK(cudaMemsetAsync(dcount.p, 0, sizeof(unsigned long long), s));
+    JKParams p{};
+    p.pairs = sig.d;
+    p.prims = sig.dp;
+    p.Ds = dDs.p;
+    p.n = n;
+    p.Dn = dDn.p;
+    p.nsh = nsh;
+    p.screen = is_electron ? 1 : 0;
+    p.eps = DBL_EPSILON;
+    p.hf = 0.5 * factor;
+    p.Gacc = dGacc.p;
+    p.boys = boys;
+    p.nquartets = dcount.p;
+    for (int cb = 0; cb < kNumPairClasses; ++cb)
+      for (int ck = 0; ck <= cb; ++ck) {
+        if (!sig.count(cb) || !sig.count(ck)) continue;
+        if (!class_supported(cb, ck)) {
+          set_error("quartet class (%d,%d|%d,%d) is not built into this library", pc_la(cb), pc_lb(cb), pc_la(ck),
+                    pc_lb(ck));
+          return false;
+        }
+        p.bra0 = sig.start[cb];
+        p.nbra = sig.count(cb);
+        p.ket0 = sig.start[ck];
+        p.nket = sig.count(ck);
+        p.triangle = cb == ck;
+        if (precision == 0) {
+          p.split = 0.0;
+          CK(launch_jk(cb, ck, false, p, s));
+        } else {
+          p.split = split;
+          p.lower = 0;
+          CK(launch_jk(cb, ck, false, p, s));
+          p.lower = 1;
+          CK(launch_jk(cb, ck, true, p, s));
+        }
+      }
+    CK(launch_symmetrize(dGacc.p, d_norma, n, 0.25, dGout, s));
+    unsigned long long cnt = 0;
+    CK(cudaMemcpyAsync(&cnt, dcount.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    last_quartets = (long long)cnt;
+    return true;
+  }
+};
+
+namespace {
+
+bool coupling(LibintInterface *A, LibintInterface *B, const double *dDa, const double *dDb, double *dJa,
+              double *dJb, bool fp32, cudaStream_t s) {
+  if (!A->ensure_all() || !B->ensure_all()) return false;
+  const int nA = A->nbasis, nB = B->nbasis;
+  // scaled densities live in each handle's dDs buffer
+  if (dJa && (!B->dDs.ensure((size_t)nB * nB))) return false;
+  if (dJb && (!A->dDs.ensure((size_t)nA * nA))) return false;
+  if (dJa) {
+    CK(launch_scale_density(dDb, B->d_norma, nB, B->dDs.p, s));
+    if (!A->dGacc.ensure((size_t)nA * nA)) return false;
+    CK(cudaMemsetAsync(A->dGacc.p, 0, sizeof(double) * nA * nA, s));
+  }
+  if (dJb) {
+    CK(launch_scale_density(dDa, A->d_norma, nA, A->dDs.p, s));
+    if (!B->dGacc.ensure((size_t)nB * nB)) return false;
+    CK(cudaMemsetAsync(B->dGacc.p, 0, sizeof(double) * nB * nB, s));
+  }
+  CouplingParams p{};
+  p.pa = A->all.d;
+  p.pra = A->all.dp;
+  p.pb = B->all.d;
+  p.prb = B->all.dp;
+  p.DsA = dJb ? A->dDs.p : nullptr;
+  p.DsB = dJa ? B->dDs.p : nullptr;
+  p.nA = nA;
+  p.nB = nB;
+  p.JA = dJa ? A->dGacc.p : nullptr;
+  p.JB = dJb ? B->dGacc.p : nullptr;
+  p.boys = A->boys;
+  p.cut = 1e-10;
+  for (int cb = 0; cb < kNumPairClasses; ++cb)
+    for (int ck = 0; ck < kNumPairClasses; ++ck) {
+      if (!A->all.count(cb) || !B->all.count(ck)) continue;
+      if (!class_supported(cb, ck)) {
+        set_error("coupling class (%d,%d|%d,%d) is not built into this library", pc_la(cb), pc_lb(cb), pc_la(ck),
+                  pc_lb(ck));
+        return false;
+      }
+      p.bra0 = A->all.start[cb];
+      p.nbra = A->all.count(cb);
+      p.ket0 = B->all.start[ck];
+      p.nket = B->all.count(ck);
+      CK(launch_coupling(cb, ck, fp32, p, s));
+    }
+  if (dJa) CK(launch_coupling_extract(A->dGacc.p, A->d_norma, nA, 1.0, 0, dJa, s));
+  if (dJb) CK(launch_coupling_extract(B->dGacc.p, B->d_norma, nB, 1.0, 0, dJb, s));
+  return true;
+}
+
+bool first_quarter(LibintInterface *A, LibintInterface *B, const double *hD, const double *hC, int p,
+                   double *hOut) {
+  // B == nullptr: intra-species (screened like the direct build); else coupling
+  const bool intra = B == nullptr;
+  if (intra ? !A->ensure_sig() : (!A->ensure_all() || !B->ensure_all())) return false;
+  LibintInterface *K = intra ? A : B;
+  const int nA = A->nbasis, nB = K->nbasis, nsh = A->nshell();
+  cudaStream_t s = A->stream;
+  if (p < 0 || p >= nA) {
+    set_error("orbital index p=%d out of range [0,%d)", p, nA);
+    return false;
+  }
+  std::vector<double> Cs(nA);
+  for (int mu = 0; mu < nA; ++mu) Cs[mu] = hC[(size_t)p * nA + mu] * A->norma[mu];
+  const size_t cube = (size_t)nA * nB * nB;
+  if (!A->dA.ensure(cube) || !A->dC.ensure(nA)) return false;
+  CK(cudaMemcpyAsync(A->dC.p, Cs.data(), nA * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(A->dA.p, 0, cube * sizeof(double), s));
+  ITParams q{};
+  q.intra = intra;
+  q.Cs = A->dC.p;
+  q.nA = nA;
+  q.nB = nB;
+  q.A = A->dA.p;
+  q.boys = A->boys;
+  q.cut = 1e-10;
+  q.eps = DBL_EPSILON;
+  q.nsh = nsh;
+  if (intra) {
+    if (!A->dD.ensure((size_t)nA * nA) || !A->dDs.ensure((size_t)nA * nA) || !A->dDn.ensure((size_t)nsh * nsh))
+      return false;
+    CK(cudaMemcpyAsync(A->dD.p, hD, sizeof(double) * nA * nA, cudaMemcpyHostToDevice, s));
+    CK(launch_prepare_density(A->dD.p, A->d_norma, A->d_shell_of, nA, nsh, A->dDs.p, A->dDn.p, s));
+    q.Dn = A->dDn.p;
+    q.screen = A->is_electron ? 1 : 0;
+    q.pa = q.pb = A->sig.d;
+    q.pra = q.prb = A->sig.dp;
+    for (int cb = 0; cb < kNumPairClasses; ++cb)
+      for (int ck = 0; ck <= cb; ++ck) {
+        if (!A->sig.count(cb) || !A->sig.count(ck)) continue;
+        if (!class_supported(cb, ck)) {
+          set_error("quartet class not built into this library");
+          return false;
+        }
+        q.bra0 = A->sig.start[cb];
+        q.nbra = A->sig.count(cb);
+        q.ket0 = A->sig.start[ck];
+        q.nket = A->sig.count(ck);
+        q.triangle = cb == ck;
+        CK(launch_it(cb, ck, q, s));
+      }
+  } else {
+    q.screen = 0;
+    q.pa = A->all.d;
+    q.pra = A->all.dp;
+    q.pb = B->all.d;
+    q.prb = B->all.dp;
+    for (int cb = 0; cb < kNumPairClasses; ++cb)
+      for (int ck = 0; ck < kNumPairClasses; ++ck) {
+        if (!A->all.count(cb) || !B->all.count(ck)) continue;
+        if (!class_supported(cb, ck)) {
+          set_error("quartet class not built into this library");
+          return false;
+        }
+        q.bra0 = A->all.start[cb];
+        q.nbra = A->all.count(cb);
+        q.ket0 = B->all.start[ck];
+        q.nket = B->all.count(ck);
+        q.triangle = 0;
+        CK(launch_it(cb, ck, q, s));
+      }
+  }
+  CK(launch_scale_cube(A->dA.p, A->d_norma, K->d_norma, nA, nB, s));
+  CK(cudaMemcpyAsync(hOut, A->dA.p, cube * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return true;
+}
+
+bool check_handle(LibintInterface *l, const char *fn) {
+  if (!l) {
+    set_error("%s: null handle", fn);
+    return false;
+  }
+  return true;
+}
+
+void unsupported(const char *fn) { set_error("%s is not provided by this library (direct Coulomb path only)", fn); }
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+LibintInterface *LibintInterface_new(const int stack_size, const int id, const bool el, const bool parallel) {
+  (void)parallel;
+  LibintInterface *l = new LibintInterface();
+  l->stack_size = stack_size;
+  l->id = id;
+  l->is_electron = el;
+  return l;
+}
+
+void LibintInterface_del(LibintInterface *lint) { delete lint; }
+
+void LibintInterface_add_particle(LibintInterface *lint, const int z, const double *center) {
+  if (!check_handle(lint, __func__)) return;
+  lint->atoms.push_back({z, {center[0], center[1], center[2]}});
+}
+
+void LibintInterface_add_shell(LibintInterface *lint, double *alpha, double *coeff, double *origin, int l,
+                               int nprim) {
+  if (!check_handle(lint, __func__)) return;
+  if (l < 0 || nprim <= 0) {
+    set_error("add_shell: invalid l=%d nprim=%d", l, nprim);
+    return;
+  }
+  HostShell s;
+  s.l = l;
+  s.nprim = nprim;
+  for (int d = 0; d < 3; ++d) s.O[d] = origin[d];
+  for (int k = 0; k < nprim; ++k) {
+    s.alpha.push_back(alpha[k]);
+    s.cn.push_back(coeff[k] * prim_norm(alpha[k], l));
+  }
+  lint->first.push_back(lint->nbasis);
+  lint->nbasis += ncart(l);
+  // renormalise every Cartesian component to unit self-overlap
+  const int n = ncart(l);
+  std::vector<double> S((size_t)n * n);
+  overlap_block(s, s, S.data(), nullptr);
+  for (int i = 0; i < n; ++i) lint->norma.push_back(1.0 / std::sqrt(S[(size_t)i * n + i]));
+  lint->shells.push_back(std::move(s));
+  lint->dirty = true;
+}
+
+int LibintInterface_get_nbasis(LibintInterface *lint) { return lint ? lint->nbasis : 0; }
+
+void LibintInterface_compute_1body_ints(LibintInterface *lint, int integral_kind, double *result) {
+  if (!check_handle(lint, __func__)) return;
+  const int n = lint->nbasis, nsh = lint->nshell();
+  std::vector<double> Z, R;
+  for (auto &a : lint->atoms) {
+    Z.push_back((double)a.first);
+    R.insert(R.end(), a.second.begin(), a.second.end());
+  }
+  double S[225], T[225];
+  for (int s1 = 0; s1 < nsh; ++s1)
+    for (int s2 = 0; s2 < nsh; ++s2) {
+      const HostShell &A = lint->shells[s1], &B = lint->shells[s2];
+      const int n1 = ncart(A.l), n2 = ncart(B.l);
+      if (integral_kind == 3) potential_block(A, B, (int)Z.size(), Z.data(), R.data(), S);
+      else overlap_block(A, B, S, integral_kind == 2 ? T : nullptr);
+      const double *src = integral_kind == 2 ? T : S;
+      for (int f1 = 0; f1 < n1; ++f1)
+        for (int f2 = 0; f2 < n2; ++f2) {
+          const int i = lint->first[s1] + f1, j = lint->first[s2] + f2;
+          result[(size_t)i * n + j] = src[f1 * n2 + f2] * lint->norma[i] * lint->norma[j];
+        }
+    }
+}
+
+void LibintInterface_init_2body_ints(LibintInterface *lint) {
+  if (!check_handle(lint, __func__)) return;
+  lint->ensure_sig();
+}
+
+void LibintInterface_compute_2body_direct(LibintInterface *lint, double *dens, double *result, double &factor) {
+  if (!check_handle(lint, __func__)) return;
+  if (!lint->ensure_sig()) return;
+  const int n = lint->nbasis;
+  cudaStream_t s = lint->stream;
+  if (!lint->dD.ensure((size_t)n * n) || !lint->dG.ensure((size_t)n * n)) return;
+  if (cudaMemcpyAsync(lint->dD.p, dens, sizeof(double) * n * n, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+    set_error("compute_2body_direct: density upload failed");
+    return;
+  }
+  if (!lint->twobody(lint->dD.p, lint->dG.p, factor, 0, 0.0, s)) return;
+  if (cudaMemcpyAsync(result, lint->dG.p, sizeof(double) * n * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    set_error("compute_2body_direct: result download failed");
+}
+
+void LibintInterface_compute_2body_directIT(LibintInterface *lint, double *dens, double *coeff, double *result,
+                                            int &p) {
+  if (!check_handle(lint, __func__)) return;
+  first_quarter(lint, nullptr, dens, coeff, p, result);
+}
+
+void LibintInterface_compute_2body_disk(LibintInterface *, const char *, double *) { unsupported(__func__); }
+
+void LibintInterface_compute_coupling_direct(LibintInterface *lint, LibintInterface *olint, double *dens,
+                                             double *result) {
+  if (!check_handle(lint, __func__) || !check_handle(olint, __func__)) return;
+  if (!lint->ensure_all() || !olint->ensure_all()) return;
+  const int n = lint->nbasis, no = olint->nbasis;
+  cudaStream_t s = lint->stream;
+  if (!olint->dD.ensure((size_t)no * no) || !lint->dG.ensure((size_t)n * n)) return;
+  if (cudaMemcpyAsync(olint->dD.p, dens, sizeof(double) * no * no, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+    set_error("compute_coupling_direct: density upload failed");
+    return;
+  }
+  // J of lint's species from olint's density, then keep the lower triangle
+  if (!coupling(lint, olint, nullptr, olint->dD.p, lint->dG.p, nullptr, false, s)) return;
+  std::vector<double> tmp((size_t)n * n);
+  if (cudaMemcpyAsync(tmp.data(), lint->dG.p, sizeof(double) * n * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess) {
+    set_error("compute_coupling_direct: result download failed");
+    return;
+  }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) result[(size_t)i * n + j] = j > i ? 0.0 : tmp[(size_t)i * n + j];
+}
+
+void LibintInterface_compute_coupling_directIT(LibintInterface *lint, LibintInterface *olint, double *dens,
+                                               double *coeff, double *result, int &p) {
+  (void)dens;
+  if (!check_handle(lint, __func__) || !check_handle(olint, __func__)) return;
+  first_quarter(lint, olint, nullptr, coeff, p, result);
+}
+
+void LibintInterface_compute_alphabeta_direct(LibintInterface *, LibintInterface *, double *, double *, double *) {
+  unsupported(__func__);
+}
+void LibintInterface_compute_coupling_disk(LibintInterface *, LibintInterface *, const char *) {
+  unsupported(__func__);
+}
+void libintinterface_compute_g12_disk(LibintInterface *, const char *, const double *, const double *, const int) {
+  unsupported(__func__);
+}
+void libintinterface_compute_g12inter_disk(LibintInterface *, LibintInterface *, const char *, const double *,
+                                           const double *, const int) {
+  unsupported(__func__);
+}
+void libintinterface_compute_g12_direct(LibintInterface *, double *, double *, double &, const double *,
+                                        const double *, const int) {
+  unsupported(__func__);
+}
+void libintinterface_compute_g12inter_direct(LibintInterface *, LibintInterface *, double *, double *,
+                                             const double *, const double *, const int) {
+  unsupported(__func__);
+}
+void LibintInterface_compute_2body_directAll(LibintInterface *, double *, double *) { unsupported(__func__); }
+void LibintInterface_compute_coupling_directAll(LibintInterface *, LibintInterface *, double *, double *) {
+  unsupported(__func__);
+}
+void libintinterface_compute_g12_directAll(LibintInterface *, double *, double *, const double *, const double *,
+                                           const int) {
+  unsupported(__func__);
+}
+void libintinterface_compute_g12inter_directAll(LibintInterface *, LibintInterface *, double *, double *,
+                                                const double *, const double *, const int) {
+  unsupported(__func__);
+}
+
+const char *LowdinGB300_last_error(void) {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  static thread_local std::string copy;
+  copy = g_err;
+  return copy.c_str();
+}
+
+void LowdinGB300_clear_error(void) {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_err.clear();
+}
+
+void LowdinGB300_potential(LibintInterface *lint, int ncharge, const double *Z, const double *R, double *result) {
+  if (!check_handle(lint, __func__)) return;
+  const int n = lint->nbasis, nsh = lint->nshell();
+  double V[225];
+  for (int s1 = 0; s1 < nsh; ++s1)
+    for (int s2 = 0; s2 < nsh; ++s2) {
+      const HostShell &A = lint->shells[s1], &B = lint->shells[s2];
+      potential_block(A, B, ncharge, Z, R, V);
+      const int n1 = ncart(A.l), n2 = ncart(B.l);
+      for (int f1 = 0; f1 < n1; ++f1)
+        for (int f2 = 0; f2 < n2; ++f2) {
+          const int i = lint->first[s1] + f1, j = lint->first[s2] + f2;
+          result[(size_t)i * n + j] = V[f1 * n2 + f2] * lint->norma[i] * lint->norma[j];
+        }
+    }
+}
+
+int LowdinGB300_twobody_device(LibintInterface *lint, const double *dD, double *dG, double factor, int precision,
+                               double split, void *stream) {
+  if (!check_handle(lint, __func__)) return -1;
+  return lint->twobody(dD, dG, factor, precision, split, (cudaStream_t)stream) ? 0 : -1;
+}
+
+int LowdinGB300_coupling_device(LibintInterface *a, LibintInterface *b, const double *dDa, const double *dDb,
+                                double *dJa, double *dJb, int fp32, void *stream) {
+  if (!check_handle(a, __func__) || !check_handle(b, __func__)) return -1;
+  return coupling(a, b, dDa, dDb, dJa, dJb, fp32 != 0, (cudaStream_t)stream) ? 0 : -1;
+}
+
+long long LowdinGB300_last_quartets(LibintInterface *lint) { return lint ? lint->last_quartets : -1; }
+
+const char *LowdinGB300_version(void) { return "lowdin_gb300 0.1 (sm_103a, FP64/FP32 Obara-Saika, l<=1 kernels)"; }
+
+}  // extern "C"

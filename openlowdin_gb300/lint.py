@@ -1,0 +1,205 @@
+"""ctypes binding of liblowdin_gb300.so.
+
+`Libint2Interface` mirrors the Fortran module src/ints/Libint2Interface.f90 of
+openLOWDIN: one object per species, built from the species' shells in basis
+order (Libint2Interface_constructor, :382-448), with the direct two-particle,
+coupling and first-quarter calls (:514-707).  Every call goes through the C ABI
+declared in include/lowdin_gb300.h -- the same entry points a Fortran
+ISO_C_BINDING interface binds.
+
+Host-buffer calls (`compute_2body_direct`, ...) behave like the reference: they
+take and return numpy arrays and synchronise.  Device calls
+(`twobody_device`, `coupling_device`) take raw device pointers (e.g.
+torch.Tensor.data_ptr()) and a CUDA stream handle and queue work only.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liblowdin_gb300.so")
+_LIB = None
+
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_vp = ctypes.c_void_p
+
+
+class LowdinGB300Error(RuntimeError):
+    pass
+
+
+def lib():
+    """Load the in-tree CUDA library; raises if it has not been built."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise LowdinGB300Error(
+                f"{LIB_PATH} is missing: build it with `python -m openlowdin_gb300.build` "
+                "(nvcc, sm_103a). There is no CPU fallback.")
+        L = ctypes.CDLL(LIB_PATH)
+        L.LibintInterface_new.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_bool, ctypes.c_bool]
+        L.LibintInterface_new.restype = _vp
+        L.LibintInterface_del.argtypes = [_vp]
+        L.LibintInterface_add_particle.argtypes = [_vp, ctypes.c_int, _f64p]
+        L.LibintInterface_add_shell.argtypes = [_vp, _f64p, _f64p, _f64p, ctypes.c_int, ctypes.c_int]
+        L.LibintInterface_get_nbasis.argtypes = [_vp]
+        L.LibintInterface_get_nbasis.restype = ctypes.c_int
+        L.LibintInterface_compute_1body_ints.argtypes = [_vp, ctypes.c_int, _f64p]
+        L.LibintInterface_init_2body_ints.argtypes = [_vp]
+        L.LibintInterface_compute_2body_direct.argtypes = [_vp, _f64p, _f64p, ctypes.POINTER(ctypes.c_double)]
+        L.LibintInterface_compute_2body_directIT.argtypes = [_vp, _f64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int)]
+        L.LibintInterface_compute_coupling_direct.argtypes = [_vp, _vp, _f64p, _f64p]
+        L.LibintInterface_compute_coupling_directIT.argtypes = [_vp, _vp, _f64p, _f64p, _f64p,
+                                                                ctypes.POINTER(ctypes.c_int)]
+        L.LowdinGB300_last_error.restype = ctypes.c_char_p
+        L.LowdinGB300_potential.argtypes = [_vp, ctypes.c_int, _f64p, _f64p, _f64p]
+        L.LowdinGB300_twobody_device.argtypes = [_vp, _vp, _vp, ctypes.c_double, ctypes.c_int, ctypes.c_double, _vp]
+        L.LowdinGB300_twobody_device.restype = ctypes.c_int
+        L.LowdinGB300_coupling_device.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]
+        L.LowdinGB300_coupling_device.restype = ctypes.c_int
+        L.LowdinGB300_last_quartets.argtypes = [_vp]
+        L.LowdinGB300_last_quartets.restype = ctypes.c_longlong
+        L.LowdinGB300_version.restype = ctypes.c_char_p
+        _LIB = L
+    return _LIB
+
+
+# every symbol include/lowdin_gb300.h declares
+EXPORTED_SYMBOLS = [
+    "LibintInterface_new", "LibintInterface_del", "LibintInterface_add_particle", "LibintInterface_add_shell",
+    "LibintInterface_get_nbasis", "LibintInterface_compute_1body_ints", "LibintInterface_init_2body_ints",
+    "LibintInterface_compute_2body_direct", "LibintInterface_compute_2body_directIT",
+    "LibintInterface_compute_2body_disk", "LibintInterface_compute_coupling_direct",
+    "LibintInterface_compute_coupling_directIT", "LibintInterface_compute_alphabeta_direct",
+    "LibintInterface_compute_coupling_disk", "libintinterface_compute_g12_disk",
+    "libintinterface_compute_g12inter_disk", "libintinterface_compute_g12_direct",
+    "libintinterface_compute_g12inter_direct", "LibintInterface_compute_2body_directAll",
+    "LibintInterface_compute_coupling_directAll", "libintinterface_compute_g12_directAll",
+    "libintinterface_compute_g12inter_directAll", "LowdinGB300_last_error", "LowdinGB300_clear_error",
+    "LowdinGB300_potential", "LowdinGB300_twobody_device", "LowdinGB300_coupling_device",
+    "LowdinGB300_last_quartets", "LowdinGB300_version",
+]
+
+
+def last_error() -> str:
+    return lib().LowdinGB300_last_error().decode()
+
+
+def _check():
+    err = last_error()
+    if err:
+        lib().LowdinGB300_clear_error()
+        raise LowdinGB300Error(err)
+
+
+class Libint2Interface:
+    """One species' handle (the reference's Libint2Instance(speciesID))."""
+
+    def __init__(self, species: dict, species_id: int, stack_size: int = 30000):
+        L = lib()
+        self.species = species
+        self.species_id = int(species_id)
+        self.is_electron = bool(species.get("is_electron", False))
+        self.h = L.LibintInterface_new(int(stack_size), self.species_id, self.is_electron, True)
+        for l, alphas, coefs, origin in species["shells"]:
+            a = np.ascontiguousarray(alphas, np.float64)
+            c = np.ascontiguousarray(coefs, np.float64)
+            o = np.ascontiguousarray(origin, np.float64)
+            L.LibintInterface_add_shell(self.h, a, c, o, int(l), len(a))
+        self.nbasis = L.LibintInterface_get_nbasis(self.h)
+        _check()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().LibintInterface_del(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---------------------------------------------------- host-buffer calls --
+    def init_2body_ints(self):
+        lib().LibintInterface_init_2body_ints(self.h)
+        _check()
+
+    def compute_2body_direct(self, density: np.ndarray, factor: float) -> np.ndarray:
+        """Libint2Interface_compute2BodyIntraspecies_direct (before the q^2 scaling)."""
+        n = self.nbasis
+        D = np.ascontiguousarray(density, np.float64)
+        out = np.empty((n, n))
+        f = ctypes.c_double(factor)
+        lib().LibintInterface_compute_2body_direct(self.h, D, out, ctypes.byref(f))
+        _check()
+        return out
+
+    def compute_coupling_direct(self, other: "Libint2Interface", other_density: np.ndarray) -> np.ndarray:
+        """Libint2Interface_compute2BodyInterspecies_direct: lower triangle (row >= col)."""
+        n = self.nbasis
+        out = np.empty((n, n))
+        lib().LibintInterface_compute_coupling_direct(self.h, other.h, np.ascontiguousarray(other_density, np.float64),
+                                                      out)
+        _check()
+        return out
+
+    def compute_2body_directIT(self, density, coefficients, p: int) -> np.ndarray:
+        n = self.nbasis
+        out = np.empty(n * n * n)
+        pp = ctypes.c_int(p)
+        lib().LibintInterface_compute_2body_directIT(self.h, np.ascontiguousarray(density, np.float64),
+                                                     np.ascontiguousarray(coefficients, np.float64), out,
+                                                     ctypes.byref(pp))
+        _check()
+        return out.reshape(n, n, n)
+
+    def compute_coupling_directIT(self, other: "Libint2Interface", coefficients, p: int) -> np.ndarray:
+        n, on = self.nbasis, other.nbasis
+        out = np.empty(n * on * on)
+        pp = ctypes.c_int(p)
+        dummy = np.zeros((n, n))
+        lib().LibintInterface_compute_coupling_directIT(self.h, other.h, dummy,
+                                                        np.ascontiguousarray(coefficients, np.float64), out,
+                                                        ctypes.byref(pp))
+        _check()
+        return out.reshape(n, on, on)
+
+    def one_body(self, kind: int) -> np.ndarray:
+        n = self.nbasis
+        out = np.empty((n, n))
+        lib().LibintInterface_compute_1body_ints(self.h, int(kind), out)
+        _check()
+        return out
+
+    def potential(self, charges, positions) -> np.ndarray:
+        n = self.nbasis
+        out = np.empty((n, n))
+        Z = np.ascontiguousarray(charges, np.float64)
+        R = np.ascontiguousarray(positions, np.float64).reshape(-1)
+        lib().LowdinGB300_potential(self.h, len(Z), Z, R if len(R) else np.zeros(3), out)
+        _check()
+        return out
+
+    # -------------------------------------------------------- device calls --
+    def twobody_device(self, d_ptr: int, g_ptr: int, factor: float, precision: int = 0, split: float = 0.0,
+                       stream: int = 0):
+        rc = lib().LowdinGB300_twobody_device(self.h, d_ptr, g_ptr, float(factor), int(precision), float(split),
+                                              stream)
+        if rc != 0:
+            _check()
+            raise LowdinGB300Error("twobody_device failed")
+
+    def last_quartets(self) -> int:
+        return int(lib().LowdinGB300_last_quartets(self.h))
+
+
+def coupling_device(a: Libint2Interface, b: Libint2Interface, da_ptr: int, db_ptr: int, ja_ptr: int, jb_ptr: int,
+                    fp32: bool = False, stream: int = 0):
+    rc = lib().LowdinGB300_coupling_device(a.h, b.h, da_ptr, db_ptr, ja_ptr, jb_ptr, int(fp32), stream)
+    if rc != 0:
+        _check()
+        raise LowdinGB300Error("coupling_device failed")

@@ -1,0 +1,160 @@
+"""GPU parity: the C-ABI library against the oracle, element-wise.
+
+Tolerance: 1e-10 absolute on every element of the two-particle / coupling
+matrices (plain FP64); 1e-9 on first-quarter tensors (they sum n raw products
+with coefficients of order 1-10).
+"""
+import numpy as np
+import pytest
+
+from openlowdin_gb300 import systems as S
+from tests import golden_systems as GS
+
+pytestmark = pytest.mark.gpu
+
+TOL_FOCK = 1e-10
+TOL_IT = 1e-9
+
+
+@pytest.fixture(scope="module")
+def L():
+    from openlowdin_gb300 import build, lint
+    build.build()
+    return lint
+
+
+def _sym(rng, n, scale=0.3):
+    X = rng.normal(size=(n, n)) * scale
+    return X + X.T
+
+
+def _scf_density(oracle, sysd, species=0):
+    res = oracle.scf(oracle.from_plain(sysd), tol_energy=1e-9, tol_density=1e-6)
+    return res.densities[species]
+
+
+def test_twobody_water_scf_density(L, oracle):
+    """c0 workload, converged density: screening active, factor -1/2."""
+    sysd = S.water()
+    sp = sysd["species"][0]
+    D = _scf_density(oracle, sysd)
+    h = L.Libint2Interface(sp, 1)
+    G = h.compute_2body_direct(D, -0.5)
+    ref = oracle.two_body_direct(oracle.Basis.from_shells(sp["shells"]), True, D, -0.5)
+    assert np.max(np.abs(G - ref)) < TOL_FOCK
+    assert np.max(np.abs(G - G.T)) == 0.0
+    h.close()
+
+
+def test_twobody_contracted_golden_basis(L, oracle, golden):
+    """6-311G (contracted s/p shells) of test/H2O.BOA.DIRECT."""
+    sysd = GS.h2o_boa(golden)
+    sp = sysd["species"][0]
+    rng = np.random.default_rng(11)
+    D = _sym(rng, S.nbasis(sp))
+    h = L.Libint2Interface(sp, 1)
+    G = h.compute_2body_direct(D, -0.5)
+    ref = oracle.two_body_direct(oracle.Basis.from_shells(sp["shells"]), True, D, -0.5)
+    assert np.max(np.abs(G - ref)) < TOL_FOCK
+    h.close()
+
+
+def test_twobody_protons_unscreened(L, oracle):
+    """Non-electron species: no Schwarz screening, factor kappa/eta = -1."""
+    sysd = S.water_cluster(2, seed=1, quantum_protons=True)
+    sp = sysd["species"][1]
+    rng = np.random.default_rng(5)
+    D = _sym(rng, S.nbasis(sp), 0.05)
+    h = L.Libint2Interface(sp, 2)
+    G = h.compute_2body_direct(D, -1.0)
+    ref = oracle.two_body_direct(oracle.Basis.from_shells(sp["shells"]), False, D, -1.0)
+    assert np.max(np.abs(G - ref)) < TOL_FOCK
+    h.close()
+
+
+def test_twobody_apmo_cluster_electrons(L, oracle):
+    """Electrons of the 4-water APMO cluster (136 functions)."""
+    sysd = S.water_cluster(4, seed=0, quantum_protons=True)
+    sp = sysd["species"][0]
+    rng = np.random.default_rng(3)
+    D = _sym(rng, S.nbasis(sp), 0.1)
+    h = L.Libint2Interface(sp, 1)
+    G = h.compute_2body_direct(D, -0.5)
+    ref = oracle.two_body_direct(oracle.Basis.from_shells(sp["shells"]), True, D, -0.5)
+    assert np.max(np.abs(G - ref)) < TOL_FOCK
+    assert h.last_quartets() == oracle.last_quartet_count()
+    h.close()
+
+
+@pytest.mark.parametrize("ids", [(1, 2), (2, 1)])
+def test_coupling_both_orders(L, oracle, ids):
+    sysd = S.water_cluster(1, seed=0, quantum_protons=True, place=False)
+    e, p = sysd["species"]
+    rng = np.random.default_rng(4)
+    Dp = _sym(rng, S.nbasis(p), 0.2)
+    he = L.Libint2Interface(e, ids[0])
+    hp = L.Libint2Interface(p, ids[1])
+    B = he.compute_coupling_direct(hp, Dp)
+    ref = oracle.coupling_direct(oracle.Basis.from_shells(e["shells"]), ids[0],
+                                 oracle.Basis.from_shells(p["shells"]), ids[1], Dp)
+    assert np.max(np.abs(B - ref)) < TOL_FOCK
+    assert np.all(np.triu(B, 1) == 0.0)
+    he.close(); hp.close()
+
+
+def test_first_quarter_intra(L, oracle):
+    sysd = S.water()
+    sp = sysd["species"][0]
+    n = S.nbasis(sp)
+    rng = np.random.default_rng(6)
+    C = rng.normal(size=(n, n))
+    D = _scf_density(oracle, sysd)
+    h = L.Libint2Interface(sp, 1)
+    for p in (0, 4):
+        A = h.compute_2body_directIT(D, C, p)
+        ref = oracle.two_body_directIT(oracle.Basis.from_shells(sp["shells"]), True, D, C, p)
+        assert np.max(np.abs(A - ref)) < TOL_IT
+    h.close()
+
+
+def test_first_quarter_coupling(L, oracle):
+    sysd = S.water_cluster(1, seed=0, quantum_protons=True, place=False)
+    e, p = sysd["species"]
+    ne = S.nbasis(e)
+    rng = np.random.default_rng(8)
+    C = rng.normal(size=(ne, ne))
+    he = L.Libint2Interface(e, 1)
+    hp = L.Libint2Interface(p, 2)
+    A = he.compute_coupling_directIT(hp, C, 2)
+    ref = oracle.coupling_directIT(oracle.Basis.from_shells(e["shells"]), 1,
+                                   oracle.Basis.from_shells(p["shells"]), 2, C, 2)
+    assert np.max(np.abs(A - ref)) < TOL_IT
+    he.close(); hp.close()
+
+
+def test_device_entry_points_match_host_calls(L, oracle):
+    torch = pytest.importorskip("torch")
+    sysd = S.water_cluster(1, seed=0, quantum_protons=True, place=False)
+    e, p = sysd["species"]
+    rng = np.random.default_rng(9)
+    De, Dp = _sym(rng, S.nbasis(e), 0.2), _sym(rng, S.nbasis(p), 0.2)
+    he = L.Libint2Interface(e, 1)
+    hp = L.Libint2Interface(p, 2)
+    dDe = torch.tensor(De, device="cuda")
+    dDp = torch.tensor(Dp, device="cuda")
+    dG = torch.empty_like(dDe)
+    dJe = torch.empty_like(dDe)
+    dJp = torch.empty_like(dDp)
+    stream = torch.cuda.current_stream().cuda_stream
+    he.twobody_device(dDe.data_ptr(), dG.data_ptr(), -0.5, stream=stream)
+    L.coupling_device(he, hp, dDe.data_ptr(), dDp.data_ptr(), dJe.data_ptr(), dJp.data_ptr(), stream=stream)
+    torch.cuda.synchronize()
+    G = he.compute_2body_direct(De, -0.5)
+    assert np.max(np.abs(dG.cpu().numpy() - G)) < 1e-12
+    Be = he.compute_coupling_direct(hp, Dp)
+    Bp = hp.compute_coupling_direct(he, De)
+    Je, Jp = dJe.cpu().numpy(), dJp.cpu().numpy()
+    assert np.max(np.abs(np.tril(Je) - Be)) < TOL_FOCK
+    assert np.max(np.abs(np.tril(Jp) - Bp)) < TOL_FOCK
+    assert np.max(np.abs(Je - Je.T)) < 1e-14
+    he.close(); hp.close()
