@@ -1,0 +1,335 @@
+#!/usr/bin/env python
+"""Benchmark: SCF solves/s of the APMO workload on GB300.
+
+Workload (one "step"): B independent APMO Hartree-Fock solves of seeded
+4-water clusters (electrons: 136 Cartesian functions, 40 e-; quantum protons:
+one H_1 species, 56 functions, 8 protons), each from the core-Hamiltonian guess
+to |dE| < 1e-8 Eh and rms(dP) < 1e-6, including the per-molecule setup (one-
+electron integrals, pair lists, Schwarz factors).  Synthetic inputs generated
+by openlowdin_gb300.systems (seeds rank*B + i).
+
+Arms:
+  default        -- GPU, device-resident SCF driver (plain FP64 integrals);
+                    `value` is solves/s over all ranks.  Also reports the mixed
+                    FP32/FP64 variant, the end-to-end number through the host-
+                    buffer C ABI (`e2e`), the roofline of the dominant kernel
+                    and a CPU baseline of the oracle port on the host cores.
+  --impl reference -- the CPU restatement of the reference's direct path
+                    (oracle/, C + OpenMP, all host threads) on the same
+                    workload; no GPU work.
+Multi-GPU: replicas (each rank solves its own molecules, no collective in the
+data path); rank 0 prints the JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SCF(+MP2) solves/s and p50/p99 latency, mixed vs plain FP64 GPU at 1e-6 Eh"
+UNIT = "solves/s"
+WORKLOAD = "APMO HF, 4-water cluster (e- 136 fn + H_1 56 fn, 8 quantum protons), dE<1e-8"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=4, help="molecules per step")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def systems_for(rank, batch):
+    from openlowdin_gb300 import systems as S
+    return [S.water_cluster(4, seed=rank * batch + i, quantum_protons=True) for i in range(batch)]
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------- CPU oracle --
+def cpu_iteration_sample(sysd, nthreads):
+    """One APMO Fock-build iteration of the oracle (all intra and coupling
+    matrices from the core-Hamiltonian-guess densities) on host cores."""
+    import numpy as np
+    from oracle import lowdin_oracle as O
+    O.build()
+    sysO = O.from_plain(sysd)
+    sp = sysO.species
+    P = []
+    for s in sp:
+        Sm, T = O.overlap_kinetic(s.basis)
+        V = O.potential(s.basis, sysO.point_charges, sysO.point_positions)
+        H = T / s.mass + s.charge * V
+        w, U = np.linalg.eigh(Sm)
+        X = (U * w ** -0.5) @ U.T
+        e, Cp = np.linalg.eigh(X.T @ H @ X)
+        C = X @ Cp
+        P.append(s.eta * C[:, :s.n_occ] @ C[:, :s.n_occ].T)
+    t0 = time.perf_counter()
+    for i, s in enumerate(sp):
+        if s.n_particles > 1:
+            O.two_body_direct(s.basis, s.is_electron, P[i], s.exchange_factor, nthreads)
+        for j, o in enumerate(sp):
+            if j != i:
+                O.coupling_direct(s.basis, i + 1, o.basis, j + 1, P[j], nthreads)
+    return time.perf_counter() - t0
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import lowdin_oracle as O
+    O.build()
+    nthreads = O.nthreads_default()
+    sysd = systems_for(0, 1)[0]
+    # warm-up: one complete oracle SCF (gives the iteration count of a solve)
+    t0 = time.perf_counter()
+    res = O.scf(O.from_plain(sysd), tol_energy=1e-8, tol_density=1e-6, nthreads=nthreads)
+    full = time.perf_counter() - t0
+    iters = res.iterations
+    for _ in range(max(0, args.warmup - 1)):
+        cpu_iteration_sample(sysd, nthreads)
+    times = [cpu_iteration_sample(sysd, nthreads) for _ in range(args.steps)]
+    t_it = sum(times) / len(times)
+    value = 1.0 / (t_it * iters)
+    sample = (f"oracle port (C/OpenMP, {nthreads} threads): {args.steps} timed Fock-build iterations of the "
+              f"4-water APMO system (G_e, G_p, both couplings); solve = {iters} iterations "
+              f"(full oracle solve in warm-up took {full:.1f} s)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_it * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "step": "one Fock-build iteration (bounded CPU sample)",
+                       "parallelism": "rank 0 only"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ----------------------------------------------------------------- GPU arm --
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import numpy as np
+    import torch
+    from openlowdin_gb300 import flops as FL
+    from openlowdin_gb300 import lint, scf
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    mols = systems_for(rank, args.batch)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step(precision):
+        res = []
+        for m in mols:
+            s = scf.DeviceSCF(m, precision=precision)
+            res.append(s.solve(tol_energy=1e-8, tol_density=1e-6))
+            s.close()
+        return res
+
+    def timed(precision, steps, warmup):
+        for _ in range(warmup):
+            step(precision)
+        barrier()
+        total_ms, results = 0.0, []
+        st = torch.cuda.current_stream()
+        for _ in range(steps):
+            flush.fill_(1.0)               # L2 flush (256 MiB write) between timed steps
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            results += step(precision)
+            b.record(st)
+            torch.cuda.synchronize()
+            total_ms += a.elapsed_time(b)
+        barrier()
+        return total_ms, results
+
+    # plain FP64: the headline
+    launches0 = lint.launch_count()
+    clk = ClockSampler(local)
+    clk.start()
+    ms_plain, res_plain = timed("fp64", args.steps, args.warmup)
+    clocks = clk.stop()
+    launches = lint.launch_count() - launches0
+    # mixed FP32/FP64 integrals
+    ms_mixed, res_mixed = timed("mixed", args.steps, max(1, args.warmup // 2))
+    t = torch.tensor([ms_plain, ms_mixed], dtype=torch.float64, device=dev)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_plain, ms_mixed = float(t[0]), float(t[1])
+    solves = args.batch * args.steps * world
+    value = solves / (ms_plain * 1e-3)
+    value_mixed = solves / (ms_mixed * 1e-3)
+    mixed_err = max(abs(a.energy - b.energy) for a, b in zip(res_plain, res_mixed))
+    iters = float(np.mean([r.iterations for r in res_plain]))
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_plain / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "molecules_per_step_per_gpu": args.batch,
+                      "iterations_per_solve": iters, "l2": "flushed between timed steps (256 MiB write)",
+                      "parallelism": "replicas" if world > 1 else "single GPU",
+                      "driver": "device-resident SCF (torch FP64 linear algebra, library integral kernels)"},
+           "variants": {"mixed_fp32_fp64": {"value": value_mixed, "unit": UNIT,
+                                            "max_energy_diff_vs_plain_Eh": mixed_err,
+                                            "ms_per_step": ms_mixed / args.steps},
+                        "plain_energies_Eh": [r.energy for r in res_plain[:args.batch]]},
+           "clocks": clocks, "gpu_launches": int(launches)}
+
+    if rank == 0:
+        # ---- e2e: the reference-shaped C ABI with host buffers every iteration
+        e2e_steps = max(1, min(2, args.steps))
+        h2d = d2h = 0
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            for m in mols:
+                hs = scf.HostSCF(m)
+                r = hs.solve(tol_energy=1e-8, tol_density=1e-6)
+                ne, npn = hs.handles[0].nbasis, hs.handles[1].nbasis
+                # per iteration: G_e (D up, G down), G_p, coupling e<-p, coupling p<-e
+                h2d += r.iterations * 8 * (ne * ne + npn * npn + npn * npn + ne * ne)
+                d2h += r.iterations * 8 * (ne * ne + npn * npn + ne * ne + npn * npn)
+                hs.close()
+        e2e_s = time.perf_counter() - t0
+        out["e2e"] = {"value": args.batch * e2e_steps / e2e_s, "unit": UNIT,
+                      "h2d_bytes_per_step": h2d // e2e_steps, "d2h_bytes_per_step": d2h // e2e_steps,
+                      "path": "HostSCF: LibintInterface_compute_2body_direct / _compute_coupling_direct with "
+                              "host buffers each iteration (numpy linear algebra on the host)"}
+
+        # ---- roofline of the dominant kernel family: electron J/K build
+        s = scf.DeviceSCF(mols[0], precision="fp64")
+        r = s.solve(tol_energy=1e-8, tol_density=1e-6)
+        he = s.handles[0]
+        D = torch.tensor(r.densities[0], device=dev)
+        G = torch.empty_like(D)
+        stv = torch.cuda.current_stream().cuda_stream
+        for _ in range(3):
+            he.twobody_device(D.data_ptr(), G.data_ptr(), -0.5, 0, 0.0, stv)
+        reps = 20
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            he.twobody_device(D.data_ptr(), G.data_ptr(), -0.5, 0, 0.0, stv)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / reps
+        counts = he.last_class_quartets()
+        fl = FL.class_table_flops(counts, "jk")
+        peak64 = lint.measure_fma_tflops(True)
+        peak32 = lint.measure_fma_tflops(False)
+        achieved = fl / (ms * 1e-3) / 1e12
+        traffic = None
+        prof = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+        if os.path.exists(prof):
+            try:
+                traffic = json.load(open(prof)).get("jk_electrons_bytes_per_build")
+            except Exception:
+                traffic = None
+        out["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
+                           "frac": achieved / peak64 if peak64 > 0 else None, "traffic": traffic,
+                           "kernel": "jk_kernel (electron two-particle build, all classes, one build)",
+                           "ms_per_build": ms, "quartets": int(counts.sum()), "flop_per_build": fl,
+                           "peak_source": "measured FP64 FMA throughput of this GPU in this run "
+                                          "(MEASURED_PEAKS.json has no FP64 entry)",
+                           "fp32_peak_tflops": peak32}
+        s.close()
+
+        # ---- CPU baseline (oracle port on the host cores), bounded sample
+        if not args.no_cpu_baseline:
+            from oracle import lowdin_oracle as O
+            nth = O.nthreads_default()
+            t_it = cpu_iteration_sample(mols[0], nth)
+            out["cpu_baseline"] = {"value": 1.0 / (t_it * iters), "unit": UNIT, "cores": nth, "kind": "port",
+                                   "sample": f"one APMO Fock-build iteration (G_e, G_p, both couplings) of the "
+                                             f"oracle on {nth} host threads: {t_it:.2f} s; solves/s = "
+                                             f"1/(t_iter x {iters:.1f} iterations)"}
+        print(json.dumps(out))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

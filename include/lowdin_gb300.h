@@ -153,6 +153,21 @@ int LowdinGB300_coupling_device(LibintInterface *a, LibintInterface *b, const do
    handle (after screening), or -1. */
 long long LowdinGB300_last_quartets(LibintInterface *lint);
 
+/* Shell quartets per (bra pair class, ket pair class) of the last two-particle
+   build, 36 entries (pair classes ss, ps, pp, ds, dp, dd); returns 36 or -1. */
+int LowdinGB300_last_class_quartets(LibintInterface *lint, long long *out);
+
+/* Number of shell pairs per pair class (6 entries): significant pairs when
+   all_pairs = 0, every unordered pair when 1.  Returns 6 or -1. */
+int LowdinGB300_pair_class_counts(LibintInterface *lint, int all_pairs, int *out);
+
+/* Measured FMA throughput of the current GPU in TFLOP/s (fp64 = 1: FP64,
+   0: FP32), from independent FMA chains on every SM; -1 on error. */
+double LowdinGB300_measure_fma_tflops(int fp64);
+
+/* Number of CUDA kernels this library has launched in the process. */
+long long LowdinGB300_launch_count(void);
+
 /* Library and device description (static string). */
 const char *LowdinGB300_version(void);
 

@@ -45,6 +45,7 @@ cudaError_t launch_jk(int pcb, int pck, bool fp32, const JKParams &p, cudaStream
   if (p.nbra <= 0 || p.nket <= 0) return cudaSuccess;
   JKFn f = fp32 ? kJK32[pcb][pck] : kJK64[pcb][pck];
   f<<<quartet_grid(p.nbra, p.nket), kBlock, 0, s>>>(p);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -53,6 +54,7 @@ cudaError_t launch_coupling(int pcb, int pck, bool fp32, const CouplingParams &p
   if (p.nbra <= 0 || p.nket <= 0) return cudaSuccess;
   CPFn f = fp32 ? kCP32[pcb][pck] : kCP64[pcb][pck];
   f<<<quartet_grid(p.nbra, p.nket), kBlock, 0, s>>>(p);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -60,6 +62,7 @@ cudaError_t launch_it(int pcb, int pck, const ITParams &p, cudaStream_t s) {
   if (!class_supported(pcb, pck)) return cudaErrorNotSupported;
   if (p.nbra <= 0 || p.nket <= 0) return cudaSuccess;
   kIT[pcb][pck]<<<quartet_grid(p.nbra, p.nket), kBlock, 0, s>>>(p);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -67,6 +70,7 @@ cudaError_t launch_schwarz(int pc, const SchwarzParams &p, cudaStream_t s) {
   if (pc < 0 || pc >= kSPClasses) return cudaErrorNotSupported;
   if (p.np <= 0) return cudaSuccess;
   kSZ[pc]<<<(p.np + 127) / 128, 128, 0, s>>>(p);
+  count_launches(1);
   return cudaGetLastError();
 }
 

@@ -1,6 +1,8 @@
 // Element-wise helpers around the integral kernels: density preparation,
 // symmetrisation and output scaling.  All are HBM-streaming O(n^2) / O(n^3)
 // kernels with grid-stride loops.
+#include <atomic>
+
 #include "kernels.cuh"
 
 namespace lgb {
@@ -67,36 +69,96 @@ __global__ void scale_cube_kernel(double *__restrict__ A, const double *__restri
   }
 }
 
+// 8 independent FMA chains per thread; the result is stored so nothing is
+// removed by the compiler.
+template <typename T>
+__global__ void __launch_bounds__(256) fma_probe_kernel(T *out, int iters, T a, T b) {
+  T x0 = T(threadIdx.x) * T(1e-3), x1 = x0 + T(1), x2 = x0 + T(2), x3 = x0 + T(3);
+  T x4 = x0 + T(4), x5 = x0 + T(5), x6 = x0 + T(6), x7 = x0 + T(7);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      x0 = x0 * a + b; x1 = x1 * a + b; x2 = x2 * a + b; x3 = x3 * a + b;
+      x4 = x4 * a + b; x5 = x5 * a + b; x6 = x6 * a + b; x7 = x7 * a + b;
+    }
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+std::atomic<long long> g_launches{0};
+
 }  // namespace
+
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+cudaError_t measure_fma_tflops(bool fp64, double *tflops) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int blocks = sms * 8, threads = 256;
+  const int iters = fp64 ? 512 : 4096;
+  void *buf = nullptr;
+  e = cudaMalloc(&buf, (size_t)blocks * threads * 8);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(a);
+    if (fp64) fma_probe_kernel<double><<<blocks, threads>>>((double *)buf, iters, 0.999999, 1e-7);
+    else fma_probe_kernel<float><<<blocks, threads>>>((float *)buf, iters, 0.999999f, 1e-7f);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  e = cudaGetLastError();
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(buf);
+  const double flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return e;
+}
 
 cudaError_t launch_prepare_density(const double *D, const double *norma, const int *shell_of, int n, int nsh,
                                    double *Ds, double *Dn, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(Dn, 0, sizeof(double) * nsh * nsh, s);
   if (e != cudaSuccess) return e;
   prepare_density_kernel<<<grid_for((size_t)n * n, 256), 256, 0, s>>>(D, norma, shell_of, n, nsh, Ds, Dn);
+  count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_scale_density(const double *D, const double *norma, int n, double *Ds, cudaStream_t s) {
   scale_density_kernel<<<grid_for((size_t)n * n, 256), 256, 0, s>>>(D, norma, n, Ds);
+  count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_symmetrize(const double *Gacc, const double *norma, int n, double scale, double *G,
                               cudaStream_t s) {
   symmetrize_kernel<<<grid_for((size_t)n * n, 256), 256, 0, s>>>(Gacc, norma, n, scale, G);
+  count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_coupling_extract(const double *J, const double *norma, int n, double scale, int lower_only,
                                     double *out, cudaStream_t s) {
   coupling_extract_kernel<<<grid_for((size_t)n * n, 256), 256, 0, s>>>(J, norma, n, scale, lower_only, out);
+  count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_scale_cube(double *A, const double *normA, const double *normB, int nA, int nB,
                               cudaStream_t s) {
   scale_cube_kernel<<<grid_for((size_t)nA * nB * nB, 256), 256, 0, s>>>(A, normA, normB, nA, nB);
+  count_launches(1);
   return cudaGetLastError();
 }
 

@@ -100,6 +100,12 @@ cudaError_t launch_symmetrize(const double *Gacc, const double *norma, int n, do
                               cudaStream_t s);
 cudaError_t launch_coupling_extract(const double *J, const double *norma, int n, double scale, int lower_only,
                                     double *out, cudaStream_t s);
+// number of kernels this library has launched (process-wide)
+void count_launches(long long n);
+long long launch_count();
+
+// FMA throughput of the GPU (independent FMA chains on every SM), TFLOP/s
+cudaError_t measure_fma_tflops(bool fp64, double *tflops);
 cudaError_t launch_scale_cube(double *A, const double *normA, const double *normB, int nA, int nB,
                               cudaStream_t s);
 

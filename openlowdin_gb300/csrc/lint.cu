@@ -329,6 +329,7 @@ struct LibintInterface {
   DevBuf<double> dD, dDs, dDn, dGacc, dG, dA, dC;
   DevBuf<unsigned long long> dcount;
   long long last_quartets = -1;
+  long long class_quartets[kNumPairClasses * kNumPairClasses] = {0};
 
   ~LibintInterface() { release_device(); }
 
@@ -499,12 +500,13 @@ struct LibintInterface {
   bool twobody(const double *dDin, double *dGout, double factor, int precision, double split, cudaStream_t s) {
     if (!ensure_sig()) return false;
     const int n = nbasis, nsh = nshell();
+    constexpr int NQC = kNumPairClasses * kNumPairClasses;
     if (!dDs.ensure((size_t)n * n) || !dDn.ensure((size_t)nsh * nsh) || !dGacc.ensure((size_t)n * n) ||
-        !dcount.ensure(1))
+        !dcount.ensure(NQC))
       return false;
     CK(launch_prepare_density(dDin, d_norma, d_shell_of, n, nsh, dDs.p, dDn.p, s));
     CK(cudaMemsetAsync(dGacc.p, 0, sizeof(double) * n * n, s));
-    CK(cudaMemsetAsync(dcount.p, 0, sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(dcount.p, 0, sizeof(unsigned long long) * NQC, s));
     JKParams p{};
     p.pairs = sig.d;
     p.prims = sig.dp;
@@ -531,6 +533,7 @@ struct LibintInterface {
         p.ket0 = sig.start[ck];
         p.nket = sig.count(ck);
         p.triangle = cb == ck;
+        p.nquartets = dcount.p + cb * kNumPairClasses + ck;
         if (precision == 0) {
           p.split = 0.0;
           CK(launch_jk(cb, ck, false, p, s));
@@ -543,10 +546,14 @@ struct LibintInterface {
         }
       }
     CK(launch_symmetrize(dGacc.p, d_norma, n, 0.25, dGout, s));
-    unsigned long long cnt = 0;
-    CK(cudaMemcpyAsync(&cnt, dcount.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+    unsigned long long cnt[NQC];
+    CK(cudaMemcpyAsync(cnt, dcount.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    last_quartets = (long long)cnt;
+    last_quartets = 0;
+    for (int c = 0; c < NQC; ++c) {
+      class_quartets[c] = (long long)cnt[c];
+      last_quartets += (long long)cnt[c];
+    }
     return true;
   }
 };
@@ -898,6 +905,31 @@ int LowdinGB300_coupling_device(LibintInterface *a, LibintInterface *b, const do
 }
 
 long long LowdinGB300_last_quartets(LibintInterface *lint) { return lint ? lint->last_quartets : -1; }
+
+long long LowdinGB300_launch_count(void) { return lgb::launch_count(); }
+
+int LowdinGB300_last_class_quartets(LibintInterface *lint, long long *out) {
+  if (!check_handle(lint, __func__)) return -1;
+  for (int c = 0; c < kNumPairClasses * kNumPairClasses; ++c) out[c] = lint->class_quartets[c];
+  return kNumPairClasses * kNumPairClasses;
+}
+
+int LowdinGB300_pair_class_counts(LibintInterface *lint, int all_pairs, int *out) {
+  if (!check_handle(lint, __func__)) return -1;
+  if (!(all_pairs ? lint->ensure_all() : lint->ensure_sig())) return -1;
+  const PairList &L = all_pairs ? lint->all : lint->sig;
+  for (int c = 0; c < kNumPairClasses; ++c) out[c] = L.count(c);
+  return kNumPairClasses;
+}
+
+double LowdinGB300_measure_fma_tflops(int fp64) {
+  double t = 0;
+  if (lgb::measure_fma_tflops(fp64 != 0, &t) != cudaSuccess) {
+    set_error("FMA throughput probe failed");
+    return -1.0;
+  }
+  return t;
+}
 
 const char *LowdinGB300_version(void) { return "lowdin_gb300 0.1 (sm_103a, FP64/FP32 Obara-Saika, l<=1 kernels)"; }
 

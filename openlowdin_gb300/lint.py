@@ -63,6 +63,13 @@ def lib():
         L.LowdinGB300_last_quartets.argtypes = [_vp]
         L.LowdinGB300_last_quartets.restype = ctypes.c_longlong
         L.LowdinGB300_version.restype = ctypes.c_char_p
+        L.LowdinGB300_last_class_quartets.argtypes = [_vp, np.ctypeslib.ndpointer(dtype=np.int64)]
+        L.LowdinGB300_last_class_quartets.restype = ctypes.c_int
+        L.LowdinGB300_pair_class_counts.argtypes = [_vp, ctypes.c_int, np.ctypeslib.ndpointer(dtype=np.int32)]
+        L.LowdinGB300_pair_class_counts.restype = ctypes.c_int
+        L.LowdinGB300_measure_fma_tflops.argtypes = [ctypes.c_int]
+        L.LowdinGB300_measure_fma_tflops.restype = ctypes.c_double
+        L.LowdinGB300_launch_count.restype = ctypes.c_longlong
         _LIB = L
     return _LIB
 
@@ -80,8 +87,14 @@ EXPORTED_SYMBOLS = [
     "LibintInterface_compute_coupling_directAll", "libintinterface_compute_g12_directAll",
     "libintinterface_compute_g12inter_directAll", "LowdinGB300_last_error", "LowdinGB300_clear_error",
     "LowdinGB300_potential", "LowdinGB300_twobody_device", "LowdinGB300_coupling_device",
-    "LowdinGB300_last_quartets", "LowdinGB300_version",
+    "LowdinGB300_last_quartets", "LowdinGB300_version", "LowdinGB300_last_class_quartets",
+    "LowdinGB300_pair_class_counts", "LowdinGB300_measure_fma_tflops", "LowdinGB300_launch_count",
 ]
+
+
+def launch_count() -> int:
+    """Kernels launched by the library so far in this process."""
+    return int(lib().LowdinGB300_launch_count())
 
 
 def last_error() -> str:
@@ -195,6 +208,26 @@ class Libint2Interface:
 
     def last_quartets(self) -> int:
         return int(lib().LowdinGB300_last_quartets(self.h))
+
+    def last_class_quartets(self) -> np.ndarray:
+        """[6][6] quartets per (bra pair class, ket pair class) of the last build."""
+        out = np.zeros(36, np.int64)
+        lib().LowdinGB300_last_class_quartets(self.h, out)
+        return out.reshape(6, 6)
+
+    def pair_class_counts(self, all_pairs: bool) -> np.ndarray:
+        out = np.zeros(6, np.int32)
+        if lib().LowdinGB300_pair_class_counts(self.h, int(all_pairs), out) < 0:
+            _check()
+        return out
+
+
+def measure_fma_tflops(fp64: bool = True) -> float:
+    """Measured FMA throughput of the current GPU (TFLOP/s)."""
+    v = float(lib().LowdinGB300_measure_fma_tflops(int(fp64)))
+    if v < 0:
+        _check()
+    return v
 
 
 def coupling_device(a: Libint2Interface, b: Libint2Interface, da_ptr: int, db_ptr: int, ja_ptr: int, jb_ptr: int,

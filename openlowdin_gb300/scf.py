@@ -1,0 +1,285 @@
+"""Multi-species Hartree-Fock drivers over the GPU two-particle library.
+
+These are the caller side of the integral boundary, restated from openLOWDIN's
+src/scf (MultiSCF.f90:276-440 iteration scheme 3, WaveFunction.f90):
+
+  H_i = T_i / m_i + q_i V_i                          (WaveFunction.f90:471-570)
+  X_i = S_i^{-1/2} (eigenvalues below 1e-8 dropped)  (WaveFunction.f90:394-467)
+  P_i from the core-Hamiltonian guess
+  every iteration, for every species i:
+    G_i = q_i^2 (J[P_i] + kappa_i/eta_i K[P_i])  when the species has > 1 particle
+                                                     (WaveFunction.f90:817-1159)
+    J_i = sum_{j != i} q_i q_j J_i[P_j]              (WaveFunction.f90:1432-1505)
+    F_i = H_i + G_i + J_i                            (WaveFunction.f90:1768-1826)
+  E = E_nuc + sum_i tr P_i (H_i + G_i / 2) + sum_{i<j} tr P_i J_ij
+  Pulay DIIS over all species (one coefficient set), F' = X^T F X, C = X C',
+  P_i = eta_i C_occ C_occ^T; converged when |dE| < tol and rms(dP) < tol_p.
+
+HostSCF keeps matrices in host memory and calls the reference-shaped C ABI
+(LibintInterface_compute_2body_direct / _compute_coupling_direct) with host
+buffers each iteration, the way the Fortran program does.  DeviceSCF keeps every
+matrix in HBM (torch FP64 tensors), calls the device entry points, fuses both
+coupling directions into one pass per species pair, and synchronises once per
+iteration for the convergence test.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import lint
+
+
+def nuclear_repulsion(sysd) -> float:
+    Z = np.asarray(sysd["point_charges"], float)
+    R = np.asarray(sysd["point_positions"], float).reshape(-1, 3)
+    e = 0.0
+    for a in range(len(Z)):
+        for b in range(a):
+            e += Z[a] * Z[b] / float(np.linalg.norm(R[a] - R[b]))
+    return e
+
+
+def n_occ(sp) -> int:
+    return int(round(sp["n_particles"] * sp["particles_fraction"]))
+
+
+@dataclass
+class SCFResult:
+    energy: float
+    iterations: int
+    converged: bool
+    seconds: float
+    orbital_energies: list = field(default_factory=list)
+    coefficients: list = field(default_factory=list)
+    densities: list = field(default_factory=list)
+    quartets: int = 0
+
+
+def _one_body(handles, sysd):
+    H, S = [], []
+    for h, sp in zip(handles, sysd["species"]):
+        Sm = h.one_body(1)
+        T = h.one_body(2)
+        V = h.potential(sysd["point_charges"], sysd["point_positions"])
+        H.append(T / sp["mass"] + sp["charge"] * V)
+        S.append(Sm)
+    return H, S
+
+
+def _orthogonaliser_np(S, cut=1e-8):
+    w, U = np.linalg.eigh(S)
+    keep = w > cut
+    if keep.all():
+        return (U * w ** -0.5) @ U.T
+    return U[:, keep] / np.sqrt(w[keep])
+
+
+class _DIIS:
+    def __init__(self, xp, size=10):
+        self.xp, self.size = xp, size
+        self.F, self.E = [], []
+
+    def __call__(self, Fs, errs):
+        xp = self.xp
+        self.F.append([f.clone() if hasattr(f, "clone") else f.copy() for f in Fs])
+        self.E.append(errs)
+        if len(self.F) > self.size:
+            self.F.pop(0)
+            self.E.pop(0)
+        m = len(self.F)
+        if m < 2:
+            return Fs
+        B = np.zeros((m + 1, m + 1))
+        B[m, :] = B[:, m] = -1.0
+        B[m, m] = 0.0
+        if xp is np:
+            for i in range(m):
+                for j in range(i + 1):
+                    B[i, j] = B[j, i] = sum(float(np.vdot(a, b)) for a, b in zip(self.E[i], self.E[j]))
+        else:
+            flat = xp.stack([xp.cat([e.reshape(-1) for e in E]) for E in self.E])
+            G = (flat @ flat.T).cpu().numpy()
+            B[:m, :m] = G
+        rhs = np.zeros(m + 1)
+        rhs[m] = -1.0
+        c = np.linalg.lstsq(B, rhs, rcond=1e-14)[0]
+        return [sum(float(c[i]) * self.F[i][k] for i in range(m)) for k in range(len(Fs))]
+
+
+class HostSCF:
+    """SCF whose integral work goes through the host-buffer C ABI each
+    iteration (the reference program's calling pattern)."""
+
+    def __init__(self, sysd):
+        self.sysd = sysd
+        self.species = sysd["species"]
+        self.handles = [lint.Libint2Interface(sp, i + 1) for i, sp in enumerate(self.species)]
+        for h in self.handles:
+            h.init_2body_ints()
+        self.H, self.S = _one_body(self.handles, sysd)
+        self.X = [_orthogonaliser_np(S) for S in self.S]
+        self.enuc = nuclear_repulsion(sysd)
+
+    def close(self):
+        for h in self.handles:
+            h.close()
+
+    def solve(self, tol_energy=1e-8, tol_density=1e-6, max_iter=100) -> SCFResult:
+        t0 = time.perf_counter()
+        sp, H, S, X = self.species, self.H, self.S, self.X
+        ns = len(sp)
+        P, C, eps = [], [], []
+        for i in range(ns):
+            e, Cp = np.linalg.eigh(X[i].T @ H[i] @ X[i])
+            Ci = X[i] @ Cp
+            C.append(Ci); eps.append(e)
+            o = n_occ(sp[i])
+            P.append(sp[i]["eta"] * Ci[:, :o] @ Ci[:, :o].T)
+        diis = _DIIS(np)
+        e_old, converged, it, quartets = None, False, 0, 0
+        energy = 0.0
+        for it in range(1, max_iter + 1):
+            G, J = [], [[None] * ns for _ in range(ns)]
+            for i in range(ns):
+                if sp[i]["n_particles"] > 1:
+                    f = sp[i]["kappa"] / sp[i]["eta"]
+                    G.append(self.handles[i].compute_2body_direct(P[i], f) * sp[i]["charge"] ** 2)
+                    quartets += max(0, self.handles[i].last_quartets())
+                else:
+                    G.append(np.zeros_like(H[i]))
+                for j in range(ns):
+                    if j == i:
+                        continue
+                    B = self.handles[i].compute_coupling_direct(self.handles[j], P[j])
+                    B = (np.tril(B) + np.tril(B, -1).T) * sp[i]["charge"] * sp[j]["charge"]
+                    J[i][j] = B
+            F = [H[i] + G[i] + sum(J[i][j] for j in range(ns) if j != i) for i in range(ns)]
+            energy = self.enuc
+            for i in range(ns):
+                energy += float(np.sum(P[i] * (H[i] + 0.5 * G[i])))
+                for j in range(i + 1, ns):
+                    energy += float(np.sum(P[i] * J[i][j]))
+            errs = [X[i].T @ (F[i] @ P[i] @ S[i] - S[i] @ P[i] @ F[i]) @ X[i] for i in range(ns)]
+            Fx = diis(F, errs)
+            dmax = 0.0
+            newP = []
+            for i in range(ns):
+                e, Cp = np.linalg.eigh(X[i].T @ Fx[i] @ X[i])
+                Ci = X[i] @ Cp
+                C[i], eps[i] = Ci, e
+                o = n_occ(sp[i])
+                Pn = sp[i]["eta"] * Ci[:, :o] @ Ci[:, :o].T
+                dmax = max(dmax, float(np.sqrt(np.mean((Pn - P[i]) ** 2))))
+                newP.append(Pn)
+            if e_old is not None and abs(energy - e_old) < tol_energy and dmax < tol_density:
+                converged = True
+                break
+            e_old = energy
+            P = newP
+        return SCFResult(energy, it, converged, time.perf_counter() - t0, eps, C, P, quartets)
+
+
+class DeviceSCF:
+    """SCF with every matrix resident in HBM (torch FP64 on cuda)."""
+
+    def __init__(self, sysd, device="cuda", precision="fp64", split=1e-5, stream=None):
+        import torch
+        self.torch = torch
+        self.sysd = sysd
+        self.species = sysd["species"]
+        self.dev = torch.device(device)
+        self.precision = precision
+        self.split = split
+        self.handles = [lint.Libint2Interface(sp, i + 1) for i, sp in enumerate(self.species)]
+        for h in self.handles:
+            h.init_2body_ints()
+        H, S = _one_body(self.handles, sysd)
+        self.H = [torch.tensor(x, device=self.dev) for x in H]
+        self.S = [torch.tensor(x, device=self.dev) for x in S]
+        self.X = [torch.tensor(_orthogonaliser_np(x), device=self.dev) for x in S]
+        self.enuc = nuclear_repulsion(sysd)
+        self.stream = stream
+
+    def close(self):
+        for h in self.handles:
+            h.close()
+
+    def _stream(self):
+        return self.torch.cuda.current_stream(self.dev).cuda_stream
+
+    def solve(self, tol_energy=1e-8, tol_density=1e-6, max_iter=100) -> SCFResult:
+        torch = self.torch
+        t0 = time.perf_counter()
+        sp, H, S, X = self.species, self.H, self.S, self.X
+        ns = len(sp)
+        st = self._stream()
+        occ = [n_occ(s) for s in sp]
+        eta = [s["eta"] for s in sp]
+        q = [s["charge"] for s in sp]
+        P, C, eps = [], [None] * ns, [None] * ns
+        for i in range(ns):
+            e, Cp = torch.linalg.eigh(X[i].T @ H[i] @ X[i])
+            Ci = X[i] @ Cp
+            C[i], eps[i] = Ci, e
+            P.append(eta[i] * Ci[:, :occ[i]] @ Ci[:, :occ[i]].T)
+        G = [torch.zeros_like(h) for h in H]
+        Jbuf = {}
+        for i in range(ns):
+            for j in range(ns):
+                if i != j:
+                    Jbuf[(i, j)] = torch.empty_like(H[i])
+        diis = _DIIS(torch)
+        mixed = self.precision == "mixed"
+        e_old, converged, it, quartets = None, False, 0, 0
+        energy = 0.0
+        for it in range(1, max_iter + 1):
+            for i in range(ns):
+                if sp[i]["n_particles"] > 1:
+                    Pi = P[i].contiguous()
+                    self.handles[i].twobody_device(Pi.data_ptr(), G[i].data_ptr(), sp[i]["kappa"] / eta[i],
+                                                   1 if mixed else 0, self.split, st)
+                    quartets += max(0, self.handles[i].last_quartets())
+                    G[i] *= q[i] ** 2
+            for i in range(ns):
+                for j in range(i + 1, ns):
+                    Pi, Pj = P[i].contiguous(), P[j].contiguous()
+                    lint.coupling_device(self.handles[i], self.handles[j], Pi.data_ptr(), Pj.data_ptr(),
+                                         Jbuf[(i, j)].data_ptr(), Jbuf[(j, i)].data_ptr(), mixed, st)
+                    Jbuf[(i, j)] *= q[i] * q[j]
+                    Jbuf[(j, i)] *= q[i] * q[j]
+            F = []
+            en = torch.zeros((), dtype=torch.float64, device=self.dev)
+            for i in range(ns):
+                Fi = H[i] + G[i]
+                for j in range(ns):
+                    if j != i:
+                        Fi = Fi + Jbuf[(i, j)]
+                F.append(Fi)
+                en = en + torch.sum(P[i] * (H[i] + 0.5 * G[i]))
+                for j in range(i + 1, ns):
+                    en = en + torch.sum(P[i] * Jbuf[(i, j)])
+            errs = [X[i].T @ (F[i] @ P[i] @ S[i] - S[i] @ P[i] @ F[i]) @ X[i] for i in range(ns)]
+            Fx = diis(F, errs)
+            newP, dP = [], []
+            for i in range(ns):
+                e, Cp = torch.linalg.eigh(X[i].T @ Fx[i] @ X[i])
+                Ci = X[i] @ Cp
+                C[i], eps[i] = Ci, e
+                Pn = eta[i] * Ci[:, :occ[i]] @ Ci[:, :occ[i]].T
+                dP.append(torch.sqrt(torch.mean((Pn - P[i]) ** 2)))
+                newP.append(Pn)
+            stats = torch.stack([en] + dP).cpu().numpy()
+            energy = float(stats[0]) + self.enuc
+            dmax = float(np.max(stats[1:]))
+            if e_old is not None and abs(energy - e_old) < tol_energy and dmax < tol_density:
+                converged = True
+                break
+            e_old = energy
+            P = newP
+        return SCFResult(energy, it, converged, time.perf_counter() - t0,
+                         [e.cpu().numpy() for e in eps], [c.cpu().numpy() for c in C],
+                         [p.cpu().numpy() for p in P], quartets)
