@@ -197,12 +197,12 @@ def main():
     mols = systems_for(rank, args.batch)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
+    from openlowdin_gb300.batch_scf import BatchSCF
+
     def step(precision):
-        res = []
-        for m in mols:
-            s = scf.DeviceSCF(m, precision=precision)
-            res.append(s.solve(tol_energy=1e-8, tol_density=1e-6))
-            s.close()
+        s = BatchSCF(mols, precision=precision)
+        res = s.solve(tol_energy=1e-8, tol_density=1e-6)
+        s.close()
         return res
 
     def timed(precision, steps, warmup):
@@ -265,10 +265,18 @@ def main():
             for m in mols:
                 hs = scf.HostSCF(m)
                 r = hs.solve(tol_energy=1e-8, tol_density=1e-6)
-                ne, npn = hs.handles[0].nbasis, hs.handles[1].nbasis
-                # per iteration: G_e (D up, G down), G_p, coupling e<-p, coupling p<-e
-                h2d += r.iterations * 8 * (ne * ne + npn * npn + npn * npn + ne * ne)
-                d2h += r.iterations * 8 * (ne * ne + npn * npn + ne * ne + npn * npn)
+                nb = [h.nbasis for h in hs.handles]
+                sps = m["species"]
+                # per iteration: each two-particle call moves D up and G down; each
+                # coupling call (i <- j) moves D_j up and the n_i x n_i result down
+                for i, sp in enumerate(sps):
+                    if sp["n_particles"] > 1:
+                        h2d += r.iterations * 8 * nb[i] ** 2
+                        d2h += r.iterations * 8 * nb[i] ** 2
+                    for j in range(len(sps)):
+                        if j != i:
+                            h2d += r.iterations * 8 * nb[j] ** 2
+                            d2h += r.iterations * 8 * nb[i] ** 2
                 hs.close()
         e2e_s = time.perf_counter() - t0
         out["e2e"] = {"value": args.batch * e2e_steps / e2e_s, "unit": UNIT,
@@ -276,26 +284,25 @@ def main():
                       "path": "HostSCF: LibintInterface_compute_2body_direct / _compute_coupling_direct with "
                               "host buffers each iteration (numpy linear algebra on the host)"}
 
-        # ---- roofline of the dominant kernel family: electron J/K build
-        s = scf.DeviceSCF(mols[0], precision="fp64")
-        r = s.solve(tol_energy=1e-8, tol_density=1e-6)
-        he = s.handles[0]
-        D = torch.tensor(r.densities[0], device=dev)
-        G = torch.empty_like(D)
+        # ---- roofline of the integral kernels: one batched Fock build (all
+        # J/K and coupling launches of the step's molecules) at converged densities
+        s = BatchSCF(mols, precision="fp64")
+        s.solve(tol_energy=1e-8, tol_density=1e-6)
         stv = torch.cuda.current_stream().cuda_stream
         for _ in range(3):
-            he.twobody_device(D.data_ptr(), G.data_ptr(), -0.5, 0, 0.0, stv)
+            s.batch.fock(0, 0.0, stv)
         reps = 20
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record()
         for _ in range(reps):
-            he.twobody_device(D.data_ptr(), G.data_ptr(), -0.5, 0, 0.0, stv)
+            s.batch.fock(0, 0.0, stv)
         b.record()
         torch.cuda.synchronize()
         ms = a.elapsed_time(b) / reps
-        counts = he.last_class_quartets()
-        fl = FL.class_table_flops(counts, "jk")
+        counts = s.batch.quartets(stv)
+        cpc = s.batch.coupling_quartets()
+        fl = FL.class_table_flops(counts, "jk") + FL.class_table_flops(cpc, "coupling")
         peak64 = lint.measure_fma_tflops(True)
         peak32 = lint.measure_fma_tflops(False)
         achieved = fl / (ms * 1e-3) / 1e12
@@ -308,8 +315,10 @@ def main():
                 traffic = None
         out["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
                            "frac": achieved / peak64 if peak64 > 0 else None, "traffic": traffic,
-                           "kernel": "jk_kernel (electron two-particle build, all classes, one build)",
-                           "ms_per_build": ms, "quartets": int(counts.sum()), "flop_per_build": fl,
+                           "kernel": "jk_tasks_kernel + cp_tasks_kernel (one batched Fock build of the step's "
+                                     "molecules, FP64, converged densities)",
+                           "ms_per_build": ms, "quartets_jk": int(counts.sum()),
+                           "quartets_coupling": int(cpc.sum()), "flop_per_build": fl,
                            "peak_source": "measured FP64 FMA throughput of this GPU in this run "
                                           "(MEASURED_PEAKS.json has no FP64 entry)",
                            "fp32_peak_tflops": peak32}

@@ -165,6 +165,30 @@ int LowdinGB300_pair_class_counts(LibintInterface *lint, int all_pairs, int *out
    0: FP32), from independent FMA chains on every SM; -1 on error. */
 double LowdinGB300_measure_fma_tflops(int fp64);
 
+/* Batches: many molecular systems, each a list of species handles, built
+   together.  For every species k of a system the caller gives device buffers
+   dP[k] (density, input), dG[k] (two-particle matrix q^2 (J + f K)[P], may be
+   NULL when two_body[k] = 0) and dJ[k] (sum over the other species j of the
+   system of q_k q_j J_k[P_j]); charges[k] = q_k, factors[k] = kappa/eta.
+   batch_fock queues the whole build on `stream` without waiting on the host
+   (a fixed sequence of launches that can be captured in a CUDA graph). */
+typedef struct LowdinGB300_Batch LowdinGB300_Batch;
+LowdinGB300_Batch *LowdinGB300_batch_new(void);
+void LowdinGB300_batch_del(LowdinGB300_Batch *b);
+/* returns the index of the system's first species in the batch, -1 on error */
+int LowdinGB300_batch_add_system(LowdinGB300_Batch *b, LibintInterface **species, int nspecies,
+                                 const double *charges, const double *factors, const int *two_body,
+                                 const double **dP, double **dG, double **dJ);
+/* builds pair data, task lists and work arenas (synchronises `stream`) */
+int LowdinGB300_batch_finalize(LowdinGB300_Batch *b, void *stream);
+/* precision 0 = FP64, 1 = mixed (quartets below `split` in FP32) */
+int LowdinGB300_batch_fock(LowdinGB300_Batch *b, int precision, double split, void *stream);
+/* quartets evaluated per (bra pair class, ket pair class) by the last J/K
+   build of the batch (36 entries; synchronises `stream`), and the coupling
+   quartets per class (every pair of a species pair, no screening) */
+int LowdinGB300_batch_quartets(LowdinGB300_Batch *b, long long *out, void *stream);
+int LowdinGB300_batch_coupling_quartets(LowdinGB300_Batch *b, long long *out);
+
 /* Number of CUDA kernels this library has launched in the process. */
 long long LowdinGB300_launch_count(void);
 

@@ -1,0 +1,216 @@
+"""Batched, device-resident multi-species Hartree-Fock.
+
+Every matrix of every species of every molecule stays in HBM.  Species are
+grouped by (basis size, occupied count, eta) into stacked tensors [m, n, n], so
+one SCF iteration over any number of molecules is
+
+  1 library build (LowdinGB300_batch_fock: all J/K and coupling work, ~20
+    kernel launches whatever the batch size),
+  a fixed number of batched tensor ops per size group (Fock assembly, energy,
+    commutator error, orthogonal transform, batched eigh, densities),
+  one small host read (energies and density changes) for convergence,
+
+which follows openLOWDIN's iteration scheme 3 (src/scf/MultiSCF.f90:276-440):
+every species of a molecule is updated once per global iteration from the
+previous densities, with Pulay DIIS over all species of the molecule.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import lint
+from .scf import SCFResult, _one_body, _orthogonaliser_np, n_occ, nuclear_repulsion
+
+
+@dataclass
+class _Group:
+    n: int
+    occ: int
+    eta: float
+    members: list        # (system index, species index)
+    H: object = None
+    S: object = None
+    X: object = None
+    P: object = None
+    G: object = None
+    J: object = None
+    C: object = None
+    eps: object = None
+
+
+class BatchSCF:
+    """SCF of many independent systems at once on one GPU."""
+
+    def __init__(self, systems, device="cuda", precision="fp64", split=1e-5, diis_size=10):
+        import torch
+        self.torch = torch
+        self.dev = torch.device(device)
+        self.systems = systems
+        self.precision = precision
+        self.split = split
+        self.diis_size = diis_size
+        self.handles = []       # per system: list of handles
+        groups = {}
+        self.where = []         # per system: list of (group key, slot)
+        hostmats = {}
+        for si, sysd in enumerate(systems):
+            hs = [lint.Libint2Interface(sp, k + 1) for k, sp in enumerate(sysd["species"])]
+            self.handles.append(hs)
+            H, S = _one_body(hs, sysd)
+            w = []
+            for k, sp in enumerate(sysd["species"]):
+                key = (hs[k].nbasis, n_occ(sp), float(sp["eta"]))
+                g = groups.setdefault(key, _Group(key[0], key[1], key[2], []))
+                w.append((key, len(g.members)))
+                g.members.append((si, k))
+                hostmats.setdefault(key, []).append((H[k], S[k]))
+            self.where.append(w)
+        self.groups = groups
+        for key, g in groups.items():
+            Hs = np.stack([h for h, _ in hostmats[key]])
+            Ss = np.stack([s for _, s in hostmats[key]])
+            Xs = np.stack([_orthogonaliser_np(s) for s in Ss])
+            g.H = torch.tensor(Hs, device=self.dev)
+            g.S = torch.tensor(Ss, device=self.dev)
+            g.X = torch.tensor(Xs, device=self.dev)
+            m = len(g.members)
+            g.P = torch.zeros((m, g.n, g.n), dtype=torch.float64, device=self.dev)
+            g.G = torch.zeros_like(g.P)
+            g.J = torch.zeros_like(g.P)
+        self.enuc = torch.tensor([nuclear_repulsion(s) for s in systems], dtype=torch.float64, device=self.dev)
+        self.nsys = len(systems)
+        # library batch: species buffers are slices of the stacked tensors
+        self.batch = lint.Batch()
+        for si, sysd in enumerate(systems):
+            sps = sysd["species"]
+            P, G, J = [], [], []
+            for k, sp in enumerate(sps):
+                key, slot = self.where[si][k]
+                g = groups[key]
+                P.append(g.P[slot]); G.append(g.G[slot]); J.append(g.J[slot])
+            self.batch.add_system(self.handles[si], [sp["charge"] for sp in sps],
+                                  [sp["kappa"] / sp["eta"] for sp in sps],
+                                  [1 if sp["n_particles"] > 1 else 0 for sp in sps], P, G, J)
+        self.batch.finalize(torch.cuda.current_stream(self.dev).cuda_stream)
+        for key, g in groups.items():
+            g.sys_index = torch.tensor([s for s, _ in g.members], device=self.dev)
+
+    def close(self):
+        self.batch.close()
+        for hs in self.handles:
+            for h in hs:
+                h.close()
+
+    # --------------------------------------------------------------- pieces --
+    def _diag(self, g, F):
+        torch = self.torch
+        Fp = g.X.transpose(1, 2) @ F @ g.X
+        e, Cp = torch.linalg.eigh(Fp)
+        C = g.X @ Cp
+        Co = C[:, :, :g.occ]
+        return e, C, g.eta * Co @ Co.transpose(1, 2)
+
+    def solve(self, tol_energy=1e-8, tol_density=1e-6, max_iter=100):
+        torch = self.torch
+        t0 = time.perf_counter()
+        stream = torch.cuda.current_stream(self.dev).cuda_stream
+        groups = list(self.groups.values())
+        for g in groups:
+            g.eps, g.C, P = self._diag(g, g.H)
+            g.P.copy_(P)
+        prec = 1 if self.precision == "mixed" else 0
+        hist_F, hist_E = [], []         # per iteration: list over groups
+        hist_B = []                      # per iteration: dots with earlier entries [nsys, h]
+        e_old = np.full(self.nsys, np.nan)
+        final_e = np.zeros(self.nsys)
+        conv = np.zeros(self.nsys, bool)
+        iters = np.zeros(self.nsys, int)
+        frozen = torch.zeros(self.nsys, dtype=torch.bool, device=self.dev)
+        quartets = 0
+        it = 0
+        for it in range(1, max_iter + 1):
+            self.batch.fock(prec, self.split, stream)
+            energy = self.enuc.clone()
+            Fs, Es = [], []
+            for g in groups:
+                F = g.H + g.G + g.J
+                e_sp = torch.sum(g.P * (g.H + 0.5 * g.G + 0.5 * g.J), dim=(1, 2))
+                energy.index_add_(0, g.sys_index, e_sp)
+                FPS = F @ g.P @ g.S
+                err = g.X.transpose(1, 2) @ (FPS - FPS.transpose(1, 2)) @ g.X
+                Fs.append(F)
+                Es.append(err)
+            # Pulay DIIS per system over all of its species
+            hist_F.append(Fs)
+            hist_E.append(Es)
+            if len(hist_F) > self.diis_size:
+                hist_F.pop(0); hist_E.pop(0); hist_B.pop(0)
+                hist_B = [b[:, 1:] for b in hist_B]
+            h = len(hist_F)
+            row = torch.zeros((self.nsys, h), dtype=torch.float64, device=self.dev)
+            for gi, g in enumerate(groups):
+                cur = Es[gi].reshape(len(g.members), -1)
+                for j in range(h):
+                    d = torch.sum(cur * hist_E[j][gi].reshape(len(g.members), -1), dim=1)
+                    row[:, j].index_add_(0, g.sys_index, d)
+            hist_B.append(row)
+            if h >= 2:
+                B = torch.zeros((self.nsys, h + 1, h + 1), dtype=torch.float64, device=self.dev)
+                for i in range(h):
+                    B[:, i, :i + 1] = hist_B[i][:, :i + 1]
+                    B[:, :i + 1, i] = hist_B[i][:, :i + 1]
+                B[:, h, :h] = -1.0
+                B[:, :h, h] = -1.0
+                # scale for conditioning, then solve every system at once
+                scale = torch.clamp(B[:, h - 1, h - 1].abs(), min=1e-300)
+                B[:, :h, :h] /= scale[:, None, None]
+                rhs = torch.zeros((self.nsys, h + 1, 1), dtype=torch.float64, device=self.dev)
+                rhs[:, h, 0] = -1.0
+                coef = torch.linalg.lstsq(B.cpu(), rhs.cpu()).solution[:, :h, 0].to(self.dev)
+            else:
+                coef = None
+            dP = torch.zeros(self.nsys, dtype=torch.float64, device=self.dev)
+            for gi, g in enumerate(groups):
+                if coef is None:
+                    Fx = Fs[gi]
+                else:
+                    c = coef[g.sys_index]                               # [m, h]
+                    Fx = sum(c[:, j, None, None] * hist_F[j][gi] for j in range(h))
+                e, C, Pn = self._diag(g, Fx)
+                keep = frozen[g.sys_index]
+                d = torch.sqrt(torch.mean((Pn - g.P) ** 2, dim=(1, 2)))
+                dP = torch.maximum(dP, torch.zeros_like(dP).index_reduce_(0, g.sys_index, d, "amax"))
+                Pn = torch.where(keep[:, None, None], g.P, Pn)
+                g.eps = torch.where(keep[:, None], g.eps, e)
+                g.C = torch.where(keep[:, None, None], g.C, C)
+                g.P.copy_(Pn)
+            stats = torch.stack([energy, dP]).cpu().numpy()
+            en, dpn = stats[0], stats[1]
+            active = ~conv
+            final_e[active] = en[active]
+            iters[active] = it
+            newly = active & (np.abs(en - e_old) < tol_energy) & (dpn < tol_density)
+            e_old[active] = en[active]
+            conv |= newly
+            if newly.any():
+                # a converged system keeps its energy and density from here on
+                frozen |= torch.tensor(newly, device=self.dev)
+            if conv.all():
+                break
+        q = self.batch.quartets(stream)
+        quartets = int(q.sum())
+        self.last_class_quartets = q
+        out = []
+        for si in range(self.nsys):
+            eps, C, P = [], [], []
+            for key, slot in self.where[si]:
+                g = self.groups[key]
+                eps.append(g.eps[slot].cpu().numpy())
+                C.append(g.C[slot].cpu().numpy())
+                P.append(g.P[slot].cpu().numpy())
+            out.append(SCFResult(float(final_e[si]), int(iters[si]), bool(conv[si]),
+                                 time.perf_counter() - t0, eps, C, P, quartets))
+        return out

@@ -1,13 +1,11 @@
 // Kernel templates: Schwarz factors, intra-species J/K, fused inter-species
-// coupling and first-quarter transforms.  Included by the per-class-group
-// translation units that instantiate them.
+// coupling and first-quarter transforms.  Included by the translation units
+// that instantiate them for a set of quartet classes.
 #pragma once
 #include "eri.cuh"
 #include "kernels.cuh"
 
 namespace lgb {
-
-constexpr int kWarpsPerBlock = 4;  // bra pairs per block (one per warp)
 
 template <typename R>
 __device__ __forceinline__ R warp_sum(R v) {
@@ -26,6 +24,18 @@ __device__ __forceinline__ double dnorm6(const double *__restrict__ Dn, int nsh,
   return m;
 }
 
+// task owning flattened block b: last task with blk0 <= b (tasks sorted by blk0)
+template <typename T>
+__device__ __forceinline__ int find_task(const T *__restrict__ tasks, int ntasks, int b) {
+  int lo = 0, hi = ntasks - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&tasks[mid].blk0) <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 // ----------------------------------------------------------------- Schwarz --
 template <int LA, int LB>
 __global__ void __launch_bounds__(128) schwarz_kernel(SchwarzParams P) {
@@ -42,48 +52,54 @@ __global__ void __launch_bounds__(128) schwarz_kernel(SchwarzParams P) {
 }
 
 // --------------------------------------------------------------------- J/K --
-// Thread (x, y) of a block evaluates quartet (bra = block.y*4 + y, ket =
-// block.x*32 + x) of the class.  The 32 lanes of a warp share the bra pair, so
-// the bra-block Coulomb term is reduced across the warp before its atomics.
+// Lane x of warp y in a block evaluates quartet (bra = tile_y*4 + y, ket =
+// tile_x*32 + x) of its task.  The 32 lanes of a warp share the bra pair, so the
+// bra-block Coulomb term is reduced across the warp before its atomics.
 // Digestion follows the six updates of a permutation-unique quartet
 // (g12 += D34 v, g34 += D12 v, g13/g24/g14/g23 += 0.5 f D v, all x degeneracy);
-// with G = (Gacc + Gacc^T)/4 this equals J[D] + f K[D].
+// with G = (Gacc + Gacc^T)/4 this is J[D] + f K[D].
 template <typename R, int LA, int LB, int LC, int LD>
-__global__ void __launch_bounds__(128) jk_kernel(JKParams P) {
+__global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict__ tasks, TaskLaunch TL) {
   using Q = QClass<LA, LB, LC, LD>;
   constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND;
-  if (P.triangle && blockIdx.x * 32 > blockIdx.y * kWarpsPerBlock + kWarpsPerBlock - 1) return;
-  const int kpos = blockIdx.x * 32 + threadIdx.x;
-  const int bpos = blockIdx.y * kWarpsPerBlock + threadIdx.y;
-  if (bpos >= P.nbra) return;  // warp-uniform
-  bool active = kpos < P.nket && (!P.triangle || kpos <= bpos);
-  const int bi = P.bra0 + bpos;
-  const int ki = P.ket0 + min(kpos, P.nket - 1);
-  const PairRec &bra = P.pairs[bi];
-  const PairRec ket = P.pairs[ki];
+  const int t = find_task(tasks, TL.ntasks, blockIdx.x);
+  const JKTask &T = tasks[t];
+  const int local = blockIdx.x - T.blk0;
+  const int tx = local % T.nbx, ty = local / T.nbx;
+  if (T.triangle && tx * 32 > ty * kWarpsPerBlock + kWarpsPerBlock - 1) return;
+  const int kpos = tx * 32 + threadIdx.x;
+  const int bpos = ty * kWarpsPerBlock + threadIdx.y;
+  if (bpos >= T.nbra) return;  // warp-uniform
+  bool active = kpos < T.nket && (!T.triangle || kpos <= bpos);
+  const int bi = T.bra0 + bpos;
+  const int ki = T.ket0 + min(kpos, T.nket - 1);
+  const PairRec &bra = T.pairs[bi];
+  const PairRec ket = T.pairs[ki];
   double bound = bra.Q * ket.Q;
-  if (P.screen) bound *= dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
-  if (P.screen && bound < P.eps) active = false;
-  if (P.split > 0.0) {
-    if (P.lower ? !(bound < P.split) : (bound < P.split)) active = false;
+  if (T.screen) {
+    bound *= dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
+    if (bound < TL.eps) active = false;
+  }
+  if (TL.split > 0.0) {
+    if (TL.lower ? !(bound < TL.split) : (bound < TL.split)) active = false;
   }
   if (__all_sync(0xffffffffu, !active)) return;
-  R I[Q::NINT];
-  if (P.nquartets) {
+  if (T.count) {
     const unsigned cnt = __popc(__ballot_sync(0xffffffffu, active));
-    if (threadIdx.x == 0) atomicAdd(P.nquartets, (unsigned long long)cnt);
+    if (threadIdx.x == 0) atomicAdd(T.count, (unsigned long long)cnt);
   }
+  R I[Q::NINT];
   if (active) {
-    eri_quartet<R, LA, LB, LC, LD>(bra, P.prims, ket, P.prims, P.boys.f64, P.boys.f32, I);
+    eri_quartet<R, LA, LB, LC, LD>(bra, T.prims, ket, T.prims, TL.boys.f64, TL.boys.f32, I);
   } else {
 #pragma unroll
     for (int x = 0; x < Q::NINT; ++x) I[x] = R(0);
   }
   const R deg = active ? R((bra.sa == bra.sb ? 1 : 2) * (ket.sa == ket.sb ? 1 : 2) * (bi == ki ? 1 : 2)) : R(0);
-  const R hdeg = deg * R(P.hf);
-  const double *__restrict__ D = P.Ds;
-  const int n = P.n;
-  double *G = P.Gacc;
+  const R hdeg = deg * R(T.hf);
+  const double *__restrict__ D = T.Ds;
+  const int n = T.n;
+  double *G = T.Gacc;
   const int fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb;
   auto Iat = [&](int a, int b, int c, int d) -> R { return I[((a * NB + b) * NC + c) * ND + d]; };
   // J12: bra block, warp-reduced
@@ -164,36 +180,42 @@ __global__ void __launch_bounds__(128) jk_kernel(JKParams P) {
 
 // ---------------------------------------------------------------- coupling --
 // Bra pairs of species A (every unordered shell pair), ket pairs of species B.
-// J_A[i][j] = sum_{kl} D_B[k][l] (ij|kl), J_B[k][l] = sum_{ij} D_A[i][j] (ij|kl),
-// both accumulated as full symmetric matrices; raw |v| < cut is dropped.
+// J_A[i][j] += scale sum_{kl} D_B[k][l] (ij|kl), J_B[k][l] += scale
+// sum_{ij} D_A[i][j] (ij|kl), both as full symmetric matrices; raw |v| < cut is
+// dropped (the reference's 1e-10 test on each integral).
 template <typename R, int LA, int LB, int LC, int LD>
-__global__ void __launch_bounds__(128) coupling_kernel(CouplingParams P) {
+__global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict__ tasks, TaskLaunch TL) {
   using Q = QClass<LA, LB, LC, LD>;
   constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND;
-  const int kpos = blockIdx.x * 32 + threadIdx.x;
-  const int bpos = blockIdx.y * kWarpsPerBlock + threadIdx.y;
-  if (bpos >= P.nbra) return;
-  const bool active = kpos < P.nket;
-  const PairRec &bra = P.pa[P.bra0 + bpos];
-  const PairRec ket = P.pb[P.ket0 + min(kpos, P.nket - 1)];
+  const int t = find_task(tasks, TL.ntasks, blockIdx.x);
+  const CPTask &T = tasks[t];
+  const int local = blockIdx.x - T.blk0;
+  const int tx = local % T.nbx, ty = local / T.nbx;
+  const int kpos = tx * 32 + threadIdx.x;
+  const int bpos = ty * kWarpsPerBlock + threadIdx.y;
+  if (bpos >= T.nbra) return;
+  const bool active = kpos < T.nket;
+  const PairRec &bra = T.pa[T.bra0 + bpos];
+  const PairRec ket = T.pb[T.ket0 + min(kpos, T.nket - 1)];
   R I[Q::NINT];
   if (active) {
-    eri_quartet<R, LA, LB, LC, LD>(bra, P.pra, ket, P.prb, P.boys.f64, P.boys.f32, I);
+    eri_quartet<R, LA, LB, LC, LD>(bra, T.pra, ket, T.prb, TL.boys.f64, TL.boys.f32, I);
   } else {
 #pragma unroll
     for (int x = 0; x < Q::NINT; ++x) I[x] = R(0);
   }
-  const R cut = R(P.cut);
+  const R cut = R(TL.cut);
 #pragma unroll
   for (int x = 0; x < Q::NINT; ++x)
     if (!(fabs(I[x]) >= cut)) I[x] = R(0);
   auto Iat = [&](int a, int b, int c, int d) -> R { return I[((a * NB + b) * NC + c) * ND + d]; };
   const int fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb;
   const bool abdiff = bra.sa != bra.sb, cddiff = ket.sa != ket.sb;
-  if (P.JA) {
-    const R wk = active ? R(cddiff ? 2 : 1) : R(0);
-    const double *__restrict__ D = P.DsB;
-    const int nB = P.nB, nA = P.nA;
+  const R scale = R(T.scale);
+  if (T.JA) {
+    const R wk = active ? R(cddiff ? 2 : 1) * scale : R(0);
+    const double *__restrict__ D = T.DsB;
+    const int nB = T.nB, nA = T.nA;
 #pragma unroll
     for (int a = 0; a < NA; ++a)
 #pragma unroll
@@ -205,15 +227,15 @@ __global__ void __launch_bounds__(128) coupling_kernel(CouplingParams P) {
           for (int d = 0; d < ND; ++d) s += R(__ldg(D + (fc + c) * nB + fd + d)) * Iat(a, b, c, d);
         s = warp_sum(s * wk);
         if (threadIdx.x == 0) {
-          atomicAdd(P.JA + (fa + a) * nA + fb + b, double(s));
-          if (abdiff) atomicAdd(P.JA + (fb + b) * nA + fa + a, double(s));
+          atomicAdd(T.JA + (fa + a) * nA + fb + b, double(s));
+          if (abdiff) atomicAdd(T.JA + (fb + b) * nA + fa + a, double(s));
         }
       }
   }
-  if (P.JB && active) {
-    const R wb = R(abdiff ? 2 : 1);
-    const double *__restrict__ D = P.DsA;
-    const int nA = P.nA, nB = P.nB;
+  if (T.JB && active) {
+    const R wb = R(abdiff ? 2 : 1) * scale;
+    const double *__restrict__ D = T.DsA;
+    const int nA = T.nA, nB = T.nB;
 #pragma unroll
     for (int c = 0; c < NC; ++c)
 #pragma unroll
@@ -224,8 +246,8 @@ __global__ void __launch_bounds__(128) coupling_kernel(CouplingParams P) {
 #pragma unroll
           for (int b = 0; b < NB; ++b) s += R(__ldg(D + (fa + a) * nA + fb + b)) * Iat(a, b, c, d);
         s *= wb;
-        atomicAdd(P.JB + (fc + c) * nB + fd + d, double(s));
-        if (cddiff) atomicAdd(P.JB + (fd + d) * nB + fc + c, double(s));
+        atomicAdd(T.JB + (fc + c) * nB + fd + d, double(s));
+        if (cddiff) atomicAdd(T.JB + (fd + d) * nB + fc + c, double(s));
       }
   }
 }

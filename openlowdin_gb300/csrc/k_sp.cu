@@ -1,5 +1,5 @@
 // Instantiations and launchers of the class-templated kernels for s and p
-// shells (every quartet class built from pair classes ss, ps, pp).
+// shells (every quartet class built from the pair classes ss, ps, pp).
 #include "fock_kernels.cuh"
 
 namespace lgb {
@@ -8,15 +8,15 @@ namespace {
 
 constexpr int kSPClasses = 3;  // pair classes handled here: 0 (ss), 1 (ps), 2 (pp)
 
-using JKFn = void (*)(JKParams);
-using CPFn = void (*)(CouplingParams);
+using JKFn = void (*)(const JKTask *, TaskLaunch);
+using CPFn = void (*)(const CPTask *, TaskLaunch);
 using ITFn = void (*)(ITParams);
 using SZFn = void (*)(SchwarzParams);
 
 template <typename R, int B, int K>
-constexpr JKFn jkf() { return &jk_kernel<R, pc_la(B), pc_lb(B), pc_la(K), pc_lb(K)>; }
+constexpr JKFn jkf() { return &jk_tasks_kernel<R, pc_la(B), pc_lb(B), pc_la(K), pc_lb(K)>; }
 template <typename R, int B, int K>
-constexpr CPFn cpf() { return &coupling_kernel<R, pc_la(B), pc_lb(B), pc_la(K), pc_lb(K)>; }
+constexpr CPFn cpf() { return &cp_tasks_kernel<R, pc_la(B), pc_lb(B), pc_la(K), pc_lb(K)>; }
 template <int B, int K>
 constexpr ITFn itf() { return &it_kernel<pc_la(B), pc_lb(B), pc_la(K), pc_lb(K)>; }
 
@@ -31,29 +31,28 @@ const ITFn kIT[3][3] = {{itf<0, 0>(), itf<0, 1>(), itf<0, 2>()},
                         {itf<2, 0>(), itf<2, 1>(), itf<2, 2>()}};
 const SZFn kSZ[3] = {&schwarz_kernel<0, 0>, &schwarz_kernel<1, 0>, &schwarz_kernel<1, 1>};
 
-dim3 quartet_grid(int nbra, int nket) {
-  return dim3((unsigned)((nket + 31) / 32), (unsigned)((nbra + kWarpsPerBlock - 1) / kWarpsPerBlock));
-}
 const dim3 kBlock(32, kWarpsPerBlock);
 
 }  // namespace
 
 bool class_supported(int pcb, int pck) { return pcb >= 0 && pck >= 0 && pcb < kSPClasses && pck < kSPClasses; }
 
-cudaError_t launch_jk(int pcb, int pck, bool fp32, const JKParams &p, cudaStream_t s) {
+cudaError_t launch_jk_tasks(int pcb, int pck, bool fp32, const JKTask *dtasks, const TaskLaunch &tl,
+                            cudaStream_t s) {
   if (!class_supported(pcb, pck)) return cudaErrorNotSupported;
-  if (p.nbra <= 0 || p.nket <= 0) return cudaSuccess;
+  if (tl.ntasks <= 0 || tl.nblocks <= 0) return cudaSuccess;
   JKFn f = fp32 ? kJK32[pcb][pck] : kJK64[pcb][pck];
-  f<<<quartet_grid(p.nbra, p.nket), kBlock, 0, s>>>(p);
+  f<<<tl.nblocks, kBlock, 0, s>>>(dtasks, tl);
   count_launches(1);
   return cudaGetLastError();
 }
 
-cudaError_t launch_coupling(int pcb, int pck, bool fp32, const CouplingParams &p, cudaStream_t s) {
+cudaError_t launch_cp_tasks(int pcb, int pck, bool fp32, const CPTask *dtasks, const TaskLaunch &tl,
+                            cudaStream_t s) {
   if (!class_supported(pcb, pck)) return cudaErrorNotSupported;
-  if (p.nbra <= 0 || p.nket <= 0) return cudaSuccess;
+  if (tl.ntasks <= 0 || tl.nblocks <= 0) return cudaSuccess;
   CPFn f = fp32 ? kCP32[pcb][pck] : kCP64[pcb][pck];
-  f<<<quartet_grid(p.nbra, p.nket), kBlock, 0, s>>>(p);
+  f<<<tl.nblocks, kBlock, 0, s>>>(dtasks, tl);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -61,7 +60,8 @@ cudaError_t launch_coupling(int pcb, int pck, bool fp32, const CouplingParams &p
 cudaError_t launch_it(int pcb, int pck, const ITParams &p, cudaStream_t s) {
   if (!class_supported(pcb, pck)) return cudaErrorNotSupported;
   if (p.nbra <= 0 || p.nket <= 0) return cudaSuccess;
-  kIT[pcb][pck]<<<quartet_grid(p.nbra, p.nket), kBlock, 0, s>>>(p);
+  const dim3 grid((unsigned)((p.nket + 31) / 32), (unsigned)((p.nbra + kWarpsPerBlock - 1) / kWarpsPerBlock));
+  kIT[pcb][pck]<<<grid, kBlock, 0, s>>>(p);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -87,7 +87,62 @@ __global__ void __launch_bounds__(256) fma_probe_kernel(T *out, int iters, T a, 
 
 std::atomic<long long> g_launches{0};
 
+__device__ __forceinline__ int find_slot(const SpeciesSlot *__restrict__ slots, int nslots, long long x) {
+  int lo = 0, hi = nslots - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (slots[mid].off <= x) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// every species of a batch: Ds = N P N, Dn = shell-block max |P| (when used),
+// and zeroed accumulators
+__global__ void prepare_batch_kernel(const SpeciesSlot *__restrict__ slots, int nslots, long long total) {
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+       x += (long long)gridDim.x * blockDim.x) {
+    const SpeciesSlot &S = slots[find_slot(slots, nslots, x)];
+    const long long e = x - S.off;
+    const int i = (int)(e / S.n), j = (int)(e % S.n);
+    const double p = S.P[e];
+    S.Ds[e] = p * S.norma[i] * S.norma[j];
+    if (S.Gacc) S.Gacc[e] = 0.0;
+    S.Jacc[e] = 0.0;
+    if (S.Dn)
+      atomicMax(reinterpret_cast<unsigned long long *>(S.Dn) + S.shell_of[i] * S.nsh + S.shell_of[j],
+                (unsigned long long)__double_as_longlong(fabs(p)));
+  }
+}
+
+// G = gscale N (Gacc + Gacc^T) N (0 when the species builds none), J = N Jacc N
+__global__ void finalize_batch_kernel(const SpeciesSlot *__restrict__ slots, int nslots, long long total) {
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+       x += (long long)gridDim.x * blockDim.x) {
+    const SpeciesSlot &S = slots[find_slot(slots, nslots, x)];
+    const long long e = x - S.off;
+    const int i = (int)(e / S.n), j = (int)(e % S.n);
+    const double nn = S.norma[i] * S.norma[j];
+    if (S.G) S.G[e] = S.Gacc ? S.gscale * nn * (S.Gacc[e] + S.Gacc[(long long)j * S.n + i]) : 0.0;
+    S.J[e] = nn * S.Jacc[e];
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_prepare_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s) {
+  if (total <= 0) return cudaSuccess;
+  prepare_batch_kernel<<<grid_for((size_t)total, 256), 256, 0, s>>>(slots, nslots, total);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s) {
+  if (total <= 0) return cudaSuccess;
+  finalize_batch_kernel<<<grid_for((size_t)total, 256), 256, 0, s>>>(slots, nslots, total);
+  count_launches(1);
+  return cudaGetLastError();
+}
 
 void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }

@@ -1,4 +1,11 @@
 // Launch parameters and host-side launchers of the integral kernels.
+//
+// The two-particle (J/K) and inter-species coupling builds run from task
+// lists: a task is one (bra pair-class range) x (ket pair-class range) block of
+// quartets of one species (J/K) or of one species pair (coupling).  All tasks of
+// the same quartet class -- across species, species pairs and molecules of a
+// batch -- go into one launch; block b of the flattened grid finds its task by
+// binary search on the tasks' first-block offsets.
 #pragma once
 #include "common.cuh"
 
@@ -10,49 +17,56 @@ constexpr int kNumPairClasses = (kMaxL + 1) * (kMaxL + 2) / 2;
 __host__ __device__ constexpr int pc_la(int pc) { return pc >= 3 ? 2 : (pc >= 1 ? 1 : 0); }
 __host__ __device__ constexpr int pc_lb(int pc) { return pc - pc_la(pc) * (pc_la(pc) + 1) / 2; }
 
+constexpr int kWarpsPerBlock = 4;  // bra pairs per block (one per warp); 32 kets per warp
+
 struct BoysTables {
   const double *f64;
   const float *f32;
 };
 
-// Intra-species J/K build over the quartets (bra pair, ket pair) of one class.
-struct JKParams {
+// One J/K task: quartets (bra in [bra0, bra0+nbra), ket in [ket0, ket0+nket))
+// of one species' significant pairs.
+struct JKTask {
   const PairRec *pairs;
   const PrimRec *prims;
-  int bra0, nbra, ket0, nket;
-  int triangle;           // same pair class: only ket position <= bra position
   const double *Ds;       // norma-scaled density N D N, n x n row-major
-  int n;
   const double *Dn;       // max |D| of each shell block, nsh x nsh
-  int nsh;
-  int screen;             // Schwarz x density screening (electrons only)
-  double eps;             // screening threshold
+  double *Gacc;           // n x n accumulator (symmetrised by the finaliser)
+  unsigned long long *count;  // quartets evaluated (may be null)
   double hf;              // 0.5 * exchange factor
-  double *Gacc;           // n x n accumulator (raw-weighted; symmetrised later)
-  BoysTables boys;
-  unsigned long long *nquartets;  // quartets evaluated (may be null)
-  // mixed precision: quartets with bound >= split go to FP64, the rest to FP32;
-  // split <= 0 sends every quartet to the precision of the kernel.
-  double split;
-  int lower;              // 1: this launch takes the quartets below split
+  int bra0, nbra, ket0, nket;
+  int n, nsh;
+  int triangle;           // same pair class: only ket position <= bra position
+  int screen;             // Schwarz x density screening (electrons only)
+  int blk0;               // first flattened block of the task
+  int nbx;                // blocks along the ket axis
 };
 
-// Fused inter-species Coulomb coupling over (A pair | B pair) quartets:
-// J_A += D_B contraction and/or J_B += D_A contraction in one pass.
-struct CouplingParams {
+// One coupling task: quartets (A pair | B pair) of two species; accumulates
+// JA += scale * sum D_B (..) and JB += scale * sum D_A (..).
+struct CPTask {
   const PairRec *pa;
   const PrimRec *pra;
-  int bra0, nbra;
   const PairRec *pb;
   const PrimRec *prb;
-  int ket0, nket;
-  const double *DsA;      // norma-scaled density of A (feeds J_B), may be null
-  const double *DsB;      // norma-scaled density of B (feeds J_A), may be null
-  int nA, nB;
+  const double *DsA;      // norma-scaled density of A (feeds JB), null if JB is null
+  const double *DsB;      // norma-scaled density of B (feeds JA), null if JA is null
   double *JA;             // nA x nA full symmetric accumulator (or null)
   double *JB;             // nB x nB (or null)
+  double scale;           // q_A q_B (1 for the reference-shaped calls)
+  int bra0, nbra, ket0, nket;
+  int nA, nB;
+  int blk0, nbx;
+};
+
+struct TaskLaunch {
+  int ntasks;
+  int nblocks;            // total flattened blocks
+  double eps;             // screening threshold
+  double split;           // mixed precision: quartets with bound >= split run in FP64
+  int lower;              // 1: this launch takes the quartets below split
+  double cut;             // coupling: |raw| < cut is dropped
   BoysTables boys;
-  double cut;             // |raw| < cut is dropped (1e-10)
 };
 
 // First-quarter transform A[nu][lam][sig] += sum_mu C_p(mu) (mu nu|lam sig).
@@ -84,10 +98,15 @@ struct SchwarzParams {
   BoysTables boys;
 };
 
-// launchers (return cudaError_t of the launch; the kernels exist for every
-// class with la, lb, lc, ld <= kMaxL)
-cudaError_t launch_jk(int pcb, int pck, bool fp32, const JKParams &p, cudaStream_t s);
-cudaError_t launch_coupling(int pcb, int pck, bool fp32, const CouplingParams &p, cudaStream_t s);
+// blocks of one task (grid tile of 32 kets x kWarpsPerBlock bras)
+inline int task_nbx(int nket) { return (nket + 31) / 32; }
+inline int task_nby(int nbra) { return (nbra + kWarpsPerBlock - 1) / kWarpsPerBlock; }
+
+// launchers (kernels exist for every class with l <= class_max_l())
+cudaError_t launch_jk_tasks(int pcb, int pck, bool fp32, const JKTask *dtasks, const TaskLaunch &tl,
+                            cudaStream_t s);
+cudaError_t launch_cp_tasks(int pcb, int pck, bool fp32, const CPTask *dtasks, const TaskLaunch &tl,
+                            cudaStream_t s);
 cudaError_t launch_it(int pcb, int pck, const ITParams &p, cudaStream_t s);
 cudaError_t launch_schwarz(int pc, const SchwarzParams &p, cudaStream_t s);
 bool class_supported(int pcb, int pck);
@@ -100,6 +119,23 @@ cudaError_t launch_symmetrize(const double *Gacc, const double *norma, int n, do
                               cudaStream_t s);
 cudaError_t launch_coupling_extract(const double *J, const double *norma, int n, double scale, int lower_only,
                                     double *out, cudaStream_t s);
+
+// batched element-wise work over many species of a batch
+struct SpeciesSlot {
+  const double *P;        // density (input)
+  double *Ds;             // N P N
+  double *Dn;             // shell-block max |P| (null: not needed)
+  const double *norma;
+  const int *shell_of;
+  double *Gacc, *Jacc;    // accumulators
+  double *G, *J;          // outputs (G may be null)
+  double gscale;          // 0.25 q^2 for the two-particle matrix
+  int n, nsh;
+  long long off;          // prefix of n*n over the slots
+};
+cudaError_t launch_prepare_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s);
+cudaError_t launch_finalize_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s);
+
 // number of kernels this library has launched (process-wide)
 void count_launches(long long n);
 long long launch_count();

@@ -304,6 +304,55 @@ struct DevBuf {
   }
 };
 
+constexpr int kNQC = kNumPairClasses * kNumPairClasses;
+
+// Tasks grouped by quartet class (bra pair class * 6 + ket pair class); one
+// device array holds every group, each group is one launch.
+template <typename T>
+struct TaskSet {
+  std::vector<T> group[kNQC];
+  T *d = nullptr;
+  size_t cap = 0;
+  int off[kNQC] = {0}, cnt[kNQC] = {0}, nblk[kNQC] = {0};
+  void clear() {
+    for (auto &g : group) g.clear();
+  }
+  void add(int cb, int ck, const T &t) { group[cb * kNumPairClasses + ck].push_back(t); }
+  // assigns blk0 / nbx and copies all groups to the device, ordered on stream s
+  bool upload(cudaStream_t s) {
+    std::vector<T> flat;
+    for (int c = 0; c < kNQC; ++c) {
+      off[c] = (int)flat.size();
+      cnt[c] = (int)group[c].size();
+      int b = 0;
+      for (T t : group[c]) {
+        t.nbx = task_nbx(t.nket);
+        t.blk0 = b;
+        b += t.nbx * task_nby(t.nbra);
+        flat.push_back(t);
+      }
+      nblk[c] = b;
+    }
+    if (flat.empty()) return true;
+    if (flat.size() > cap) {
+      if (d) cudaFree(d);
+      d = nullptr;
+      cap = 0;
+      CK(cudaMalloc(&d, flat.size() * sizeof(T)));
+      cap = flat.size();
+    }
+    // pageable source: the call returns once the data is staged, the copy is
+    // ordered on s after the kernels that read the previous contents
+    CK(cudaMemcpyAsync(d, flat.data(), flat.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return true;
+  }
+  void release() {
+    if (d) cudaFree(d);
+    d = nullptr;
+    cap = 0;
+  }
+};
+
 }  // namespace
 
 struct LibintInterface {
@@ -326,10 +375,14 @@ struct LibintInterface {
   bool have_sig = false, have_all = false;
   double *d_norma = nullptr;
   int *d_shell_of = nullptr;
-  DevBuf<double> dD, dDs, dDn, dGacc, dG, dA, dC;
+  DevBuf<double> dD, dDs, dDn, dGacc, dG, dA, dC, dDsC, dJacc;
   DevBuf<unsigned long long> dcount;
   long long last_quartets = -1;
-  long long class_quartets[kNumPairClasses * kNumPairClasses] = {0};
+  long long class_quartets[kNQC] = {0};
+  TaskSet<JKTask> jk;        // cached J/K tasks of the handle's own buffers
+  double jk_hf = 0.0;
+  bool jk_ready = false;
+  TaskSet<CPTask> cp;        // coupling tasks of the last coupling call (this handle as bra)
 
   ~LibintInterface() { release_device(); }
 
@@ -341,7 +394,11 @@ struct LibintInterface {
     d_norma = nullptr;
     d_shell_of = nullptr;
     dD.release(); dDs.release(); dDn.release(); dGacc.release(); dG.release(); dA.release(); dC.release();
+    dDsC.release(); dJacc.release();
     dcount.release();
+    jk.release();
+    cp.release();
+    jk_ready = false;
     if (stream) cudaStreamDestroy(stream);
     stream = nullptr;
     have_sig = have_all = false;
@@ -372,6 +429,7 @@ struct LibintInterface {
     if (!dev_upload(d_norma, norma)) return false;
     if (!dev_upload(d_shell_of, shell_of)) return false;
     have_sig = have_all = false;
+    jk_ready = false;
     dirty = false;
     return true;
   }
@@ -500,26 +558,36 @@ struct LibintInterface {
   bool twobody(const double *dDin, double *dGout, double factor, int precision, double split, cudaStream_t s) {
     if (!ensure_sig()) return false;
     const int n = nbasis, nsh = nshell();
-    constexpr int NQC = kNumPairClasses * kNumPairClasses;
     if (!dDs.ensure((size_t)n * n) || !dDn.ensure((size_t)nsh * nsh) || !dGacc.ensure((size_t)n * n) ||
-        !dcount.ensure(NQC))
+        !dcount.ensure(kNQC))
       return false;
+    if (!jk_ready || jk_hf != 0.5 * factor) {
+      jk.clear();
+      if (!add_jk_tasks(jk, dDs.p, dDn.p, dGacc.p, 0.5 * factor, dcount.p)) return false;
+      if (!jk.upload(s)) return false;
+      jk_hf = 0.5 * factor;
+      jk_ready = true;
+    }
     CK(launch_prepare_density(dDin, d_norma, d_shell_of, n, nsh, dDs.p, dDn.p, s));
     CK(cudaMemsetAsync(dGacc.p, 0, sizeof(double) * n * n, s));
-    CK(cudaMemsetAsync(dcount.p, 0, sizeof(unsigned long long) * NQC, s));
-    JKParams p{};
-    p.pairs = sig.d;
-    p.prims = sig.dp;
-    p.Ds = dDs.p;
-    p.n = n;
-    p.Dn = dDn.p;
-    p.nsh = nsh;
-    p.screen = is_electron ? 1 : 0;
-    p.eps = DBL_EPSILON;
-    p.hf = 0.5 * factor;
-    p.Gacc = dGacc.p;
-    p.boys = boys;
-    p.nquartets = dcount.p;
+    CK(cudaMemsetAsync(dcount.p, 0, sizeof(unsigned long long) * kNQC, s));
+    if (!launch_jk_groups(jk, precision, split, boys, s)) return false;
+    CK(launch_symmetrize(dGacc.p, d_norma, n, 0.25, dGout, s));
+    unsigned long long cnt[kNQC];
+    CK(cudaMemcpyAsync(cnt, dcount.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    last_quartets = 0;
+    for (int c = 0; c < kNQC; ++c) {
+      class_quartets[c] = (long long)cnt[c];
+      last_quartets += (long long)cnt[c];
+    }
+    return true;
+  }
+
+  // J/K tasks of this species into ts: one task per (bra class >= ket class)
+  bool add_jk_tasks(TaskSet<JKTask> &ts, const double *Ds, const double *Dn, double *Gacc, double hf,
+                    unsigned long long *counters) {
+    if (!ensure_sig()) return false;
     for (int cb = 0; cb < kNumPairClasses; ++cb)
       for (int ck = 0; ck <= cb; ++ck) {
         if (!sig.count(cb) || !sig.count(ck)) continue;
@@ -528,68 +596,57 @@ struct LibintInterface {
                     pc_lb(ck));
           return false;
         }
-        p.bra0 = sig.start[cb];
-        p.nbra = sig.count(cb);
-        p.ket0 = sig.start[ck];
-        p.nket = sig.count(ck);
-        p.triangle = cb == ck;
-        p.nquartets = dcount.p + cb * kNumPairClasses + ck;
-        if (precision == 0) {
-          p.split = 0.0;
-          CK(launch_jk(cb, ck, false, p, s));
-        } else {
-          p.split = split;
-          p.lower = 0;
-          CK(launch_jk(cb, ck, false, p, s));
-          p.lower = 1;
-          CK(launch_jk(cb, ck, true, p, s));
-        }
+        JKTask t{};
+        t.pairs = sig.d;
+        t.prims = sig.dp;
+        t.Ds = Ds;
+        t.Dn = Dn;
+        t.Gacc = Gacc;
+        t.count = counters ? counters + cb * kNumPairClasses + ck : nullptr;
+        t.hf = hf;
+        t.bra0 = sig.start[cb];
+        t.nbra = sig.count(cb);
+        t.ket0 = sig.start[ck];
+        t.nket = sig.count(ck);
+        t.n = nbasis;
+        t.nsh = nshell();
+        t.triangle = cb == ck;
+        t.screen = is_electron ? 1 : 0;
+        ts.add(cb, ck, t);
       }
-    CK(launch_symmetrize(dGacc.p, d_norma, n, 0.25, dGout, s));
-    unsigned long long cnt[NQC];
-    CK(cudaMemcpyAsync(cnt, dcount.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    last_quartets = 0;
-    for (int c = 0; c < NQC; ++c) {
-      class_quartets[c] = (long long)cnt[c];
-      last_quartets += (long long)cnt[c];
+    return true;
+  }
+
+  static bool launch_jk_groups(const TaskSet<JKTask> &ts, int precision, double split, BoysTables boys,
+                               cudaStream_t s) {
+    for (int c = 0; c < kNQC; ++c) {
+      if (!ts.cnt[c]) continue;
+      TaskLaunch tl{};
+      tl.ntasks = ts.cnt[c];
+      tl.nblocks = ts.nblk[c];
+      tl.eps = DBL_EPSILON;
+      tl.cut = 1e-10;
+      tl.boys = boys;
+      const int cb = c / kNumPairClasses, ck = c % kNumPairClasses;
+      if (precision == 0) {
+        tl.split = 0.0;
+        CK(launch_jk_tasks(cb, ck, false, ts.d + ts.off[c], tl, s));
+      } else {
+        tl.split = split;
+        tl.lower = 0;
+        CK(launch_jk_tasks(cb, ck, false, ts.d + ts.off[c], tl, s));
+        tl.lower = 1;
+        CK(launch_jk_tasks(cb, ck, true, ts.d + ts.off[c], tl, s));
+      }
     }
     return true;
   }
 };
 
-namespace {
-
-bool coupling(LibintInterface *A, LibintInterface *B, const double *dDa, const double *dDb, double *dJa,
-              double *dJb, bool fp32, cudaStream_t s) {
+// coupling tasks of species pair (A bra, B ket) into ts
+bool add_cp_tasks(TaskSet<CPTask> &ts, LibintInterface *A, LibintInterface *B, const double *DsA,
+                  const double *DsB, double *JA, double *JB, double scale) {
   if (!A->ensure_all() || !B->ensure_all()) return false;
-  const int nA = A->nbasis, nB = B->nbasis;
-  // scaled densities live in each handle's dDs buffer
-  if (dJa && (!B->dDs.ensure((size_t)nB * nB))) return false;
-  if (dJb && (!A->dDs.ensure((size_t)nA * nA))) return false;
-  if (dJa) {
-    CK(launch_scale_density(dDb, B->d_norma, nB, B->dDs.p, s));
-    if (!A->dGacc.ensure((size_t)nA * nA)) return false;
-    CK(cudaMemsetAsync(A->dGacc.p, 0, sizeof(double) * nA * nA, s));
-  }
-  if (dJb) {
-    CK(launch_scale_density(dDa, A->d_norma, nA, A->dDs.p, s));
-    if (!B->dGacc.ensure((size_t)nB * nB)) return false;
-    CK(cudaMemsetAsync(B->dGacc.p, 0, sizeof(double) * nB * nB, s));
-  }
-  CouplingParams p{};
-  p.pa = A->all.d;
-  p.pra = A->all.dp;
-  p.pb = B->all.d;
-  p.prb = B->all.dp;
-  p.DsA = dJb ? A->dDs.p : nullptr;
-  p.DsB = dJa ? B->dDs.p : nullptr;
-  p.nA = nA;
-  p.nB = nB;
-  p.JA = dJa ? A->dGacc.p : nullptr;
-  p.JB = dJb ? B->dGacc.p : nullptr;
-  p.boys = A->boys;
-  p.cut = 1e-10;
   for (int cb = 0; cb < kNumPairClasses; ++cb)
     for (int ck = 0; ck < kNumPairClasses; ++ck) {
       if (!A->all.count(cb) || !B->all.count(ck)) continue;
@@ -598,14 +655,66 @@ bool coupling(LibintInterface *A, LibintInterface *B, const double *dDa, const d
                   pc_lb(ck));
         return false;
       }
-      p.bra0 = A->all.start[cb];
-      p.nbra = A->all.count(cb);
-      p.ket0 = B->all.start[ck];
-      p.nket = B->all.count(ck);
-      CK(launch_coupling(cb, ck, fp32, p, s));
+      CPTask t{};
+      t.pa = A->all.d;
+      t.pra = A->all.dp;
+      t.pb = B->all.d;
+      t.prb = B->all.dp;
+      t.DsA = JB ? DsA : nullptr;
+      t.DsB = JA ? DsB : nullptr;
+      t.JA = JA;
+      t.JB = JB;
+      t.scale = scale;
+      t.bra0 = A->all.start[cb];
+      t.nbra = A->all.count(cb);
+      t.ket0 = B->all.start[ck];
+      t.nket = B->all.count(ck);
+      t.nA = A->nbasis;
+      t.nB = B->nbasis;
+      ts.add(cb, ck, t);
     }
-  if (dJa) CK(launch_coupling_extract(A->dGacc.p, A->d_norma, nA, 1.0, 0, dJa, s));
-  if (dJb) CK(launch_coupling_extract(B->dGacc.p, B->d_norma, nB, 1.0, 0, dJb, s));
+  return true;
+}
+
+bool launch_cp_groups(const TaskSet<CPTask> &ts, bool fp32, BoysTables boys, cudaStream_t s) {
+  for (int c = 0; c < kNQC; ++c) {
+    if (!ts.cnt[c]) continue;
+    TaskLaunch tl{};
+    tl.ntasks = ts.cnt[c];
+    tl.nblocks = ts.nblk[c];
+    tl.eps = DBL_EPSILON;
+    tl.cut = 1e-10;
+    tl.boys = boys;
+    CK(launch_cp_tasks(c / kNumPairClasses, c % kNumPairClasses, fp32, ts.d + ts.off[c], tl, s));
+  }
+  return true;
+}
+
+namespace {
+
+bool coupling(LibintInterface *A, LibintInterface *B, const double *dDa, const double *dDb, double *dJa,
+              double *dJb, bool fp32, cudaStream_t s) {
+  if (!A->ensure_all() || !B->ensure_all()) return false;
+  const int nA = A->nbasis, nB = B->nbasis;
+  // scaled densities in each handle's dDsC, accumulators in dJacc
+  if (dJa && (!B->dDsC.ensure((size_t)nB * nB) || !A->dJacc.ensure((size_t)nA * nA))) return false;
+  if (dJb && (!A->dDsC.ensure((size_t)nA * nA) || !B->dJacc.ensure((size_t)nB * nB))) return false;
+  if (dJa) {
+    CK(launch_scale_density(dDb, B->d_norma, nB, B->dDsC.p, s));
+    CK(cudaMemsetAsync(A->dJacc.p, 0, sizeof(double) * nA * nA, s));
+  }
+  if (dJb) {
+    CK(launch_scale_density(dDa, A->d_norma, nA, A->dDsC.p, s));
+    CK(cudaMemsetAsync(B->dJacc.p, 0, sizeof(double) * nB * nB, s));
+  }
+  A->cp.clear();
+  if (!add_cp_tasks(A->cp, A, B, dJb ? A->dDsC.p : nullptr, dJa ? B->dDsC.p : nullptr, dJa ? A->dJacc.p : nullptr,
+                    dJb ? B->dJacc.p : nullptr, 1.0))
+    return false;
+  if (!A->cp.upload(s)) return false;
+  if (!launch_cp_groups(A->cp, fp32, A->boys, s)) return false;
+  if (dJa) CK(launch_coupling_extract(A->dJacc.p, A->d_norma, nA, 1.0, 0, dJa, s));
+  if (dJb) CK(launch_coupling_extract(B->dJacc.p, B->d_norma, nB, 1.0, 0, dJb, s));
   return true;
 }
 
@@ -932,5 +1041,182 @@ double LowdinGB300_measure_fma_tflops(int fp64) {
 }
 
 const char *LowdinGB300_version(void) { return "lowdin_gb300 0.1 (sm_103a, FP64/FP32 Obara-Saika, l<=1 kernels)"; }
+
+}  // extern "C"
+
+// ================================================================== batches
+// A batch holds many molecular systems (each a list of species handles) whose
+// two-particle and coupling builds run together: every species' density
+// preparation in one kernel, every J/K task of a quartet class in one launch,
+// every coupling task of a class in one launch, every output in one kernel.
+// Nothing in LowdinGB300_batch_fock waits on the host, so the sequence can be
+// captured in a CUDA graph once the batch is finalised.
+struct LowdinGB300_Batch {
+  struct Spec {
+    LibintInterface *h;
+    double q, factor;
+    int two_body;
+    const double *P;
+    double *G, *J;
+    int sys;
+  };
+  std::vector<Spec> sp;
+  std::vector<int> sys_first;
+  bool finalized = false;
+  DevBuf<double> Ds, Dn, Gacc, Jacc;
+  DevBuf<unsigned long long> cnt;
+  DevBuf<SpeciesSlot> slots;
+  long long total = 0;
+  int nslots = 0;
+  TaskSet<JKTask> jk;
+  TaskSet<CPTask> cp;
+  BoysTables boys{nullptr, nullptr};
+  long long class_quartets[kNQC] = {0};
+
+  ~LowdinGB300_Batch() {
+    Ds.release(); Dn.release(); Gacc.release(); Jacc.release(); cnt.release(); slots.release();
+    jk.release(); cp.release();
+  }
+
+  bool finalize(cudaStream_t s) {
+    if (sp.empty()) {
+      set_error("batch_finalize: empty batch");
+      return false;
+    }
+    if (!device_boys(boys)) return false;
+    // device buffers of the handles
+    for (auto &x : sp) {
+      if (!x.h->ensure_all()) return false;
+      if (x.two_body && !x.h->ensure_sig()) return false;
+    }
+    // arena layout
+    std::vector<long long> off(sp.size()), dnoff(sp.size(), -1);
+    long long tot = 0, dtot = 0;
+    for (size_t k = 0; k < sp.size(); ++k) {
+      off[k] = tot;
+      tot += (long long)sp[k].h->nbasis * sp[k].h->nbasis;
+      if (sp[k].two_body && sp[k].h->is_electron) {
+        dnoff[k] = dtot;
+        dtot += (long long)sp[k].h->nshell() * sp[k].h->nshell();
+      }
+    }
+    total = tot;
+    if (!Ds.ensure(tot) || !Gacc.ensure(tot) || !Jacc.ensure(tot) || !Dn.ensure(dtot > 0 ? dtot : 1) ||
+        !cnt.ensure(kNQC))
+      return false;
+    std::vector<SpeciesSlot> hs(sp.size());
+    jk.clear();
+    cp.clear();
+    for (size_t k = 0; k < sp.size(); ++k) {
+      const Spec &x = sp[k];
+      SpeciesSlot &S = hs[k];
+      S.P = x.P;
+      S.Ds = Ds.p + off[k];
+      S.Dn = dnoff[k] >= 0 ? Dn.p + dnoff[k] : nullptr;
+      S.norma = x.h->d_norma;
+      S.shell_of = x.h->d_shell_of;
+      S.Gacc = x.two_body ? Gacc.p + off[k] : nullptr;
+      S.Jacc = Jacc.p + off[k];
+      S.G = x.G;
+      S.J = x.J;
+      S.gscale = 0.25 * x.q * x.q;
+      S.n = x.h->nbasis;
+      S.nsh = x.h->nshell();
+      S.off = off[k];
+      if (x.two_body) {
+        if (!x.h->add_jk_tasks(jk, S.Ds, S.Dn ? S.Dn : Dn.p, S.Gacc, 0.5 * x.factor, cnt.p)) return false;
+        if (!S.Dn) {
+          // non-electron species are not screened: the Dn pointer is never read
+        }
+      }
+    }
+    // coupling tasks: every species pair of a system
+    for (size_t a = 0; a < sp.size(); ++a)
+      for (size_t b = a + 1; b < sp.size(); ++b) {
+        if (sp[a].sys != sp[b].sys) continue;
+        if (!add_cp_tasks(cp, sp[a].h, sp[b].h, hs[a].Ds, hs[b].Ds, hs[a].Jacc, hs[b].Jacc, sp[a].q * sp[b].q))
+          return false;
+      }
+    nslots = (int)hs.size();
+    if (!slots.ensure(hs.size())) return false;
+    CK(cudaMemcpyAsync(slots.p, hs.data(), hs.size() * sizeof(SpeciesSlot), cudaMemcpyHostToDevice, s));
+    if (!jk.upload(s) || !cp.upload(s)) return false;
+    CK(cudaStreamSynchronize(s));
+    finalized = true;
+    return true;
+  }
+
+  bool fock(int precision, double split, cudaStream_t s) {
+    if (!finalized) {
+      set_error("batch_fock: batch not finalised");
+      return false;
+    }
+    CK(cudaMemsetAsync(Dn.p, 0, Dn.n * sizeof(double), s));
+    CK(cudaMemsetAsync(cnt.p, 0, kNQC * sizeof(unsigned long long), s));
+    CK(launch_prepare_batch(slots.p, nslots, total, s));
+    if (!LibintInterface::launch_jk_groups(jk, precision, precision ? split : 0.0, boys, s)) return false;
+    if (!launch_cp_groups(cp, precision != 0, boys, s)) return false;
+    CK(launch_finalize_batch(slots.p, nslots, total, s));
+    return true;
+  }
+};
+
+extern "C" {
+
+LowdinGB300_Batch *LowdinGB300_batch_new(void) { return new LowdinGB300_Batch(); }
+
+void LowdinGB300_batch_del(LowdinGB300_Batch *b) { delete b; }
+
+int LowdinGB300_batch_add_system(LowdinGB300_Batch *b, LibintInterface **species, int nspecies,
+                                 const double *charges, const double *factors, const int *two_body,
+                                 const double **dP, double **dG, double **dJ) {
+  if (!b || !species || nspecies <= 0) {
+    set_error("batch_add_system: invalid arguments");
+    return -1;
+  }
+  const int sys = (int)b->sys_first.size();
+  const int first = (int)b->sp.size();
+  b->sys_first.push_back(first);
+  for (int k = 0; k < nspecies; ++k) {
+    if (!check_handle(species[k], __func__)) return -1;
+    LowdinGB300_Batch::Spec x{species[k], charges[k], factors[k], two_body[k], dP[k], dG ? dG[k] : nullptr,
+                              dJ[k], sys};
+    b->sp.push_back(x);
+  }
+  b->finalized = false;
+  return first;
+}
+
+int LowdinGB300_batch_finalize(LowdinGB300_Batch *b, void *stream) {
+  if (!b) return -1;
+  return b->finalize((cudaStream_t)stream) ? 0 : -1;
+}
+
+int LowdinGB300_batch_fock(LowdinGB300_Batch *b, int precision, double split, void *stream) {
+  if (!b) return -1;
+  return b->fock(precision, split, (cudaStream_t)stream) ? 0 : -1;
+}
+
+int LowdinGB300_batch_quartets(LowdinGB300_Batch *b, long long *out, void *stream) {
+  if (!b || !b->finalized) return -1;
+  unsigned long long c[kNQC];
+  if (cudaMemcpyAsync(c, b->cnt.p, sizeof(c), cudaMemcpyDeviceToHost, (cudaStream_t)stream) != cudaSuccess ||
+      cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) {
+    set_error("batch_quartets: copy failed");
+    return -1;
+  }
+  for (int k = 0; k < kNQC; ++k) out[k] = (long long)c[k];
+  return kNQC;
+}
+
+int LowdinGB300_batch_coupling_quartets(LowdinGB300_Batch *b, long long *out) {
+  if (!b || !b->finalized) return -1;
+  for (int c = 0; c < kNQC; ++c) {
+    long long q = 0;
+    for (const auto &t : b->cp.group[c]) q += (long long)t.nbra * t.nket;
+    out[c] = q;
+  }
+  return kNQC;
+}
 
 }  // extern "C"

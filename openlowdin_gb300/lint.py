@@ -70,6 +70,20 @@ def lib():
         L.LowdinGB300_measure_fma_tflops.argtypes = [ctypes.c_int]
         L.LowdinGB300_measure_fma_tflops.restype = ctypes.c_double
         L.LowdinGB300_launch_count.restype = ctypes.c_longlong
+        L.LowdinGB300_batch_new.restype = _vp
+        L.LowdinGB300_batch_del.argtypes = [_vp]
+        L.LowdinGB300_batch_add_system.argtypes = [_vp, ctypes.POINTER(_vp), ctypes.c_int, _f64p, _f64p,
+                                                   np.ctypeslib.ndpointer(dtype=np.int32), ctypes.POINTER(_vp),
+                                                   ctypes.POINTER(_vp), ctypes.POINTER(_vp)]
+        L.LowdinGB300_batch_add_system.restype = ctypes.c_int
+        L.LowdinGB300_batch_finalize.argtypes = [_vp, _vp]
+        L.LowdinGB300_batch_finalize.restype = ctypes.c_int
+        L.LowdinGB300_batch_fock.argtypes = [_vp, ctypes.c_int, ctypes.c_double, _vp]
+        L.LowdinGB300_batch_fock.restype = ctypes.c_int
+        L.LowdinGB300_batch_quartets.argtypes = [_vp, np.ctypeslib.ndpointer(dtype=np.int64), _vp]
+        L.LowdinGB300_batch_quartets.restype = ctypes.c_int
+        L.LowdinGB300_batch_coupling_quartets.argtypes = [_vp, np.ctypeslib.ndpointer(dtype=np.int64)]
+        L.LowdinGB300_batch_coupling_quartets.restype = ctypes.c_int
         _LIB = L
     return _LIB
 
@@ -89,7 +103,69 @@ EXPORTED_SYMBOLS = [
     "LowdinGB300_potential", "LowdinGB300_twobody_device", "LowdinGB300_coupling_device",
     "LowdinGB300_last_quartets", "LowdinGB300_version", "LowdinGB300_last_class_quartets",
     "LowdinGB300_pair_class_counts", "LowdinGB300_measure_fma_tflops", "LowdinGB300_launch_count",
+    "LowdinGB300_batch_new", "LowdinGB300_batch_del", "LowdinGB300_batch_add_system",
+    "LowdinGB300_batch_finalize", "LowdinGB300_batch_fock", "LowdinGB300_batch_quartets",
+    "LowdinGB300_batch_coupling_quartets",
 ]
+
+
+class Batch:
+    """Many systems' two-particle + coupling builds in one set of launches.
+
+    add_system(handles, charges, factors, two_body, P, G, J) takes torch
+    tensors (or raw device pointers) for each species' density / outputs."""
+
+    def __init__(self):
+        self.h = lib().LowdinGB300_batch_new()
+        self._keep = []
+
+    def add_system(self, handles, charges, factors, two_body, P, G, J) -> int:
+        ns = len(handles)
+        ptr = lambda x: x if isinstance(x, int) else (0 if x is None else x.data_ptr())
+        hs = (_vp * ns)(*[h.h for h in handles])
+        pP = (_vp * ns)(*[ptr(x) for x in P])
+        pG = (_vp * ns)(*[ptr(x) for x in G])
+        pJ = (_vp * ns)(*[ptr(x) for x in J])
+        self._keep.append((handles, P, G, J))
+        k = lib().LowdinGB300_batch_add_system(self.h, hs, ns, np.ascontiguousarray(charges, np.float64),
+                                               np.ascontiguousarray(factors, np.float64),
+                                               np.ascontiguousarray(two_body, np.int32), pP, pG, pJ)
+        if k < 0:
+            _check()
+        return k
+
+    def finalize(self, stream: int = 0):
+        if lib().LowdinGB300_batch_finalize(self.h, stream) != 0:
+            _check()
+            raise LowdinGB300Error("batch finalize failed")
+
+    def fock(self, precision: int = 0, split: float = 0.0, stream: int = 0):
+        if lib().LowdinGB300_batch_fock(self.h, int(precision), float(split), stream) != 0:
+            _check()
+            raise LowdinGB300Error("batch fock failed")
+
+    def quartets(self, stream: int = 0) -> np.ndarray:
+        out = np.zeros(36, np.int64)
+        if lib().LowdinGB300_batch_quartets(self.h, out, stream) < 0:
+            _check()
+        return out.reshape(6, 6)
+
+    def coupling_quartets(self) -> np.ndarray:
+        out = np.zeros(36, np.int64)
+        lib().LowdinGB300_batch_coupling_quartets(self.h, out)
+        return out.reshape(6, 6)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().LowdinGB300_batch_del(self.h)
+            self.h = None
+        self._keep = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def launch_count() -> int:

@@ -184,102 +184,17 @@ class HostSCF:
 
 
 class DeviceSCF:
-    """SCF with every matrix resident in HBM (torch FP64 on cuda)."""
+    """SCF of one system with every matrix resident in HBM: a one-system
+    BatchSCF (the library's batched build and batched tensor algebra)."""
 
-    def __init__(self, sysd, device="cuda", precision="fp64", split=1e-5, stream=None):
-        import torch
-        self.torch = torch
+    def __init__(self, sysd, device="cuda", precision="fp64", split=1e-5):
+        from .batch_scf import BatchSCF
         self.sysd = sysd
-        self.species = sysd["species"]
-        self.dev = torch.device(device)
-        self.precision = precision
-        self.split = split
-        self.handles = [lint.Libint2Interface(sp, i + 1) for i, sp in enumerate(self.species)]
-        for h in self.handles:
-            h.init_2body_ints()
-        H, S = _one_body(self.handles, sysd)
-        self.H = [torch.tensor(x, device=self.dev) for x in H]
-        self.S = [torch.tensor(x, device=self.dev) for x in S]
-        self.X = [torch.tensor(_orthogonaliser_np(x), device=self.dev) for x in S]
-        self.enuc = nuclear_repulsion(sysd)
-        self.stream = stream
+        self.inner = BatchSCF([sysd], device=device, precision=precision, split=split)
+        self.handles = self.inner.handles[0]
 
     def close(self):
-        for h in self.handles:
-            h.close()
-
-    def _stream(self):
-        return self.torch.cuda.current_stream(self.dev).cuda_stream
+        self.inner.close()
 
     def solve(self, tol_energy=1e-8, tol_density=1e-6, max_iter=100) -> SCFResult:
-        torch = self.torch
-        t0 = time.perf_counter()
-        sp, H, S, X = self.species, self.H, self.S, self.X
-        ns = len(sp)
-        st = self._stream()
-        occ = [n_occ(s) for s in sp]
-        eta = [s["eta"] for s in sp]
-        q = [s["charge"] for s in sp]
-        P, C, eps = [], [None] * ns, [None] * ns
-        for i in range(ns):
-            e, Cp = torch.linalg.eigh(X[i].T @ H[i] @ X[i])
-            Ci = X[i] @ Cp
-            C[i], eps[i] = Ci, e
-            P.append(eta[i] * Ci[:, :occ[i]] @ Ci[:, :occ[i]].T)
-        G = [torch.zeros_like(h) for h in H]
-        Jbuf = {}
-        for i in range(ns):
-            for j in range(ns):
-                if i != j:
-                    Jbuf[(i, j)] = torch.empty_like(H[i])
-        diis = _DIIS(torch)
-        mixed = self.precision == "mixed"
-        e_old, converged, it, quartets = None, False, 0, 0
-        energy = 0.0
-        for it in range(1, max_iter + 1):
-            for i in range(ns):
-                if sp[i]["n_particles"] > 1:
-                    Pi = P[i].contiguous()
-                    self.handles[i].twobody_device(Pi.data_ptr(), G[i].data_ptr(), sp[i]["kappa"] / eta[i],
-                                                   1 if mixed else 0, self.split, st)
-                    quartets += max(0, self.handles[i].last_quartets())
-                    G[i] *= q[i] ** 2
-            for i in range(ns):
-                for j in range(i + 1, ns):
-                    Pi, Pj = P[i].contiguous(), P[j].contiguous()
-                    lint.coupling_device(self.handles[i], self.handles[j], Pi.data_ptr(), Pj.data_ptr(),
-                                         Jbuf[(i, j)].data_ptr(), Jbuf[(j, i)].data_ptr(), mixed, st)
-                    Jbuf[(i, j)] *= q[i] * q[j]
-                    Jbuf[(j, i)] *= q[i] * q[j]
-            F = []
-            en = torch.zeros((), dtype=torch.float64, device=self.dev)
-            for i in range(ns):
-                Fi = H[i] + G[i]
-                for j in range(ns):
-                    if j != i:
-                        Fi = Fi + Jbuf[(i, j)]
-                F.append(Fi)
-                en = en + torch.sum(P[i] * (H[i] + 0.5 * G[i]))
-                for j in range(i + 1, ns):
-                    en = en + torch.sum(P[i] * Jbuf[(i, j)])
-            errs = [X[i].T @ (F[i] @ P[i] @ S[i] - S[i] @ P[i] @ F[i]) @ X[i] for i in range(ns)]
-            Fx = diis(F, errs)
-            newP, dP = [], []
-            for i in range(ns):
-                e, Cp = torch.linalg.eigh(X[i].T @ Fx[i] @ X[i])
-                Ci = X[i] @ Cp
-                C[i], eps[i] = Ci, e
-                Pn = eta[i] * Ci[:, :occ[i]] @ Ci[:, :occ[i]].T
-                dP.append(torch.sqrt(torch.mean((Pn - P[i]) ** 2)))
-                newP.append(Pn)
-            stats = torch.stack([en] + dP).cpu().numpy()
-            energy = float(stats[0]) + self.enuc
-            dmax = float(np.max(stats[1:]))
-            if e_old is not None and abs(energy - e_old) < tol_energy and dmax < tol_density:
-                converged = True
-                break
-            e_old = energy
-            P = newP
-        return SCFResult(energy, it, converged, time.perf_counter() - t0,
-                         [e.cpu().numpy() for e in eps], [c.cpu().numpy() for c in C],
-                         [p.cpu().numpy() for p in P], quartets)
+        return self.inner.solve(tol_energy, tol_density, max_iter)[0]

@@ -21,10 +21,11 @@ Workloads (all basis sets uncontracted, even-tempered, Cartesian):
   water_cluster(n, seed, ...) -- n waters with uniform random rotations and
                     rejection-sampled translations (all O-O >= 5.1 bohr) in a
                     cube of edge 5.1*ceil(n^(1/3))*1.5 bohr.
-                    quantum_protons=True: every H is a quantum proton (one H_1
-                    species, s 4, 8, 16, 24 and p 16 per proton, mass
-                    1836.15267247); O stays a point charge.  4 waters -> e- 136
-                    functions, H_1 56 functions, 8 protons.
+                    quantum_protons=True: every H is a quantum proton (s 4, 8,
+                    16, 24 and p 16 per proton, mass 1836.15267247), by default
+                    each its own one-particle species; O stays a point charge.
+                    4 waters -> e- 136 functions + 8 proton species of 7
+                    functions (56 in total).
                     o_d=True: one Cartesian d shell (exponent 1.2) on O
                     (40 functions per water).
   chain_molecule(seed, ...) -- H/C/N/O self-avoiding chain, 3-30 atoms,
@@ -121,7 +122,12 @@ def water(d_shell=False):
     return water_cluster(1, seed=0, quantum_protons=False, o_d=d_shell, place=False)
 
 
-def water_cluster(n_waters: int, seed: int = 0, quantum_protons=False, o_d=False, place=True):
+def water_cluster(n_waters: int, seed: int = 0, quantum_protons=False, o_d=False, place=True,
+                  proton_species_mode="per_proton"):
+    """proton_species_mode: "per_proton" gives every quantum proton its own
+    one-particle species (H-1_1, H-2_1, ..., the convention of the reference's
+    APMO tests, e.g. H-a_1 / H-b_1 in test/H2O.APMO.MP2.lowdin); "single" puts
+    all protons in one H_1 species (fermions with exchange)."""
     mols = cluster_positions(n_waters, seed) if place else [water_geometry()]
     e_shells, p_shells, Z, R = [], [], [], []
     for O, H1, H2 in mols:
@@ -129,12 +135,16 @@ def water_cluster(n_waters: int, seed: int = 0, quantum_protons=False, o_d=False
         e_shells += _h_shells(H1) + _h_shells(H2)
         Z.append(8.0); R.append(list(O))
         if quantum_protons:
-            p_shells += _proton_shells(H1) + _proton_shells(H2)
+            p_shells.append(_proton_shells(H1))
+            p_shells.append(_proton_shells(H2))
         else:
             Z += [1.0, 1.0]; R += [list(H1), list(H2)]
     species = [electron_species(e_shells, 10 * len(mols))]
     if quantum_protons:
-        species.append(proton_species(p_shells, 2 * len(mols)))
+        if proton_species_mode == "single":
+            species.append(proton_species([s for p in p_shells for s in p], 2 * len(mols)))
+        else:
+            species += [proton_species(p, 1, name=f"H-{k + 1}_1") for k, p in enumerate(p_shells)]
     return {"species": species, "point_charges": Z, "point_positions": R,
             "name": f"water{len(mols)}" + ("-apmo" if quantum_protons else "") + ("-d" if o_d else "")}
 

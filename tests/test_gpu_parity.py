@@ -61,7 +61,7 @@ def test_twobody_contracted_golden_basis(L, oracle, golden):
 
 def test_twobody_protons_unscreened(L, oracle):
     """Non-electron species: no Schwarz screening, factor kappa/eta = -1."""
-    sysd = S.water_cluster(2, seed=1, quantum_protons=True)
+    sysd = S.water_cluster(2, seed=1, quantum_protons=True, proton_species_mode="single")
     sp = sysd["species"][1]
     rng = np.random.default_rng(5)
     D = _sym(rng, S.nbasis(sp), 0.05)
@@ -88,7 +88,7 @@ def test_twobody_apmo_cluster_electrons(L, oracle):
 
 @pytest.mark.parametrize("ids", [(1, 2), (2, 1)])
 def test_coupling_both_orders(L, oracle, ids):
-    sysd = S.water_cluster(1, seed=0, quantum_protons=True, place=False)
+    sysd = S.water_cluster(1, seed=0, quantum_protons=True, place=False, proton_species_mode="single")
     e, p = sysd["species"]
     rng = np.random.default_rng(4)
     Dp = _sym(rng, S.nbasis(p), 0.2)
@@ -118,7 +118,7 @@ def test_first_quarter_intra(L, oracle):
 
 
 def test_first_quarter_coupling(L, oracle):
-    sysd = S.water_cluster(1, seed=0, quantum_protons=True, place=False)
+    sysd = S.water_cluster(1, seed=0, quantum_protons=True, place=False, proton_species_mode="single")
     e, p = sysd["species"]
     ne = S.nbasis(e)
     rng = np.random.default_rng(8)
@@ -134,7 +134,7 @@ def test_first_quarter_coupling(L, oracle):
 
 def test_device_entry_points_match_host_calls(L, oracle):
     torch = pytest.importorskip("torch")
-    sysd = S.water_cluster(1, seed=0, quantum_protons=True, place=False)
+    sysd = S.water_cluster(1, seed=0, quantum_protons=True, place=False, proton_species_mode="single")
     e, p = sysd["species"]
     rng = np.random.default_rng(9)
     De, Dp = _sym(rng, S.nbasis(e), 0.2), _sym(rng, S.nbasis(p), 0.2)

@@ -125,7 +125,7 @@ def test_first_quarter_restatement(oracle):
 
 
 def test_coupling_restatement(oracle, golden):
-    sysd = S.water_cluster(1, 0, quantum_protons=True, place=False)
+    sysd = S.water_cluster(1, 0, quantum_protons=True, place=False, proton_species_mode="single")
     e = oracle.Basis.from_shells(sysd["species"][0]["shells"])
     p = oracle.Basis.from_shells(sysd["species"][1]["shells"])
     rng = np.random.default_rng(3)
