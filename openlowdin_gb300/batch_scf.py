@@ -44,9 +44,10 @@ class _Group:
 class BatchSCF:
     """SCF of many independent systems at once on one GPU."""
 
-    def __init__(self, systems, device="cuda", precision="fp64", split=1e-5, diis_size=10):
+    def __init__(self, systems, device="cuda", precision="fp64", split=1e-5, diis_size=10, rebuild_every=8):
         import torch
         self.torch = torch
+        self.rebuild_every = rebuild_every
         self.dev = torch.device(device)
         self.systems = systems
         self.precision = precision
@@ -80,6 +81,11 @@ class BatchSCF:
             g.P = torch.zeros((m, g.n, g.n), dtype=torch.float64, device=self.dev)
             g.G = torch.zeros_like(g.P)
             g.J = torch.zeros_like(g.P)
+            # library build buffers: input density (P or P - P_ref) and outputs
+            g.Pin = torch.zeros_like(g.P)
+            g.Gb = torch.zeros_like(g.P)
+            g.Jb = torch.zeros_like(g.P)
+            g.Pref = torch.zeros_like(g.P)
         self.enuc = torch.tensor([nuclear_repulsion(s) for s in systems], dtype=torch.float64, device=self.dev)
         self.nsys = len(systems)
         # library batch: species buffers are slices of the stacked tensors
@@ -90,7 +96,7 @@ class BatchSCF:
             for k, sp in enumerate(sps):
                 key, slot = self.where[si][k]
                 g = groups[key]
-                P.append(g.P[slot]); G.append(g.G[slot]); J.append(g.J[slot])
+                P.append(g.Pin[slot]); G.append(g.Gb[slot]); J.append(g.Jb[slot])
             self.batch.add_system(self.handles[si], [sp["charge"] for sp in sps],
                                   [sp["kappa"] / sp["eta"] for sp in sps],
                                   [1 if sp["n_particles"] > 1 else 0 for sp in sps], P, G, J)
@@ -105,6 +111,37 @@ class BatchSCF:
                 h.close()
 
     # --------------------------------------------------------------- pieces --
+    def _purify(self, g, F, max_iter=200, tol=1e-11):
+        """Density of the n_occ lowest orbitals of F (all species of the group
+        at once) by trace-conserving canonical purification (Palser and
+        Manolopoulos, Phys. Rev. B 58, 12704 (1998)): batched GEMMs and traces
+        only, no eigensolver.  Returns eta X P' X^T."""
+        torch = self.torch
+        Fp = g.X.transpose(1, 2) @ F @ g.X
+        m, n = Fp.shape[0], Fp.shape[-1]
+        N = float(g.occ)
+        I = torch.eye(n, dtype=Fp.dtype, device=Fp.device).expand(m, n, n)
+        d = torch.diagonal(Fp, dim1=1, dim2=2)
+        r = Fp.abs().sum(-1) - d.abs()
+        fmin = (d - r).min(-1).values
+        fmax = (d + r).max(-1).values
+        mu = d.mean(-1)
+        lam = torch.minimum(N / (fmax - mu), (n - N) / (mu - fmin))
+        P = (lam / n)[:, None, None] * (mu[:, None, None] * I - Fp) + (N / n) * I
+        for it in range(max_iter):
+            P2 = P @ P
+            P3 = P2 @ P
+            t1 = torch.diagonal(P - P2, dim1=1, dim2=2).sum(-1)
+            t2 = torch.diagonal(P2 - P3, dim1=1, dim2=2).sum(-1)
+            c = torch.where(t1.abs() > 1e-300, t2 / t1, torch.full_like(t1, 0.5))
+            up = ((1 + c)[:, None, None] * P2 - P3) / c[:, None, None]
+            lo = ((1 - 2 * c)[:, None, None] * P + (1 + c)[:, None, None] * P2 - P3) / (1 - c)[:, None, None]
+            P = torch.where((c >= 0.5)[:, None, None], up, lo)
+            if it % 8 == 7 and float(t1.abs().max()) < tol:
+                break
+        P = 0.5 * (P + P.transpose(1, 2))
+        return g.eta * (g.X @ P @ g.X.transpose(1, 2))
+
     def _diag(self, g, F):
         torch = self.torch
         Fp = g.X.transpose(1, 2) @ F @ g.X
@@ -119,9 +156,9 @@ class BatchSCF:
         stream = torch.cuda.current_stream(self.dev).cuda_stream
         groups = list(self.groups.values())
         for g in groups:
-            g.eps, g.C, P = self._diag(g, g.H)
-            g.P.copy_(P)
-        prec = 1 if self.precision == "mixed" else 0
+            g.P.copy_(self._purify(g, g.H))       # core-Hamiltonian guess
+            g.Flast = g.H.clone()
+        mixed = self.precision == "mixed"
         hist_F, hist_E = [], []         # per iteration: list over groups
         hist_B = []                      # per iteration: dots with earlier entries [nsys, h]
         e_old = np.full(self.nsys, np.nan)
@@ -132,7 +169,26 @@ class BatchSCF:
         quartets = 0
         it = 0
         for it in range(1, max_iter + 1):
-            self.batch.fock(prec, self.split, stream)
+            # plain: full build from P every iteration (the reference's scheme).
+            # mixed: incremental build from dP = P - P_ref on top of the previous
+            # matrices, full FP64 rebuild on the first and every rebuild_every-th
+            # iteration; quartets whose Schwarz x |dP| bound is below the split
+            # run in FP32 (two-particle) and incremental couplings run in FP32.
+            full = (not mixed) or (it - 1) % self.rebuild_every == 0
+            for g in groups:
+                if full:
+                    g.Pin.copy_(g.P)
+                else:
+                    torch.sub(g.P, g.Pref, out=g.Pin)
+            self.batch.fock(0 if full else 3, self.split, stream)
+            for g in groups:
+                if full:
+                    g.G.copy_(g.Gb)
+                    g.J.copy_(g.Jb)
+                else:
+                    g.G += g.Gb
+                    g.J += g.Jb
+                g.Pref.copy_(g.P)
             energy = self.enuc.clone()
             Fs, Es = [], []
             for g in groups:
@@ -179,13 +235,12 @@ class BatchSCF:
                 else:
                     c = coef[g.sys_index]                               # [m, h]
                     Fx = sum(c[:, j, None, None] * hist_F[j][gi] for j in range(h))
-                e, C, Pn = self._diag(g, Fx)
+                Pn = self._purify(g, Fx)
                 keep = frozen[g.sys_index]
                 d = torch.sqrt(torch.mean((Pn - g.P) ** 2, dim=(1, 2)))
-                dP = torch.maximum(dP, torch.zeros_like(dP).index_reduce_(0, g.sys_index, d, "amax"))
+                dP = torch.maximum(dP, torch.zeros_like(dP).scatter_reduce_(0, g.sys_index, d, reduce="amax"))
                 Pn = torch.where(keep[:, None, None], g.P, Pn)
-                g.eps = torch.where(keep[:, None], g.eps, e)
-                g.C = torch.where(keep[:, None, None], g.C, C)
+                g.Flast = torch.where(keep[:, None, None], g.Flast, Fs[gi])
                 g.P.copy_(Pn)
             stats = torch.stack([energy, dP]).cpu().numpy()
             en, dpn = stats[0], stats[1]
@@ -200,6 +255,9 @@ class BatchSCF:
                 frozen |= torch.tensor(newly, device=self.dev)
             if conv.all():
                 break
+        # Roothaan orbitals of the last Fock matrix of every species (one eigh)
+        for g in groups:
+            g.eps, g.C, _ = self._diag(g, g.Flast)
         q = self.batch.quartets(stream)
         quartets = int(q.sum())
         self.last_class_quartets = q

@@ -1154,8 +1154,9 @@ struct LowdinGB300_Batch {
     CK(cudaMemsetAsync(Dn.p, 0, Dn.n * sizeof(double), s));
     CK(cudaMemsetAsync(cnt.p, 0, kNQC * sizeof(unsigned long long), s));
     CK(launch_prepare_batch(slots.p, nslots, total, s));
-    if (!LibintInterface::launch_jk_groups(jk, precision, precision ? split : 0.0, boys, s)) return false;
-    if (!launch_cp_groups(cp, precision != 0, boys, s)) return false;
+    const int jk_mixed = precision & 1;
+    if (!LibintInterface::launch_jk_groups(jk, jk_mixed, jk_mixed ? split : 0.0, boys, s)) return false;
+    if (!launch_cp_groups(cp, (precision & 2) != 0, boys, s)) return false;
     CK(launch_finalize_batch(slots.p, nslots, total, s));
     return true;
   }
