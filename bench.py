@@ -46,7 +46,34 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=4, help="molecules per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-fock", type=int, default=0,
+                    help="profiling case: N batched Fock builds (FP64) of the step's molecules at the "
+                         "core-Hamiltonian-guess densities, then exit")
     return ap.parse_args()
+
+
+def profile_fock(args):
+    """Small, self-contained case for ncu: setup + N batched builds."""
+    import torch
+    from openlowdin_gb300.batch_scf import BatchSCF
+    torch.cuda.set_device(0)
+    mols = systems_for(0, args.batch)
+    s = BatchSCF(mols)
+    st = torch.cuda.current_stream().cuda_stream
+    for g in s.groups.values():
+        g.Pin.copy_(s._purify(g, g.H))
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(args.profile_fock):
+        s.batch.fock(0, 0.0, st)
+    b.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_fock_builds": args.profile_fock, "molecules": args.batch,
+                      "ms_per_build": a.elapsed_time(b) / max(1, args.profile_fock)}))
+    s.close()
+    return 0
 
 
 def systems_for(rank, batch):
@@ -174,6 +201,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_fock:
+        return profile_fock(args)
     import numpy as np
     import torch
     from openlowdin_gb300 import flops as FL
