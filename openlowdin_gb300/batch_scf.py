@@ -24,6 +24,8 @@ import numpy as np
 from . import lint
 from .scf import SCFResult, _one_body, _orthogonaliser_np, n_occ, nuclear_repulsion
 
+HOST_EIGH_MAX = 512   # matrices below this size are diagonalised on the host
+
 
 @dataclass
 class _Group:
@@ -44,7 +46,7 @@ class _Group:
 class BatchSCF:
     """SCF of many independent systems at once on one GPU."""
 
-    def __init__(self, systems, device="cuda", precision="fp64", split=1e-5, diis_size=10, rebuild_every=8):
+    def __init__(self, systems, device="cuda", precision="fp64", split=1e-5, diis_size=10, rebuild_every=1000):
         import torch
         self.torch = torch
         self.rebuild_every = rebuild_every
@@ -142,6 +144,38 @@ class BatchSCF:
         P = 0.5 * (P + P.transpose(1, 2))
         return g.eta * (g.X @ P @ g.X.transpose(1, 2))
 
+    _pool = None
+
+    def _density(self, g, F):
+        """eta C_occ C_occ^T of the Roothaan problem F C = S C e.  Matrices
+        below HOST_EIGH_MAX functions are diagonalised by LAPACK on a host
+        thread pool (a 136 x 136 FP64 eigensolve takes ~2 ms there against
+        ~5 ms for the GPU solver, whose cost is latency, not arithmetic);
+        larger ones use the GPU solver.  The orthogonal transforms and the
+        density product stay on the GPU."""
+        torch = self.torch
+        Fp = g.X.transpose(1, 2) @ F @ g.X
+        if g.n >= HOST_EIGH_MAX:
+            e, Cp = torch.linalg.eigh(Fp)
+            Co = g.X @ Cp[:, :, :g.occ]
+            return g.eta * Co @ Co.transpose(1, 2)
+        import concurrent.futures as cf
+        import os
+        if BatchSCF._pool is None:
+            BatchSCF._pool = cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)))
+        host = Fp.cpu().numpy()
+        occ = g.occ
+        vecs = np.empty((host.shape[0], host.shape[1], occ))
+
+        def work(i):
+            w, V = np.linalg.eigh(host[i])
+            vecs[i] = V[:, :occ]
+
+        list(BatchSCF._pool.map(work, range(host.shape[0])))
+        Cp = torch.from_numpy(vecs).to(self.dev, non_blocking=True)
+        Co = g.X @ Cp
+        return g.eta * Co @ Co.transpose(1, 2)
+
     def _diag(self, g, F):
         torch = self.torch
         Fp = g.X.transpose(1, 2) @ F @ g.X
@@ -156,7 +190,7 @@ class BatchSCF:
         stream = torch.cuda.current_stream(self.dev).cuda_stream
         groups = list(self.groups.values())
         for g in groups:
-            g.P.copy_(self._purify(g, g.H))       # core-Hamiltonian guess
+            g.P.copy_(self._density(g, g.H))      # core-Hamiltonian guess
             g.Flast = g.H.clone()
         mixed = self.precision == "mixed"
         hist_F, hist_E = [], []         # per iteration: list over groups
@@ -171,16 +205,18 @@ class BatchSCF:
         for it in range(1, max_iter + 1):
             # plain: full build from P every iteration (the reference's scheme).
             # mixed: incremental build from dP = P - P_ref on top of the previous
-            # matrices, full FP64 rebuild on the first and every rebuild_every-th
-            # iteration; quartets whose Schwarz x |dP| bound is below the split
-            # run in FP32 (two-particle) and incremental couplings run in FP32.
+            # matrices, a full build (FP64 couplings) on the first and every
+            # rebuild_every-th iteration; two-particle quartets whose Schwarz x
+            # |dP| bound is below the split run in FP32, the rest in FP64, and
+            # incremental couplings run in FP32 (their size scales with |dP|).
             full = (not mixed) or (it - 1) % self.rebuild_every == 0
             for g in groups:
                 if full:
                     g.Pin.copy_(g.P)
                 else:
                     torch.sub(g.P, g.Pref, out=g.Pin)
-            self.batch.fock(0 if full else 3, self.split, stream)
+            # precision bits: 1 = two-particle split FP32/FP64, 2 = FP32 coupling
+            self.batch.fock(0 if not mixed else (1 if full else 3), self.split, stream)
             for g in groups:
                 if full:
                     g.G.copy_(g.Gb)
@@ -235,7 +271,7 @@ class BatchSCF:
                 else:
                     c = coef[g.sys_index]                               # [m, h]
                     Fx = sum(c[:, j, None, None] * hist_F[j][gi] for j in range(h))
-                Pn = self._purify(g, Fx)
+                Pn = self._density(g, Fx)
                 keep = frozen[g.sys_index]
                 d = torch.sqrt(torch.mean((Pn - g.P) ** 2, dim=(1, 2)))
                 dP = torch.maximum(dP, torch.zeros_like(dP).scatter_reduce_(0, g.sys_index, d, reduce="amax"))

@@ -55,24 +55,37 @@ __device__ __forceinline__ void sfor(F &&f) {
 // ---- device records ---------------------------------------------------------
 // One shell pair of a species, stored in canonical order (la >= lb).  Pairs are
 // grouped by class (la, lb) and, inside a class, sorted by decreasing Schwarz
-// factor so that a contiguous range is one class.
-struct alignas(16) PairRec {
+// factor so that a contiguous range is one class.  R = double for the FP64
+// kernels, float for the FP32 kernels (a separate copy, so the FP32 kernels
+// issue no FP64 conversions).
+template <typename R>
+struct alignas(16) PairT {
   int sa, sb;      // shell indices inside the species
   int fa, fb;      // first basis function of each shell
   int prim0, nprim;// primitive-pair range
   int la, lb;
-  double A[3];     // centre of shell a
-  double AB[3];    // A - B
-  double Q;        // Schwarz factor sqrt(max |(ab|ab)|) of raw integrals
-  double pad;
+  R A[3];          // centre of shell a
+  R AB[3];         // A - B
+  R Q;             // Schwarz factor sqrt(max |(ab|ab)|) of raw integrals
+  R pad;
 };
+using PairRec = PairT<double>;
+using PairRec32 = PairT<float>;
 
-// One primitive pair: exponent sum, Gaussian-product centre and the prefactor
-// exp(-ab/p |AB|^2) * c_a N_a * c_b N_b (coefficient times the primitive norm
-// of the x^l component).
-struct alignas(16) PrimRec {
-  double p, Px, Py, Pz, K, pad;
+// One primitive pair: exponent sum p, its reciprocal, the Gaussian-product
+// centre P, P - A, and Kt = sqrt(2 pi^{5/2}) exp(-ab/p |AB|^2) c_a N_a c_b N_b / p
+// (coefficients times the primitive norm of the x^l component), so that the
+// quartet prefactor is Kt_ab Kt_cd / sqrt(p + q).
+template <typename R>
+struct alignas(16) PrimT {
+  R p, inv_p, Kt, pad;
+  R P[3];
+  R PA[3];
 };
+using PrimRec = PrimT<double>;
+using PrimRec32 = PrimT<float>;
+
+constexpr double kSqrt2Pi52 = 5.914967172795612;  // sqrt(2 pi^{5/2})
 
 // ---- Boys function ----------------------------------------------------------
 // F_m(T) = int_0^1 t^{2m} exp(-T t^2) dt.
@@ -113,7 +126,9 @@ __device__ __forceinline__ void boys_f64(double T, double (&F)[L + 1], const dou
   }
 }
 
-// FP32 Boys: Taylor about the float table; large arguments are evaluated in FP64.
+// FP32 Boys: Taylor about the float table; for T >= 36 the closed form
+// sqrt(pi/T)/2 (erfc(6) < 3e-17 relative) with the upward recursion, both exact
+// to FP32 rounding, so no FP64 instruction is issued.
 template <int L>
 __device__ __forceinline__ void boys_f32(float T, float (&F)[L + 1], const float *__restrict__ tab) {
   if (T < (float)kBoysTMax) {
@@ -131,16 +146,11 @@ __device__ __forceinline__ void boys_f32(float T, float (&F)[L + 1], const float
       for (int m = L - 1; m >= 0; --m) F[m] = fmaf(twoT, F[m + 1], e) * (1.0f / (2 * m + 1));
     }
   } else {
-    const double Td = T;
-    const double e = exp(-Td);
-    double f = 0.88622692545275801365 / sqrt(Td);
-    F[0] = (float)f;
-    const double o2T = 0.5 / Td;
+    const float e = __expf(-T);
+    F[0] = 0.886226925f * rsqrtf(T);
+    const float o2T = 0.5f / T;
 #pragma unroll
-    for (int m = 0; m < L; ++m) {
-      f = ((2 * m + 1) * f - e) * o2T;
-      F[m + 1] = (float)f;
-    }
+    for (int m = 0; m < L; ++m) F[m + 1] = fmaf((float)(2 * m + 1), F[m], -e) * o2T;
   }
 }
 

@@ -35,30 +35,31 @@ struct QClass {
 // Accumulate one primitive quartet into X[(e-E0)*nF + (f-F0)].
 template <typename R, int LA, int LB, int LC, int LD>
 __device__ __forceinline__ void vrr_prim(R (&X)[QClass<LA, LB, LC, LD>::nE * QClass<LA, LB, LC, LD>::nF],
-                                         R p, const R (&P)[3], const R (&A)[3], R Kab,
-                                         R q, const R (&Q)[3], const R (&C)[3], R Kcd,
-                                         const double *boys64, const float *boys32) {
+                                         const PrimT<R> &pb, const PrimT<R> &pk, const double *boys64,
+                                         const float *boys32) {
   using QC_ = QClass<LA, LB, LC, LD>;
   constexpr int L = QC_::L, L2 = QC_::L2, NE = QC_::NE, NF = QC_::NF, E0 = QC_::E0, F0 = QC_::F0,
                 nF = QC_::nF;
-  const R pq = p + q;
-  const R opq = R(1) / pq;
-  const R rho = p * q * opq;
+  const R p = pb.p, q = pk.p;
+  const R opq = R(1) / (p + q);
+  const R rp = q * opq;          // rho / p
+  const R rq = p * opq;          // rho / q
+  const R rho = p * rq;
   R PQ2 = 0, PA[3], WP[3], QCv[3], WQ[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const R W = (p * P[d] + q * Q[d]) * opq;
-    PA[d] = P[d] - A[d];
-    WP[d] = W - P[d];
-    QCv[d] = Q[d] - C[d];
-    WQ[d] = W - Q[d];
-    PQ2 += (P[d] - Q[d]) * (P[d] - Q[d]);
+    const R PQ = pb.P[d] - pk.P[d];
+    PA[d] = pb.PA[d];
+    QCv[d] = pk.PA[d];
+    WP[d] = -rp * PQ;            // W - P = q (Q - P) / (p + q)
+    WQ[d] = rq * PQ;             // W - Q = p (P - Q) / (p + q)
+    PQ2 += PQ * PQ;
   }
   R F[L + 1];
   BoysTab<R>::template eval<L>(rho * PQ2, F, boys64, boys32);
-  // 2 pi^{5/2} = 34.986836655249725
-  const R pref = R(34.986836655249725) / (p * q * sqrt(pq)) * Kab * Kcd;
-  const R o2p = R(0.5) / p, o2q = R(0.5) / q, o2pq = R(0.5) * opq, rp = rho / p, rq = rho / q;
+  // 2 pi^{5/2} K_ab K_cd / (p q sqrt(p + q)) with the constants folded into Kt
+  const R pref = pb.Kt * pk.Kt * sqrt(opq);
+  const R o2p = R(0.5) * pb.inv_p, o2q = R(0.5) * pk.inv_p, o2pq = R(0.5) * opq;
 
   // bra nodes Vb[e][m], m <= L - |e|
   R Vb[NE][L + 1];
@@ -205,27 +206,23 @@ __device__ __forceinline__ void hrr_ket(const R *in, const R (&CD)[3], R *out) {
 // Full contracted quartet: out[NA*NB*NC*ND] row-major (a, b, c, d).  The bra
 // and ket primitive pairs may come from different species.
 template <typename R, int LA, int LB, int LC, int LD>
-__device__ __forceinline__ void eri_quartet(const PairRec &bra, const PrimRec *__restrict__ pbra,
-                                            const PairRec &ket, const PrimRec *__restrict__ pket,
+__device__ __forceinline__ void eri_quartet(const PairT<R> &bra, const PrimT<R> *__restrict__ pbra,
+                                            const PairT<R> &ket, const PrimT<R> *__restrict__ pket,
                                             const double *boys64, const float *boys32,
                                             R (&out)[QClass<LA, LB, LC, LD>::NINT]) {
   using QC_ = QClass<LA, LB, LC, LD>;
   R X[QC_::nE * QC_::nF];
 #pragma unroll
   for (int i = 0; i < QC_::nE * QC_::nF; ++i) X[i] = R(0);
-  const R A[3] = {R(bra.A[0]), R(bra.A[1]), R(bra.A[2])};
-  const R C[3] = {R(ket.A[0]), R(ket.A[1]), R(ket.A[2])};
   for (int ib = 0; ib < bra.nprim; ++ib) {
-    const PrimRec pb = pbra[bra.prim0 + ib];
-    const R P[3] = {R(pb.Px), R(pb.Py), R(pb.Pz)};
+    const PrimT<R> pb = pbra[bra.prim0 + ib];
     for (int ik = 0; ik < ket.nprim; ++ik) {
-      const PrimRec pk = pket[ket.prim0 + ik];
-      const R Q[3] = {R(pk.Px), R(pk.Py), R(pk.Pz)};
-      vrr_prim<R, LA, LB, LC, LD>(X, R(pb.p), P, A, R(pb.K), R(pk.p), Q, C, R(pk.K), boys64, boys32);
+      const PrimT<R> pk = pket[ket.prim0 + ik];
+      vrr_prim<R, LA, LB, LC, LD>(X, pb, pk, boys64, boys32);
     }
   }
-  const R AB[3] = {R(bra.AB[0]), R(bra.AB[1]), R(bra.AB[2])};
-  const R CD[3] = {R(ket.AB[0]), R(ket.AB[1]), R(ket.AB[2])};
+  const R AB[3] = {bra.AB[0], bra.AB[1], bra.AB[2]};
+  const R CD[3] = {ket.AB[0], ket.AB[1], ket.AB[2]};
   R Y[QC_::NA * QC_::NB * QC_::nF];
   hrr<R, LA, LB, QC_::nF>(X, AB, Y);
   hrr_ket<R, LC, LD, QC_::NA * QC_::NB>(Y, CD, out);

@@ -2,6 +2,8 @@
 // coupling and first-quarter transforms.  Included by the translation units
 // that instantiate them for a set of quartet classes.
 #pragma once
+#include <type_traits>
+
 #include "eri.cuh"
 #include "kernels.cuh"
 
@@ -14,13 +16,14 @@ __device__ __forceinline__ R warp_sum(R v) {
   return v;
 }
 
-__device__ __forceinline__ double dnorm6(const double *__restrict__ Dn, int nsh, int a, int b, int c, int d) {
-  double m = __ldg(Dn + a * nsh + b);
-  m = fmax(m, __ldg(Dn + a * nsh + c));
-  m = fmax(m, __ldg(Dn + b * nsh + c));
-  m = fmax(m, __ldg(Dn + a * nsh + d));
-  m = fmax(m, __ldg(Dn + b * nsh + d));
-  m = fmax(m, __ldg(Dn + c * nsh + d));
+template <typename T>
+__device__ __forceinline__ T dnorm6(const T *__restrict__ Dn, int nsh, int a, int b, int c, int d) {
+  T m = __ldg(Dn + a * nsh + b);
+  m = max(m, __ldg(Dn + a * nsh + c));
+  m = max(m, __ldg(Dn + b * nsh + c));
+  m = max(m, __ldg(Dn + a * nsh + d));
+  m = max(m, __ldg(Dn + b * nsh + d));
+  m = max(m, __ldg(Dn + c * nsh + d));
   return m;
 }
 
@@ -34,6 +37,12 @@ __device__ __forceinline__ int find_task(const T *__restrict__ tasks, int ntasks
     else hi = mid - 1;
   }
   return lo;
+}
+
+template <typename R>
+__device__ __forceinline__ void atomic_acc(double *g64, float *g32, size_t i, R v) {
+  if constexpr (std::is_same<R, double>::value) atomicAdd(g64 + i, v);
+  else atomicAdd(g32 + i, v);
 }
 
 // ----------------------------------------------------------------- Schwarz --
@@ -58,9 +67,14 @@ __global__ void __launch_bounds__(128) schwarz_kernel(SchwarzParams P) {
 // Digestion follows the six updates of a permutation-unique quartet
 // (g12 += D34 v, g34 += D12 v, g13/g24/g14/g23 += 0.5 f D v, all x degeneracy);
 // with G = (Gacc + Gacc^T)/4 this is J[D] + f K[D].
+// Screening bound: plain launches (split = 0) use the FP64 product
+// Q_ab Q_cd max|D| as the reference does; mixed launches compute it in FP32
+// from the FP32 records in both kernels, so each quartet lands in exactly one
+// of the FP64 (bound >= split) and FP32 (bound < split) launches.
 template <typename R, int LA, int LB, int LC, int LD>
 __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict__ tasks, TaskLaunch TL) {
   using Q = QClass<LA, LB, LC, LD>;
+  constexpr bool F64 = std::is_same<R, double>::value;
   constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND;
   const int t = find_task(tasks, TL.ntasks, blockIdx.x);
   const JKTask &T = tasks[t];
@@ -73,15 +87,26 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
   bool active = kpos < T.nket && (!T.triangle || kpos <= bpos);
   const int bi = T.bra0 + bpos;
   const int ki = T.ket0 + min(kpos, T.nket - 1);
-  const PairRec &bra = T.pairs[bi];
-  const PairRec ket = T.pairs[ki];
-  double bound = bra.Q * ket.Q;
-  if (T.screen) {
-    bound *= dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
-    if (bound < TL.eps) active = false;
+  const PairT<R> *pairs;
+  const PrimT<R> *prims;
+  const R *D;
+  if constexpr (F64) {
+    pairs = T.pairs; prims = T.prims; D = T.Ds;
+  } else {
+    pairs = T.pairs32; prims = T.prims32; D = T.Ds32;
   }
+  const PairT<R> &bra = pairs[bi];
+  const PairT<R> ket = pairs[ki];
   if (TL.split > 0.0) {
-    if (TL.lower ? !(bound < TL.split) : (bound < TL.split)) active = false;
+    float b = T.pairs32[bi].Q * T.pairs32[ki].Q;
+    if (T.screen) {
+      b *= dnorm6(T.Dn32, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
+      if (b < (float)TL.eps) active = false;
+    }
+    if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) active = false;
+  } else if (T.screen) {
+    const double b = T.pairs[bi].Q * T.pairs[ki].Q * dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
+    if (b < TL.eps) active = false;
   }
   if (__all_sync(0xffffffffu, !active)) return;
   if (T.count) {
@@ -90,16 +115,16 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
   }
   R I[Q::NINT];
   if (active) {
-    eri_quartet<R, LA, LB, LC, LD>(bra, T.prims, ket, T.prims, TL.boys.f64, TL.boys.f32, I);
+    eri_quartet<R, LA, LB, LC, LD>(bra, prims, ket, prims, TL.boys.f64, TL.boys.f32, I);
   } else {
 #pragma unroll
     for (int x = 0; x < Q::NINT; ++x) I[x] = R(0);
   }
   const R deg = active ? R((bra.sa == bra.sb ? 1 : 2) * (ket.sa == ket.sb ? 1 : 2) * (bi == ki ? 1 : 2)) : R(0);
   const R hdeg = deg * R(T.hf);
-  const double *__restrict__ D = T.Ds;
   const int n = T.n;
   double *G = T.Gacc;
+  float *G32 = T.Gacc32;
   const int fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb;
   auto Iat = [&](int a, int b, int c, int d) -> R { return I[((a * NB + b) * NC + c) * ND + d]; };
   // J12: bra block, warp-reduced
@@ -111,9 +136,9 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
 #pragma unroll
       for (int c = 0; c < NC; ++c)
 #pragma unroll
-        for (int d = 0; d < ND; ++d) s += R(__ldg(D + (fc + c) * n + fd + d)) * Iat(a, b, c, d);
+        for (int d = 0; d < ND; ++d) s += __ldg(D + (fc + c) * n + fd + d) * Iat(a, b, c, d);
       s = warp_sum(s * deg);
-      if (threadIdx.x == 0) atomicAdd(G + (fa + a) * n + fb + b, double(s));
+      if (threadIdx.x == 0) atomic_acc<R>(G, G32, (size_t)(fa + a) * n + fb + b, s);
     }
   if (!active) return;
   // J34
@@ -125,8 +150,8 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
 #pragma unroll
       for (int a = 0; a < NA; ++a)
 #pragma unroll
-        for (int b = 0; b < NB; ++b) s += R(__ldg(D + (fa + a) * n + fb + b)) * Iat(a, b, c, d);
-      atomicAdd(G + (fc + c) * n + fd + d, double(s * deg));
+        for (int b = 0; b < NB; ++b) s += __ldg(D + (fa + a) * n + fb + b) * Iat(a, b, c, d);
+      atomic_acc<R>(G, G32, (size_t)(fc + c) * n + fd + d, s * deg);
     }
   // K13 (i,k) += D(j,l)
 #pragma unroll
@@ -137,8 +162,8 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
 #pragma unroll
       for (int b = 0; b < NB; ++b)
 #pragma unroll
-        for (int d = 0; d < ND; ++d) s += R(__ldg(D + (fb + b) * n + fd + d)) * Iat(a, b, c, d);
-      atomicAdd(G + (fa + a) * n + fc + c, double(s * hdeg));
+        for (int d = 0; d < ND; ++d) s += __ldg(D + (fb + b) * n + fd + d) * Iat(a, b, c, d);
+      atomic_acc<R>(G, G32, (size_t)(fa + a) * n + fc + c, s * hdeg);
     }
   // K24 (j,l) += D(i,k)
 #pragma unroll
@@ -149,8 +174,8 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
 #pragma unroll
       for (int a = 0; a < NA; ++a)
 #pragma unroll
-        for (int c = 0; c < NC; ++c) s += R(__ldg(D + (fa + a) * n + fc + c)) * Iat(a, b, c, d);
-      atomicAdd(G + (fb + b) * n + fd + d, double(s * hdeg));
+        for (int c = 0; c < NC; ++c) s += __ldg(D + (fa + a) * n + fc + c) * Iat(a, b, c, d);
+      atomic_acc<R>(G, G32, (size_t)(fb + b) * n + fd + d, s * hdeg);
     }
   // K14 (i,l) += D(j,k)
 #pragma unroll
@@ -161,8 +186,8 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
 #pragma unroll
       for (int b = 0; b < NB; ++b)
 #pragma unroll
-        for (int c = 0; c < NC; ++c) s += R(__ldg(D + (fb + b) * n + fc + c)) * Iat(a, b, c, d);
-      atomicAdd(G + (fa + a) * n + fd + d, double(s * hdeg));
+        for (int c = 0; c < NC; ++c) s += __ldg(D + (fb + b) * n + fc + c) * Iat(a, b, c, d);
+      atomic_acc<R>(G, G32, (size_t)(fa + a) * n + fd + d, s * hdeg);
     }
   // K23 (j,k) += D(i,l)
 #pragma unroll
@@ -173,8 +198,8 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
 #pragma unroll
       for (int a = 0; a < NA; ++a)
 #pragma unroll
-        for (int d = 0; d < ND; ++d) s += R(__ldg(D + (fa + a) * n + fd + d)) * Iat(a, b, c, d);
-      atomicAdd(G + (fb + b) * n + fc + c, double(s * hdeg));
+        for (int d = 0; d < ND; ++d) s += __ldg(D + (fa + a) * n + fd + d) * Iat(a, b, c, d);
+      atomic_acc<R>(G, G32, (size_t)(fb + b) * n + fc + c, s * hdeg);
     }
 }
 
@@ -186,6 +211,7 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
 template <typename R, int LA, int LB, int LC, int LD>
 __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict__ tasks, TaskLaunch TL) {
   using Q = QClass<LA, LB, LC, LD>;
+  constexpr bool F64 = std::is_same<R, double>::value;
   constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND;
   const int t = find_task(tasks, TL.ntasks, blockIdx.x);
   const CPTask &T = tasks[t];
@@ -195,11 +221,19 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
   const int bpos = ty * kWarpsPerBlock + threadIdx.y;
   if (bpos >= T.nbra) return;
   const bool active = kpos < T.nket;
-  const PairRec &bra = T.pa[T.bra0 + bpos];
-  const PairRec ket = T.pb[T.ket0 + min(kpos, T.nket - 1)];
+  const PairT<R> *pa, *pb;
+  const PrimT<R> *pra, *prb;
+  const R *DA, *DB;
+  if constexpr (F64) {
+    pa = T.pa; pb = T.pb; pra = T.pra; prb = T.prb; DA = T.DsA; DB = T.DsB;
+  } else {
+    pa = T.pa32; pb = T.pb32; pra = T.pra32; prb = T.prb32; DA = T.DsA32; DB = T.DsB32;
+  }
+  const PairT<R> &bra = pa[T.bra0 + bpos];
+  const PairT<R> ket = pb[T.ket0 + min(kpos, T.nket - 1)];
   R I[Q::NINT];
   if (active) {
-    eri_quartet<R, LA, LB, LC, LD>(bra, T.pra, ket, T.prb, TL.boys.f64, TL.boys.f32, I);
+    eri_quartet<R, LA, LB, LC, LD>(bra, pra, ket, prb, TL.boys.f64, TL.boys.f32, I);
   } else {
 #pragma unroll
     for (int x = 0; x < Q::NINT; ++x) I[x] = R(0);
@@ -214,7 +248,6 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
   const R scale = R(T.scale);
   if (T.JA) {
     const R wk = active ? R(cddiff ? 2 : 1) * scale : R(0);
-    const double *__restrict__ D = T.DsB;
     const int nB = T.nB, nA = T.nA;
 #pragma unroll
     for (int a = 0; a < NA; ++a)
@@ -224,17 +257,16 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
 #pragma unroll
         for (int c = 0; c < NC; ++c)
 #pragma unroll
-          for (int d = 0; d < ND; ++d) s += R(__ldg(D + (fc + c) * nB + fd + d)) * Iat(a, b, c, d);
+          for (int d = 0; d < ND; ++d) s += __ldg(DB + (fc + c) * nB + fd + d) * Iat(a, b, c, d);
         s = warp_sum(s * wk);
         if (threadIdx.x == 0) {
-          atomicAdd(T.JA + (fa + a) * nA + fb + b, double(s));
-          if (abdiff) atomicAdd(T.JA + (fb + b) * nA + fa + a, double(s));
+          atomic_acc<R>(T.JA, T.JA32, (size_t)(fa + a) * nA + fb + b, s);
+          if (abdiff) atomic_acc<R>(T.JA, T.JA32, (size_t)(fb + b) * nA + fa + a, s);
         }
       }
   }
   if (T.JB && active) {
     const R wb = R(abdiff ? 2 : 1) * scale;
-    const double *__restrict__ D = T.DsA;
     const int nA = T.nA, nB = T.nB;
 #pragma unroll
     for (int c = 0; c < NC; ++c)
@@ -244,10 +276,10 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
 #pragma unroll
         for (int a = 0; a < NA; ++a)
 #pragma unroll
-          for (int b = 0; b < NB; ++b) s += R(__ldg(D + (fa + a) * nA + fb + b)) * Iat(a, b, c, d);
+          for (int b = 0; b < NB; ++b) s += __ldg(DA + (fa + a) * nA + fb + b) * Iat(a, b, c, d);
         s *= wb;
-        atomicAdd(T.JB + (fc + c) * nB + fd + d, double(s));
-        if (cddiff) atomicAdd(T.JB + (fd + d) * nB + fc + c, double(s));
+        atomic_acc<R>(T.JB, T.JB32, (size_t)(fc + c) * nB + fd + d, s);
+        if (cddiff) atomic_acc<R>(T.JB, T.JB32, (size_t)(fd + d) * nB + fc + c, s);
       }
   }
 }

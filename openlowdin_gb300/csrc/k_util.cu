@@ -14,47 +14,66 @@ int grid_for(size_t n, int block) {
   return (int)(g > 152 * 16 ? 152 * 16 : (g == 0 ? 1 : g));
 }
 
-// Ds = N D N and Dn[s1][s2] = max |D| over the shell block (unscaled D)
+// max of non-negative values through their bit patterns (IEEE order == integer
+// order for x >= 0), exact
+__device__ __forceinline__ void atomic_max_nonneg(double *p, double v) {
+  atomicMax(reinterpret_cast<unsigned long long *>(p), (unsigned long long)__double_as_longlong(v));
+}
+__device__ __forceinline__ void atomic_max_nonneg(float *p, float v) {
+  atomicMax(reinterpret_cast<unsigned int *>(p), (unsigned int)__float_as_int(v));
+}
+
+// Ds = N D N (FP64 and FP32 copies) and Dn[s1][s2] = max |D| over the shell
+// block (unscaled D)
 __global__ void prepare_density_kernel(const double *__restrict__ D, const double *__restrict__ norma,
                                        const int *__restrict__ shell_of, int n, int nsh, double *__restrict__ Ds,
-                                       double *__restrict__ Dn) {
+                                       float *__restrict__ Ds32, double *__restrict__ Dn, float *__restrict__ Dn32) {
   const size_t nn = (size_t)n * n;
   for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < nn; x += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(x / n), j = (int)(x % n);
     const double d = D[x];
-    Ds[x] = d * norma[i] * norma[j];
-    // |d| >= 0, so the IEEE bit pattern orders like the value: integer max is exact
-    atomicMax(reinterpret_cast<unsigned long long *>(Dn) + shell_of[i] * nsh + shell_of[j],
-              (unsigned long long)__double_as_longlong(fabs(d)));
+    const double s = d * norma[i] * norma[j];
+    Ds[x] = s;
+    if (Ds32) Ds32[x] = (float)s;
+    const int b = shell_of[i] * nsh + shell_of[j];
+    atomic_max_nonneg(Dn + b, fabs(d));
+    if (Dn32) atomic_max_nonneg(Dn32 + b, (float)fabs(d));
   }
 }
 
 __global__ void scale_density_kernel(const double *__restrict__ D, const double *__restrict__ norma, int n,
-                                     double *__restrict__ Ds) {
+                                     double *__restrict__ Ds, float *__restrict__ Ds32) {
   const size_t nn = (size_t)n * n;
   for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < nn; x += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(x / n), j = (int)(x % n);
-    Ds[x] = D[x] * norma[i] * norma[j];
+    const double s = D[x] * norma[i] * norma[j];
+    Ds[x] = s;
+    if (Ds32) Ds32[x] = (float)s;
   }
 }
 
-// G = scale * N_i N_j (Gacc + Gacc^T)
-__global__ void symmetrize_kernel(const double *__restrict__ Gacc, const double *__restrict__ norma, int n,
-                                  double scale, double *__restrict__ G) {
+// G = scale * N_i N_j (Gacc + Gacc^T) (+ the FP32 accumulator when present)
+__global__ void symmetrize_kernel(const double *__restrict__ Gacc, const float *__restrict__ Gacc32,
+                                  const double *__restrict__ norma, int n, double scale, double *__restrict__ G) {
   const size_t nn = (size_t)n * n;
   for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < nn; x += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(x / n), j = (int)(x % n);
-    G[x] = scale * norma[i] * norma[j] * (Gacc[x] + Gacc[(size_t)j * n + i]);
+    const size_t y = (size_t)j * n + i;
+    double g = Gacc[x] + Gacc[y];
+    if (Gacc32) g += (double)Gacc32[x] + (double)Gacc32[y];
+    G[x] = scale * norma[i] * norma[j] * g;
   }
 }
 
 // out = scale * N_i N_j J (row >= col only when lower_only, zero above)
-__global__ void coupling_extract_kernel(const double *__restrict__ J, const double *__restrict__ norma, int n,
-                                        double scale, int lower_only, double *__restrict__ out) {
+__global__ void coupling_extract_kernel(const double *__restrict__ J, const float *__restrict__ J32,
+                                        const double *__restrict__ norma, int n, double scale, int lower_only,
+                                        double *__restrict__ out) {
   const size_t nn = (size_t)n * n;
   for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < nn; x += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(x / n), j = (int)(x % n);
-    out[x] = (lower_only && j > i) ? 0.0 : scale * norma[i] * norma[j] * J[x];
+    const double v = J[x] + (J32 ? (double)J32[x] : 0.0);
+    out[x] = (lower_only && j > i) ? 0.0 : scale * norma[i] * norma[j] * v;
   }
 }
 
@@ -97,8 +116,8 @@ __device__ __forceinline__ int find_slot(const SpeciesSlot *__restrict__ slots, 
   return lo;
 }
 
-// every species of a batch: Ds = N P N, Dn = shell-block max |P| (when used),
-// and zeroed accumulators
+// every species of a batch: Ds = N P N (FP64 and FP32), Dn = shell-block max
+// |P| (when used) and zeroed accumulators
 __global__ void prepare_batch_kernel(const SpeciesSlot *__restrict__ slots, int nslots, long long total) {
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
        x += (long long)gridDim.x * blockDim.x) {
@@ -106,16 +125,25 @@ __global__ void prepare_batch_kernel(const SpeciesSlot *__restrict__ slots, int 
     const long long e = x - S.off;
     const int i = (int)(e / S.n), j = (int)(e % S.n);
     const double p = S.P[e];
-    S.Ds[e] = p * S.norma[i] * S.norma[j];
-    if (S.Gacc) S.Gacc[e] = 0.0;
+    const double s = p * S.norma[i] * S.norma[j];
+    S.Ds[e] = s;
+    S.Ds32[e] = (float)s;
+    if (S.Gacc) {
+      S.Gacc[e] = 0.0;
+      S.Gacc32[e] = 0.0f;
+    }
     S.Jacc[e] = 0.0;
-    if (S.Dn)
-      atomicMax(reinterpret_cast<unsigned long long *>(S.Dn) + S.shell_of[i] * S.nsh + S.shell_of[j],
-                (unsigned long long)__double_as_longlong(fabs(p)));
+    S.Jacc32[e] = 0.0f;
+    if (S.Dn) {
+      const int b = S.shell_of[i] * S.nsh + S.shell_of[j];
+      atomic_max_nonneg(S.Dn + b, fabs(p));
+      atomic_max_nonneg(S.Dn32 + b, (float)fabs(p));
+    }
   }
 }
 
-// G = gscale N (Gacc + Gacc^T) N (0 when the species builds none), J = N Jacc N
+// G = gscale N (Gacc + Gacc^T) N (0 when the species builds none), J = N Jacc N,
+// FP32 accumulators added in
 __global__ void finalize_batch_kernel(const SpeciesSlot *__restrict__ slots, int nslots, long long total) {
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
        x += (long long)gridDim.x * blockDim.x) {
@@ -123,12 +151,23 @@ __global__ void finalize_batch_kernel(const SpeciesSlot *__restrict__ slots, int
     const long long e = x - S.off;
     const int i = (int)(e / S.n), j = (int)(e % S.n);
     const double nn = S.norma[i] * S.norma[j];
-    if (S.G) S.G[e] = S.Gacc ? S.gscale * nn * (S.Gacc[e] + S.Gacc[(long long)j * S.n + i]) : 0.0;
-    S.J[e] = nn * S.Jacc[e];
+    if (S.G) {
+      if (S.Gacc) {
+        const long long y = (long long)j * S.n + i;
+        const double g = S.Gacc[e] + S.Gacc[y] + (double)S.Gacc32[e] + (double)S.Gacc32[y];
+        S.G[e] = S.gscale * nn * g;
+      } else {
+        S.G[e] = 0.0;
+      }
+    }
+    S.J[e] = nn * (S.Jacc[e] + (double)S.Jacc32[e]);
   }
 }
 
 }  // namespace
+
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 cudaError_t launch_prepare_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s) {
   if (total <= 0) return cudaSuccess;
@@ -143,9 +182,6 @@ cudaError_t launch_finalize_batch(const SpeciesSlot *slots, int nslots, long lon
   count_launches(1);
   return cudaGetLastError();
 }
-
-void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
-long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 cudaError_t measure_fma_tflops(bool fp64, double *tflops) {
   int dev = 0, sms = 0;
@@ -182,30 +218,36 @@ cudaError_t measure_fma_tflops(bool fp64, double *tflops) {
 }
 
 cudaError_t launch_prepare_density(const double *D, const double *norma, const int *shell_of, int n, int nsh,
-                                   double *Ds, double *Dn, cudaStream_t s) {
+                                   double *Ds, float *Ds32, double *Dn, float *Dn32, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(Dn, 0, sizeof(double) * nsh * nsh, s);
   if (e != cudaSuccess) return e;
-  prepare_density_kernel<<<grid_for((size_t)n * n, 256), 256, 0, s>>>(D, norma, shell_of, n, nsh, Ds, Dn);
+  if (Dn32) {
+    e = cudaMemsetAsync(Dn32, 0, sizeof(float) * nsh * nsh, s);
+    if (e != cudaSuccess) return e;
+  }
+  prepare_density_kernel<<<grid_for((size_t)n * n, 256), 256, 0, s>>>(D, norma, shell_of, n, nsh, Ds, Ds32, Dn,
+                                                                      Dn32);
   count_launches(1);
   return cudaGetLastError();
 }
 
-cudaError_t launch_scale_density(const double *D, const double *norma, int n, double *Ds, cudaStream_t s) {
-  scale_density_kernel<<<grid_for((size_t)n * n, 256), 256, 0, s>>>(D, norma, n, Ds);
+cudaError_t launch_scale_density(const double *D, const double *norma, int n, double *Ds, float *Ds32,
+                                 cudaStream_t s) {
+  scale_density_kernel<<<grid_for((size_t)n * n, 256), 256, 0, s>>>(D, norma, n, Ds, Ds32);
   count_launches(1);
   return cudaGetLastError();
 }
 
-cudaError_t launch_symmetrize(const double *Gacc, const double *norma, int n, double scale, double *G,
-                              cudaStream_t s) {
-  symmetrize_kernel<<<grid_for((size_t)n * n, 256), 256, 0, s>>>(Gacc, norma, n, scale, G);
+cudaError_t launch_symmetrize(const double *Gacc, const float *Gacc32, const double *norma, int n, double scale,
+                              double *G, cudaStream_t s) {
+  symmetrize_kernel<<<grid_for((size_t)n * n, 256), 256, 0, s>>>(Gacc, Gacc32, norma, n, scale, G);
   count_launches(1);
   return cudaGetLastError();
 }
 
-cudaError_t launch_coupling_extract(const double *J, const double *norma, int n, double scale, int lower_only,
-                                    double *out, cudaStream_t s) {
-  coupling_extract_kernel<<<grid_for((size_t)n * n, 256), 256, 0, s>>>(J, norma, n, scale, lower_only, out);
+cudaError_t launch_coupling_extract(const double *J, const float *J32, const double *norma, int n, double scale,
+                                    int lower_only, double *out, cudaStream_t s) {
+  coupling_extract_kernel<<<grid_for((size_t)n * n, 256), 256, 0, s>>>(J, J32, norma, n, scale, lower_only, out);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -26,12 +26,19 @@ struct BoysTables {
 
 // One J/K task: quartets (bra in [bra0, bra0+nbra), ket in [ket0, ket0+nket))
 // of one species' significant pairs.
+// Every array exists in FP64 (used by the FP64 kernels) and FP32 (used by the
+// FP32 kernels of the mixed-precision path).
 struct JKTask {
   const PairRec *pairs;
   const PrimRec *prims;
+  const PairRec32 *pairs32;
+  const PrimRec32 *prims32;
   const double *Ds;       // norma-scaled density N D N, n x n row-major
+  const float *Ds32;
   const double *Dn;       // max |D| of each shell block, nsh x nsh
+  const float *Dn32;
   double *Gacc;           // n x n accumulator (symmetrised by the finaliser)
+  float *Gacc32;          // FP32 kernels accumulate here (added by the finaliser)
   unsigned long long *count;  // quartets evaluated (may be null)
   double hf;              // 0.5 * exchange factor
   int bra0, nbra, ket0, nket;
@@ -49,10 +56,18 @@ struct CPTask {
   const PrimRec *pra;
   const PairRec *pb;
   const PrimRec *prb;
+  const PairRec32 *pa32;
+  const PrimRec32 *pra32;
+  const PairRec32 *pb32;
+  const PrimRec32 *prb32;
   const double *DsA;      // norma-scaled density of A (feeds JB), null if JB is null
   const double *DsB;      // norma-scaled density of B (feeds JA), null if JA is null
+  const float *DsA32;
+  const float *DsB32;
   double *JA;             // nA x nA full symmetric accumulator (or null)
   double *JB;             // nB x nB (or null)
+  float *JA32;            // FP32 accumulators of the FP32 kernels
+  float *JB32;
   double scale;           // q_A q_B (1 for the reference-shaped calls)
   int bra0, nbra, ket0, nket;
   int nA, nB;
@@ -111,23 +126,27 @@ cudaError_t launch_it(int pcb, int pck, const ITParams &p, cudaStream_t s);
 cudaError_t launch_schwarz(int pc, const SchwarzParams &p, cudaStream_t s);
 bool class_supported(int pcb, int pck);
 
-// small kernels
+// small kernels (the *32 arguments may be null)
 cudaError_t launch_prepare_density(const double *D, const double *norma, const int *shell_of, int n, int nsh,
-                                   double *Ds, double *Dn, cudaStream_t s);
-cudaError_t launch_scale_density(const double *D, const double *norma, int n, double *Ds, cudaStream_t s);
-cudaError_t launch_symmetrize(const double *Gacc, const double *norma, int n, double scale, double *G,
-                              cudaStream_t s);
-cudaError_t launch_coupling_extract(const double *J, const double *norma, int n, double scale, int lower_only,
-                                    double *out, cudaStream_t s);
+                                   double *Ds, float *Ds32, double *Dn, float *Dn32, cudaStream_t s);
+cudaError_t launch_scale_density(const double *D, const double *norma, int n, double *Ds, float *Ds32,
+                                 cudaStream_t s);
+cudaError_t launch_symmetrize(const double *Gacc, const float *Gacc32, const double *norma, int n, double scale,
+                              double *G, cudaStream_t s);
+cudaError_t launch_coupling_extract(const double *J, const float *J32, const double *norma, int n, double scale,
+                                    int lower_only, double *out, cudaStream_t s);
 
 // batched element-wise work over many species of a batch
 struct SpeciesSlot {
   const double *P;        // density (input)
   double *Ds;             // N P N
+  float *Ds32;
   double *Dn;             // shell-block max |P| (null: not needed)
+  float *Dn32;
   const double *norma;
   const int *shell_of;
   double *Gacc, *Jacc;    // accumulators
+  float *Gacc32, *Jacc32;
   double *G, *J;          // outputs (G may be null)
   double gscale;          // 0.25 q^2 for the two-particle matrix
   int n, nsh;

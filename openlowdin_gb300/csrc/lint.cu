@@ -275,13 +275,47 @@ struct PairList {
   int start[kNumPairClasses + 1] = {0};
   PairRec *d = nullptr;
   PrimRec *dp = nullptr;
+  PairRec32 *d32 = nullptr;   // FP32 copies for the FP32 kernels
+  PrimRec32 *dp32 = nullptr;
   void release() {
     if (d) cudaFree(d);
     if (dp) cudaFree(dp);
+    if (d32) cudaFree(d32);
+    if (dp32) cudaFree(dp32);
     d = nullptr;
     dp = nullptr;
+    d32 = nullptr;
+    dp32 = nullptr;
   }
   int count(int pc) const { return start[pc + 1] - start[pc]; }
+  // uploads the FP64 records and their FP32 copies
+  bool upload() {
+    release();
+    std::vector<PairRec32> h32(h.size());
+    std::vector<PrimRec32> hp32(hp.size());
+    for (size_t i = 0; i < h.size(); ++i) {
+      const PairRec &a = h[i];
+      PairRec32 &b = h32[i];
+      b.sa = a.sa; b.sb = a.sb; b.fa = a.fa; b.fb = a.fb; b.prim0 = a.prim0; b.nprim = a.nprim;
+      b.la = a.la; b.lb = a.lb;
+      for (int k = 0; k < 3; ++k) {
+        b.A[k] = (float)a.A[k];
+        b.AB[k] = (float)a.AB[k];
+      }
+      b.Q = (float)a.Q;
+      b.pad = 0.f;
+    }
+    for (size_t i = 0; i < hp.size(); ++i) {
+      const PrimRec &a = hp[i];
+      PrimRec32 &b = hp32[i];
+      b.p = (float)a.p; b.inv_p = (float)a.inv_p; b.Kt = (float)a.Kt; b.pad = 0.f;
+      for (int k = 0; k < 3; ++k) {
+        b.P[k] = (float)a.P[k];
+        b.PA[k] = (float)a.PA[k];
+      }
+    }
+    return dev_upload(d, h) && dev_upload(dp, hp) && dev_upload(d32, h32) && dev_upload(dp32, hp32);
+  }
 };
 
 template <typename T>
@@ -305,6 +339,17 @@ struct DevBuf {
 };
 
 constexpr int kNQC = kNumPairClasses * kNumPairClasses;
+
+// device buffers of one species in one build: scaled density (FP64 + FP32),
+// shell-block norms (FP64 + FP32) and the output accumulators (FP64 + FP32)
+struct SpeciesBufs {
+  const double *Ds;
+  const float *Ds32;
+  const double *Dn;
+  const float *Dn32;
+  double *G;
+  float *G32;
+};
 
 // Tasks grouped by quartet class (bra pair class * 6 + ket pair class); one
 // device array holds every group, each group is one launch.
@@ -376,6 +421,7 @@ struct LibintInterface {
   double *d_norma = nullptr;
   int *d_shell_of = nullptr;
   DevBuf<double> dD, dDs, dDn, dGacc, dG, dA, dC, dDsC, dJacc;
+  DevBuf<float> dDs32, dDn32, dGacc32, dDsC32, dJacc32;
   DevBuf<unsigned long long> dcount;
   long long last_quartets = -1;
   long long class_quartets[kNQC] = {0};
@@ -395,6 +441,7 @@ struct LibintInterface {
     d_shell_of = nullptr;
     dD.release(); dDs.release(); dDn.release(); dGacc.release(); dG.release(); dA.release(); dC.release();
     dDsC.release(); dJacc.release();
+    dDs32.release(); dDn32.release(); dGacc32.release(); dDsC32.release(); dJacc32.release();
     dcount.release();
     jk.release();
     cp.release();
@@ -460,10 +507,12 @@ struct LibintInterface {
         const double x = A.alpha[i], y = B.alpha[j], p = x + y;
         PrimRec q{};
         q.p = p;
-        q.Px = (x * A.O[0] + y * B.O[0]) / p;
-        q.Py = (x * A.O[1] + y * B.O[1]) / p;
-        q.Pz = (x * A.O[2] + y * B.O[2]) / p;
-        q.K = std::exp(-x * y / p * AB2) * A.cn[i] * B.cn[j];
+        q.inv_p = 1.0 / p;
+        for (int d = 0; d < 3; ++d) {
+          q.P[d] = (x * A.O[d] + y * B.O[d]) / p;
+          q.PA[d] = q.P[d] - A.O[d];
+        }
+        q.Kt = kSqrt2Pi52 * std::exp(-x * y / p * AB2) * A.cn[i] * B.cn[j] / p;
         prims.push_back(q);
       }
     return r;
@@ -527,15 +576,13 @@ struct LibintInterface {
         if (sigf) raw.push_back(make_pair(s1, s2, rawp));
       }
     bin_pairs(sig, raw, rawp, false);
-    sig.release();
-    if (!dev_upload(sig.d, sig.h) || !dev_upload(sig.dp, sig.hp)) return false;
+    if (!sig.upload()) return false;
     if (!compute_schwarz(sig)) return false;
     // sort by decreasing Schwarz factor inside each class
     std::vector<PairRec> tmp = sig.h;
     std::vector<PrimRec> tmpp = sig.hp;
     bin_pairs(sig, tmp, tmpp, true);
-    sig.release();
-    if (!dev_upload(sig.d, sig.h) || !dev_upload(sig.dp, sig.hp)) return false;
+    if (!sig.upload()) return false;
     have_sig = true;
     return true;
   }
@@ -548,8 +595,7 @@ struct LibintInterface {
     for (int s1 = 0; s1 < nshell(); ++s1)
       for (int s2 = 0; s2 <= s1; ++s2) raw.push_back(make_pair(s1, s2, rawp));
     bin_pairs(all, raw, rawp, false);
-    all.release();
-    if (!dev_upload(all.d, all.h) || !dev_upload(all.dp, all.hp)) return false;
+    if (!all.upload()) return false;
     have_all = true;
     return true;
   }
@@ -559,20 +605,23 @@ struct LibintInterface {
     if (!ensure_sig()) return false;
     const int n = nbasis, nsh = nshell();
     if (!dDs.ensure((size_t)n * n) || !dDn.ensure((size_t)nsh * nsh) || !dGacc.ensure((size_t)n * n) ||
+        !dDs32.ensure((size_t)n * n) || !dDn32.ensure((size_t)nsh * nsh) || !dGacc32.ensure((size_t)n * n) ||
         !dcount.ensure(kNQC))
       return false;
     if (!jk_ready || jk_hf != 0.5 * factor) {
       jk.clear();
-      if (!add_jk_tasks(jk, dDs.p, dDn.p, dGacc.p, 0.5 * factor, dcount.p)) return false;
+      SpeciesBufs b{dDs.p, dDs32.p, dDn.p, dDn32.p, dGacc.p, dGacc32.p};
+      if (!add_jk_tasks(jk, b, 0.5 * factor, dcount.p)) return false;
       if (!jk.upload(s)) return false;
       jk_hf = 0.5 * factor;
       jk_ready = true;
     }
-    CK(launch_prepare_density(dDin, d_norma, d_shell_of, n, nsh, dDs.p, dDn.p, s));
+    CK(launch_prepare_density(dDin, d_norma, d_shell_of, n, nsh, dDs.p, dDs32.p, dDn.p, dDn32.p, s));
     CK(cudaMemsetAsync(dGacc.p, 0, sizeof(double) * n * n, s));
+    CK(cudaMemsetAsync(dGacc32.p, 0, sizeof(float) * n * n, s));
     CK(cudaMemsetAsync(dcount.p, 0, sizeof(unsigned long long) * kNQC, s));
     if (!launch_jk_groups(jk, precision, split, boys, s)) return false;
-    CK(launch_symmetrize(dGacc.p, d_norma, n, 0.25, dGout, s));
+    CK(launch_symmetrize(dGacc.p, dGacc32.p, d_norma, n, 0.25, dGout, s));
     unsigned long long cnt[kNQC];
     CK(cudaMemcpyAsync(cnt, dcount.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -585,8 +634,7 @@ struct LibintInterface {
   }
 
   // J/K tasks of this species into ts: one task per (bra class >= ket class)
-  bool add_jk_tasks(TaskSet<JKTask> &ts, const double *Ds, const double *Dn, double *Gacc, double hf,
-                    unsigned long long *counters) {
+  bool add_jk_tasks(TaskSet<JKTask> &ts, const SpeciesBufs &bf, double hf, unsigned long long *counters) {
     if (!ensure_sig()) return false;
     for (int cb = 0; cb < kNumPairClasses; ++cb)
       for (int ck = 0; ck <= cb; ++ck) {
@@ -599,9 +647,14 @@ struct LibintInterface {
         JKTask t{};
         t.pairs = sig.d;
         t.prims = sig.dp;
-        t.Ds = Ds;
-        t.Dn = Dn;
-        t.Gacc = Gacc;
+        t.pairs32 = sig.d32;
+        t.prims32 = sig.dp32;
+        t.Ds = bf.Ds;
+        t.Ds32 = bf.Ds32;
+        t.Dn = bf.Dn;
+        t.Dn32 = bf.Dn32;
+        t.Gacc = bf.G;
+        t.Gacc32 = bf.G32;
         t.count = counters ? counters + cb * kNumPairClasses + ck : nullptr;
         t.hf = hf;
         t.bra0 = sig.start[cb];
@@ -644,8 +697,10 @@ struct LibintInterface {
 };
 
 // coupling tasks of species pair (A bra, B ket) into ts
-bool add_cp_tasks(TaskSet<CPTask> &ts, LibintInterface *A, LibintInterface *B, const double *DsA,
-                  const double *DsB, double *JA, double *JB, double scale) {
+bool add_cp_tasks(TaskSet<CPTask> &ts, LibintInterface *A, LibintInterface *B, const SpeciesBufs &ba,
+                  const SpeciesBufs &bb, bool want_a, bool want_b, double scale) {
+  // JA (from D_B) accumulates into ba.G / ba.G32, JB (from D_A) into bb.G / bb.G32
+  double *JA = want_a ? ba.G : nullptr, *JB = want_b ? bb.G : nullptr;
   if (!A->ensure_all() || !B->ensure_all()) return false;
   for (int cb = 0; cb < kNumPairClasses; ++cb)
     for (int ck = 0; ck < kNumPairClasses; ++ck) {
@@ -660,10 +715,18 @@ bool add_cp_tasks(TaskSet<CPTask> &ts, LibintInterface *A, LibintInterface *B, c
       t.pra = A->all.dp;
       t.pb = B->all.d;
       t.prb = B->all.dp;
-      t.DsA = JB ? DsA : nullptr;
-      t.DsB = JA ? DsB : nullptr;
+      t.pa32 = A->all.d32;
+      t.pra32 = A->all.dp32;
+      t.pb32 = B->all.d32;
+      t.prb32 = B->all.dp32;
+      t.DsA = JB ? ba.Ds : nullptr;
+      t.DsA32 = JB ? ba.Ds32 : nullptr;
+      t.DsB = JA ? bb.Ds : nullptr;
+      t.DsB32 = JA ? bb.Ds32 : nullptr;
       t.JA = JA;
+      t.JA32 = JA ? ba.G32 : nullptr;
       t.JB = JB;
+      t.JB32 = JB ? bb.G32 : nullptr;
       t.scale = scale;
       t.bra0 = A->all.start[cb];
       t.nbra = A->all.count(cb);
@@ -696,25 +759,30 @@ bool coupling(LibintInterface *A, LibintInterface *B, const double *dDa, const d
               double *dJb, bool fp32, cudaStream_t s) {
   if (!A->ensure_all() || !B->ensure_all()) return false;
   const int nA = A->nbasis, nB = B->nbasis;
-  // scaled densities in each handle's dDsC, accumulators in dJacc
-  if (dJa && (!B->dDsC.ensure((size_t)nB * nB) || !A->dJacc.ensure((size_t)nA * nA))) return false;
-  if (dJb && (!A->dDsC.ensure((size_t)nA * nA) || !B->dJacc.ensure((size_t)nB * nB))) return false;
+  // scaled densities in each handle's dDsC(32), accumulators in dJacc(32)
+  auto bufs = [](LibintInterface *X, int n) {
+    return X->dDsC.ensure((size_t)n * n) && X->dDsC32.ensure((size_t)n * n) && X->dJacc.ensure((size_t)n * n) &&
+           X->dJacc32.ensure((size_t)n * n);
+  };
+  if (!bufs(A, nA) || !bufs(B, nB)) return false;
   if (dJa) {
-    CK(launch_scale_density(dDb, B->d_norma, nB, B->dDsC.p, s));
+    CK(launch_scale_density(dDb, B->d_norma, nB, B->dDsC.p, B->dDsC32.p, s));
     CK(cudaMemsetAsync(A->dJacc.p, 0, sizeof(double) * nA * nA, s));
+    CK(cudaMemsetAsync(A->dJacc32.p, 0, sizeof(float) * nA * nA, s));
   }
   if (dJb) {
-    CK(launch_scale_density(dDa, A->d_norma, nA, A->dDsC.p, s));
+    CK(launch_scale_density(dDa, A->d_norma, nA, A->dDsC.p, A->dDsC32.p, s));
     CK(cudaMemsetAsync(B->dJacc.p, 0, sizeof(double) * nB * nB, s));
+    CK(cudaMemsetAsync(B->dJacc32.p, 0, sizeof(float) * nB * nB, s));
   }
   A->cp.clear();
-  if (!add_cp_tasks(A->cp, A, B, dJb ? A->dDsC.p : nullptr, dJa ? B->dDsC.p : nullptr, dJa ? A->dJacc.p : nullptr,
-                    dJb ? B->dJacc.p : nullptr, 1.0))
-    return false;
+  SpeciesBufs ba{A->dDsC.p, A->dDsC32.p, nullptr, nullptr, A->dJacc.p, A->dJacc32.p};
+  SpeciesBufs bb{B->dDsC.p, B->dDsC32.p, nullptr, nullptr, B->dJacc.p, B->dJacc32.p};
+  if (!add_cp_tasks(A->cp, A, B, ba, bb, dJa != nullptr, dJb != nullptr, 1.0)) return false;
   if (!A->cp.upload(s)) return false;
   if (!launch_cp_groups(A->cp, fp32, A->boys, s)) return false;
-  if (dJa) CK(launch_coupling_extract(A->dJacc.p, A->d_norma, nA, 1.0, 0, dJa, s));
-  if (dJb) CK(launch_coupling_extract(B->dJacc.p, B->d_norma, nB, 1.0, 0, dJb, s));
+  if (dJa) CK(launch_coupling_extract(A->dJacc.p, A->dJacc32.p, A->d_norma, nA, 1.0, 0, dJa, s));
+  if (dJb) CK(launch_coupling_extract(B->dJacc.p, B->dJacc32.p, B->d_norma, nB, 1.0, 0, dJb, s));
   return true;
 }
 
@@ -750,7 +818,8 @@ bool first_quarter(LibintInterface *A, LibintInterface *B, const double *hD, con
     if (!A->dD.ensure((size_t)nA * nA) || !A->dDs.ensure((size_t)nA * nA) || !A->dDn.ensure((size_t)nsh * nsh))
       return false;
     CK(cudaMemcpyAsync(A->dD.p, hD, sizeof(double) * nA * nA, cudaMemcpyHostToDevice, s));
-    CK(launch_prepare_density(A->dD.p, A->d_norma, A->d_shell_of, nA, nsh, A->dDs.p, A->dDn.p, s));
+    CK(launch_prepare_density(A->dD.p, A->d_norma, A->d_shell_of, nA, nsh, A->dDs.p, nullptr, A->dDn.p, nullptr,
+                              s));
     q.Dn = A->dDn.p;
     q.screen = A->is_electron ? 1 : 0;
     q.pa = q.pb = A->sig.d;
@@ -1064,6 +1133,7 @@ struct LowdinGB300_Batch {
   std::vector<int> sys_first;
   bool finalized = false;
   DevBuf<double> Ds, Dn, Gacc, Jacc;
+  DevBuf<float> Ds32, Dn32, Gacc32, Jacc32;
   DevBuf<unsigned long long> cnt;
   DevBuf<SpeciesSlot> slots;
   long long total = 0;
@@ -1075,6 +1145,7 @@ struct LowdinGB300_Batch {
 
   ~LowdinGB300_Batch() {
     Ds.release(); Dn.release(); Gacc.release(); Jacc.release(); cnt.release(); slots.release();
+    Ds32.release(); Dn32.release(); Gacc32.release(); Jacc32.release();
     jk.release(); cp.release();
   }
 
@@ -1101,10 +1172,12 @@ struct LowdinGB300_Batch {
       }
     }
     total = tot;
-    if (!Ds.ensure(tot) || !Gacc.ensure(tot) || !Jacc.ensure(tot) || !Dn.ensure(dtot > 0 ? dtot : 1) ||
-        !cnt.ensure(kNQC))
+    const long long dsz = dtot > 0 ? dtot : 1;
+    if (!Ds.ensure(tot) || !Gacc.ensure(tot) || !Jacc.ensure(tot) || !Dn.ensure(dsz) || !Ds32.ensure(tot) ||
+        !Gacc32.ensure(tot) || !Jacc32.ensure(tot) || !Dn32.ensure(dsz) || !cnt.ensure(kNQC))
       return false;
     std::vector<SpeciesSlot> hs(sp.size());
+    std::vector<SpeciesBufs> bf(sp.size());
     jk.clear();
     cp.clear();
     for (size_t k = 0; k < sp.size(); ++k) {
@@ -1112,11 +1185,15 @@ struct LowdinGB300_Batch {
       SpeciesSlot &S = hs[k];
       S.P = x.P;
       S.Ds = Ds.p + off[k];
+      S.Ds32 = Ds32.p + off[k];
       S.Dn = dnoff[k] >= 0 ? Dn.p + dnoff[k] : nullptr;
+      S.Dn32 = dnoff[k] >= 0 ? Dn32.p + dnoff[k] : nullptr;
       S.norma = x.h->d_norma;
       S.shell_of = x.h->d_shell_of;
       S.Gacc = x.two_body ? Gacc.p + off[k] : nullptr;
+      S.Gacc32 = x.two_body ? Gacc32.p + off[k] : nullptr;
       S.Jacc = Jacc.p + off[k];
+      S.Jacc32 = Jacc32.p + off[k];
       S.G = x.G;
       S.J = x.J;
       S.gscale = 0.25 * x.q * x.q;
@@ -1124,18 +1201,17 @@ struct LowdinGB300_Batch {
       S.nsh = x.h->nshell();
       S.off = off[k];
       if (x.two_body) {
-        if (!x.h->add_jk_tasks(jk, S.Ds, S.Dn ? S.Dn : Dn.p, S.Gacc, 0.5 * x.factor, cnt.p)) return false;
-        if (!S.Dn) {
-          // non-electron species are not screened: the Dn pointer is never read
-        }
+        // non-electron species are not screened: their norm pointers are never read
+        SpeciesBufs b{S.Ds, S.Ds32, S.Dn ? S.Dn : Dn.p, S.Dn32 ? S.Dn32 : Dn32.p, S.Gacc, S.Gacc32};
+        if (!x.h->add_jk_tasks(jk, b, 0.5 * x.factor, cnt.p)) return false;
       }
+      bf[k] = SpeciesBufs{S.Ds, S.Ds32, nullptr, nullptr, S.Jacc, S.Jacc32};
     }
     // coupling tasks: every species pair of a system
     for (size_t a = 0; a < sp.size(); ++a)
       for (size_t b = a + 1; b < sp.size(); ++b) {
         if (sp[a].sys != sp[b].sys) continue;
-        if (!add_cp_tasks(cp, sp[a].h, sp[b].h, hs[a].Ds, hs[b].Ds, hs[a].Jacc, hs[b].Jacc, sp[a].q * sp[b].q))
-          return false;
+        if (!add_cp_tasks(cp, sp[a].h, sp[b].h, bf[a], bf[b], true, true, sp[a].q * sp[b].q)) return false;
       }
     nslots = (int)hs.size();
     if (!slots.ensure(hs.size())) return false;
@@ -1152,6 +1228,7 @@ struct LowdinGB300_Batch {
       return false;
     }
     CK(cudaMemsetAsync(Dn.p, 0, Dn.n * sizeof(double), s));
+    CK(cudaMemsetAsync(Dn32.p, 0, Dn32.n * sizeof(float), s));
     CK(cudaMemsetAsync(cnt.p, 0, kNQC * sizeof(unsigned long long), s));
     CK(launch_prepare_batch(slots.p, nslots, total, s));
     const int jk_mixed = precision & 1;
