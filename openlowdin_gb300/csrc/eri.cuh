@@ -44,7 +44,7 @@ __device__ __forceinline__ void vrr_prim(R (&X)[QClass<LA, LB, LC, LD>::nE * QCl
   const R opq = R(1) / (p + q);
   const R rp = q * opq;          // rho / p
   const R rq = p * opq;          // rho / q
-  const R rho = p * rq;
+  const R rho = p * rp;          // p q / (p + q)
   R PQ2 = 0, PA[3], WP[3], QCv[3], WQ[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
