@@ -181,8 +181,9 @@ int LowdinGB300_batch_add_system(LowdinGB300_Batch *b, LibintInterface **species
                                  const double **dP, double **dG, double **dJ);
 /* builds pair data, task lists and work arenas (synchronises `stream`) */
 int LowdinGB300_batch_finalize(LowdinGB300_Batch *b, void *stream);
-/* precision bits: 1 = two-particle quartets whose Schwarz-density bound is
-   below `split` run in FP32 (the rest FP64); 2 = coupling quartets in FP32.
+/* precision bits: 1 = two-particle quartets whose Schwarz-density bound
+   Q_ab Q_cd max|D block| is below `split` run in FP32 (the rest FP64); 2 = the
+   same split for coupling quartets (bound Q_ab Q_cd max(|D_A|, |D_B|)).
    0 = FP64 throughout. */
 int LowdinGB300_batch_fock(LowdinGB300_Batch *b, int precision, double split, void *stream);
 /* quartets evaluated per (bra pair class, ket pair class) by the last J/K

@@ -50,6 +50,7 @@ class BatchSCF:
         import torch
         self.torch = torch
         self.rebuild_every = rebuild_every
+        self.trace = None
         self.dev = torch.device(device)
         self.systems = systems
         self.precision = precision
@@ -202,6 +203,19 @@ class BatchSCF:
         frozen = torch.zeros(self.nsys, dtype=torch.bool, device=self.dev)
         quartets = 0
         it = 0
+        # optional phase timing (self.trace = {} before solve): synchronises
+        # the device at each phase boundary, so only for diagnostics
+        trace = self.trace
+        last = [time.perf_counter()]
+
+        def tick(name):
+            if trace is None:
+                return
+            torch.cuda.synchronize(self.dev)
+            now = time.perf_counter()
+            trace[name] = trace.get(name, 0.0) + (now - last[0])
+            last[0] = now
+
         for it in range(1, max_iter + 1):
             # plain: full build from P every iteration (the reference's scheme).
             # mixed: incremental build from dP = P - P_ref on top of the previous
@@ -215,8 +229,9 @@ class BatchSCF:
                     g.Pin.copy_(g.P)
                 else:
                     torch.sub(g.P, g.Pref, out=g.Pin)
-            # precision bits: 1 = two-particle split FP32/FP64, 2 = FP32 coupling
-            self.batch.fock(0 if not mixed else (1 if full else 3), self.split, stream)
+            # precision bits: 1 = two-particle FP32/FP64 split, 2 = coupling split
+            self.batch.fock(3 if mixed else 0, self.split, stream)
+            tick("fock")
             for g in groups:
                 if full:
                     g.G.copy_(g.Gb)
@@ -235,6 +250,7 @@ class BatchSCF:
                 err = g.X.transpose(1, 2) @ (FPS - FPS.transpose(1, 2)) @ g.X
                 Fs.append(F)
                 Es.append(err)
+            tick("assemble")
             # Pulay DIIS per system over all of its species
             hist_F.append(Fs)
             hist_E.append(Es)
@@ -264,6 +280,7 @@ class BatchSCF:
                 coef = torch.linalg.lstsq(B.cpu(), rhs.cpu()).solution[:, :h, 0].to(self.dev)
             else:
                 coef = None
+            tick("diis")
             dP = torch.zeros(self.nsys, dtype=torch.float64, device=self.dev)
             for gi, g in enumerate(groups):
                 if coef is None:
@@ -278,7 +295,9 @@ class BatchSCF:
                 Pn = torch.where(keep[:, None, None], g.P, Pn)
                 g.Flast = torch.where(keep[:, None, None], g.Flast, Fs[gi])
                 g.P.copy_(Pn)
+            tick("density")
             stats = torch.stack([energy, dP]).cpu().numpy()
+            tick("convergence")
             en, dpn = stats[0], stats[1]
             active = ~conv
             final_e[active] = en[active]

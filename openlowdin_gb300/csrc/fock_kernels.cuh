@@ -220,7 +220,20 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
   const int kpos = tx * 32 + threadIdx.x;
   const int bpos = ty * kWarpsPerBlock + threadIdx.y;
   if (bpos >= T.nbra) return;
-  const bool active = kpos < T.nket;
+  bool active = kpos < T.nket;
+  if (TL.split > 0.0) {
+    // mixed precision: FP32 for quartets whose Q_ab Q_cd max(|D_A|, |D_B|)
+    // bound (FP32, identical in both launches) is below the split
+    const int bi = T.bra0 + bpos, ki = T.ket0 + min(kpos, T.nket - 1);
+    const PairRec32 &b32 = T.pa32[bi];
+    const PairRec32 &k32 = T.pb32[ki];
+    float dm = 0.f;
+    if (T.DnA32) dm = __ldg(T.DnA32 + b32.sa * T.nshA + b32.sb);
+    if (T.DnB32) dm = fmaxf(dm, __ldg(T.DnB32 + k32.sa * T.nshB + k32.sb));
+    const float b = b32.Q * k32.Q * dm;
+    if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) active = false;
+  }
+  if (__all_sync(0xffffffffu, !active)) return;
   const PairT<R> *pa, *pb;
   const PrimT<R> *pra, *prb;
   const R *DA, *DB;

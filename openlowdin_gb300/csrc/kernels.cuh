@@ -68,6 +68,9 @@ struct CPTask {
   double *JB;             // nB x nB (or null)
   float *JA32;            // FP32 accumulators of the FP32 kernels
   float *JB32;
+  const float *DnA32;     // shell-block max |D| of A and B (mixed-precision split)
+  const float *DnB32;
+  int nshA, nshB;
   double scale;           // q_A q_B (1 for the reference-shaped calls)
   int bra0, nbra, ket0, nket;
   int nA, nB;

@@ -596,6 +596,9 @@ struct LibintInterface {
       for (int s2 = 0; s2 <= s1; ++s2) raw.push_back(make_pair(s1, s2, rawp));
     bin_pairs(all, raw, rawp, false);
     if (!all.upload()) return false;
+    // Schwarz factors of every pair (the mixed-precision split of couplings)
+    if (!compute_schwarz(all)) return false;
+    if (!all.upload()) return false;
     have_all = true;
     return true;
   }
@@ -727,6 +730,10 @@ bool add_cp_tasks(TaskSet<CPTask> &ts, LibintInterface *A, LibintInterface *B, c
       t.JA32 = JA ? ba.G32 : nullptr;
       t.JB = JB;
       t.JB32 = JB ? bb.G32 : nullptr;
+      t.DnA32 = ba.Dn32;
+      t.DnB32 = bb.Dn32;
+      t.nshA = A->nshell();
+      t.nshB = B->nshell();
       t.scale = scale;
       t.bra0 = A->all.start[cb];
       t.nbra = A->all.count(cb);
@@ -739,7 +746,8 @@ bool add_cp_tasks(TaskSet<CPTask> &ts, LibintInterface *A, LibintInterface *B, c
   return true;
 }
 
-bool launch_cp_groups(const TaskSet<CPTask> &ts, bool fp32, BoysTables boys, cudaStream_t s) {
+// mode 0: FP64, 1: FP32 throughout, 2: split at `split` (FP64 above, FP32 below)
+bool launch_cp_groups(const TaskSet<CPTask> &ts, int mode, double split, BoysTables boys, cudaStream_t s) {
   for (int c = 0; c < kNQC; ++c) {
     if (!ts.cnt[c]) continue;
     TaskLaunch tl{};
@@ -748,7 +756,16 @@ bool launch_cp_groups(const TaskSet<CPTask> &ts, bool fp32, BoysTables boys, cud
     tl.eps = DBL_EPSILON;
     tl.cut = 1e-10;
     tl.boys = boys;
-    CK(launch_cp_tasks(c / kNumPairClasses, c % kNumPairClasses, fp32, ts.d + ts.off[c], tl, s));
+    const int cb = c / kNumPairClasses, ck = c % kNumPairClasses;
+    if (mode == 2) {
+      tl.split = split;
+      tl.lower = 0;
+      CK(launch_cp_tasks(cb, ck, false, ts.d + ts.off[c], tl, s));
+      tl.lower = 1;
+      CK(launch_cp_tasks(cb, ck, true, ts.d + ts.off[c], tl, s));
+    } else {
+      CK(launch_cp_tasks(cb, ck, mode == 1, ts.d + ts.off[c], tl, s));
+    }
   }
   return true;
 }
@@ -780,7 +797,7 @@ bool coupling(LibintInterface *A, LibintInterface *B, const double *dDa, const d
   SpeciesBufs bb{B->dDsC.p, B->dDsC32.p, nullptr, nullptr, B->dJacc.p, B->dJacc32.p};
   if (!add_cp_tasks(A->cp, A, B, ba, bb, dJa != nullptr, dJb != nullptr, 1.0)) return false;
   if (!A->cp.upload(s)) return false;
-  if (!launch_cp_groups(A->cp, fp32, A->boys, s)) return false;
+  if (!launch_cp_groups(A->cp, fp32 ? 1 : 0, 0.0, A->boys, s)) return false;
   if (dJa) CK(launch_coupling_extract(A->dJacc.p, A->dJacc32.p, A->d_norma, nA, 1.0, 0, dJa, s));
   if (dJb) CK(launch_coupling_extract(B->dJacc.p, B->dJacc32.p, B->d_norma, nB, 1.0, 0, dJb, s));
   return true;
@@ -1166,10 +1183,10 @@ struct LowdinGB300_Batch {
     for (size_t k = 0; k < sp.size(); ++k) {
       off[k] = tot;
       tot += (long long)sp[k].h->nbasis * sp[k].h->nbasis;
-      if (sp[k].two_body && sp[k].h->is_electron) {
-        dnoff[k] = dtot;
-        dtot += (long long)sp[k].h->nshell() * sp[k].h->nshell();
-      }
+      // shell-block norms of every species: J/K screening (electrons) and the
+      // mixed-precision split of J/K and couplings
+      dnoff[k] = dtot;
+      dtot += (long long)sp[k].h->nshell() * sp[k].h->nshell();
     }
     total = tot;
     const long long dsz = dtot > 0 ? dtot : 1;
@@ -1205,7 +1222,7 @@ struct LowdinGB300_Batch {
         SpeciesBufs b{S.Ds, S.Ds32, S.Dn ? S.Dn : Dn.p, S.Dn32 ? S.Dn32 : Dn32.p, S.Gacc, S.Gacc32};
         if (!x.h->add_jk_tasks(jk, b, 0.5 * x.factor, cnt.p)) return false;
       }
-      bf[k] = SpeciesBufs{S.Ds, S.Ds32, nullptr, nullptr, S.Jacc, S.Jacc32};
+      bf[k] = SpeciesBufs{S.Ds, S.Ds32, S.Dn, S.Dn32, S.Jacc, S.Jacc32};
     }
     // coupling tasks: every species pair of a system
     for (size_t a = 0; a < sp.size(); ++a)
@@ -1233,7 +1250,7 @@ struct LowdinGB300_Batch {
     CK(launch_prepare_batch(slots.p, nslots, total, s));
     const int jk_mixed = precision & 1;
     if (!LibintInterface::launch_jk_groups(jk, jk_mixed, jk_mixed ? split : 0.0, boys, s)) return false;
-    if (!launch_cp_groups(cp, (precision & 2) != 0, boys, s)) return false;
+    if (!launch_cp_groups(cp, (precision & 2) ? 2 : 0, split, boys, s)) return false;
     CK(launch_finalize_batch(slots.p, nslots, total, s));
     return true;
   }
