@@ -30,6 +30,9 @@ import sys
 import threading
 import time
 
+# one BLAS thread per host eigensolver worker (set before numpy is imported)
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -44,7 +47,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=4, help="molecules per step")
+    ap.add_argument("--batch", type=int, default=8, help="molecules per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-fock", type=int, default=0,
                     help="profiling case: N batched Fock builds (FP64) of the step's molecules at the "

@@ -60,10 +60,14 @@ class BatchSCF:
         groups = {}
         self.where = []         # per system: list of (group key, slot)
         hostmats = {}
+        for sysd in systems:
+            self.handles.append([lint.Libint2Interface(sp, k + 1) for k, sp in enumerate(sysd["species"])])
+        # one-electron matrices of all molecules on the host pool (the C++
+        # integral code runs without the interpreter lock)
+        one_body = list(self._host_pool().map(lambda a: _one_body(*a), zip(self.handles, systems)))
         for si, sysd in enumerate(systems):
-            hs = [lint.Libint2Interface(sp, k + 1) for k, sp in enumerate(sysd["species"])]
-            self.handles.append(hs)
-            H, S = _one_body(hs, sysd)
+            hs = self.handles[si]
+            H, S = one_body[si]
             w = []
             for k, sp in enumerate(sysd["species"]):
                 key = (hs[k].nbasis, n_occ(sp), float(sp["eta"]))
@@ -147,6 +151,14 @@ class BatchSCF:
 
     _pool = None
 
+    @staticmethod
+    def _host_pool():
+        import concurrent.futures as cf
+        import os
+        if BatchSCF._pool is None:
+            BatchSCF._pool = cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)))
+        return BatchSCF._pool
+
     def _density(self, g, F):
         """eta C_occ C_occ^T of the Roothaan problem F C = S C e.  Matrices
         below HOST_EIGH_MAX functions are diagonalised by LAPACK on a host
@@ -160,10 +172,6 @@ class BatchSCF:
             e, Cp = torch.linalg.eigh(Fp)
             Co = g.X @ Cp[:, :, :g.occ]
             return g.eta * Co @ Co.transpose(1, 2)
-        import concurrent.futures as cf
-        import os
-        if BatchSCF._pool is None:
-            BatchSCF._pool = cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)))
         host = Fp.cpu().numpy()
         occ = g.occ
         vecs = np.empty((host.shape[0], host.shape[1], occ))
@@ -172,7 +180,7 @@ class BatchSCF:
             w, V = np.linalg.eigh(host[i])
             vecs[i] = V[:, :occ]
 
-        list(BatchSCF._pool.map(work, range(host.shape[0])))
+        list(self._host_pool().map(work, range(host.shape[0])))
         Cp = torch.from_numpy(vecs).to(self.dev, non_blocking=True)
         Co = g.X @ Cp
         return g.eta * Co @ Co.transpose(1, 2)
