@@ -50,8 +50,10 @@ def parse():
     ap.add_argument("--batch", type=int, default=8, help="molecules per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-fock", type=int, default=0,
-                    help="profiling case: N batched Fock builds (FP64) of the step's molecules at the "
+                    help="profiling case: N batched Fock builds of the step's molecules at the "
                          "core-Hamiltonian-guess densities, then exit")
+    ap.add_argument("--profile-precision", type=int, default=0,
+                    help="precision bits of the profiled builds (0 FP64, 3 mixed split)")
     return ap.parse_args()
 
 
@@ -70,7 +72,7 @@ def profile_fock(args):
     b = torch.cuda.Event(enable_timing=True)
     a.record()
     for _ in range(args.profile_fock):
-        s.batch.fock(0, 0.0, st)
+        s.batch.fock(args.profile_precision, 1e-5, st)
     b.record()
     torch.cuda.synchronize()
     print(json.dumps({"profile_fock_builds": args.profile_fock, "molecules": args.batch,
