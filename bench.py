@@ -3,7 +3,7 @@
 
 Workload (one "step"): B independent APMO Hartree-Fock solves of seeded
 4-water clusters (electrons: 136 Cartesian functions, 40 e-; quantum protons:
-one H_1 species, 56 functions, 8 protons), each from the core-Hamiltonian guess
+8 one-particle species of 7 functions each), each from the core-Hamiltonian guess
 to |dE| < 1e-8 Eh and rms(dP) < 1e-6, including the per-molecule setup (one-
 electron integrals, pair lists, Schwarz factors).  Synthetic inputs generated
 by openlowdin_gb300.systems (seeds rank*B + i).
@@ -38,7 +38,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "SCF(+MP2) solves/s and p50/p99 latency, mixed vs plain FP64 GPU at 1e-6 Eh"
 UNIT = "solves/s"
-WORKLOAD = "APMO HF, 4-water cluster (e- 136 fn + H_1 56 fn, 8 quantum protons), dE<1e-8"
+WORKLOAD = ("APMO HF, 4-water cluster: e- 136 Cartesian fn (40 e-) + 8 one-proton species "
+            "(7 fn each, s 4/8/16/24 + p 16), classical O; dE<1e-8 Eh, rms dP<1e-6")
 
 
 def parse():
@@ -344,7 +345,7 @@ def main():
         prof = os.path.join(ROOT, "profiles", "roofline_traffic.json")
         if os.path.exists(prof):
             try:
-                traffic = json.load(open(prof)).get("jk_electrons_bytes_per_build")
+                traffic = json.load(open(prof)).get("bytes_per_build")
             except Exception:
                 traffic = None
         out["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
