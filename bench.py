@@ -336,7 +336,7 @@ def main():
         torch.cuda.synchronize()
         ms = a.elapsed_time(b) / reps
         counts = s.batch.quartets(stv)
-        cpc = s.batch.coupling_quartets()
+        cpc = s.batch.coupling_quartets(stv)
         fl = FL.class_table_flops(counts, "jk") + FL.class_table_flops(cpc, "coupling")
         peak64 = lint.measure_fma_tflops(True)
         peak32 = lint.measure_fma_tflops(False)

@@ -187,10 +187,10 @@ int LowdinGB300_batch_finalize(LowdinGB300_Batch *b, void *stream);
    0 = FP64 throughout. */
 int LowdinGB300_batch_fock(LowdinGB300_Batch *b, int precision, double split, void *stream);
 /* quartets evaluated per (bra pair class, ket pair class) by the last J/K
-   build of the batch (36 entries; synchronises `stream`), and the coupling
-   quartets per class (every pair of a species pair, no screening) */
+   build and by the last coupling build of the batch (36 entries each;
+   synchronise `stream`) */
 int LowdinGB300_batch_quartets(LowdinGB300_Batch *b, long long *out, void *stream);
-int LowdinGB300_batch_coupling_quartets(LowdinGB300_Batch *b, long long *out);
+int LowdinGB300_batch_coupling_quartets(LowdinGB300_Batch *b, long long *out, void *stream);
 
 /* Number of CUDA kernels this library has launched in the process. */
 long long LowdinGB300_launch_count(void);

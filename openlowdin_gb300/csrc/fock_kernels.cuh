@@ -221,6 +221,15 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
   const int bpos = ty * kWarpsPerBlock + threadIdx.y;
   if (bpos >= T.nbra) return;
   bool active = kpos < T.nket;
+  {
+    // |(ij|kl)| <= Q_ab Q_cd for every component (Schwarz), and raw values
+    // below the cut are dropped, so such a quartet contributes nothing; the
+    // test is done in FP32 in mixed launches so both launches agree
+    const int bi = T.bra0 + bpos, ki = T.ket0 + min(kpos, T.nket - 1);
+    const bool tiny = TL.split > 0.0 ? T.pa32[bi].Q * T.pb32[ki].Q * 0.999f < (float)TL.cut
+                                     : T.pa[bi].Q * T.pb[ki].Q * (1.0 - 1e-9) < TL.cut;
+    if (tiny) active = false;
+  }
   if (TL.split > 0.0) {
     // mixed precision: FP32 for quartets whose Q_ab Q_cd max(|D_A|, |D_B|)
     // bound (FP32, identical in both launches) is below the split
@@ -234,6 +243,10 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
     if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) active = false;
   }
   if (__all_sync(0xffffffffu, !active)) return;
+  if (T.count) {
+    const unsigned cnt = __popc(__ballot_sync(0xffffffffu, active));
+    if (threadIdx.x == 0) atomicAdd(T.count, (unsigned long long)cnt);
+  }
   const PairT<R> *pa, *pb;
   const PrimT<R> *pra, *prb;
   const R *DA, *DB;
@@ -329,6 +342,8 @@ __global__ void __launch_bounds__(128) it_kernel(ITParams P) {
   const int bi = P.bra0 + bpos, ki = P.ket0 + kpos;
   const PairRec bra = P.pa[bi];
   const PairRec ket = P.pb[ki];
+  // every raw integral is bounded by Q_ab Q_cd (Schwarz) and only |v| > cut is used
+  if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) return;
   if (P.screen) {
     const double b = bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
     if (b < P.eps) return;

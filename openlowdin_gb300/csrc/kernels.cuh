@@ -70,6 +70,7 @@ struct CPTask {
   float *JB32;
   const float *DnA32;     // shell-block max |D| of A and B (mixed-precision split)
   const float *DnB32;
+  unsigned long long *count;  // quartets evaluated (may be null)
   int nshA, nshB;
   double scale;           // q_A q_B (1 for the reference-shaped calls)
   int bra0, nbra, ket0, nket;

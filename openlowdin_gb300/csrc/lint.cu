@@ -596,8 +596,13 @@ struct LibintInterface {
       for (int s2 = 0; s2 <= s1; ++s2) raw.push_back(make_pair(s1, s2, rawp));
     bin_pairs(all, raw, rawp, false);
     if (!all.upload()) return false;
-    // Schwarz factors of every pair (the mixed-precision split of couplings)
+    // Schwarz factors of every pair: exact skip of quartets whose bound is
+    // below the coupling cut, and the mixed-precision split; sorted by Q inside
+    // a class so skipped quartets cluster into whole warps
     if (!compute_schwarz(all)) return false;
+    std::vector<PairRec> tmp = all.h;
+    std::vector<PrimRec> tmpp = all.hp;
+    bin_pairs(all, tmp, tmpp, true);
     if (!all.upload()) return false;
     have_all = true;
     return true;
@@ -701,7 +706,8 @@ struct LibintInterface {
 
 // coupling tasks of species pair (A bra, B ket) into ts
 bool add_cp_tasks(TaskSet<CPTask> &ts, LibintInterface *A, LibintInterface *B, const SpeciesBufs &ba,
-                  const SpeciesBufs &bb, bool want_a, bool want_b, double scale) {
+                  const SpeciesBufs &bb, bool want_a, bool want_b, double scale,
+                  unsigned long long *counters = nullptr) {
   // JA (from D_B) accumulates into ba.G / ba.G32, JB (from D_A) into bb.G / bb.G32
   double *JA = want_a ? ba.G : nullptr, *JB = want_b ? bb.G : nullptr;
   if (!A->ensure_all() || !B->ensure_all()) return false;
@@ -732,6 +738,7 @@ bool add_cp_tasks(TaskSet<CPTask> &ts, LibintInterface *A, LibintInterface *B, c
       t.JB32 = JB ? bb.G32 : nullptr;
       t.DnA32 = ba.Dn32;
       t.DnB32 = bb.Dn32;
+      t.count = counters ? counters + cb * kNumPairClasses + ck : nullptr;
       t.nshA = A->nshell();
       t.nshB = B->nshell();
       t.scale = scale;
@@ -1191,7 +1198,7 @@ struct LowdinGB300_Batch {
     total = tot;
     const long long dsz = dtot > 0 ? dtot : 1;
     if (!Ds.ensure(tot) || !Gacc.ensure(tot) || !Jacc.ensure(tot) || !Dn.ensure(dsz) || !Ds32.ensure(tot) ||
-        !Gacc32.ensure(tot) || !Jacc32.ensure(tot) || !Dn32.ensure(dsz) || !cnt.ensure(kNQC))
+        !Gacc32.ensure(tot) || !Jacc32.ensure(tot) || !Dn32.ensure(dsz) || !cnt.ensure(2 * kNQC))
       return false;
     std::vector<SpeciesSlot> hs(sp.size());
     std::vector<SpeciesBufs> bf(sp.size());
@@ -1228,7 +1235,8 @@ struct LowdinGB300_Batch {
     for (size_t a = 0; a < sp.size(); ++a)
       for (size_t b = a + 1; b < sp.size(); ++b) {
         if (sp[a].sys != sp[b].sys) continue;
-        if (!add_cp_tasks(cp, sp[a].h, sp[b].h, bf[a], bf[b], true, true, sp[a].q * sp[b].q)) return false;
+        if (!add_cp_tasks(cp, sp[a].h, sp[b].h, bf[a], bf[b], true, true, sp[a].q * sp[b].q, cnt.p + kNQC))
+          return false;
       }
     nslots = (int)hs.size();
     if (!slots.ensure(hs.size())) return false;
@@ -1246,7 +1254,7 @@ struct LowdinGB300_Batch {
     }
     CK(cudaMemsetAsync(Dn.p, 0, Dn.n * sizeof(double), s));
     CK(cudaMemsetAsync(Dn32.p, 0, Dn32.n * sizeof(float), s));
-    CK(cudaMemsetAsync(cnt.p, 0, kNQC * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(cnt.p, 0, 2 * kNQC * sizeof(unsigned long long), s));
     CK(launch_prepare_batch(slots.p, nslots, total, s));
     const int jk_mixed = precision & 1;
     if (!LibintInterface::launch_jk_groups(jk, jk_mixed, jk_mixed ? split : 0.0, boys, s)) return false;
@@ -1304,13 +1312,16 @@ int LowdinGB300_batch_quartets(LowdinGB300_Batch *b, long long *out, void *strea
   return kNQC;
 }
 
-int LowdinGB300_batch_coupling_quartets(LowdinGB300_Batch *b, long long *out) {
+int LowdinGB300_batch_coupling_quartets(LowdinGB300_Batch *b, long long *out, void *stream) {
   if (!b || !b->finalized) return -1;
-  for (int c = 0; c < kNQC; ++c) {
-    long long q = 0;
-    for (const auto &t : b->cp.group[c]) q += (long long)t.nbra * t.nket;
-    out[c] = q;
+  unsigned long long c[kNQC];
+  if (cudaMemcpyAsync(c, b->cnt.p + kNQC, sizeof(c), cudaMemcpyDeviceToHost, (cudaStream_t)stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) {
+    set_error("batch_coupling_quartets: copy failed");
+    return -1;
   }
+  for (int k = 0; k < kNQC; ++k) out[k] = (long long)c[k];
   return kNQC;
 }
 

@@ -82,7 +82,7 @@ def lib():
         L.LowdinGB300_batch_fock.restype = ctypes.c_int
         L.LowdinGB300_batch_quartets.argtypes = [_vp, np.ctypeslib.ndpointer(dtype=np.int64), _vp]
         L.LowdinGB300_batch_quartets.restype = ctypes.c_int
-        L.LowdinGB300_batch_coupling_quartets.argtypes = [_vp, np.ctypeslib.ndpointer(dtype=np.int64)]
+        L.LowdinGB300_batch_coupling_quartets.argtypes = [_vp, np.ctypeslib.ndpointer(dtype=np.int64), _vp]
         L.LowdinGB300_batch_coupling_quartets.restype = ctypes.c_int
         _LIB = L
     return _LIB
@@ -150,9 +150,10 @@ class Batch:
             _check()
         return out.reshape(6, 6)
 
-    def coupling_quartets(self) -> np.ndarray:
+    def coupling_quartets(self, stream: int = 0) -> np.ndarray:
         out = np.zeros(36, np.int64)
-        lib().LowdinGB300_batch_coupling_quartets(self.h, out)
+        if lib().LowdinGB300_batch_coupling_quartets(self.h, out, stream) < 0:
+            _check()
         return out.reshape(6, 6)
 
     def close(self):
