@@ -192,6 +192,24 @@ int LowdinGB300_batch_fock(LowdinGB300_Batch *b, int precision, double split, vo
 int LowdinGB300_batch_quartets(LowdinGB300_Batch *b, long long *out, void *stream);
 int LowdinGB300_batch_coupling_quartets(LowdinGB300_Batch *b, long long *out, void *stream);
 
+/* Allocation-free two-particle build (no counterpart in the reference).
+   Same result as LowdinGB300_twobody_device, for callers that cannot allocate
+   device memory once running: a host program whose device memory is owned by
+   its own pool, a serving loop that forbids allocations after warm-up, or code
+   queuing into a captured stream.  Work buffers live in one static device
+   array (LowdinGB300_noalloc_scratch_bytes() bytes, ~9.5 MB, held by every GPU
+   that loads the library until the process exits); species are limited to 512
+   Cartesian functions and 512 shells, larger ones are rejected with an error.
+   The handle must have been set up with LibintInterface_init_2body_ints (which
+   does allocate).  The first call on a device looks up the array's device
+   address (cudaGetSymbolAddress): make that first call before any stream
+   capture.  Every call shares the array and clears what it accumulates; calls
+   whose work overlaps on the GPU (other streams, other handles) race.
+   Returns 0, or -1 with LowdinGB300_last_error() set. */
+size_t LowdinGB300_noalloc_scratch_bytes(void);
+int LowdinGB300_twobody_device_noalloc(LibintInterface *lint, const double *dD, double *dG, double factor,
+                                       int precision, double split, void *stream);
+
 /* Number of CUDA kernels this library has launched in the process. */
 long long LowdinGB300_launch_count(void);
 

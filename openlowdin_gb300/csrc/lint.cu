@@ -1326,3 +1326,131 @@ int LowdinGB300_batch_coupling_quartets(LowdinGB300_Batch *b, long long *out, vo
 }
 
 }  // extern "C"
+
+// ====================================================== allocation-free build
+// LowdinGB300_twobody_device_noalloc: the device two-particle build for
+// callers that must not allocate device memory once they are running -- a host
+// program that owns every device byte through its own pool, a serving loop that
+// forbids allocations after warm-up, or code queuing work into a captured
+// stream.  Its work buffers (scaled densities, shell-block norms, accumulators,
+// task list, counters) live in one file-scope device array instead of
+// cudaMalloc'd memory; the handle's shell-pair data must already exist
+// (LibintInterface_init_2body_ints, which does allocate, is called at set-up).
+namespace {
+
+constexpr int kNoAllocMaxBasis = 512;   // largest species (Cartesian functions)
+constexpr int kNoAllocMaxShells = 512;  // largest species (shells)
+constexpr int kNoAllocMaxTasks = 64;
+constexpr size_t kNaN2 = (size_t)kNoAllocMaxBasis * kNoAllocMaxBasis;
+constexpr size_t kNaS2 = (size_t)kNoAllocMaxShells * kNoAllocMaxShells;
+constexpr size_t na_align(size_t x) { return (x + 255) / 256 * 256; }
+constexpr size_t kNaOffDs = 0;
+constexpr size_t kNaOffGacc = na_align(kNaOffDs + 8 * kNaN2);
+constexpr size_t kNaOffDn = na_align(kNaOffGacc + 8 * kNaN2);
+constexpr size_t kNaOffDs32 = na_align(kNaOffDn + 8 * kNaS2);
+constexpr size_t kNaOffGacc32 = na_align(kNaOffDs32 + 4 * kNaN2);
+constexpr size_t kNaOffDn32 = na_align(kNaOffGacc32 + 4 * kNaN2);
+constexpr size_t kNaOffCnt = na_align(kNaOffDn32 + 4 * kNaS2);
+constexpr size_t kNaOffTasks = na_align(kNaOffCnt + 8 * kNQC);
+constexpr size_t kNaBytes = na_align(kNaOffTasks + sizeof(JKTask) * kNoAllocMaxTasks);  // ~9.5 MB
+
+// Every GPU that loads the library holds this array until the process exits.
+// In host code the name is only a host-side stand-in: the device address comes
+// from cudaGetSymbolAddress, once per device.
+__device__ __align__(256) unsigned char g_twobody_scratch[kNaBytes];
+
+std::mutex g_na_mu;
+std::vector<std::pair<int, unsigned char *>> g_na_addr;
+
+// device address of the scratch array on the current device (set-up on the
+// first call per device, with that device current)
+bool noalloc_scratch(unsigned char **out) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_na_mu);
+  for (auto &e : g_na_addr)
+    if (e.first == dev) {
+      *out = e.second;
+      return true;
+    }
+  unsigned char *p = nullptr;
+  CK(cudaGetSymbolAddress((void **)&p, g_twobody_scratch));
+  g_na_addr.push_back({dev, p});
+  *out = p;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t LowdinGB300_noalloc_scratch_bytes(void) { return kNaBytes; }
+
+int LowdinGB300_twobody_device_noalloc(LibintInterface *lint, const double *dD, double *dG, double factor,
+                                       int precision, double split, void *stream) {
+  if (!check_handle(lint, __func__)) return -1;
+  if (lint->dirty || !lint->have_sig || !lint->stream) {
+    set_error("%s: call LibintInterface_init_2body_ints on this handle first (set-up allocates the shell-pair "
+              "data; this entry point allocates nothing)",
+              __func__);
+    return -1;
+  }
+  const int n = lint->nbasis, nsh = lint->nshell();
+  if (n > kNoAllocMaxBasis || nsh > kNoAllocMaxShells) {
+    set_error("%s: species with %d functions / %d shells exceeds the allocation-free limit of %d functions and "
+              "%d shells; use LowdinGB300_twobody_device",
+              __func__, n, nsh, kNoAllocMaxBasis, kNoAllocMaxShells);
+    return -1;
+  }
+  unsigned char *base = nullptr;
+  if (!noalloc_scratch(&base)) return -1;
+  cudaStream_t s = (cudaStream_t)stream;
+  double *Ds = (double *)(base + kNaOffDs), *Gacc = (double *)(base + kNaOffGacc), *Dn = (double *)(base + kNaOffDn);
+  float *Ds32 = (float *)(base + kNaOffDs32), *Gacc32 = (float *)(base + kNaOffGacc32);
+  float *Dn32 = (float *)(base + kNaOffDn32);
+  unsigned long long *cnt = (unsigned long long *)(base + kNaOffCnt);
+  JKTask *dtasks = (JKTask *)(base + kNaOffTasks);
+  // task list on the host, flattened into the scratch array
+  TaskSet<JKTask> ts;
+  SpeciesBufs bf{Ds, Ds32, Dn, Dn32, Gacc, Gacc32};
+  if (!lint->add_jk_tasks(ts, bf, 0.5 * factor, cnt)) return -1;
+  std::vector<JKTask> flat;
+  for (int c = 0; c < kNQC; ++c) {
+    ts.off[c] = (int)flat.size();
+    ts.cnt[c] = (int)ts.group[c].size();
+    int b = 0;
+    for (JKTask t : ts.group[c]) {
+      t.nbx = task_nbx(t.nket);
+      t.blk0 = b;
+      b += t.nbx * task_nby(t.nbra);
+      flat.push_back(t);
+    }
+    ts.nblk[c] = b;
+  }
+  if ((int)flat.size() > kNoAllocMaxTasks) {
+    set_error("%s: %d tasks exceed the allocation-free limit of %d", __func__, (int)flat.size(), kNoAllocMaxTasks);
+    return -1;
+  }
+  if (!flat.empty() &&
+      cudaMemcpyAsync(dtasks, flat.data(), flat.size() * sizeof(JKTask), cudaMemcpyHostToDevice, s) != cudaSuccess) {
+    set_error("%s: task upload failed", __func__);
+    return -1;
+  }
+  ts.d = dtasks;
+  // the array keeps the previous call's contents: clear what accumulates
+  if (launch_prepare_density(dD, lint->d_norma, lint->d_shell_of, n, nsh, Ds, Ds32, Dn, Dn32, s) != cudaSuccess ||
+      cudaMemsetAsync(Gacc, 0, sizeof(double) * n * n, s) != cudaSuccess ||
+      cudaMemsetAsync(Gacc32, 0, sizeof(float) * n * n, s) != cudaSuccess ||
+      cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * kNQC, s) != cudaSuccess) {
+    set_error("%s: preparation failed", __func__);
+    return -1;
+  }
+  if (!LibintInterface::launch_jk_groups(ts, precision, split, lint->boys, s)) return -1;
+  if (launch_symmetrize(Gacc, Gacc32, lint->d_norma, n, 0.25, dG, s) != cudaSuccess) {
+    set_error("%s: symmetrisation failed", __func__);
+    return -1;
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -70,6 +70,10 @@ def lib():
         L.LowdinGB300_measure_fma_tflops.argtypes = [ctypes.c_int]
         L.LowdinGB300_measure_fma_tflops.restype = ctypes.c_double
         L.LowdinGB300_launch_count.restype = ctypes.c_longlong
+        L.LowdinGB300_noalloc_scratch_bytes.restype = ctypes.c_size_t
+        L.LowdinGB300_twobody_device_noalloc.argtypes = [_vp, _vp, _vp, ctypes.c_double, ctypes.c_int,
+                                                         ctypes.c_double, _vp]
+        L.LowdinGB300_twobody_device_noalloc.restype = ctypes.c_int
         L.LowdinGB300_batch_new.restype = _vp
         L.LowdinGB300_batch_del.argtypes = [_vp]
         L.LowdinGB300_batch_add_system.argtypes = [_vp, ctypes.POINTER(_vp), ctypes.c_int, _f64p, _f64p,
@@ -105,7 +109,8 @@ EXPORTED_SYMBOLS = [
     "LowdinGB300_pair_class_counts", "LowdinGB300_measure_fma_tflops", "LowdinGB300_launch_count",
     "LowdinGB300_batch_new", "LowdinGB300_batch_del", "LowdinGB300_batch_add_system",
     "LowdinGB300_batch_finalize", "LowdinGB300_batch_fock", "LowdinGB300_batch_quartets",
-    "LowdinGB300_batch_coupling_quartets",
+    "LowdinGB300_batch_coupling_quartets", "LowdinGB300_noalloc_scratch_bytes",
+    "LowdinGB300_twobody_device_noalloc",
 ]
 
 
