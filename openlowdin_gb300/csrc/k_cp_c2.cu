@@ -1,0 +1,6 @@
+// coupling kernels (FP64 and FP32) of bra pair class 2 (pp) for every ket pair class.
+#include "class_tables.cuh"
+
+namespace lgb {
+LGB_CP_TABLES(2)
+}  // namespace lgb

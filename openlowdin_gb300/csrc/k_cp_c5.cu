@@ -1,0 +1,6 @@
+// coupling kernels (FP64 and FP32) of bra pair class 5 (dd) for every ket pair class.
+#include "class_tables.cuh"
+
+namespace lgb {
+LGB_CP_TABLES(5)
+}  // namespace lgb

@@ -1,0 +1,6 @@
+// first-quarter kernels of bra pair class 2 (pp) for every ket pair class.
+#include "class_tables.cuh"
+
+namespace lgb {
+LGB_IT_TABLE(2)
+}  // namespace lgb

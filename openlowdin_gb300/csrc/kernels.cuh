@@ -86,7 +86,24 @@ struct TaskLaunch {
   int lower;              // 1: this launch takes the quartets below split
   double cut;             // coupling: |raw| < cut is dropped
   BoysTables boys;
+  double *scratch;        // generic (runtime-class) kernels: per-thread work arrays
+  int scratch_blocks;     // blocks the scratch holds slots for
 };
+
+// Kernel entry types of the class-templated launch tables (class_tables.cuh);
+// null entries are served by the generic runtime-class kernels (classes of
+// total angular momentum above kTemplatedMaxL).
+using JKFn = void (*)(const JKTask *, TaskLaunch);
+using CPFn = void (*)(const CPTask *, TaskLaunch);
+struct ITParams;
+using ITFn = void (*)(ITParams);
+__host__ __device__ constexpr int pc_L(int pc) { return pc_la(pc) + pc_lb(pc); }
+constexpr int kTemplatedMaxL = 6;   // classes above this total use the generic kernels
+
+// scratch of the generic kernels: doubles per thread, threads per block, blocks
+int generic_scratch_doubles();
+constexpr int kGenericThreads = 32 * kWarpsPerBlock;
+constexpr int kGenericBlocks = 152;
 
 // First-quarter transform A[nu][lam][sig] += sum_mu C_p(mu) (mu nu|lam sig).
 struct ITParams {
@@ -107,6 +124,7 @@ struct ITParams {
   double *A;
   BoysTables boys;
   double cut;             // raw values with |v| <= cut are dropped (1e-10)
+  double *scratch;        // generic classes only
 };
 
 struct SchwarzParams {
@@ -115,13 +133,15 @@ struct SchwarzParams {
   int p0, np;
   double *Q;              // per pair record
   BoysTables boys;
+  double *scratch;        // generic classes only
 };
 
 // blocks of one task (grid tile of 32 kets x kWarpsPerBlock bras)
 inline int task_nbx(int nket) { return (nket + 31) / 32; }
 inline int task_nby(int nbra) { return (nbra + kWarpsPerBlock - 1) / kWarpsPerBlock; }
 
-// launchers (kernels exist for every class with l <= class_max_l())
+// launchers (every class with l <= kMaxL; generic classes need tl.scratch /
+// p.scratch of kGenericBlocks * kGenericThreads * generic_scratch_doubles())
 cudaError_t launch_jk_tasks(int pcb, int pck, bool fp32, const JKTask *dtasks, const TaskLaunch &tl,
                             cudaStream_t s);
 cudaError_t launch_cp_tasks(int pcb, int pck, bool fp32, const CPTask *dtasks, const TaskLaunch &tl,
@@ -129,6 +149,7 @@ cudaError_t launch_cp_tasks(int pcb, int pck, bool fp32, const CPTask *dtasks, c
 cudaError_t launch_it(int pcb, int pck, const ITParams &p, cudaStream_t s);
 cudaError_t launch_schwarz(int pc, const SchwarzParams &p, cudaStream_t s);
 bool class_supported(int pcb, int pck);
+inline bool class_generic(int pcb, int pck) { return pc_L(pcb) + pc_L(pck) > kTemplatedMaxL; }
 
 // small kernels (the *32 arguments may be null)
 cudaError_t launch_prepare_density(const double *D, const double *norma, const int *shell_of, int n, int nsh,

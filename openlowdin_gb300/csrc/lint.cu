@@ -396,7 +396,16 @@ struct TaskSet {
     d = nullptr;
     cap = 0;
   }
+  // true if a group of the set runs on the generic (runtime-class) kernels
+  bool needs_generic() const {
+    for (int c = 0; c < kNQC; ++c)
+      if (cnt[c] && class_generic(c / kNumPairClasses, c % kNumPairClasses)) return true;
+    return false;
+  }
 };
+
+// doubles of the generic kernels' work arrays (one slot per thread of their grid)
+size_t generic_scratch_size() { return (size_t)kGenericBlocks * kGenericThreads * generic_scratch_doubles(); }
 
 }  // namespace
 
@@ -423,6 +432,7 @@ struct LibintInterface {
   DevBuf<double> dD, dDs, dDn, dGacc, dG, dA, dC, dDsC, dJacc;
   DevBuf<float> dDs32, dDn32, dGacc32, dDsC32, dJacc32;
   DevBuf<unsigned long long> dcount;
+  DevBuf<double> dgen;       // work arrays of the generic kernels (species with d-shell pairs)
   long long last_quartets = -1;
   long long class_quartets[kNQC] = {0};
   TaskSet<JKTask> jk;        // cached J/K tasks of the handle's own buffers
@@ -443,6 +453,7 @@ struct LibintInterface {
     dDsC.release(); dJacc.release();
     dDs32.release(); dDn32.release(); dGacc32.release(); dDsC32.release(); dJacc32.release();
     dcount.release();
+    dgen.release();
     jk.release();
     cp.release();
     jk_ready = false;
@@ -452,6 +463,7 @@ struct LibintInterface {
     dirty = true;
   }
   int nshell() const { return (int)shells.size(); }
+  double *gen_scratch() { return dgen.ensure(generic_scratch_size()) ? dgen.p : nullptr; }
 
   bool ensure_base() {
     if (!dirty && stream) return true;
@@ -544,7 +556,8 @@ struct LibintInterface {
     if (!dq.ensure(L.h.size())) return false;
     for (int pc = 0; pc < kNumPairClasses; ++pc) {
       if (!L.count(pc)) continue;
-      SchwarzParams sp{L.d, L.dp, L.start[pc], L.count(pc), dq.p, boys};
+      SchwarzParams sp{L.d, L.dp, L.start[pc], L.count(pc), dq.p, boys, nullptr};
+      if (pc_L(pc) * 2 > kTemplatedMaxL && !(sp.scratch = gen_scratch())) return false;
       CK(launch_schwarz(pc, sp, stream));
     }
     std::vector<double> q(L.h.size());
@@ -628,7 +641,9 @@ struct LibintInterface {
     CK(cudaMemsetAsync(dGacc.p, 0, sizeof(double) * n * n, s));
     CK(cudaMemsetAsync(dGacc32.p, 0, sizeof(float) * n * n, s));
     CK(cudaMemsetAsync(dcount.p, 0, sizeof(unsigned long long) * kNQC, s));
-    if (!launch_jk_groups(jk, precision, split, boys, s)) return false;
+    double *scr = nullptr;
+    if (jk.needs_generic() && !(scr = gen_scratch())) return false;
+    if (!launch_jk_groups(jk, precision, split, boys, scr, s)) return false;
     CK(launch_symmetrize(dGacc.p, dGacc32.p, d_norma, n, 0.25, dGout, s));
     unsigned long long cnt[kNQC];
     CK(cudaMemcpyAsync(cnt, dcount.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
@@ -678,11 +693,14 @@ struct LibintInterface {
     return true;
   }
 
+  // scratch: work arrays of the generic kernels (needed when ts.needs_generic())
   static bool launch_jk_groups(const TaskSet<JKTask> &ts, int precision, double split, BoysTables boys,
-                               cudaStream_t s) {
+                               double *scratch, cudaStream_t s) {
     for (int c = 0; c < kNQC; ++c) {
       if (!ts.cnt[c]) continue;
       TaskLaunch tl{};
+      tl.scratch = scratch;
+      tl.scratch_blocks = kGenericBlocks;
       tl.ntasks = ts.cnt[c];
       tl.nblocks = ts.nblk[c];
       tl.eps = DBL_EPSILON;
@@ -754,10 +772,13 @@ bool add_cp_tasks(TaskSet<CPTask> &ts, LibintInterface *A, LibintInterface *B, c
 }
 
 // mode 0: FP64, 1: FP32 throughout, 2: split at `split` (FP64 above, FP32 below)
-bool launch_cp_groups(const TaskSet<CPTask> &ts, int mode, double split, BoysTables boys, cudaStream_t s) {
+bool launch_cp_groups(const TaskSet<CPTask> &ts, int mode, double split, BoysTables boys, double *scratch,
+                      cudaStream_t s) {
   for (int c = 0; c < kNQC; ++c) {
     if (!ts.cnt[c]) continue;
     TaskLaunch tl{};
+    tl.scratch = scratch;
+    tl.scratch_blocks = kGenericBlocks;
     tl.ntasks = ts.cnt[c];
     tl.nblocks = ts.nblk[c];
     tl.eps = DBL_EPSILON;
@@ -804,7 +825,9 @@ bool coupling(LibintInterface *A, LibintInterface *B, const double *dDa, const d
   SpeciesBufs bb{B->dDsC.p, B->dDsC32.p, nullptr, nullptr, B->dJacc.p, B->dJacc32.p};
   if (!add_cp_tasks(A->cp, A, B, ba, bb, dJa != nullptr, dJb != nullptr, 1.0)) return false;
   if (!A->cp.upload(s)) return false;
-  if (!launch_cp_groups(A->cp, fp32 ? 1 : 0, 0.0, A->boys, s)) return false;
+  double *scr = nullptr;
+  if (A->cp.needs_generic() && !(scr = A->gen_scratch())) return false;
+  if (!launch_cp_groups(A->cp, fp32 ? 1 : 0, 0.0, A->boys, scr, s)) return false;
   if (dJa) CK(launch_coupling_extract(A->dJacc.p, A->dJacc32.p, A->d_norma, nA, 1.0, 0, dJa, s));
   if (dJb) CK(launch_coupling_extract(B->dJacc.p, B->dJacc32.p, B->d_norma, nB, 1.0, 0, dJb, s));
   return true;
@@ -860,6 +883,7 @@ bool first_quarter(LibintInterface *A, LibintInterface *B, const double *hD, con
         q.ket0 = A->sig.start[ck];
         q.nket = A->sig.count(ck);
         q.triangle = cb == ck;
+        if (class_generic(cb, ck) && !q.scratch && !(q.scratch = A->gen_scratch())) return false;
         CK(launch_it(cb, ck, q, s));
       }
   } else {
@@ -880,6 +904,7 @@ bool first_quarter(LibintInterface *A, LibintInterface *B, const double *hD, con
         q.ket0 = B->all.start[ck];
         q.nket = B->all.count(ck);
         q.triangle = 0;
+        if (class_generic(cb, ck) && !q.scratch && !(q.scratch = A->gen_scratch())) return false;
         CK(launch_it(cb, ck, q, s));
       }
   }
@@ -1133,7 +1158,7 @@ double LowdinGB300_measure_fma_tflops(int fp64) {
   return t;
 }
 
-const char *LowdinGB300_version(void) { return "lowdin_gb300 0.1 (sm_103a, FP64/FP32 Obara-Saika, l<=1 kernels)"; }
+const char *LowdinGB300_version(void) { return "lowdin_gb300 0.1 (sm_103a, FP64/FP32 Obara-Saika, s p d shells)"; }
 
 }  // extern "C"
 
@@ -1160,6 +1185,7 @@ struct LowdinGB300_Batch {
   DevBuf<float> Ds32, Dn32, Gacc32, Jacc32;
   DevBuf<unsigned long long> cnt;
   DevBuf<SpeciesSlot> slots;
+  DevBuf<double> gen;  // work arrays of the generic kernels (systems with d-shell pairs)
   long long total = 0;
   int nslots = 0;
   TaskSet<JKTask> jk;
@@ -1170,6 +1196,7 @@ struct LowdinGB300_Batch {
   ~LowdinGB300_Batch() {
     Ds.release(); Dn.release(); Gacc.release(); Jacc.release(); cnt.release(); slots.release();
     Ds32.release(); Dn32.release(); Gacc32.release(); Jacc32.release();
+    gen.release();
     jk.release(); cp.release();
   }
 
@@ -1242,6 +1269,7 @@ struct LowdinGB300_Batch {
     if (!slots.ensure(hs.size())) return false;
     CK(cudaMemcpyAsync(slots.p, hs.data(), hs.size() * sizeof(SpeciesSlot), cudaMemcpyHostToDevice, s));
     if (!jk.upload(s) || !cp.upload(s)) return false;
+    if ((jk.needs_generic() || cp.needs_generic()) && !gen.ensure(generic_scratch_size())) return false;
     CK(cudaStreamSynchronize(s));
     finalized = true;
     return true;
@@ -1257,8 +1285,8 @@ struct LowdinGB300_Batch {
     CK(cudaMemsetAsync(cnt.p, 0, 2 * kNQC * sizeof(unsigned long long), s));
     CK(launch_prepare_batch(slots.p, nslots, total, s));
     const int jk_mixed = precision & 1;
-    if (!LibintInterface::launch_jk_groups(jk, jk_mixed, jk_mixed ? split : 0.0, boys, s)) return false;
-    if (!launch_cp_groups(cp, (precision & 2) ? 2 : 0, split, boys, s)) return false;
+    if (!LibintInterface::launch_jk_groups(jk, jk_mixed, jk_mixed ? split : 0.0, boys, gen.p, s)) return false;
+    if (!launch_cp_groups(cp, (precision & 2) ? 2 : 0, split, boys, gen.p, s)) return false;
     CK(launch_finalize_batch(slots.p, nslots, total, s));
     return true;
   }
@@ -1427,6 +1455,12 @@ int LowdinGB300_twobody_device_noalloc(LibintInterface *lint, const double *dD, 
     }
     ts.nblk[c] = b;
   }
+  if (ts.needs_generic()) {
+    set_error("%s: species with d-shell pair classes of total angular momentum above %d need the generic "
+              "kernels' work arrays (%zu MB); use LowdinGB300_twobody_device",
+              __func__, kTemplatedMaxL, generic_scratch_size() * sizeof(double) >> 20);
+    return -1;
+  }
   if ((int)flat.size() > kNoAllocMaxTasks) {
     set_error("%s: %d tasks exceed the allocation-free limit of %d", __func__, (int)flat.size(), kNoAllocMaxTasks);
     return -1;
@@ -1445,7 +1479,7 @@ int LowdinGB300_twobody_device_noalloc(LibintInterface *lint, const double *dD, 
     set_error("%s: preparation failed", __func__);
     return -1;
   }
-  if (!LibintInterface::launch_jk_groups(ts, precision, split, lint->boys, s)) return -1;
+  if (!LibintInterface::launch_jk_groups(ts, precision, split, lint->boys, nullptr, s)) return -1;
   if (launch_symmetrize(Gacc, Gacc32, lint->d_norma, n, 0.25, dG, s) != cudaSuccess) {
     set_error("%s: symmetrisation failed", __func__);
     return -1;
