@@ -210,6 +210,24 @@ size_t LowdinGB300_noalloc_scratch_bytes(void);
 int LowdinGB300_twobody_device_noalloc(LibintInterface *lint, const double *dD, double *dG, double factor,
                                        int precision, double split, void *stream);
 
+/* Closed-shell MP2 of one electron species with the four-index transform on
+   the device (replaces the DIRECT branch of TransformIntegralsC.f90:472-665,
+   which calls LibintInterface_compute_2body_directIT once per occupied orbital
+   (Libint2Iface.cpp:620-921), and the energy sum of MPFunctions.f90:514-662).
+   Same integral set as that path: significant shell pairs, quartets dropped by
+   the density screening with dD, raw |v| <= 1e-10 dropped, MO integrals with
+   |(ia|jb)| <= 1e-10 read as zero.  dD: device n x n density; dC: device n x n
+   coefficients, row p = orbital p (the layout LibintInterface_compute_2body_directIT
+   reads); eps: host orbital energies (n); orbitals [n_frozen, n_occ) are the
+   active occupied ones, [n_occ, n) the virtual ones.  precision 0: FP64
+   throughout (cuBLAS DGEMM for the dense contractions).  x_budget_gb bounds the
+   per-batch integral array (0: 8 GB).  Writes E_MP2 to *e2 (host) and
+   synchronises `stream`.  Returns 0, or -1 with LowdinGB300_last_error() set. */
+int LowdinGB300_mp2_direct(LibintInterface *lint, const double *dD, const double *dC, const double *eps,
+                           int n_occ, int n_frozen, int precision, double x_budget_gb, double *e2, void *stream);
+/* ket-component columns of the last LowdinGB300_mp2_direct call */
+long long LowdinGB300_mp2_last_columns(void);
+
 /* Number of CUDA kernels this library has launched in the process. */
 long long LowdinGB300_launch_count(void);
 

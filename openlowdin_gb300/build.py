@@ -59,7 +59,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
                 if verbose:
                     print("compiled", os.path.basename(o))
     if jobs or not os.path.exists(LIB):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lcublas"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

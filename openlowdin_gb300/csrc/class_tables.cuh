@@ -28,6 +28,12 @@ constexpr ITFn it_entry() {
   else return nullptr;
 }
 
+template <int B, int K>
+constexpr MXFn mx_entry() {
+  if constexpr (templated_class<B, K>()) return &mp2x_kernel<pc_la(B), pc_lb(B), pc_la(K), pc_lb(K)>;
+  else return nullptr;
+}
+
 #define LGB_ROW6(F, ...) \
   { F<__VA_ARGS__, 0>(), F<__VA_ARGS__, 1>(), F<__VA_ARGS__, 2>(), F<__VA_ARGS__, 3>(), F<__VA_ARGS__, 4>(), F<__VA_ARGS__, 5>() }
 
@@ -43,8 +49,10 @@ constexpr ITFn it_entry() {
   const CPFn kCP64_##B[6] = LGB_ROW6(cp_entry, double, B); \
   const CPFn kCP32_##B[6] = LGB_ROW6(cp_entry, float, B);
 
-#define LGB_IT_TABLE(B)          \
-  extern const ITFn kIT_##B[6];  \
-  const ITFn kIT_##B[6] = LGB_ROW6(it_entry, B);
+#define LGB_IT_TABLE(B)                      \
+  extern const ITFn kIT_##B[6];              \
+  extern const MXFn kMX_##B[6];              \
+  const ITFn kIT_##B[6] = LGB_ROW6(it_entry, B); \
+  const MXFn kMX_##B[6] = LGB_ROW6(mx_entry, B);
 
 }  // namespace lgb

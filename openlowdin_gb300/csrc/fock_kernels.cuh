@@ -377,4 +377,46 @@ __global__ void __launch_bounds__(128) it_kernel(ITParams P) {
   }
 }
 
+// ------------------------------------------------------ MP2 transform input --
+// Lane x of warp y: bra pair tile_y*4 + y, ket pair tile_x*32 + x of the batch.
+template <int LA, int LB, int LC, int LD>
+__global__ void __launch_bounds__(128) mp2x_kernel(MXParams P) {
+  using Q = QClass<LA, LB, LC, LD>;
+  constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND;
+  const int kpos = blockIdx.x * 32 + threadIdx.x;
+  const int bpos = blockIdx.y * kWarpsPerBlock + threadIdx.y;
+  if (bpos >= P.nbra || kpos >= P.nket) return;
+  const int bi = P.bra0 + bpos, ki = P.ket0 + kpos;
+  const PairRec bra = P.pairs[bi];
+  const PairRec ket = P.pairs[ki];
+  if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) return;
+  if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) return;
+  double I[Q::NINT];
+  eri_quartet<double, LA, LB, LC, LD>(bra, P.prims, ket, P.prims, P.boys.f64, P.boys.f32, I);
+  const int col0 = __ldg(P.colbase + ki) - P.col_first;
+  const bool two = bra.sa != bra.sb;
+  const size_t n = P.n, ncol = P.ncol;
+#pragma unroll
+  for (int a = 0; a < NA; ++a)
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+          const double v = I[((a * NB + b) * NC + c) * ND + d];
+          if (!(fabs(v) > P.cut)) continue;
+          const size_t col = col0 + c * ND + d;
+          const size_t i1 = ((bra.fa + a) * ncol + col) * n + bra.fb + b;
+          const size_t i2 = ((bra.fb + b) * ncol + col) * n + bra.fa + a;
+          if (P.X) {
+            P.X[i1] = v;
+            if (two) P.X[i2] = v;
+          } else {
+            P.X32[i1] = (float)v;
+            if (two) P.X32[i2] = (float)v;
+          }
+        }
+}
+
 }  // namespace lgb

@@ -18,6 +18,7 @@ extern const JKFn kJK32_0[6], kJK32_1[6], kJK32_2[6], kJK32_3[6], kJK32_4[6], kJ
 extern const CPFn kCP64_0[6], kCP64_1[6], kCP64_2[6], kCP64_3[6], kCP64_4[6], kCP64_5[6];
 extern const CPFn kCP32_0[6], kCP32_1[6], kCP32_2[6], kCP32_3[6], kCP32_4[6], kCP32_5[6];
 extern const ITFn kIT_0[6], kIT_1[6], kIT_2[6], kIT_3[6], kIT_4[6], kIT_5[6];
+extern const MXFn kMX_0[6], kMX_1[6], kMX_2[6], kMX_3[6], kMX_4[6], kMX_5[6];
 
 namespace {
 
@@ -26,6 +27,7 @@ const JKFn *const kJK32[6] = {kJK32_0, kJK32_1, kJK32_2, kJK32_3, kJK32_4, kJK32
 const CPFn *const kCP64[6] = {kCP64_0, kCP64_1, kCP64_2, kCP64_3, kCP64_4, kCP64_5};
 const CPFn *const kCP32[6] = {kCP32_0, kCP32_1, kCP32_2, kCP32_3, kCP32_4, kCP32_5};
 const ITFn *const kIT[6] = {kIT_0, kIT_1, kIT_2, kIT_3, kIT_4, kIT_5};
+const MXFn *const kMX[6] = {kMX_0, kMX_1, kMX_2, kMX_3, kMX_4, kMX_5};
 
 const dim3 kBlock(32, kWarpsPerBlock);
 
@@ -262,6 +264,47 @@ __global__ void __launch_bounds__(128) it_generic_kernel(ITParams P, GenClass K)
   }
 }
 
+// ------------------------------------------------------ MP2 transform input --
+__global__ void __launch_bounds__(128) mp2x_generic_kernel(MXParams P, GenClass K) {
+  size_t stride;
+  double *scr = thread_scratch(P.scratch, &stride);
+  const int NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld), NA = ncart(K.la);
+  const Strided I{scr + (size_t)(kGenScratch - kGenOut) * stride, stride};
+  const int nbx = (P.nket + 31) / 32, nby = (P.nbra + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  for (int blk = blockIdx.x; blk < nbx * nby; blk += gridDim.x) {
+    const int tx = blk % nbx, ty = blk / nbx;
+    const int kpos = tx * 32 + threadIdx.x;
+    const int bpos = ty * kWarpsPerBlock + threadIdx.y;
+    if (bpos >= P.nbra || kpos >= P.nket) continue;
+    const int bi = P.bra0 + bpos, ki = P.ket0 + kpos;
+    const PairRec bra = P.pairs[bi];
+    const PairRec ket = P.pairs[ki];
+    if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) continue;
+    if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) continue;
+    eri_generic(K.la, K.lb, K.lc, K.ld, bra, P.prims, ket, P.prims, P.boys.f64, scr, stride, 0);
+    const int col0 = __ldg(P.colbase + ki) - P.col_first;
+    const bool two = bra.sa != bra.sb;
+    const size_t n = P.n, ncol = P.ncol;
+    for (int a = 0; a < NA; ++a)
+      for (int b = 0; b < NB; ++b)
+        for (int c = 0; c < NC; ++c)
+          for (int d = 0; d < ND; ++d) {
+            const double v = I[((a * NB + b) * NC + c) * ND + d];
+            if (!(fabs(v) > P.cut)) continue;
+            const size_t col = col0 + c * ND + d;
+            const size_t i1 = ((bra.fa + a) * ncol + col) * n + bra.fb + b;
+            const size_t i2 = ((bra.fb + b) * ncol + col) * n + bra.fa + a;
+            if (P.X) {
+              P.X[i1] = v;
+              if (two) P.X[i2] = v;
+            } else {
+              P.X32[i1] = (float)v;
+              if (two) P.X32[i2] = (float)v;
+            }
+          }
+  }
+}
+
 // ----------------------------------------------------------------- Schwarz --
 __global__ void __launch_bounds__(128) schwarz_generic_kernel(SchwarzParams P, int la, int lb) {
   size_t stride;
@@ -332,6 +375,21 @@ cudaError_t launch_it(int pcb, int pck, const ITParams &p, cudaStream_t s) {
   } else {
     if (!p.scratch) return cudaErrorInvalidValue;
     it_generic_kernel<<<kGenericBlocks, kBlock, 0, s>>>(p, gen_class(pcb, pck));
+  }
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mp2x(int pcb, int pck, const MXParams &p, cudaStream_t s) {
+  if (!class_supported(pcb, pck)) return cudaErrorNotSupported;
+  if (p.nbra <= 0 || p.nket <= 0) return cudaSuccess;
+  const MXFn f = kMX[pcb][pck];
+  if (f) {
+    const dim3 grid((unsigned)((p.nket + 31) / 32), (unsigned)((p.nbra + kWarpsPerBlock - 1) / kWarpsPerBlock));
+    f<<<grid, kBlock, 0, s>>>(p);
+  } else {
+    if (!p.scratch) return cudaErrorInvalidValue;
+    mp2x_generic_kernel<<<kGenericBlocks, kBlock, 0, s>>>(p, gen_class(pcb, pck));
   }
   count_launches(1);
   return cudaGetLastError();

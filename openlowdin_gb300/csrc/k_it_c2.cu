@@ -1,4 +1,4 @@
-// first-quarter kernels of bra pair class 2 (pp) for every ket pair class.
+// first-quarter and MP2 transform-input kernels of bra pair class 2 (pp) for every ket pair class.
 #include "class_tables.cuh"
 
 namespace lgb {

@@ -1,0 +1,122 @@
+// MP2 transform helpers: coefficient preparation, unpacking of the packed
+// ket-pair columns into a full (lam, sig) square, and the pair-energy sum.
+#include "kernels.cuh"
+
+namespace lgb {
+namespace {
+
+__global__ void mp2_coeffs_kernel(const double *__restrict__ C, const double *__restrict__ norma, int n, int n_frozen,
+                                  int n_occ, double *Co, double *Cv, float *Co32, float *Cv32) {
+  const int o = n_occ - n_frozen, v = n - n_occ;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * n) return;
+  const int mu = (int)(t / n), p = (int)(t % n);   // output row mu, orbital column p
+  if (p < n_frozen) return;
+  const double x = C[(size_t)p * n + mu] * norma[mu];
+  if (p < n_occ) {
+    const size_t k = (size_t)mu * o + (p - n_frozen);
+    if (Co) Co[k] = x;
+    if (Co32) Co32[k] = (float)x;
+  } else {
+    const size_t k = (size_t)mu * v + (p - n_occ);
+    if (Cv) Cv[k] = x;
+    if (Cv32) Cv32[k] = (float)x;
+  }
+}
+
+template <typename T>
+__global__ void mp2_unpack_kernel(const T *__restrict__ Y, const unsigned *__restrict__ colpair, long long ncols,
+                                  int n, int v, T *Z) {
+  for (long long col = blockIdx.x; col < ncols; col += gridDim.x) {
+    const unsigned cp = __ldg(colpair + col);
+    const int lam = cp & 0xffff, sig = (cp >> 16) & 0x7fff;
+    const bool two = cp >> 31;
+    const T *y = Y + col * v;
+    T *z1 = Z + ((size_t)lam * n + sig) * v;
+    T *z2 = Z + ((size_t)sig * n + lam) * v;
+    for (int a = threadIdx.x; a < v; a += blockDim.x) {
+      const T x = y[a];
+      z1[a] = x;
+      if (two) z2[a] = x;
+    }
+  }
+}
+
+// 32 x 32 (b, a) tiles of one j; the transposed tile comes through shared memory
+template <typename T>
+__global__ void __launch_bounds__(256) mp2_energy_kernel(const T *__restrict__ M, int v, double ei,
+                                                         const double *__restrict__ eo,
+                                                         const double *__restrict__ ev, double cut, double *e2) {
+  __shared__ T tr[32][33];
+  __shared__ double red[8];
+  const int j = blockIdx.z;
+  const int a0 = blockIdx.x * 32, b0 = blockIdx.y * 32;
+  const T *Mj = M + (size_t)j * v * v;
+  // tr[x][y] = M[j][a0 + y][b0 + x]
+  for (int y = threadIdx.y; y < 32; y += 8) {
+    const int a = a0 + y, b = b0 + threadIdx.x;
+    tr[threadIdx.x][y] = (a < v && b < v) ? Mj[(size_t)a * v + b] : T(0);
+  }
+  __syncthreads();
+  const double eij = ei + eo[j];
+  double acc = 0.0;
+  for (int y = threadIdx.y; y < 32; y += 8) {
+    const int b = b0 + y, a = a0 + threadIdx.x;
+    if (a < v && b < v) {
+      double x = (double)Mj[(size_t)b * v + a];      // (ia|jb)
+      double t = (double)tr[y][threadIdx.x];          // (ib|ja) = M[j][a][b]
+      if (!(fabs(x) > cut)) x = 0.0;
+      if (!(fabs(t) > cut)) t = 0.0;
+      acc += x * (2.0 * x - t) / (eij - ev[a] - ev[b]);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (threadIdx.x == 0) red[threadIdx.y] = acc;
+  __syncthreads();
+  if (threadIdx.y == 0 && threadIdx.x == 0) {
+    double s = 0;
+    for (int k = 0; k < 8; ++k) s += red[k];
+    atomicAdd(e2, s);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_mp2_coeffs(const double *C, const double *norma, int n, int n_frozen, int n_occ, double *Co,
+                              double *Cv, float *Co32, float *Cv32, cudaStream_t s) {
+  const long long tot = (long long)n * n;
+  mp2_coeffs_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(C, norma, n, n_frozen, n_occ, Co, Cv, Co32, Cv32);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_mp2_unpack(const T *Y, const unsigned *colpair, long long ncols, int n, int v, T *Z,
+                              cudaStream_t s) {
+  if (ncols <= 0) return cudaSuccess;
+  const unsigned blocks = (unsigned)(ncols < 152LL * 64 ? ncols : 152LL * 64);
+  mp2_unpack_kernel<T><<<blocks, 128, 0, s>>>(Y, colpair, ncols, n, v, Z);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_mp2_energy(const T *M, int o, int v, double ei, const double *eo, const double *ev, double cut,
+                              double *e2, cudaStream_t s) {
+  if (o <= 0 || v <= 0) return cudaSuccess;
+  const dim3 grid((unsigned)((v + 31) / 32), (unsigned)((v + 31) / 32), (unsigned)o);
+  mp2_energy_kernel<T><<<grid, dim3(32, 8), 0, s>>>(M, v, ei, eo, ev, cut, e2);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_mp2_unpack<double>(const double *, const unsigned *, long long, int, int, double *,
+                                               cudaStream_t);
+template cudaError_t launch_mp2_unpack<float>(const float *, const unsigned *, long long, int, int, float *,
+                                              cudaStream_t);
+template cudaError_t launch_mp2_energy<double>(const double *, int, int, double, const double *, const double *,
+                                               double, double *, cudaStream_t);
+template cudaError_t launch_mp2_energy<float>(const float *, int, int, double, const double *, const double *,
+                                              double, double *, cudaStream_t);
+
+}  // namespace lgb

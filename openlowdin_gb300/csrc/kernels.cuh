@@ -136,6 +136,32 @@ struct SchwarzParams {
   double *scratch;        // generic classes only
 };
 
+// MP2 transform input: raw integrals (mu nu|lam sig) of every significant bra
+// pair and the ket pairs of one column batch, written to
+// X[mu][col][nu] (both bra orientations), col = colbase[ket pair] + c * ND + d
+// for ket components (c, d); quartets that the screening drops and raw values
+// with |v| <= cut stay at the zero the caller cleared X to.
+struct MXParams {
+  const PairRec *pairs;
+  const PrimRec *prims;
+  int bra0, nbra;
+  int ket0, nket;
+  const int *colbase;     // per pair record: first column of its components
+  int col_first;          // first column of the batch
+  const double *Dn;       // density screening (electrons)
+  int nsh;
+  int screen;
+  double eps;
+  double cut;
+  int n;                  // basis functions
+  int ncol;               // columns of the batch
+  double *X;              // FP64 output, or
+  float *X32;             // FP32 output (mixed path), exactly one is non-null
+  BoysTables boys;
+  double *scratch;        // generic classes only
+};
+using MXFn = void (*)(MXParams);
+
 // blocks of one task (grid tile of 32 kets x kWarpsPerBlock bras)
 inline int task_nbx(int nket) { return (nket + 31) / 32; }
 inline int task_nby(int nbra) { return (nbra + kWarpsPerBlock - 1) / kWarpsPerBlock; }
@@ -148,6 +174,23 @@ cudaError_t launch_cp_tasks(int pcb, int pck, bool fp32, const CPTask *dtasks, c
                             cudaStream_t s);
 cudaError_t launch_it(int pcb, int pck, const ITParams &p, cudaStream_t s);
 cudaError_t launch_schwarz(int pc, const SchwarzParams &p, cudaStream_t s);
+cudaError_t launch_mp2x(int pcb, int pck, const MXParams &p, cudaStream_t s);
+// MP2 transform helpers (k_mp2.cu).  Coefficients: C[p][mu] rows are
+// orbitals; Co[mu][i] = norma[mu] C[n_frozen + i][mu] (n x o), Cv[mu][a] =
+// norma[mu] C[n_occ + a][mu] (n x v); the *32 outputs may be null.
+cudaError_t launch_mp2_coeffs(const double *C, const double *norma, int n, int n_frozen, int n_occ, double *Co,
+                              double *Cv, float *Co32, float *Cv32, cudaStream_t s);
+// Z[lam][sig][a] = Y[col][a] for col's (lam, sig) and, when the column's shell
+// pair is off-diagonal, Z[sig][lam][a] too; colpair[col] = lam | sig << 16 |
+// offdiag << 31 (n < 32768)
+template <typename T>
+cudaError_t launch_mp2_unpack(const T *Y, const unsigned *colpair, long long ncols, int n, int v, T *Z,
+                              cudaStream_t s);
+// e2 += sum_{j,a,b} M[j][b][a] (2 M[j][b][a] - M[j][a][b]) / (ei + e_j - e_a - e_b)
+// with |M| <= cut read as zero; M[j][b][a] = (ia|jb)
+template <typename T>
+cudaError_t launch_mp2_energy(const T *M, int o, int v, double ei, const double *eo, const double *ev, double cut,
+                              double *e2, cudaStream_t s);
 bool class_supported(int pcb, int pck);
 inline bool class_generic(int pcb, int pck) { return pc_L(pcb) + pc_L(pck) > kTemplatedMaxL; }
 

@@ -13,6 +13,8 @@
 #include <string>
 #include <vector>
 
+#include <cublas_v2.h>
+
 #include "../../include/lowdin_gb300.h"
 #include "kernels.cuh"
 
@@ -322,6 +324,10 @@ template <typename T>
 struct DevBuf {
   T *p = nullptr;
   size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
   bool ensure(size_t want) {
     if (want <= n && p) return true;
     if (p) cudaFree(p);
@@ -1486,5 +1492,236 @@ int LowdinGB300_twobody_device_noalloc(LibintInterface *lint, const double *dD, 
   }
   return 0;
 }
+
+}  // extern "C"
+
+// ========================================================= MP2 transform
+// LowdinGB300_mp2_direct: closed-shell MP2 of one electron species with the
+// four-index transform on the device.  Same integral set as the reference's
+// DIRECT transform (TransformIntegralsC.f90:472-665 over
+// LibintInterface_compute_2body_directIT, Libint2Iface.cpp:620-921):
+// significant shell pairs only, quartets dropped by the density screening,
+// raw |v| <= 1e-10 dropped; MO integrals with |(ia|jb)| <= 1e-10 read as zero
+// in the energy (only larger ones are stored, :634).  The first quarter is not
+// recomputed per occupied orbital: the integrals of every bra pair against a
+// batch of ket pairs are written once into X[mu][col][nu] and contracted by
+// GEMMs:
+//   T1[i][col][nu] = sum_mu Co[mu][i] X[mu][col][nu]          (o x N^2 P)
+//   Y[i][col][a]   = sum_nu T1[i][col][nu] Cv[nu][a]          (o v N P)
+// then for every i: Z[lam][sig][a] (unpacked Y[i]),
+//   W[j][sig][a]   = sum_lam Co[lam][j] Z[lam][sig][a]        (o^2 v N^2)
+//   M[j][b][a]     = sum_sig Cv[sig][b] W[j][sig][a] = (ia|jb) (o^2 v^2 N)
+// and the pair energies.  A column is one Cartesian component pair (c, d) of
+// a significant ket shell pair (all nc^2 of a diagonal pair).
+namespace {
+
+std::mutex g_blas_mu;
+std::vector<std::pair<int, cublasHandle_t>> g_blas;
+
+bool blas_handle(cublasHandle_t *out) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_blas_mu);
+  for (auto &e : g_blas)
+    if (e.first == dev) {
+      *out = e.second;
+      return true;
+    }
+  cublasHandle_t h = nullptr;
+  if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) {
+    set_error("cublasCreate failed");
+    return false;
+  }
+  g_blas.push_back({dev, h});
+  *out = h;
+  return true;
+}
+
+// row-major C_b = op(A_b) op(B_b), b < batch, with element strides between batches
+bool dgemm_rm(cublasHandle_t h, bool ta, bool tb, int m, int n, int k, const double *A, int lda, long long sA,
+              const double *B, int ldb, long long sB, double *C, int ldc, long long sC, int batch) {
+  const double one = 1.0, zero = 0.0;
+  const cublasStatus_t st =
+      cublasDgemmStridedBatched(h, tb ? CUBLAS_OP_T : CUBLAS_OP_N, ta ? CUBLAS_OP_T : CUBLAS_OP_N, n, m, k, &one, B,
+                                ldb, sB, A, lda, sA, &zero, C, ldc, sC, batch);
+  if (st != CUBLAS_STATUS_SUCCESS) {
+    set_error("cublasDgemmStridedBatched failed (status %d, m=%d n=%d k=%d batch=%d)", (int)st, m, n, k, batch);
+    return false;
+  }
+  return true;
+}
+
+struct MP2Stats {
+  long long ncols = 0;
+  int batches = 0;
+  double x_bytes = 0, y_bytes = 0;
+};
+MP2Stats g_mp2_last;
+
+bool mp2_direct(LibintInterface *L, const double *dD, const double *dC, const double *eps, int n_occ, int n_frozen,
+                int precision, size_t x_budget_bytes, double *e2out, cudaStream_t s) {
+  if (!L->is_electron) {
+    set_error("mp2_direct: closed-shell MP2 is defined here for an electron species");
+    return false;
+  }
+  if (precision != 0) {
+    set_error("mp2_direct: precision %d is not available (0: FP64 GEMMs)", precision);
+    return false;
+  }
+  if (!L->ensure_sig()) return false;
+  const int n = L->nbasis, nsh = L->nshell();
+  if (!(0 <= n_frozen && n_frozen < n_occ && n_occ < n)) {
+    set_error("mp2_direct: need 0 <= n_frozen < n_occ < nbasis (got %d, %d, %d)", n_frozen, n_occ, n);
+    return false;
+  }
+  if (n >= 32768) {
+    set_error("mp2_direct: %d basis functions exceed the column encoding (32767)", n);
+    return false;
+  }
+  const int o = n_occ - n_frozen, v = n - n_occ;
+  cublasHandle_t blas;
+  if (!blas_handle(&blas)) return false;
+  if (cublasSetStream(blas, s) != CUBLAS_STATUS_SUCCESS) {
+    set_error("cublasSetStream failed");
+    return false;
+  }
+  // columns of the significant ket pairs
+  const PairList &P = L->sig;
+  const int npairs = (int)P.h.size();
+  std::vector<int> colbase(npairs);
+  std::vector<unsigned> colpair;
+  for (int k = 0; k < npairs; ++k) {
+    const PairRec &r = P.h[k];
+    colbase[k] = (int)colpair.size();
+    const int nc = ncart(r.la), nd = ncart(r.lb);
+    for (int c = 0; c < nc; ++c)
+      for (int d = 0; d < nd; ++d)
+        colpair.push_back((unsigned)(r.fa + c) | (unsigned)(r.fb + d) << 16 | (r.sa != r.sb ? 1u << 31 : 0u));
+  }
+  const long long ncols = (long long)colpair.size();
+  // column batches: whole ket pairs, X[n][colB][n] within the budget
+  const size_t per_col = (size_t)n * n * sizeof(double) + (size_t)o * n * sizeof(double);
+  long long colB = (long long)(x_budget_bytes / per_col);
+  if (colB < 36) colB = 36;
+  if (colB > ncols) colB = ncols;
+  std::vector<int> bfirst;  // first pair of each batch
+  for (int k = 0; k < npairs;) {
+    bfirst.push_back(k);
+    const int c0 = colbase[k];
+    while (k < npairs && colbase[k] - c0 + ncart(P.h[k].la) * ncart(P.h[k].lb) <= colB) ++k;
+  }
+  bfirst.push_back(npairs);
+  const int nbatch = (int)bfirst.size() - 1;
+  // device memory
+  const size_t ybytes = (size_t)o * ncols * v * sizeof(double);
+  const size_t zbytes = (size_t)n * n * v * sizeof(double);
+  size_t freeb = 0, totb = 0;
+  CK(cudaMemGetInfo(&freeb, &totb));
+  const size_t need = ybytes + zbytes + (size_t)colB * per_col + (size_t)o * n * v * 8 + (size_t)o * v * v * 8;
+  if (need > freeb) {
+    set_error("mp2_direct: needs %.1f GB of device memory, %.1f GB free", need / 1e9, freeb / 1e9);
+    return false;
+  }
+  DevBuf<double> Co, Cv, Eo, Ev, Y, X, T1, Z, W, M, e2;
+  DevBuf<int> dcolbase;
+  DevBuf<unsigned> dcolpair;
+  if (!Co.ensure((size_t)n * o) || !Cv.ensure((size_t)n * v) || !Eo.ensure(o) || !Ev.ensure(v) ||
+      !Y.ensure((size_t)o * ncols * v) || !X.ensure((size_t)n * colB * n) || !T1.ensure((size_t)o * colB * n) ||
+      !Z.ensure((size_t)n * n * v) || !W.ensure((size_t)o * n * v) || !M.ensure((size_t)o * v * v) || !e2.ensure(1) ||
+      !dcolbase.ensure(npairs) || !dcolpair.ensure(ncols))
+    return false;
+  CK(cudaMemcpyAsync(dcolbase.p, colbase.data(), npairs * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dcolpair.p, colpair.data(), ncols * sizeof(unsigned), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(Eo.p, eps + n_frozen, o * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(Ev.p, eps + n_occ, v * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(e2.p, 0, sizeof(double), s));
+  CK(launch_mp2_coeffs(dC, L->d_norma, n, n_frozen, n_occ, Co.p, Cv.p, nullptr, nullptr, s));
+  // shell-block norms of D for the screening
+  if (!L->dDs.ensure((size_t)n * n) || !L->dDn.ensure((size_t)nsh * nsh)) return false;
+  CK(launch_prepare_density(dD, L->d_norma, L->d_shell_of, n, nsh, L->dDs.p, nullptr, L->dDn.p, nullptr, s));
+  double *scr = nullptr;
+  for (int cb = 0; cb < kNumPairClasses && !scr; ++cb)
+    for (int ck = 0; ck < kNumPairClasses; ++ck)
+      if (P.count(cb) && P.count(ck) && class_generic(cb, ck)) {
+        if (!(scr = L->gen_scratch())) return false;
+        break;
+      }
+  MXParams q{};
+  q.pairs = P.d;
+  q.prims = P.dp;
+  q.colbase = dcolbase.p;
+  q.Dn = L->dDn.p;
+  q.nsh = nsh;
+  q.screen = 1;
+  q.eps = DBL_EPSILON;
+  q.cut = 1e-10;
+  q.n = n;
+  q.boys = L->boys;
+  q.scratch = scr;
+  for (int bt = 0; bt < nbatch; ++bt) {
+    const int k0 = bfirst[bt], k1 = bfirst[bt + 1];
+    const int c0 = colbase[k0];
+    const int c1 = k1 < npairs ? colbase[k1] : (int)ncols;
+    const int nb = c1 - c0;
+    q.col_first = c0;
+    q.ncol = nb;
+    q.X = X.p;
+    CK(cudaMemsetAsync(X.p, 0, (size_t)n * nb * n * sizeof(double), s));
+    for (int ck = 0; ck < kNumPairClasses; ++ck) {
+      const int ka = std::max(k0, P.start[ck]), kb = std::min(k1, P.start[ck + 1]);
+      if (ka >= kb) continue;
+      for (int cb = 0; cb < kNumPairClasses; ++cb) {
+        // bra chunks within the grid's y limit
+        for (int b0 = P.start[cb]; b0 < P.start[cb + 1]; b0 += 65535 * kWarpsPerBlock) {
+          q.bra0 = b0;
+          q.nbra = std::min(P.start[cb + 1] - b0, 65535 * kWarpsPerBlock);
+          q.ket0 = ka;
+          q.nket = kb - ka;
+          CK(launch_mp2x(cb, ck, q, s));
+        }
+      }
+    }
+    // T1 (o x nb*n) = Co^T X ; Y[i][c0 + col][a] = T1[i] (nb x n) Cv
+    if (!dgemm_rm(blas, true, false, o, nb * n, n, Co.p, o, 0, X.p, nb * n, 0, T1.p, nb * n, 0, 1)) return false;
+    if (!dgemm_rm(blas, false, false, nb, v, n, T1.p, n, (long long)nb * n, Cv.p, v, 0, Y.p + (size_t)c0 * v, v,
+                  ncols * v, o))
+      return false;
+  }
+  CK(cudaMemsetAsync(Z.p, 0, zbytes, s));
+  std::vector<double> eo(eps + n_frozen, eps + n_occ);
+  for (int i = 0; i < o; ++i) {
+    CK(launch_mp2_unpack<double>(Y.p + (size_t)i * ncols * v, dcolpair.p, ncols, n, v, Z.p, s));
+    if (!dgemm_rm(blas, true, false, o, n * v, n, Co.p, o, 0, Z.p, n * v, 0, W.p, n * v, 0, 1)) return false;
+    if (!dgemm_rm(blas, true, false, v, v, n, Cv.p, v, 0, W.p, v, (long long)n * v, M.p, v, (long long)v * v, o))
+      return false;
+    CK(launch_mp2_energy<double>(M.p, o, v, eo[i], Eo.p, Ev.p, 1e-10, e2.p, s));
+  }
+  double e = 0;
+  CK(cudaMemcpyAsync(&e, e2.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  *e2out = e;
+  g_mp2_last.ncols = ncols;
+  g_mp2_last.batches = nbatch;
+  g_mp2_last.x_bytes = (double)n * colB * n * 8;
+  g_mp2_last.y_bytes = (double)ybytes;
+  return true;  // the buffers are freed on return
+}
+
+}  // namespace
+
+extern "C" {
+
+int LowdinGB300_mp2_direct(LibintInterface *lint, const double *dD, const double *dC, const double *eps, int n_occ,
+                           int n_frozen, int precision, double x_budget_gb, double *e2, void *stream) {
+  if (!check_handle(lint, __func__)) return -1;
+  if (!dD || !dC || !eps || !e2) {
+    set_error("%s: null argument", __func__);
+    return -1;
+  }
+  const size_t budget = x_budget_gb > 0 ? (size_t)(x_budget_gb * 1e9) : (size_t)8e9;
+  return mp2_direct(lint, dD, dC, eps, n_occ, n_frozen, precision, budget, e2, (cudaStream_t)stream) ? 0 : -1;
+}
+
+long long LowdinGB300_mp2_last_columns(void) { return g_mp2_last.ncols; }
 
 }  // extern "C"

@@ -74,6 +74,10 @@ def lib():
         L.LowdinGB300_twobody_device_noalloc.argtypes = [_vp, _vp, _vp, ctypes.c_double, ctypes.c_int,
                                                          ctypes.c_double, _vp]
         L.LowdinGB300_twobody_device_noalloc.restype = ctypes.c_int
+        L.LowdinGB300_mp2_direct.argtypes = [_vp, _vp, _vp, _f64p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_double, ctypes.POINTER(ctypes.c_double), _vp]
+        L.LowdinGB300_mp2_direct.restype = ctypes.c_int
+        L.LowdinGB300_mp2_last_columns.restype = ctypes.c_longlong
         L.LowdinGB300_batch_new.restype = _vp
         L.LowdinGB300_batch_del.argtypes = [_vp]
         L.LowdinGB300_batch_add_system.argtypes = [_vp, ctypes.POINTER(_vp), ctypes.c_int, _f64p, _f64p,
@@ -110,7 +114,7 @@ EXPORTED_SYMBOLS = [
     "LowdinGB300_batch_new", "LowdinGB300_batch_del", "LowdinGB300_batch_add_system",
     "LowdinGB300_batch_finalize", "LowdinGB300_batch_fock", "LowdinGB300_batch_quartets",
     "LowdinGB300_batch_coupling_quartets", "LowdinGB300_noalloc_scratch_bytes",
-    "LowdinGB300_twobody_device_noalloc",
+    "LowdinGB300_twobody_device_noalloc", "LowdinGB300_mp2_direct", "LowdinGB300_mp2_last_columns",
 ]
 
 
@@ -296,6 +300,19 @@ class Libint2Interface:
         out = np.zeros(36, np.int64)
         lib().LowdinGB300_last_class_quartets(self.h, out)
         return out.reshape(6, 6)
+
+    def mp2_direct(self, d_ptr: int, c_ptr: int, eps, n_occ: int, n_frozen: int = 0, precision: int = 0,
+                   x_budget_gb: float = 0.0, stream: int = 0) -> float:
+        """E_MP2 (closed shell) with the transform on the device; d_ptr / c_ptr:
+        device n x n density and coefficients (row p = orbital p)."""
+        e2 = ctypes.c_double(0.0)
+        rc = lib().LowdinGB300_mp2_direct(self.h, d_ptr, c_ptr, np.ascontiguousarray(eps, np.float64),
+                                          int(n_occ), int(n_frozen), int(precision), float(x_budget_gb),
+                                          ctypes.byref(e2), stream)
+        if rc != 0:
+            _check()
+            raise LowdinGB300Error("mp2_direct failed")
+        return e2.value
 
     def pair_class_counts(self, all_pairs: bool) -> np.ndarray:
         out = np.zeros(6, np.int32)

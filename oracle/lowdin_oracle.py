@@ -388,6 +388,34 @@ def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthrea
     return SCFResult(energy, it, converged, P, C, eps, F, H, G, J)
 
 
+MO_CUT = 1e-10
+
+
+def rmp2_direct(b: Basis, D: np.ndarray, C: np.ndarray, eps: np.ndarray, n_occ: int, n_frozen: int = 0) -> float:
+    """Closed-shell MP2 through the reference's DIRECT transform.
+
+    TransformIntegralsC.f90:472-665: for every active occupied i the first
+    quarter A_i[nu][lam][sig] = sum_mu C(mu,i) (mu nu|lam sig) comes from
+    LibintInterface_compute_2body_directIT (density-screened, |raw| > 1e-10),
+    quarters 2-4 are dense sums, and only MO integrals with |(ia|jb)| > 1e-10
+    are stored (:634).  MPFunctions.f90:514-662 then sums, for closed-shell
+    electrons (lambda = 2, q^4 / (2 * particlesFraction) = 1),
+    (ia|jb) [2 (ia|jb) - (ib|ja)] / (e_i + e_j - e_a - e_b), with integrals
+    absent from the file read as zero.  C: columns are orbitals (n x n)."""
+    Co = C[:, n_frozen:n_occ]
+    Cv = C[:, n_occ:]
+    eo, ev = eps[n_frozen:n_occ], eps[n_occ:]
+    Crow = np.ascontiguousarray(C.T)
+    e2 = 0.0
+    for k, i in enumerate(range(n_frozen, n_occ)):
+        A = two_body_directIT(b, True, D, Crow, i)
+        M = np.einsum("nls,na,lj,sb->jab", A, Cv, Co, Cv, optimize=True)   # M[j][a][b] = (ia|jb)
+        M[np.abs(M) <= MO_CUT] = 0.0
+        den = eo[k] + eo[:, None, None] - ev[None, :, None] - ev[None, None, :]
+        e2 += float(np.sum(M * (2.0 * M - M.transpose(0, 2, 1)) / den))
+    return e2
+
+
 def rmp2(eri_ao: np.ndarray, C: np.ndarray, eps: np.ndarray, n_occ: int, n_frozen: int = 0) -> float:
     """Closed-shell MP2 correlation energy, sum (ia|jb)[2(ia|jb)-(ib|ja)]/D."""
     o = C[:, n_frozen:n_occ]

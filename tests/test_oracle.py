@@ -83,6 +83,26 @@ def test_golden_h2o_rhf_and_mp2(oracle, golden):
     assert abs(res.energy + e2 - ref[0]) <= ref[1]
 
 
+def test_direct_mp2_restatement(oracle, golden):
+    """MP2 through the first-quarter direct transform (TransformIntegralsC DIRECT
+    branch) equals the full-tensor MP2 and reproduces the golden MP2 energy;
+    frozen core on the d-shell water."""
+    sysd = GS.h2o_boa(golden)
+    res = oracle.scf(oracle.from_plain(sysd))
+    b = oracle.Basis.from_shells(sysd["species"][0]["shells"])
+    C, eps, D = res.coefficients[0], res.orbital_energies[0], res.densities[0]
+    e_dir = oracle.rmp2_direct(b, D, C, eps, 5)
+    assert abs(e_dir - oracle.rmp2(oracle.eri_full(b), C, eps, 5)) < 1e-12
+    ref = golden["values"]["H2O.BOA.MP2.DIRECT"]["MP2 energy"]
+    assert abs(res.energy + e_dir - ref[0]) <= ref[1]
+    sysd = S.water(d_shell=True)
+    res = oracle.scf(oracle.from_plain(sysd))
+    b = oracle.Basis.from_shells(sysd["species"][0]["shells"])
+    C, eps, D = res.coefficients[0], res.orbital_energies[0], res.densities[0]
+    e_dir = oracle.rmp2_direct(b, D, C, eps, 5, 1)
+    assert abs(e_dir - oracle.rmp2(oracle.eri_full(b), C, eps, 5, 1)) < 1e-12
+
+
 def test_golden_h2o_apmo(oracle, golden):
     """test/H2O.APMO.MP2.py (RHF-APMO total energy, quantum protons)."""
     res = oracle.scf(oracle.from_plain(GS.h2o_apmo(golden)))
