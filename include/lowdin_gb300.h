@@ -228,6 +228,14 @@ int LowdinGB300_mp2_direct(LibintInterface *lint, const double *dD, const double
 /* ket-component columns of the last LowdinGB300_mp2_direct call */
 long long LowdinGB300_mp2_last_columns(void);
 
+/* 3-term split-BF16 GEMM on the tensor cores (no counterpart in the
+   reference; the engine of the mixed-precision MP2 transform): C (M x N) =
+   A (M x K) B^T with B given as N x K, all row-major FP32 device arrays.  Each
+   operand is split into BF16 hi + lo parts, C accumulates hi*hi + hi*lo +
+   lo*hi in FP32 (relative error about 2^-16 per product).  Synchronises
+   `stream`.  Returns 0, or -1 with LowdinGB300_last_error() set. */
+int LowdinGB300_gemm_bf16x3(const float *dA, const float *dB, float *dC, int M, int N, int K, void *stream);
+
 /* Number of CUDA kernels this library has launched in the process. */
 long long LowdinGB300_launch_count(void);
 

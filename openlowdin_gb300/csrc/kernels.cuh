@@ -7,6 +7,8 @@
 // batch -- go into one launch; block b of the flattened grid finds its task by
 // binary search on the tasks' first-block offsets.
 #pragma once
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 
 namespace lgb {
@@ -222,6 +224,30 @@ struct SpeciesSlot {
 };
 cudaError_t launch_prepare_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s);
 cudaError_t launch_finalize_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s);
+
+// 3-term split-BF16 tensor-core GEMM (k_gemm.cu):
+//   C_z[m][n] = sum_k A[z * a_batch_rows + m][k] B[z * b_batch_rows + n][k]
+// with A = A.hi + A.lo, B = B.hi + B.lo (BF16, rows of Kp elements, Kp a
+// multiple of 64, zero beyond the true K); a_rows / b_rows: rows of the whole
+// A / B arrays (loads past them read zeros); FP32 accumulation.
+struct Bf16Split {
+  const __nv_bfloat16 *hi, *lo;
+};
+struct GemmOut {
+  float *C;                   // FP32 output, or (C null)
+  __nv_bfloat16 *Ch, *Cl;     // split BF16 output
+  long long ldc;              // row stride of the output
+  long long c_batch;          // element offset of batch z
+  long long grp_rows, grp_stride, row0;  // output row of m: (m / grp_rows) * grp_stride + m % grp_rows + row0
+                                          // (grp_rows 0: row m + row0)
+};
+cudaError_t launch_gemm_bf16x3(const Bf16Split &A, long long a_rows, const Bf16Split &B, long long b_rows, int Kp,
+                               int M, int N, int batch, int a_batch_rows, int b_batch_rows, const GemmOut &out,
+                               int *derr, cudaStream_t s);
+// src [rows][cols] (row stride lds) -> hi / lo [rows][ldo], x = hi + lo + O(2^-17 x)
+template <typename T>
+cudaError_t launch_split_bf16(const T *src, long long rows, int cols, long long lds, __nv_bfloat16 *hi,
+                              __nv_bfloat16 *lo, long long ldo, cudaStream_t s);
 
 // number of kernels this library has launched (process-wide)
 void count_launches(long long n);

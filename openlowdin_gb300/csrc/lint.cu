@@ -1725,3 +1725,51 @@ int LowdinGB300_mp2_direct(LibintInterface *lint, const double *dD, const double
 long long LowdinGB300_mp2_last_columns(void) { return g_mp2_last.ncols; }
 
 }  // extern "C"
+
+// ============================================== split-BF16 tensor-core GEMM
+extern "C" {
+
+int LowdinGB300_gemm_bf16x3(const float *dA, const float *dB, float *dC, int M, int N, int K, void *stream) {
+  if (!dA || !dB || !dC || M <= 0 || N <= 0 || K <= 0) {
+    set_error("%s: invalid arguments", __func__);
+    return -1;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int Kp = (K + 63) / 64 * 64;
+  DevBuf<__nv_bfloat16> Ah, Al, Bh, Bl;
+  DevBuf<int> err;
+  if (!Ah.ensure((size_t)M * Kp) || !Al.ensure((size_t)M * Kp) || !Bh.ensure((size_t)N * Kp) ||
+      !Bl.ensure((size_t)N * Kp) || !err.ensure(1))
+    return -1;
+  auto fail = [&](const char *what, cudaError_t e) {
+    set_error("%s: %s (%s)", __func__, what, cudaGetErrorString(e));
+    return -1;
+  };
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(Ah.p, 0, (size_t)M * Kp * 2, s)) != cudaSuccess ||
+      (e = cudaMemsetAsync(Al.p, 0, (size_t)M * Kp * 2, s)) != cudaSuccess ||
+      (e = cudaMemsetAsync(Bh.p, 0, (size_t)N * Kp * 2, s)) != cudaSuccess ||
+      (e = cudaMemsetAsync(Bl.p, 0, (size_t)N * Kp * 2, s)) != cudaSuccess ||
+      (e = cudaMemsetAsync(err.p, 0, sizeof(int), s)) != cudaSuccess)
+    return fail("clear", e);
+  if ((e = launch_split_bf16<float>(dA, M, K, K, Ah.p, Al.p, Kp, s)) != cudaSuccess ||
+      (e = launch_split_bf16<float>(dB, N, K, K, Bh.p, Bl.p, Kp, s)) != cudaSuccess)
+    return fail("split", e);
+  GemmOut out{};
+  out.C = dC;
+  out.ldc = N;
+  if ((e = launch_gemm_bf16x3(Bf16Split{Ah.p, Al.p}, M, Bf16Split{Bh.p, Bl.p}, N, Kp, M, N, 1, 0, 0, out, err.p,
+                              s)) != cudaSuccess)
+    return fail("gemm launch", e);
+  int herr = 0;
+  if ((e = cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return fail("gemm", e);
+  if (herr) {
+    set_error("%s: a pipeline wait ran out (code %d)", __func__, herr);
+    return -1;
+  }
+  return 0;
+}
+
+}  // extern "C"
