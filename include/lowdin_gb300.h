@@ -220,21 +220,31 @@ int LowdinGB300_twobody_device_noalloc(LibintInterface *lint, const double *dD, 
    coefficients, row p = orbital p (the layout LibintInterface_compute_2body_directIT
    reads); eps: host orbital energies (n); orbitals [n_frozen, n_occ) are the
    active occupied ones, [n_occ, n) the virtual ones.  precision 0: FP64
-   throughout (cuBLAS DGEMM for the dense contractions).  x_budget_gb bounds the
-   per-batch integral array (0: 8 GB).  Writes E_MP2 to *e2 (host) and
+   throughout (cuBLAS DGEMM for the dense contractions); 1 / 2: the four dense
+   contractions as split-BF16 tensor-core products, operands in 2 / 3 BF16
+   pieces (LowdinGB300_gemm_bf16_split's engine; with 3 pieces the first
+   quarter uses LowdinGB300_gemm_bf16_precise's), integrals and the energy sum
+   in FP64.  x_budget_gb bounds the per-batch integral array (0: 8 GB).  Writes E_MP2 to *e2 (host) and
    synchronises `stream`.  Returns 0, or -1 with LowdinGB300_last_error() set. */
 int LowdinGB300_mp2_direct(LibintInterface *lint, const double *dD, const double *dC, const double *eps,
                            int n_occ, int n_frozen, int precision, double x_budget_gb, double *e2, void *stream);
 /* ket-component columns of the last LowdinGB300_mp2_direct call */
 long long LowdinGB300_mp2_last_columns(void);
 
-/* 3-term split-BF16 GEMM on the tensor cores (no counterpart in the
-   reference; the engine of the mixed-precision MP2 transform): C (M x N) =
-   A (M x K) B^T with B given as N x K, all row-major FP32 device arrays.  Each
-   operand is split into BF16 hi + lo parts, C accumulates hi*hi + hi*lo +
-   lo*hi in FP32 (relative error about 2^-16 per product).  Synchronises
-   `stream`.  Returns 0, or -1 with LowdinGB300_last_error() set. */
-int LowdinGB300_gemm_bf16x3(const float *dA, const float *dB, float *dC, int M, int N, int K, void *stream);
+/* Split-BF16 GEMM on the tensor cores (no counterpart in the reference; the
+   engine of the mixed-precision MP2 transform): C (M x N) = A (M x K) B^T with
+   B given as N x K, all row-major FP32 device arrays.  Each operand is split
+   into `pieces` BF16 parts (2 or 3); C accumulates, in FP32, the products
+   p0q0 + p0q1 + p1q0 (pieces 2, relative error ~2^-16 per product) or those
+   plus p1q1 + p0q2 + p2q0 (pieces 3, ~2^-24).  Synchronises `stream`.
+   Returns 0, or -1 with LowdinGB300_last_error() set. */
+int LowdinGB300_gemm_bf16_split(const float *dA, const float *dB, float *dC, int M, int N, int K, int pieces,
+                                void *stream);
+/* Same product, three pieces per operand, eight products (adds p1q2 + p2q1)
+   and no long FP32 running sums: every 16-wide K slab's main product is
+   rounded once and all partial results are added in FP64.  For contractions
+   with strong cancellation (the MP2 transform's first quarter). */
+int LowdinGB300_gemm_bf16_precise(const float *dA, const float *dB, float *dC, int M, int N, int K, void *stream);
 
 /* Number of CUDA kernels this library has launched in the process. */
 long long LowdinGB300_launch_count(void);

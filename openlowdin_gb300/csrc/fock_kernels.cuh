@@ -413,8 +413,16 @@ __global__ void __launch_bounds__(128) mp2x_kernel(MXParams P) {
             P.X[i1] = v;
             if (two) P.X[i2] = v;
           } else {
-            P.X32[i1] = (float)v;
-            if (two) P.X32[i2] = (float)v;
+            // Xt[col * Kp + nu][mu] and the mirrored bra orientation
+            __nv_bfloat16 pc[kMaxPieces];
+            bf16_pieces(v, P.np, pc);
+            const size_t kp = P.Kp;
+            const size_t j1 = (col * kp + bra.fb + b) * kp + bra.fa + a;
+            const size_t j2 = (col * kp + bra.fa + a) * kp + bra.fb + b;
+            for (int k = 0; k < P.np; ++k) {
+              P.Xp[k][j1] = pc[k];
+              if (two) P.Xp[k][j2] = pc[k];
+            }
           }
         }
 }

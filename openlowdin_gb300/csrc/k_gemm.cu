@@ -1,27 +1,29 @@
-// 3-term split-BF16 GEMM on the fifth-generation tensor cores (tcgen05).
+// Split-BF16 GEMM on the fifth-generation tensor cores (tcgen05).
 //
-// C[m][n] = sum_k A[m][k] B[n][k] with A = Ah + Al and B = Bh + Bl, each term a
-// BF16 array (K contiguous, K padded to a multiple of 64 with zeros):
-//   C ~= Ah Bh + Ah Bl + Al Bh,    FP32 accumulation in tensor memory.
-// The dropped Al Bl term and the two-term representation leave a relative
-// error of about 2^-16 per product.
+// C[m][n] = sum_k A[m][k] B[n][k] with A and B each given as NP BF16 pieces
+// (K contiguous, K padded to a multiple of 64 with zeros):
+//   NP = 2:  C ~= A0 B0 + A0 B1 + A1 B0                        (~2^-16 relative)
+//   NP = 3:  C ~= A0 B0 + A0 B1 + A1 B0 + A1 B1 + A0 B2 + A2 B0 (~2^-24 relative)
+// with FP32 accumulation in tensor memory.
 //
 // One CTA computes one 128 x 128 tile of C with four warps:
-//   warp 0 lane 0  TMA producer: per 64-wide K step, the four operand tiles
-//                  (Ah, Al: 128 x 64; Bh, Bl: 128 x 64, 16 KB each) into a
-//                  3-stage ring of 128-byte-swizzled shared-memory buffers;
-//   warp 1 lane 0  MMA issuer: 3 x 4 tcgen05.mma (M 128, N 128, K 16) per step
-//                  into a 128-column FP32 accumulator in tensor memory; each
-//                  step's tcgen05.commit releases its ring slot;
+//   warp 0 lane 0  TMA producer: per 64-wide K step, the 2 NP operand tiles
+//                  (128 x 64 BF16, 16 KB each) into a ring of 128-byte-swizzled
+//                  shared-memory stages (3 stages for NP = 2, 2 for NP = 3);
+//   warp 1 lane 0  MMA issuer: 4 x (products) tcgen05.mma (M 128, N 128, K 16)
+//                  per step into a 128-column FP32 accumulator in tensor memory;
+//                  each step's tcgen05.commit releases its stage;
 //   all 4 warps    epilogue: tcgen05.ld of their 32 accumulator lanes (rows),
-//                  FP32 or split-BF16 (hi, lo) stores with an optional grouped
-//                  row remap.
+//                  FP32 or split-BF16 stores with optional grouped row / column
+//                  remaps.
 // Every wait on an mbarrier is bounded; a wait that runs out sets *err and the
 // CTA skips to its clean-up (TMEM is always released).
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
+#include <cstring>
 #include <mutex>
 
 #include "kernels.cuh"
@@ -29,21 +31,35 @@
 namespace lgb {
 namespace {
 
-constexpr int kBM = 128, kBN = 128, kBK = 64, kStages = 3;
+constexpr int kBM = 128, kBN = 128, kBK = 64;
 constexpr int kTileBytes = 128 * kBK * 2;               // one operand tile, 16 KB
-constexpr int kStageBytes = 4 * kTileBytes;             // Ah, Al, Bh, Bl
 constexpr int kTmemCols = 128;                          // FP32 accumulator columns (= kBN)
-constexpr int kSmemBytes = kStages * kStageBytes + 1024 /*alignment*/ + 256 /*barriers*/;
 constexpr uint32_t kSpinLimit = 1u << 22;
+
+template <int NP>
+struct GemmCfg {
+  static constexpr int kStages = NP == 2 ? 3 : 2;
+  static constexpr int kStageBytes = 2 * NP * kTileBytes;
+  static constexpr int kSmemBytes = kStages * kStageBytes + 1024 /*alignment*/ + 256 /*barriers*/;
+  static constexpr int kProducts = NP == 2 ? 3 : 6;
+};
+// (A piece, B piece) of product t, in issue order: (0,0) (0,1) (1,0) (1,1) (0,2) (2,0)
+__host__ __device__ constexpr int prod_a(int t) { return t == 2 || t == 3 ? 1 : (t == 5 ? 2 : 0); }
+__host__ __device__ constexpr int prod_b(int t) { return t == 1 || t == 3 ? 1 : (t == 4 ? 2 : 0); }
+
+struct TmapSet {
+  CUtensorMap a[kMaxPieces], b[kMaxPieces];
+};
 
 struct GemmArgs {
   int M, N, Kp;
   int a_batch_rows, b_batch_rows;   // row offset of batch z in the A / B tensors
   long long c_batch;                // element offset of batch z in C
   float *C;                         // FP32 output, or
-  __nv_bfloat16 *Ch, *Cl;           // split output (hi, lo)
+  __nv_bfloat16 *Cp[kMaxPieces];    // split output
   long long ldc;
   long long grp_rows, grp_stride, row0;   // out row = (m / grp_rows) * grp_stride + m % grp_rows + row0
+  long long grp_cols, gcol_stride, col0;  // out column = (n / grp_cols) * gcol_stride + n % grp_cols + col0
   int *err;
 };
 
@@ -131,10 +147,10 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(128, 1)
-    gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
-                       const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl,
-                       GemmArgs g) {
+template <int NP>
+__global__ void __launch_bounds__(128, 1) gemm_split_kernel(const __grid_constant__ TmapSet maps, GemmArgs g) {
+  using Cfg = GemmCfg<NP>;
+  constexpr int kStages = Cfg::kStages, kStageBytes = Cfg::kStageBytes;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + kStages * kStageBytes);
@@ -166,7 +182,7 @@ __global__ void __launch_bounds__(128, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0 && lane == 0) {
-    // producer
+    // producer: stage s holds A pieces 0..NP-1 then B pieces 0..NP-1
     int issued = 0;
     for (int k = 0; k < nk; ++k) {
       const int s = k % kStages;
@@ -178,14 +194,15 @@ __global__ void __launch_bounds__(128, 1)
       uint8_t *st = smem + s * kStageBytes;
       mbar_expect_tx(&full[s], kStageBytes);
       const int ya = z * g.a_batch_rows + m0, yb = z * g.b_batch_rows + n0;
-      tma_load_2d(st, &tAh, &full[s], k * kBK, ya);
-      tma_load_2d(st + kTileBytes, &tAl, &full[s], k * kBK, ya);
-      tma_load_2d(st + 2 * kTileBytes, &tBh, &full[s], k * kBK, yb);
-      tma_load_2d(st + 3 * kTileBytes, &tBl, &full[s], k * kBK, yb);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        tma_load_2d(st + q * kTileBytes, &maps.a[q], &full[s], k * kBK, ya);
+        tma_load_2d(st + (NP + q) * kTileBytes, &maps.b[q], &full[s], k * kBK, yb);
+      }
       ++issued;
     }
     // loads still in flight land before the CTA releases its shared memory:
-    // wait (bounded) for the full barrier of the last issued step of each slot
+    // wait (bounded) for the full barrier of the last issued step of each stage
     for (int k = issued - kStages; k < issued; ++k) {
       if (k < 0) continue;
       mbar_wait(&full[k % kStages], (uint32_t)(k / kStages) & 1u);
@@ -202,14 +219,18 @@ __global__ void __launch_bounds__(128, 1)
       }
       tc_fence_after();
       const uint8_t *st = smem + s * kStageBytes;
-      const uint64_t dAh = smem_desc(st), dAl = smem_desc(st + kTileBytes);
-      const uint64_t dBh = smem_desc(st + 2 * kTileBytes), dBl = smem_desc(st + 3 * kTileBytes);
+      uint64_t da[NP], db[NP];
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        da[q] = smem_desc(st + q * kTileBytes);
+        db[q] = smem_desc(st + (NP + q) * kTileBytes);
+      }
 #pragma unroll
       for (int kk = 0; kk < kBK / 16; ++kk) {
         const uint64_t off = (uint64_t)(kk * 16 * 2) >> 4;   // K step of 16 BF16 = 32 bytes
-        umma_bf16(tmem, dAh + off, dBh + off, idesc, (k | kk) != 0);
-        umma_bf16(tmem, dAh + off, dBl + off, idesc, 1u);
-        umma_bf16(tmem, dAl + off, dBh + off, idesc, 1u);
+#pragma unroll
+        for (int t = 0; t < Cfg::kProducts; ++t)
+          umma_bf16(tmem, da[prod_a(t)] + off, db[prod_b(t)] + off, idesc, (k | kk | t) != 0);
       }
       umma_commit(&empty[s]);
     }
@@ -233,22 +254,22 @@ __global__ void __launch_bounds__(128, 1)
     if (!ready || row >= g.M) continue;
     const int ncol = min(32, g.N - (n0 + c0));
     if (ncol <= 0) continue;
-    if (g.C) {
-      float *dst = g.C + cbase + n0 + c0;
 #pragma unroll
-      for (int j = 0; j < 32; ++j)
-        if (j < ncol) dst[j] = __uint_as_float(r[j]);
-    } else {
-      __nv_bfloat16 *dh = g.Ch + cbase + n0 + c0, *dl = g.Cl + cbase + n0 + c0;
+    for (int j = 0; j < 32; ++j)
+      if (j < ncol) {
+        const long long nn = n0 + c0 + j;
+        const long long oc =
+            cbase + (g.grp_cols ? (nn / g.grp_cols) * g.gcol_stride + nn % g.grp_cols + g.col0 : nn);
+        const float x = __uint_as_float(r[j]);
+        if (g.C) {
+          g.C[oc] = x;
+        } else {
+          __nv_bfloat16 pc[kMaxPieces];
+          bf16_pieces(x, NP, pc);
 #pragma unroll
-      for (int j = 0; j < 32; ++j)
-        if (j < ncol) {
-          const float x = __uint_as_float(r[j]);
-          const __nv_bfloat16 h = __float2bfloat16_rn(x);
-          dh[j] = h;
-          dl[j] = __float2bfloat16_rn(x - __bfloat162float(h));
+          for (int q = 0; q < NP; ++q) g.Cp[q][oc] = pc[q];
         }
-    }
+      }
   }
   tc_fence_before();
   __syncthreads();
@@ -256,26 +277,221 @@ __global__ void __launch_bounds__(128, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
 }
 
-// FP32 / FP64 row-major [rows][cols] -> BF16 hi / lo [rows][ldo] (columns
+// ------------------------------------------------------------ precise mode --
+// Three pieces per operand, eight products (p0q0 + p0q1 + p1q0 + p1q1 + p0q2
+// + p2q0 + p1q2 + p2q1), and no long FP32 accumulation: the p0q0 product of
+// every 16-wide K slab goes to a fresh tensor-memory accumulator, the seven
+// smaller products of a 64-wide K step to one more, and four accumulator warps
+// add them into FP64 registers after every step.  The tensor cores then round
+// each slab's main sum once (toward zero, to FP32) instead of carrying a
+// 640-term FP32 running sum, which is what limits a plain FP32-accumulated
+// product on inputs with strong cancellation.
+// Warps: 0 TMA producer, 1 MMA issuer, 2-5 accumulators / epilogue (warp w
+// reads tensor-memory lanes 32 (w % 4) .. + 31).  Tiles 128 x 32; persistent
+// CTAs walk the N tiles; accumulator buffers are double-buffered across steps.
+constexpr int kPBN = 32, kPStages = 3;
+constexpr int kPTileA = 128 * kBK * 2, kPTileB = kPBN * kBK * 2;
+constexpr int kPStageBytes = 3 * kPTileA + 3 * kPTileB;
+constexpr int kPBufCols = 5 * kPBN;                 // 4 slab accumulators + 1 correction accumulator
+constexpr int kPTmemCols = 512;
+constexpr int kPSmemBytes = kPStages * kPStageBytes + 1024 + 256;
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__global__ void __launch_bounds__(192, 1) gemm_precise_kernel(const __grid_constant__ TmapSet maps, GemmArgs g) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + kPStages * kPStageBytes);
+  uint64_t *empty = full + kPStages;
+  uint64_t *acc_full = empty + kPStages;
+  uint64_t *acc_free = acc_full + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_free + 2);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * kBM, z = blockIdx.z;
+  const int nk = g.Kp / kBK;
+  const int ntiles = (g.N + kPBN - 1) / kPBN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kPStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_free[b], 4);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    __syncwarp();
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kPTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      long long gs = 0, issued = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const int n0 = t * kPBN;
+        for (int k = 0; k < nk; ++k, ++gs) {
+          const int s = (int)(gs % kPStages);
+          if (!mbar_wait(&empty[s], (uint32_t)((gs / kPStages) & 1) ^ 1u)) {
+            atomicExch(g.err, 11);
+            ok = false;
+            break;
+          }
+          uint8_t *st = smem + s * kPStageBytes;
+          mbar_expect_tx(&full[s], kPStageBytes);
+          const int ya = z * g.a_batch_rows + m0, yb = z * g.b_batch_rows + n0;
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            tma_load_2d(st + q * kPTileA, &maps.a[q], &full[s], k * kBK, ya);
+            tma_load_2d(st + 3 * kPTileA + q * kPTileB, &maps.b[q], &full[s], k * kBK, yb);
+          }
+          ++issued;
+        }
+      }
+      for (long long k = issued - kPStages; k < issued; ++k) {
+        if (k < 0) continue;
+        mbar_wait(&full[k % kPStages], (uint32_t)((k / kPStages) & 1));
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = make_idesc(kBM, kPBN);
+      long long gs = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        for (int k = 0; k < nk; ++k, ++gs) {
+          const int s = (int)(gs % kPStages), b = (int)(gs & 1);
+          if (gs >= 2 && !mbar_wait(&acc_free[b], (uint32_t)(((gs - 2) >> 1) & 1))) {
+            atomicExch(g.err, 12);
+            ok = false;
+            break;
+          }
+          if (!mbar_wait(&full[s], (uint32_t)((gs / kPStages) & 1))) {
+            atomicExch(g.err, 13);
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint8_t *st = smem + s * kPStageBytes;
+          uint64_t da[3], db[3];
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            da[q] = smem_desc(st + q * kPTileA);
+            db[q] = smem_desc(st + 3 * kPTileA + q * kPTileB);
+          }
+          const uint32_t tb = tmem + (uint32_t)(b * kPBufCols);
+#pragma unroll
+          for (int kk = 0; kk < kBK / 16; ++kk) {
+            const uint64_t off = (uint64_t)(kk * 16 * 2) >> 4;
+            umma_bf16(tb + (uint32_t)(kk * kPBN), da[0] + off, db[0] + off, idesc, 0u);   // fresh per slab
+#pragma unroll
+            for (int p = 1; p < 8; ++p) {
+              const int qa = p == 2 || p == 3 || p == 7 ? 1 : (p == 5 || p == 6 ? 2 : 0);
+              const int qb = p == 1 || p == 3 || p == 6 ? 1 : (p == 4 || p == 7 ? 2 : 0);
+              umma_bf16(tb + (uint32_t)(4 * kPBN), da[qa] + off, db[qb] + off, idesc, (kk | (p - 1)) != 0);
+            }
+          }
+          umma_commit(&empty[s]);
+          umma_commit(&acc_full[b]);
+        }
+      }
+    }
+  } else {
+    // accumulator warps
+    const int wq = warp & 3;
+    const int row = m0 + wq * 32 + lane;
+    long long orow = 0;
+    if (row < g.M) orow = (long long)(row / g.grp_rows) * g.grp_stride + row % g.grp_rows + g.row0;
+    const long long cbase = (long long)z * g.c_batch + orow * g.ldc;
+    long long gs = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      const int n0 = t * kPBN;
+      double acc[kPBN];
+#pragma unroll
+      for (int j = 0; j < kPBN; ++j) acc[j] = 0.0;
+      for (int k = 0; k < nk; ++k, ++gs) {
+        const int b = (int)(gs & 1);
+        const bool got = mbar_wait(&acc_full[b], (uint32_t)((gs >> 1) & 1));
+        if (!got) {
+          if (lane == 0) atomicExch(g.err, 14);
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        __syncwarp();
+        const uint32_t ta = tmem + ((uint32_t)(wq * 32) << 16) + (uint32_t)(b * kPBufCols);
+#pragma unroll 1
+        for (int c = 0; c < 5; ++c) {
+          uint32_t r[32];
+          tmem_ld32(ta + (uint32_t)(c * kPBN), r);
+#pragma unroll
+          for (int j = 0; j < kPBN; ++j) acc[j] += (double)__uint_as_float(r[j]);
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_free[b]);
+      }
+      if (!ok || row >= g.M) continue;
+      const int ncol = min(kPBN, g.N - n0);
+#pragma unroll
+      for (int j = 0; j < kPBN; ++j)
+        if (j < ncol) {
+          const long long nn = n0 + j;
+          const long long oc =
+              cbase + (g.grp_cols ? (nn / g.grp_cols) * g.gcol_stride + nn % g.grp_cols + g.col0 : nn);
+          if (g.C) {
+            g.C[oc] = (float)acc[j];
+          } else {
+            __nv_bfloat16 pc[kMaxPieces];
+            bf16_pieces(acc[j], 3, pc);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) g.Cp[q][oc] = pc[q];
+          }
+        }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    __syncwarp();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kPTmemCols) : "memory");
+  }
+}
+
+// FP32 / FP64 row-major [rows][cols] -> np BF16 pieces [rows][ldo] (columns
 // >= cols are left as they are: the caller clears the padding once)
 template <typename T>
-__global__ void split_bf16_kernel(const T *__restrict__ src, long long rows, int cols, long long lds,
-                                  __nv_bfloat16 *hi, __nv_bfloat16 *lo, long long ldo) {
+__global__ void split_bf16_kernel(const T *__restrict__ src, long long rows, int cols, long long lds, int np,
+                                  __nv_bfloat16 *o0, __nv_bfloat16 *o1, __nv_bfloat16 *o2, long long ldo) {
   const long long tot = rows * cols;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
     const long long r = t / cols;
     const int c = (int)(t % cols);
-    const double x = (double)src[r * lds + c];
-    const __nv_bfloat16 h = __float2bfloat16_rn((float)x);
-    hi[r * ldo + c] = h;
-    lo[r * ldo + c] = __float2bfloat16_rn((float)(x - (double)__bfloat162float(h)));
+    __nv_bfloat16 pc[kMaxPieces] = {};
+    bf16_pieces((double)src[r * lds + c], np, pc);
+    o0[r * ldo + c] = pc[0];
+    o1[r * ldo + c] = pc[1];
+    if (np > 2) o2[r * ldo + c] = pc[2];
   }
 }
 
 std::once_flag g_encode_once;
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
-bool tensor_map(CUtensorMap *m, const void *base, long long rows, int Kp) {
+bool tensor_map(CUtensorMap *m, const void *base, long long rows, int Kp, int box_rows = 128) {
   std::call_once(g_encode_once, [] {
     cudaDriverEntryPointQueryResult q;
     void *fn = nullptr;
@@ -287,35 +503,47 @@ bool tensor_map(CUtensorMap *m, const void *base, long long rows, int Kp) {
   if (!g_encode) return false;
   const cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
-  const cuuint32_t box[2] = {(cuuint32_t)kBK, 128u};
+  const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
   const cuuint32_t estr[2] = {1u, 1u};
   return g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-}  // namespace
-
-cudaError_t launch_gemm_bf16x3(const Bf16Split &A, long long a_rows, const Bf16Split &B, long long b_rows, int Kp,
-                               int M, int N, int batch, int a_batch_rows, int b_batch_rows, const GemmOut &out,
-                               int *derr, cudaStream_t s) {
-  if (Kp <= 0 || Kp % kBK || M <= 0 || N <= 0 || batch <= 0) return cudaErrorInvalidValue;
-  if ((reinterpret_cast<uintptr_t>(A.hi) | reinterpret_cast<uintptr_t>(A.lo) | reinterpret_cast<uintptr_t>(B.hi) |
-       reinterpret_cast<uintptr_t>(B.lo)) & 15u)
-    return cudaErrorMisalignedAddress;
-  const long long nt = (N + kBN - 1) / kBN, mt = (M + kBM - 1) / kBM;
-  if (nt > 0x7fffffffLL || mt > 65535 || batch > 65535) return cudaErrorInvalidConfiguration;
-  CUtensorMap tAh, tAl, tBh, tBl;
-  if (!tensor_map(&tAh, A.hi, a_rows, Kp) || !tensor_map(&tAl, A.lo, a_rows, Kp) ||
-      !tensor_map(&tBh, B.hi, b_rows, Kp) || !tensor_map(&tBl, B.lo, b_rows, Kp))
-    return cudaErrorInvalidValue;
+template <int NP>
+cudaError_t launch_gemm_np(const TmapSet &maps, const GemmArgs &g, unsigned nt, unsigned mt, unsigned batch,
+                           cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    const cudaError_t e = cudaFuncSetAttribute(gemm_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               kSmemBytes);
+    const cudaError_t e = cudaFuncSetAttribute(gemm_split_kernel<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               GemmCfg<NP>::kSmemBytes);
     if (e != cudaSuccess) return e;
     attr = true;
   }
+  gemm_split_kernel<NP><<<dim3(nt, mt, batch), 128, GemmCfg<NP>::kSmemBytes, s>>>(maps, g);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_gemm_split(const Bf16Split &A, long long a_rows, const Bf16Split &B, long long b_rows, int Kp,
+                              int M, int N, int batch, int a_batch_rows, int b_batch_rows, int np,
+                              const GemmOut &out, int *derr, cudaStream_t s) {
+  if (Kp <= 0 || Kp % kBK || M <= 0 || N <= 0 || batch <= 0 || np < 2 || np > kMaxPieces)
+    return cudaErrorInvalidValue;
+  uintptr_t bits = 0;
+  for (int q = 0; q < np; ++q) {
+    if (!A.p[q] || !B.p[q] || (!out.C && !out.Cp[q])) return cudaErrorInvalidValue;
+    bits |= reinterpret_cast<uintptr_t>(A.p[q]) | reinterpret_cast<uintptr_t>(B.p[q]);
+  }
+  if (bits & 15u) return cudaErrorMisalignedAddress;
+  const long long nt = (N + kBN - 1) / kBN, mt = (M + kBM - 1) / kBM;
+  if (nt > 0x7fffffffLL || mt > 65535 || batch > 65535) return cudaErrorInvalidConfiguration;
+  TmapSet maps;
+  memset(&maps, 0, sizeof(maps));
+  for (int q = 0; q < np; ++q)
+    if (!tensor_map(&maps.a[q], A.p[q], a_rows, Kp) || !tensor_map(&maps.b[q], B.p[q], b_rows, Kp))
+      return cudaErrorInvalidValue;
   GemmArgs g{};
   g.M = M;
   g.N = N;
@@ -324,33 +552,86 @@ cudaError_t launch_gemm_bf16x3(const Bf16Split &A, long long a_rows, const Bf16S
   g.b_batch_rows = b_batch_rows;
   g.c_batch = out.c_batch;
   g.C = out.C;
-  g.Ch = out.Ch;
-  g.Cl = out.Cl;
+  for (int q = 0; q < kMaxPieces; ++q) g.Cp[q] = out.Cp[q];
   g.ldc = out.ldc;
   g.grp_rows = out.grp_rows > 0 ? out.grp_rows : (long long)M;
   g.grp_stride = out.grp_rows > 0 ? out.grp_stride : 0;
   g.row0 = out.row0;
+  g.grp_cols = out.grp_cols;
+  g.gcol_stride = out.gcol_stride;
+  g.col0 = out.col0;
   g.err = derr;
-  gemm_bf16x3_kernel<<<dim3((unsigned)nt, (unsigned)mt, (unsigned)batch), 128, kSmemBytes, s>>>(tAh, tAl, tBh, tBl,
-                                                                                             g);
+  const cudaError_t e = np == 2 ? launch_gemm_np<2>(maps, g, (unsigned)nt, (unsigned)mt, (unsigned)batch, s)
+                                : launch_gemm_np<3>(maps, g, (unsigned)nt, (unsigned)mt, (unsigned)batch, s);
+  count_launches(1);
+  return e;
+}
+
+cudaError_t launch_gemm_precise(const Bf16Split &A, long long a_rows, const Bf16Split &B, long long b_rows, int Kp,
+                                int M, int N, int batch, int a_batch_rows, int b_batch_rows, const GemmOut &out,
+                                int *derr, cudaStream_t s) {
+  if (Kp <= 0 || Kp % kBK || M <= 0 || N <= 0 || batch <= 0) return cudaErrorInvalidValue;
+  uintptr_t bits = 0;
+  for (int q = 0; q < 3; ++q) {
+    if (!A.p[q] || !B.p[q] || (!out.C && !out.Cp[q])) return cudaErrorInvalidValue;
+    bits |= reinterpret_cast<uintptr_t>(A.p[q]) | reinterpret_cast<uintptr_t>(B.p[q]);
+  }
+  if (bits & 15u) return cudaErrorMisalignedAddress;
+  const long long nt = (N + kPBN - 1) / kPBN, mt = (M + kBM - 1) / kBM;
+  if (mt > 65535 || batch > 65535) return cudaErrorInvalidConfiguration;
+  TmapSet maps;
+  memset(&maps, 0, sizeof(maps));
+  for (int q = 0; q < 3; ++q)
+    if (!tensor_map(&maps.a[q], A.p[q], a_rows, Kp, 128) || !tensor_map(&maps.b[q], B.p[q], b_rows, Kp, kPBN))
+      return cudaErrorInvalidValue;
+  GemmArgs g{};
+  g.M = M;
+  g.N = N;
+  g.Kp = Kp;
+  g.a_batch_rows = a_batch_rows;
+  g.b_batch_rows = b_batch_rows;
+  g.c_batch = out.c_batch;
+  g.C = out.C;
+  for (int q = 0; q < kMaxPieces; ++q) g.Cp[q] = out.Cp[q];
+  g.ldc = out.ldc;
+  g.grp_rows = out.grp_rows > 0 ? out.grp_rows : (long long)M;
+  g.grp_stride = out.grp_rows > 0 ? out.grp_stride : 0;
+  g.row0 = out.row0;
+  g.grp_cols = out.grp_cols;
+  g.gcol_stride = out.gcol_stride;
+  g.col0 = out.col0;
+  g.err = derr;
+  static bool attr = false;
+  if (!attr) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(gemm_precise_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  // persistent CTAs: one wave over the SMs (one CTA fits an SM), split over (M tiles x batches)
+  long long per = (152LL + mt * batch - 1) / (mt * batch);
+  const unsigned gx = (unsigned)std::max<long long>(1, std::min<long long>(nt, per));
+  gemm_precise_kernel<<<dim3(gx, (unsigned)mt, (unsigned)batch), 192, kPSmemBytes, s>>>(maps, g);
   count_launches(1);
   return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t launch_split_bf16(const T *src, long long rows, int cols, long long lds, __nv_bfloat16 *hi,
-                              __nv_bfloat16 *lo, long long ldo, cudaStream_t s) {
+cudaError_t launch_split_bf16(const T *src, long long rows, int cols, long long lds, int np, __nv_bfloat16 *const *out,
+                              long long ldo, cudaStream_t s) {
   const long long tot = rows * cols;
   if (tot <= 0) return cudaSuccess;
+  if (np < 2 || np > kMaxPieces) return cudaErrorInvalidValue;
   const long long blocks = std::min<long long>((tot + 255) / 256, 152LL * 32);
-  split_bf16_kernel<T><<<(unsigned)blocks, 256, 0, s>>>(src, rows, cols, lds, hi, lo, ldo);
+  split_bf16_kernel<T><<<(unsigned)blocks, 256, 0, s>>>(src, rows, cols, lds, np, out[0], out[1],
+                                                        np > 2 ? out[2] : nullptr, ldo);
   count_launches(1);
   return cudaGetLastError();
 }
 
-template cudaError_t launch_split_bf16<float>(const float *, long long, int, long long, __nv_bfloat16 *,
-                                              __nv_bfloat16 *, long long, cudaStream_t);
-template cudaError_t launch_split_bf16<double>(const double *, long long, int, long long, __nv_bfloat16 *,
-                                               __nv_bfloat16 *, long long, cudaStream_t);
+template cudaError_t launch_split_bf16<float>(const float *, long long, int, long long, int, __nv_bfloat16 *const *,
+                                              long long, cudaStream_t);
+template cudaError_t launch_split_bf16<double>(const double *, long long, int, long long, int,
+                                               __nv_bfloat16 *const *, long long, cudaStream_t);
 
 }  // namespace lgb

@@ -80,7 +80,90 @@ __global__ void __launch_bounds__(256) mp2_energy_kernel(const T *__restrict__ M
   }
 }
 
+__global__ void mp2_coeffs_bf16_kernel(const double *__restrict__ C, const double *__restrict__ norma, int n,
+                                       int n_frozen, int n_occ, int Kp, int np, __nv_bfloat16 *CoT0,
+                                       __nv_bfloat16 *CoT1, __nv_bfloat16 *CoT2, __nv_bfloat16 *CvT0,
+                                       __nv_bfloat16 *CvT1, __nv_bfloat16 *CvT2) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * n) return;
+  const int p = (int)(t / n), mu = (int)(t % n);   // orbital row p, function mu
+  if (p < n_frozen) return;
+  __nv_bfloat16 pc[kMaxPieces];
+  bf16_pieces(C[t] * norma[mu], np, pc);
+  const bool occ = p < n_occ;
+  const size_t k = (size_t)(occ ? p - n_frozen : p - n_occ) * Kp + mu;
+  __nv_bfloat16 *dst[kMaxPieces] = {occ ? CoT0 : CvT0, occ ? CoT1 : CvT1, occ ? CoT2 : CvT2};
+  for (int q = 0; q < np; ++q) dst[q][k] = pc[q];
+}
+
+// block (sig chunk of 16 rows, a): gather the chunk's entries into a shared
+// FP32 tile [16][Kp], then write its rows as split BF16 with 16-byte stores
+constexpr int kUnpackRows = 16;
+__global__ void __launch_bounds__(256) mp2_unpack_csr_kernel(const float *__restrict__ Yp, long long ystride,
+                                                             const int *__restrict__ rowptr,
+                                                             const int2 *__restrict__ ent, int n, int Kp, int np,
+                                                             __nv_bfloat16 *Z0, __nv_bfloat16 *Z1,
+                                                             __nv_bfloat16 *Z2) {
+  extern __shared__ float tile[];
+  const int s0 = blockIdx.x * kUnpackRows, a = blockIdx.y;
+  const int s1 = min(s0 + kUnpackRows, n);
+  for (int k = threadIdx.x; k < kUnpackRows * Kp; k += blockDim.x) tile[k] = 0.f;
+  __syncthreads();
+  const float *y = Yp + (size_t)a * ystride;
+  for (int e = __ldg(rowptr + s0) + threadIdx.x; e < __ldg(rowptr + s1); e += blockDim.x) {
+    const int2 t = __ldg(ent + e);
+    const int lam = t.x & 0xffff, sig = t.x >> 16;
+    tile[(sig - s0) * Kp + lam] = __ldg(y + t.y);
+  }
+  __syncthreads();
+  __nv_bfloat16 *Z[kMaxPieces] = {Z0, Z1, Z2};
+  const int nvec = (s1 - s0) * Kp / 8;   // Kp is a multiple of 64
+  for (int k = threadIdx.x; k < nvec; k += blockDim.x) {
+    const int r = (k * 8) / Kp, c = (k * 8) % Kp;
+    const float *src = tile + r * Kp + c;
+    __align__(16) __nv_bfloat16 pv[kMaxPieces][8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      __nv_bfloat16 pc[kMaxPieces] = {};
+      bf16_pieces(src[q], np, pc);
+#pragma unroll
+      for (int j = 0; j < kMaxPieces; ++j) pv[j][q] = pc[j];
+    }
+    const size_t o = ((size_t)a * Kp + s0 + r) * Kp + c;
+    for (int j = 0; j < np; ++j) *reinterpret_cast<uint4 *>(Z[j] + o) = *reinterpret_cast<const uint4 *>(pv[j]);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_mp2_coeffs_bf16(const double *C, const double *norma, int n, int n_frozen, int n_occ, int Kp,
+                                   int np, __nv_bfloat16 *const *CoT, __nv_bfloat16 *const *CvT, cudaStream_t s) {
+  if (np < 2 || np > kMaxPieces) return cudaErrorInvalidValue;
+  const long long tot = (long long)n * n;
+  mp2_coeffs_bf16_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(
+      C, norma, n, n_frozen, n_occ, Kp, np, CoT[0], CoT[1], np > 2 ? CoT[2] : nullptr, CvT[0], CvT[1],
+      np > 2 ? CvT[2] : nullptr);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mp2_unpack_csr(const float *Yp, long long ystride, const int *rowptr, const int2 *ent, int n,
+                                  int Kp, int v, int np, __nv_bfloat16 *const *Z, cudaStream_t s) {
+  if (Kp % 64 || v <= 0 || v > 65535 || np < 2 || np > kMaxPieces) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)kUnpackRows * Kp * sizeof(float);
+  static int attr_kp = 0;
+  if (smem > 48 * 1024 && Kp > attr_kp) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(mp2_unpack_csr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_kp = Kp;
+  }
+  const dim3 grid((unsigned)((n + kUnpackRows - 1) / kUnpackRows), (unsigned)v);
+  mp2_unpack_csr_kernel<<<grid, 256, smem, s>>>(Yp, ystride, rowptr, ent, n, Kp, np, Z[0], Z[1],
+                                                 np > 2 ? Z[2] : nullptr);
+  count_launches(1);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_mp2_coeffs(const double *C, const double *norma, int n, int n_frozen, int n_occ, double *Co,
                               double *Cv, float *Co32, float *Cv32, cudaStream_t s) {

@@ -157,8 +157,10 @@ struct MXParams {
   double cut;
   int n;                  // basis functions
   int ncol;               // columns of the batch
-  double *X;              // FP64 output, or
-  float *X32;             // FP32 output (mixed path), exactly one is non-null
+  double *X;              // FP64 output X[mu][col][nu], or (X null)
+  __nv_bfloat16 *Xp[3];   // split-BF16 output Xt[col * Kp + nu][mu] (K-major for the tensor cores)
+  int np;                 // pieces of the split output
+  int Kp;                 // padded function count of the split layout
   BoysTables boys;
   double *scratch;        // generic classes only
 };
@@ -190,6 +192,15 @@ cudaError_t launch_mp2_unpack(const T *Y, const unsigned *colpair, long long nco
                               cudaStream_t s);
 // e2 += sum_{j,a,b} M[j][b][a] (2 M[j][b][a] - M[j][a][b]) / (ei + e_j - e_a - e_b)
 // with |M| <= cut read as zero; M[j][b][a] = (ia|jb)
+// split-BF16 coefficients (np pieces), K-major and padded to Kp (padding
+// cleared by the caller): CoT[i][mu] = norma[mu] C[n_frozen + i][mu], CvT[a][mu] = norma[mu] C[n_occ + a][mu]
+cudaError_t launch_mp2_coeffs_bf16(const double *C, const double *norma, int n, int n_frozen, int n_occ, int Kp,
+                                   int np, __nv_bfloat16 *const *CoT, __nv_bfloat16 *const *CvT, cudaStream_t s);
+// Zt[a][sig][lam] (split BF16, rows of Kp) = Y'[a][lam sig column] for every
+// entry of the sig-row lists: rowptr[sig] .. rowptr[sig+1] hold (lam | sig << 16, col);
+// Yp points at Y'[0][i][0], a-rows ystride apart
+cudaError_t launch_mp2_unpack_csr(const float *Yp, long long ystride, const int *rowptr, const int2 *ent, int n,
+                                  int Kp, int v, int np, __nv_bfloat16 *const *Z, cudaStream_t s);
 template <typename T>
 cudaError_t launch_mp2_energy(const T *M, int o, int v, double ei, const double *eo, const double *ev, double cut,
                               double *e2, cudaStream_t s);
@@ -225,29 +236,54 @@ struct SpeciesSlot {
 cudaError_t launch_prepare_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s);
 cudaError_t launch_finalize_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s);
 
-// 3-term split-BF16 tensor-core GEMM (k_gemm.cu):
-//   C_z[m][n] = sum_k A[z * a_batch_rows + m][k] B[z * b_batch_rows + n][k]
-// with A = A.hi + A.lo, B = B.hi + B.lo (BF16, rows of Kp elements, Kp a
-// multiple of 64, zero beyond the true K); a_rows / b_rows: rows of the whole
-// A / B arrays (loads past them read zeros); FP32 accumulation.
+// Split-BF16 operands: x ~= p[0] + p[1] (+ p[2]), each piece the BF16
+// rounding of what the previous pieces leave.  Two pieces keep ~16 bits of x,
+// three ~24 bits.
+constexpr int kMaxPieces = 3;
+template <typename T>
+__device__ __forceinline__ void bf16_pieces(T x, int np, __nv_bfloat16 *p) {
+#pragma unroll
+  for (int k = 0; k < kMaxPieces; ++k)
+    if (k < np) {
+      p[k] = __float2bfloat16_rn((float)x);
+      x -= (T)__bfloat162float(p[k]);
+    }
+}
 struct Bf16Split {
-  const __nv_bfloat16 *hi, *lo;
+  const __nv_bfloat16 *p[kMaxPieces];
 };
+
+// Split-BF16 tensor-core GEMM (k_gemm.cu):
+//   C_z[m][n] = sum_k A[z * a_batch_rows + m][k] B[z * b_batch_rows + n][k]
+// A and B in np pieces (rows of Kp BF16, Kp a multiple of 64, zero beyond the
+// true K); a_rows / b_rows: rows of the whole arrays (loads past them read
+// zeros).  np = 2: products p0q0 + p0q1 + p1q0 (3 per K step, ~2^-16
+// relative per product); np = 3: adds p1q1 + p0q2 + p2q0 (6, ~2^-24).  FP32
+// accumulation.
 struct GemmOut {
   float *C;                   // FP32 output, or (C null)
-  __nv_bfloat16 *Ch, *Cl;     // split BF16 output
+  __nv_bfloat16 *Cp[kMaxPieces];  // split output in np pieces
   long long ldc;              // row stride of the output
   long long c_batch;          // element offset of batch z
   long long grp_rows, grp_stride, row0;  // output row of m: (m / grp_rows) * grp_stride + m % grp_rows + row0
                                           // (grp_rows 0: row m + row0)
+  long long grp_cols, gcol_stride, col0; // output column of n: (n / grp_cols) * gcol_stride + n % grp_cols + col0
+                                          // (grp_cols 0: column n)
 };
-cudaError_t launch_gemm_bf16x3(const Bf16Split &A, long long a_rows, const Bf16Split &B, long long b_rows, int Kp,
-                               int M, int N, int batch, int a_batch_rows, int b_batch_rows, const GemmOut &out,
-                               int *derr, cudaStream_t s);
-// src [rows][cols] (row stride lds) -> hi / lo [rows][ldo], x = hi + lo + O(2^-17 x)
+cudaError_t launch_gemm_split(const Bf16Split &A, long long a_rows, const Bf16Split &B, long long b_rows, int Kp,
+                              int M, int N, int batch, int a_batch_rows, int b_batch_rows, int np,
+                              const GemmOut &out, int *derr, cudaStream_t s);
+// Same product with three pieces per operand, eight products and per-slab
+// FP64 accumulation (about FP64-level error on the kept ~24 bits per
+// operand): for contractions with strong cancellation.  Output in three pieces
+// or FP32.
+cudaError_t launch_gemm_precise(const Bf16Split &A, long long a_rows, const Bf16Split &B, long long b_rows, int Kp,
+                                int M, int N, int batch, int a_batch_rows, int b_batch_rows, const GemmOut &out,
+                                int *derr, cudaStream_t s);
+// src [rows][cols] (row stride lds) -> np pieces [rows][ldo]
 template <typename T>
-cudaError_t launch_split_bf16(const T *src, long long rows, int cols, long long lds, __nv_bfloat16 *hi,
-                              __nv_bfloat16 *lo, long long ldo, cudaStream_t s);
+cudaError_t launch_split_bf16(const T *src, long long rows, int cols, long long lds, int np, __nv_bfloat16 *const *out,
+                              long long ldo, cudaStream_t s);
 
 // number of kernels this library has launched (process-wide)
 void count_launches(long long n);

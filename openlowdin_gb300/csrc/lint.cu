@@ -1554,9 +1554,291 @@ bool dgemm_rm(cublasHandle_t h, bool ta, bool tb, int m, int n, int k, const dou
 struct MP2Stats {
   long long ncols = 0;
   int batches = 0;
-  double x_bytes = 0, y_bytes = 0;
 };
 MP2Stats g_mp2_last;
+
+// Columns of the significant ket pairs (colbase per pair record; colpair =
+// lam | sig << 16 | offdiag << 31) and batches of whole ket pairs with at most
+// colB columns (bfirst: first pair of each batch, then npairs).
+struct MP2Columns {
+  std::vector<int> colbase;
+  std::vector<unsigned> colpair;
+  std::vector<int> bfirst;
+  long long ncols = 0;
+};
+
+void mp2_columns(const PairList &P, long long colB, MP2Columns &mc) {
+  const int npairs = (int)P.h.size();
+  mc.colbase.assign(npairs, 0);
+  mc.colpair.clear();
+  for (int k = 0; k < npairs; ++k) {
+    const PairRec &r = P.h[k];
+    mc.colbase[k] = (int)mc.colpair.size();
+    const int nc = ncart(r.la), nd = ncart(r.lb);
+    for (int c = 0; c < nc; ++c)
+      for (int d = 0; d < nd; ++d)
+        mc.colpair.push_back((unsigned)(r.fa + c) | (unsigned)(r.fb + d) << 16 | (r.sa != r.sb ? 1u << 31 : 0u));
+  }
+  mc.ncols = (long long)mc.colpair.size();
+  mc.bfirst.clear();
+  for (int k = 0; k < npairs;) {
+    mc.bfirst.push_back(k);
+    const int c0 = mc.colbase[k];
+    while (k < npairs && mc.colbase[k] - c0 + ncart(P.h[k].la) * ncart(P.h[k].lb) <= colB) ++k;
+  }
+  mc.bfirst.push_back(npairs);
+}
+
+// integrals of every significant bra pair against the ket pairs [k0, k1)
+bool mp2_batch_ints(const PairList &P, MXParams q, int k0, int k1, cudaStream_t s) {
+  for (int ck = 0; ck < kNumPairClasses; ++ck) {
+    const int ka = std::max(k0, P.start[ck]), kb = std::min(k1, P.start[ck + 1]);
+    if (ka >= kb) continue;
+    for (int cb = 0; cb < kNumPairClasses; ++cb)
+      for (int b0 = P.start[cb]; b0 < P.start[cb + 1]; b0 += 65535 * kWarpsPerBlock) {  // grid y limit
+        q.bra0 = b0;
+        q.nbra = std::min(P.start[cb + 1] - b0, 65535 * kWarpsPerBlock);
+        q.ket0 = ka;
+        q.nket = kb - ka;
+        CK(launch_mp2x(cb, ck, q, s));
+      }
+  }
+  return true;
+}
+
+struct MP2Setup {
+  LibintInterface *L;
+  int n, nsh, o, v, n_occ, n_frozen;
+  const double *dC, *eps;
+  MXParams q;      // common integral parameters
+};
+
+bool mp2_need(size_t bytes) {
+  size_t freeb = 0, totb = 0;
+  CK(cudaMemGetInfo(&freeb, &totb));
+  if (bytes > freeb) {
+    set_error("mp2_direct: needs %.1f GB of device memory, %.1f GB free", bytes / 1e9, freeb / 1e9);
+    return false;
+  }
+  return true;
+}
+
+// FP64 back end: cuBLAS DGEMM for the four quarters
+bool mp2_fp64(MP2Setup &S, size_t budget, double *e2out, cudaStream_t s) {
+  const int n = S.n, o = S.o, v = S.v;
+  cublasHandle_t blas;
+  if (!blas_handle(&blas)) return false;
+  if (cublasSetStream(blas, s) != CUBLAS_STATUS_SUCCESS) {
+    set_error("cublasSetStream failed");
+    return false;
+  }
+  const PairList &P = S.L->sig;
+  const size_t per_col = (size_t)n * n * sizeof(double) + (size_t)o * n * sizeof(double);
+  MP2Columns mc;
+  mp2_columns(P, std::max<long long>(36, (long long)(budget / per_col)), mc);
+  const long long ncols = mc.ncols;
+  long long colB = 0;
+  for (size_t b = 0; b + 1 < mc.bfirst.size(); ++b) {
+    const int k1 = mc.bfirst[b + 1];
+    colB = std::max<long long>(colB, (k1 < (int)P.h.size() ? mc.colbase[k1] : ncols) - mc.colbase[mc.bfirst[b]]);
+  }
+  if (!mp2_need((size_t)o * ncols * v * 8 + (size_t)n * n * v * 8 + (size_t)colB * per_col + (size_t)o * n * v * 8 +
+                (size_t)o * v * v * 8))
+    return false;
+  DevBuf<double> Co, Cv, Eo, Ev, Y, X, T1, Z, W, M, e2;
+  DevBuf<int> dcolbase;
+  DevBuf<unsigned> dcolpair;
+  if (!Co.ensure((size_t)n * o) || !Cv.ensure((size_t)n * v) || !Eo.ensure(o) || !Ev.ensure(v) ||
+      !Y.ensure((size_t)o * ncols * v) || !X.ensure((size_t)n * colB * n) || !T1.ensure((size_t)o * colB * n) ||
+      !Z.ensure((size_t)n * n * v) || !W.ensure((size_t)o * n * v) || !M.ensure((size_t)o * v * v) || !e2.ensure(1) ||
+      !dcolbase.ensure(P.h.size()) || !dcolpair.ensure(ncols))
+    return false;
+  CK(cudaMemcpyAsync(dcolbase.p, mc.colbase.data(), P.h.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dcolpair.p, mc.colpair.data(), ncols * sizeof(unsigned), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(Eo.p, S.eps + S.n_frozen, o * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(Ev.p, S.eps + S.n_occ, v * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(e2.p, 0, sizeof(double), s));
+  CK(launch_mp2_coeffs(S.dC, S.L->d_norma, n, S.n_frozen, S.n_occ, Co.p, Cv.p, nullptr, nullptr, s));
+  MXParams q = S.q;
+  q.colbase = dcolbase.p;
+  q.X = X.p;
+  const int nbatch = (int)mc.bfirst.size() - 1;
+  for (int bt = 0; bt < nbatch; ++bt) {
+    const int k0 = mc.bfirst[bt], k1 = mc.bfirst[bt + 1];
+    const int c0 = mc.colbase[k0];
+    const int nb = (int)((k1 < (int)P.h.size() ? mc.colbase[k1] : ncols) - c0);
+    q.col_first = c0;
+    q.ncol = nb;
+    CK(cudaMemsetAsync(X.p, 0, (size_t)n * nb * n * sizeof(double), s));
+    if (!mp2_batch_ints(P, q, k0, k1, s)) return false;
+    // T1 (o x nb*n) = Co^T X ; Y[i][c0 + col][a] = T1[i] (nb x n) Cv
+    if (!dgemm_rm(blas, true, false, o, nb * n, n, Co.p, o, 0, X.p, nb * n, 0, T1.p, nb * n, 0, 1)) return false;
+    if (!dgemm_rm(blas, false, false, nb, v, n, T1.p, n, (long long)nb * n, Cv.p, v, 0, Y.p + (size_t)c0 * v, v,
+                  ncols * v, o))
+      return false;
+  }
+  CK(cudaMemsetAsync(Z.p, 0, (size_t)n * n * v * sizeof(double), s));
+  for (int i = 0; i < o; ++i) {
+    CK(launch_mp2_unpack<double>(Y.p + (size_t)i * ncols * v, dcolpair.p, ncols, n, v, Z.p, s));
+    if (!dgemm_rm(blas, true, false, o, n * v, n, Co.p, o, 0, Z.p, n * v, 0, W.p, n * v, 0, 1)) return false;
+    if (!dgemm_rm(blas, true, false, v, v, n, Cv.p, v, 0, W.p, v, (long long)n * v, M.p, v, (long long)v * v, o))
+      return false;
+    CK(launch_mp2_energy<double>(M.p, o, v, S.eps[S.n_frozen + i], Eo.p, Ev.p, 1e-10, e2.p, s));
+  }
+  double e = 0;
+  CK(cudaMemcpyAsync(&e, e2.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  *e2out = e;
+  g_mp2_last.ncols = ncols;
+  g_mp2_last.batches = nbatch;
+  return true;  // the buffers are freed on return
+}
+
+// Split-BF16 back end: the same quarters on the tensor cores (np BF16 pieces
+// per operand, FP32 accumulation), operands written K-major by their producers:
+//   Xt[col][nu][mu]   (integral kernel)          GEMM1: T1[i][col nu] = CoT Xt^T
+//   Y'[a][i][col]     (GEMM2 = CvT T1^T, FP32)   per i: Zt[a][sig][lam] (gather)
+//   GEMM3: Wt[j][a sig] = CoT Zt^T               GEMM4: M_j[b][a] = CvT Wt_j^T
+struct SplitBuf {
+  DevBuf<__nv_bfloat16> p[kMaxPieces];
+  bool ensure(int np, size_t n) {
+    for (int q = 0; q < np; ++q)
+      if (!p[q].ensure(n)) return false;
+    return true;
+  }
+  Bf16Split in() const { return Bf16Split{{p[0].p, p[1].p, p[2].p}}; }
+  void out(GemmOut &o) const {
+    for (int q = 0; q < kMaxPieces; ++q) o.Cp[q] = p[q].p;
+  }
+  __nv_bfloat16 *const *ptrs(__nv_bfloat16 *(&tmp)[kMaxPieces]) const {
+    for (int q = 0; q < kMaxPieces; ++q) tmp[q] = p[q].p;
+    return tmp;
+  }
+};
+
+bool mp2_split(MP2Setup &S, int np, size_t budget, double *e2out, cudaStream_t s) {
+  using bf = __nv_bfloat16;
+  const int n = S.n, o = S.o, v = S.v;
+  const int Kp = (n + 63) / 64 * 64;
+  const PairList &P = S.L->sig;
+  const size_t per_col = (size_t)Kp * Kp * 2 * np + (size_t)o * Kp * 2 * np;   // Xt and T1 pieces
+  MP2Columns mc;
+  mp2_columns(P, std::max<long long>(36, (long long)(budget / per_col)), mc);
+  const long long ncols = mc.ncols;
+  long long colB = 0;
+  for (size_t b = 0; b + 1 < mc.bfirst.size(); ++b) {
+    const int k1 = mc.bfirst[b + 1];
+    colB = std::max<long long>(colB, (k1 < (int)P.h.size() ? mc.colbase[k1] : ncols) - mc.colbase[mc.bfirst[b]]);
+  }
+  // gather lists: row sig -> (lam, col) with Z[lam][sig] = Y[col]
+  std::vector<int> rowptr(n + 1, 0);
+  for (long long c = 0; c < ncols; ++c) {
+    const unsigned cp = mc.colpair[c];
+    rowptr[((cp >> 16) & 0x7fff) + 1]++;
+    if (cp >> 31) rowptr[(cp & 0xffff) + 1]++;
+  }
+  for (int r = 0; r < n; ++r) rowptr[r + 1] += rowptr[r];
+  std::vector<int2> ent(rowptr[n]);
+  {
+    std::vector<int> fill(rowptr.begin(), rowptr.end() - 1);
+    for (long long c = 0; c < ncols; ++c) {
+      const unsigned cp = mc.colpair[c];
+      const int lam = cp & 0xffff, sig = (cp >> 16) & 0x7fff;
+      ent[fill[sig]++] = make_int2(lam | sig << 16, (int)c);
+      if (cp >> 31) ent[fill[lam]++] = make_int2(sig | lam << 16, (int)c);
+    }
+  }
+  const size_t need = (size_t)v * o * ncols * 4 + (size_t)colB * per_col + ((size_t)v * Kp * Kp + (size_t)o * v * Kp +
+                      (size_t)(o + v) * Kp) * 2 * np + (size_t)o * v * v * 4 + ent.size() * 8;
+  if (!mp2_need(need)) return false;
+  SplitBuf CoT, CvT, X, T1, Z, W;
+  DevBuf<float> Y, M;
+  DevBuf<double> Eo, Ev, e2;
+  DevBuf<int> dcolbase, drowptr, err;
+  DevBuf<int2> dent;
+  const size_t xsz = (size_t)colB * Kp * Kp, t1sz = (size_t)o * colB * Kp, zsz = (size_t)v * Kp * Kp,
+               wsz = (size_t)o * v * Kp;
+  if (!CoT.ensure(np, (size_t)o * Kp) || !CvT.ensure(np, (size_t)v * Kp) || !X.ensure(np, xsz) ||
+      !T1.ensure(np, t1sz) || !Z.ensure(np, zsz) || !W.ensure(np, wsz) || !Y.ensure((size_t)v * o * ncols) ||
+      !M.ensure((size_t)o * v * v) || !Eo.ensure(o) || !Ev.ensure(v) || !e2.ensure(1) ||
+      !dcolbase.ensure(P.h.size()) || !drowptr.ensure(n + 1) || !err.ensure(1) ||
+      !dent.ensure(std::max<size_t>(1, ent.size())))
+    return false;
+  CK(cudaMemcpyAsync(dcolbase.p, mc.colbase.data(), P.h.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(drowptr.p, rowptr.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dent.p, ent.data(), ent.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(Eo.p, S.eps + S.n_frozen, o * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(Ev.p, S.eps + S.n_occ, v * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(e2.p, 0, sizeof(double), s));
+  CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+  for (const SplitBuf *b : {&CoT, &CvT, &Z})
+    for (int q = 0; q < np; ++q) CK(cudaMemsetAsync(b->p[q].p, 0, b->p[q].n * sizeof(bf), s));
+  bf *t0[kMaxPieces], *t1[kMaxPieces];
+  CK(launch_mp2_coeffs_bf16(S.dC, S.L->d_norma, n, S.n_frozen, S.n_occ, Kp, np, CoT.ptrs(t0), CvT.ptrs(t1), s));
+  // np 3: every quarter on the precise engine (the tensor cores round their
+  // FP32 running sums toward zero; over a 640-term contraction that bias, not
+  // the BF16 pieces, dominated the energy error); np 2: the plain engine
+  auto gemm = [&](const Bf16Split &A, long long ar, const Bf16Split &B, long long br, int M, int N, int batch,
+                  int abr, int bbr, const GemmOut &out) {
+    return np == 3 ? launch_gemm_precise(A, ar, B, br, Kp, M, N, batch, abr, bbr, out, err.p, s)
+                   : launch_gemm_split(A, ar, B, br, Kp, M, N, batch, abr, bbr, np, out, err.p, s);
+  };
+  MXParams q = S.q;
+  q.colbase = dcolbase.p;
+  q.X = nullptr;
+  for (int k = 0; k < kMaxPieces; ++k) q.Xp[k] = X.p[k].p;
+  q.np = np;
+  q.Kp = Kp;
+  const int nbatch = (int)mc.bfirst.size() - 1;
+  for (int bt = 0; bt < nbatch; ++bt) {
+    const int k0 = mc.bfirst[bt], k1 = mc.bfirst[bt + 1];
+    const int c0 = mc.colbase[k0];
+    const int nb = (int)((k1 < (int)P.h.size() ? mc.colbase[k1] : ncols) - c0);
+    q.col_first = c0;
+    q.ncol = nb;
+    for (int k = 0; k < np; ++k) CK(cudaMemsetAsync(X.p[k].p, 0, (size_t)nb * Kp * Kp * sizeof(bf), s));
+    if (!mp2_batch_ints(P, q, k0, k1, s)) return false;
+    GemmOut o1{};
+    T1.out(o1);
+    o1.ldc = (long long)nb * Kp;
+    CK(gemm(CoT.in(), o, X.in(), (long long)nb * Kp, o, nb * Kp, 1, 0, 0, o1));
+    GemmOut o2{};
+    o2.C = Y.p;
+    o2.ldc = (long long)o * ncols;
+    o2.grp_cols = nb;
+    o2.gcol_stride = ncols;
+    o2.col0 = c0;
+    CK(gemm(CvT.in(), v, T1.in(), (long long)o * nb, v, o * nb, 1, 0, 0, o2));
+  }
+  bf *tz[kMaxPieces];
+  for (int i = 0; i < o; ++i) {
+    CK(launch_mp2_unpack_csr(Y.p + (size_t)i * ncols, (long long)o * ncols, drowptr.p, dent.p, n, Kp, v, np,
+                             Z.ptrs(tz), s));
+    GemmOut o3{};
+    W.out(o3);
+    o3.ldc = (long long)v * Kp;
+    CK(gemm(CoT.in(), o, Z.in(), (long long)v * Kp, o, v * Kp, 1, 0, 0, o3));
+    GemmOut o4{};
+    o4.C = M.p;
+    o4.ldc = v;
+    o4.c_batch = (long long)v * v;
+    CK(gemm(CvT.in(), v, W.in(), (long long)o * v, v, v, o, 0, v, o4));
+    CK(launch_mp2_energy<float>(M.p, o, v, S.eps[S.n_frozen + i], Eo.p, Ev.p, 1e-10, e2.p, s));
+  }
+  double e = 0;
+  int herr = 0;
+  CK(cudaMemcpyAsync(&e, e2.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (herr) {
+    set_error("mp2_direct: a tensor-core GEMM pipeline wait ran out (code %d)", herr);
+    return false;
+  }
+  *e2out = e;
+  g_mp2_last.ncols = ncols;
+  g_mp2_last.batches = nbatch;
+  return true;
+}
 
 bool mp2_direct(LibintInterface *L, const double *dD, const double *dC, const double *eps, int n_occ, int n_frozen,
                 int precision, size_t x_budget_bytes, double *e2out, cudaStream_t s) {
@@ -1564,8 +1846,8 @@ bool mp2_direct(LibintInterface *L, const double *dD, const double *dC, const do
     set_error("mp2_direct: closed-shell MP2 is defined here for an electron species");
     return false;
   }
-  if (precision != 0) {
-    set_error("mp2_direct: precision %d is not available (0: FP64 GEMMs)", precision);
+  if (precision < 0 || precision > 2) {
+    set_error("mp2_direct: precision %d is not available (0: FP64, 1 / 2: split BF16 in 2 / 3 pieces)", precision);
     return false;
   }
   if (!L->ensure_sig()) return false;
@@ -1578,78 +1860,30 @@ bool mp2_direct(LibintInterface *L, const double *dD, const double *dC, const do
     set_error("mp2_direct: %d basis functions exceed the column encoding (32767)", n);
     return false;
   }
-  const int o = n_occ - n_frozen, v = n - n_occ;
-  cublasHandle_t blas;
-  if (!blas_handle(&blas)) return false;
-  if (cublasSetStream(blas, s) != CUBLAS_STATUS_SUCCESS) {
-    set_error("cublasSetStream failed");
-    return false;
-  }
-  // columns of the significant ket pairs
-  const PairList &P = L->sig;
-  const int npairs = (int)P.h.size();
-  std::vector<int> colbase(npairs);
-  std::vector<unsigned> colpair;
-  for (int k = 0; k < npairs; ++k) {
-    const PairRec &r = P.h[k];
-    colbase[k] = (int)colpair.size();
-    const int nc = ncart(r.la), nd = ncart(r.lb);
-    for (int c = 0; c < nc; ++c)
-      for (int d = 0; d < nd; ++d)
-        colpair.push_back((unsigned)(r.fa + c) | (unsigned)(r.fb + d) << 16 | (r.sa != r.sb ? 1u << 31 : 0u));
-  }
-  const long long ncols = (long long)colpair.size();
-  // column batches: whole ket pairs, X[n][colB][n] within the budget
-  const size_t per_col = (size_t)n * n * sizeof(double) + (size_t)o * n * sizeof(double);
-  long long colB = (long long)(x_budget_bytes / per_col);
-  if (colB < 36) colB = 36;
-  if (colB > ncols) colB = ncols;
-  std::vector<int> bfirst;  // first pair of each batch
-  for (int k = 0; k < npairs;) {
-    bfirst.push_back(k);
-    const int c0 = colbase[k];
-    while (k < npairs && colbase[k] - c0 + ncart(P.h[k].la) * ncart(P.h[k].lb) <= colB) ++k;
-  }
-  bfirst.push_back(npairs);
-  const int nbatch = (int)bfirst.size() - 1;
-  // device memory
-  const size_t ybytes = (size_t)o * ncols * v * sizeof(double);
-  const size_t zbytes = (size_t)n * n * v * sizeof(double);
-  size_t freeb = 0, totb = 0;
-  CK(cudaMemGetInfo(&freeb, &totb));
-  const size_t need = ybytes + zbytes + (size_t)colB * per_col + (size_t)o * n * v * 8 + (size_t)o * v * v * 8;
-  if (need > freeb) {
-    set_error("mp2_direct: needs %.1f GB of device memory, %.1f GB free", need / 1e9, freeb / 1e9);
-    return false;
-  }
-  DevBuf<double> Co, Cv, Eo, Ev, Y, X, T1, Z, W, M, e2;
-  DevBuf<int> dcolbase;
-  DevBuf<unsigned> dcolpair;
-  if (!Co.ensure((size_t)n * o) || !Cv.ensure((size_t)n * v) || !Eo.ensure(o) || !Ev.ensure(v) ||
-      !Y.ensure((size_t)o * ncols * v) || !X.ensure((size_t)n * colB * n) || !T1.ensure((size_t)o * colB * n) ||
-      !Z.ensure((size_t)n * n * v) || !W.ensure((size_t)o * n * v) || !M.ensure((size_t)o * v * v) || !e2.ensure(1) ||
-      !dcolbase.ensure(npairs) || !dcolpair.ensure(ncols))
-    return false;
-  CK(cudaMemcpyAsync(dcolbase.p, colbase.data(), npairs * sizeof(int), cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(dcolpair.p, colpair.data(), ncols * sizeof(unsigned), cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(Eo.p, eps + n_frozen, o * sizeof(double), cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(Ev.p, eps + n_occ, v * sizeof(double), cudaMemcpyHostToDevice, s));
-  CK(cudaMemsetAsync(e2.p, 0, sizeof(double), s));
-  CK(launch_mp2_coeffs(dC, L->d_norma, n, n_frozen, n_occ, Co.p, Cv.p, nullptr, nullptr, s));
+  MP2Setup S{};
+  S.L = L;
+  S.n = n;
+  S.nsh = nsh;
+  S.n_occ = n_occ;
+  S.n_frozen = n_frozen;
+  S.o = n_occ - n_frozen;
+  S.v = n - n_occ;
+  S.dC = dC;
+  S.eps = eps;
   // shell-block norms of D for the screening
   if (!L->dDs.ensure((size_t)n * n) || !L->dDn.ensure((size_t)nsh * nsh)) return false;
   CK(launch_prepare_density(dD, L->d_norma, L->d_shell_of, n, nsh, L->dDs.p, nullptr, L->dDn.p, nullptr, s));
   double *scr = nullptr;
+  const PairList &P = L->sig;
   for (int cb = 0; cb < kNumPairClasses && !scr; ++cb)
     for (int ck = 0; ck < kNumPairClasses; ++ck)
       if (P.count(cb) && P.count(ck) && class_generic(cb, ck)) {
         if (!(scr = L->gen_scratch())) return false;
         break;
       }
-  MXParams q{};
+  MXParams &q = S.q;
   q.pairs = P.d;
   q.prims = P.dp;
-  q.colbase = dcolbase.p;
   q.Dn = L->dDn.p;
   q.nsh = nsh;
   q.screen = 1;
@@ -1658,53 +1892,7 @@ bool mp2_direct(LibintInterface *L, const double *dD, const double *dC, const do
   q.n = n;
   q.boys = L->boys;
   q.scratch = scr;
-  for (int bt = 0; bt < nbatch; ++bt) {
-    const int k0 = bfirst[bt], k1 = bfirst[bt + 1];
-    const int c0 = colbase[k0];
-    const int c1 = k1 < npairs ? colbase[k1] : (int)ncols;
-    const int nb = c1 - c0;
-    q.col_first = c0;
-    q.ncol = nb;
-    q.X = X.p;
-    CK(cudaMemsetAsync(X.p, 0, (size_t)n * nb * n * sizeof(double), s));
-    for (int ck = 0; ck < kNumPairClasses; ++ck) {
-      const int ka = std::max(k0, P.start[ck]), kb = std::min(k1, P.start[ck + 1]);
-      if (ka >= kb) continue;
-      for (int cb = 0; cb < kNumPairClasses; ++cb) {
-        // bra chunks within the grid's y limit
-        for (int b0 = P.start[cb]; b0 < P.start[cb + 1]; b0 += 65535 * kWarpsPerBlock) {
-          q.bra0 = b0;
-          q.nbra = std::min(P.start[cb + 1] - b0, 65535 * kWarpsPerBlock);
-          q.ket0 = ka;
-          q.nket = kb - ka;
-          CK(launch_mp2x(cb, ck, q, s));
-        }
-      }
-    }
-    // T1 (o x nb*n) = Co^T X ; Y[i][c0 + col][a] = T1[i] (nb x n) Cv
-    if (!dgemm_rm(blas, true, false, o, nb * n, n, Co.p, o, 0, X.p, nb * n, 0, T1.p, nb * n, 0, 1)) return false;
-    if (!dgemm_rm(blas, false, false, nb, v, n, T1.p, n, (long long)nb * n, Cv.p, v, 0, Y.p + (size_t)c0 * v, v,
-                  ncols * v, o))
-      return false;
-  }
-  CK(cudaMemsetAsync(Z.p, 0, zbytes, s));
-  std::vector<double> eo(eps + n_frozen, eps + n_occ);
-  for (int i = 0; i < o; ++i) {
-    CK(launch_mp2_unpack<double>(Y.p + (size_t)i * ncols * v, dcolpair.p, ncols, n, v, Z.p, s));
-    if (!dgemm_rm(blas, true, false, o, n * v, n, Co.p, o, 0, Z.p, n * v, 0, W.p, n * v, 0, 1)) return false;
-    if (!dgemm_rm(blas, true, false, v, v, n, Cv.p, v, 0, W.p, v, (long long)n * v, M.p, v, (long long)v * v, o))
-      return false;
-    CK(launch_mp2_energy<double>(M.p, o, v, eo[i], Eo.p, Ev.p, 1e-10, e2.p, s));
-  }
-  double e = 0;
-  CK(cudaMemcpyAsync(&e, e2.p, sizeof(double), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  *e2out = e;
-  g_mp2_last.ncols = ncols;
-  g_mp2_last.batches = nbatch;
-  g_mp2_last.x_bytes = (double)n * colB * n * 8;
-  g_mp2_last.y_bytes = (double)ybytes;
-  return true;  // the buffers are freed on return
+  return precision == 0 ? mp2_fp64(S, x_budget_bytes, e2out, s) : mp2_split(S, precision + 1, x_budget_bytes, e2out, s);
 }
 
 }  // namespace
@@ -1727,49 +1915,60 @@ long long LowdinGB300_mp2_last_columns(void) { return g_mp2_last.ncols; }
 }  // extern "C"
 
 // ============================================== split-BF16 tensor-core GEMM
-extern "C" {
-
-int LowdinGB300_gemm_bf16x3(const float *dA, const float *dB, float *dC, int M, int N, int K, void *stream) {
-  if (!dA || !dB || !dC || M <= 0 || N <= 0 || K <= 0) {
-    set_error("%s: invalid arguments", __func__);
+namespace {
+int gemm_entry(const char *fn, const float *dA, const float *dB, float *dC, int M, int N, int K, int pieces,
+               bool precise, void *stream) {
+  if (!dA || !dB || !dC || M <= 0 || N <= 0 || K <= 0 || pieces < 2 || pieces > kMaxPieces) {
+    set_error("%s: invalid arguments", fn);
     return -1;
   }
   cudaStream_t s = (cudaStream_t)stream;
   const int Kp = (K + 63) / 64 * 64;
-  DevBuf<__nv_bfloat16> Ah, Al, Bh, Bl;
+  SplitBuf A, B;
   DevBuf<int> err;
-  if (!Ah.ensure((size_t)M * Kp) || !Al.ensure((size_t)M * Kp) || !Bh.ensure((size_t)N * Kp) ||
-      !Bl.ensure((size_t)N * Kp) || !err.ensure(1))
-    return -1;
+  if (!A.ensure(pieces, (size_t)M * Kp) || !B.ensure(pieces, (size_t)N * Kp) || !err.ensure(1)) return -1;
   auto fail = [&](const char *what, cudaError_t e) {
-    set_error("%s: %s (%s)", __func__, what, cudaGetErrorString(e));
+    set_error("%s: %s (%s)", fn, what, cudaGetErrorString(e));
     return -1;
   };
   cudaError_t e;
-  if ((e = cudaMemsetAsync(Ah.p, 0, (size_t)M * Kp * 2, s)) != cudaSuccess ||
-      (e = cudaMemsetAsync(Al.p, 0, (size_t)M * Kp * 2, s)) != cudaSuccess ||
-      (e = cudaMemsetAsync(Bh.p, 0, (size_t)N * Kp * 2, s)) != cudaSuccess ||
-      (e = cudaMemsetAsync(Bl.p, 0, (size_t)N * Kp * 2, s)) != cudaSuccess ||
-      (e = cudaMemsetAsync(err.p, 0, sizeof(int), s)) != cudaSuccess)
-    return fail("clear", e);
-  if ((e = launch_split_bf16<float>(dA, M, K, K, Ah.p, Al.p, Kp, s)) != cudaSuccess ||
-      (e = launch_split_bf16<float>(dB, N, K, K, Bh.p, Bl.p, Kp, s)) != cudaSuccess)
+  for (int q = 0; q < pieces; ++q)
+    if ((e = cudaMemsetAsync(A.p[q].p, 0, (size_t)M * Kp * 2, s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(B.p[q].p, 0, (size_t)N * Kp * 2, s)) != cudaSuccess)
+      return fail("clear", e);
+  if ((e = cudaMemsetAsync(err.p, 0, sizeof(int), s)) != cudaSuccess) return fail("clear", e);
+  __nv_bfloat16 *ta[kMaxPieces], *tb[kMaxPieces];
+  if ((e = launch_split_bf16<float>(dA, M, K, K, pieces, A.ptrs(ta), Kp, s)) != cudaSuccess ||
+      (e = launch_split_bf16<float>(dB, N, K, K, pieces, B.ptrs(tb), Kp, s)) != cudaSuccess)
     return fail("split", e);
   GemmOut out{};
   out.C = dC;
   out.ldc = N;
-  if ((e = launch_gemm_bf16x3(Bf16Split{Ah.p, Al.p}, M, Bf16Split{Bh.p, Bl.p}, N, Kp, M, N, 1, 0, 0, out, err.p,
-                              s)) != cudaSuccess)
-    return fail("gemm launch", e);
+  e = precise ? launch_gemm_precise(A.in(), M, B.in(), N, Kp, M, N, 1, 0, 0, out, err.p, s)
+              : launch_gemm_split(A.in(), M, B.in(), N, Kp, M, N, 1, 0, 0, pieces, out, err.p, s);
+  if (e != cudaSuccess) return fail("gemm launch", e);
   int herr = 0;
   if ((e = cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
       (e = cudaStreamSynchronize(s)) != cudaSuccess)
     return fail("gemm", e);
   if (herr) {
-    set_error("%s: a pipeline wait ran out (code %d)", __func__, herr);
+    set_error("%s: a pipeline wait ran out (code %d)", fn, herr);
     return -1;
   }
   return 0;
+}
+}  // namespace
+
+extern "C" {
+
+
+int LowdinGB300_gemm_bf16_split(const float *dA, const float *dB, float *dC, int M, int N, int K, int pieces,
+                                void *stream) {
+  return gemm_entry(__func__, dA, dB, dC, M, N, K, pieces, false, stream);
+}
+
+int LowdinGB300_gemm_bf16_precise(const float *dA, const float *dB, float *dC, int M, int N, int K, void *stream) {
+  return gemm_entry(__func__, dA, dB, dC, M, N, K, 3, true, stream);
 }
 
 }  // extern "C"

@@ -78,8 +78,11 @@ def lib():
                                              ctypes.c_double, ctypes.POINTER(ctypes.c_double), _vp]
         L.LowdinGB300_mp2_direct.restype = ctypes.c_int
         L.LowdinGB300_mp2_last_columns.restype = ctypes.c_longlong
-        L.LowdinGB300_gemm_bf16x3.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp]
-        L.LowdinGB300_gemm_bf16x3.restype = ctypes.c_int
+        L.LowdinGB300_gemm_bf16_split.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                  ctypes.c_int, _vp]
+        L.LowdinGB300_gemm_bf16_split.restype = ctypes.c_int
+        L.LowdinGB300_gemm_bf16_precise.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp]
+        L.LowdinGB300_gemm_bf16_precise.restype = ctypes.c_int
         L.LowdinGB300_batch_new.restype = _vp
         L.LowdinGB300_batch_del.argtypes = [_vp]
         L.LowdinGB300_batch_add_system.argtypes = [_vp, ctypes.POINTER(_vp), ctypes.c_int, _f64p, _f64p,
@@ -117,7 +120,7 @@ EXPORTED_SYMBOLS = [
     "LowdinGB300_batch_finalize", "LowdinGB300_batch_fock", "LowdinGB300_batch_quartets",
     "LowdinGB300_batch_coupling_quartets", "LowdinGB300_noalloc_scratch_bytes",
     "LowdinGB300_twobody_device_noalloc", "LowdinGB300_mp2_direct", "LowdinGB300_mp2_last_columns",
-    "LowdinGB300_gemm_bf16x3",
+    "LowdinGB300_gemm_bf16_split", "LowdinGB300_gemm_bf16_precise",
 ]
 
 
@@ -324,11 +327,19 @@ class Libint2Interface:
         return out
 
 
-def gemm_bf16x3(a_ptr: int, b_ptr: int, c_ptr: int, M: int, N: int, K: int, stream: int = 0):
-    """C (M x N) = A (M x K) B^T (B: N x K), FP32 device arrays, 3-term split-BF16 tensor cores."""
-    if lib().LowdinGB300_gemm_bf16x3(a_ptr, b_ptr, c_ptr, int(M), int(N), int(K), stream) != 0:
+def gemm_bf16_split(a_ptr: int, b_ptr: int, c_ptr: int, M: int, N: int, K: int, pieces: int = 3,
+                    stream: int = 0):
+    """C (M x N) = A (M x K) B^T (B: N x K), FP32 device arrays, split-BF16 tensor cores."""
+    if lib().LowdinGB300_gemm_bf16_split(a_ptr, b_ptr, c_ptr, int(M), int(N), int(K), int(pieces), stream) != 0:
         _check()
-        raise LowdinGB300Error("gemm_bf16x3 failed")
+        raise LowdinGB300Error("gemm_bf16_split failed")
+
+
+def gemm_bf16_precise(a_ptr: int, b_ptr: int, c_ptr: int, M: int, N: int, K: int, stream: int = 0):
+    """C = A B^T with three BF16 pieces, eight products and FP64 slab accumulation."""
+    if lib().LowdinGB300_gemm_bf16_precise(a_ptr, b_ptr, c_ptr, int(M), int(N), int(K), stream) != 0:
+        _check()
+        raise LowdinGB300Error("gemm_bf16_precise failed")
 
 
 def measure_fma_tflops(fp64: bool = True) -> float:

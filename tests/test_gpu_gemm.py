@@ -1,13 +1,18 @@
-"""3-term split-BF16 tensor-core GEMM against an FP64 product.
+"""Split-BF16 tensor-core GEMM against an FP64 product.
 
-Bound per element: |C - A B^T| <= 6e-5 (|A| |B|^T) + 1e-6 |A B^T|: the
-two-term BF16 representation keeps about 16 bits of each operand (the dropped
-lo*lo term and the rounding of hi and lo give ~2^-16 relative per product) and
-the FP32 accumulator adds ~K 2^-24.
+Bounds per element, with S = |A| |B|^T:
+  2 pieces: |C - A B^T| <= 6e-5 S + 1e-6 |A B^T|  (~16 bits kept per operand,
+            dropped p1q1 term: ~2^-16 relative per product)
+  3 pieces: |C - A B^T| <= 2e-6 S + 1e-6 |A B^T|  (~24 bits per operand; the
+            FP32 accumulator, ~K 2^-24 at worst, dominates)
+  precise:  |C - A B^T| <= 1e-7 S + 1e-7 |A B^T|  (eight products, FP64 sums of
+            once-rounded slab products; the FP32 output rounding is 6e-8)
 """
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+SHAPES = [(128, 128, 64), (200, 300, 100), (64, 1000, 640), (1000, 560, 640), (7, 5, 3), (333, 129, 1216)]
 
 
 @pytest.fixture(scope="module")
@@ -17,18 +22,34 @@ def L():
     return lint
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (200, 300, 100), (64, 1000, 640), (1000, 560, 640),
-                                   (7, 5, 3), (333, 129, 1216)])
-def test_gemm_bf16x3_matches_fp64(L, M, N, K):
+@pytest.mark.parametrize("pieces,rel", [(2, 6e-5), (3, 2e-6)])
+@pytest.mark.parametrize("M,N,K", SHAPES)
+def test_gemm_split_matches_fp64(L, M, N, K, pieces, rel):
     torch = pytest.importorskip("torch")
     g = torch.Generator(device="cuda").manual_seed(M * 7919 + N * 31 + K)
     A = torch.randn(M, K, device="cuda", generator=g, dtype=torch.float32)
     B = torch.randn(N, K, device="cuda", generator=g, dtype=torch.float32) * 1e-3
     C = torch.full((M, N), float("nan"), device="cuda", dtype=torch.float32)
-    L.gemm_bf16x3(A.data_ptr(), B.data_ptr(), C.data_ptr(), M, N, K,
-                  stream=torch.cuda.current_stream().cuda_stream)
+    L.gemm_bf16_split(A.data_ptr(), B.data_ptr(), C.data_ptr(), M, N, K, pieces,
+                      stream=torch.cuda.current_stream().cuda_stream)
     ref = A.double() @ B.double().T
-    bound = 6e-5 * (A.double().abs() @ B.double().abs().T) + 1e-6 * ref.abs()
+    bound = rel * (A.double().abs() @ B.double().abs().T) + 1e-6 * ref.abs()
+    err = (C.double() - ref).abs()
+    assert torch.isfinite(C).all()
+    assert bool((err <= bound).all()), float((err / bound).max())
+
+
+@pytest.mark.parametrize("M,N,K", SHAPES)
+def test_gemm_precise_matches_fp64(L, M, N, K):
+    torch = pytest.importorskip("torch")
+    g = torch.Generator(device="cuda").manual_seed(M * 13 + N * 7 + K)
+    A = torch.randn(M, K, device="cuda", generator=g, dtype=torch.float32)
+    B = torch.randn(N, K, device="cuda", generator=g, dtype=torch.float32) * 1e3
+    C = torch.full((M, N), float("nan"), device="cuda", dtype=torch.float32)
+    L.gemm_bf16_precise(A.data_ptr(), B.data_ptr(), C.data_ptr(), M, N, K,
+                        stream=torch.cuda.current_stream().cuda_stream)
+    ref = A.double() @ B.double().T
+    bound = 1e-7 * (A.double().abs() @ B.double().abs().T) + 1e-7 * ref.abs()
     err = (C.double() - ref).abs()
     assert torch.isfinite(C).all()
     assert bool((err <= bound).all()), float((err / bound).max())

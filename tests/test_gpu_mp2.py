@@ -2,7 +2,9 @@
 restatement of the reference's DIRECT transform, on the same SCF inputs.
 
 Tolerance: 1e-10 Eh on E_MP2 for the FP64 path (the benchmark spec's MP2 bar is
-1e-8 Eh); the golden MP2 total energy within its test tolerance.
+1e-8 Eh); the golden MP2 total energy within its test tolerance; the
+split-BF16 tensor-core path within 1e-6 Eh of the oracle (the per-job bar of
+the mixed-precision forms).
 """
 import numpy as np
 import pytest
@@ -13,6 +15,7 @@ from tests import golden_systems as GS
 pytestmark = pytest.mark.gpu
 
 TOL_E2 = 1e-10
+TOL_MIXED = 1e-6
 
 
 @pytest.fixture(scope="module")
@@ -70,3 +73,29 @@ def test_mp2_two_waters_d(L, oracle):
     b = oracle.Basis.from_shells(sp["shells"])
     ref = oracle.rmp2_direct(b, res.densities[0], res.coefficients[0], res.orbital_energies[0], 10, 2)
     assert abs(e2 - ref) < TOL_E2
+
+
+@pytest.mark.parametrize("budget", [0.0, 2e-4])
+def test_mp2_split_bf16_tensor_cores(L, oracle, budget):
+    """precision 2: the four contractions on the tensor cores, 3 BF16 pieces
+    per operand (6 products) -- within the 1e-6 Eh bar; precision 1 (2
+    pieces, 3 products) is reported, its error is ~1e-5 relative."""
+    sysd = S.water_cluster(2, seed=3, o_d=True)
+    res = oracle.scf(oracle.from_plain(sysd))
+    sp = sysd["species"][0]
+    b = oracle.Basis.from_shells(sp["shells"])
+    ref = oracle.rmp2_direct(b, res.densities[0], res.coefficients[0], res.orbital_energies[0], 10, 2)
+    e2 = _device_mp2(L, sp, res, 10, 2, precision=2, x_budget_gb=budget)
+    assert abs(e2 - ref) < TOL_MIXED, (e2, ref)
+    e2_3term = _device_mp2(L, sp, res, 10, 2, precision=1, x_budget_gb=budget)
+    assert abs(e2_3term - ref) < 5e-5 * abs(ref), (e2_3term, ref)
+
+
+def test_mp2_split_bf16_golden_h2o(L, oracle, golden):
+    sysd = GS.h2o_boa(golden)
+    res = oracle.scf(oracle.from_plain(sysd))
+    sp = sysd["species"][0]
+    b = oracle.Basis.from_shells(sp["shells"])
+    ref = oracle.rmp2_direct(b, res.densities[0], res.coefficients[0], res.orbital_energies[0], 5)
+    e2 = _device_mp2(L, sp, res, 5, 0, precision=2)
+    assert abs(e2 - ref) < TOL_MIXED, (e2, ref)
