@@ -1,15 +1,19 @@
-// Generic (runtime-class) kernels for the quartet classes of total angular
-// momentum 7 and 8, the Schwarz kernels, and the dispatch of every class to its
-// templated or generic kernel.
+// Block-cooperative kernels for the quartet classes of total angular momentum
+// above kTemplatedMaxL, the Schwarz kernels, and the dispatch of every class
+// to its templated or cooperative kernel.
 //
-// The generic kernels run a fixed grid of kGenericBlocks persistent blocks;
-// block g owns scratch slots g*128 .. g*128+127 and walks the tiles g,
-// g + kGenericBlocks, ... of the task list, so every running thread has its own
-// work arrays.  They compute in FP64 (also when a mixed launch asks for the FP32
-// half: the split decides which quartets a launch takes, the generic kernel
-// evaluates them in FP64 and accumulates into the FP64 arrays).
+// A cooperative kernel runs a persistent grid of CTAs (three per SM fit their
+// shared work arrays); each CTA takes work units -- a bra pair and 8 ket pairs
+// of a task's 4 x 32 tile -- and evaluates their quartets one after another,
+// all 128 threads on each quartet (eri_coop), then digests the quartet's
+// integrals with the threads split over the output elements.  They compute in
+// FP64 (also when a mixed launch asks for the FP32 half: the split decides
+// which quartets a launch takes, the quartets are evaluated in FP64 and
+// accumulated into the FP64 arrays).
 #include "eri_generic.cuh"
 #include "fock_kernels.cuh"
+
+#include <algorithm>
 
 namespace lgb {
 
@@ -30,302 +34,290 @@ const ITFn *const kIT[6] = {kIT_0, kIT_1, kIT_2, kIT_3, kIT_4, kIT_5};
 const MXFn *const kMX[6] = {kMX_0, kMX_1, kMX_2, kMX_3, kMX_4, kMX_5};
 
 const dim3 kBlock(32, kWarpsPerBlock);
+constexpr int kCoThreads = 128;
+constexpr int kCoUnitsPerTile = kWarpsPerBlock * 4;   // (bra row, group of 8 kets)
+constexpr int kCoCtas = 152 * 3;
 
 struct GenClass {
   int la, lb, lc, ld;
 };
 
-__device__ __forceinline__ double *thread_scratch(double *scratch, size_t *stride) {
-  *stride = (size_t)gridDim.x * kGenericThreads;
-  return scratch + (size_t)blockIdx.x * kGenericThreads + threadIdx.y * 32 + threadIdx.x;
+// work unit u of a task-tiled launch -> tile, bra position, first ket position
+template <typename Task>
+__device__ __forceinline__ const Task &coop_unit(const Task *tasks, int ntasks, int u, int *bpos, int *kpos0) {
+  const int blk = u / kCoUnitsPerTile, sub = u % kCoUnitsPerTile;
+  const Task &T = tasks[find_task(tasks, ntasks, blk)];
+  const int local = blk - T.blk0;
+  const int tx = local % T.nbx, ty = local / T.nbx;
+  *bpos = ty * kWarpsPerBlock + sub / 4;
+  *kpos0 = tx * 32 + (sub % 4) * 8;
+  return T;
 }
 
 // ------------------------------------------------------------------ J/K --
-__global__ void __launch_bounds__(128) jk_generic_kernel(const JKTask *__restrict__ tasks, TaskLaunch TL, GenClass K) {
-  size_t stride;
-  double *scr = thread_scratch(TL.scratch, &stride);
+__global__ void __launch_bounds__(kCoThreads) jk_coop_kernel(const JKTask *__restrict__ tasks, TaskLaunch TL,
+                                                             GenClass K) {
+  extern __shared__ double sm[];
+  const int tid = threadIdx.x;
   const int NA = ncart(K.la), NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld);
-  const Strided I{scr + (size_t)(kGenScratch - kGenOut) * stride, stride};
-  for (int blk = blockIdx.x; blk < TL.nblocks; blk += gridDim.x) {
-    const int t = find_task(tasks, TL.ntasks, blk);
-    const JKTask &T = tasks[t];
-    const int local = blk - T.blk0;
-    const int tx = local % T.nbx, ty = local / T.nbx;
-    if (T.triangle && tx * 32 > ty * kWarpsPerBlock + kWarpsPerBlock - 1) continue;
-    const int kpos = tx * 32 + threadIdx.x;
-    const int bpos = ty * kWarpsPerBlock + threadIdx.y;
-    if (bpos >= T.nbra) continue;  // warp-uniform
-    bool active = kpos < T.nket && (!T.triangle || kpos <= bpos);
-    const int bi = T.bra0 + bpos;
-    const int ki = T.ket0 + min(kpos, T.nket - 1);
-    const PairRec &bra = T.pairs[bi];
-    const PairRec ket = T.pairs[ki];
-    if (TL.split > 0.0) {
-      float b = T.pairs32[bi].Q * T.pairs32[ki].Q;
-      if (T.screen) {
-        b *= dnorm6(T.Dn32, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
-        if (b < (float)TL.eps) active = false;
+  const double *I = sm + kCoOut;
+  for (int u = blockIdx.x; u < TL.nblocks * kCoUnitsPerTile; u += gridDim.x) {
+    int bpos, kpos0;
+    const JKTask &T = coop_unit(tasks, TL.ntasks, u, &bpos, &kpos0);
+    if (bpos >= T.nbra) continue;
+    for (int kpos = kpos0; kpos < kpos0 + 8 && kpos < T.nket; ++kpos) {
+      if (T.triangle && kpos > bpos) break;
+      const int bi = T.bra0 + bpos, ki = T.ket0 + kpos;
+      const PairRec &bra = T.pairs[bi];
+      const PairRec &ket = T.pairs[ki];
+      bool active = true;
+      if (TL.split > 0.0) {
+        float b = T.pairs32[bi].Q * T.pairs32[ki].Q;
+        if (T.screen) {
+          b *= dnorm6(T.Dn32, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
+          if (b < (float)TL.eps) active = false;
+        }
+        if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) active = false;
+      } else if (T.screen) {
+        if (bra.Q * ket.Q * dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < TL.eps) active = false;
       }
-      if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) active = false;
-    } else if (T.screen) {
-      const double b = bra.Q * ket.Q * dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
-      if (b < TL.eps) active = false;
+      if (!active) continue;   // uniform across the block
+      if (T.count && tid == 0) atomicAdd(T.count, 1ull);
+      eri_coop(K.la, K.lb, K.lc, K.ld, bra, T.prims, ket, T.prims, TL.boys.f64, sm);
+      const double deg = (bra.sa == bra.sb ? 1 : 2) * (ket.sa == ket.sb ? 1 : 2) * (bi == ki ? 1 : 2);
+      const double hdeg = deg * T.hf;
+      const double *__restrict__ D = T.Ds;
+      const int n = T.n, fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb;
+      auto Iat = [&](int a, int b, int c, int d) { return I[((a * NB + b) * NC + c) * ND + d]; };
+      // the six updates, threads over their output elements
+      const int n12 = NA * NB, n34 = NC * ND, n13 = NA * NC, n24 = NB * ND, n14 = NA * ND, n23 = NB * NC;
+      for (int t = tid; t < n12 + n34 + n13 + n24 + n14 + n23; t += kCoThreads) {
+        int x = t;
+        double s = 0;
+        if (x < n12) {
+          const int a = x / NB, b = x % NB;
+          for (int c = 0; c < NC; ++c)
+            for (int d = 0; d < ND; ++d) s += __ldg(D + (fc + c) * n + fd + d) * Iat(a, b, c, d);
+          atomicAdd(T.Gacc + (size_t)(fa + a) * n + fb + b, s * deg);
+          continue;
+        }
+        x -= n12;
+        if (x < n34) {
+          const int c = x / ND, d = x % ND;
+          for (int a = 0; a < NA; ++a)
+            for (int b = 0; b < NB; ++b) s += __ldg(D + (fa + a) * n + fb + b) * Iat(a, b, c, d);
+          atomicAdd(T.Gacc + (size_t)(fc + c) * n + fd + d, s * deg);
+          continue;
+        }
+        x -= n34;
+        if (x < n13) {
+          const int a = x / NC, c = x % NC;
+          for (int b = 0; b < NB; ++b)
+            for (int d = 0; d < ND; ++d) s += __ldg(D + (fb + b) * n + fd + d) * Iat(a, b, c, d);
+          atomicAdd(T.Gacc + (size_t)(fa + a) * n + fc + c, s * hdeg);
+          continue;
+        }
+        x -= n13;
+        if (x < n24) {
+          const int b = x / ND, d = x % ND;
+          for (int a = 0; a < NA; ++a)
+            for (int c = 0; c < NC; ++c) s += __ldg(D + (fa + a) * n + fc + c) * Iat(a, b, c, d);
+          atomicAdd(T.Gacc + (size_t)(fb + b) * n + fd + d, s * hdeg);
+          continue;
+        }
+        x -= n24;
+        if (x < n14) {
+          const int a = x / ND, d = x % ND;
+          for (int b = 0; b < NB; ++b)
+            for (int c = 0; c < NC; ++c) s += __ldg(D + (fb + b) * n + fc + c) * Iat(a, b, c, d);
+          atomicAdd(T.Gacc + (size_t)(fa + a) * n + fd + d, s * hdeg);
+          continue;
+        }
+        x -= n14;
+        {
+          const int b = x / NC, c = x % NC;
+          for (int a = 0; a < NA; ++a)
+            for (int d = 0; d < ND; ++d) s += __ldg(D + (fa + a) * n + fd + d) * Iat(a, b, c, d);
+          atomicAdd(T.Gacc + (size_t)(fb + b) * n + fc + c, s * hdeg);
+        }
+      }
     }
-    if (__all_sync(0xffffffffu, !active)) continue;
-    if (T.count) {
-      const unsigned cnt = __popc(__ballot_sync(0xffffffffu, active));
-      if (threadIdx.x == 0) atomicAdd(T.count, (unsigned long long)cnt);
-    }
-    if (active) eri_generic(K.la, K.lb, K.lc, K.ld, bra, T.prims, ket, T.prims, TL.boys.f64, scr, stride, 0);
-    const double deg = active ? (bra.sa == bra.sb ? 1 : 2) * (ket.sa == ket.sb ? 1 : 2) * (bi == ki ? 1 : 2) : 0.0;
-    const double hdeg = deg * T.hf;
-    const double *__restrict__ D = T.Ds;
-    const int n = T.n;
-    double *G = T.Gacc;
-    const int fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb;
-    auto Iat = [&](int a, int b, int c, int d) -> double { return active ? I[((a * NB + b) * NC + c) * ND + d] : 0.0; };
-    for (int a = 0; a < NA; ++a)
-      for (int b = 0; b < NB; ++b) {
-        double s = 0;
-        for (int c = 0; c < NC; ++c)
-          for (int d = 0; d < ND; ++d) s += __ldg(D + (fc + c) * n + fd + d) * Iat(a, b, c, d);
-        s = warp_sum(s * deg);
-        if (threadIdx.x == 0) atomicAdd(G + (size_t)(fa + a) * n + fb + b, s);
-      }
-    if (!active) continue;
-    for (int c = 0; c < NC; ++c)
-      for (int d = 0; d < ND; ++d) {
-        double s = 0;
-        for (int a = 0; a < NA; ++a)
-          for (int b = 0; b < NB; ++b) s += __ldg(D + (fa + a) * n + fb + b) * Iat(a, b, c, d);
-        atomicAdd(G + (size_t)(fc + c) * n + fd + d, s * deg);
-      }
-    for (int a = 0; a < NA; ++a)
-      for (int c = 0; c < NC; ++c) {
-        double s = 0;
-        for (int b = 0; b < NB; ++b)
-          for (int d = 0; d < ND; ++d) s += __ldg(D + (fb + b) * n + fd + d) * Iat(a, b, c, d);
-        atomicAdd(G + (size_t)(fa + a) * n + fc + c, s * hdeg);
-      }
-    for (int b = 0; b < NB; ++b)
-      for (int d = 0; d < ND; ++d) {
-        double s = 0;
-        for (int a = 0; a < NA; ++a)
-          for (int c = 0; c < NC; ++c) s += __ldg(D + (fa + a) * n + fc + c) * Iat(a, b, c, d);
-        atomicAdd(G + (size_t)(fb + b) * n + fd + d, s * hdeg);
-      }
-    for (int a = 0; a < NA; ++a)
-      for (int d = 0; d < ND; ++d) {
-        double s = 0;
-        for (int b = 0; b < NB; ++b)
-          for (int c = 0; c < NC; ++c) s += __ldg(D + (fb + b) * n + fc + c) * Iat(a, b, c, d);
-        atomicAdd(G + (size_t)(fa + a) * n + fd + d, s * hdeg);
-      }
-    for (int b = 0; b < NB; ++b)
-      for (int c = 0; c < NC; ++c) {
-        double s = 0;
-        for (int a = 0; a < NA; ++a)
-          for (int d = 0; d < ND; ++d) s += __ldg(D + (fa + a) * n + fd + d) * Iat(a, b, c, d);
-        atomicAdd(G + (size_t)(fb + b) * n + fc + c, s * hdeg);
-      }
   }
 }
 
 // ------------------------------------------------------------- coupling --
-__global__ void __launch_bounds__(128) cp_generic_kernel(const CPTask *__restrict__ tasks, TaskLaunch TL, GenClass K) {
-  size_t stride;
-  double *scr = thread_scratch(TL.scratch, &stride);
+__global__ void __launch_bounds__(kCoThreads) cp_coop_kernel(const CPTask *__restrict__ tasks, TaskLaunch TL,
+                                                             GenClass K) {
+  extern __shared__ double sm[];
+  const int tid = threadIdx.x;
   const int NA = ncart(K.la), NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld);
-  const Strided I{scr + (size_t)(kGenScratch - kGenOut) * stride, stride};
-  for (int blk = blockIdx.x; blk < TL.nblocks; blk += gridDim.x) {
-    const int t = find_task(tasks, TL.ntasks, blk);
-    const CPTask &T = tasks[t];
-    const int local = blk - T.blk0;
-    const int tx = local % T.nbx, ty = local / T.nbx;
-    const int kpos = tx * 32 + threadIdx.x;
-    const int bpos = ty * kWarpsPerBlock + threadIdx.y;
+  const double *I = sm + kCoOut;
+  for (int u = blockIdx.x; u < TL.nblocks * kCoUnitsPerTile; u += gridDim.x) {
+    int bpos, kpos0;
+    const CPTask &T = coop_unit(tasks, TL.ntasks, u, &bpos, &kpos0);
     if (bpos >= T.nbra) continue;
-    bool active = kpos < T.nket;
-    const int bi = T.bra0 + bpos, ki = T.ket0 + min(kpos, T.nket - 1);
-    const bool tiny = TL.split > 0.0 ? T.pa32[bi].Q * T.pb32[ki].Q * 0.999f < (float)TL.cut
-                                     : T.pa[bi].Q * T.pb[ki].Q * (1.0 - 1e-9) < TL.cut;
-    if (tiny) active = false;
-    if (TL.split > 0.0) {
-      const PairRec32 &b32 = T.pa32[bi];
-      const PairRec32 &k32 = T.pb32[ki];
-      float dm = 0.f;
-      if (T.DnA32) dm = __ldg(T.DnA32 + b32.sa * T.nshA + b32.sb);
-      if (T.DnB32) dm = fmaxf(dm, __ldg(T.DnB32 + k32.sa * T.nshB + k32.sb));
-      const float b = b32.Q * k32.Q * dm;
-      if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) active = false;
-    }
-    if (__all_sync(0xffffffffu, !active)) continue;
-    if (T.count) {
-      const unsigned cnt = __popc(__ballot_sync(0xffffffffu, active));
-      if (threadIdx.x == 0) atomicAdd(T.count, (unsigned long long)cnt);
-    }
-    const PairRec &bra = T.pa[bi];
-    const PairRec ket = T.pb[ki];
-    if (active) eri_generic(K.la, K.lb, K.lc, K.ld, bra, T.pra, ket, T.prb, TL.boys.f64, scr, stride, 0);
-    auto Iat = [&](int a, int b, int c, int d) -> double {
-      if (!active) return 0.0;
-      const double v = I[((a * NB + b) * NC + c) * ND + d];
-      return fabs(v) >= TL.cut ? v : 0.0;
-    };
-    const int fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb;
-    const bool abdiff = bra.sa != bra.sb, cddiff = ket.sa != ket.sb;
-    if (T.JA) {
-      const double wk = active ? (cddiff ? 2.0 : 1.0) * T.scale : 0.0;
-      for (int a = 0; a < NA; ++a)
-        for (int b = 0; b < NB; ++b) {
-          double s = 0;
+    for (int kpos = kpos0; kpos < kpos0 + 8 && kpos < T.nket; ++kpos) {
+      const int bi = T.bra0 + bpos, ki = T.ket0 + kpos;
+      const bool tiny = TL.split > 0.0 ? T.pa32[bi].Q * T.pb32[ki].Q * 0.999f < (float)TL.cut
+                                       : T.pa[bi].Q * T.pb[ki].Q * (1.0 - 1e-9) < TL.cut;
+      if (tiny) continue;
+      if (TL.split > 0.0) {
+        const PairRec32 &b32 = T.pa32[bi];
+        const PairRec32 &k32 = T.pb32[ki];
+        float dm = 0.f;
+        if (T.DnA32) dm = __ldg(T.DnA32 + b32.sa * T.nshA + b32.sb);
+        if (T.DnB32) dm = fmaxf(dm, __ldg(T.DnB32 + k32.sa * T.nshB + k32.sb));
+        const float b = b32.Q * k32.Q * dm;
+        if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) continue;
+      }
+      if (T.count && tid == 0) atomicAdd(T.count, 1ull);
+      const PairRec &bra = T.pa[bi];
+      const PairRec &ket = T.pb[ki];
+      eri_coop(K.la, K.lb, K.lc, K.ld, bra, T.pra, ket, T.prb, TL.boys.f64, sm);
+      auto Iat = [&](int a, int b, int c, int d) {
+        const double v = I[((a * NB + b) * NC + c) * ND + d];
+        return fabs(v) >= TL.cut ? v : 0.0;
+      };
+      const int fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb;
+      const bool abdiff = bra.sa != bra.sb, cddiff = ket.sa != ket.sb;
+      const int nja = T.JA ? NA * NB : 0, njb = T.JB ? NC * ND : 0;
+      for (int t = tid; t < nja + njb; t += kCoThreads) {
+        double s = 0;
+        if (t < nja) {
+          const int a = t / NB, b = t % NB;
           for (int c = 0; c < NC; ++c)
             for (int d = 0; d < ND; ++d) s += __ldg(T.DsB + (fc + c) * T.nB + fd + d) * Iat(a, b, c, d);
-          s = warp_sum(s * wk);
-          if (threadIdx.x == 0) {
-            atomicAdd(T.JA + (size_t)(fa + a) * T.nA + fb + b, s);
-            if (abdiff) atomicAdd(T.JA + (size_t)(fb + b) * T.nA + fa + a, s);
-          }
-        }
-    }
-    if (T.JB && active) {
-      const double wb = (abdiff ? 2.0 : 1.0) * T.scale;
-      for (int c = 0; c < NC; ++c)
-        for (int d = 0; d < ND; ++d) {
-          double s = 0;
+          s *= (cddiff ? 2.0 : 1.0) * T.scale;
+          atomicAdd(T.JA + (size_t)(fa + a) * T.nA + fb + b, s);
+          if (abdiff) atomicAdd(T.JA + (size_t)(fb + b) * T.nA + fa + a, s);
+        } else {
+          const int x = t - nja, c = x / ND, d = x % ND;
           for (int a = 0; a < NA; ++a)
             for (int b = 0; b < NB; ++b) s += __ldg(T.DsA + (fa + a) * T.nA + fb + b) * Iat(a, b, c, d);
-          s *= wb;
+          s *= (abdiff ? 2.0 : 1.0) * T.scale;
           atomicAdd(T.JB + (size_t)(fc + c) * T.nB + fd + d, s);
           if (cddiff) atomicAdd(T.JB + (size_t)(fd + d) * T.nB + fc + c, s);
         }
+      }
     }
   }
 }
 
 // -------------------------------------------------------- first quarter --
-__device__ __forceinline__ void it_role_rt(const Strided &I, int NA, int NB, int NC, int ND, int roleperm,
-                                           const double *__restrict__ Cs, int fmu, int fnu, int fl, int fs, int nmu,
-                                           int nnu, int nl, int ns, double *A, int nB, double cut) {
-  // roleperm selects how (mu, nu, l, s) map onto the quartet's (a, b, c, d)
-  for (int nu = 0; nu < nnu; ++nu)
-    for (int l = 0; l < nl; ++l)
-      for (int s = 0; s < ns; ++s) {
+// role r of the permutational orbit: (mu, nu, l, s) -> quartet indices (a, b, c, d)
+__device__ __forceinline__ void it_map(int r, int mu, int nu, int l, int s, int *a, int *b, int *c, int *d) {
+  switch (r) {
+    case 0: *a = mu; *b = nu; *c = l; *d = s; break;   // (a b|c d)
+    case 1: *a = nu; *b = mu; *c = l; *d = s; break;   // (b a|c d)
+    case 2: *a = mu; *b = nu; *c = s; *d = l; break;   // (a b|d c)
+    case 3: *a = nu; *b = mu; *c = s; *d = l; break;   // (b a|d c)
+    case 4: *a = l; *b = s; *c = mu; *d = nu; break;   // (c d|a b)
+    case 5: *a = l; *b = s; *c = nu; *d = mu; break;   // (d c|a b)
+    case 6: *a = s; *b = l; *c = mu; *d = nu; break;   // (c d|b a)
+    default: *a = s; *b = l; *c = nu; *d = mu; break;  // (d c|b a)
+  }
+}
+
+__global__ void __launch_bounds__(kCoThreads) it_coop_kernel(ITParams P, GenClass K) {
+  extern __shared__ double sm[];
+  const int tid = threadIdx.x;
+  const int NA = ncart(K.la), NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld);
+  const double *I = sm + kCoOut;
+  const long long nq = (long long)P.nbra * P.nket;
+  for (long long q = blockIdx.x; q < nq; q += gridDim.x) {
+    const int bpos = (int)(q / P.nket), kpos = (int)(q % P.nket);
+    if (P.triangle && kpos > bpos) continue;
+    const int bi = P.bra0 + bpos, ki = P.ket0 + kpos;
+    const PairRec &bra = P.pa[bi];
+    const PairRec &ket = P.pb[ki];
+    if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) continue;
+    if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) continue;
+    eri_coop(K.la, K.lb, K.lc, K.ld, bra, P.pra, ket, P.prb, P.boys.f64, sm);
+    const bool ab = bra.sa != bra.sb, cd = ket.sa != ket.sb;
+    const bool mirror = P.intra && bi != ki;
+    const int f[4] = {bra.fa, bra.fb, ket.fa, ket.fb};
+    const int nn[4] = {NA, NB, NC, ND};
+    for (int r = 0; r < 8; ++r) {
+      if ((r & 1) && !ab && r < 4) continue;
+      if ((r >= 2 && r < 4) && !cd) continue;
+      if (r >= 4 && !mirror) continue;
+      if ((r == 5 || r == 7) && !cd) continue;
+      if ((r == 6 || r == 7) && !ab) continue;
+      // index slots of (mu, nu, l, s) in role r
+      int sa, sb, sc, sd;
+      it_map(r, 0, 1, 2, 3, &sa, &sb, &sc, &sd);   // slot of quartet position a, b, c, d
+      int slot_of[4];
+      slot_of[sa] = 0; slot_of[sb] = 1; slot_of[sc] = 2; slot_of[sd] = 3;   // role index -> quartet position
+      const int nmu = nn[slot_of[0]], nnu = nn[slot_of[1]], nl = nn[slot_of[2]], ns = nn[slot_of[3]];
+      const int fmu = f[slot_of[0]], fnu = f[slot_of[1]], fl = f[slot_of[2]], fs = f[slot_of[3]];
+      for (int t = tid; t < nnu * nl * ns; t += kCoThreads) {
+        const int nu = t / (nl * ns), l = (t / ns) % nl, s = t % ns;
         double acc = 0;
         for (int mu = 0; mu < nmu; ++mu) {
           int a, b, c, d;
-          switch (roleperm) {
-            case 0: a = mu; b = nu; c = l; d = s; break;   // (a b|c d)
-            case 1: a = nu; b = mu; c = l; d = s; break;   // (b a|c d)
-            case 2: a = mu; b = nu; c = s; d = l; break;   // (a b|d c)
-            case 3: a = nu; b = mu; c = s; d = l; break;   // (b a|d c)
-            case 4: a = l; b = s; c = mu; d = nu; break;   // (c d|a b)
-            case 5: a = l; b = s; c = nu; d = mu; break;   // (d c|a b)
-            case 6: a = s; b = l; c = mu; d = nu; break;   // (c d|b a)
-            default: a = s; b = l; c = nu; d = mu; break;  // (d c|b a)
-          }
+          it_map(r, mu, nu, l, s, &a, &b, &c, &d);
           const double v = I[((a * NB + b) * NC + c) * ND + d];
-          if (fabs(v) > cut) acc += __ldg(Cs + fmu + mu) * v;
+          if (fabs(v) > P.cut) acc += __ldg(P.Cs + fmu + mu) * v;
         }
-        atomicAdd(A + ((size_t)(fnu + nu) * nB + fl + l) * nB + fs + s, acc);
+        atomicAdd(P.A + ((size_t)(fnu + nu) * P.nB + fl + l) * P.nB + fs + s, acc);
       }
-}
-
-__global__ void __launch_bounds__(128) it_generic_kernel(ITParams P, GenClass K) {
-  size_t stride;
-  double *scr = thread_scratch(P.scratch, &stride);
-  const int NA = ncart(K.la), NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld);
-  const Strided I{scr + (size_t)(kGenScratch - kGenOut) * stride, stride};
-  const int nbx = (P.nket + 31) / 32, nby = (P.nbra + kWarpsPerBlock - 1) / kWarpsPerBlock;
-  for (int blk = blockIdx.x; blk < nbx * nby; blk += gridDim.x) {
-    const int tx = blk % nbx, ty = blk / nbx;
-    const int kpos = tx * 32 + threadIdx.x;
-    const int bpos = ty * kWarpsPerBlock + threadIdx.y;
-    if (bpos >= P.nbra || kpos >= P.nket) continue;
-    if (P.triangle && kpos > bpos) continue;
-    const int bi = P.bra0 + bpos, ki = P.ket0 + kpos;
-    const PairRec bra = P.pa[bi];
-    const PairRec ket = P.pb[ki];
-    if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) continue;
-    if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) continue;
-    eri_generic(K.la, K.lb, K.lc, K.ld, bra, P.pra, ket, P.prb, P.boys.f64, scr, stride, 0);
-    const bool ab = bra.sa != bra.sb, cd = ket.sa != ket.sb;
-    const int fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb;
-    it_role_rt(I, NA, NB, NC, ND, 0, P.Cs, fa, fb, fc, fd, NA, NB, NC, ND, P.A, P.nB, P.cut);
-    if (ab) it_role_rt(I, NA, NB, NC, ND, 1, P.Cs, fb, fa, fc, fd, NB, NA, NC, ND, P.A, P.nB, P.cut);
-    if (cd) it_role_rt(I, NA, NB, NC, ND, 2, P.Cs, fa, fb, fd, fc, NA, NB, ND, NC, P.A, P.nB, P.cut);
-    if (ab && cd) it_role_rt(I, NA, NB, NC, ND, 3, P.Cs, fb, fa, fd, fc, NB, NA, ND, NC, P.A, P.nB, P.cut);
-    if (P.intra && bi != ki) {
-      it_role_rt(I, NA, NB, NC, ND, 4, P.Cs, fc, fd, fa, fb, NC, ND, NA, NB, P.A, P.nB, P.cut);
-      if (cd) it_role_rt(I, NA, NB, NC, ND, 5, P.Cs, fd, fc, fa, fb, ND, NC, NA, NB, P.A, P.nB, P.cut);
-      if (ab) it_role_rt(I, NA, NB, NC, ND, 6, P.Cs, fc, fd, fb, fa, NC, ND, NB, NA, P.A, P.nB, P.cut);
-      if (ab && cd) it_role_rt(I, NA, NB, NC, ND, 7, P.Cs, fd, fc, fb, fa, ND, NC, NB, NA, P.A, P.nB, P.cut);
     }
   }
 }
 
 // ------------------------------------------------------ MP2 transform input --
-__global__ void __launch_bounds__(128) mp2x_generic_kernel(MXParams P, GenClass K) {
-  size_t stride;
-  double *scr = thread_scratch(P.scratch, &stride);
-  const int NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld), NA = ncart(K.la);
-  const Strided I{scr + (size_t)(kGenScratch - kGenOut) * stride, stride};
-  const int nbx = (P.nket + 31) / 32, nby = (P.nbra + kWarpsPerBlock - 1) / kWarpsPerBlock;
-  for (int blk = blockIdx.x; blk < nbx * nby; blk += gridDim.x) {
-    const int tx = blk % nbx, ty = blk / nbx;
-    const int kpos = tx * 32 + threadIdx.x;
-    const int bpos = ty * kWarpsPerBlock + threadIdx.y;
-    if (bpos >= P.nbra || kpos >= P.nket) continue;
-    const int bi = P.bra0 + bpos, ki = P.ket0 + kpos;
-    const PairRec bra = P.pairs[bi];
-    const PairRec ket = P.pairs[ki];
+__global__ void __launch_bounds__(kCoThreads) mp2x_coop_kernel(MXParams P, GenClass K) {
+  extern __shared__ double sm[];
+  const int tid = threadIdx.x;
+  const int NA = ncart(K.la), NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld);
+  const double *I = sm + kCoOut;
+  const long long nq = (long long)P.nbra * P.nket;
+  for (long long q = blockIdx.x; q < nq; q += gridDim.x) {
+    const int bi = P.bra0 + (int)(q / P.nket), ki = P.ket0 + (int)(q % P.nket);
+    const PairRec &bra = P.pairs[bi];
+    const PairRec &ket = P.pairs[ki];
     if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) continue;
     if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) continue;
-    eri_generic(K.la, K.lb, K.lc, K.ld, bra, P.prims, ket, P.prims, P.boys.f64, scr, stride, 0);
+    eri_coop(K.la, K.lb, K.lc, K.ld, bra, P.prims, ket, P.prims, P.boys.f64, sm);
     const int col0 = __ldg(P.colbase + ki) - P.col_first;
     const bool two = bra.sa != bra.sb;
     const size_t n = P.n, ncol = P.ncol;
-    for (int a = 0; a < NA; ++a)
-      for (int b = 0; b < NB; ++b)
-        for (int c = 0; c < NC; ++c)
-          for (int d = 0; d < ND; ++d) {
-            const double v = I[((a * NB + b) * NC + c) * ND + d];
-            if (!(fabs(v) > P.cut)) continue;
-            const size_t col = col0 + c * ND + d;
-            const size_t i1 = ((bra.fa + a) * ncol + col) * n + bra.fb + b;
-            const size_t i2 = ((bra.fb + b) * ncol + col) * n + bra.fa + a;
-            if (P.X) {
-              P.X[i1] = v;
-              if (two) P.X[i2] = v;
-            } else {
-              // Xt[col * Kp + nu][mu] and the mirrored bra orientation
-              __nv_bfloat16 pc[kMaxPieces];
-              bf16_pieces(v, P.np, pc);
-              const size_t kp = P.Kp;
-              const size_t j1 = (col * kp + bra.fb + b) * kp + bra.fa + a;
-              const size_t j2 = (col * kp + bra.fa + a) * kp + bra.fb + b;
-              for (int k = 0; k < P.np; ++k) {
-                P.Xp[k][j1] = pc[k];
-                if (two) P.Xp[k][j2] = pc[k];
-              }
-            }
-          }
+    for (int t = tid; t < NA * NB * NC * ND; t += kCoThreads) {
+      const int a = t / (NB * NC * ND), b = (t / (NC * ND)) % NB, c = (t / ND) % NC, d = t % ND;
+      const double v = I[t];
+      if (!(fabs(v) > P.cut)) continue;
+      const size_t col = col0 + c * ND + d;
+      if (P.X) {
+        P.X[((bra.fa + a) * ncol + col) * n + bra.fb + b] = v;
+        if (two) P.X[((bra.fb + b) * ncol + col) * n + bra.fa + a] = v;
+      } else {
+        // Xt[col * Kp + nu][mu] and the mirrored bra orientation
+        __nv_bfloat16 pc[kMaxPieces];
+        bf16_pieces(v, P.np, pc);
+        const size_t kp = P.Kp;
+        const size_t j1 = (col * kp + bra.fb + b) * kp + bra.fa + a;
+        const size_t j2 = (col * kp + bra.fa + a) * kp + bra.fb + b;
+        for (int k = 0; k < P.np; ++k) {
+          P.Xp[k][j1] = pc[k];
+          if (two) P.Xp[k][j2] = pc[k];
+        }
+      }
+    }
   }
 }
 
 // ----------------------------------------------------------------- Schwarz --
-__global__ void __launch_bounds__(128) schwarz_generic_kernel(SchwarzParams P, int la, int lb) {
-  size_t stride;
-  double *scr = thread_scratch(P.scratch, &stride);
-  const Strided I{scr + (size_t)(kGenScratch - kGenOut) * stride, stride};
+__global__ void __launch_bounds__(kCoThreads) schwarz_coop_kernel(SchwarzParams P, int la, int lb) {
+  extern __shared__ double sm[];
   const int N = ncart(la) * ncart(lb);
-  for (int t = blockIdx.x * kGenericThreads + threadIdx.y * 32 + threadIdx.x; t < P.np;
-       t += gridDim.x * kGenericThreads) {
-    const PairRec pr = P.pairs[P.p0 + t];
-    eri_generic(la, lb, la, lb, pr, P.prims, pr, P.prims, P.boys.f64, scr, stride, 0);
-    double m = 0;
-    for (int i = 0; i < N; ++i) m = fmax(m, fabs(I[i * N + i]));
-    P.Q[P.p0 + t] = sqrt(m);
+  for (int t = blockIdx.x; t < P.np; t += gridDim.x) {
+    const PairRec &pr = P.pairs[P.p0 + t];
+    eri_coop(la, lb, la, lb, pr, P.prims, pr, P.prims, P.boys.f64, sm);
+    if (threadIdx.x == 0) {
+      double m = 0;
+      for (int i = 0; i < N; ++i) m = fmax(m, fabs(sm[kCoOut + i * N + i]));
+      P.Q[P.p0 + t] = sqrt(m);
+    }
   }
 }
 
@@ -335,9 +327,25 @@ const SZFn kSZ[5] = {&schwarz_kernel<0, 0>, &schwarz_kernel<1, 0>, &schwarz_kern
 
 GenClass gen_class(int pcb, int pck) { return GenClass{pc_la(pcb), pc_lb(pcb), pc_la(pck), pc_lb(pck)}; }
 
-}  // namespace
+template <typename F>
+cudaError_t coop_attr(F *fn) {
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCoSmemBytes);
+}
 
-int generic_scratch_doubles() { return kGenScratch; }
+bool coop_ready() {
+  static bool done = false;
+  if (done) return true;
+  if (coop_attr(jk_coop_kernel) != cudaSuccess || coop_attr(cp_coop_kernel) != cudaSuccess ||
+      coop_attr(it_coop_kernel) != cudaSuccess || coop_attr(mp2x_coop_kernel) != cudaSuccess ||
+      coop_attr(schwarz_coop_kernel) != cudaSuccess)
+    return false;
+  done = true;
+  return true;
+}
+
+unsigned coop_grid(long long units) { return (unsigned)std::max<long long>(1, std::min<long long>(units, kCoCtas)); }
+
+}  // namespace
 
 bool class_supported(int pcb, int pck) {
   return pcb >= 0 && pck >= 0 && pcb < kNumPairClasses && pck < kNumPairClasses;
@@ -351,8 +359,9 @@ cudaError_t launch_jk_tasks(int pcb, int pck, bool fp32, const JKTask *dtasks, c
   if (f) {
     f<<<tl.nblocks, kBlock, 0, s>>>(dtasks, tl);
   } else {
-    if (!tl.scratch) return cudaErrorInvalidValue;
-    jk_generic_kernel<<<kGenericBlocks, kBlock, 0, s>>>(dtasks, tl, gen_class(pcb, pck));
+    if (!coop_ready()) return cudaErrorInvalidValue;
+    jk_coop_kernel<<<coop_grid((long long)tl.nblocks * kCoUnitsPerTile), kCoThreads, kCoSmemBytes, s>>>(
+        dtasks, tl, gen_class(pcb, pck));
   }
   count_launches(1);
   return cudaGetLastError();
@@ -366,8 +375,9 @@ cudaError_t launch_cp_tasks(int pcb, int pck, bool fp32, const CPTask *dtasks, c
   if (f) {
     f<<<tl.nblocks, kBlock, 0, s>>>(dtasks, tl);
   } else {
-    if (!tl.scratch) return cudaErrorInvalidValue;
-    cp_generic_kernel<<<kGenericBlocks, kBlock, 0, s>>>(dtasks, tl, gen_class(pcb, pck));
+    if (!coop_ready()) return cudaErrorInvalidValue;
+    cp_coop_kernel<<<coop_grid((long long)tl.nblocks * kCoUnitsPerTile), kCoThreads, kCoSmemBytes, s>>>(
+        dtasks, tl, gen_class(pcb, pck));
   }
   count_launches(1);
   return cudaGetLastError();
@@ -381,8 +391,8 @@ cudaError_t launch_it(int pcb, int pck, const ITParams &p, cudaStream_t s) {
     const dim3 grid((unsigned)((p.nket + 31) / 32), (unsigned)((p.nbra + kWarpsPerBlock - 1) / kWarpsPerBlock));
     f<<<grid, kBlock, 0, s>>>(p);
   } else {
-    if (!p.scratch) return cudaErrorInvalidValue;
-    it_generic_kernel<<<kGenericBlocks, kBlock, 0, s>>>(p, gen_class(pcb, pck));
+    if (!coop_ready()) return cudaErrorInvalidValue;
+    it_coop_kernel<<<coop_grid((long long)p.nbra * p.nket), kCoThreads, kCoSmemBytes, s>>>(p, gen_class(pcb, pck));
   }
   count_launches(1);
   return cudaGetLastError();
@@ -396,8 +406,9 @@ cudaError_t launch_mp2x(int pcb, int pck, const MXParams &p, cudaStream_t s) {
     const dim3 grid((unsigned)((p.nket + 31) / 32), (unsigned)((p.nbra + kWarpsPerBlock - 1) / kWarpsPerBlock));
     f<<<grid, kBlock, 0, s>>>(p);
   } else {
-    if (!p.scratch) return cudaErrorInvalidValue;
-    mp2x_generic_kernel<<<kGenericBlocks, kBlock, 0, s>>>(p, gen_class(pcb, pck));
+    if (!coop_ready()) return cudaErrorInvalidValue;
+    mp2x_coop_kernel<<<coop_grid((long long)p.nbra * p.nket), kCoThreads, kCoSmemBytes, s>>>(p,
+                                                                                          gen_class(pcb, pck));
   }
   count_launches(1);
   return cudaGetLastError();
@@ -406,11 +417,11 @@ cudaError_t launch_mp2x(int pcb, int pck, const MXParams &p, cudaStream_t s) {
 cudaError_t launch_schwarz(int pc, const SchwarzParams &p, cudaStream_t s) {
   if (pc < 0 || pc >= kNumPairClasses) return cudaErrorNotSupported;
   if (p.np <= 0) return cudaSuccess;
-  if (pc < 5) {
+  if (2 * pc_L(pc) <= kTemplatedMaxL) {
     kSZ[pc]<<<(p.np + 127) / 128, 128, 0, s>>>(p);
   } else {
-    if (!p.scratch) return cudaErrorInvalidValue;
-    schwarz_generic_kernel<<<kGenericBlocks, kBlock, 0, s>>>(p, pc_la(pc), pc_lb(pc));
+    if (!coop_ready()) return cudaErrorInvalidValue;
+    schwarz_coop_kernel<<<coop_grid(p.np), kCoThreads, kCoSmemBytes, s>>>(p, pc_la(pc), pc_lb(pc));
   }
   count_launches(1);
   return cudaGetLastError();

@@ -88,24 +88,19 @@ struct TaskLaunch {
   int lower;              // 1: this launch takes the quartets below split
   double cut;             // coupling: |raw| < cut is dropped
   BoysTables boys;
-  double *scratch;        // generic (runtime-class) kernels: per-thread work arrays
-  int scratch_blocks;     // blocks the scratch holds slots for
 };
 
 // Kernel entry types of the class-templated launch tables (class_tables.cuh);
-// null entries are served by the generic runtime-class kernels (classes of
-// total angular momentum above kTemplatedMaxL).
+// null entries are served by the block-cooperative kernels (classes of total
+// angular momentum above kTemplatedMaxL).
 using JKFn = void (*)(const JKTask *, TaskLaunch);
 using CPFn = void (*)(const CPTask *, TaskLaunch);
 struct ITParams;
 using ITFn = void (*)(ITParams);
 __host__ __device__ constexpr int pc_L(int pc) { return pc_la(pc) + pc_lb(pc); }
-constexpr int kTemplatedMaxL = 6;   // classes above this total use the generic kernels
-
-// scratch of the generic kernels: doubles per thread, threads per block, blocks
-int generic_scratch_doubles();
-constexpr int kGenericThreads = 32 * kWarpsPerBlock;
-constexpr int kGenericBlocks = 152;
+// classes above this total angular momentum use the block-cooperative kernels
+// (the fully unrolled one-thread-per-quartet kernels of heavier classes spill)
+constexpr int kTemplatedMaxL = 4;
 
 // First-quarter transform A[nu][lam][sig] += sum_mu C_p(mu) (mu nu|lam sig).
 struct ITParams {
@@ -126,7 +121,6 @@ struct ITParams {
   double *A;
   BoysTables boys;
   double cut;             // raw values with |v| <= cut are dropped (1e-10)
-  double *scratch;        // generic classes only
 };
 
 struct SchwarzParams {
@@ -135,7 +129,6 @@ struct SchwarzParams {
   int p0, np;
   double *Q;              // per pair record
   BoysTables boys;
-  double *scratch;        // generic classes only
 };
 
 // MP2 transform input: raw integrals (mu nu|lam sig) of every significant bra
@@ -162,7 +155,6 @@ struct MXParams {
   int np;                 // pieces of the split output
   int Kp;                 // padded function count of the split layout
   BoysTables boys;
-  double *scratch;        // generic classes only
 };
 using MXFn = void (*)(MXParams);
 
@@ -170,8 +162,7 @@ using MXFn = void (*)(MXParams);
 inline int task_nbx(int nket) { return (nket + 31) / 32; }
 inline int task_nby(int nbra) { return (nbra + kWarpsPerBlock - 1) / kWarpsPerBlock; }
 
-// launchers (every class with l <= kMaxL; generic classes need tl.scratch /
-// p.scratch of kGenericBlocks * kGenericThreads * generic_scratch_doubles())
+// launchers (every class with l <= kMaxL)
 cudaError_t launch_jk_tasks(int pcb, int pck, bool fp32, const JKTask *dtasks, const TaskLaunch &tl,
                             cudaStream_t s);
 cudaError_t launch_cp_tasks(int pcb, int pck, bool fp32, const CPTask *dtasks, const TaskLaunch &tl,

@@ -402,16 +402,8 @@ struct TaskSet {
     d = nullptr;
     cap = 0;
   }
-  // true if a group of the set runs on the generic (runtime-class) kernels
-  bool needs_generic() const {
-    for (int c = 0; c < kNQC; ++c)
-      if (cnt[c] && class_generic(c / kNumPairClasses, c % kNumPairClasses)) return true;
-    return false;
-  }
 };
 
-// doubles of the generic kernels' work arrays (one slot per thread of their grid)
-size_t generic_scratch_size() { return (size_t)kGenericBlocks * kGenericThreads * generic_scratch_doubles(); }
 
 }  // namespace
 
@@ -438,7 +430,6 @@ struct LibintInterface {
   DevBuf<double> dD, dDs, dDn, dGacc, dG, dA, dC, dDsC, dJacc;
   DevBuf<float> dDs32, dDn32, dGacc32, dDsC32, dJacc32;
   DevBuf<unsigned long long> dcount;
-  DevBuf<double> dgen;       // work arrays of the generic kernels (species with d-shell pairs)
   long long last_quartets = -1;
   long long class_quartets[kNQC] = {0};
   TaskSet<JKTask> jk;        // cached J/K tasks of the handle's own buffers
@@ -459,7 +450,6 @@ struct LibintInterface {
     dDsC.release(); dJacc.release();
     dDs32.release(); dDn32.release(); dGacc32.release(); dDsC32.release(); dJacc32.release();
     dcount.release();
-    dgen.release();
     jk.release();
     cp.release();
     jk_ready = false;
@@ -469,7 +459,6 @@ struct LibintInterface {
     dirty = true;
   }
   int nshell() const { return (int)shells.size(); }
-  double *gen_scratch() { return dgen.ensure(generic_scratch_size()) ? dgen.p : nullptr; }
 
   bool ensure_base() {
     if (!dirty && stream) return true;
@@ -562,8 +551,7 @@ struct LibintInterface {
     if (!dq.ensure(L.h.size())) return false;
     for (int pc = 0; pc < kNumPairClasses; ++pc) {
       if (!L.count(pc)) continue;
-      SchwarzParams sp{L.d, L.dp, L.start[pc], L.count(pc), dq.p, boys, nullptr};
-      if (pc_L(pc) * 2 > kTemplatedMaxL && !(sp.scratch = gen_scratch())) return false;
+      SchwarzParams sp{L.d, L.dp, L.start[pc], L.count(pc), dq.p, boys};
       CK(launch_schwarz(pc, sp, stream));
     }
     std::vector<double> q(L.h.size());
@@ -647,9 +635,7 @@ struct LibintInterface {
     CK(cudaMemsetAsync(dGacc.p, 0, sizeof(double) * n * n, s));
     CK(cudaMemsetAsync(dGacc32.p, 0, sizeof(float) * n * n, s));
     CK(cudaMemsetAsync(dcount.p, 0, sizeof(unsigned long long) * kNQC, s));
-    double *scr = nullptr;
-    if (jk.needs_generic() && !(scr = gen_scratch())) return false;
-    if (!launch_jk_groups(jk, precision, split, boys, scr, s)) return false;
+    if (!launch_jk_groups(jk, precision, split, boys, s)) return false;
     CK(launch_symmetrize(dGacc.p, dGacc32.p, d_norma, n, 0.25, dGout, s));
     unsigned long long cnt[kNQC];
     CK(cudaMemcpyAsync(cnt, dcount.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
@@ -699,14 +685,11 @@ struct LibintInterface {
     return true;
   }
 
-  // scratch: work arrays of the generic kernels (needed when ts.needs_generic())
   static bool launch_jk_groups(const TaskSet<JKTask> &ts, int precision, double split, BoysTables boys,
-                               double *scratch, cudaStream_t s) {
+                               cudaStream_t s) {
     for (int c = 0; c < kNQC; ++c) {
       if (!ts.cnt[c]) continue;
       TaskLaunch tl{};
-      tl.scratch = scratch;
-      tl.scratch_blocks = kGenericBlocks;
       tl.ntasks = ts.cnt[c];
       tl.nblocks = ts.nblk[c];
       tl.eps = DBL_EPSILON;
@@ -778,13 +761,10 @@ bool add_cp_tasks(TaskSet<CPTask> &ts, LibintInterface *A, LibintInterface *B, c
 }
 
 // mode 0: FP64, 1: FP32 throughout, 2: split at `split` (FP64 above, FP32 below)
-bool launch_cp_groups(const TaskSet<CPTask> &ts, int mode, double split, BoysTables boys, double *scratch,
-                      cudaStream_t s) {
+bool launch_cp_groups(const TaskSet<CPTask> &ts, int mode, double split, BoysTables boys, cudaStream_t s) {
   for (int c = 0; c < kNQC; ++c) {
     if (!ts.cnt[c]) continue;
     TaskLaunch tl{};
-    tl.scratch = scratch;
-    tl.scratch_blocks = kGenericBlocks;
     tl.ntasks = ts.cnt[c];
     tl.nblocks = ts.nblk[c];
     tl.eps = DBL_EPSILON;
@@ -831,9 +811,7 @@ bool coupling(LibintInterface *A, LibintInterface *B, const double *dDa, const d
   SpeciesBufs bb{B->dDsC.p, B->dDsC32.p, nullptr, nullptr, B->dJacc.p, B->dJacc32.p};
   if (!add_cp_tasks(A->cp, A, B, ba, bb, dJa != nullptr, dJb != nullptr, 1.0)) return false;
   if (!A->cp.upload(s)) return false;
-  double *scr = nullptr;
-  if (A->cp.needs_generic() && !(scr = A->gen_scratch())) return false;
-  if (!launch_cp_groups(A->cp, fp32 ? 1 : 0, 0.0, A->boys, scr, s)) return false;
+  if (!launch_cp_groups(A->cp, fp32 ? 1 : 0, 0.0, A->boys, s)) return false;
   if (dJa) CK(launch_coupling_extract(A->dJacc.p, A->dJacc32.p, A->d_norma, nA, 1.0, 0, dJa, s));
   if (dJb) CK(launch_coupling_extract(B->dJacc.p, B->dJacc32.p, B->d_norma, nB, 1.0, 0, dJb, s));
   return true;
@@ -889,7 +867,6 @@ bool first_quarter(LibintInterface *A, LibintInterface *B, const double *hD, con
         q.ket0 = A->sig.start[ck];
         q.nket = A->sig.count(ck);
         q.triangle = cb == ck;
-        if (class_generic(cb, ck) && !q.scratch && !(q.scratch = A->gen_scratch())) return false;
         CK(launch_it(cb, ck, q, s));
       }
   } else {
@@ -910,7 +887,6 @@ bool first_quarter(LibintInterface *A, LibintInterface *B, const double *hD, con
         q.ket0 = B->all.start[ck];
         q.nket = B->all.count(ck);
         q.triangle = 0;
-        if (class_generic(cb, ck) && !q.scratch && !(q.scratch = A->gen_scratch())) return false;
         CK(launch_it(cb, ck, q, s));
       }
   }
@@ -1191,7 +1167,6 @@ struct LowdinGB300_Batch {
   DevBuf<float> Ds32, Dn32, Gacc32, Jacc32;
   DevBuf<unsigned long long> cnt;
   DevBuf<SpeciesSlot> slots;
-  DevBuf<double> gen;  // work arrays of the generic kernels (systems with d-shell pairs)
   long long total = 0;
   int nslots = 0;
   TaskSet<JKTask> jk;
@@ -1202,7 +1177,6 @@ struct LowdinGB300_Batch {
   ~LowdinGB300_Batch() {
     Ds.release(); Dn.release(); Gacc.release(); Jacc.release(); cnt.release(); slots.release();
     Ds32.release(); Dn32.release(); Gacc32.release(); Jacc32.release();
-    gen.release();
     jk.release(); cp.release();
   }
 
@@ -1275,7 +1249,6 @@ struct LowdinGB300_Batch {
     if (!slots.ensure(hs.size())) return false;
     CK(cudaMemcpyAsync(slots.p, hs.data(), hs.size() * sizeof(SpeciesSlot), cudaMemcpyHostToDevice, s));
     if (!jk.upload(s) || !cp.upload(s)) return false;
-    if ((jk.needs_generic() || cp.needs_generic()) && !gen.ensure(generic_scratch_size())) return false;
     CK(cudaStreamSynchronize(s));
     finalized = true;
     return true;
@@ -1291,8 +1264,8 @@ struct LowdinGB300_Batch {
     CK(cudaMemsetAsync(cnt.p, 0, 2 * kNQC * sizeof(unsigned long long), s));
     CK(launch_prepare_batch(slots.p, nslots, total, s));
     const int jk_mixed = precision & 1;
-    if (!LibintInterface::launch_jk_groups(jk, jk_mixed, jk_mixed ? split : 0.0, boys, gen.p, s)) return false;
-    if (!launch_cp_groups(cp, (precision & 2) ? 2 : 0, split, boys, gen.p, s)) return false;
+    if (!LibintInterface::launch_jk_groups(jk, jk_mixed, jk_mixed ? split : 0.0, boys, s)) return false;
+    if (!launch_cp_groups(cp, (precision & 2) ? 2 : 0, split, boys, s)) return false;
     CK(launch_finalize_batch(slots.p, nslots, total, s));
     return true;
   }
@@ -1461,12 +1434,6 @@ int LowdinGB300_twobody_device_noalloc(LibintInterface *lint, const double *dD, 
     }
     ts.nblk[c] = b;
   }
-  if (ts.needs_generic()) {
-    set_error("%s: species with d-shell pair classes of total angular momentum above %d need the generic "
-              "kernels' work arrays (%zu MB); use LowdinGB300_twobody_device",
-              __func__, kTemplatedMaxL, generic_scratch_size() * sizeof(double) >> 20);
-    return -1;
-  }
   if ((int)flat.size() > kNoAllocMaxTasks) {
     set_error("%s: %d tasks exceed the allocation-free limit of %d", __func__, (int)flat.size(), kNoAllocMaxTasks);
     return -1;
@@ -1485,7 +1452,7 @@ int LowdinGB300_twobody_device_noalloc(LibintInterface *lint, const double *dD, 
     set_error("%s: preparation failed", __func__);
     return -1;
   }
-  if (!LibintInterface::launch_jk_groups(ts, precision, split, lint->boys, nullptr, s)) return -1;
+  if (!LibintInterface::launch_jk_groups(ts, precision, split, lint->boys, s)) return -1;
   if (launch_symmetrize(Gacc, Gacc32, lint->d_norma, n, 0.25, dG, s) != cudaSuccess) {
     set_error("%s: symmetrisation failed", __func__);
     return -1;
@@ -1873,14 +1840,7 @@ bool mp2_direct(LibintInterface *L, const double *dD, const double *dC, const do
   // shell-block norms of D for the screening
   if (!L->dDs.ensure((size_t)n * n) || !L->dDn.ensure((size_t)nsh * nsh)) return false;
   CK(launch_prepare_density(dD, L->d_norma, L->d_shell_of, n, nsh, L->dDs.p, nullptr, L->dDn.p, nullptr, s));
-  double *scr = nullptr;
   const PairList &P = L->sig;
-  for (int cb = 0; cb < kNumPairClasses && !scr; ++cb)
-    for (int ck = 0; ck < kNumPairClasses; ++ck)
-      if (P.count(cb) && P.count(ck) && class_generic(cb, ck)) {
-        if (!(scr = L->gen_scratch())) return false;
-        break;
-      }
   MXParams &q = S.q;
   q.pairs = P.d;
   q.prims = P.dp;
@@ -1891,7 +1851,6 @@ bool mp2_direct(LibintInterface *L, const double *dD, const double *dC, const do
   q.cut = 1e-10;
   q.n = n;
   q.boys = L->boys;
-  q.scratch = scr;
   return precision == 0 ? mp2_fp64(S, x_budget_bytes, e2out, s) : mp2_split(S, precision + 1, x_budget_bytes, e2out, s);
 }
 

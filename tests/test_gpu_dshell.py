@@ -1,5 +1,5 @@
 """GPU parity with d shells: every quartet class up to (dd|dd), including the
-generic runtime-class kernels (total angular momentum 7 and 8), against the
+block-cooperative kernels (total angular momentum 5 to 8), against the
 oracle element-wise, and the golden APMO energy whose proton basis
 (NAKAI-5-SPD) carries d shells.
 
@@ -51,7 +51,7 @@ def test_twobody_d_shells_random_density(L, oracle):
     assert np.max(np.abs(G - ref)) < TOL_FOCK
     assert h.last_quartets() == oracle.last_quartet_count()
     cq = np.array(h.last_class_quartets()).reshape(6, 6)
-    assert cq[5, 5] > 0 and cq[5, 4] > 0       # generic classes evaluated
+    assert cq[5, 5] > 0 and cq[5, 4] > 0       # cooperative classes evaluated
     h.close()
 
 
@@ -86,7 +86,7 @@ def test_golden_apmo_proton_d_shells(L, oracle, golden):
 
 def test_coupling_generic_classes(L, oracle):
     """(dd|dd) coupling quartets: d-shell electrons against NAKAI-5-SPD-like
-    proton shells (the d shells of both species meet in the generic kernel)."""
+    proton shells (the d shells of both species meet in the cooperative kernel)."""
     sysd = S.water(d_shell=True)
     e = sysd["species"][0]
     O = e["shells"][0][3]
@@ -138,7 +138,7 @@ def test_first_quarter_coupling_d_shells(L, oracle, golden):
 
 
 def test_mixed_precision_d_shells_close_to_fp64(L):
-    """FP32 templated classes + FP64 generic classes under the split."""
+    """FP32 templated classes + FP64 cooperative classes under the split."""
     torch = pytest.importorskip("torch")
     sysd = _dwater2()
     sp = sysd["species"][0]
@@ -157,19 +157,24 @@ def test_mixed_precision_d_shells_close_to_fp64(L):
     h.close()
 
 
-def test_noalloc_rejects_generic_classes(L):
+def test_noalloc_d_shells_match(L):
+    """The allocation-free entry serves d-shell species too (the cooperative
+    kernels keep their work arrays in shared memory)."""
     torch = pytest.importorskip("torch")
     sp = _dwater2()["species"][0]
     h = L.Libint2Interface(sp, 1)
     h.init_2body_ints()
     n = h.nbasis
-    dD = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    rng = np.random.default_rng(37)
+    dD = torch.tensor(_sym(rng, n, 0.1), device="cuda")
     dG = torch.zeros_like(dD)
+    dG2 = torch.zeros_like(dD)
     st = torch.cuda.current_stream().cuda_stream
     rc = L.lib().LowdinGB300_twobody_device_noalloc(h.h, dD.data_ptr(), dG.data_ptr(), -0.5, 0, 0.0, st)
-    assert rc != 0
-    assert "generic" in L.last_error()
-    L.lib().LowdinGB300_clear_error()
+    assert rc == 0, L.last_error()
+    h.twobody_device(dD.data_ptr(), dG2.data_ptr(), -0.5, stream=st)
+    torch.cuda.synchronize()
+    assert float((dG - dG2).abs().max()) < 1e-12
     h.close()
 
 
