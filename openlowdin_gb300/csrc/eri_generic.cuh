@@ -1,30 +1,53 @@
-// Block-cooperative electron-repulsion integrals for the heavy quartet
-// classes (total angular momentum above kTemplatedMaxL).  Same recursion as
-// eri.cuh -- Obara-Saika vertical recursion on the bra then on the ket,
-// contraction, horizontal transfer on bra and ket -- with runtime loops: the
-// threads of one CTA evaluate one quartet together, every recursion level
-// split across the threads, the work arrays in shared memory.
+// Cooperative electron-repulsion integrals for the heavy quartet classes
+// (total angular momentum above kTemplatedMaxL).  Same recursion as eri.cuh --
+// Obara-Saika vertical recursion on the bra then on the ket, contraction,
+// horizontal transfer on bra and ket -- with runtime loops: the threads of a
+// group (a warp) evaluate one quartet together, every recursion level split
+// across the threads, the work arrays in shared memory.
 #pragma once
 #include "common.cuh"
 
 namespace lgb {
 
-constexpr int kGenMaxL1 = 2 * kMaxL;                                               // bra (or ket) total
-constexpr int kGenNcum = (kGenMaxL1 + 1) * (kGenMaxL1 + 2) * (kGenMaxL1 + 3) / 6;  // 35
-constexpr int kGenMaxL = 4 * kMaxL;                                                // 8
-// shared work array regions (doubles)
-constexpr int kGenVb = kGenNcum * (kGenMaxL + 1);  // bra nodes [e][m]
-constexpr int kGenVk = kGenNcum * 65;              // ket nodes: blocks [f][e][m], sum_f (L2-|f|+1) <= 65
-constexpr int kGenX = 31 * 31;                     // contracted [e][f] (largest for (dd|dd))
-constexpr int kGenH = 36 * 16 * 3;                 // first horizontal-transfer level (ket: 36 rows x 16 x 3)
-constexpr int kGenY = 36 * 31;                     // after the bra transfer
-constexpr int kGenOut = 36 * 36;                   // (dd|dd)
-constexpr int kCoVb = 0, kCoVk = kCoVb + kGenVb, kCoX = kCoVk + kGenVk, kCoH = kCoX + kGenX, kCoY = kCoH + kGenH,
-              kCoOut = kCoY + kGenY, kCoMisc = kCoOut + kGenOut;
-constexpr int kCoMiscN = 32;                        // scalars of the primitive quartet + Boys values
-constexpr int kCoDoubles = kCoMisc + kCoMiscN;
-constexpr int kCoKb = 40;                           // ket block offsets (ints) after the doubles
-constexpr size_t kCoSmemBytes = (size_t)kCoDoubles * sizeof(double) + kCoKb * sizeof(int);
+constexpr int kGenMaxL = 4 * kMaxL;   // largest total angular momentum of a quartet
+// Shared work arrays of one quartet evaluation, sized for its class (offsets
+// in doubles): bra nodes Vb[e][m], ket nodes Vk (blocks [f][e][m]), the
+// contracted X[e][f], the first horizontal-transfer level H, Y after the bra
+// transfer, the integrals, scalars of the primitive quartet, ket block
+// offsets (ints).
+struct CoLayout {
+  int vb, vk, x, h, y, out, misc, kb, total;
+};
+constexpr int kCoMiscN = 32;
+constexpr int kCoKbN = 20;   // doubles holding 40 ints
+
+__host__ __device__ inline CoLayout co_layout(int la, int lb, int lc, int ld) {
+  const int L1 = la + lb, L2 = lc + ld, L = L1 + L2;
+  const int NE = coff(L1 + 1), NF = coff(L2 + 1), nE = NE - coff(la), nF = NF - coff(lc);
+  const int NA = ncart(la), NB = ncart(lb), NC = ncart(lc), ND = ncart(ld);
+  int nvk = 0;
+  for (int f = 1; f < NF; ++f) nvk += NE * (L2 - clevel(f) + 1);
+  const int hb = lb == 2 ? (coff(la + 2) - coff(la)) * 3 * nF : 0;          // bra level 1 of 2
+  const int hk = ld == 2 ? NA * NB * (coff(lc + 2) - coff(lc)) * 3 : 0;     // ket level 1 of 2
+  CoLayout o;
+  o.vb = 0;
+  o.vk = o.vb + NE * (L + 1);
+  o.x = o.vk + nvk;
+  o.h = o.x + nE * nF;
+  o.y = o.h + (hb > hk ? hb : hk);
+  o.out = o.y + NA * NB * nF;
+  o.misc = o.out + NA * NB * NC * ND;
+  o.kb = o.misc + kCoMiscN;
+  o.total = (o.kb + kCoKbN + 1) & ~1;   // keep 16-byte alignment between groups
+  return o;
+}
+
+// cooperating threads: a warp (one quartet per warp) or a whole CTA
+struct WarpGroup {
+  __device__ __forceinline__ int tid() const { return threadIdx.x & 31; }
+  __device__ __forceinline__ int nt() const { return 32; }
+  __device__ __forceinline__ void sync() const { __syncwarp(); }
+};
 
 __device__ inline void boys_f64_rt(int L, double T, double *F, const double *__restrict__ tab) {
   if (T < kBoysTMax) {
@@ -45,20 +68,21 @@ __device__ inline void boys_f64_rt(int L, double T, double *F, const double *__r
 }
 
 // Raw contracted integrals of one quartet of runtime class (la lb|lc ld),
-// evaluated by all threads of the block; result in sm[kCoOut ...], row-major
-// (a, b, c, d).  Every thread of the block must call it (it synchronises the
-// block); the result is valid after the call returns.
-__device__ inline void eri_coop(int la, int lb, int lc, int ld, const PairRec &bra, const PrimRec *__restrict__ pbra,
-                                const PairRec &ket, const PrimRec *__restrict__ pket, const double *boys64,
-                                double *sm) {
-  const int tid = threadIdx.x + threadIdx.y * blockDim.x, nt = blockDim.x * blockDim.y;
+// evaluated by the threads of group g together; result in sm[Lo.out ...],
+// row-major (a, b, c, d).  Every thread of the group must call it (it
+// synchronises the group); the result is valid after the call returns.
+template <typename G>
+__device__ inline void eri_coop(G g, const CoLayout &Lo, int la, int lb, int lc, int ld, const PairRec &bra,
+                                const PrimRec *__restrict__ pbra, const PairRec &ket,
+                                const PrimRec *__restrict__ pket, const double *boys64, double *sm) {
+  const int tid = g.tid(), nt = g.nt();
   const int L1 = la + lb, L2 = lc + ld, L = L1 + L2, M = L + 1;
   const int NE = coff(L1 + 1), NF = coff(L2 + 1), E0 = coff(la), F0 = coff(lc);
   const int nE = NE - E0, nF = NF - F0;
-  double *Vb = sm + kCoVb, *Vk = sm + kCoVk, *X = sm + kCoX, *H = sm + kCoH, *Y = sm + kCoY, *out = sm + kCoOut;
-  double *misc = sm + kCoMisc;
-  int *kb = reinterpret_cast<int *>(sm + kCoDoubles);
-  __syncthreads();   // the previous quartet's readers of the work arrays are done
+  double *Vb = sm + Lo.vb, *Vk = sm + Lo.vk, *X = sm + Lo.x, *H = sm + Lo.h, *Y = sm + Lo.y, *out = sm + Lo.out;
+  double *misc = sm + Lo.misc;
+  int *kb = reinterpret_cast<int *>(sm + Lo.kb);
+  g.sync();   // the previous quartet's readers of the work arrays are done
   for (int i = tid; i < nE * nF; i += nt) X[i] = 0.0;
   if (tid == 0) {
     // first Vk entry of ket node f (nodes with |f| >= 1, blocks [e][m], m <= L2 - |f|)
@@ -70,7 +94,7 @@ __device__ inline void eri_coop(int la, int lb, int lc, int ld, const PairRec &b
   }
   for (int ib = 0; ib < bra.nprim; ++ib)
     for (int ik = 0; ik < ket.nprim; ++ik) {
-      __syncthreads();
+      g.sync();
       if (tid == 0) {
         const PrimRec pb = pbra[bra.prim0 + ib];
         const PrimRec pk = pket[ket.prim0 + ik];
@@ -96,7 +120,7 @@ __device__ inline void eri_coop(int la, int lb, int lc, int ld, const PairRec &b
         const double pref = pb.Kt * pk.Kt * sqrt(opq);
         for (int m = 0; m <= L; ++m) Vb[m] = pref * F[m];
       }
-      __syncthreads();
+      g.sync();
       const double rp = misc[12], rq = misc[13], o2p = misc[14], o2q = misc[15], o2pq = misc[16];
       // bra vertical recursion, one angular-momentum level at a time
       for (int lev = 1; lev <= L1; ++lev) {
@@ -111,7 +135,7 @@ __device__ inline void eri_coop(int la, int lb, int lc, int ld, const PairRec &b
           }
           Vb[e * M + m] = v;
         }
-        __syncthreads();
+        g.sync();
       }
       if (NF == 1) {
         for (int i = tid; i < nE; i += nt) X[i] += Vb[(E0 + i) * M];
@@ -140,19 +164,19 @@ __device__ inline void eri_coop(int la, int lb, int lc, int ld, const PairRec &b
           }
           Vk[kb[f] + e * mf + m] = v;
         }
-        __syncthreads();
+        g.sync();
       }
       for (int i = tid; i < nE * nF; i += nt) {
         const int e = E0 + i / nF, f = F0 + i % nF;
         X[i] += Vk[kb[f] + e * (L2 - clevel(f) + 1)];
       }
     }
-  __syncthreads();
+  g.sync();
   // bra transfer: X [a over totals la..la+lb][nF] -> Y [NA][NB][nF]
   const int NA = ncart(la), NB = ncart(lb), NC = ncart(lc), ND = ncart(ld);
   if (lb == 0) {
     for (int i = tid; i < NA * nF; i += nt) Y[i] = X[i];
-    __syncthreads();
+    g.sync();
   } else {
     for (int j = 1; j <= lb; ++j) {
       const int na = (j == lb) ? NA : coff(la + lb - j + 1) - E0, nb = ncart(j), pnb = j == 1 ? 1 : ncart(j - 1);
@@ -166,14 +190,14 @@ __device__ inline void eri_coop(int la, int lb, int lc, int ld, const PairRec &b
         const int apr = cplus(E0 + ar, d) - E0;
         dst[(ar * nb + bi) * nF + k] = src[(apr * pnb + bm) * nF + k] + bra.AB[d] * src[(ar * pnb + bm) * nF + k];
       }
-      __syncthreads();
+      g.sync();
     }
   }
   // ket transfer for every (a, b) row: Y [row][nF] -> out [row][NC][ND]
   const int R = NA * NB;
   if (ld == 0) {
     for (int i = tid; i < R * NC; i += nt) out[i] = Y[(i / NC) * nF + i % NC];
-    __syncthreads();
+    g.sync();
   } else {
     for (int j = 1; j <= ld; ++j) {
       const int nc = (j == ld) ? NC : coff(lc + ld - j + 1) - F0, nd = ncart(j), pnd = j == 1 ? 1 : ncart(j - 1);
@@ -195,7 +219,7 @@ __device__ inline void eri_coop(int la, int lb, int lc, int ld, const PairRec &b
         if (j == ld) out[(r * NC + cr) * ND + di] = v;
         else H[(r * nc + cr) * nd + di] = v;
       }
-      __syncthreads();
+      g.sync();
     }
   }
 }

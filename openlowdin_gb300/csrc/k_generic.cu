@@ -2,11 +2,12 @@
 // above kTemplatedMaxL, the Schwarz kernels, and the dispatch of every class
 // to its templated or cooperative kernel.
 //
-// A cooperative kernel runs a persistent grid of CTAs (three per SM fit their
-// shared work arrays); each CTA takes work units -- a bra pair and 8 ket pairs
-// of a task's 4 x 32 tile -- and evaluates their quartets one after another,
-// all 128 threads on each quartet (eri_coop), then digests the quartet's
-// integrals with the threads split over the output elements.  They compute in
+// In a cooperative kernel every warp is a worker with its own class-sized
+// shared work arrays (up to 4 warps per CTA, a persistent grid); a warp takes
+// work units -- a bra pair and 8 ket pairs of a task's 4 x 32 tile, or one
+// quartet -- and evaluates their quartets one after another, its 32 lanes
+// together on each (eri_coop), then digests the quartet's integrals with the
+// lanes split over the output elements.  They compute in
 // FP64 (also when a mixed launch asks for the FP32 half: the split decides
 // which quartets a launch takes, the quartets are evaluated in FP64 and
 // accumulated into the FP64 arrays).
@@ -34,15 +35,14 @@ const ITFn *const kIT[6] = {kIT_0, kIT_1, kIT_2, kIT_3, kIT_4, kIT_5};
 const MXFn *const kMX[6] = {kMX_0, kMX_1, kMX_2, kMX_3, kMX_4, kMX_5};
 
 const dim3 kBlock(32, kWarpsPerBlock);
-constexpr int kCoThreads = 128;
 constexpr int kCoUnitsPerTile = kWarpsPerBlock * 4;   // (bra row, group of 8 kets)
-constexpr int kCoCtas = 152 * 3;
+constexpr int kCoMaxSmem = 200 * 1024;                 // dynamic shared memory of a cooperative CTA
 
 struct GenClass {
   int la, lb, lc, ld;
 };
 
-// work unit u of a task-tiled launch -> tile, bra position, first ket position
+// work unit u of a task-tiled launch -> task, bra position, first ket position
 template <typename Task>
 __device__ __forceinline__ const Task &coop_unit(const Task *tasks, int ntasks, int u, int *bpos, int *kpos0) {
   const int blk = u / kCoUnitsPerTile, sub = u % kCoUnitsPerTile;
@@ -54,16 +54,24 @@ __device__ __forceinline__ const Task &coop_unit(const Task *tasks, int ntasks, 
   return T;
 }
 
+// every warp of a cooperative CTA is an independent worker with its own work arrays
+#define LGB_COOP_PROLOGUE(K)                                              \
+  extern __shared__ double smem[];                                        \
+  const CoLayout Lo = co_layout(K.la, K.lb, K.lc, K.ld);                  \
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;             \
+  const int nwarps = blockDim.x >> 5;                                     \
+  double *sm = smem + (size_t)warp * Lo.total;                            \
+  const double *I = sm + Lo.out;                                          \
+  const WarpGroup g;                                                      \
+  const long long w0 = (long long)blockIdx.x * nwarps + warp, wstep = (long long)gridDim.x * nwarps;
+
 // ------------------------------------------------------------------ J/K --
-__global__ void __launch_bounds__(kCoThreads) jk_coop_kernel(const JKTask *__restrict__ tasks, TaskLaunch TL,
-                                                             GenClass K) {
-  extern __shared__ double sm[];
-  const int tid = threadIdx.x;
+__global__ void __launch_bounds__(128) jk_coop_kernel(const JKTask *__restrict__ tasks, TaskLaunch TL, GenClass K) {
+  LGB_COOP_PROLOGUE(K)
   const int NA = ncart(K.la), NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld);
-  const double *I = sm + kCoOut;
-  for (int u = blockIdx.x; u < TL.nblocks * kCoUnitsPerTile; u += gridDim.x) {
+  for (long long u = w0; u < (long long)TL.nblocks * kCoUnitsPerTile; u += wstep) {
     int bpos, kpos0;
-    const JKTask &T = coop_unit(tasks, TL.ntasks, u, &bpos, &kpos0);
+    const JKTask &T = coop_unit(tasks, TL.ntasks, (int)u, &bpos, &kpos0);
     if (bpos >= T.nbra) continue;
     for (int kpos = kpos0; kpos < kpos0 + 8 && kpos < T.nket; ++kpos) {
       if (T.triangle && kpos > bpos) break;
@@ -81,17 +89,17 @@ __global__ void __launch_bounds__(kCoThreads) jk_coop_kernel(const JKTask *__res
       } else if (T.screen) {
         if (bra.Q * ket.Q * dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < TL.eps) active = false;
       }
-      if (!active) continue;   // uniform across the block
-      if (T.count && tid == 0) atomicAdd(T.count, 1ull);
-      eri_coop(K.la, K.lb, K.lc, K.ld, bra, T.prims, ket, T.prims, TL.boys.f64, sm);
+      if (!active) continue;   // uniform across the warp
+      if (T.count && lane == 0) atomicAdd(T.count, 1ull);
+      eri_coop(g, Lo, K.la, K.lb, K.lc, K.ld, bra, T.prims, ket, T.prims, TL.boys.f64, sm);
       const double deg = (bra.sa == bra.sb ? 1 : 2) * (ket.sa == ket.sb ? 1 : 2) * (bi == ki ? 1 : 2);
       const double hdeg = deg * T.hf;
       const double *__restrict__ D = T.Ds;
       const int n = T.n, fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb;
       auto Iat = [&](int a, int b, int c, int d) { return I[((a * NB + b) * NC + c) * ND + d]; };
-      // the six updates, threads over their output elements
+      // the six updates, lanes over their output elements
       const int n12 = NA * NB, n34 = NC * ND, n13 = NA * NC, n24 = NB * ND, n14 = NA * ND, n23 = NB * NC;
-      for (int t = tid; t < n12 + n34 + n13 + n24 + n14 + n23; t += kCoThreads) {
+      for (int t = lane; t < n12 + n34 + n13 + n24 + n14 + n23; t += 32) {
         int x = t;
         double s = 0;
         if (x < n12) {
@@ -146,15 +154,12 @@ __global__ void __launch_bounds__(kCoThreads) jk_coop_kernel(const JKTask *__res
 }
 
 // ------------------------------------------------------------- coupling --
-__global__ void __launch_bounds__(kCoThreads) cp_coop_kernel(const CPTask *__restrict__ tasks, TaskLaunch TL,
-                                                             GenClass K) {
-  extern __shared__ double sm[];
-  const int tid = threadIdx.x;
+__global__ void __launch_bounds__(128) cp_coop_kernel(const CPTask *__restrict__ tasks, TaskLaunch TL, GenClass K) {
+  LGB_COOP_PROLOGUE(K)
   const int NA = ncart(K.la), NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld);
-  const double *I = sm + kCoOut;
-  for (int u = blockIdx.x; u < TL.nblocks * kCoUnitsPerTile; u += gridDim.x) {
+  for (long long u = w0; u < (long long)TL.nblocks * kCoUnitsPerTile; u += wstep) {
     int bpos, kpos0;
-    const CPTask &T = coop_unit(tasks, TL.ntasks, u, &bpos, &kpos0);
+    const CPTask &T = coop_unit(tasks, TL.ntasks, (int)u, &bpos, &kpos0);
     if (bpos >= T.nbra) continue;
     for (int kpos = kpos0; kpos < kpos0 + 8 && kpos < T.nket; ++kpos) {
       const int bi = T.bra0 + bpos, ki = T.ket0 + kpos;
@@ -170,10 +175,10 @@ __global__ void __launch_bounds__(kCoThreads) cp_coop_kernel(const CPTask *__res
         const float b = b32.Q * k32.Q * dm;
         if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) continue;
       }
-      if (T.count && tid == 0) atomicAdd(T.count, 1ull);
+      if (T.count && lane == 0) atomicAdd(T.count, 1ull);
       const PairRec &bra = T.pa[bi];
       const PairRec &ket = T.pb[ki];
-      eri_coop(K.la, K.lb, K.lc, K.ld, bra, T.pra, ket, T.prb, TL.boys.f64, sm);
+      eri_coop(g, Lo, K.la, K.lb, K.lc, K.ld, bra, T.pra, ket, T.prb, TL.boys.f64, sm);
       auto Iat = [&](int a, int b, int c, int d) {
         const double v = I[((a * NB + b) * NC + c) * ND + d];
         return fabs(v) >= TL.cut ? v : 0.0;
@@ -181,7 +186,7 @@ __global__ void __launch_bounds__(kCoThreads) cp_coop_kernel(const CPTask *__res
       const int fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb;
       const bool abdiff = bra.sa != bra.sb, cddiff = ket.sa != ket.sb;
       const int nja = T.JA ? NA * NB : 0, njb = T.JB ? NC * ND : 0;
-      for (int t = tid; t < nja + njb; t += kCoThreads) {
+      for (int t = lane; t < nja + njb; t += 32) {
         double s = 0;
         if (t < nja) {
           const int a = t / NB, b = t % NB;
@@ -218,13 +223,11 @@ __device__ __forceinline__ void it_map(int r, int mu, int nu, int l, int s, int 
   }
 }
 
-__global__ void __launch_bounds__(kCoThreads) it_coop_kernel(ITParams P, GenClass K) {
-  extern __shared__ double sm[];
-  const int tid = threadIdx.x;
+__global__ void __launch_bounds__(128) it_coop_kernel(ITParams P, GenClass K) {
+  LGB_COOP_PROLOGUE(K)
   const int NA = ncart(K.la), NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld);
-  const double *I = sm + kCoOut;
   const long long nq = (long long)P.nbra * P.nket;
-  for (long long q = blockIdx.x; q < nq; q += gridDim.x) {
+  for (long long q = w0; q < nq; q += wstep) {
     const int bpos = (int)(q / P.nket), kpos = (int)(q % P.nket);
     if (P.triangle && kpos > bpos) continue;
     const int bi = P.bra0 + bpos, ki = P.ket0 + kpos;
@@ -232,7 +235,7 @@ __global__ void __launch_bounds__(kCoThreads) it_coop_kernel(ITParams P, GenClas
     const PairRec &ket = P.pb[ki];
     if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) continue;
     if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) continue;
-    eri_coop(K.la, K.lb, K.lc, K.ld, bra, P.pra, ket, P.prb, P.boys.f64, sm);
+    eri_coop(g, Lo, K.la, K.lb, K.lc, K.ld, bra, P.pra, ket, P.prb, P.boys.f64, sm);
     const bool ab = bra.sa != bra.sb, cd = ket.sa != ket.sb;
     const bool mirror = P.intra && bi != ki;
     const int f[4] = {bra.fa, bra.fb, ket.fa, ket.fb};
@@ -243,14 +246,16 @@ __global__ void __launch_bounds__(kCoThreads) it_coop_kernel(ITParams P, GenClas
       if (r >= 4 && !mirror) continue;
       if ((r == 5 || r == 7) && !cd) continue;
       if ((r == 6 || r == 7) && !ab) continue;
-      // index slots of (mu, nu, l, s) in role r
-      int sa, sb, sc, sd;
-      it_map(r, 0, 1, 2, 3, &sa, &sb, &sc, &sd);   // slot of quartet position a, b, c, d
-      int slot_of[4];
-      slot_of[sa] = 0; slot_of[sb] = 1; slot_of[sc] = 2; slot_of[sd] = 3;   // role index -> quartet position
-      const int nmu = nn[slot_of[0]], nnu = nn[slot_of[1]], nl = nn[slot_of[2]], ns = nn[slot_of[3]];
-      const int fmu = f[slot_of[0]], fnu = f[slot_of[1]], fl = f[slot_of[2]], fs = f[slot_of[3]];
-      for (int t = tid; t < nnu * nl * ns; t += kCoThreads) {
+      int qa, qb, qc, qd;
+      it_map(r, 0, 1, 2, 3, &qa, &qb, &qc, &qd);   // role index at quartet positions a, b, c, d
+      int pos[4];                                    // role index -> quartet position
+      pos[qa] = 0;
+      pos[qb] = 1;
+      pos[qc] = 2;
+      pos[qd] = 3;
+      const int nmu = nn[pos[0]], nnu = nn[pos[1]], nl = nn[pos[2]], ns = nn[pos[3]];
+      const int fmu = f[pos[0]], fnu = f[pos[1]], fl = f[pos[2]], fs = f[pos[3]];
+      for (int t = lane; t < nnu * nl * ns; t += 32) {
         const int nu = t / (nl * ns), l = (t / ns) % nl, s = t % ns;
         double acc = 0;
         for (int mu = 0; mu < nmu; ++mu) {
@@ -266,23 +271,21 @@ __global__ void __launch_bounds__(kCoThreads) it_coop_kernel(ITParams P, GenClas
 }
 
 // ------------------------------------------------------ MP2 transform input --
-__global__ void __launch_bounds__(kCoThreads) mp2x_coop_kernel(MXParams P, GenClass K) {
-  extern __shared__ double sm[];
-  const int tid = threadIdx.x;
-  const int NA = ncart(K.la), NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld);
-  const double *I = sm + kCoOut;
+__global__ void __launch_bounds__(128) mp2x_coop_kernel(MXParams P, GenClass K) {
+  LGB_COOP_PROLOGUE(K)
+  const int NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld), NA = ncart(K.la);
   const long long nq = (long long)P.nbra * P.nket;
-  for (long long q = blockIdx.x; q < nq; q += gridDim.x) {
+  for (long long q = w0; q < nq; q += wstep) {
     const int bi = P.bra0 + (int)(q / P.nket), ki = P.ket0 + (int)(q % P.nket);
     const PairRec &bra = P.pairs[bi];
     const PairRec &ket = P.pairs[ki];
     if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) continue;
     if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) continue;
-    eri_coop(K.la, K.lb, K.lc, K.ld, bra, P.prims, ket, P.prims, P.boys.f64, sm);
+    eri_coop(g, Lo, K.la, K.lb, K.lc, K.ld, bra, P.prims, ket, P.prims, P.boys.f64, sm);
     const int col0 = __ldg(P.colbase + ki) - P.col_first;
     const bool two = bra.sa != bra.sb;
     const size_t n = P.n, ncol = P.ncol;
-    for (int t = tid; t < NA * NB * NC * ND; t += kCoThreads) {
+    for (int t = lane; t < NA * NB * NC * ND; t += 32) {
       const int a = t / (NB * NC * ND), b = (t / (NC * ND)) % NB, c = (t / ND) % NC, d = t % ND;
       const double v = I[t];
       if (!(fabs(v) > P.cut)) continue;
@@ -307,15 +310,15 @@ __global__ void __launch_bounds__(kCoThreads) mp2x_coop_kernel(MXParams P, GenCl
 }
 
 // ----------------------------------------------------------------- Schwarz --
-__global__ void __launch_bounds__(kCoThreads) schwarz_coop_kernel(SchwarzParams P, int la, int lb) {
-  extern __shared__ double sm[];
-  const int N = ncart(la) * ncart(lb);
-  for (int t = blockIdx.x; t < P.np; t += gridDim.x) {
+__global__ void __launch_bounds__(128) schwarz_coop_kernel(SchwarzParams P, GenClass K) {
+  LGB_COOP_PROLOGUE(K)
+  const int N = ncart(K.la) * ncart(K.lb);
+  for (long long t = w0; t < P.np; t += wstep) {
     const PairRec &pr = P.pairs[P.p0 + t];
-    eri_coop(la, lb, la, lb, pr, P.prims, pr, P.prims, P.boys.f64, sm);
-    if (threadIdx.x == 0) {
+    eri_coop(g, Lo, K.la, K.lb, K.la, K.lb, pr, P.prims, pr, P.prims, P.boys.f64, sm);
+    if (lane == 0) {
       double m = 0;
-      for (int i = 0; i < N; ++i) m = fmax(m, fabs(sm[kCoOut + i * N + i]));
+      for (int i = 0; i < N; ++i) m = fmax(m, fabs(I[i * N + i]));
       P.Q[P.p0 + t] = sqrt(m);
     }
   }
@@ -329,7 +332,7 @@ GenClass gen_class(int pcb, int pck) { return GenClass{pc_la(pcb), pc_lb(pcb), p
 
 template <typename F>
 cudaError_t coop_attr(F *fn) {
-  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCoSmemBytes);
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kCoMaxSmem);
 }
 
 bool coop_ready() {
@@ -343,7 +346,19 @@ bool coop_ready() {
   return true;
 }
 
-unsigned coop_grid(long long units) { return (unsigned)std::max<long long>(1, std::min<long long>(units, kCoCtas)); }
+// launch shape of a cooperative kernel for class K: warps per CTA (each with
+// its class-sized work arrays), dynamic shared memory, grid over `units`
+struct CoopShape {
+  dim3 grid, block;
+  size_t smem;
+};
+CoopShape coop_shape(const GenClass &K, long long units) {
+  const size_t per = (size_t)co_layout(K.la, K.lb, K.lc, K.ld).total * sizeof(double);
+  int w = (int)std::min<size_t>(4, kCoMaxSmem / per);
+  if (w < 1) w = 1;
+  const long long ctas = std::max<long long>(1, std::min<long long>((units + w - 1) / w, 152LL * 16));
+  return CoopShape{dim3((unsigned)ctas), dim3((unsigned)(32 * w)), per * w};
+}
 
 }  // namespace
 
@@ -360,8 +375,9 @@ cudaError_t launch_jk_tasks(int pcb, int pck, bool fp32, const JKTask *dtasks, c
     f<<<tl.nblocks, kBlock, 0, s>>>(dtasks, tl);
   } else {
     if (!coop_ready()) return cudaErrorInvalidValue;
-    jk_coop_kernel<<<coop_grid((long long)tl.nblocks * kCoUnitsPerTile), kCoThreads, kCoSmemBytes, s>>>(
-        dtasks, tl, gen_class(pcb, pck));
+    const GenClass K = gen_class(pcb, pck);
+    const CoopShape c = coop_shape(K, (long long)tl.nblocks * kCoUnitsPerTile);
+    jk_coop_kernel<<<c.grid, c.block, c.smem, s>>>(dtasks, tl, K);
   }
   count_launches(1);
   return cudaGetLastError();
@@ -376,8 +392,9 @@ cudaError_t launch_cp_tasks(int pcb, int pck, bool fp32, const CPTask *dtasks, c
     f<<<tl.nblocks, kBlock, 0, s>>>(dtasks, tl);
   } else {
     if (!coop_ready()) return cudaErrorInvalidValue;
-    cp_coop_kernel<<<coop_grid((long long)tl.nblocks * kCoUnitsPerTile), kCoThreads, kCoSmemBytes, s>>>(
-        dtasks, tl, gen_class(pcb, pck));
+    const GenClass K = gen_class(pcb, pck);
+    const CoopShape c = coop_shape(K, (long long)tl.nblocks * kCoUnitsPerTile);
+    cp_coop_kernel<<<c.grid, c.block, c.smem, s>>>(dtasks, tl, K);
   }
   count_launches(1);
   return cudaGetLastError();
@@ -392,7 +409,9 @@ cudaError_t launch_it(int pcb, int pck, const ITParams &p, cudaStream_t s) {
     f<<<grid, kBlock, 0, s>>>(p);
   } else {
     if (!coop_ready()) return cudaErrorInvalidValue;
-    it_coop_kernel<<<coop_grid((long long)p.nbra * p.nket), kCoThreads, kCoSmemBytes, s>>>(p, gen_class(pcb, pck));
+    const GenClass K = gen_class(pcb, pck);
+    const CoopShape c = coop_shape(K, (long long)p.nbra * p.nket);
+    it_coop_kernel<<<c.grid, c.block, c.smem, s>>>(p, K);
   }
   count_launches(1);
   return cudaGetLastError();
@@ -407,8 +426,9 @@ cudaError_t launch_mp2x(int pcb, int pck, const MXParams &p, cudaStream_t s) {
     f<<<grid, kBlock, 0, s>>>(p);
   } else {
     if (!coop_ready()) return cudaErrorInvalidValue;
-    mp2x_coop_kernel<<<coop_grid((long long)p.nbra * p.nket), kCoThreads, kCoSmemBytes, s>>>(p,
-                                                                                          gen_class(pcb, pck));
+    const GenClass K = gen_class(pcb, pck);
+    const CoopShape c = coop_shape(K, (long long)p.nbra * p.nket);
+    mp2x_coop_kernel<<<c.grid, c.block, c.smem, s>>>(p, K);
   }
   count_launches(1);
   return cudaGetLastError();
@@ -421,7 +441,9 @@ cudaError_t launch_schwarz(int pc, const SchwarzParams &p, cudaStream_t s) {
     kSZ[pc]<<<(p.np + 127) / 128, 128, 0, s>>>(p);
   } else {
     if (!coop_ready()) return cudaErrorInvalidValue;
-    schwarz_coop_kernel<<<coop_grid(p.np), kCoThreads, kCoSmemBytes, s>>>(p, pc_la(pc), pc_lb(pc));
+    const GenClass K{pc_la(pc), pc_lb(pc), pc_la(pc), pc_lb(pc)};
+    const CoopShape c = coop_shape(K, p.np);
+    schwarz_coop_kernel<<<c.grid, c.block, c.smem, s>>>(p, K);
   }
   count_launches(1);
   return cudaGetLastError();

@@ -1,7 +1,11 @@
 import os
 import sys
 
-import pytest
+# the host eigensolver pool of the SCF drivers runs one LAPACK call per worker
+# thread; BLAS must not spawn its own threads under it (set before numpy loads)
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+
+import pytest  # noqa: E402
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
