@@ -1,0 +1,477 @@
+"""Continuous-batching SCF / SCF+MP2 serving on one GPU.
+
+Requests (a molecular system, "scf" or "scf+mp2") arrive over time.  The
+engine loop
+
+  1. admits waiting requests in arrival order while their estimated device
+     footprint fits the HBM budget and the active set has room,
+  2. (re)builds the library batch when the active set changed -- every active
+     job's species in one LowdinGB300_Batch, so one batch_fock call per
+     iteration builds the two-particle and coupling matrices of all of them,
+  3. runs one SCF iteration of every active job (openLOWDIN's scheme 3,
+     src/scf/MultiSCF.f90:276-440: each species updated from the previous
+     densities, Pulay DIIS over all species of a job),
+  4. retires converged jobs: "scf" jobs finish, "scf+mp2" jobs hand their
+     orbitals to an MP2 worker thread that runs LowdinGB300_mp2_direct on its
+     own CUDA stream, so their transforms overlap the next SCF iterations.
+
+Densities, Fock matrices, DIIS histories and the handles' Schwarz tables stay
+on the device for a job's whole life.  A job's result does not depend on the
+other jobs in the mix: its J/K and coupling tasks touch only its own buffers.
+"""
+from __future__ import annotations
+
+import queue
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import lint
+from .scf import _one_body, _orthogonaliser_np, n_occ, nuclear_repulsion
+from .systems import n_core
+
+HOST_EIGH_MAX = 512
+
+
+@dataclass
+class Request:
+    system: dict
+    kind: str = "scf"            # "scf" or "scf+mp2"
+    arrival: float = 0.0         # seconds after the start of the stream
+    rid: int = 0
+
+
+@dataclass
+class Result:
+    rid: int
+    kind: str
+    energy: float
+    e2: float | None
+    iterations: int
+    converged: bool
+    arrival: float
+    admitted: float
+    finished: float
+    nbasis: int
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+
+@dataclass
+class _Species:
+    n: int
+    occ: int
+    eta: float
+    H: object
+    S: object
+    X: object
+    P: object
+    G: object
+    J: object
+    Pin: object
+    Gb: object
+    Jb: object
+    Pref: object
+    Flast: object = None
+
+
+@dataclass
+class _Job:
+    req: Request
+    handles: list
+    sp: list
+    enuc: float
+    footprint: float
+    admitted: float
+    it: int = 0
+    e_old: float = float("nan")
+    energy: float = float("nan")
+    hist_F: list = field(default_factory=list)
+    hist_E: list = field(default_factory=list)
+    hist_B: list = field(default_factory=list)
+
+
+def footprint_bytes(sysd, kind: str, diis_size: int = 10, mp2_budget_gb: float = 8.0) -> float:
+    """Device bytes a job holds while active: per species 11 n^2 matrices plus
+    2 * diis_size history matrices (FP64), the handle's pair data, and for
+    MP2 jobs the transform's arrays (split-BF16 path: Y' in FP32, the integral
+    batch, the per-orbital square)."""
+    tot = 0.0
+    for sp in sysd["species"]:
+        n = sum((l + 1) * (l + 2) // 2 for l, _, _, _ in sp["shells"])
+        ns = len(sp["shells"])
+        tot += (11 + 2 * diis_size) * n * n * 8 + ns * ns * 300
+    if kind == "scf+mp2":
+        sp = sysd["species"][0]
+        n = sum((l + 1) * (l + 2) // 2 for l, _, _, _ in sp["shells"])
+        o = n_occ(sp)
+        v = n - o
+        ncols = n * (n + 1) / 2 * 1.2
+        kp = (n + 63) // 64 * 64
+        tot += v * o * ncols * 4 + mp2_budget_gb * 1e9 + v * kp * kp * 6 + o * v * v * 4
+    return tot
+
+
+class ServingEngine:
+    def __init__(self, device="cuda", precision="fp64", split=1e-5, hbm_budget_gb=150.0, max_active=256,
+                 diis_size=10, tol_energy=1e-8, tol_density=1e-6, max_iter=100, mp2_precision=None,
+                 mp2_budget_gb=8.0):
+        import torch
+        self.torch = torch
+        self.dev = torch.device(device)
+        self.precision = precision
+        self.split = split
+        self.budget = hbm_budget_gb * 1e9
+        self.max_active = max_active
+        self.diis_size = diis_size
+        self.tol_energy = tol_energy
+        self.tol_density = tol_density
+        self.max_iter = max_iter
+        self.mp2_precision = (2 if precision == "mixed" else 0) if mp2_precision is None else mp2_precision
+        self.mp2_budget_gb = mp2_budget_gb
+        self.stream = torch.cuda.current_stream(self.dev)
+        self.mp2_stream = torch.cuda.Stream(self.dev)
+        self._pool = None
+        # optional phase timing (set to {} before run): synchronises the device
+        # at each phase boundary, so only for diagnostics
+        self.trace = None
+        self._last = 0.0
+
+    def _tick(self, name):
+        if self.trace is None:
+            return
+        self.torch.cuda.synchronize(self.dev)
+        now = time.perf_counter()
+        self.trace[name] = self.trace.get(name, 0.0) + (now - self._last)
+        self._last = now
+
+    # ------------------------------------------------------------ helpers --
+    def _host_pool(self):
+        import concurrent.futures as cf
+        import os
+        if self._pool is None:
+            self._pool = cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)))
+        return self._pool
+
+    def _new_job(self, req: Request, now: float, footprint: float) -> _Job:
+        torch = self.torch
+        sysd = req.system
+        handles = [lint.Libint2Interface(sp, k + 1) for k, sp in enumerate(sysd["species"])]
+        H, S = _one_body(handles, sysd)
+        sps = []
+        for k, sp in enumerate(sysd["species"]):
+            n = handles[k].nbasis
+            Ht = torch.tensor(H[k], device=self.dev)
+            St = torch.tensor(S[k], device=self.dev)
+            Xt = torch.tensor(_orthogonaliser_np(S[k]), device=self.dev)
+            z = lambda: torch.zeros((n, n), dtype=torch.float64, device=self.dev)  # noqa: E731
+            sps.append(_Species(n, n_occ(sp), float(sp["eta"]), Ht, St, Xt, z(), z(), z(), z(), z(), z(), z()))
+        job = _Job(req, handles, sps, nuclear_repulsion(sysd), footprint, now)
+        for s, P in zip(job.sp, self._densities([(s, s.H) for s in job.sp])):
+            s.P.copy_(P)                                  # core-Hamiltonian guess
+            s.Flast = s.H.clone()
+        return job
+
+    def _densities(self, items):
+        return self._density_collect(self._density_submit(items))
+
+    def _density_submit(self, items):
+        """Start eta C_occ C_occ^T for a list of (species, F): small matrices are
+        diagonalised by LAPACK on the host pool (one transfer, futures returned
+        at once so the host work overlaps later GPU work), large ones by the
+        GPU solver."""
+        torch = self.torch
+        out = [None] * len(items)
+        host_idx, host_mats = [], []
+        for i, (s, F) in enumerate(items):
+            Fp = s.X.T @ F @ s.X
+            if s.n >= HOST_EIGH_MAX:
+                e, Cp = torch.linalg.eigh(Fp)
+                Co = s.X @ Cp[:, :s.occ]
+                out[i] = s.eta * Co @ Co.T
+            else:
+                host_idx.append(i)
+                host_mats.append(Fp)
+        futs = []
+        if host_idx:
+            sizes = [m.numel() for m in host_mats]
+            flat = torch.cat([m.reshape(-1) for m in host_mats]).cpu().numpy()
+            offs = np.cumsum([0] + sizes)
+
+            def work(j):
+                i = host_idx[j]
+                n = items[i][0].n
+                w, V = np.linalg.eigh(flat[offs[j]:offs[j + 1]].reshape(n, n))
+                return np.ascontiguousarray(V[:, :items[i][0].occ])
+
+            futs = [self._host_pool().submit(work, j) for j in range(len(host_idx))]
+        return items, out, host_idx, futs
+
+    def _density_collect(self, pending):
+        torch = self.torch
+        items, out, host_idx, futs = pending
+        if host_idx:
+            vecs = [f.result() for f in futs]
+            allv = torch.from_numpy(np.concatenate([v.reshape(-1) for v in vecs])).to(self.dev, non_blocking=True)
+            o = 0
+            for j, i in enumerate(host_idx):
+                s = items[i][0]
+                Cp = allv[o:o + s.n * s.occ].reshape(s.n, s.occ)
+                o += s.n * s.occ
+                Co = s.X @ Cp
+                out[i] = s.eta * Co @ Co.T
+        return out
+
+    def _build_batch(self, jobs):
+        b = lint.Batch()
+        for job in jobs:
+            sps = job.req.system["species"]
+            b.add_system(job.handles, [sp["charge"] for sp in sps], [sp["kappa"] / sp["eta"] for sp in sps],
+                         [1 if sp["n_particles"] > 1 else 0 for sp in sps],
+                         [s.Pin for s in job.sp], [s.Gb for s in job.sp], [s.Jb for s in job.sp])
+        b.finalize(self.stream.cuda_stream)
+        return b
+
+    # --------------------------------------------------------- SCF step --
+    def _iterate(self, jobs, batch):
+        """One SCF iteration of every job of the list; returns the jobs that
+        converged (or ran out of iterations)."""
+        return self._iter_finish(self._iter_start(jobs, batch))
+
+    def _iter_start(self, jobs, batch):
+        """Fock build, assembly and DIIS of an SCF iteration; the eigensolves are
+        left running on the host pool."""
+        torch = self.torch
+        mixed = self.precision == "mixed"
+        for job in jobs:
+            full = (not mixed) or job.it == 0
+            for s in job.sp:
+                if full:
+                    s.Pin.copy_(s.P)
+                else:
+                    torch.sub(s.P, s.Pref, out=s.Pin)
+        self._tick("other")
+        batch.fock(3 if mixed else 0, self.split, self.stream.cuda_stream)
+        self._tick("fock")
+        stats = []
+        dmats = []
+        for job in jobs:
+            full = (not mixed) or job.it == 0
+            Fs, Es = [], []
+            energy = torch.tensor(job.enuc, dtype=torch.float64, device=self.dev)
+            for s in job.sp:
+                if full:
+                    s.G.copy_(s.Gb)
+                    s.J.copy_(s.Jb)
+                else:
+                    s.G += s.Gb
+                    s.J += s.Jb
+                s.Pref.copy_(s.P)
+                F = s.H + s.G + s.J
+                energy = energy + torch.sum(s.P * (s.H + 0.5 * s.G + 0.5 * s.J))
+                FPS = F @ s.P @ s.S
+                Fs.append(F)
+                Es.append(s.X.T @ (FPS - FPS.T) @ s.X)
+            job.hist_F.append(Fs)
+            job.hist_E.append(Es)
+            if len(job.hist_F) > self.diis_size:
+                job.hist_F.pop(0)
+                job.hist_E.pop(0)
+                job.hist_B.pop(0)
+                job.hist_B = [b[1:] for b in job.hist_B]
+            h = len(job.hist_F)
+            row = torch.stack([sum(torch.sum(e * f) for e, f in zip(Es, job.hist_E[j])) for j in range(h)])
+            job.hist_B.append(row)
+            stats.append(energy)
+        self._tick("assemble")
+        # DIIS coefficients of all jobs: their error-product rows in one
+        # transfer, the small Pulay systems solved on the host
+        flat = torch.cat([torch.cat(job.hist_B) for job in jobs]).cpu().numpy()
+        o = 0
+        coefs = []
+        for job in jobs:
+            h = len(job.hist_F)
+            B = np.zeros((h + 1, h + 1))
+            for i in range(h):
+                B[i, :i + 1] = flat[o:o + i + 1]
+                B[:i + 1, i] = flat[o:o + i + 1]
+                o += len(job.hist_B[i])
+            B[:h, :h] /= max(abs(B[h - 1, h - 1]), 1e-300)
+            B[h, :h] = B[:h, h] = -1.0
+            rhs = np.zeros(h + 1)
+            rhs[h] = -1.0
+            coefs.append(np.linalg.lstsq(B, rhs, rcond=None)[0][:h] if h >= 2 else None)
+        for job, c in zip(jobs, coefs):
+            h = len(job.hist_F)
+            for k, s in enumerate(job.sp):
+                Fx = job.hist_F[-1][k] if c is None else sum(float(c[j]) * job.hist_F[j][k] for j in range(h))
+                dmats.append((s, Fx))
+        self._tick("diis")
+        return jobs, stats, self._density_submit(dmats)
+
+    def _iter_finish(self, started):
+        """Collect the eigensolves of an iteration started by _iter_start: new
+        densities, convergence test."""
+        torch = self.torch
+        jobs, stats, pending = started
+        newP = self._density_collect(pending)
+        self._tick("density")
+        dP = []
+        k = 0
+        for job in jobs:
+            d = torch.zeros((), dtype=torch.float64, device=self.dev)
+            for s in job.sp:
+                Pn = newP[k]
+                k += 1
+                d = torch.maximum(d, torch.sqrt(torch.mean((Pn - s.P) ** 2)))
+                s.Flast = job.hist_F[-1][job.sp.index(s)]
+                s.P.copy_(Pn)
+            dP.append(d)
+        vals = torch.stack([torch.stack(stats), torch.stack(dP)]).cpu().numpy()
+        self._tick("convergence")
+        done = []
+        for q, job in enumerate(jobs):
+            job.it += 1
+            e, d = float(vals[0, q]), float(vals[1, q])
+            conv = abs(e - job.e_old) < self.tol_energy and d < self.tol_density
+            job.e_old = e
+            job.energy = e
+            job.converged = conv
+            if conv or job.it >= self.max_iter:
+                done.append(job)
+        return done
+
+    # --------------------------------------------------------------- MP2 --
+    def _mp2_worker(self, inbox, results, start):
+        torch = self.torch
+        while True:
+            item = inbox.get()
+            if item is None:
+                return
+            job, C, eps, P = item
+            try:
+                self._mp2_one(job, C, eps, P, results, start)
+            finally:
+                with self._lock:
+                    self._used -= job.footprint
+
+    def _mp2_one(self, job, C, eps, P, results, start):
+        torch = self.torch
+        sysd = job.req.system
+        sp = sysd["species"][0]
+        with torch.cuda.stream(self.mp2_stream):
+            dC = torch.tensor(np.ascontiguousarray(C.T), device=self.dev)
+            dD = torch.tensor(P, device=self.dev)
+            e2 = job.handles[0].mp2_direct(dD.data_ptr(), dC.data_ptr(), eps, n_occ(sp), n_core(sysd),
+                                           self.mp2_precision, self.mp2_budget_gb,
+                                           stream=self.mp2_stream.cuda_stream)
+        results.append(self._finish(job, e2, start))
+
+    def _finish(self, job, e2, start):
+        now = time.perf_counter() - start
+        for h in job.handles:
+            h.close()
+        return Result(job.req.rid, job.req.kind, job.energy, e2, job.it, bool(getattr(job, "converged", False)),
+                      job.req.arrival, job.admitted, now, job.sp[0].n)
+
+    # -------------------------------------------------------------- loop --
+    def run(self, requests, realtime=True, on_iteration=None):
+        """Serve `requests` (sorted by arrival).  realtime: requests become
+        visible at start + arrival; otherwise all are visible at once.
+        Returns the results in completion order.
+
+        Active jobs form two cohorts, each with its own library batch, worked
+        alternately: while one cohort's eigensolves run on the host pool, the
+        other cohort's Fock build runs on the GPU."""
+        torch = self.torch
+        pending = sorted(requests, key=lambda r: r.arrival)
+        results = []
+        cohorts = [[], []]
+        batches = [None, None]
+        dirty = [True, True]
+        inflight = [None, None]
+        self._used = 0.0
+        self._lock = threading.Lock()
+        inbox = queue.Queue()
+        start = time.perf_counter()
+        worker = threading.Thread(target=self._mp2_worker, args=(inbox, results, start), daemon=True)
+        worker.start()
+        pi = 0
+        step = 0
+
+        def retire(done):
+            for job in done:
+                for c in (0, 1):
+                    if job in cohorts[c]:
+                        cohorts[c].remove(job)
+                        dirty[c] = True
+                if job.req.kind == "scf+mp2":
+                    sp0 = job.sp[0]
+                    Fp = (sp0.X.T @ sp0.Flast @ sp0.X).cpu().numpy()
+                    w, V = np.linalg.eigh(Fp)
+                    C = sp0.X.cpu().numpy() @ V
+                    torch.cuda.current_stream(self.dev).synchronize()
+                    inbox.put((job, C, w, sp0.P.cpu().numpy()))
+                else:
+                    results.append(self._finish(job, None, start))
+                    with self._lock:
+                        self._used -= job.footprint
+
+        try:
+            while pi < len(pending) or cohorts[0] or cohorts[1] or inflight[0] or inflight[1]:
+                c = step % 2
+                step += 1
+                # finish this cohort's previous iteration (its eigensolves ran
+                # while the other cohort used the GPU)
+                if inflight[c] is not None:
+                    retire(self._iter_finish(inflight[c]))
+                    inflight[c] = None
+                # admission in arrival order under the HBM budget
+                now = time.perf_counter() - start
+                nact = len(cohorts[0]) + len(cohorts[1])
+                while pi < len(pending) and (not realtime or pending[pi].arrival <= now) and nact < self.max_active:
+                    req = pending[pi]
+                    fp = footprint_bytes(req.system, req.kind, self.diis_size, self.mp2_budget_gb)
+                    with self._lock:
+                        if (nact or self._used > 0) and self._used + fp > self.budget:
+                            break
+                        self._used += fp
+                    self._tick("other")
+                    cohorts[c].append(self._new_job(req, now, fp))
+                    self._tick("admit")
+                    dirty[c] = True
+                    nact += 1
+                    pi += 1
+                if not cohorts[c]:
+                    if not cohorts[1 - c] and inflight[1 - c] is None and pi < len(pending):
+                        # idle: next arrival, or memory held by MP2 transforms still running
+                        time.sleep(max(0.001, min(0.05, pending[pi].arrival - (time.perf_counter() - start))))
+                    continue
+                if dirty[c]:
+                    if batches[c] is not None:
+                        batches[c].close()
+                    self._tick("other")
+                    batches[c] = self._build_batch(cohorts[c])
+                    self._tick("batch_build")
+                    dirty[c] = False
+                inflight[c] = self._iter_start(list(cohorts[c]), batches[c])
+                if on_iteration is not None:
+                    on_iteration(len(cohorts[0]) + len(cohorts[1]))
+        finally:
+            inbox.put(None)
+            worker.join()
+            for b in batches:
+                if b is not None:
+                    b.close()
+        return results
+
+
+def latency_stats(results):
+    lat = np.array([r.latency for r in results])
+    if not len(lat):
+        return {"p50_s": None, "p99_s": None}
+    return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99))}

@@ -189,5 +189,20 @@ def chain_molecule(seed: int, n_atoms=None, min_atoms=3, max_atoms=30):
             "name": f"chain{len(elems)}-s{seed}"}
 
 
+def chain_for_basis(seed: int, target_nbf: int, max_atoms: int = 400):
+    """The chain generator grown (same seed, more atoms) until the electron
+    basis reaches target_nbf functions."""
+    for n in range(3, max_atoms + 1):
+        m = chain_molecule(seed, n_atoms=n)
+        if nbasis(m["species"][0]) >= target_nbf:
+            return m
+    return m
+
+
+def n_core(sysd) -> int:
+    """Frozen-core orbitals: one 1s orbital per atom heavier than He."""
+    return int(sum(1 for z in sysd["point_charges"] if z > 2.0))
+
+
 def nbasis(species) -> int:
     return int(sum((l + 1) * (l + 2) // 2 for l, _, _, _ in species["shells"]))
