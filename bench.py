@@ -50,6 +50,11 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=8, help="molecules per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-stream section")
+    ap.add_argument("--no-mp2", action="store_true", help="skip the MP2 transform section")
+    ap.add_argument("--serve-requests", type=int, default=40)
+    ap.add_argument("--serve-rate", type=float, default=100.0, help="Poisson arrival rate (req/s)")
+    ap.add_argument("--mp2-waters", type=int, default=8)
     ap.add_argument("--profile-fock", type=int, default=0,
                     help="profiling case: N batched Fock builds of the step's molecules at the "
                          "core-Hamiltonian-guess densities, then exit")
@@ -139,6 +144,108 @@ class ClockSampler:
         sm.sort()
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- serving --
+def serving_requests(n, rate, seed=0, lo=30, hi=300, mp2_frac=0.3):
+    """Seeded open-loop stream: Poisson arrivals, chain molecules with sizes
+    log-uniform in [lo, hi] functions, mp2_frac of the requests SCF+MP2."""
+    import numpy as np
+    from openlowdin_gb300 import serve, systems as S
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t, reqs = 0.0, []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate)
+        nbf = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        kind = "scf+mp2" if rng.random() < mp2_frac else "scf"
+        reqs.append(serve.Request(S.chain_for_basis(10_000 + seed * 100_000 + i, nbf), kind, t, i))
+    return reqs
+
+
+def serving_section(args):
+    """The continuous-batching engine on a bounded sample of the serving
+    stream, plain FP64 and mixed, same requests."""
+    import numpy as np
+    from openlowdin_gb300 import serve
+    warm = serving_requests(6, 1000.0, seed=9)
+    for prec in ("fp64", "mixed"):
+        serve.ServingEngine(precision=prec).run(warm, realtime=False)
+    reqs = serving_requests(args.serve_requests, args.serve_rate)
+    out = {"requests": len(reqs), "arrivals": f"Poisson, {args.serve_rate:g} req/s",
+           "sizes": "chain molecules (H/C/N/O generator), 30-300 functions log-uniform", "mp2_fraction": 0.3,
+           "hbm_budget_gb": 150, "note": "bounded sample of the 10,000-request stream (30-1200 functions) "
+                                         "so the benchmark finishes in minutes"}
+    res = {}
+    for prec in ("fp64", "mixed"):
+        eng = serve.ServingEngine(precision=prec)
+        t0 = time.perf_counter()
+        r = eng.run(reqs)
+        wall = time.perf_counter() - t0
+        res[prec] = {x.rid: x for x in r}
+        lat = serve.latency_stats(r)
+        out["plain" if prec == "fp64" else "mixed"] = {
+            "solves_per_s": len(r) / wall, "p50_s": lat["p50_s"], "p99_s": lat["p99_s"], "wall_s": wall,
+            "converged": int(sum(x.converged for x in r))}
+    both = [i for i in res["fp64"] if res["fp64"][i].converged and res["mixed"][i].converged]
+    de = [abs(res["mixed"][i].energy - res["fp64"][i].energy) for i in both]
+    de2 = [abs(res["mixed"][i].e2 - res["fp64"][i].e2) for i in both if res["fp64"][i].e2 is not None]
+    out["jobs_converged_in_both"] = len(both)
+    out["unconverged_jobs"] = sorted(set(res["fp64"]) - set(both))
+    out["max_abs_dE_mixed_vs_plain_Eh"] = float(max(de)) if de else None
+    out["max_abs_dE_mp2_mixed_vs_plain_Eh"] = float(max(de2)) if de2 else None
+    out["throughput_ratio_mixed_over_plain"] = out["mixed"]["solves_per_s"] / out["plain"]["solves_per_s"]
+    return out
+
+
+def mp2_section(args):
+    """MP2 four-index transform of a d-shell water cluster: FP64 (cuBLAS
+    DGEMM) vs split-BF16 tensor cores (3 pieces, 8 products), same SCF
+    orbitals; plus the tensor-core GEMM engine alone on the transform's
+    first-quarter shape."""
+    import numpy as np
+    import torch
+    from openlowdin_gb300 import lint, systems as S
+    from openlowdin_gb300.batch_scf import BatchSCF
+    nw = args.mp2_waters
+    sysd = S.water_cluster(nw, seed=0, o_d=True)
+    sp = sysd["species"][0]
+    s = BatchSCF([sysd])
+    r = s.solve(tol_energy=1e-9, tol_density=1e-7)[0]
+    s.close()
+    h = lint.Libint2Interface(sp, 1)
+    dD = torch.tensor(r.densities[0], device="cuda")
+    dC = torch.tensor(np.ascontiguousarray(r.coefficients[0].T), device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    nocc, nfz = 5 * nw, nw
+    out = {"system": f"{nw} waters, one Cartesian d (1.2) on O: {h.nbasis} functions, {nocc - nfz} active "
+                     f"occupied, {h.nbasis - nocc} virtual, frozen core {nfz}"}
+    e2 = {}
+    for prec, name in ((2, "split_bf16_tensor_cores"), (0, "fp64_dgemm")):
+        h.mp2_direct(dD.data_ptr(), dC.data_ptr(), r.orbital_energies[0], nocc, nfz, prec, 0.0, stream=st)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2[prec] = h.mp2_direct(dD.data_ptr(), dC.data_ptr(), r.orbital_energies[0], nocc, nfz, prec, 0.0,
+                                stream=st)
+        out[name] = {"seconds": time.perf_counter() - t0, "e2_Eh": e2[prec]}
+    h.close()
+    out["abs_dE2_split_vs_fp64_Eh"] = abs(e2[2] - e2[0])
+    out["speedup_split_over_fp64"] = out["fp64_dgemm"]["seconds"] / out["split_bf16_tensor_cores"]["seconds"]
+    # the GEMM engines alone (kernel time, CUDA events): first-quarter shape
+    M, N, K = 128, 1 << 17, 640
+    peak = None
+    try:
+        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"]
+    except Exception:
+        pass
+    gemms = {}
+    for name, mode, products in (("split2_3products", 2, 3), ("split3_6products", 3, 6),
+                                 ("precise_8products", 8, 8)):
+        ms = lint.gemm_bench(M, N, K, mode, 5, st)
+        useful = 2.0 * M * N * K / (ms * 1e-3) / 1e12
+        gemms[name] = {"ms_per_launch": ms, "useful_tflops": useful, "tensor_tflops": useful * products,
+                       "tensor_frac_of_measured_bf16": (useful * products / peak) if peak else None}
+    out["gemm_engines"] = {"shape": f"M={M} N={N} K={K}, FP32 out", **gemms}
+    return out
 
 
 # ------------------------------------------------------------- CPU oracle --
@@ -368,6 +475,10 @@ def main():
                                    "sample": f"one APMO Fock-build iteration (G_e, G_p, both couplings) of the "
                                              f"oracle on {nth} host threads: {t_it:.2f} s; solves/s = "
                                              f"1/(t_iter x {iters:.1f} iterations)"}
+        if not args.no_serving:
+            out["serving"] = serving_section(args)
+        if not args.no_mp2:
+            out["mp2"] = mp2_section(args)
         print(json.dumps(out))
     if dist is not None:
         dist.barrier()

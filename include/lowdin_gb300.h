@@ -245,6 +245,11 @@ int LowdinGB300_gemm_bf16_split(const float *dA, const float *dB, float *dC, int
    rounded once and all partial results are added in FP64.  For contractions
    with strong cancellation (the MP2 transform's first quarter). */
 int LowdinGB300_gemm_bf16_precise(const float *dA, const float *dB, float *dC, int M, int N, int K, void *stream);
+/* Benchmark of the tensor-core GEMM engines (no counterpart in the reference):
+   operands of M x K and N x K pseudo-random values split once, then `reps`
+   launches timed with CUDA events on `stream`; mode 2 / 3: split engine with
+   2 / 3 pieces, 8: precise engine.  Returns milliseconds per launch, or -1. */
+double LowdinGB300_gemm_bench(int M, int N, int K, int mode, int reps, void *stream);
 
 /* Number of CUDA kernels this library has launched in the process. */
 long long LowdinGB300_launch_count(void);

@@ -279,28 +279,56 @@ __global__ void __launch_bounds__(128, 1) gemm_split_kernel(const __grid_constan
 
 // ------------------------------------------------------------ precise mode --
 // Three pieces per operand, eight products (p0q0 + p0q1 + p1q0 + p1q1 + p0q2
-// + p2q0 + p1q2 + p2q1), and no long FP32 accumulation: the p0q0 product of
-// every 16-wide K slab goes to a fresh tensor-memory accumulator, the seven
-// smaller products of a 64-wide K step to one more, and four accumulator warps
-// add them into FP64 registers after every step.  The tensor cores then round
-// each slab's main sum once (toward zero, to FP32) instead of carrying a
-// 640-term FP32 running sum, which is what limits a plain FP32-accumulated
-// product on inputs with strong cancellation.
-// Warps: 0 TMA producer, 1 MMA issuer, 2-5 accumulators / epilogue (warp w
-// reads tensor-memory lanes 32 (w % 4) .. + 31).  Tiles 128 x 32; persistent
-// CTAs walk the N tiles; accumulator buffers are double-buffered across steps.
-constexpr int kPBN = 32, kPStages = 3;
+// + p2q0 + p1q2 + p2q1), and no long FP32 running sum in the tensor cores:
+// the p0q0 product of every 16-wide K slab goes to a fresh tensor-memory
+// accumulator, the seven smaller products of a 64-wide K step to one more,
+// and accumulator warps add them into compensated FP32 pairs (hi + lo, Knuth's
+// error-free TwoSum for the main terms) after every step.  The tensor cores
+// then round each slab's main sum once (toward zero, to FP32) instead of
+// carrying a 640-term FP32 running sum, which is what limits a plain
+// FP32-accumulated product on inputs with strong cancellation; the FP32 pipe
+// (64x the FP64 rate on this part) keeps up with the tensor cores.
+// Warps: 0 TMA producer, 1 MMA issuer, 2-9 accumulators / epilogue (warp w
+// reads tensor-memory lanes 32 (w % 4) .. + 31, columns 24 ((w - 2) / 4) ..
+// + 23 of each accumulator).  Tiles 128 x 48; persistent CTAs walk the N
+// tiles; accumulator buffers are double-buffered across steps.
+constexpr int kPBN = 48, kPStages = 3, kPAccWarps = 8, kPColsPerWarp = kPBN / 2;
 constexpr int kPTileA = 128 * kBK * 2, kPTileB = kPBN * kBK * 2;
 constexpr int kPStageBytes = 3 * kPTileA + 3 * kPTileB;
 constexpr int kPBufCols = 5 * kPBN;                 // 4 slab accumulators + 1 correction accumulator
 constexpr int kPTmemCols = 512;
+constexpr int kPThreads = 32 * (2 + kPAccWarps);
 constexpr int kPSmemBytes = kPStages * kPStageBytes + 1024 + 256;
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-__global__ void __launch_bounds__(192, 1) gemm_precise_kernel(const __grid_constant__ TmapSet maps, GemmArgs g) {
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t *r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+
+// hi + lo += x without rounding error in the sum (TwoSum), the error kept in lo
+__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x) {
+  const float s = hi + x;
+  const float bb = s - hi;
+  const float e = (hi - (s - bb)) + (x - bb);
+  hi = s;
+  lo += e;
+}
+
+__global__ void __launch_bounds__(kPThreads, 1) gemm_precise_kernel(const __grid_constant__ TmapSet maps, GemmArgs g) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + kPStages * kPStageBytes);
@@ -320,7 +348,7 @@ __global__ void __launch_bounds__(192, 1) gemm_precise_kernel(const __grid_const
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_free[b], 4);
+      mbar_init(&acc_free[b], kPAccWarps);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -409,8 +437,8 @@ __global__ void __launch_bounds__(192, 1) gemm_precise_kernel(const __grid_const
       }
     }
   } else {
-    // accumulator warps
-    const int wq = warp & 3;
+    // accumulator warps: lane quarter wq, columns c0 .. c0 + 23 of every accumulator
+    const int wq = warp & 3, c0 = ((warp - 2) >> 2) * kPColsPerWarp;
     const int row = m0 + wq * 32 + lane;
     long long orow = 0;
     if (row < g.M) orow = (long long)(row / g.grp_rows) * g.grp_stride + row % g.grp_rows + g.row0;
@@ -419,9 +447,9 @@ __global__ void __launch_bounds__(192, 1) gemm_precise_kernel(const __grid_const
     bool ok = true;
     for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
       const int n0 = t * kPBN;
-      double acc[kPBN];
+      float hi[kPColsPerWarp], lo[kPColsPerWarp];
 #pragma unroll
-      for (int j = 0; j < kPBN; ++j) acc[j] = 0.0;
+      for (int j = 0; j < kPColsPerWarp; ++j) hi[j] = lo[j] = 0.f;
       for (int k = 0; k < nk; ++k, ++gs) {
         const int b = (int)(gs & 1);
         const bool got = mbar_wait(&acc_full[b], (uint32_t)((gs >> 1) & 1));
@@ -432,35 +460,48 @@ __global__ void __launch_bounds__(192, 1) gemm_precise_kernel(const __grid_const
         }
         tc_fence_after();
         __syncwarp();
-        const uint32_t ta = tmem + ((uint32_t)(wq * 32) << 16) + (uint32_t)(b * kPBufCols);
-#pragma unroll 1
-        for (int c = 0; c < 5; ++c) {
-          uint32_t r[32];
-          tmem_ld32(ta + (uint32_t)(c * kPBN), r);
+        const uint32_t ta = tmem + ((uint32_t)(wq * 32) << 16) + (uint32_t)(b * kPBufCols + c0);
+        uint32_t r[kPColsPerWarp];
 #pragma unroll
-          for (int j = 0; j < kPBN; ++j) acc[j] += (double)__uint_as_float(r[j]);
+        for (int c = 0; c < 5; ++c) {
+          // loads at column offsets aligned to their width
+          if (c0 == 0) {
+            tmem_ld16(ta + (uint32_t)(c * kPBN), r);
+            tmem_ld8(ta + (uint32_t)(c * kPBN + 16), r + 16);
+          } else {
+            tmem_ld8(ta + (uint32_t)(c * kPBN), r);
+            tmem_ld16(ta + (uint32_t)(c * kPBN + 8), r + 8);
+          }
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          if (c < 4) {
+#pragma unroll
+            for (int j = 0; j < kPColsPerWarp; ++j) two_sum_acc(hi[j], lo[j], __uint_as_float(r[j]));
+          } else {
+#pragma unroll
+            for (int j = 0; j < kPColsPerWarp; ++j) lo[j] += __uint_as_float(r[j]);
+          }
         }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&acc_free[b]);
       }
       if (!ok || row >= g.M) continue;
-      const int ncol = min(kPBN, g.N - n0);
 #pragma unroll
-      for (int j = 0; j < kPBN; ++j)
-        if (j < ncol) {
-          const long long nn = n0 + j;
-          const long long oc =
-              cbase + (g.grp_cols ? (nn / g.grp_cols) * g.gcol_stride + nn % g.grp_cols + g.col0 : nn);
-          if (g.C) {
-            g.C[oc] = (float)acc[j];
-          } else {
-            __nv_bfloat16 pc[kMaxPieces];
-            bf16_pieces(acc[j], 3, pc);
+      for (int j = 0; j < kPColsPerWarp; ++j) {
+        const long long nn = n0 + c0 + j;
+        if (nn >= g.N) continue;
+        const long long oc =
+            cbase + (g.grp_cols ? (nn / g.grp_cols) * g.gcol_stride + nn % g.grp_cols + g.col0 : nn);
+        const double v = (double)hi[j] + (double)lo[j];
+        if (g.C) {
+          g.C[oc] = (float)v;
+        } else {
+          __nv_bfloat16 pc[kMaxPieces];
+          bf16_pieces(v, 3, pc);
 #pragma unroll
-            for (int q = 0; q < 3; ++q) g.Cp[q][oc] = pc[q];
-          }
+          for (int q = 0; q < 3; ++q) g.Cp[q][oc] = pc[q];
         }
+      }
     }
   }
   tc_fence_before();
@@ -611,7 +652,7 @@ cudaError_t launch_gemm_precise(const Bf16Split &A, long long a_rows, const Bf16
   // persistent CTAs: one wave over the SMs (one CTA fits an SM), split over (M tiles x batches)
   long long per = (152LL + mt * batch - 1) / (mt * batch);
   const unsigned gx = (unsigned)std::max<long long>(1, std::min<long long>(nt, per));
-  gemm_precise_kernel<<<dim3(gx, (unsigned)mt, (unsigned)batch), 192, kPSmemBytes, s>>>(maps, g);
+  gemm_precise_kernel<<<dim3(gx, (unsigned)mt, (unsigned)batch), kPThreads, kPSmemBytes, s>>>(maps, g);
   count_launches(1);
   return cudaGetLastError();
 }

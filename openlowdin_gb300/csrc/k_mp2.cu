@@ -134,7 +134,23 @@ __global__ void __launch_bounds__(256) mp2_unpack_csr_kernel(const float *__rest
   }
 }
 
+__global__ void fill_hash_kernel(float *x, long long n, unsigned seed) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    unsigned h = (unsigned)i * 2654435761u ^ seed;
+    h ^= h >> 16;
+    h *= 2246822519u;
+    h ^= h >> 13;
+    x[i] = (float)(h & 0xFFFFFF) * (2.0f / 16777216.0f) - 1.0f;
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_fill_hash(float *x, long long n, unsigned seed, cudaStream_t s) {
+  fill_hash_kernel<<<152 * 8, 256, 0, s>>>(x, n, seed);
+  count_launches(1);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_mp2_coeffs_bf16(const double *C, const double *norma, int n, int n_frozen, int n_occ, int Kp,
                                    int np, __nv_bfloat16 *const *CoT, __nv_bfloat16 *const *CvT, cudaStream_t s) {

@@ -276,6 +276,9 @@ template <typename T>
 cudaError_t launch_split_bf16(const T *src, long long rows, int cols, long long lds, int np, __nv_bfloat16 *const *out,
                               long long ldo, cudaStream_t s);
 
+// x[i] = deterministic pseudo-random values in [-1, 1) (benchmark operands)
+cudaError_t launch_fill_hash(float *x, long long n, unsigned seed, cudaStream_t s);
+
 // number of kernels this library has launched (process-wide)
 void count_launches(long long n);
 long long launch_count();

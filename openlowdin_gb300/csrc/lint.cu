@@ -1930,4 +1930,52 @@ int LowdinGB300_gemm_bf16_precise(const float *dA, const float *dB, float *dC, i
   return gemm_entry(__func__, dA, dB, dC, M, N, K, 3, true, stream);
 }
 
+double LowdinGB300_gemm_bench(int M, int N, int K, int mode, int reps, void *stream) {
+  const int pieces = mode == 2 ? 2 : 3;
+  if (M <= 0 || N <= 0 || K <= 0 || reps <= 0 || (mode != 2 && mode != 3 && mode != 8)) {
+    set_error("%s: invalid arguments (mode 2, 3 or 8)", __func__);
+    return -1.0;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int Kp = (K + 63) / 64 * 64;
+  SplitBuf A, B;
+  DevBuf<float> src, C;
+  DevBuf<int> err;
+  if (!A.ensure(pieces, (size_t)M * Kp) || !B.ensure(pieces, (size_t)N * Kp) ||
+      !src.ensure((size_t)std::max(M, N) * K) || !C.ensure((size_t)M * N) || !err.ensure(1))
+    return -1.0;
+  __nv_bfloat16 *ta[kMaxPieces], *tb[kMaxPieces];
+  cudaEvent_t e0, e1;
+  bool ok = cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+  for (int q = 0; ok && q < pieces; ++q)
+    ok = cudaMemsetAsync(A.p[q].p, 0, (size_t)M * Kp * 2, s) == cudaSuccess &&
+         cudaMemsetAsync(B.p[q].p, 0, (size_t)N * Kp * 2, s) == cudaSuccess;
+  ok = ok && cudaMemsetAsync(err.p, 0, sizeof(int), s) == cudaSuccess &&
+       launch_fill_hash(src.p, (long long)M * K, 1u, s) == cudaSuccess &&
+       launch_split_bf16<float>(src.p, M, K, K, pieces, A.ptrs(ta), Kp, s) == cudaSuccess &&
+       launch_fill_hash(src.p, (long long)N * K, 2u, s) == cudaSuccess &&
+       launch_split_bf16<float>(src.p, N, K, K, pieces, B.ptrs(tb), Kp, s) == cudaSuccess;
+  GemmOut out{};
+  out.C = C.p;
+  out.ldc = N;
+  auto run = [&]() {
+    return mode == 8 ? launch_gemm_precise(A.in(), M, B.in(), N, Kp, M, N, 1, 0, 0, out, err.p, s)
+                     : launch_gemm_split(A.in(), M, B.in(), N, Kp, M, N, 1, 0, 0, pieces, out, err.p, s);
+  };
+  ok = ok && run() == cudaSuccess && cudaEventRecord(e0, s) == cudaSuccess;
+  for (int r = 0; ok && r < reps; ++r) ok = run() == cudaSuccess;
+  float ms = 0.f;
+  int herr = 0;
+  ok = ok && cudaEventRecord(e1, s) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess &&
+       cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
+       cudaMemcpy(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!ok || herr) {
+    set_error("%s: failed (%s, pipeline code %d)", __func__, cudaGetErrorString(cudaGetLastError()), herr);
+    return -1.0;
+  }
+  return (double)ms / reps;
+}
+
 }  // extern "C"

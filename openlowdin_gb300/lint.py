@@ -83,6 +83,9 @@ def lib():
         L.LowdinGB300_gemm_bf16_split.restype = ctypes.c_int
         L.LowdinGB300_gemm_bf16_precise.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp]
         L.LowdinGB300_gemm_bf16_precise.restype = ctypes.c_int
+        L.LowdinGB300_gemm_bench.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             _vp]
+        L.LowdinGB300_gemm_bench.restype = ctypes.c_double
         L.LowdinGB300_batch_new.restype = _vp
         L.LowdinGB300_batch_del.argtypes = [_vp]
         L.LowdinGB300_batch_add_system.argtypes = [_vp, ctypes.POINTER(_vp), ctypes.c_int, _f64p, _f64p,
@@ -121,6 +124,7 @@ EXPORTED_SYMBOLS = [
     "LowdinGB300_batch_coupling_quartets", "LowdinGB300_noalloc_scratch_bytes",
     "LowdinGB300_twobody_device_noalloc", "LowdinGB300_mp2_direct", "LowdinGB300_mp2_last_columns",
     "LowdinGB300_gemm_bf16_split", "LowdinGB300_gemm_bf16_precise",
+    "LowdinGB300_gemm_bench",
 ]
 
 
@@ -340,6 +344,15 @@ def gemm_bf16_precise(a_ptr: int, b_ptr: int, c_ptr: int, M: int, N: int, K: int
     if lib().LowdinGB300_gemm_bf16_precise(a_ptr, b_ptr, c_ptr, int(M), int(N), int(K), stream) != 0:
         _check()
         raise LowdinGB300Error("gemm_bf16_precise failed")
+
+
+def gemm_bench(M: int, N: int, K: int, mode: int, reps: int = 5, stream: int = 0) -> float:
+    """Milliseconds per launch of a tensor-core GEMM engine (mode 2, 3 or 8)."""
+    v = float(lib().LowdinGB300_gemm_bench(int(M), int(N), int(K), int(mode), int(reps), stream))
+    if v < 0:
+        _check()
+        raise LowdinGB300Error("gemm_bench failed")
+    return v
 
 
 def measure_fma_tflops(fp64: bool = True) -> float:
