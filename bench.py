@@ -60,6 +60,12 @@ def parse():
                          "core-Hamiltonian-guess densities, then exit")
     ap.add_argument("--profile-precision", type=int, default=0,
                     help="precision bits of the profiled builds (0 FP64, 3 mixed split)")
+    ap.add_argument("--profile-gemm", type=int, default=0,
+                    help="profiling case: tensor-core GEMM engine (2 / 3 pieces, 8 precise) on the MP2 "
+                         "first-quarter shape M=128 N=65536 K=640, three launches, then exit")
+    ap.add_argument("--profile-mp2", type=int, default=-1,
+                    help="profiling case: one MP2 of the d-shell water cluster (--mp2-waters) at this "
+                         "precision (0 FP64, 1 / 2 split BF16), then exit")
     return ap.parse_args()
 
 
@@ -197,6 +203,26 @@ def serving_section(args):
     return out
 
 
+def mp2_profile_case(args):
+    import numpy as np
+    import torch
+    from openlowdin_gb300 import lint, systems as S
+    from openlowdin_gb300.batch_scf import BatchSCF
+    nw = args.mp2_waters
+    sysd = S.water_cluster(nw, seed=0, o_d=True)
+    s = BatchSCF([sysd])
+    r = s.solve(tol_energy=1e-9, tol_density=1e-7)[0]
+    s.close()
+    h = lint.Libint2Interface(sysd["species"][0], 1)
+    dD = torch.tensor(r.densities[0], device="cuda")
+    dC = torch.tensor(np.ascontiguousarray(r.coefficients[0].T), device="cuda")
+    t0 = time.perf_counter()
+    e2 = h.mp2_direct(dD.data_ptr(), dC.data_ptr(), r.orbital_energies[0], 5 * nw, nw, args.profile_mp2, 0.0,
+                      stream=torch.cuda.current_stream().cuda_stream)
+    h.close()
+    return {"profile_mp2_precision": args.profile_mp2, "waters": nw, "e2": e2, "seconds": time.perf_counter() - t0}
+
+
 def mp2_section(args):
     """MP2 four-index transform of a d-shell water cluster: FP64 (cuBLAS
     DGEMM) vs split-BF16 tensor cores (3 pieces, 8 products), same SCF
@@ -316,6 +342,18 @@ def main():
         return run_reference(args)
     if args.profile_fock:
         return profile_fock(args)
+    if args.profile_gemm:
+        import torch
+        from openlowdin_gb300 import lint
+        torch.cuda.set_device(0)
+        ms = lint.gemm_bench(128, 1 << 16, 640, args.profile_gemm, 2)
+        print(json.dumps({"profile_gemm_mode": args.profile_gemm, "ms_per_launch": ms}))
+        return 0
+    if args.profile_mp2 >= 0:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(mp2_profile_case(args)))
+        return 0
     import numpy as np
     import torch
     from openlowdin_gb300 import flops as FL

@@ -188,7 +188,19 @@ class BatchSCF:
     def _diag(self, g, F):
         torch = self.torch
         Fp = g.X.transpose(1, 2) @ F @ g.X
-        e, Cp = torch.linalg.eigh(Fp)
+        if g.n >= HOST_EIGH_MAX:
+            e, Cp = torch.linalg.eigh(Fp)
+        else:
+            host = Fp.cpu().numpy()
+            w = np.empty(host.shape[:2])
+            V = np.empty_like(host)
+
+            def work(i):
+                w[i], V[i] = np.linalg.eigh(host[i])
+
+            list(self._host_pool().map(work, range(host.shape[0])))
+            e = torch.from_numpy(w).to(self.dev)
+            Cp = torch.from_numpy(V).to(self.dev)
         C = g.X @ Cp
         Co = C[:, :, :g.occ]
         return e, C, g.eta * Co @ Co.transpose(1, 2)
