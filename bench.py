@@ -93,9 +93,30 @@ def profile_fock(args):
     return 0
 
 
+def replica_seeds(rank, batch):
+    """Molecule seeds of one rank: replicas solve disjoint molecules, so the
+    multi-GPU form has no collective in the data path."""
+    return [rank * batch + i for i in range(batch)]
+
+
+def reduce_step_times(values, dist, device):
+    """Max over ranks of this rank's timed totals (the slowest rank sets the
+    whole job's time); returns floats."""
+    import torch
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
+def whole_job_rate(units_per_rank, world, total_ms):
+    """Units of all ranks per second of the max-over-ranks time."""
+    return units_per_rank * world / (total_ms * 1e-3)
+
+
 def systems_for(rank, batch):
     from openlowdin_gb300 import systems as S
-    return [S.water_cluster(4, seed=rank * batch + i, quantum_protons=True) for i in range(batch)]
+    return [S.water_cluster(4, seed=sd, quantum_protons=True) for sd in replica_seeds(rank, batch)]
 
 
 # ------------------------------------------------------------------ clocks --
@@ -413,13 +434,9 @@ def main():
     launches = lint.launch_count() - launches0
     # mixed FP32/FP64 integrals
     ms_mixed, res_mixed = timed("mixed", args.steps, max(1, args.warmup // 2))
-    t = torch.tensor([ms_plain, ms_mixed], dtype=torch.float64, device=dev)
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_plain, ms_mixed = float(t[0]), float(t[1])
-    solves = args.batch * args.steps * world
-    value = solves / (ms_plain * 1e-3)
-    value_mixed = solves / (ms_mixed * 1e-3)
+    ms_plain, ms_mixed = reduce_step_times([ms_plain, ms_mixed], dist, dev)
+    value = whole_job_rate(args.batch * args.steps, world, ms_plain)
+    value_mixed = whole_job_rate(args.batch * args.steps, world, ms_mixed)
     mixed_err = max(abs(a.energy - b.energy) for a, b in zip(res_plain, res_mixed))
     iters = float(np.mean([r.iterations for r in res_plain]))
 
