@@ -10,6 +10,42 @@
 namespace lgb {
 
 constexpr int kGenMaxL = 4 * kMaxL;   // largest total angular momentum of a quartet
+
+// Cartesian index table (cumulative index c through total 5): total,
+// exponents, recursion axis, c - 1_d and c + 1_d.  The cooperative kernels
+// copy it to shared memory; the runtime forms of clevel / cx / cminus ... loop.
+struct CartInfo {
+  unsigned char lev, xyz[3], dir, m[3], p[3], pad;
+};
+constexpr int kCartN = 56;
+struct CartTable {
+  CartInfo e[kCartN];
+};
+__host__ __device__ constexpr CartTable make_cart_table() {
+  CartTable t{};
+  for (int c = 0; c < kCartN; ++c) {
+    CartInfo &q = t.e[c];
+    q.lev = (unsigned char)clevel(c);
+    q.xyz[0] = (unsigned char)cx(c);
+    q.xyz[1] = (unsigned char)cy(c);
+    q.xyz[2] = (unsigned char)cz(c);
+    q.dir = (unsigned char)cdir(c);
+    for (int d = 0; d < 3; ++d) {
+      q.m[d] = (unsigned char)(ccomp(c, d) > 0 ? cminus(c, d) : 0);
+      q.p[d] = (unsigned char)(clevel(c) < 5 ? cplus(c, d) : 0);
+    }
+    q.pad = 0;
+  }
+  return t;
+}
+__device__ const CartTable kCartTable = make_cart_table();
+
+// copy of the table in shared memory, filled by the whole block
+__device__ __forceinline__ const CartInfo *cart_shared(CartInfo *dst) {
+  for (int i = threadIdx.x; i < kCartN; i += blockDim.x) dst[i] = kCartTable.e[i];
+  __syncthreads();
+  return dst;
+}
 // Shared work arrays of one quartet evaluation, sized for its class (offsets
 // in doubles): bra nodes Vb[e][m], ket nodes Vk (blocks [f][e][m]), the
 // contracted X[e][f], the first horizontal-transfer level H, Y after the bra
@@ -72,8 +108,8 @@ __device__ inline void boys_f64_rt(int L, double T, double *F, const double *__r
 // row-major (a, b, c, d).  Every thread of the group must call it (it
 // synchronises the group); the result is valid after the call returns.
 template <typename G>
-__device__ inline void eri_coop(G g, const CoLayout &Lo, int la, int lb, int lc, int ld, const PairRec &bra,
-                                const PrimRec *__restrict__ pbra, const PairRec &ket,
+__device__ inline void eri_coop(G g, const CartInfo *__restrict__ ct, const CoLayout &Lo, int la, int lb, int lc,
+                                int ld, const PairRec &bra, const PrimRec *__restrict__ pbra, const PairRec &ket,
                                 const PrimRec *__restrict__ pket, const double *boys64, double *sm) {
   const int tid = g.tid(), nt = g.nt();
   const int L1 = la + lb, L2 = lc + ld, L = L1 + L2, M = L + 1;
@@ -89,7 +125,7 @@ __device__ inline void eri_coop(G g, const CoLayout &Lo, int la, int lb, int lc,
     int off = 0;
     for (int f = 1; f < NF; ++f) {
       kb[f] = off;
-      off += NE * (L2 - clevel(f) + 1);
+      off += NE * (L2 - ct[f].lev + 1);
     }
   }
   for (int ib = 0; ib < bra.nprim; ++ib)
@@ -127,10 +163,10 @@ __device__ inline void eri_coop(G g, const CoLayout &Lo, int la, int lb, int lc,
         const int e0 = coff(lev), mm = L - lev + 1;
         for (int idx = tid; idx < ncart(lev) * mm; idx += nt) {
           const int e = e0 + idx / mm, m = idx % mm;
-          const int d = cdir(e), em = cminus(e, d), ei = ccomp(e, d) - 1;
+          const int d = ct[e].dir, em = ct[e].m[d], ei = ct[e].xyz[d] - 1;
           double v = misc[d] * Vb[em * M + m] + misc[3 + d] * Vb[em * M + m + 1];
           if (ei > 0) {
-            const int emm = cminus(em, d);
+            const int emm = ct[em].m[d];
             v += ei * o2p * (Vb[emm * M + m] - rp * Vb[emm * M + m + 1]);
           }
           Vb[e * M + m] = v;
@@ -146,20 +182,20 @@ __device__ inline void eri_coop(G g, const CoLayout &Lo, int la, int lb, int lc,
         const int f0 = coff(lev), mf = L2 - lev + 1, per = NE * mf;
         for (int idx = tid; idx < ncart(lev) * per; idx += nt) {
           const int f = f0 + idx / per, rem = idx % per, e = rem / mf, m = rem % mf;
-          const int d = cdir(f), fm = cminus(f, d), fi = ccomp(f, d) - 1;
-          const int mfm = L2 - clevel(fm) + 1;
+          const int d = ct[f].dir, fm = ct[f].m[d], fi = ct[f].xyz[d] - 1;
+          const int mfm = L2 - ct[fm].lev + 1;
           const double x0 = fm == 0 ? Vb[e * M + m] : Vk[kb[fm] + e * mfm + m];
           const double x1 = fm == 0 ? Vb[e * M + m + 1] : Vk[kb[fm] + e * mfm + m + 1];
           double v = misc[6 + d] * x0 + misc[9 + d] * x1;
           if (fi > 0) {
-            const int fmm = cminus(fm, d), mfmm = L2 - clevel(fmm) + 1;
+            const int fmm = ct[fm].m[d], mfmm = L2 - ct[fmm].lev + 1;
             const double y0 = fmm == 0 ? Vb[e * M + m] : Vk[kb[fmm] + e * mfmm + m];
             const double y1 = fmm == 0 ? Vb[e * M + m + 1] : Vk[kb[fmm] + e * mfmm + m + 1];
             v += fi * o2q * (y0 - rq * y1);
           }
-          const int ed = ccomp(e, d);
+          const int ed = ct[e].xyz[d];
           if (ed > 0) {
-            const int em = cminus(e, d);
+            const int em = ct[e].m[d];
             v += ed * o2pq * (fm == 0 ? Vb[em * M + m + 1] : Vk[kb[fm] + em * mfm + m + 1]);
           }
           Vk[kb[f] + e * mf + m] = v;
@@ -168,7 +204,7 @@ __device__ inline void eri_coop(G g, const CoLayout &Lo, int la, int lb, int lc,
       }
       for (int i = tid; i < nE * nF; i += nt) {
         const int e = E0 + i / nF, f = F0 + i % nF;
-        X[i] += Vk[kb[f] + e * (L2 - clevel(f) + 1)];
+        X[i] += Vk[kb[f] + e * (L2 - ct[f].lev + 1)];
       }
     }
   g.sync();
@@ -186,8 +222,8 @@ __device__ inline void eri_coop(G g, const CoLayout &Lo, int la, int lb, int lc,
       // source and destination never coincide
       for (int idx = tid; idx < na * nb * nF; idx += nt) {
         const int ar = idx / (nb * nF), rem = idx % (nb * nF), bi = rem / nF, k = rem % nF;
-        const int b = coff(j) + bi, d = cdir(b), bm = cminus(b, d) - coff(j - 1);
-        const int apr = cplus(E0 + ar, d) - E0;
+        const int b = coff(j) + bi, d = ct[b].dir, bm = ct[b].m[d] - coff(j - 1);
+        const int apr = ct[E0 + ar].p[d] - E0;
         dst[(ar * nb + bi) * nF + k] = src[(apr * pnb + bm) * nF + k] + bra.AB[d] * src[(ar * pnb + bm) * nF + k];
       }
       g.sync();
@@ -203,8 +239,8 @@ __device__ inline void eri_coop(G g, const CoLayout &Lo, int la, int lb, int lc,
       const int nc = (j == ld) ? NC : coff(lc + ld - j + 1) - F0, nd = ncart(j), pnd = j == 1 ? 1 : ncart(j - 1);
       for (int idx = tid; idx < R * nc * nd; idx += nt) {
         const int r = idx / (nc * nd), rem = idx % (nc * nd), cr = rem / nd, di = rem % nd;
-        const int dd = coff(j) + di, d = cdir(dd), dm = cminus(dd, d) - coff(j - 1);
-        const int cpr = cplus(F0 + cr, d) - F0;
+        const int dd = coff(j) + di, d = ct[dd].dir, dm = ct[dd].m[d] - coff(j - 1);
+        const int cpr = ct[F0 + cr].p[d] - F0;
         double v1, v0;
         if (j == 1) {
           v1 = Y[r * nF + cpr];

@@ -57,6 +57,8 @@ __device__ __forceinline__ const Task &coop_unit(const Task *tasks, int ntasks, 
 // every warp of a cooperative CTA is an independent worker with its own work arrays
 #define LGB_COOP_PROLOGUE(K)                                              \
   extern __shared__ double smem[];                                        \
+  __shared__ CartInfo cart_sm[kCartN];                                    \
+  const CartInfo *ct = cart_shared(cart_sm);                              \
   const CoLayout Lo = co_layout(K.la, K.lb, K.lc, K.ld);                  \
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;             \
   const int nwarps = blockDim.x >> 5;                                     \
@@ -91,7 +93,7 @@ __global__ void __launch_bounds__(128) jk_coop_kernel(const JKTask *__restrict__
       }
       if (!active) continue;   // uniform across the warp
       if (T.count && lane == 0) atomicAdd(T.count, 1ull);
-      eri_coop(g, Lo, K.la, K.lb, K.lc, K.ld, bra, T.prims, ket, T.prims, TL.boys.f64, sm);
+      eri_coop(g, ct, Lo, K.la, K.lb, K.lc, K.ld, bra, T.prims, ket, T.prims, TL.boys.f64, sm);
       const double deg = (bra.sa == bra.sb ? 1 : 2) * (ket.sa == ket.sb ? 1 : 2) * (bi == ki ? 1 : 2);
       const double hdeg = deg * T.hf;
       const double *__restrict__ D = T.Ds;
@@ -178,7 +180,7 @@ __global__ void __launch_bounds__(128) cp_coop_kernel(const CPTask *__restrict__
       if (T.count && lane == 0) atomicAdd(T.count, 1ull);
       const PairRec &bra = T.pa[bi];
       const PairRec &ket = T.pb[ki];
-      eri_coop(g, Lo, K.la, K.lb, K.lc, K.ld, bra, T.pra, ket, T.prb, TL.boys.f64, sm);
+      eri_coop(g, ct, Lo, K.la, K.lb, K.lc, K.ld, bra, T.pra, ket, T.prb, TL.boys.f64, sm);
       auto Iat = [&](int a, int b, int c, int d) {
         const double v = I[((a * NB + b) * NC + c) * ND + d];
         return fabs(v) >= TL.cut ? v : 0.0;
@@ -235,7 +237,7 @@ __global__ void __launch_bounds__(128) it_coop_kernel(ITParams P, GenClass K) {
     const PairRec &ket = P.pb[ki];
     if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) continue;
     if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) continue;
-    eri_coop(g, Lo, K.la, K.lb, K.lc, K.ld, bra, P.pra, ket, P.prb, P.boys.f64, sm);
+    eri_coop(g, ct, Lo, K.la, K.lb, K.lc, K.ld, bra, P.pra, ket, P.prb, P.boys.f64, sm);
     const bool ab = bra.sa != bra.sb, cd = ket.sa != ket.sb;
     const bool mirror = P.intra && bi != ki;
     const int f[4] = {bra.fa, bra.fb, ket.fa, ket.fb};
@@ -281,7 +283,7 @@ __global__ void __launch_bounds__(128) mp2x_coop_kernel(MXParams P, GenClass K) 
     const PairRec &ket = P.pairs[ki];
     if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) continue;
     if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) continue;
-    eri_coop(g, Lo, K.la, K.lb, K.lc, K.ld, bra, P.prims, ket, P.prims, P.boys.f64, sm);
+    eri_coop(g, ct, Lo, K.la, K.lb, K.lc, K.ld, bra, P.prims, ket, P.prims, P.boys.f64, sm);
     const int col0 = __ldg(P.colbase + ki) - P.col_first;
     const bool two = bra.sa != bra.sb;
     const size_t n = P.n, ncol = P.ncol;
@@ -315,7 +317,7 @@ __global__ void __launch_bounds__(128) schwarz_coop_kernel(SchwarzParams P, GenC
   const int N = ncart(K.la) * ncart(K.lb);
   for (long long t = w0; t < P.np; t += wstep) {
     const PairRec &pr = P.pairs[P.p0 + t];
-    eri_coop(g, Lo, K.la, K.lb, K.la, K.lb, pr, P.prims, pr, P.prims, P.boys.f64, sm);
+    eri_coop(g, ct, Lo, K.la, K.lb, K.la, K.lb, pr, P.prims, pr, P.prims, P.boys.f64, sm);
     if (lane == 0) {
       double m = 0;
       for (int i = 0; i < N; ++i) m = fmax(m, fabs(I[i * N + i]));
