@@ -205,135 +205,192 @@ class BatchSCF:
         Co = C[:, :, :g.occ]
         return e, C, g.eta * Co @ Co.transpose(1, 2)
 
-    def solve(self, tol_energy=1e-8, tol_density=1e-6, max_iter=100):
+    # ------------------------------------------------ asynchronous densities --
+    def _density_submit(self, g, F):
+        """Start eta C_occ C_occ^T of F C = S C e for every species of group g:
+        below HOST_EIGH_MAX functions the eigensolves go to the host pool and
+        return futures (the GPU stays free for other work meanwhile); larger
+        matrices are solved on the GPU at once."""
         torch = self.torch
-        t0 = time.perf_counter()
-        stream = torch.cuda.current_stream(self.dev).cuda_stream
-        groups = list(self.groups.values())
-        for g in groups:
+        Fp = g.X.transpose(1, 2) @ F @ g.X
+        if g.n >= HOST_EIGH_MAX:
+            e, Cp = torch.linalg.eigh(Fp)
+            Co = g.X @ Cp[:, :, :g.occ]
+            return ("done", g.eta * Co @ Co.transpose(1, 2))
+        host = Fp.cpu().numpy()
+        occ = g.occ
+        vecs = np.empty((host.shape[0], host.shape[1], occ))
+
+        def work(i0, i1):
+            for i in range(i0, i1):
+                w, V = np.linalg.eigh(host[i])
+                vecs[i] = V[:, :occ]
+
+        m = host.shape[0]
+        nchunk = min(m, 16)
+        bounds = [(m * k // nchunk, m * (k + 1) // nchunk) for k in range(nchunk)]
+        return ("host", vecs, [self._host_pool().submit(work, a, b) for a, b in bounds])
+
+    def _density_collect(self, g, pending):
+        if pending[0] == "done":
+            return pending[1]
+        _, vecs, futs = pending
+        for f in futs:
+            f.result()
+        Cp = self.torch.from_numpy(vecs).to(self.dev, non_blocking=True)
+        Co = g.X @ Cp
+        return g.eta * Co @ Co.transpose(1, 2)
+
+    # ---------------------------------------------------------- iteration --
+    class _State:
+        pass
+
+    def _state(self, tol_energy, tol_density, max_iter):
+        torch = self.torch
+        st = BatchSCF._State()
+        st.t0 = time.perf_counter()
+        st.stream = torch.cuda.current_stream(self.dev).cuda_stream
+        st.groups = list(self.groups.values())
+        for g in st.groups:
             g.P.copy_(self._density(g, g.H))      # core-Hamiltonian guess
             g.Flast = g.H.clone()
+        st.hist_F, st.hist_E, st.hist_B = [], [], []
+        st.e_old = np.full(self.nsys, np.nan)
+        st.final_e = np.zeros(self.nsys)
+        st.conv = np.zeros(self.nsys, bool)
+        st.iters = np.zeros(self.nsys, int)
+        st.frozen = torch.zeros(self.nsys, dtype=torch.bool, device=self.dev)
+        st.it = 0
+        st.done = False
+        st.tol_energy, st.tol_density, st.max_iter = tol_energy, tol_density, max_iter
+        st.trace = self.trace
+        st.last = [time.perf_counter()]
+        return st
+
+    def _tick(self, st, name):
+        if st.trace is None:
+            return
+        self.torch.cuda.synchronize(self.dev)
+        now = time.perf_counter()
+        st.trace[name] = st.trace.get(name, 0.0) + (now - st.last[0])
+        st.last[0] = now
+
+    def _start(self, st):
+        """Fock build, assembly and DIIS of one iteration; the eigensolves of
+        the new densities are left running (see _finish)."""
+        torch = self.torch
+        st.it += 1
+        it = st.it
+        groups = st.groups
         mixed = self.precision == "mixed"
-        hist_F, hist_E = [], []         # per iteration: list over groups
-        hist_B = []                      # per iteration: dots with earlier entries [nsys, h]
-        e_old = np.full(self.nsys, np.nan)
-        final_e = np.zeros(self.nsys)
-        conv = np.zeros(self.nsys, bool)
-        iters = np.zeros(self.nsys, int)
-        frozen = torch.zeros(self.nsys, dtype=torch.bool, device=self.dev)
-        quartets = 0
-        it = 0
-        # optional phase timing (self.trace = {} before solve): synchronises
-        # the device at each phase boundary, so only for diagnostics
-        trace = self.trace
-        last = [time.perf_counter()]
-
-        def tick(name):
-            if trace is None:
-                return
-            torch.cuda.synchronize(self.dev)
-            now = time.perf_counter()
-            trace[name] = trace.get(name, 0.0) + (now - last[0])
-            last[0] = now
-
-        for it in range(1, max_iter + 1):
-            # plain: full build from P every iteration (the reference's scheme).
-            # mixed: incremental build from dP = P - P_ref on top of the previous
-            # matrices, a full build (FP64 couplings) on the first and every
-            # rebuild_every-th iteration; two-particle quartets whose Schwarz x
-            # |dP| bound is below the split run in FP32, the rest in FP64, and
-            # incremental couplings run in FP32 (their size scales with |dP|).
-            full = (not mixed) or (it - 1) % self.rebuild_every == 0
-            for g in groups:
-                if full:
-                    g.Pin.copy_(g.P)
-                else:
-                    torch.sub(g.P, g.Pref, out=g.Pin)
-            # precision bits: 1 = two-particle FP32/FP64 split, 2 = coupling split
-            self.batch.fock(3 if mixed else 0, self.split, stream)
-            tick("fock")
-            for g in groups:
-                if full:
-                    g.G.copy_(g.Gb)
-                    g.J.copy_(g.Jb)
-                else:
-                    g.G += g.Gb
-                    g.J += g.Jb
-                g.Pref.copy_(g.P)
-            energy = self.enuc.clone()
-            Fs, Es = [], []
-            for g in groups:
-                F = g.H + g.G + g.J
-                e_sp = torch.sum(g.P * (g.H + 0.5 * g.G + 0.5 * g.J), dim=(1, 2))
-                energy.index_add_(0, g.sys_index, e_sp)
-                FPS = F @ g.P @ g.S
-                err = g.X.transpose(1, 2) @ (FPS - FPS.transpose(1, 2)) @ g.X
-                Fs.append(F)
-                Es.append(err)
-            tick("assemble")
-            # Pulay DIIS per system over all of its species
-            hist_F.append(Fs)
-            hist_E.append(Es)
-            if len(hist_F) > self.diis_size:
-                hist_F.pop(0); hist_E.pop(0); hist_B.pop(0)
-                hist_B = [b[:, 1:] for b in hist_B]
-            h = len(hist_F)
-            row = torch.zeros((self.nsys, h), dtype=torch.float64, device=self.dev)
-            for gi, g in enumerate(groups):
-                cur = Es[gi].reshape(len(g.members), -1)
-                for j in range(h):
-                    d = torch.sum(cur * hist_E[j][gi].reshape(len(g.members), -1), dim=1)
-                    row[:, j].index_add_(0, g.sys_index, d)
-            hist_B.append(row)
-            if h >= 2:
-                B = torch.zeros((self.nsys, h + 1, h + 1), dtype=torch.float64, device=self.dev)
-                for i in range(h):
-                    B[:, i, :i + 1] = hist_B[i][:, :i + 1]
-                    B[:, :i + 1, i] = hist_B[i][:, :i + 1]
-                B[:, h, :h] = -1.0
-                B[:, :h, h] = -1.0
-                # scale for conditioning, then solve every system at once
-                scale = torch.clamp(B[:, h - 1, h - 1].abs(), min=1e-300)
-                B[:, :h, :h] /= scale[:, None, None]
-                rhs = torch.zeros((self.nsys, h + 1, 1), dtype=torch.float64, device=self.dev)
-                rhs[:, h, 0] = -1.0
-                coef = torch.linalg.lstsq(B.cpu(), rhs.cpu()).solution[:, :h, 0].to(self.dev)
-            else:
-                coef = None
-            tick("diis")
-            dP = torch.zeros(self.nsys, dtype=torch.float64, device=self.dev)
-            for gi, g in enumerate(groups):
-                if coef is None:
-                    Fx = Fs[gi]
-                else:
-                    c = coef[g.sys_index]                               # [m, h]
-                    Fx = sum(c[:, j, None, None] * hist_F[j][gi] for j in range(h))
-                Pn = self._density(g, Fx)
-                keep = frozen[g.sys_index]
-                d = torch.sqrt(torch.mean((Pn - g.P) ** 2, dim=(1, 2)))
-                dP = torch.maximum(dP, torch.zeros_like(dP).scatter_reduce_(0, g.sys_index, d, reduce="amax"))
-                Pn = torch.where(keep[:, None, None], g.P, Pn)
-                g.Flast = torch.where(keep[:, None, None], g.Flast, Fs[gi])
-                g.P.copy_(Pn)
-            tick("density")
-            stats = torch.stack([energy, dP]).cpu().numpy()
-            tick("convergence")
-            en, dpn = stats[0], stats[1]
-            active = ~conv
-            final_e[active] = en[active]
-            iters[active] = it
-            newly = active & (np.abs(en - e_old) < tol_energy) & (dpn < tol_density)
-            e_old[active] = en[active]
-            conv |= newly
-            if newly.any():
-                # a converged system keeps its energy and density from here on
-                frozen |= torch.tensor(newly, device=self.dev)
-            if conv.all():
-                break
-        # Roothaan orbitals of the last Fock matrix of every species (one eigh)
+        # plain: full build from P every iteration (the reference's scheme).
+        # mixed: incremental build from dP = P - P_ref on top of the previous
+        # matrices, a full build (FP64 couplings) on the first and every
+        # rebuild_every-th iteration; two-particle quartets whose Schwarz x
+        # |dP| bound is below the split run in FP32, the rest in FP64, and
+        # incremental couplings run in FP32 (their size scales with |dP|).
+        full = (not mixed) or (it - 1) % self.rebuild_every == 0
         for g in groups:
+            if full:
+                g.Pin.copy_(g.P)
+            else:
+                torch.sub(g.P, g.Pref, out=g.Pin)
+        # precision bits: 1 = two-particle FP32/FP64 split, 2 = coupling split
+        self.batch.fock(3 if mixed else 0, self.split, st.stream)
+        self._tick(st, "fock")
+        for g in groups:
+            if full:
+                g.G.copy_(g.Gb)
+                g.J.copy_(g.Jb)
+            else:
+                g.G += g.Gb
+                g.J += g.Jb
+            g.Pref.copy_(g.P)
+        energy = self.enuc.clone()
+        Fs, Es = [], []
+        for g in groups:
+            F = g.H + g.G + g.J
+            e_sp = torch.sum(g.P * (g.H + 0.5 * g.G + 0.5 * g.J), dim=(1, 2))
+            energy.index_add_(0, g.sys_index, e_sp)
+            FPS = F @ g.P @ g.S
+            err = g.X.transpose(1, 2) @ (FPS - FPS.transpose(1, 2)) @ g.X
+            Fs.append(F)
+            Es.append(err)
+        self._tick(st, "assemble")
+        # Pulay DIIS per system over all of its species
+        st.hist_F.append(Fs)
+        st.hist_E.append(Es)
+        if len(st.hist_F) > self.diis_size:
+            st.hist_F.pop(0); st.hist_E.pop(0); st.hist_B.pop(0)
+            st.hist_B = [b[:, 1:] for b in st.hist_B]
+        h = len(st.hist_F)
+        row = torch.zeros((self.nsys, h), dtype=torch.float64, device=self.dev)
+        for gi, g in enumerate(groups):
+            cur = Es[gi].reshape(len(g.members), -1)
+            for j in range(h):
+                d = torch.sum(cur * st.hist_E[j][gi].reshape(len(g.members), -1), dim=1)
+                row[:, j].index_add_(0, g.sys_index, d)
+        st.hist_B.append(row)
+        if h >= 2:
+            B = torch.zeros((self.nsys, h + 1, h + 1), dtype=torch.float64, device=self.dev)
+            for i in range(h):
+                B[:, i, :i + 1] = st.hist_B[i][:, :i + 1]
+                B[:, :i + 1, i] = st.hist_B[i][:, :i + 1]
+            B[:, h, :h] = -1.0
+            B[:, :h, h] = -1.0
+            # scale for conditioning, then solve every system at once
+            scale = torch.clamp(B[:, h - 1, h - 1].abs(), min=1e-300)
+            B[:, :h, :h] /= scale[:, None, None]
+            rhs = torch.zeros((self.nsys, h + 1, 1), dtype=torch.float64, device=self.dev)
+            rhs[:, h, 0] = -1.0
+            coef = torch.linalg.lstsq(B.cpu(), rhs.cpu()).solution[:, :h, 0].to(self.dev)
+        else:
+            coef = None
+        self._tick(st, "diis")
+        st.pending = []
+        for gi, g in enumerate(groups):
+            if coef is None:
+                Fx = Fs[gi]
+            else:
+                c = coef[g.sys_index]                               # [m, h]
+                Fx = sum(c[:, j, None, None] * st.hist_F[j][gi] for j in range(h))
+            st.pending.append(self._density_submit(g, Fx))
+        st.Fs = Fs
+        st.energy = energy
+
+    def _finish(self, st):
+        """Collect the eigensolves started by _start: new densities and the
+        convergence test; sets st.done."""
+        torch = self.torch
+        dP = torch.zeros(self.nsys, dtype=torch.float64, device=self.dev)
+        for gi, g in enumerate(st.groups):
+            Pn = self._density_collect(g, st.pending[gi])
+            keep = st.frozen[g.sys_index]
+            d = torch.sqrt(torch.mean((Pn - g.P) ** 2, dim=(1, 2)))
+            dP = torch.maximum(dP, torch.zeros_like(dP).scatter_reduce_(0, g.sys_index, d, reduce="amax"))
+            Pn = torch.where(keep[:, None, None], g.P, Pn)
+            g.Flast = torch.where(keep[:, None, None], g.Flast, st.Fs[gi])
+            g.P.copy_(Pn)
+        self._tick(st, "density")
+        stats = torch.stack([st.energy, dP]).cpu().numpy()
+        self._tick(st, "convergence")
+        en, dpn = stats[0], stats[1]
+        active = ~st.conv
+        st.final_e[active] = en[active]
+        st.iters[active] = st.it
+        newly = active & (np.abs(en - st.e_old) < st.tol_energy) & (dpn < st.tol_density)
+        st.e_old[active] = en[active]
+        st.conv |= newly
+        if newly.any():
+            # a converged system keeps its energy and density from here on
+            st.frozen |= torch.tensor(newly, device=self.dev)
+        st.done = bool(st.conv.all()) or st.it >= st.max_iter
+
+    def _results(self, st):
+        # Roothaan orbitals of the last Fock matrix of every species (one eigh)
+        for g in st.groups:
             g.eps, g.C, _ = self._diag(g, g.Flast)
-        q = self.batch.quartets(stream)
+        q = self.batch.quartets(st.stream)
         quartets = int(q.sum())
         self.last_class_quartets = q
         out = []
@@ -344,6 +401,48 @@ class BatchSCF:
                 eps.append(g.eps[slot].cpu().numpy())
                 C.append(g.C[slot].cpu().numpy())
                 P.append(g.P[slot].cpu().numpy())
-            out.append(SCFResult(float(final_e[si]), int(iters[si]), bool(conv[si]),
-                                 time.perf_counter() - t0, eps, C, P, quartets))
+            out.append(SCFResult(float(st.final_e[si]), int(st.iters[si]), bool(st.conv[si]),
+                                 time.perf_counter() - st.t0, eps, C, P, quartets))
         return out
+
+    def solve(self, tol_energy=1e-8, tol_density=1e-6, max_iter=100):
+        st = self._state(tol_energy, tol_density, max_iter)
+        while not st.done:
+            self._start(st)
+            self._finish(st)
+        return self._results(st)
+
+
+class PipelinedSCF:
+    """Two BatchSCF halves iterated alternately: while one half's host
+    eigensolves run, the other half's Fock build, assembly and DIIS run on the
+    GPU.  Same iteration scheme and results as BatchSCF (each system's
+    arithmetic is unchanged; only the order of work across systems differs)."""
+
+    def __init__(self, systems, **kw):
+        if len(systems) < 2:
+            raise ValueError("PipelinedSCF needs at least two systems")
+        h = (len(systems) + 1) // 2
+        self.halves = [BatchSCF(systems[:h], **kw), BatchSCF(systems[h:], **kw)]
+
+    def close(self):
+        for b in self.halves:
+            b.close()
+
+    def solve(self, tol_energy=1e-8, tol_density=1e-6, max_iter=100):
+        a, b = self.halves
+        sa = a._state(tol_energy, tol_density, max_iter)
+        sb = b._state(tol_energy, tol_density, max_iter)
+        a._start(sa)
+        while not (sa.done and sb.done):
+            if not sb.done:
+                b._start(sb)        # half b on the GPU while half a's eigensolves run
+            if not sa.done:
+                a._finish(sa)
+                if not sa.done:
+                    a._start(sa)    # half a on the GPU while half b's eigensolves run
+            if not sb.done:
+                b._finish(sb)
+        if not sa.done:
+            a._finish(sa)
+        return a._results(sa) + b._results(sb)

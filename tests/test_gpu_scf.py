@@ -97,3 +97,19 @@ def test_batched_scf_matches_oracle_per_molecule(oracle):
         ro = oracle.scf(oracle.from_plain(m), tol_energy=1e-10, tol_density=1e-8)
         assert r.converged
         assert abs(r.energy - ro.energy) < 1e-8
+
+
+def test_pipelined_halves_match_single_batch():
+    """Two halves iterated alternately give the same solves as one batch."""
+    from openlowdin_gb300.batch_scf import BatchSCF, PipelinedSCF
+    mols = [S.water_cluster(2, seed=i, quantum_protons=True) for i in range(3)] + [S.water()]
+    a = BatchSCF(mols)
+    ra = a.solve(tol_energy=1e-10, tol_density=1e-8)
+    a.close()
+    for prec in ("fp64", "mixed"):
+        b = PipelinedSCF(mols, precision=prec)
+        rb = b.solve(tol_energy=1e-10, tol_density=1e-8)
+        b.close()
+        for x, y in zip(ra, rb):
+            assert y.converged
+            assert abs(x.energy - y.energy) < (1e-9 if prec == "fp64" else 1e-6)
