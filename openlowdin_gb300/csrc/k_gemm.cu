@@ -281,9 +281,10 @@ __global__ void __launch_bounds__(128, 1) gemm_split_kernel(const __grid_constan
 // Three pieces per operand, eight products (p0q0 + p0q1 + p1q0 + p1q1 + p0q2
 // + p2q0 + p1q2 + p2q1), and no long FP32 running sum in the tensor cores:
 // the p0q0 product of every 16-wide K slab goes to a fresh tensor-memory
-// accumulator, the seven smaller products of a 64-wide K step to one more,
-// and accumulator warps add them into compensated FP32 pairs (hi + lo, Knuth's
-// error-free TwoSum for the main terms) after every step.  The tensor cores
+// accumulator, the seven smaller products of a 64-wide K step to one more;
+// after every step the accumulator warps add the four slab sums in FP32 and
+// enter the step total into a compensated FP32 pair (hi + lo, Knuth's
+// error-free TwoSum), the corrections into the low part.  The tensor cores
 // then round each slab's main sum once (toward zero, to FP32) instead of
 // carrying a 640-term FP32 running sum, which is what limits a plain
 // FP32-accumulated product on inputs with strong cancellation; the FP32 pipe
@@ -461,6 +462,10 @@ __global__ void __launch_bounds__(kPThreads, 1) gemm_precise_kernel(const __grid
         tc_fence_after();
         __syncwarp();
         const uint32_t ta = tmem + ((uint32_t)(wq * 32) << 16) + (uint32_t)(b * kPBufCols + c0);
+        // the step's four slab sums (each rounded once by the tensor cores)
+        // add in FP32, round to nearest; the step total enters the running
+        // pair by TwoSum; the correction products go to the low part
+        float stepsum[kPColsPerWarp];
         uint32_t r[kPColsPerWarp];
 #pragma unroll
         for (int c = 0; c < 5; ++c) {
@@ -473,12 +478,18 @@ __global__ void __launch_bounds__(kPThreads, 1) gemm_precise_kernel(const __grid
             tmem_ld16(ta + (uint32_t)(c * kPBN + 8), r + 8);
           }
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-          if (c < 4) {
+          if (c == 0) {
 #pragma unroll
-            for (int j = 0; j < kPColsPerWarp; ++j) two_sum_acc(hi[j], lo[j], __uint_as_float(r[j]));
+            for (int j = 0; j < kPColsPerWarp; ++j) stepsum[j] = __uint_as_float(r[j]);
+          } else if (c < 4) {
+#pragma unroll
+            for (int j = 0; j < kPColsPerWarp; ++j) stepsum[j] += __uint_as_float(r[j]);
           } else {
 #pragma unroll
-            for (int j = 0; j < kPColsPerWarp; ++j) lo[j] += __uint_as_float(r[j]);
+            for (int j = 0; j < kPColsPerWarp; ++j) {
+              two_sum_acc(hi[j], lo[j], stepsum[j]);
+              lo[j] += __uint_as_float(r[j]);
+            }
           }
         }
         tc_fence_before();
