@@ -228,7 +228,20 @@ int LowdinGB300_twobody_device_noalloc(LibintInterface *lint, const double *dD, 
    synchronises `stream`.  Returns 0, or -1 with LowdinGB300_last_error() set. */
 int LowdinGB300_mp2_direct(LibintInterface *lint, const double *dD, const double *dC, const double *eps,
                            int n_occ, int n_frozen, int precision, double x_budget_gb, double *e2, void *stream);
-/* ket-component columns of the last LowdinGB300_mp2_direct call */
+/* Inter-species MP2 term of species a and b (APMO; replaces the two-species
+   branch of TransformIntegralsC.f90 over LibintInterface_compute_coupling_directIT,
+   Libint2Iface.cpp:1296-1622, and the coupling sum of MPFunctions.f90:682-886):
+   e2 = factor * sum_{i,a in A; j,b in B} (ia|jb)^2 / (e_i + e_j - e_a - e_b)
+   with factor = (q_A q_B)^2 lambda_A lambda_B.  Same integral set as that path
+   (no density screening, raw |v| <= 1e-10 dropped, |(ia|jb)| <= 1e-10 read as
+   zero).  dCa / dCb: device coefficients (row p = orbital p); eps_a / eps_b:
+   host orbital energies; precision as for LowdinGB300_mp2_direct.  Writes
+   *e2 and synchronises `stream`.  Returns 0, or -1 with the error set. */
+int LowdinGB300_mp2_coupling(LibintInterface *a, LibintInterface *b, const double *dCa, const double *dCb,
+                             const double *eps_a, const double *eps_b, int n_occ_a, int n_frozen_a, int n_occ_b,
+                             int n_frozen_b, double factor, int precision, double x_budget_gb, double *e2,
+                             void *stream);
+/* ket-component columns of the last LowdinGB300_mp2_direct / _mp2_coupling call */
 long long LowdinGB300_mp2_last_columns(void);
 
 /* Split-BF16 GEMM on the tensor cores (no counterpart in the reference; the

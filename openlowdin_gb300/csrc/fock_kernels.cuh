@@ -388,11 +388,11 @@ __global__ void __launch_bounds__(128) mp2x_kernel(MXParams P) {
   if (bpos >= P.nbra || kpos >= P.nket) return;
   const int bi = P.bra0 + bpos, ki = P.ket0 + kpos;
   const PairRec bra = P.pairs[bi];
-  const PairRec ket = P.pairs[ki];
+  const PairRec ket = P.kpairs[ki];
   if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) return;
   if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) return;
   double I[Q::NINT];
-  eri_quartet<double, LA, LB, LC, LD>(bra, P.prims, ket, P.prims, P.boys.f64, P.boys.f32, I);
+  eri_quartet<double, LA, LB, LC, LD>(bra, P.prims, ket, P.kprims, P.boys.f64, P.boys.f32, I);
   const int col0 = __ldg(P.colbase + ki) - P.col_first;
   const bool two = bra.sa != bra.sb;
   const size_t n = P.n, ncol = P.ncol;

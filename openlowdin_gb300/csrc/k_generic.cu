@@ -280,10 +280,10 @@ __global__ void __launch_bounds__(128) mp2x_coop_kernel(MXParams P, GenClass K) 
   for (long long q = w0; q < nq; q += wstep) {
     const int bi = P.bra0 + (int)(q / P.nket), ki = P.ket0 + (int)(q % P.nket);
     const PairRec &bra = P.pairs[bi];
-    const PairRec &ket = P.pairs[ki];
+    const PairRec &ket = P.kpairs[ki];
     if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) continue;
     if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) continue;
-    eri_coop(g, ct, Lo, K.la, K.lb, K.lc, K.ld, bra, P.prims, ket, P.prims, P.boys.f64, sm);
+    eri_coop(g, ct, Lo, K.la, K.lb, K.lc, K.ld, bra, P.prims, ket, P.kprims, P.boys.f64, sm);
     const int col0 = __ldg(P.colbase + ki) - P.col_first;
     const bool two = bra.sa != bra.sb;
     const size_t n = P.n, ncol = P.ncol;

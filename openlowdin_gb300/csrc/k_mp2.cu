@@ -1,5 +1,7 @@
 // MP2 transform helpers: coefficient preparation, unpacking of the packed
 // ket-pair columns into a full (lam, sig) square, and the pair-energy sum.
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace lgb {
@@ -134,6 +136,33 @@ __global__ void __launch_bounds__(256) mp2_unpack_csr_kernel(const float *__rest
   }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(256) mp2_energy_coupling_kernel(const T *__restrict__ M, int vB, int vA, double ei,
+                                                                  const double *__restrict__ eo,
+                                                                  const double *__restrict__ evA,
+                                                                  const double *__restrict__ evB, double cut,
+                                                                  double factor, double *e2) {
+  __shared__ double red[8];
+  const int j = blockIdx.y;
+  const T *Mj = M + (size_t)j * vB * vA;
+  const double eij = ei + eo[j];
+  double acc = 0.0;
+  for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < (long long)vB * vA; t += (long long)gridDim.x * 256) {
+    const int b = (int)(t / vA), a = (int)(t % vA);
+    double x = (double)Mj[t];
+    if (!(fabs(x) > cut)) x = 0.0;
+    acc += x * x / (eij - evA[a] - evB[b]);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0;
+    for (int k = 0; k < 8; ++k) s += red[k];
+    atomicAdd(e2, s * factor);
+  }
+}
+
 __global__ void fill_hash_kernel(float *x, long long n, unsigned seed) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     unsigned h = (unsigned)i * 2654435761u ^ seed;
@@ -209,6 +238,24 @@ cudaError_t launch_mp2_energy(const T *M, int o, int v, double ei, const double 
   return cudaGetLastError();
 }
 
+template <typename T>
+cudaError_t launch_mp2_energy_coupling(const T *M, int o, int vB, int vA, double ei, const double *eo,
+                                       const double *evA, const double *evB, double cut, double factor, double *e2,
+                                       cudaStream_t s) {
+  if (o <= 0 || vA <= 0 || vB <= 0) return cudaSuccess;
+  const long long per = (long long)vB * vA;
+  const unsigned gx = (unsigned)std::min<long long>((per + 255) / 256, 64);
+  mp2_energy_coupling_kernel<T><<<dim3(gx, (unsigned)o), 256, 0, s>>>(M, vB, vA, ei, eo, evA, evB, cut, factor, e2);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_mp2_energy_coupling<double>(const double *, int, int, int, double, const double *,
+                                                        const double *, const double *, double, double, double *,
+                                                        cudaStream_t);
+template cudaError_t launch_mp2_energy_coupling<float>(const float *, int, int, int, double, const double *,
+                                                       const double *, const double *, double, double, double *,
+                                                       cudaStream_t);
 template cudaError_t launch_mp2_unpack<double>(const double *, const unsigned *, long long, int, int, double *,
                                                cudaStream_t);
 template cudaError_t launch_mp2_unpack<float>(const float *, const unsigned *, long long, int, int, float *,

@@ -137,8 +137,10 @@ struct SchwarzParams {
 // for ket components (c, d); quartets that the screening drops and raw values
 // with |v| <= cut stay at the zero the caller cleared X to.
 struct MXParams {
-  const PairRec *pairs;
+  const PairRec *pairs;   // bra pairs (species A)
   const PrimRec *prims;
+  const PairRec *kpairs;  // ket pairs (species B; A's own list for one species)
+  const PrimRec *kprims;
   int bra0, nbra;
   int ket0, nket;
   const int *colbase;     // per pair record: first column of its components
@@ -192,6 +194,12 @@ cudaError_t launch_mp2_coeffs_bf16(const double *C, const double *norma, int n, 
 // Yp points at Y'[0][i][0], a-rows ystride apart
 cudaError_t launch_mp2_unpack_csr(const float *Yp, long long ystride, const int *rowptr, const int2 *ent, int n,
                                   int Kp, int v, int np, __nv_bfloat16 *const *Z, cudaStream_t s);
+// coupling pair energies: e2 += factor sum_{j,b,a} M[j][b][a]^2 / (ei + eo[j] - evA[a] - evB[b]),
+// M [o][vB][vA], |M| <= cut read as zero
+template <typename T>
+cudaError_t launch_mp2_energy_coupling(const T *M, int o, int vB, int vA, double ei, const double *eo,
+                                       const double *evA, const double *evB, double cut, double factor, double *e2,
+                                       cudaStream_t s);
 template <typename T>
 cudaError_t launch_mp2_energy(const T *M, int o, int v, double ei, const double *eo, const double *ev, double cut,
                               double *e2, cudaStream_t s);

@@ -1556,15 +1556,15 @@ void mp2_columns(const PairList &P, long long colB, MP2Columns &mc) {
   mc.bfirst.push_back(npairs);
 }
 
-// integrals of every significant bra pair against the ket pairs [k0, k1)
-bool mp2_batch_ints(const PairList &P, MXParams q, int k0, int k1, cudaStream_t s) {
+// integrals of every bra pair of PA against the ket pairs [k0, k1) of PB
+bool mp2_batch_ints(const PairList &PA, const PairList &PB, MXParams q, int k0, int k1, cudaStream_t s) {
   for (int ck = 0; ck < kNumPairClasses; ++ck) {
-    const int ka = std::max(k0, P.start[ck]), kb = std::min(k1, P.start[ck + 1]);
+    const int ka = std::max(k0, PB.start[ck]), kb = std::min(k1, PB.start[ck + 1]);
     if (ka >= kb) continue;
     for (int cb = 0; cb < kNumPairClasses; ++cb)
-      for (int b0 = P.start[cb]; b0 < P.start[cb + 1]; b0 += 65535 * kWarpsPerBlock) {  // grid y limit
+      for (int b0 = PA.start[cb]; b0 < PA.start[cb + 1]; b0 += 65535 * kWarpsPerBlock) {  // grid y limit
         q.bra0 = b0;
-        q.nbra = std::min(P.start[cb + 1] - b0, 65535 * kWarpsPerBlock);
+        q.nbra = std::min(PA.start[cb + 1] - b0, 65535 * kWarpsPerBlock);
         q.ket0 = ka;
         q.nket = kb - ka;
         CK(launch_mp2x(cb, ck, q, s));
@@ -1573,10 +1573,17 @@ bool mp2_batch_ints(const PairList &P, MXParams q, int k0, int k1, cudaStream_t 
   return true;
 }
 
+// One MP2 term: intra-species (A == B, closed shell: (ia|jb)[2(ia|jb) -
+// (ib|ja)]/D) or inter-species (A != B: factor (ia|jb)^2 / D, factor = (q_A
+// q_B)^2 lambda_A lambda_B).  The bra index pairs (mu nu) belong to A, the ket
+// columns (lam sig) to B.
 struct MP2Setup {
-  LibintInterface *L;
-  int n, nsh, o, v, n_occ, n_frozen;
-  const double *dC, *eps;
+  LibintInterface *A, *B;
+  const PairList *PA, *PB;
+  bool coupling;
+  double factor;
+  int nA, nB, oA, vA, oB, vB, noccA, nfA, noccB, nfB;
+  const double *dCA, *dCB, *epsA, *epsB;
   MXParams q;      // common integral parameters
 };
 
@@ -1584,48 +1591,56 @@ bool mp2_need(size_t bytes) {
   size_t freeb = 0, totb = 0;
   CK(cudaMemGetInfo(&freeb, &totb));
   if (bytes > freeb) {
-    set_error("mp2_direct: needs %.1f GB of device memory, %.1f GB free", bytes / 1e9, freeb / 1e9);
+    set_error("mp2: needs %.1f GB of device memory, %.1f GB free", bytes / 1e9, freeb / 1e9);
     return false;
   }
   return true;
 }
 
+long long mp2_max_batch(const MP2Columns &mc, const PairList &P) {
+  long long colB = 0;
+  for (size_t b = 0; b + 1 < mc.bfirst.size(); ++b) {
+    const int k1 = mc.bfirst[b + 1];
+    colB = std::max<long long>(colB, (k1 < (int)P.h.size() ? mc.colbase[k1] : mc.ncols) - mc.colbase[mc.bfirst[b]]);
+  }
+  return colB;
+}
+
 // FP64 back end: cuBLAS DGEMM for the four quarters
 bool mp2_fp64(MP2Setup &S, size_t budget, double *e2out, cudaStream_t s) {
-  const int n = S.n, o = S.o, v = S.v;
+  const int nA = S.nA, nB = S.nB, oA = S.oA, vA = S.vA, oB = S.oB, vB = S.vB;
   cublasHandle_t blas;
   if (!blas_handle(&blas)) return false;
   if (cublasSetStream(blas, s) != CUBLAS_STATUS_SUCCESS) {
     set_error("cublasSetStream failed");
     return false;
   }
-  const PairList &P = S.L->sig;
-  const size_t per_col = (size_t)n * n * sizeof(double) + (size_t)o * n * sizeof(double);
+  const PairList &PB = *S.PB;
+  const size_t per_col = (size_t)nA * nA * sizeof(double) + (size_t)oA * nA * sizeof(double);
   MP2Columns mc;
-  mp2_columns(P, std::max<long long>(36, (long long)(budget / per_col)), mc);
+  mp2_columns(PB, std::max<long long>(36, (long long)(budget / per_col)), mc);
   const long long ncols = mc.ncols;
-  long long colB = 0;
-  for (size_t b = 0; b + 1 < mc.bfirst.size(); ++b) {
-    const int k1 = mc.bfirst[b + 1];
-    colB = std::max<long long>(colB, (k1 < (int)P.h.size() ? mc.colbase[k1] : ncols) - mc.colbase[mc.bfirst[b]]);
-  }
-  if (!mp2_need((size_t)o * ncols * v * 8 + (size_t)n * n * v * 8 + (size_t)colB * per_col + (size_t)o * n * v * 8 +
-                (size_t)o * v * v * 8))
+  const long long colB = mp2_max_batch(mc, PB);
+  if (!mp2_need((size_t)oA * ncols * vA * 8 + (size_t)nB * nB * vA * 8 + (size_t)colB * per_col +
+                (size_t)oB * nB * vA * 8 + (size_t)oB * vB * vA * 8))
     return false;
-  DevBuf<double> Co, Cv, Eo, Ev, Y, X, T1, Z, W, M, e2;
+  DevBuf<double> CoA, CvA, CoB, CvB, EoB, EvA, EvB, Y, X, T1, Z, W, M, e2;
   DevBuf<int> dcolbase;
   DevBuf<unsigned> dcolpair;
-  if (!Co.ensure((size_t)n * o) || !Cv.ensure((size_t)n * v) || !Eo.ensure(o) || !Ev.ensure(v) ||
-      !Y.ensure((size_t)o * ncols * v) || !X.ensure((size_t)n * colB * n) || !T1.ensure((size_t)o * colB * n) ||
-      !Z.ensure((size_t)n * n * v) || !W.ensure((size_t)o * n * v) || !M.ensure((size_t)o * v * v) || !e2.ensure(1) ||
-      !dcolbase.ensure(P.h.size()) || !dcolpair.ensure(ncols))
+  if (!CoA.ensure((size_t)nA * oA) || !CvA.ensure((size_t)nA * vA) || !CoB.ensure((size_t)nB * oB) ||
+      !CvB.ensure((size_t)nB * vB) || !EoB.ensure(oB) || !EvA.ensure(vA) || !EvB.ensure(vB) ||
+      !Y.ensure((size_t)oA * ncols * vA) || !X.ensure((size_t)nA * colB * nA) || !T1.ensure((size_t)oA * colB * nA) ||
+      !Z.ensure((size_t)nB * nB * vA) || !W.ensure((size_t)oB * nB * vA) || !M.ensure((size_t)oB * vB * vA) ||
+      !e2.ensure(1) || !dcolbase.ensure(PB.h.size()) || !dcolpair.ensure(ncols))
     return false;
-  CK(cudaMemcpyAsync(dcolbase.p, mc.colbase.data(), P.h.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dcolbase.p, mc.colbase.data(), PB.h.size() * sizeof(int), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(dcolpair.p, mc.colpair.data(), ncols * sizeof(unsigned), cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(Eo.p, S.eps + S.n_frozen, o * sizeof(double), cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(Ev.p, S.eps + S.n_occ, v * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(EoB.p, S.epsB + S.nfB, oB * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(EvA.p, S.epsA + S.noccA, vA * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(EvB.p, S.epsB + S.noccB, vB * sizeof(double), cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(e2.p, 0, sizeof(double), s));
-  CK(launch_mp2_coeffs(S.dC, S.L->d_norma, n, S.n_frozen, S.n_occ, Co.p, Cv.p, nullptr, nullptr, s));
+  CK(launch_mp2_coeffs(S.dCA, S.A->d_norma, nA, S.nfA, S.noccA, CoA.p, CvA.p, nullptr, nullptr, s));
+  CK(launch_mp2_coeffs(S.dCB, S.B->d_norma, nB, S.nfB, S.noccB, CoB.p, CvB.p, nullptr, nullptr, s));
   MXParams q = S.q;
   q.colbase = dcolbase.p;
   q.X = X.p;
@@ -1633,24 +1648,32 @@ bool mp2_fp64(MP2Setup &S, size_t budget, double *e2out, cudaStream_t s) {
   for (int bt = 0; bt < nbatch; ++bt) {
     const int k0 = mc.bfirst[bt], k1 = mc.bfirst[bt + 1];
     const int c0 = mc.colbase[k0];
-    const int nb = (int)((k1 < (int)P.h.size() ? mc.colbase[k1] : ncols) - c0);
+    const int nb = (int)((k1 < (int)PB.h.size() ? mc.colbase[k1] : ncols) - c0);
     q.col_first = c0;
     q.ncol = nb;
-    CK(cudaMemsetAsync(X.p, 0, (size_t)n * nb * n * sizeof(double), s));
-    if (!mp2_batch_ints(P, q, k0, k1, s)) return false;
-    // T1 (o x nb*n) = Co^T X ; Y[i][c0 + col][a] = T1[i] (nb x n) Cv
-    if (!dgemm_rm(blas, true, false, o, nb * n, n, Co.p, o, 0, X.p, nb * n, 0, T1.p, nb * n, 0, 1)) return false;
-    if (!dgemm_rm(blas, false, false, nb, v, n, T1.p, n, (long long)nb * n, Cv.p, v, 0, Y.p + (size_t)c0 * v, v,
-                  ncols * v, o))
+    CK(cudaMemsetAsync(X.p, 0, (size_t)nA * nb * nA * sizeof(double), s));
+    if (!mp2_batch_ints(*S.PA, PB, q, k0, k1, s)) return false;
+    // T1 (oA x nb*nA) = CoA^T X ; Y[i][c0 + col][a] = T1[i] (nb x nA) CvA
+    if (!dgemm_rm(blas, true, false, oA, nb * nA, nA, CoA.p, oA, 0, X.p, nb * nA, 0, T1.p, nb * nA, 0, 1))
+      return false;
+    if (!dgemm_rm(blas, false, false, nb, vA, nA, T1.p, nA, (long long)nb * nA, CvA.p, vA, 0, Y.p + (size_t)c0 * vA,
+                  vA, ncols * vA, oA))
       return false;
   }
-  CK(cudaMemsetAsync(Z.p, 0, (size_t)n * n * v * sizeof(double), s));
-  for (int i = 0; i < o; ++i) {
-    CK(launch_mp2_unpack<double>(Y.p + (size_t)i * ncols * v, dcolpair.p, ncols, n, v, Z.p, s));
-    if (!dgemm_rm(blas, true, false, o, n * v, n, Co.p, o, 0, Z.p, n * v, 0, W.p, n * v, 0, 1)) return false;
-    if (!dgemm_rm(blas, true, false, v, v, n, Cv.p, v, 0, W.p, v, (long long)n * v, M.p, v, (long long)v * v, o))
+  CK(cudaMemsetAsync(Z.p, 0, (size_t)nB * nB * vA * sizeof(double), s));
+  for (int i = 0; i < oA; ++i) {
+    CK(launch_mp2_unpack<double>(Y.p + (size_t)i * ncols * vA, dcolpair.p, ncols, nB, vA, Z.p, s));
+    // W (oB x nB*vA) = CoB^T Z ; M_j (vB x vA) = CvB^T W_j
+    if (!dgemm_rm(blas, true, false, oB, nB * vA, nB, CoB.p, oB, 0, Z.p, nB * vA, 0, W.p, nB * vA, 0, 1))
       return false;
-    CK(launch_mp2_energy<double>(M.p, o, v, S.eps[S.n_frozen + i], Eo.p, Ev.p, 1e-10, e2.p, s));
+    if (!dgemm_rm(blas, true, false, vB, vA, nB, CvB.p, vB, 0, W.p, vA, (long long)nB * vA, M.p, vA,
+                  (long long)vB * vA, oB))
+      return false;
+    const double ei = S.epsA[S.nfA + i];
+    if (S.coupling)
+      CK(launch_mp2_energy_coupling<double>(M.p, oB, vB, vA, ei, EoB.p, EvA.p, EvB.p, 1e-10, S.factor, e2.p, s));
+    else
+      CK(launch_mp2_energy<double>(M.p, oB, vB, ei, EoB.p, EvB.p, 1e-10, e2.p, s));
   }
   double e = 0;
   CK(cudaMemcpyAsync(&e, e2.p, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -1663,9 +1686,9 @@ bool mp2_fp64(MP2Setup &S, size_t budget, double *e2out, cudaStream_t s) {
 
 // Split-BF16 back end: the same quarters on the tensor cores (np BF16 pieces
 // per operand, FP32 accumulation), operands written K-major by their producers:
-//   Xt[col][nu][mu]   (integral kernel)          GEMM1: T1[i][col nu] = CoT Xt^T
-//   Y'[a][i][col]     (GEMM2 = CvT T1^T, FP32)   per i: Zt[a][sig][lam] (gather)
-//   GEMM3: Wt[j][a sig] = CoT Zt^T               GEMM4: M_j[b][a] = CvT Wt_j^T
+//   Xt[col][nu][mu]   (integral kernel)          GEMM1: T1[i][col nu] = CoT_A Xt^T
+//   Y'[a][i][col]     (GEMM2 = CvT_A T1^T, FP32) per i: Zt[a][sig][lam] (gather)
+//   GEMM3: Wt[j][a sig] = CoT_B Zt^T             GEMM4: M_j[b][a] = CvT_B Wt_j^T
 struct SplitBuf {
   DevBuf<__nv_bfloat16> p[kMaxPieces];
   bool ensure(int np, size_t n) {
@@ -1685,27 +1708,23 @@ struct SplitBuf {
 
 bool mp2_split(MP2Setup &S, int np, size_t budget, double *e2out, cudaStream_t s) {
   using bf = __nv_bfloat16;
-  const int n = S.n, o = S.o, v = S.v;
-  const int Kp = (n + 63) / 64 * 64;
-  const PairList &P = S.L->sig;
-  const size_t per_col = (size_t)Kp * Kp * 2 * np + (size_t)o * Kp * 2 * np;   // Xt and T1 pieces
+  const int nA = S.nA, nB = S.nB, oA = S.oA, vA = S.vA, oB = S.oB, vB = S.vB;
+  const int KA = (nA + 63) / 64 * 64, KB = (nB + 63) / 64 * 64;
+  const PairList &PB = *S.PB;
+  const size_t per_col = (size_t)KA * KA * 2 * np + (size_t)oA * KA * 2 * np;   // Xt and T1 pieces
   MP2Columns mc;
-  mp2_columns(P, std::max<long long>(36, (long long)(budget / per_col)), mc);
+  mp2_columns(PB, std::max<long long>(36, (long long)(budget / per_col)), mc);
   const long long ncols = mc.ncols;
-  long long colB = 0;
-  for (size_t b = 0; b + 1 < mc.bfirst.size(); ++b) {
-    const int k1 = mc.bfirst[b + 1];
-    colB = std::max<long long>(colB, (k1 < (int)P.h.size() ? mc.colbase[k1] : ncols) - mc.colbase[mc.bfirst[b]]);
-  }
-  // gather lists: row sig -> (lam, col) with Z[lam][sig] = Y[col]
-  std::vector<int> rowptr(n + 1, 0);
+  const long long colB = mp2_max_batch(mc, PB);
+  // gather lists over B's functions: row sig -> (lam, col) with Z[lam][sig] = Y[col]
+  std::vector<int> rowptr(nB + 1, 0);
   for (long long c = 0; c < ncols; ++c) {
     const unsigned cp = mc.colpair[c];
     rowptr[((cp >> 16) & 0x7fff) + 1]++;
     if (cp >> 31) rowptr[(cp & 0xffff) + 1]++;
   }
-  for (int r = 0; r < n; ++r) rowptr[r + 1] += rowptr[r];
-  std::vector<int2> ent(rowptr[n]);
+  for (int r = 0; r < nB; ++r) rowptr[r + 1] += rowptr[r];
+  std::vector<int2> ent(rowptr[nB]);
   {
     std::vector<int> fill(rowptr.begin(), rowptr.end() - 1);
     for (long long c = 0; c < ncols; ++c) {
@@ -1715,82 +1734,90 @@ bool mp2_split(MP2Setup &S, int np, size_t budget, double *e2out, cudaStream_t s
       if (cp >> 31) ent[fill[lam]++] = make_int2(sig | lam << 16, (int)c);
     }
   }
-  const size_t need = (size_t)v * o * ncols * 4 + (size_t)colB * per_col + ((size_t)v * Kp * Kp + (size_t)o * v * Kp +
-                      (size_t)(o + v) * Kp) * 2 * np + (size_t)o * v * v * 4 + ent.size() * 8;
+  const size_t need = (size_t)vA * oA * ncols * 4 + (size_t)colB * per_col +
+                      ((size_t)vA * KB * KB + (size_t)oB * vA * KB + (size_t)(oA + vA) * KA + (size_t)(oB + vB) * KB) *
+                          2 * np +
+                      (size_t)oB * vB * vA * 4 + ent.size() * 8;
   if (!mp2_need(need)) return false;
-  SplitBuf CoT, CvT, X, T1, Z, W;
+  SplitBuf CoTA, CvTA, CoTB, CvTB, X, T1, Z, W;
   DevBuf<float> Y, M;
-  DevBuf<double> Eo, Ev, e2;
+  DevBuf<double> EoB, EvA, EvB, e2;
   DevBuf<int> dcolbase, drowptr, err;
   DevBuf<int2> dent;
-  const size_t xsz = (size_t)colB * Kp * Kp, t1sz = (size_t)o * colB * Kp, zsz = (size_t)v * Kp * Kp,
-               wsz = (size_t)o * v * Kp;
-  if (!CoT.ensure(np, (size_t)o * Kp) || !CvT.ensure(np, (size_t)v * Kp) || !X.ensure(np, xsz) ||
-      !T1.ensure(np, t1sz) || !Z.ensure(np, zsz) || !W.ensure(np, wsz) || !Y.ensure((size_t)v * o * ncols) ||
-      !M.ensure((size_t)o * v * v) || !Eo.ensure(o) || !Ev.ensure(v) || !e2.ensure(1) ||
-      !dcolbase.ensure(P.h.size()) || !drowptr.ensure(n + 1) || !err.ensure(1) ||
-      !dent.ensure(std::max<size_t>(1, ent.size())))
+  const size_t xsz = (size_t)colB * KA * KA, t1sz = (size_t)oA * colB * KA, zsz = (size_t)vA * KB * KB,
+               wsz = (size_t)oB * vA * KB;
+  if (!CoTA.ensure(np, (size_t)oA * KA) || !CvTA.ensure(np, (size_t)vA * KA) || !CoTB.ensure(np, (size_t)oB * KB) ||
+      !CvTB.ensure(np, (size_t)vB * KB) || !X.ensure(np, xsz) || !T1.ensure(np, t1sz) || !Z.ensure(np, zsz) ||
+      !W.ensure(np, wsz) || !Y.ensure((size_t)vA * oA * ncols) || !M.ensure((size_t)oB * vB * vA) ||
+      !EoB.ensure(oB) || !EvA.ensure(vA) || !EvB.ensure(vB) || !e2.ensure(1) || !dcolbase.ensure(PB.h.size()) ||
+      !drowptr.ensure(nB + 1) || !err.ensure(1) || !dent.ensure(std::max<size_t>(1, ent.size())))
     return false;
-  CK(cudaMemcpyAsync(dcolbase.p, mc.colbase.data(), P.h.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(drowptr.p, rowptr.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dcolbase.p, mc.colbase.data(), PB.h.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(drowptr.p, rowptr.data(), (nB + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(dent.p, ent.data(), ent.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(Eo.p, S.eps + S.n_frozen, o * sizeof(double), cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(Ev.p, S.eps + S.n_occ, v * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(EoB.p, S.epsB + S.nfB, oB * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(EvA.p, S.epsA + S.noccA, vA * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(EvB.p, S.epsB + S.noccB, vB * sizeof(double), cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(e2.p, 0, sizeof(double), s));
   CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
-  for (const SplitBuf *b : {&CoT, &CvT, &Z})
-    for (int q = 0; q < np; ++q) CK(cudaMemsetAsync(b->p[q].p, 0, b->p[q].n * sizeof(bf), s));
+  for (const SplitBuf *b : {&CoTA, &CvTA, &CoTB, &CvTB, &Z})
+    for (int k = 0; k < np; ++k) CK(cudaMemsetAsync(b->p[k].p, 0, b->p[k].n * sizeof(bf), s));
   bf *t0[kMaxPieces], *t1[kMaxPieces];
-  CK(launch_mp2_coeffs_bf16(S.dC, S.L->d_norma, n, S.n_frozen, S.n_occ, Kp, np, CoT.ptrs(t0), CvT.ptrs(t1), s));
+  CK(launch_mp2_coeffs_bf16(S.dCA, S.A->d_norma, nA, S.nfA, S.noccA, KA, np, CoTA.ptrs(t0), CvTA.ptrs(t1), s));
+  CK(launch_mp2_coeffs_bf16(S.dCB, S.B->d_norma, nB, S.nfB, S.noccB, KB, np, CoTB.ptrs(t0), CvTB.ptrs(t1), s));
   // np 3: every quarter on the precise engine (the tensor cores round their
-  // FP32 running sums toward zero; over a 640-term contraction that bias, not
-  // the BF16 pieces, dominated the energy error); np 2: the plain engine
-  auto gemm = [&](const Bf16Split &A, long long ar, const Bf16Split &B, long long br, int M, int N, int batch,
-                  int abr, int bbr, const GemmOut &out) {
-    return np == 3 ? launch_gemm_precise(A, ar, B, br, Kp, M, N, batch, abr, bbr, out, err.p, s)
-                   : launch_gemm_split(A, ar, B, br, Kp, M, N, batch, abr, bbr, np, out, err.p, s);
+  // FP32 running sums toward zero; over a long contraction that bias, not
+  // the BF16 pieces, dominated the energy error); np 2: the split engine
+  auto gemm = [&](const Bf16Split &Am, long long ar, const Bf16Split &Bm, long long br, int Kp, int Mr, int Nc,
+                  int batch, int abr, int bbr, const GemmOut &out) {
+    return np == 3 ? launch_gemm_precise(Am, ar, Bm, br, Kp, Mr, Nc, batch, abr, bbr, out, err.p, s)
+                   : launch_gemm_split(Am, ar, Bm, br, Kp, Mr, Nc, batch, abr, bbr, np, out, err.p, s);
   };
   MXParams q = S.q;
   q.colbase = dcolbase.p;
   q.X = nullptr;
   for (int k = 0; k < kMaxPieces; ++k) q.Xp[k] = X.p[k].p;
   q.np = np;
-  q.Kp = Kp;
+  q.Kp = KA;
   const int nbatch = (int)mc.bfirst.size() - 1;
   for (int bt = 0; bt < nbatch; ++bt) {
     const int k0 = mc.bfirst[bt], k1 = mc.bfirst[bt + 1];
     const int c0 = mc.colbase[k0];
-    const int nb = (int)((k1 < (int)P.h.size() ? mc.colbase[k1] : ncols) - c0);
+    const int nb = (int)((k1 < (int)PB.h.size() ? mc.colbase[k1] : ncols) - c0);
     q.col_first = c0;
     q.ncol = nb;
-    for (int k = 0; k < np; ++k) CK(cudaMemsetAsync(X.p[k].p, 0, (size_t)nb * Kp * Kp * sizeof(bf), s));
-    if (!mp2_batch_ints(P, q, k0, k1, s)) return false;
+    for (int k = 0; k < np; ++k) CK(cudaMemsetAsync(X.p[k].p, 0, (size_t)nb * KA * KA * sizeof(bf), s));
+    if (!mp2_batch_ints(*S.PA, PB, q, k0, k1, s)) return false;
     GemmOut o1{};
     T1.out(o1);
-    o1.ldc = (long long)nb * Kp;
-    CK(gemm(CoT.in(), o, X.in(), (long long)nb * Kp, o, nb * Kp, 1, 0, 0, o1));
+    o1.ldc = (long long)nb * KA;
+    CK(gemm(CoTA.in(), oA, X.in(), (long long)nb * KA, KA, oA, nb * KA, 1, 0, 0, o1));
     GemmOut o2{};
     o2.C = Y.p;
-    o2.ldc = (long long)o * ncols;
+    o2.ldc = (long long)oA * ncols;
     o2.grp_cols = nb;
     o2.gcol_stride = ncols;
     o2.col0 = c0;
-    CK(gemm(CvT.in(), v, T1.in(), (long long)o * nb, v, o * nb, 1, 0, 0, o2));
+    CK(gemm(CvTA.in(), vA, T1.in(), (long long)oA * nb, KA, vA, oA * nb, 1, 0, 0, o2));
   }
   bf *tz[kMaxPieces];
-  for (int i = 0; i < o; ++i) {
-    CK(launch_mp2_unpack_csr(Y.p + (size_t)i * ncols, (long long)o * ncols, drowptr.p, dent.p, n, Kp, v, np,
+  for (int i = 0; i < oA; ++i) {
+    CK(launch_mp2_unpack_csr(Y.p + (size_t)i * ncols, (long long)oA * ncols, drowptr.p, dent.p, nB, KB, vA, np,
                              Z.ptrs(tz), s));
     GemmOut o3{};
     W.out(o3);
-    o3.ldc = (long long)v * Kp;
-    CK(gemm(CoT.in(), o, Z.in(), (long long)v * Kp, o, v * Kp, 1, 0, 0, o3));
+    o3.ldc = (long long)vA * KB;
+    CK(gemm(CoTB.in(), oB, Z.in(), (long long)vA * KB, KB, oB, vA * KB, 1, 0, 0, o3));
     GemmOut o4{};
     o4.C = M.p;
-    o4.ldc = v;
-    o4.c_batch = (long long)v * v;
-    CK(gemm(CvT.in(), v, W.in(), (long long)o * v, v, v, o, 0, v, o4));
-    CK(launch_mp2_energy<float>(M.p, o, v, S.eps[S.n_frozen + i], Eo.p, Ev.p, 1e-10, e2.p, s));
+    o4.ldc = vA;
+    o4.c_batch = (long long)vB * vA;
+    CK(gemm(CvTB.in(), vB, W.in(), (long long)oB * vA, KB, vB, vA, oB, 0, vA, o4));
+    const double ei = S.epsA[S.nfA + i];
+    if (S.coupling)
+      CK(launch_mp2_energy_coupling<float>(M.p, oB, vB, vA, ei, EoB.p, EvA.p, EvB.p, 1e-10, S.factor, e2.p, s));
+    else
+      CK(launch_mp2_energy<float>(M.p, oB, vB, ei, EoB.p, EvB.p, 1e-10, e2.p, s));
   }
   double e = 0;
   int herr = 0;
@@ -1798,7 +1825,7 @@ bool mp2_split(MP2Setup &S, int np, size_t budget, double *e2out, cudaStream_t s
   CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   if (herr) {
-    set_error("mp2_direct: a tensor-core GEMM pipeline wait ran out (code %d)", herr);
+    set_error("mp2: a tensor-core GEMM pipeline wait ran out (code %d)", herr);
     return false;
   }
   *e2out = e;
@@ -1807,14 +1834,22 @@ bool mp2_split(MP2Setup &S, int np, size_t budget, double *e2out, cudaStream_t s
   return true;
 }
 
+bool mp2_run(MP2Setup &S, int precision, size_t budget, double *e2out, cudaStream_t s) {
+  if (precision < 0 || precision > 2) {
+    set_error("mp2: precision %d is not available (0: FP64, 1 / 2: split BF16 in 2 / 3 pieces)", precision);
+    return false;
+  }
+  if (S.nA >= 32768 || S.nB >= 32768) {
+    set_error("mp2: more than 32767 basis functions exceed the column encoding");
+    return false;
+  }
+  return precision == 0 ? mp2_fp64(S, budget, e2out, s) : mp2_split(S, precision + 1, budget, e2out, s);
+}
+
 bool mp2_direct(LibintInterface *L, const double *dD, const double *dC, const double *eps, int n_occ, int n_frozen,
                 int precision, size_t x_budget_bytes, double *e2out, cudaStream_t s) {
   if (!L->is_electron) {
     set_error("mp2_direct: closed-shell MP2 is defined here for an electron species");
-    return false;
-  }
-  if (precision < 0 || precision > 2) {
-    set_error("mp2_direct: precision %d is not available (0: FP64, 1 / 2: split BF16 in 2 / 3 pieces)", precision);
     return false;
   }
   if (!L->ensure_sig()) return false;
@@ -1823,27 +1858,24 @@ bool mp2_direct(LibintInterface *L, const double *dD, const double *dC, const do
     set_error("mp2_direct: need 0 <= n_frozen < n_occ < nbasis (got %d, %d, %d)", n_frozen, n_occ, n);
     return false;
   }
-  if (n >= 32768) {
-    set_error("mp2_direct: %d basis functions exceed the column encoding (32767)", n);
-    return false;
-  }
   MP2Setup S{};
-  S.L = L;
-  S.n = n;
-  S.nsh = nsh;
-  S.n_occ = n_occ;
-  S.n_frozen = n_frozen;
-  S.o = n_occ - n_frozen;
-  S.v = n - n_occ;
-  S.dC = dC;
-  S.eps = eps;
+  S.A = S.B = L;
+  S.PA = S.PB = &L->sig;
+  S.coupling = false;
+  S.factor = 1.0;
+  S.nA = S.nB = n;
+  S.noccA = S.noccB = n_occ;
+  S.nfA = S.nfB = n_frozen;
+  S.oA = S.oB = n_occ - n_frozen;
+  S.vA = S.vB = n - n_occ;
+  S.dCA = S.dCB = dC;
+  S.epsA = S.epsB = eps;
   // shell-block norms of D for the screening
   if (!L->dDs.ensure((size_t)n * n) || !L->dDn.ensure((size_t)nsh * nsh)) return false;
   CK(launch_prepare_density(dD, L->d_norma, L->d_shell_of, n, nsh, L->dDs.p, nullptr, L->dDn.p, nullptr, s));
-  const PairList &P = L->sig;
   MXParams &q = S.q;
-  q.pairs = P.d;
-  q.prims = P.dp;
+  q.pairs = q.kpairs = L->sig.d;
+  q.prims = q.kprims = L->sig.dp;
   q.Dn = L->dDn.p;
   q.nsh = nsh;
   q.screen = 1;
@@ -1851,7 +1883,56 @@ bool mp2_direct(LibintInterface *L, const double *dD, const double *dC, const do
   q.cut = 1e-10;
   q.n = n;
   q.boys = L->boys;
-  return precision == 0 ? mp2_fp64(S, x_budget_bytes, e2out, s) : mp2_split(S, precision + 1, x_budget_bytes, e2out, s);
+  return mp2_run(S, precision, x_budget_bytes, e2out, s);
+}
+
+bool mp2_coupling(LibintInterface *A, LibintInterface *B, const double *dCA, const double *dCB, const double *epsA,
+                  const double *epsB, int noccA, int nfA, int noccB, int nfB, double factor, int precision,
+                  size_t budget, double *e2out, cudaStream_t s) {
+  if (A == B) {
+    set_error("mp2_coupling: the two handles must be different species");
+    return false;
+  }
+  if (!A->ensure_all() || !B->ensure_all()) return false;
+  const int nA = A->nbasis, nB = B->nbasis;
+  if (!(0 <= nfA && nfA < noccA && noccA < nA && 0 <= nfB && nfB < noccB && noccB < nB)) {
+    set_error("mp2_coupling: need 0 <= n_frozen < n_occ < nbasis for both species");
+    return false;
+  }
+  MP2Setup S{};
+  S.A = A;
+  S.B = B;
+  S.PA = &A->all;
+  S.PB = &B->all;
+  S.coupling = true;
+  S.factor = factor;
+  S.nA = nA;
+  S.nB = nB;
+  S.noccA = noccA;
+  S.nfA = nfA;
+  S.noccB = noccB;
+  S.nfB = nfB;
+  S.oA = noccA - nfA;
+  S.vA = nA - noccA;
+  S.oB = noccB - nfB;
+  S.vB = nB - noccB;
+  S.dCA = dCA;
+  S.dCB = dCB;
+  S.epsA = epsA;
+  S.epsB = epsB;
+  // coupling integrals: no density screening (Libint2Iface.cpp:1296-1622),
+  // quartets whose Schwarz bound is below the raw cut contribute nothing
+  MXParams &q = S.q;
+  q.pairs = A->all.d;
+  q.prims = A->all.dp;
+  q.kpairs = B->all.d;
+  q.kprims = B->all.dp;
+  q.screen = 0;
+  q.eps = 0.0;
+  q.cut = 1e-10;
+  q.n = nA;
+  q.boys = A->boys;
+  return mp2_run(S, precision, budget, e2out, s);
 }
 
 }  // namespace
@@ -1867,6 +1948,22 @@ int LowdinGB300_mp2_direct(LibintInterface *lint, const double *dD, const double
   }
   const size_t budget = x_budget_gb > 0 ? (size_t)(x_budget_gb * 1e9) : (size_t)8e9;
   return mp2_direct(lint, dD, dC, eps, n_occ, n_frozen, precision, budget, e2, (cudaStream_t)stream) ? 0 : -1;
+}
+
+int LowdinGB300_mp2_coupling(LibintInterface *a, LibintInterface *b, const double *dCa, const double *dCb,
+                             const double *eps_a, const double *eps_b, int n_occ_a, int n_frozen_a, int n_occ_b,
+                             int n_frozen_b, double factor, int precision, double x_budget_gb, double *e2,
+                             void *stream) {
+  if (!check_handle(a, __func__) || !check_handle(b, __func__)) return -1;
+  if (!dCa || !dCb || !eps_a || !eps_b || !e2) {
+    set_error("%s: null argument", __func__);
+    return -1;
+  }
+  const size_t budget = x_budget_gb > 0 ? (size_t)(x_budget_gb * 1e9) : (size_t)8e9;
+  return mp2_coupling(a, b, dCa, dCb, eps_a, eps_b, n_occ_a, n_frozen_a, n_occ_b, n_frozen_b, factor, precision,
+                      budget, e2, (cudaStream_t)stream)
+             ? 0
+             : -1;
 }
 
 long long LowdinGB300_mp2_last_columns(void) { return g_mp2_last.ncols; }

@@ -78,6 +78,10 @@ def lib():
                                              ctypes.c_double, ctypes.POINTER(ctypes.c_double), _vp]
         L.LowdinGB300_mp2_direct.restype = ctypes.c_int
         L.LowdinGB300_mp2_last_columns.restype = ctypes.c_longlong
+        L.LowdinGB300_mp2_coupling.argtypes = [_vp, _vp, _vp, _vp, _f64p, _f64p, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                               ctypes.c_double, ctypes.POINTER(ctypes.c_double), _vp]
+        L.LowdinGB300_mp2_coupling.restype = ctypes.c_int
         L.LowdinGB300_gemm_bf16_split.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                   ctypes.c_int, _vp]
         L.LowdinGB300_gemm_bf16_split.restype = ctypes.c_int
@@ -122,7 +126,7 @@ EXPORTED_SYMBOLS = [
     "LowdinGB300_batch_new", "LowdinGB300_batch_del", "LowdinGB300_batch_add_system",
     "LowdinGB300_batch_finalize", "LowdinGB300_batch_fock", "LowdinGB300_batch_quartets",
     "LowdinGB300_batch_coupling_quartets", "LowdinGB300_noalloc_scratch_bytes",
-    "LowdinGB300_twobody_device_noalloc", "LowdinGB300_mp2_direct", "LowdinGB300_mp2_last_columns",
+    "LowdinGB300_twobody_device_noalloc", "LowdinGB300_mp2_direct", "LowdinGB300_mp2_last_columns", "LowdinGB300_mp2_coupling",
     "LowdinGB300_gemm_bf16_split", "LowdinGB300_gemm_bf16_precise",
     "LowdinGB300_gemm_bench",
 ]
@@ -322,6 +326,20 @@ class Libint2Interface:
         if rc != 0:
             _check()
             raise LowdinGB300Error("mp2_direct failed")
+        return e2.value
+
+    def mp2_coupling(self, other: "Libint2Interface", ca_ptr: int, cb_ptr: int, eps_a, eps_b, n_occ_a: int,
+                     n_frozen_a: int, n_occ_b: int, n_frozen_b: int, factor: float, precision: int = 0,
+                     x_budget_gb: float = 0.0, stream: int = 0) -> float:
+        """Inter-species MP2 term of this species (A) and `other` (B)."""
+        e2 = ctypes.c_double(0.0)
+        rc = lib().LowdinGB300_mp2_coupling(self.h, other.h, ca_ptr, cb_ptr, np.ascontiguousarray(eps_a, np.float64),
+                                            np.ascontiguousarray(eps_b, np.float64), int(n_occ_a), int(n_frozen_a),
+                                            int(n_occ_b), int(n_frozen_b), float(factor), int(precision),
+                                            float(x_budget_gb), ctypes.byref(e2), stream)
+        if rc != 0:
+            _check()
+            raise LowdinGB300Error("mp2_coupling failed")
         return e2.value
 
     def pair_class_counts(self, all_pairs: bool) -> np.ndarray:

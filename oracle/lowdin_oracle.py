@@ -416,6 +416,53 @@ def rmp2_direct(b: Basis, D: np.ndarray, C: np.ndarray, eps: np.ndarray, n_occ: 
     return e2
 
 
+def mp2_coupling_direct(bA: Basis, sidA: int, CA, epsA, noccA: int, nfA: int,
+                        bB: Basis, sidB: int, CB, epsB, noccB: int, nfB: int, qAqB: float) -> float:
+    """Inter-species MP2 of species A and B through the reference's DIRECT
+    path: first quarter A_i[nu][lam][sig] = sum_mu C_A(mu,i) (mu nu|lam sig)
+    from LibintInterface_compute_coupling_directIT (|raw| > 1e-10,
+    Libint2Iface.cpp:1296-1622), quarters 2-4 dense, MO integrals with
+    |(ia|jb)| <= 1e-10 dropped (TransformIntegralsC.f90), then
+    MPFunctions.f90:682-886: sum (q_A q_B (ia|jb))^2 / (e_i + e_j - e_a - e_b)
+    (the caller multiplies by lambda_A lambda_B, :878-879).
+    C: columns are orbitals."""
+    CoB, CvB = CB[:, nfB:noccB], CB[:, noccB:]
+    CvA = CA[:, noccA:]
+    eoB, evB, evA = epsB[nfB:noccB], epsB[noccB:], epsA[noccA:]
+    Crow = np.ascontiguousarray(CA.T)
+    e2 = 0.0
+    for i in range(nfA, noccA):
+        A = coupling_directIT(bA, sidA, bB, sidB, Crow, i)            # [nu in A][lam in B][sig in B]
+        M = np.einsum("nls,na,lj,sb->ajb", A, CvA, CoB, CvB, optimize=True)   # (ia|jb)
+        M[np.abs(M) <= MO_CUT] = 0.0
+        den = epsA[i] + eoB[None, :, None] - evA[:, None, None] - evB[None, None, :]
+        e2 += float(np.sum((qAqB * M) ** 2 / den))
+    return e2
+
+
+def apmo_mp2(system, res) -> dict:
+    """Second-order correction of an APMO Hartree-Fock solution (no frozen
+    core): the closed-shell intra-species term of every electron species and
+    the inter-species term of every species pair.  One-particle species
+    (lambda = 1) have no intra-species term.  Returns the parts and the total
+    corrected energy."""
+    sp = system.species
+    parts = {}
+    for k, s in enumerate(sp):
+        if s.is_electron and s.n_particles > 1:
+            parts[(k,)] = rmp2_direct(s.basis, res.densities[k], res.coefficients[k], res.orbital_energies[k],
+                                      s.n_occ)
+    for a in range(len(sp)):
+        for b in range(a + 1, len(sp)):
+            A, B = sp[a], sp[b]
+            # lambda_A lambda_B x the pair sum (MPFunctions.f90:878-879); lambda = eta for
+            # electrons (2) and one-particle protons (1)
+            parts[(a, b)] = A.eta * B.eta * mp2_coupling_direct(
+                A.basis, a + 1, res.coefficients[a], res.orbital_energies[a], A.n_occ, 0, B.basis, b + 1,
+                res.coefficients[b], res.orbital_energies[b], B.n_occ, 0, A.charge * B.charge)
+    return {"parts": parts, "e2": sum(parts.values()), "total": res.energy + sum(parts.values())}
+
+
 def rmp2(eri_ao: np.ndarray, C: np.ndarray, eps: np.ndarray, n_occ: int, n_frozen: int = 0) -> float:
     """Closed-shell MP2 correlation energy, sum (ia|jb)[2(ia|jb)-(ib|ja)]/D."""
     o = C[:, n_frozen:n_occ]

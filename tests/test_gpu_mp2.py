@@ -99,3 +99,67 @@ def test_mp2_split_bf16_golden_h2o(L, oracle, golden):
     ref = oracle.rmp2_direct(b, res.densities[0], res.coefficients[0], res.orbital_energies[0], 5)
     e2 = _device_mp2(L, sp, res, 5, 0, precision=2)
     assert abs(e2 - ref) < TOL_MIXED, (e2, ref)
+
+
+def _apmo_device_mp2(L, sysd, res, precision):
+    torch = pytest.importorskip("torch")
+    sps = sysd["species"]
+    hs = [L.Libint2Interface(sp, k + 1) for k, sp in enumerate(sps)]
+    dC = [torch.tensor(np.ascontiguousarray(C.T), device="cuda") for C in res.coefficients]
+    st = torch.cuda.current_stream().cuda_stream
+    occ = [int(round(sp["n_particles"] * sp["particles_fraction"])) for sp in sps]
+    parts = {}
+    dD = torch.tensor(res.densities[0], device="cuda")
+    parts[(0,)] = hs[0].mp2_direct(dD.data_ptr(), dC[0].data_ptr(), res.orbital_energies[0], occ[0], 0, precision,
+                                   stream=st)
+    for a in range(len(sps)):
+        for b in range(a + 1, len(sps)):
+            f = (sps[a]["charge"] * sps[b]["charge"]) ** 2 * sps[a]["eta"] * sps[b]["eta"]
+            parts[(a, b)] = hs[a].mp2_coupling(hs[b], dC[a].data_ptr(), dC[b].data_ptr(), res.orbital_energies[a],
+                                               res.orbital_energies[b], occ[a], 0, occ[b], 0, f, precision,
+                                               stream=st)
+    for h in hs:
+        h.close()
+    return parts
+
+
+def test_apmo_mp2_golden_and_parts(L, oracle, golden):
+    """test/H2O.APMO.MP2: every term against the oracle (FP64 1e-10 Eh, split
+    BF16 1e-6 Eh) and the total against the golden MP2 energy."""
+    sysd = GS.h2o_apmo(golden)
+    sysO = oracle.from_plain(sysd)
+    res = oracle.scf(sysO)
+    ref = oracle.apmo_mp2(sysO, res)
+    for precision, tol in ((0, TOL_E2), (2, TOL_MIXED)):
+        parts = _apmo_device_mp2(L, sysd, res, precision)
+        for k, v in ref["parts"].items():
+            assert abs(parts[k] - v) < tol, (precision, k, parts[k], v)
+    g = golden["values"]["H2O.APMO.MP2"]["MP2 energy"]
+    total = res.energy + sum(_apmo_device_mp2(L, sysd, res, 0).values())
+    assert abs(total - g[0]) <= g[1]
+
+
+def test_mp2_coupling_d_shell_species(L, oracle):
+    """Coupling MP2 between d-shell electrons and a multi-shell proton species."""
+    torch = pytest.importorskip("torch")
+    sysd = S.water(d_shell=True)
+    e = sysd["species"][0]
+    O = e["shells"][0][3]
+    p = S.proton_species([(2, [1.5], [1.0], list(O)), (1, [3.0], [1.0], list(O)), (0, [8.0], [1.0], list(O))],
+                         1, name="H-D_1")
+    rng = np.random.default_rng(41)
+    ne, npn = S.nbasis(e), S.nbasis(p)
+    Ce = np.linalg.qr(rng.normal(size=(ne, ne)))[0]
+    Cp = np.linalg.qr(rng.normal(size=(npn, npn)))[0]
+    ee = np.sort(rng.normal(size=ne)) - np.arange(ne)[::-1] * 0.05
+    ep = np.sort(rng.normal(size=npn)) + 0.0
+    ep[0] -= 5.0
+    he, hp = L.Libint2Interface(e, 1), L.Libint2Interface(p, 2)
+    dCe = torch.tensor(np.ascontiguousarray(Ce.T), device="cuda")
+    dCp = torch.tensor(np.ascontiguousarray(Cp.T), device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    got = he.mp2_coupling(hp, dCe.data_ptr(), dCp.data_ptr(), ee, ep, 5, 1, 1, 0, 2.0, 0, stream=st)
+    ref = 2.0 * oracle.mp2_coupling_direct(oracle.Basis.from_shells(e["shells"]), 1, Ce, ee, 5, 1,
+                                           oracle.Basis.from_shells(p["shells"]), 2, Cp, ep, 1, 0, -1.0)
+    assert abs(got - ref) < 1e-10 * max(1.0, abs(ref))
+    he.close(); hp.close()

@@ -103,6 +103,16 @@ def test_direct_mp2_restatement(oracle, golden):
     assert abs(e_dir - oracle.rmp2(oracle.eri_full(b), C, eps, 5, 1)) < 1e-12
 
 
+def test_golden_apmo_mp2(oracle, golden):
+    """test/H2O.APMO.MP2.py: APMO-MP2 total energy (electron intra-species term
+    + electron-proton and proton-proton inter-species terms)."""
+    sysO = oracle.from_plain(GS.h2o_apmo(golden))
+    res = oracle.scf(sysO)
+    r = oracle.apmo_mp2(sysO, res)
+    ref = golden["values"]["H2O.APMO.MP2"]["MP2 energy"]
+    assert abs(r["total"] - ref[0]) <= ref[1]
+
+
 def test_golden_h2o_apmo(oracle, golden):
     """test/H2O.APMO.MP2.py (RHF-APMO total energy, quantum protons)."""
     res = oracle.scf(oracle.from_plain(GS.h2o_apmo(golden)))
