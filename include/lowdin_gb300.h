@@ -186,6 +186,9 @@ int LowdinGB300_batch_finalize(LowdinGB300_Batch *b, void *stream);
    same split for coupling quartets (bound Q_ab Q_cd max(|D_A|, |D_B|)).
    0 = FP64 throughout. */
 int LowdinGB300_batch_fock(LowdinGB300_Batch *b, int precision, double split, void *stream);
+/* batch_fock replays a CUDA graph of its launch sequence (captured once per
+   precision mode after a first eager build; default on); 0 launches eagerly. */
+int LowdinGB300_batch_use_graph(LowdinGB300_Batch *b, int on);
 /* quartets evaluated per (bra pair class, ket pair class) by the last J/K
    build and by the last coupling build of the batch (36 entries each;
    synchronise `stream`) */

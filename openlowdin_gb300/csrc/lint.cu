@@ -1174,10 +1174,33 @@ struct LowdinGB300_Batch {
   BoysTables boys{nullptr, nullptr};
   long long class_quartets[kNQC] = {0};
 
+  // The launch sequence of one build, captured once per precision mode into
+  // a CUDA graph and replayed (every pointer and task list is fixed once the
+  // batch is finalised).  The first build runs eagerly: it performs the
+  // one-time kernel set-up that must not happen inside a capture.
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    double split = 0.0;
+    long long launches = 0;
+  };
+  Graph graphs[4];
+  cudaStream_t capture = nullptr;
+  bool use_graph = true;
+  long long calls = 0;
+
   ~LowdinGB300_Batch() {
+    drop_graphs();
+    if (capture) cudaStreamDestroy(capture);
     Ds.release(); Dn.release(); Gacc.release(); Jacc.release(); cnt.release(); slots.release();
     Ds32.release(); Dn32.release(); Gacc32.release(); Jacc32.release();
     jk.release(); cp.release();
+  }
+
+  void drop_graphs() {
+    for (auto &g : graphs) {
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+      g = Graph{};
+    }
   }
 
   bool finalize(cudaStream_t s) {
@@ -1185,6 +1208,8 @@ struct LowdinGB300_Batch {
       set_error("batch_finalize: empty batch");
       return false;
     }
+    drop_graphs();
+    calls = 0;
     if (!device_boys(boys)) return false;
     // device buffers of the handles
     for (auto &x : sp) {
@@ -1259,6 +1284,41 @@ struct LowdinGB300_Batch {
       set_error("batch_fock: batch not finalised");
       return false;
     }
+    if (!use_graph || calls++ == 0) return fock_sequence(precision, split, s);
+    Graph &g = graphs[precision & 3];
+    if (!g.exec || g.split != split) {
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+      g = Graph{};
+      if (!capture) CK(cudaStreamCreateWithFlags(&capture, cudaStreamNonBlocking));
+      const long long l0 = launch_count();
+      CK(cudaStreamBeginCapture(capture, cudaStreamCaptureModeThreadLocal));
+      const bool ok = fock_sequence(precision, split, capture);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(capture, &graph);
+      const long long captured = launch_count() - l0;
+      count_launches(-captured);   // nothing ran during the capture
+      if (!ok || e != cudaSuccess || !graph) {
+        if (graph) cudaGraphDestroy(graph);
+        set_error("batch_fock: graph capture failed (%s)", cudaGetErrorString(e));
+        return false;
+      }
+      const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ei != cudaSuccess) {
+        g = Graph{};
+        set_error("batch_fock: graph instantiation failed (%s)", cudaGetErrorString(ei));
+        return false;
+      }
+      g.split = split;
+      g.launches = captured;
+    }
+    CK(cudaGraphLaunch(g.exec, s));
+    count_launches(g.launches);
+    return true;
+  }
+
+  // every launch of one build, in stream order
+  bool fock_sequence(int precision, double split, cudaStream_t s) {
     CK(cudaMemsetAsync(Dn.p, 0, Dn.n * sizeof(double), s));
     CK(cudaMemsetAsync(Dn32.p, 0, Dn32.n * sizeof(float), s));
     CK(cudaMemsetAsync(cnt.p, 0, 2 * kNQC * sizeof(unsigned long long), s));
@@ -1305,6 +1365,13 @@ int LowdinGB300_batch_finalize(LowdinGB300_Batch *b, void *stream) {
 int LowdinGB300_batch_fock(LowdinGB300_Batch *b, int precision, double split, void *stream) {
   if (!b) return -1;
   return b->fock(precision, split, (cudaStream_t)stream) ? 0 : -1;
+}
+
+int LowdinGB300_batch_use_graph(LowdinGB300_Batch *b, int on) {
+  if (!b) return -1;
+  b->use_graph = on != 0;
+  if (!b->use_graph) b->drop_graphs();
+  return 0;
 }
 
 int LowdinGB300_batch_quartets(LowdinGB300_Batch *b, long long *out, void *stream) {

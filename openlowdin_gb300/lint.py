@@ -100,6 +100,8 @@ def lib():
         L.LowdinGB300_batch_finalize.restype = ctypes.c_int
         L.LowdinGB300_batch_fock.argtypes = [_vp, ctypes.c_int, ctypes.c_double, _vp]
         L.LowdinGB300_batch_fock.restype = ctypes.c_int
+        L.LowdinGB300_batch_use_graph.argtypes = [_vp, ctypes.c_int]
+        L.LowdinGB300_batch_use_graph.restype = ctypes.c_int
         L.LowdinGB300_batch_quartets.argtypes = [_vp, np.ctypeslib.ndpointer(dtype=np.int64), _vp]
         L.LowdinGB300_batch_quartets.restype = ctypes.c_int
         L.LowdinGB300_batch_coupling_quartets.argtypes = [_vp, np.ctypeslib.ndpointer(dtype=np.int64), _vp]
@@ -124,7 +126,8 @@ EXPORTED_SYMBOLS = [
     "LowdinGB300_last_quartets", "LowdinGB300_version", "LowdinGB300_last_class_quartets",
     "LowdinGB300_pair_class_counts", "LowdinGB300_measure_fma_tflops", "LowdinGB300_launch_count",
     "LowdinGB300_batch_new", "LowdinGB300_batch_del", "LowdinGB300_batch_add_system",
-    "LowdinGB300_batch_finalize", "LowdinGB300_batch_fock", "LowdinGB300_batch_quartets",
+    "LowdinGB300_batch_finalize", "LowdinGB300_batch_fock", "LowdinGB300_batch_use_graph",
+    "LowdinGB300_batch_quartets",
     "LowdinGB300_batch_coupling_quartets", "LowdinGB300_noalloc_scratch_bytes",
     "LowdinGB300_twobody_device_noalloc", "LowdinGB300_mp2_direct", "LowdinGB300_mp2_last_columns", "LowdinGB300_mp2_coupling",
     "LowdinGB300_gemm_bf16_split", "LowdinGB300_gemm_bf16_precise",
@@ -161,6 +164,9 @@ class Batch:
         if lib().LowdinGB300_batch_finalize(self.h, stream) != 0:
             _check()
             raise LowdinGB300Error("batch finalize failed")
+
+    def use_graph(self, on: bool):
+        lib().LowdinGB300_batch_use_graph(self.h, int(bool(on)))
 
     def fock(self, precision: int = 0, split: float = 0.0, stream: int = 0):
         if lib().LowdinGB300_batch_fock(self.h, int(precision), float(split), stream) != 0:

@@ -113,3 +113,43 @@ def test_pipelined_halves_match_single_batch():
         for x, y in zip(ra, rb):
             assert y.converged
             assert abs(x.energy - y.energy) < (1e-9 if prec == "fp64" else 1e-6)
+
+
+def test_batch_fock_graph_replay_matches_eager(scf):
+    """The captured CUDA graph of a batched build gives the eager launches' results."""
+    torch = pytest.importorskip("torch")
+    from openlowdin_gb300 import lint
+    sysd = S.water_cluster(2, seed=4, quantum_protons=True)
+    sps = sysd["species"]
+    rng = np.random.default_rng(51)
+    out = {}
+    for graph in (True, False):
+        hs = [lint.Libint2Interface(sp, k + 1) for k, sp in enumerate(sps)]
+        P = [torch.zeros((h.nbasis, h.nbasis), dtype=torch.float64, device="cuda") for h in hs]
+        G = [torch.zeros_like(p) for p in P]
+        J = [torch.zeros_like(p) for p in P]
+        b = lint.Batch()
+        b.use_graph(graph)
+        b.add_system(hs, [sp["charge"] for sp in sps], [sp["kappa"] / sp["eta"] for sp in sps],
+                     [1] * len(sps), P, G, J)
+        st = torch.cuda.current_stream().cuda_stream
+        b.finalize(st)
+        res = []
+        rr = np.random.default_rng(52)
+        for it in range(4):
+            for p in P:
+                X = rr.normal(size=p.shape) * 0.1
+                p.copy_(torch.tensor(X + X.T))
+            for prec in (0, 3):
+                b.fock(prec, 1e-5, st)
+                torch.cuda.synchronize()
+                res.append((prec, [g.cpu().numpy().copy() for g in G] + [j.cpu().numpy().copy() for j in J]))
+        out[graph] = res
+        b.close()
+        for h in hs:
+            h.close()
+    # FP64 builds: same up to the order of FP64 atomics; mixed builds also
+    # accumulate FP32 atomics, whose order changes their rounding
+    for (prec, a), (_, c) in zip(out[True], out[False]):
+        for x, y in zip(a, c):
+            assert np.max(np.abs(x - y)) < (1e-10 if prec == 0 else 1e-5)
