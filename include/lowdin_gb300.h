@@ -267,6 +267,15 @@ int LowdinGB300_gemm_bf16_precise(const float *dA, const float *dB, float *dC, i
    2 / 3 pieces, 8: precise engine.  Returns milliseconds per launch, or -1. */
 double LowdinGB300_gemm_bench(int M, int N, int K, int mode, int reps, void *stream);
 
+/* One-electron matrices of a species on the device (no counterpart in the
+   reference's C ABI; computes what LibintInterface_compute_1body_ints kinds 1
+   and 2 and LowdinGB300_potential return): dS overlap, dT kinetic, dV
+   sum_C Z_C <a|1/|r-C||b> for the host point charges Z (ncharge) at R
+   (3 ncharge, bohr); device n x n row-major outputs, any may be null.
+   Queued on `stream`.  Returns 0, or -1 with the error set. */
+int LowdinGB300_one_body_device(LibintInterface *lint, int ncharge, const double *Z, const double *R, double *dS,
+                                double *dT, double *dV, void *stream);
+
 /* Number of CUDA kernels this library has launched in the process. */
 long long LowdinGB300_launch_count(void);
 

@@ -22,9 +22,9 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import lint
-from .scf import SCFResult, _one_body, _orthogonaliser_np, n_occ, nuclear_repulsion
+from .scf import SCFResult, _one_body_device, _orthogonaliser, _orthogonaliser_np, n_occ, nuclear_repulsion
 
-HOST_EIGH_MAX = 512   # matrices below this size are diagonalised on the host
+HOST_EIGH_MAX = 384   # matrices below this size are diagonalised on the host (single-threaded LAPACK beats the GPU solver up to ~350 functions)
 
 
 @dataclass
@@ -59,31 +59,33 @@ class BatchSCF:
         self.handles = []       # per system: list of handles
         groups = {}
         self.where = []         # per system: list of (group key, slot)
-        hostmats = {}
+        devmats = {}
         for sysd in systems:
             self.handles.append([lint.Libint2Interface(sp, k + 1) for k, sp in enumerate(sysd["species"])])
-        # one-electron matrices of all molecules on the host pool (the C++
-        # integral code runs without the interpreter lock)
-        one_body = list(self._host_pool().map(lambda a: _one_body(*a), zip(self.handles, systems)))
+        # one-electron matrices on the device (LowdinGB300_one_body_device)
+        stream = torch.cuda.current_stream(self.dev).cuda_stream
         for si, sysd in enumerate(systems):
             hs = self.handles[si]
-            H, S = one_body[si]
+            H, S = _one_body_device(hs, sysd, self.dev, stream)
             w = []
             for k, sp in enumerate(sysd["species"]):
                 key = (hs[k].nbasis, n_occ(sp), float(sp["eta"]))
                 g = groups.setdefault(key, _Group(key[0], key[1], key[2], []))
                 w.append((key, len(g.members)))
                 g.members.append((si, k))
-                hostmats.setdefault(key, []).append((H[k], S[k]))
+                devmats.setdefault(key, []).append((H[k], S[k]))
             self.where.append(w)
         self.groups = groups
         for key, g in groups.items():
-            Hs = np.stack([h for h, _ in hostmats[key]])
-            Ss = np.stack([s for _, s in hostmats[key]])
-            Xs = np.stack([_orthogonaliser_np(s) for s in Ss])
-            g.H = torch.tensor(Hs, device=self.dev)
-            g.S = torch.tensor(Ss, device=self.dev)
-            g.X = torch.tensor(Xs, device=self.dev)
+            g.H = torch.stack([h for h, _ in devmats[key]])
+            g.S = torch.stack([s for _, s in devmats[key]])
+            # S^-1/2 of every member: host LAPACK pool (one transfer) or the GPU solver
+            if g.n < HOST_EIGH_MAX:
+                Sh = g.S.cpu().numpy()
+                Xs = list(self._host_pool().map(_orthogonaliser_np, list(Sh)))
+                g.X = torch.from_numpy(np.stack(Xs)).to(self.dev)
+            else:
+                g.X = torch.stack([_orthogonaliser(x) for x in g.S])
             m = len(g.members)
             g.P = torch.zeros((m, g.n, g.n), dtype=torch.float64, device=self.dev)
             g.G = torch.zeros_like(g.P)

@@ -284,6 +284,24 @@ template <typename T>
 cudaError_t launch_split_bf16(const T *src, long long rows, int cols, long long lds, int np, __nv_bfloat16 *const *out,
                               long long ldo, cudaStream_t s);
 
+// one-electron matrices of one species (k_onebody.cu)
+struct DevShell {
+  int l, nprim, p0, pad;
+  double O[3];
+};
+struct OneBodyParams {
+  const DevShell *shells;
+  const double *alpha, *cn;   // per primitive: exponent, coefficient x primitive norm
+  const int *first;           // first function of each shell
+  const double *norma;
+  int nsh, n;
+  int ncharge;
+  const double *Z, *R;        // device point charges and positions (3 per charge)
+  double *S, *T, *V;          // n x n outputs (any may be null)
+  BoysTables boys;
+};
+cudaError_t launch_one_body(const OneBodyParams &p, cudaStream_t s);
+
 // x[i] = deterministic pseudo-random values in [-1, 1) (benchmark operands)
 cudaError_t launch_fill_hash(float *x, long long n, unsigned seed, cudaStream_t s);
 

@@ -427,6 +427,10 @@ struct LibintInterface {
   bool have_sig = false, have_all = false;
   double *d_norma = nullptr;
   int *d_shell_of = nullptr;
+  DevShell *d_shells = nullptr;
+  double *d_alpha = nullptr, *d_cn = nullptr;
+  int *d_first = nullptr;
+  DevBuf<double> dZR;          // point charges and positions of the last one-body call
   DevBuf<double> dD, dDs, dDn, dGacc, dG, dA, dC, dDsC, dJacc;
   DevBuf<float> dDs32, dDn32, dGacc32, dDsC32, dJacc32;
   DevBuf<unsigned long long> dcount;
@@ -444,8 +448,14 @@ struct LibintInterface {
     all.release();
     if (d_norma) cudaFree(d_norma);
     if (d_shell_of) cudaFree(d_shell_of);
+    for (void *q : {(void *)d_shells, (void *)d_alpha, (void *)d_cn, (void *)d_first})
+      if (q) cudaFree(q);
     d_norma = nullptr;
     d_shell_of = nullptr;
+    d_shells = nullptr;
+    d_alpha = d_cn = nullptr;
+    d_first = nullptr;
+    dZR.release();
     dD.release(); dDs.release(); dDn.release(); dGacc.release(); dG.release(); dA.release(); dC.release();
     dDsC.release(); dJacc.release();
     dDs32.release(); dDn32.release(); dGacc32.release(); dDsC32.release(); dJacc32.release();
@@ -482,6 +492,22 @@ struct LibintInterface {
     d_shell_of = nullptr;
     if (!dev_upload(d_norma, norma)) return false;
     if (!dev_upload(d_shell_of, shell_of)) return false;
+    // shells for the one-electron kernels
+    std::vector<DevShell> ds(nshell());
+    std::vector<double> al, cn;
+    for (int k = 0; k < nshell(); ++k) {
+      const HostShell &h = shells[k];
+      ds[k].l = h.l;
+      ds[k].nprim = h.nprim;
+      ds[k].p0 = (int)al.size();
+      ds[k].pad = 0;
+      for (int d = 0; d < 3; ++d) ds[k].O[d] = h.O[d];
+      al.insert(al.end(), h.alpha.begin(), h.alpha.end());
+      cn.insert(cn.end(), h.cn.begin(), h.cn.end());
+    }
+    if (!dev_upload(d_shells, ds) || !dev_upload(d_alpha, al) || !dev_upload(d_cn, cn) ||
+        !dev_upload(d_first, first))
+      return false;
     have_sig = have_all = false;
     jk_ready = false;
     dirty = false;
@@ -1099,6 +1125,45 @@ void LowdinGB300_potential(LibintInterface *lint, int ncharge, const double *Z, 
           result[(size_t)i * n + j] = V[f1 * n2 + f2] * lint->norma[i] * lint->norma[j];
         }
     }
+}
+
+int LowdinGB300_one_body_device(LibintInterface *lint, int ncharge, const double *Z, const double *R, double *dS,
+                                double *dT, double *dV, void *stream) {
+  if (!check_handle(lint, __func__)) return -1;
+  if (!lint->ensure_base()) return -1;
+  cudaStream_t s = (cudaStream_t)stream;
+  OneBodyParams p{};
+  p.shells = lint->d_shells;
+  p.alpha = lint->d_alpha;
+  p.cn = lint->d_cn;
+  p.first = lint->d_first;
+  p.norma = lint->d_norma;
+  p.nsh = lint->nshell();
+  p.n = lint->nbasis;
+  p.ncharge = dV ? ncharge : 0;
+  p.S = dS;
+  p.T = dT;
+  p.V = dV;
+  p.boys = lint->boys;
+  if (p.ncharge > 0) {
+    if (!lint->dZR.ensure((size_t)4 * ncharge)) return -1;
+    if (cudaMemcpyAsync(lint->dZR.p, Z, ncharge * sizeof(double), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(lint->dZR.p + ncharge, R, 3 * ncharge * sizeof(double), cudaMemcpyHostToDevice, s) !=
+            cudaSuccess) {
+      set_error("%s: charge upload failed", __func__);
+      return -1;
+    }
+    p.Z = lint->dZR.p;
+    p.R = lint->dZR.p + ncharge;
+  } else if (dV) {
+    if (cudaMemsetAsync(dV, 0, sizeof(double) * lint->nbasis * lint->nbasis, s) != cudaSuccess) return -1;
+  }
+  const cudaError_t e = launch_one_body(p, s);
+  if (e != cudaSuccess) {
+    set_error("%s: %s", __func__, cudaGetErrorString(e));
+    return -1;
+  }
+  return 0;
 }
 
 int LowdinGB300_twobody_device(LibintInterface *lint, const double *dD, double *dG, double factor, int precision,

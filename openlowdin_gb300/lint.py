@@ -58,6 +58,8 @@ def lib():
         L.LowdinGB300_potential.argtypes = [_vp, ctypes.c_int, _f64p, _f64p, _f64p]
         L.LowdinGB300_twobody_device.argtypes = [_vp, _vp, _vp, ctypes.c_double, ctypes.c_int, ctypes.c_double, _vp]
         L.LowdinGB300_twobody_device.restype = ctypes.c_int
+        L.LowdinGB300_one_body_device.argtypes = [_vp, ctypes.c_int, _f64p, _f64p, _vp, _vp, _vp, _vp]
+        L.LowdinGB300_one_body_device.restype = ctypes.c_int
         L.LowdinGB300_coupling_device.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp]
         L.LowdinGB300_coupling_device.restype = ctypes.c_int
         L.LowdinGB300_last_quartets.argtypes = [_vp]
@@ -122,7 +124,7 @@ EXPORTED_SYMBOLS = [
     "libintinterface_compute_g12inter_direct", "LibintInterface_compute_2body_directAll",
     "LibintInterface_compute_coupling_directAll", "libintinterface_compute_g12_directAll",
     "libintinterface_compute_g12inter_directAll", "LowdinGB300_last_error", "LowdinGB300_clear_error",
-    "LowdinGB300_potential", "LowdinGB300_twobody_device", "LowdinGB300_coupling_device",
+    "LowdinGB300_potential", "LowdinGB300_twobody_device", "LowdinGB300_one_body_device", "LowdinGB300_coupling_device",
     "LowdinGB300_last_quartets", "LowdinGB300_version", "LowdinGB300_last_class_quartets",
     "LowdinGB300_pair_class_counts", "LowdinGB300_measure_fma_tflops", "LowdinGB300_launch_count",
     "LowdinGB300_batch_new", "LowdinGB300_batch_del", "LowdinGB300_batch_add_system",
@@ -304,6 +306,17 @@ class Libint2Interface:
         return out
 
     # -------------------------------------------------------- device calls --
+    def one_body_device(self, charges, positions, s_ptr: int = 0, t_ptr: int = 0, v_ptr: int = 0,
+                        stream: int = 0):
+        """S, T and point-charge V on the device (pointers to n x n FP64, 0 to skip)."""
+        Z = np.ascontiguousarray(charges, np.float64)
+        R = np.ascontiguousarray(positions, np.float64).reshape(-1)
+        if lib().LowdinGB300_one_body_device(self.h, len(Z), Z if len(Z) else np.zeros(1),
+                                             R if len(R) else np.zeros(3), s_ptr or None, t_ptr or None,
+                                             v_ptr or None, stream) != 0:
+            _check()
+            raise LowdinGB300Error("one_body_device failed")
+
     def twobody_device(self, d_ptr: int, g_ptr: int, factor: float, precision: int = 0, split: float = 0.0,
                        stream: int = 0):
         rc = lib().LowdinGB300_twobody_device(self.h, d_ptr, g_ptr, float(factor), int(precision), float(split),

@@ -70,6 +70,35 @@ def _one_body(handles, sysd):
     return H, S
 
 
+def _one_body_device(handles, sysd, device, stream):
+    """H = T / mass + q V and S of every species, computed on the device."""
+    import torch
+    H, S = [], []
+    for h, sp in zip(handles, sysd["species"]):
+        n = h.nbasis
+        Sm = torch.empty((n, n), dtype=torch.float64, device=device)
+        T = torch.empty_like(Sm)
+        V = torch.empty_like(Sm)
+        h.one_body_device(sysd["point_charges"], sysd["point_positions"], Sm.data_ptr(), T.data_ptr(),
+                          V.data_ptr(), stream)
+        H.append(T / sp["mass"] + sp["charge"] * V)
+        S.append(Sm)
+    return H, S
+
+
+def _orthogonaliser(S, cut=1e-8, host_max=384):
+    """S^-1/2 (symmetric, or canonical when eigenvalues fall below cut) of a
+    device matrix: host LAPACK below host_max functions, the GPU solver above."""
+    import torch
+    if S.shape[0] < host_max:
+        return torch.from_numpy(_orthogonaliser_np(S.cpu().numpy(), cut)).to(S.device)
+    w, U = torch.linalg.eigh(S)
+    keep = w > cut
+    if bool(keep.all()):
+        return (U * w.rsqrt()) @ U.T
+    return U[:, keep] / torch.sqrt(w[keep])
+
+
 def _orthogonaliser_np(S, cut=1e-8):
     w, U = np.linalg.eigh(S)
     keep = w > cut

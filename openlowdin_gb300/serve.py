@@ -29,10 +29,10 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import lint
-from .scf import _one_body, _orthogonaliser_np, n_occ, nuclear_repulsion
+from .scf import _one_body_device, _orthogonaliser, n_occ, nuclear_repulsion
 from .systems import n_core
 
-HOST_EIGH_MAX = 512
+HOST_EIGH_MAX = 384
 
 
 @dataclass
@@ -161,15 +161,13 @@ class ServingEngine:
         torch = self.torch
         sysd = req.system
         handles = [lint.Libint2Interface(sp, k + 1) for k, sp in enumerate(sysd["species"])]
-        H, S = _one_body(handles, sysd)
+        H, S = _one_body_device(handles, sysd, self.dev, self.stream.cuda_stream)
         sps = []
         for k, sp in enumerate(sysd["species"]):
             n = handles[k].nbasis
-            Ht = torch.tensor(H[k], device=self.dev)
-            St = torch.tensor(S[k], device=self.dev)
-            Xt = torch.tensor(_orthogonaliser_np(S[k]), device=self.dev)
+            Xt = _orthogonaliser(S[k], host_max=HOST_EIGH_MAX)
             z = lambda: torch.zeros((n, n), dtype=torch.float64, device=self.dev)  # noqa: E731
-            sps.append(_Species(n, n_occ(sp), float(sp["eta"]), Ht, St, Xt, z(), z(), z(), z(), z(), z(), z()))
+            sps.append(_Species(n, n_occ(sp), float(sp["eta"]), H[k], S[k], Xt, z(), z(), z(), z(), z(), z(), z()))
         job = _Job(req, handles, sps, nuclear_repulsion(sysd), footprint, now)
         for s, P in zip(job.sp, self._densities([(s, s.H) for s in job.sp])):
             s.P.copy_(P)                                  # core-Hamiltonian guess

@@ -158,3 +158,27 @@ def test_device_entry_points_match_host_calls(L, oracle):
     assert np.max(np.abs(np.tril(Jp) - Bp)) < TOL_FOCK
     assert np.max(np.abs(Je - Je.T)) < 1e-14
     he.close(); hp.close()
+
+
+@pytest.mark.parametrize("which", ["water_d", "apmo_proton", "golden_6311g"])
+def test_one_body_device_matches_host(L, golden, which):
+    """LowdinGB300_one_body_device against the host one-electron blocks."""
+    torch = pytest.importorskip("torch")
+    if which == "water_d":
+        sysd = S.water(d_shell=True); k = 0
+    elif which == "apmo_proton":
+        sysd = S.water_cluster(2, seed=1, quantum_protons=True); k = 1
+    else:
+        sysd = GS.h2o_boa(golden); k = 0
+    sp = sysd["species"][k]
+    h = L.Libint2Interface(sp, k + 1)
+    n = h.nbasis
+    dS, dT, dV = (torch.empty((n, n), dtype=torch.float64, device="cuda") for _ in range(3))
+    h.one_body_device(sysd["point_charges"], sysd["point_positions"], dS.data_ptr(), dT.data_ptr(), dV.data_ptr(),
+                      torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.max(np.abs(dS.cpu().numpy() - h.one_body(1))) < 1e-12
+    assert np.max(np.abs(dT.cpu().numpy() - h.one_body(2))) < 1e-10
+    Vh = h.potential(sysd["point_charges"], sysd["point_positions"])
+    assert np.max(np.abs(dV.cpu().numpy() - Vh)) < 1e-10 * max(1.0, np.max(np.abs(Vh)))
+    h.close()
