@@ -60,6 +60,9 @@ def parse():
                          "core-Hamiltonian-guess densities, then exit")
     ap.add_argument("--profile-precision", type=int, default=0,
                     help="precision bits of the profiled builds (0 FP64, 3 mixed split)")
+    ap.add_argument("--profile-d-waters", type=int, default=0,
+                    help="with --profile-fock: one cluster of this many waters with a d shell on O "
+                         "instead of the APMO batch")
     ap.add_argument("--profile-gemm", type=int, default=0,
                     help="profiling case: tensor-core GEMM engine (2 / 3 pieces, 8 precise) on the MP2 "
                          "first-quarter shape M=128 N=65536 K=640, three launches, then exit")
@@ -74,7 +77,11 @@ def profile_fock(args):
     import torch
     from openlowdin_gb300.batch_scf import BatchSCF
     torch.cuda.set_device(0)
-    mols = systems_for(0, args.batch)
+    if args.profile_d_waters:
+        from openlowdin_gb300 import systems as S
+        mols = [S.water_cluster(args.profile_d_waters, seed=0, o_d=True)]
+    else:
+        mols = systems_for(0, args.batch)
     s = BatchSCF(mols)
     st = torch.cuda.current_stream().cuda_stream
     for g in s.groups.values():
@@ -87,7 +94,7 @@ def profile_fock(args):
         s.batch.fock(args.profile_precision, 1e-5, st)
     b.record()
     torch.cuda.synchronize()
-    print(json.dumps({"profile_fock_builds": args.profile_fock, "molecules": args.batch,
+    print(json.dumps({"profile_fock_builds": args.profile_fock, "molecules": len(mols),
                       "ms_per_build": a.elapsed_time(b) / max(1, args.profile_fock)}))
     s.close()
     return 0

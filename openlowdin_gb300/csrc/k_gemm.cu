@@ -503,12 +503,12 @@ __global__ void __launch_bounds__(kPThreads, 1) gemm_precise_kernel(const __grid
         if (nn >= g.N) continue;
         const long long oc =
             cbase + (g.grp_cols ? (nn / g.grp_cols) * g.gcol_stride + nn % g.grp_cols + g.col0 : nn);
-        const double v = (double)hi[j] + (double)lo[j];
+        // FP32 arithmetic only (the FP64 pipe of this part is 1/64 of the FP32 one)
         if (g.C) {
-          g.C[oc] = (float)v;
+          g.C[oc] = hi[j] + lo[j];
         } else {
           __nv_bfloat16 pc[kMaxPieces];
-          bf16_pieces(v, 3, pc);
+          bf16_pieces_pair(hi[j], lo[j], 3, pc);
 #pragma unroll
           for (int q = 0; q < 3; ++q) g.Cp[q][oc] = pc[q];
         }

@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(128) mp2x_coop_kernel(MXParams P, GenClass K) 
       } else {
         // Xt[col * Kp + nu][mu] and the mirrored bra orientation
         __nv_bfloat16 pc[kMaxPieces];
-        bf16_pieces(v, P.np, pc);
+        bf16_pieces((float)v, P.np, pc);   // three pieces hold the FP32 value exactly
         const size_t kp = P.Kp;
         const size_t j1 = (col * kp + bra.fb + b) * kp + bra.fa + a;
         const size_t j2 = (col * kp + bra.fa + a) * kp + bra.fb + b;

@@ -248,6 +248,18 @@ __device__ __forceinline__ void bf16_pieces(T x, int np, __nv_bfloat16 *p) {
       x -= (T)__bfloat162float(p[k]);
     }
 }
+// pieces of hi + lo (an FP32 pair) without FP64 arithmetic: hi - p0 is exact,
+// so the residual carries the pair to ~2^-32 relative
+__device__ __forceinline__ void bf16_pieces_pair(float hi, float lo, int np, __nv_bfloat16 *p) {
+  p[0] = __float2bfloat16_rn(hi + lo);
+  float r = (hi - __bfloat162float(p[0])) + lo;
+#pragma unroll
+  for (int k = 1; k < kMaxPieces; ++k)
+    if (k < np) {
+      p[k] = __float2bfloat16_rn(r);
+      r -= __bfloat162float(p[k]);
+    }
+}
 struct Bf16Split {
   const __nv_bfloat16 *p[kMaxPieces];
 };
