@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=40)
     ap.add_argument("--serve-rate", type=float, default=100.0, help="Poisson arrival rate (req/s)")
     ap.add_argument("--mp2-waters", type=int, default=8)
+    ap.add_argument("--random-molecules", type=int, default=0,
+                    help="batched-RHF section over this many random chain molecules (0: off)")
     ap.add_argument("--profile-fock", type=int, default=0,
                     help="profiling case: N batched Fock builds of the step's molecules at the "
                          "core-Hamiltonian-guess densities, then exit")
@@ -227,6 +229,42 @@ def serving_section(args):
     out["unconverged_jobs"] = sorted(set(res["fp64"]) - set(both))
     out["max_abs_dE_mixed_vs_plain_Eh"] = float(max(de)) if de else None
     out["max_abs_dE_mp2_mixed_vs_plain_Eh"] = float(max(de2)) if de2 else None
+    out["throughput_ratio_mixed_over_plain"] = out["mixed"]["solves_per_s"] / out["plain"]["solves_per_s"]
+    return out
+
+
+def random_batch_section(args):
+    """Batched RHF over independent random chain molecules (H/C/N/O, 3-30
+    atoms, the generator of the batched-RHF workload): padded size buckets,
+    converged molecules switched off, plain FP64 and mixed, one solve of the
+    whole batch each (a bounded sample of the 512-molecule batch)."""
+    import numpy as np
+    import torch
+    from openlowdin_gb300 import systems as S
+    from openlowdin_gb300.batch_scf import PipelinedSCF
+    mols = [S.chain_molecule(20_000 + i) for i in range(args.random_molecules)]
+    nbf = [S.nbasis(m["species"][0]) for m in mols]
+    out = {"molecules": len(mols), "functions_min": int(min(nbf)), "functions_max": int(max(nbf)),
+           "functions_total": int(sum(nbf)),
+           "note": "bounded sample of the 512-molecule batch; one SCF of every molecule per precision"}
+    res = {}
+    for prec in ("fp64", "mixed"):
+        s = PipelinedSCF(mols, precision=prec)
+        out["buckets"] = sum(len(h.groups) for h in s.halves)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = s.solve()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        s.close()
+        res[prec] = r
+        out["plain" if prec == "fp64" else "mixed"] = {
+            "solves_per_s": len(r) / wall, "wall_s": wall, "converged": int(sum(x.converged for x in r)),
+            "max_iterations": int(max(x.iterations for x in r))}
+    both = [i for i in range(len(mols)) if res["fp64"][i].converged and res["mixed"][i].converged]
+    de = [abs(res["mixed"][i].energy - res["fp64"][i].energy) for i in both]
+    out["jobs_converged_in_both"] = len(both)
+    out["max_abs_dE_mixed_vs_plain_Eh"] = float(max(de)) if de else None
     out["throughput_ratio_mixed_over_plain"] = out["mixed"]["solves_per_s"] / out["plain"]["solves_per_s"]
     return out
 
@@ -542,6 +580,8 @@ def main():
             out["serving"] = serving_section(args)
         if not args.no_mp2:
             out["mp2"] = mp2_section(args)
+        if args.random_molecules > 0:
+            out["random_batch"] = random_batch_section(args)
         print(json.dumps(out))
     if dist is not None:
         dist.barrier()

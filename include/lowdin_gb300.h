@@ -179,8 +179,19 @@ void LowdinGB300_batch_del(LowdinGB300_Batch *b);
 int LowdinGB300_batch_add_system(LowdinGB300_Batch *b, LibintInterface **species, int nspecies,
                                  const double *charges, const double *factors, const int *two_body,
                                  const double **dP, double **dG, double **dJ);
+/* Same with a row stride per species: P, G and J of species k are n_k x n_k
+   blocks of an ld[k] x ld[k] row-major array (ld[k] >= n_k), so molecules of
+   different sizes can share one padded stacked array. ld = NULL: ld[k] = n_k. */
+int LowdinGB300_batch_add_system_ld(LowdinGB300_Batch *b, LibintInterface **species, int nspecies,
+                                    const double *charges, const double *factors, const int *two_body,
+                                    const double **dP, double **dG, double **dJ, const int *ld);
 /* builds pair data, task lists and work arenas (synchronises `stream`) */
 int LowdinGB300_batch_finalize(LowdinGB300_Batch *b, void *stream);
+/* One flag per system (host array, in add order; copied on `stream`): the
+   integral launches of a system whose flag is 0 return at once, leaving its
+   G and J unwritten (a converged molecule of the batch costs no quartets).
+   All systems are active after finalize. */
+int LowdinGB300_batch_set_active(LowdinGB300_Batch *b, const int *flags, void *stream);
 /* precision bits: 1 = two-particle quartets whose Schwarz-density bound
    Q_ab Q_cd max|D block| is below `split` run in FP32 (the rest FP64); 2 = the
    same split for coupling quartets (bound Q_ab Q_cd max(|D_A|, |D_B|)).

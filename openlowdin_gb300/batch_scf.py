@@ -13,6 +13,16 @@ one SCF iteration over any number of molecules is
 which follows openLOWDIN's iteration scheme 3 (src/scf/MultiSCF.f90:276-440):
 every species of a molecule is updated once per global iteration from the
 previous densities, with Pulay DIIS over all species of the molecule.
+
+Molecules of many different sizes (a batch of random molecules) share padded
+size buckets: a member of n_i < n functions occupies the top-left n_i x n_i
+block of its n x n slot (the library reads and writes it with row stride n),
+its padding has S = 1, X = 1 and H = PAD on the diagonal (so the padded
+orbitals sit far above every real one and are never occupied), and its own
+occupation count.  Host eigensolves run on the n_i x n_i block only.  A
+molecule that has converged is switched off in the library
+(LowdinGB300_batch_set_active) and skipped by the eigensolves, so it costs
+nothing while the rest of the batch iterates.
 """
 from __future__ import annotations
 
@@ -25,6 +35,15 @@ from . import lint
 from .scf import SCFResult, _one_body_device, _orthogonaliser, _orthogonaliser_np, n_occ, nuclear_repulsion
 
 HOST_EIGH_MAX = 384   # matrices below this size are diagonalised on the host (single-threaded LAPACK beats the GPU solver up to ~350 functions)
+PAD = 1.0e4           # diagonal of H on padded rows (far above every occupied orbital energy)
+EXACT_GROUPS_MAX = 8  # bucket="auto": exact (n, occ, eta) groups up to this many, padded buckets beyond
+
+
+def bucket_size(n: int) -> int:
+    """Padded size of the bucket holding n functions: multiples of 16 up to
+    128, of 32 up to 256, of 64 above (at most ~25% padding past 64)."""
+    step = 16 if n <= 128 else 32 if n <= 256 else 64
+    return -(-n // step) * step
 
 
 @dataclass
@@ -33,6 +52,9 @@ class _Group:
     occ: int
     eta: float
     members: list        # (system index, species index)
+    ns: object = None    # per member: its own size n_i <= n (ragged groups)
+    occs: object = None  # per member: its own occupied count
+    ragged: bool = False
     H: object = None
     S: object = None
     X: object = None
@@ -46,7 +68,11 @@ class _Group:
 class BatchSCF:
     """SCF of many independent systems at once on one GPU."""
 
-    def __init__(self, systems, device="cuda", precision="fp64", split=1e-5, diis_size=10, rebuild_every=1000):
+    def __init__(self, systems, device="cuda", precision="fp64", split=1e-5, diis_size=10, rebuild_every=1000,
+                 bucket="auto"):
+        """bucket: False = one group per exact (n, occ, eta); True = padded
+        size buckets (bucket_size) with per-member sizes and occupations;
+        "auto" = exact groups when they are at most EXACT_GROUPS_MAX."""
         import torch
         self.torch = torch
         self.rebuild_every = rebuild_every
@@ -64,28 +90,52 @@ class BatchSCF:
             self.handles.append([lint.Libint2Interface(sp, k + 1) for k, sp in enumerate(sysd["species"])])
         # one-electron matrices on the device (LowdinGB300_one_body_device)
         stream = torch.cuda.current_stream(self.dev).cuda_stream
+        exact = {(h.nbasis, n_occ(sp), float(sp["eta"]))
+                 for sysd, hs in zip(systems, self.handles) for h, sp in zip(hs, sysd["species"])}
+        padded = bool(bucket) if bucket != "auto" else len(exact) > EXACT_GROUPS_MAX
         for si, sysd in enumerate(systems):
             hs = self.handles[si]
             H, S = _one_body_device(hs, sysd, self.dev, stream)
             w = []
             for k, sp in enumerate(sysd["species"]):
-                key = (hs[k].nbasis, n_occ(sp), float(sp["eta"]))
-                g = groups.setdefault(key, _Group(key[0], key[1], key[2], []))
+                n_k, occ_k, eta = hs[k].nbasis, n_occ(sp), float(sp["eta"])
+                key = (bucket_size(n_k), eta) if padded else (n_k, occ_k, eta)
+                g = groups.setdefault(key, _Group(key[0], occ_k, eta, [], [], []))
                 w.append((key, len(g.members)))
                 g.members.append((si, k))
+                g.ns.append(n_k)
+                g.occs.append(occ_k)
                 devmats.setdefault(key, []).append((H[k], S[k]))
             self.where.append(w)
         self.groups = groups
         for key, g in groups.items():
-            g.H = torch.stack([h for h, _ in devmats[key]])
-            g.S = torch.stack([s for _, s in devmats[key]])
+            g.ns = np.asarray(g.ns)
+            g.occs = np.asarray(g.occs)
+            g.occ = int(g.occs.max())
+            g.ragged = bool((g.ns != g.n).any() or (g.occs != g.occ).any())
+            if g.ragged:
+                self._pad_members(g, devmats[key])
+            else:
+                g.H = torch.stack([h for h, _ in devmats[key]])
+                g.S = torch.stack([s for _, s in devmats[key]])
             # S^-1/2 of every member: host LAPACK pool (one transfer) or the GPU solver
-            if g.n < HOST_EIGH_MAX:
+            if g.n < HOST_EIGH_MAX or g.ragged:
                 Sh = g.S.cpu().numpy()
-                Xs = list(self._host_pool().map(_orthogonaliser_np, list(Sh)))
-                g.X = torch.from_numpy(np.stack(Xs)).to(self.dev)
+                Xs = list(self._host_pool().map(_orthogonaliser_np, [Sh[i, :k, :k] for i, k in enumerate(g.ns)]))
+                Xp = np.zeros((len(Xs), g.n, g.n))
+                for i, (x, k) in enumerate(zip(Xs, g.ns)):
+                    if x.shape != (k, k):
+                        raise ValueError(f"member {g.members[i]}: overlap of {k} functions is rank-deficient")
+                    Xp[i, :k, :k] = x
+                    Xp[i, range(k, g.n), range(k, g.n)] = 1.0
+                g.X = torch.from_numpy(Xp).to(self.dev)
             else:
                 g.X = torch.stack([_orthogonaliser(x) for x in g.S])
+            g.sys_np = np.array([s for s, _ in g.members])
+            g.nsq = torch.tensor((g.ns.astype(np.float64)) ** 2, device=self.dev)
+            if g.ragged:
+                occ_mask = (np.arange(g.occ)[None, :] < g.occs[:, None]).astype(np.float64)
+                g.occ_mask = torch.from_numpy(occ_mask).to(self.dev)[:, None, :]
             m = len(g.members)
             g.P = torch.zeros((m, g.n, g.n), dtype=torch.float64, device=self.dev)
             g.G = torch.zeros_like(g.P)
@@ -101,17 +151,33 @@ class BatchSCF:
         self.batch = lint.Batch()
         for si, sysd in enumerate(systems):
             sps = sysd["species"]
-            P, G, J = [], [], []
+            P, G, J, ld = [], [], [], []
             for k, sp in enumerate(sps):
                 key, slot = self.where[si][k]
                 g = groups[key]
                 P.append(g.Pin[slot]); G.append(g.Gb[slot]); J.append(g.Jb[slot])
+                ld.append(g.n)
             self.batch.add_system(self.handles[si], [sp["charge"] for sp in sps],
                                   [sp["kappa"] / sp["eta"] for sp in sps],
-                                  [1 if sp["n_particles"] > 1 else 0 for sp in sps], P, G, J)
+                                  [1 if sp["n_particles"] > 1 else 0 for sp in sps], P, G, J, ld=ld)
         self.batch.finalize(torch.cuda.current_stream(self.dev).cuda_stream)
         for key, g in groups.items():
             g.sys_index = torch.tensor([s for s, _ in g.members], device=self.dev)
+
+    def _pad_members(self, g, mats):
+        """Stacked H and S of a ragged group: member i in the top-left
+        n_i x n_i block, PAD / 1 on the diagonal of its padding."""
+        torch = self.torch
+        m = len(mats)
+        g.H = torch.zeros((m, g.n, g.n), dtype=torch.float64, device=self.dev)
+        g.S = torch.zeros_like(g.H)
+        for i, (h, s_) in enumerate(mats):
+            k = int(g.ns[i])
+            g.H[i, :k, :k] = h
+            g.S[i, :k, :k] = s_
+            d = torch.arange(k, g.n, device=self.dev)
+            g.H[i, d, d] = PAD
+            g.S[i, d, d] = 1.0
 
     def close(self):
         self.batch.close()
@@ -124,8 +190,10 @@ class BatchSCF:
         """Density of the n_occ lowest orbitals of F (all species of the group
         at once) by trace-conserving canonical purification (Palser and
         Manolopoulos, Phys. Rev. B 58, 12704 (1998)): batched GEMMs and traces
-        only, no eigensolver.  Returns eta X P' X^T."""
+        only, no eigensolver.  Returns eta X P' X^T (exact groups only)."""
         torch = self.torch
+        if g.ragged:
+            raise ValueError("purification needs one occupation count per group")
         Fp = g.X.transpose(1, 2) @ F @ g.X
         m, n = Fp.shape[0], Fp.shape[-1]
         N = float(g.occ)
@@ -161,85 +229,92 @@ class BatchSCF:
             BatchSCF._pool = cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)))
         return BatchSCF._pool
 
+    def _eigh_host(self, g, Fp, idx, occ_only):
+        """LAPACK eigensolves of the members `idx` of group g on the host pool,
+        each on its own n_i x n_i block.  Returns (w, V) with V[j] the member's
+        n x occ (occ_only) or n x n eigenvectors, zero past its own size and
+        occupation; w[j] its eigenvalues, PAD past its size."""
+        host = Fp[idx].cpu().numpy() if len(idx) != len(g.members) else Fp.cpu().numpy()
+        ncol = g.occ if occ_only else g.n
+        V = np.zeros((host.shape[0], g.n, ncol))
+        w = np.full((host.shape[0], g.n), PAD)
+
+        def work(j0, j1):
+            for j in range(j0, j1):
+                i = idx[j]
+                k, o = int(g.ns[i]), int(g.occs[i])
+                e, U = np.linalg.eigh(host[j, :k, :k])
+                w[j, :k] = e
+                if occ_only:
+                    V[j, :k, :o] = U[:, :o]
+                else:
+                    V[j, :k, :k] = U
+                    V[j, range(k, g.n), range(k, g.n)] = 1.0
+
+        m = host.shape[0]
+        nchunk = max(1, min(m, 16))
+        bounds = [(m * c // nchunk, m * (c + 1) // nchunk) for c in range(nchunk)]
+        return w, V, [self._host_pool().submit(work, a, b) for a, b in bounds]
+
+    def _on_host(self, g):
+        return g.n < HOST_EIGH_MAX or g.ragged
+
     def _density(self, g, F):
         """eta C_occ C_occ^T of the Roothaan problem F C = S C e.  Matrices
-        below HOST_EIGH_MAX functions are diagonalised by LAPACK on a host
-        thread pool (a 136 x 136 FP64 eigensolve takes ~2 ms there against
-        ~5 ms for the GPU solver, whose cost is latency, not arithmetic);
-        larger ones use the GPU solver.  The orthogonal transforms and the
-        density product stay on the GPU."""
-        torch = self.torch
-        Fp = g.X.transpose(1, 2) @ F @ g.X
-        if g.n >= HOST_EIGH_MAX:
-            e, Cp = torch.linalg.eigh(Fp)
-            Co = g.X @ Cp[:, :, :g.occ]
-            return g.eta * Co @ Co.transpose(1, 2)
-        host = Fp.cpu().numpy()
-        occ = g.occ
-        vecs = np.empty((host.shape[0], host.shape[1], occ))
-
-        def work(i):
-            w, V = np.linalg.eigh(host[i])
-            vecs[i] = V[:, :occ]
-
-        list(self._host_pool().map(work, range(host.shape[0])))
-        Cp = torch.from_numpy(vecs).to(self.dev, non_blocking=True)
-        Co = g.X @ Cp
-        return g.eta * Co @ Co.transpose(1, 2)
+        below HOST_EIGH_MAX functions (and every member of a ragged group) are
+        diagonalised by LAPACK on a host thread pool (a 136 x 136 FP64
+        eigensolve takes ~2 ms there against ~5 ms for the GPU solver, whose
+        cost is latency, not arithmetic); larger ones use the GPU solver.  The
+        orthogonal transforms and the density product stay on the GPU."""
+        return self._density_collect(g, self._density_submit(g, F))
 
     def _diag(self, g, F):
         torch = self.torch
         Fp = g.X.transpose(1, 2) @ F @ g.X
-        if g.n >= HOST_EIGH_MAX:
+        if not self._on_host(g):
             e, Cp = torch.linalg.eigh(Fp)
         else:
-            host = Fp.cpu().numpy()
-            w = np.empty(host.shape[:2])
-            V = np.empty_like(host)
-
-            def work(i):
-                w[i], V[i] = np.linalg.eigh(host[i])
-
-            list(self._host_pool().map(work, range(host.shape[0])))
+            w, V, futs = self._eigh_host(g, Fp, np.arange(len(g.members)), False)
+            for f in futs:
+                f.result()
             e = torch.from_numpy(w).to(self.dev)
             Cp = torch.from_numpy(V).to(self.dev)
         C = g.X @ Cp
         Co = C[:, :, :g.occ]
+        if g.ragged:
+            Co = Co * g.occ_mask
         return e, C, g.eta * Co @ Co.transpose(1, 2)
 
     # ------------------------------------------------ asynchronous densities --
-    def _density_submit(self, g, F):
-        """Start eta C_occ C_occ^T of F C = S C e for every species of group g:
-        below HOST_EIGH_MAX functions the eigensolves go to the host pool and
-        return futures (the GPU stays free for other work meanwhile); larger
-        matrices are solved on the GPU at once."""
+    def _density_submit(self, g, F, skip=None):
+        """Start eta C_occ C_occ^T of F C = S C e for every species of group g
+        (members with skip[i] set are left out: their result is zero): host
+        eigensolves go to the pool and return futures (the GPU stays free for
+        other work meanwhile); large exact groups are solved on the GPU at once."""
         torch = self.torch
         Fp = g.X.transpose(1, 2) @ F @ g.X
-        if g.n >= HOST_EIGH_MAX:
+        if not self._on_host(g):
             e, Cp = torch.linalg.eigh(Fp)
             Co = g.X @ Cp[:, :, :g.occ]
             return ("done", g.eta * Co @ Co.transpose(1, 2))
-        host = Fp.cpu().numpy()
-        occ = g.occ
-        vecs = np.empty((host.shape[0], host.shape[1], occ))
-
-        def work(i0, i1):
-            for i in range(i0, i1):
-                w, V = np.linalg.eigh(host[i])
-                vecs[i] = V[:, :occ]
-
-        m = host.shape[0]
-        nchunk = min(m, 16)
-        bounds = [(m * k // nchunk, m * (k + 1) // nchunk) for k in range(nchunk)]
-        return ("host", vecs, [self._host_pool().submit(work, a, b) for a, b in bounds])
+        idx = np.arange(len(g.members)) if skip is None else np.flatnonzero(~skip)
+        if len(idx) == 0:
+            return ("done", torch.zeros_like(F))
+        _, V, futs = self._eigh_host(g, Fp, idx, True)
+        return ("host", idx, V, futs)
 
     def _density_collect(self, g, pending):
+        torch = self.torch
         if pending[0] == "done":
             return pending[1]
-        _, vecs, futs = pending
+        _, idx, V, futs = pending
         for f in futs:
             f.result()
-        Cp = self.torch.from_numpy(vecs).to(self.dev, non_blocking=True)
+        Cp = torch.from_numpy(V).to(self.dev, non_blocking=True)
+        if len(idx) != len(g.members):
+            full = torch.zeros((len(g.members), g.n, g.occ), dtype=torch.float64, device=self.dev)
+            full[torch.from_numpy(idx).to(self.dev)] = Cp
+            Cp = full
         Co = g.X @ Cp
         return g.eta * Co @ Co.transpose(1, 2)
 
@@ -262,6 +337,7 @@ class BatchSCF:
         st.conv = np.zeros(self.nsys, bool)
         st.iters = np.zeros(self.nsys, int)
         st.frozen = torch.zeros(self.nsys, dtype=torch.bool, device=self.dev)
+        self.batch.set_active(np.ones(self.nsys, np.int32), st.stream)
         st.it = 0
         st.done = False
         st.tol_energy, st.tol_density, st.max_iter = tol_energy, tol_density, max_iter
@@ -304,6 +380,11 @@ class BatchSCF:
             if full:
                 g.G.copy_(g.Gb)
                 g.J.copy_(g.Jb)
+            elif st.conv[g.sys_np].any():
+                # switched-off (converged) members: their Gb/Jb hold an old increment
+                keep = st.frozen[g.sys_index][:, None, None]
+                g.G.copy_(torch.where(keep, g.G, g.G + g.Gb))
+                g.J.copy_(torch.where(keep, g.J, g.J + g.Jb))
             else:
                 g.G += g.Gb
                 g.J += g.Jb
@@ -356,7 +437,8 @@ class BatchSCF:
             else:
                 c = coef[g.sys_index]                               # [m, h]
                 Fx = sum(c[:, j, None, None] * st.hist_F[j][gi] for j in range(h))
-            st.pending.append(self._density_submit(g, Fx))
+            skip = st.conv[g.sys_np]
+            st.pending.append(self._density_submit(g, Fx, skip if skip.any() else None))
         st.Fs = Fs
         st.energy = energy
 
@@ -368,7 +450,7 @@ class BatchSCF:
         for gi, g in enumerate(st.groups):
             Pn = self._density_collect(g, st.pending[gi])
             keep = st.frozen[g.sys_index]
-            d = torch.sqrt(torch.mean((Pn - g.P) ** 2, dim=(1, 2)))
+            d = torch.sqrt(torch.sum((Pn - g.P) ** 2, dim=(1, 2)) / g.nsq)
             dP = torch.maximum(dP, torch.zeros_like(dP).scatter_reduce_(0, g.sys_index, d, reduce="amax"))
             Pn = torch.where(keep[:, None, None], g.P, Pn)
             g.Flast = torch.where(keep[:, None, None], g.Flast, st.Fs[gi])
@@ -384,8 +466,10 @@ class BatchSCF:
         st.e_old[active] = en[active]
         st.conv |= newly
         if newly.any():
-            # a converged system keeps its energy and density from here on
+            # a converged system keeps its energy and density from here on and
+            # launches no more integral work
             st.frozen |= torch.tensor(newly, device=self.dev)
+            self.batch.set_active(~st.conv, st.stream)
         st.done = bool(st.conv.all()) or st.it >= st.max_iter
 
     def _results(self, st):
@@ -400,9 +484,10 @@ class BatchSCF:
             eps, C, P = [], [], []
             for key, slot in self.where[si]:
                 g = self.groups[key]
-                eps.append(g.eps[slot].cpu().numpy())
-                C.append(g.C[slot].cpu().numpy())
-                P.append(g.P[slot].cpu().numpy())
+                k = int(g.ns[slot])
+                eps.append(g.eps[slot, :k].cpu().numpy())
+                C.append(g.C[slot, :k, :k].cpu().numpy())
+                P.append(g.P[slot, :k, :k].cpu().numpy())
             out.append(SCFResult(float(st.final_e[si]), int(st.iters[si]), bool(st.conv[si]),
                                  time.perf_counter() - st.t0, eps, C, P, quartets))
         return out

@@ -78,6 +78,7 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
   constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND;
   const int t = find_task(tasks, TL.ntasks, blockIdx.x);
   const JKTask &T = tasks[t];
+  if (T.active && __ldg(T.active) == 0) return;   // converged system: nothing to build
   const int local = blockIdx.x - T.blk0;
   const int tx = local % T.nbx, ty = local / T.nbx;
   if (T.triangle && tx * 32 > ty * kWarpsPerBlock + kWarpsPerBlock - 1) return;
@@ -215,6 +216,7 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
   constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND;
   const int t = find_task(tasks, TL.ntasks, blockIdx.x);
   const CPTask &T = tasks[t];
+  if (T.active && __ldg(T.active) == 0) return;   // converged system: nothing to build
   const int local = blockIdx.x - T.blk0;
   const int tx = local % T.nbx, ty = local / T.nbx;
   const int kpos = tx * 32 + threadIdx.x;

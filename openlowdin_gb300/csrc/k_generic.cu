@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(128) jk_coop_kernel(const JKTask *__restrict__
   for (long long u = w0; u < (long long)TL.nblocks * kCoUnitsPerTile; u += wstep) {
     int bpos, kpos0;
     const JKTask &T = coop_unit(tasks, TL.ntasks, (int)u, &bpos, &kpos0);
-    if (bpos >= T.nbra) continue;
+    if (bpos >= T.nbra || (T.active && __ldg(T.active) == 0)) continue;
     for (int kpos = kpos0; kpos < kpos0 + 8 && kpos < T.nket; ++kpos) {
       if (T.triangle && kpos > bpos) break;
       const int bi = T.bra0 + bpos, ki = T.ket0 + kpos;
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(128) cp_coop_kernel(const CPTask *__restrict__
   for (long long u = w0; u < (long long)TL.nblocks * kCoUnitsPerTile; u += wstep) {
     int bpos, kpos0;
     const CPTask &T = coop_unit(tasks, TL.ntasks, (int)u, &bpos, &kpos0);
-    if (bpos >= T.nbra) continue;
+    if (bpos >= T.nbra || (T.active && __ldg(T.active) == 0)) continue;
     for (int kpos = kpos0; kpos < kpos0 + 8 && kpos < T.nket; ++kpos) {
       const int bi = T.bra0 + bpos, ki = T.ket0 + kpos;
       const bool tiny = TL.split > 0.0 ? T.pa32[bi].Q * T.pb32[ki].Q * 0.999f < (float)TL.cut

@@ -124,7 +124,7 @@ __global__ void prepare_batch_kernel(const SpeciesSlot *__restrict__ slots, int 
     const SpeciesSlot &S = slots[find_slot(slots, nslots, x)];
     const long long e = x - S.off;
     const int i = (int)(e / S.n), j = (int)(e % S.n);
-    const double p = S.P[e];
+    const double p = S.P[(long long)i * S.ld + j];
     const double s = p * S.norma[i] * S.norma[j];
     S.Ds[e] = s;
     S.Ds32[e] = (float)s;
@@ -151,16 +151,17 @@ __global__ void finalize_batch_kernel(const SpeciesSlot *__restrict__ slots, int
     const long long e = x - S.off;
     const int i = (int)(e / S.n), j = (int)(e % S.n);
     const double nn = S.norma[i] * S.norma[j];
+    const long long o = (long long)i * S.ld + j;   // outputs may be rows of a wider (padded) matrix
     if (S.G) {
       if (S.Gacc) {
         const long long y = (long long)j * S.n + i;
         const double g = S.Gacc[e] + S.Gacc[y] + (double)S.Gacc32[e] + (double)S.Gacc32[y];
-        S.G[e] = S.gscale * nn * g;
+        S.G[o] = S.gscale * nn * g;
       } else {
-        S.G[e] = 0.0;
+        S.G[o] = 0.0;
       }
     }
-    S.J[e] = nn * (S.Jacc[e] + (double)S.Jacc32[e]);
+    S.J[o] = nn * (S.Jacc[e] + (double)S.Jacc32[e]);
   }
 }
 

@@ -42,6 +42,7 @@ struct JKTask {
   double *Gacc;           // n x n accumulator (symmetrised by the finaliser)
   float *Gacc32;          // FP32 kernels accumulate here (added by the finaliser)
   unsigned long long *count;  // quartets evaluated (may be null)
+  const int *active;      // the task's system is built while *active != 0 (null: always)
   double hf;              // 0.5 * exchange factor
   int bra0, nbra, ket0, nket;
   int n, nsh;
@@ -73,6 +74,7 @@ struct CPTask {
   const float *DnA32;     // shell-block max |D| of A and B (mixed-precision split)
   const float *DnB32;
   unsigned long long *count;  // quartets evaluated (may be null)
+  const int *active;      // the task's system is built while *active != 0 (null: always)
   int nshA, nshB;
   double scale;           // q_A q_B (1 for the reference-shaped calls)
   int bra0, nbra, ket0, nket;
@@ -230,6 +232,7 @@ struct SpeciesSlot {
   double *G, *J;          // outputs (G may be null)
   double gscale;          // 0.25 q^2 for the two-particle matrix
   int n, nsh;
+  int ld;                 // row stride of P, G and J (>= n; the arenas are n x n)
   long long off;          // prefix of n*n over the slots
 };
 cudaError_t launch_prepare_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s);

@@ -1224,7 +1224,9 @@ struct LowdinGB300_Batch {
     const double *P;
     double *G, *J;
     int sys;
+    int ld;            // row stride of P, G, J
   };
+  DevBuf<int> active;  // per system: built while non-zero (LowdinGB300_batch_set_active)
   std::vector<Spec> sp;
   std::vector<int> sys_first;
   bool finalized = false;
@@ -1258,6 +1260,7 @@ struct LowdinGB300_Batch {
     if (capture) cudaStreamDestroy(capture);
     Ds.release(); Dn.release(); Gacc.release(); Jacc.release(); cnt.release(); slots.release();
     Ds32.release(); Dn32.release(); Gacc32.release(); Jacc32.release();
+    active.release();
     jk.release(); cp.release();
   }
 
@@ -1301,6 +1304,23 @@ struct LowdinGB300_Batch {
     std::vector<SpeciesBufs> bf(sp.size());
     jk.clear();
     cp.clear();
+    const int nsys = (int)sys_first.size();
+    if (!active.ensure(std::max(1, nsys))) return false;
+    {
+      std::vector<int> ones(std::max(1, nsys), 1);
+      CK(cudaMemcpyAsync(active.p, ones.data(), ones.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+      CK(cudaStreamSynchronize(s));
+    }
+    // tasks added since `before` belong to system `sys`: they read its active flag
+    auto mark = [&](auto &ts, const std::vector<size_t> &before, int sys) {
+      for (int c = 0; c < kNQC; ++c)
+        for (size_t i = before[c]; i < ts.group[c].size(); ++i) ts.group[c][i].active = active.p + sys;
+    };
+    auto sizes = [](const auto &ts) {
+      std::vector<size_t> v(kNQC);
+      for (int c = 0; c < kNQC; ++c) v[c] = ts.group[c].size();
+      return v;
+    };
     for (size_t k = 0; k < sp.size(); ++k) {
       const Spec &x = sp[k];
       SpeciesSlot &S = hs[k];
@@ -1321,10 +1341,13 @@ struct LowdinGB300_Batch {
       S.n = x.h->nbasis;
       S.nsh = x.h->nshell();
       S.off = off[k];
+      S.ld = x.ld > 0 ? x.ld : S.n;
       if (x.two_body) {
         // non-electron species are not screened: their norm pointers are never read
         SpeciesBufs b{S.Ds, S.Ds32, S.Dn ? S.Dn : Dn.p, S.Dn32 ? S.Dn32 : Dn32.p, S.Gacc, S.Gacc32};
+        const auto before = sizes(jk);
         if (!x.h->add_jk_tasks(jk, b, 0.5 * x.factor, cnt.p)) return false;
+        mark(jk, before, x.sys);
       }
       bf[k] = SpeciesBufs{S.Ds, S.Ds32, S.Dn, S.Dn32, S.Jacc, S.Jacc32};
     }
@@ -1332,8 +1355,10 @@ struct LowdinGB300_Batch {
     for (size_t a = 0; a < sp.size(); ++a)
       for (size_t b = a + 1; b < sp.size(); ++b) {
         if (sp[a].sys != sp[b].sys) continue;
+        const auto before = sizes(cp);
         if (!add_cp_tasks(cp, sp[a].h, sp[b].h, bf[a], bf[b], true, true, sp[a].q * sp[b].q, cnt.p + kNQC))
           return false;
+        mark(cp, before, sp[a].sys);
       }
     nslots = (int)hs.size();
     if (!slots.ensure(hs.size())) return false;
@@ -1405,6 +1430,23 @@ void LowdinGB300_batch_del(LowdinGB300_Batch *b) { delete b; }
 int LowdinGB300_batch_add_system(LowdinGB300_Batch *b, LibintInterface **species, int nspecies,
                                  const double *charges, const double *factors, const int *two_body,
                                  const double **dP, double **dG, double **dJ) {
+  return LowdinGB300_batch_add_system_ld(b, species, nspecies, charges, factors, two_body, dP, dG, dJ, nullptr);
+}
+
+int LowdinGB300_batch_set_active(LowdinGB300_Batch *b, const int *flags, void *stream) {
+  if (!b || !b->finalized || !flags) return -1;
+  const size_t nsys = b->sys_first.size();
+  if (cudaMemcpyAsync(b->active.p, flags, nsys * sizeof(int), cudaMemcpyHostToDevice, (cudaStream_t)stream) !=
+      cudaSuccess) {
+    set_error("batch_set_active: copy failed");
+    return -1;
+  }
+  return 0;
+}
+
+int LowdinGB300_batch_add_system_ld(LowdinGB300_Batch *b, LibintInterface **species, int nspecies,
+                                    const double *charges, const double *factors, const int *two_body,
+                                    const double **dP, double **dG, double **dJ, const int *ld) {
   if (!b || !species || nspecies <= 0) {
     set_error("batch_add_system: invalid arguments");
     return -1;
@@ -1414,8 +1456,12 @@ int LowdinGB300_batch_add_system(LowdinGB300_Batch *b, LibintInterface **species
   b->sys_first.push_back(first);
   for (int k = 0; k < nspecies; ++k) {
     if (!check_handle(species[k], __func__)) return -1;
+    if (ld && ld[k] < species[k]->nbasis) {
+      set_error("batch_add_system: row stride %d below the species' %d functions", ld[k], species[k]->nbasis);
+      return -1;
+    }
     LowdinGB300_Batch::Spec x{species[k], charges[k], factors[k], two_body[k], dP[k], dG ? dG[k] : nullptr,
-                              dJ[k], sys};
+                              dJ[k], sys, ld ? ld[k] : species[k]->nbasis};
     b->sp.push_back(x);
   }
   b->finalized = false;

@@ -98,6 +98,11 @@ def lib():
                                                    np.ctypeslib.ndpointer(dtype=np.int32), ctypes.POINTER(_vp),
                                                    ctypes.POINTER(_vp), ctypes.POINTER(_vp)]
         L.LowdinGB300_batch_add_system.restype = ctypes.c_int
+        L.LowdinGB300_batch_add_system_ld.argtypes = L.LowdinGB300_batch_add_system.argtypes + [
+            np.ctypeslib.ndpointer(dtype=np.int32)]
+        L.LowdinGB300_batch_add_system_ld.restype = ctypes.c_int
+        L.LowdinGB300_batch_set_active.argtypes = [_vp, np.ctypeslib.ndpointer(dtype=np.int32), _vp]
+        L.LowdinGB300_batch_set_active.restype = ctypes.c_int
         L.LowdinGB300_batch_finalize.argtypes = [_vp, _vp]
         L.LowdinGB300_batch_finalize.restype = ctypes.c_int
         L.LowdinGB300_batch_fock.argtypes = [_vp, ctypes.c_int, ctypes.c_double, _vp]
@@ -128,6 +133,7 @@ EXPORTED_SYMBOLS = [
     "LowdinGB300_last_quartets", "LowdinGB300_version", "LowdinGB300_last_class_quartets",
     "LowdinGB300_pair_class_counts", "LowdinGB300_measure_fma_tflops", "LowdinGB300_launch_count",
     "LowdinGB300_batch_new", "LowdinGB300_batch_del", "LowdinGB300_batch_add_system",
+    "LowdinGB300_batch_add_system_ld", "LowdinGB300_batch_set_active",
     "LowdinGB300_batch_finalize", "LowdinGB300_batch_fock", "LowdinGB300_batch_use_graph",
     "LowdinGB300_batch_quartets",
     "LowdinGB300_batch_coupling_quartets", "LowdinGB300_noalloc_scratch_bytes",
@@ -140,14 +146,16 @@ EXPORTED_SYMBOLS = [
 class Batch:
     """Many systems' two-particle + coupling builds in one set of launches.
 
-    add_system(handles, charges, factors, two_body, P, G, J) takes torch
-    tensors (or raw device pointers) for each species' density / outputs."""
+    add_system(handles, charges, factors, two_body, P, G, J[, ld]) takes torch
+    tensors (or raw device pointers) for each species' density / outputs; ld
+    gives each species' row stride when its matrices sit in a larger padded
+    array.  set_active(flags) switches systems' integral work off and on."""
 
     def __init__(self):
         self.h = lib().LowdinGB300_batch_new()
         self._keep = []
 
-    def add_system(self, handles, charges, factors, two_body, P, G, J) -> int:
+    def add_system(self, handles, charges, factors, two_body, P, G, J, ld=None) -> int:
         ns = len(handles)
         ptr = lambda x: x if isinstance(x, int) else (0 if x is None else x.data_ptr())
         hs = (_vp * ns)(*[h.h for h in handles])
@@ -155,12 +163,27 @@ class Batch:
         pG = (_vp * ns)(*[ptr(x) for x in G])
         pJ = (_vp * ns)(*[ptr(x) for x in J])
         self._keep.append((handles, P, G, J))
-        k = lib().LowdinGB300_batch_add_system(self.h, hs, ns, np.ascontiguousarray(charges, np.float64),
-                                               np.ascontiguousarray(factors, np.float64),
-                                               np.ascontiguousarray(two_body, np.int32), pP, pG, pJ)
+        args = (self.h, hs, ns, np.ascontiguousarray(charges, np.float64),
+                np.ascontiguousarray(factors, np.float64), np.ascontiguousarray(two_body, np.int32), pP, pG, pJ)
+        if ld is None:
+            k = lib().LowdinGB300_batch_add_system(*args)
+        else:
+            k = lib().LowdinGB300_batch_add_system_ld(*args, np.ascontiguousarray(ld, np.int32))
         if k < 0:
             _check()
+            raise LowdinGB300Error("batch add_system failed")
+        self.nsys = getattr(self, "nsys", 0) + 1
         return k
+
+    def set_active(self, flags, stream: int = 0):
+        """flags[s] != 0: system s (in add order) is built by the next fock calls."""
+        f = np.ascontiguousarray(np.asarray(flags) != 0, np.int32)
+        if f.size != getattr(self, "nsys", 0):
+            raise ValueError(f"set_active wants {getattr(self, 'nsys', 0)} flags, got {f.size}")
+        self._flags = f
+        if lib().LowdinGB300_batch_set_active(self.h, f, stream) != 0:
+            _check()
+            raise LowdinGB300Error("batch set_active failed")
 
     def finalize(self, stream: int = 0):
         if lib().LowdinGB300_batch_finalize(self.h, stream) != 0:

@@ -153,3 +153,94 @@ def test_batch_fock_graph_replay_matches_eager(scf):
     for (prec, a), (_, c) in zip(out[True], out[False]):
         for x, y in zip(a, c):
             assert np.max(np.abs(x - y)) < (1e-10 if prec == 0 else 1e-5)
+
+
+def test_batch_row_stride_and_active_flags(scf):
+    """Species matrices inside larger padded arrays (row stride ld > n) give
+    the unpadded build and leave the padding untouched; a system switched off
+    with set_active launches no quartets and keeps its outputs."""
+    torch = pytest.importorskip("torch")
+    from openlowdin_gb300 import lint
+    mols = [S.water_cluster(1, seed=0, quantum_protons=True, place=False), S.water()]
+    rng = np.random.default_rng(61)
+    st = torch.cuda.current_stream().cuda_stream
+    runs = {}
+    for padded in (False, True):
+        b = lint.Batch()
+        keep, outs = [], []
+        for m in mols:
+            sps = m["species"]
+            hs = [lint.Libint2Interface(sp, k + 1) for k, sp in enumerate(sps)]
+            P, G, J, ld = [], [], [], []
+            for h in hs:
+                n = h.nbasis
+                L = n + 7 if padded else n
+                X = np.random.default_rng(n).normal(size=(n, n)) * 0.2
+                Pf = torch.full((L, L), 3.0, dtype=torch.float64, device="cuda")
+                Pf[:n, :n] = torch.tensor(X + X.T)
+                P.append(Pf)
+                G.append(torch.full((L, L), -5.0, dtype=torch.float64, device="cuda"))
+                J.append(torch.full((L, L), -5.0, dtype=torch.float64, device="cuda"))
+                ld.append(L)
+            b.add_system(hs, [sp["charge"] for sp in sps], [sp["kappa"] / sp["eta"] for sp in sps],
+                         [1 if sp["n_particles"] > 1 else 0 for sp in sps], P, G, J, ld=ld)
+            keep.append(hs)
+            outs.append((hs, G, J))
+        b.finalize(st)
+        b.fock(0, 0.0, st)
+        q_all = b.quartets(st).sum()
+        torch.cuda.synchronize()
+        res = [[(g[:h.nbasis, :h.nbasis].cpu().numpy().copy(), j[:h.nbasis, :h.nbasis].cpu().numpy().copy())
+                for h, g, j in zip(*o)] for o in outs]
+        if padded:
+            for hs, G, J in outs:
+                for h, g, j in zip(hs, G, J):
+                    n = h.nbasis
+                    assert torch.all(g[n:, :] == -5.0) and torch.all(g[:, n:] == -5.0)
+                    assert torch.all(j[n:, :] == -5.0) and torch.all(j[:, n:] == -5.0)
+            # switch the second system off: its outputs stay, its quartets go
+            for g in outs[1][1]:
+                g.fill_(7.0)
+            b.set_active([1, 0], st)
+            b.fock(0, 0.0, st)
+            q_one = b.quartets(st).sum()
+            torch.cuda.synchronize()
+            assert all(torch.all(g == 7.0) for g in outs[1][1])
+            assert 0 < q_one < q_all
+            for (h, g, j), (g0, j0) in zip(zip(*outs[0]), res[0]):
+                n = h.nbasis
+                assert np.max(np.abs(g[:n, :n].cpu().numpy() - g0)) < 1e-12
+            b.set_active([1, 1], st)
+            b.fock(0, 0.0, st)
+            assert b.quartets(st).sum() == q_all
+        runs[padded] = res
+        b.close()
+        for hs in keep:
+            for h in hs:
+                h.close()
+    for a, c in zip(runs[False], runs[True]):
+        for (g0, j0), (g1, j1) in zip(a, c):
+            assert np.max(np.abs(g0 - g1)) < 1e-11
+            assert np.max(np.abs(j0 - j1)) < 1e-11
+
+
+def test_padded_buckets_match_exact_groups():
+    """Molecules of different sizes in padded buckets (per-member sizes and
+    occupations, converged members switched off) converge to the energies and
+    orbitals of exact-size groups."""
+    from openlowdin_gb300.batch_scf import BatchSCF
+    mols = [S.chain_molecule(700 + i, n_atoms=3 + i % 4) for i in range(6)]
+    mols.append(S.water_cluster(1, seed=0, quantum_protons=True, place=False))
+    out = {}
+    for bucket in (False, True):
+        s = BatchSCF(mols, bucket=bucket)
+        if bucket:
+            assert any(g.ragged for g in s.groups.values())
+        out[bucket] = s.solve(tol_energy=1e-10, tol_density=1e-8)
+        s.close()
+    for a, b in zip(out[False], out[True]):
+        assert a.converged and b.converged
+        assert abs(a.energy - b.energy) < 1e-9
+        for ea, eb in zip(a.orbital_energies, b.orbital_energies):
+            assert ea.shape == eb.shape
+            assert np.max(np.abs(ea - eb)) < 1e-6
