@@ -55,13 +55,15 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=40)
     ap.add_argument("--serve-rate", type=float, default=100.0, help="Poisson arrival rate (req/s)")
     ap.add_argument("--mp2-waters", type=int, default=8)
-    ap.add_argument("--random-molecules", type=int, default=0,
+    ap.add_argument("--random-molecules", type=int, default=32,
                     help="batched-RHF section over this many random chain molecules (0: off)")
     ap.add_argument("--profile-fock", type=int, default=0,
                     help="profiling case: N batched Fock builds of the step's molecules at the "
                          "core-Hamiltonian-guess densities, then exit")
     ap.add_argument("--profile-precision", type=int, default=0,
                     help="precision bits of the profiled builds (0 FP64, 3 mixed split)")
+    ap.add_argument("--profile-random", type=int, default=0,
+                    help="with --profile-fock: this many random chain molecules (batched-RHF generator)")
     ap.add_argument("--profile-d-waters", type=int, default=0,
                     help="with --profile-fock: one cluster of this many waters with a d shell on O "
                          "instead of the APMO batch")
@@ -79,15 +81,18 @@ def profile_fock(args):
     import torch
     from openlowdin_gb300.batch_scf import BatchSCF
     torch.cuda.set_device(0)
+    from openlowdin_gb300 import flops as FL
+    from openlowdin_gb300 import systems as S
     if args.profile_d_waters:
-        from openlowdin_gb300 import systems as S
         mols = [S.water_cluster(args.profile_d_waters, seed=0, o_d=True)]
+    elif args.profile_random:
+        mols = [S.chain_molecule(20_000 + i) for i in range(args.profile_random)]
     else:
         mols = systems_for(0, args.batch)
     s = BatchSCF(mols)
     st = torch.cuda.current_stream().cuda_stream
     for g in s.groups.values():
-        g.Pin.copy_(s._purify(g, g.H))
+        g.Pin.copy_(s._density(g, g.H) if g.ragged else s._purify(g, g.H))
     torch.cuda.synchronize()
     a = torch.cuda.Event(enable_timing=True)
     b = torch.cuda.Event(enable_timing=True)
@@ -96,8 +101,12 @@ def profile_fock(args):
         s.batch.fock(args.profile_precision, 1e-5, st)
     b.record()
     torch.cuda.synchronize()
-    print(json.dumps({"profile_fock_builds": args.profile_fock, "molecules": len(mols),
-                      "ms_per_build": a.elapsed_time(b) / max(1, args.profile_fock)}))
+    ms = a.elapsed_time(b) / max(1, args.profile_fock)
+    q, qc = s.batch.quartets(st), s.batch.coupling_quartets(st)
+    fl = FL.class_table_flops(q, "jk") + FL.class_table_flops(qc, "coupling")
+    print(json.dumps({"profile_fock_builds": args.profile_fock, "molecules": len(mols), "ms_per_build": ms,
+                      "quartets": int(q.sum() + qc.sum()), "quartets_by_class": q.tolist(),
+                      "tflops": fl / (ms * 1e-3) / 1e12}))
     s.close()
     return 0
 
@@ -532,6 +541,7 @@ def main():
         s = BatchSCF(mols, precision="fp64")
         s.solve(tol_energy=1e-8, tol_density=1e-6)
         stv = torch.cuda.current_stream().cuda_stream
+        s.batch.set_active([1] * len(mols), stv)   # the solve switched converged molecules off
         for _ in range(3):
             s.batch.fock(0, 0.0, stv)
         reps = 20

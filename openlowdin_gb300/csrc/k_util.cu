@@ -122,6 +122,7 @@ __global__ void prepare_batch_kernel(const SpeciesSlot *__restrict__ slots, int 
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
        x += (long long)gridDim.x * blockDim.x) {
     const SpeciesSlot &S = slots[find_slot(slots, nslots, x)];
+    if (S.active && __ldg(S.active) == 0) continue;
     const long long e = x - S.off;
     const int i = (int)(e / S.n), j = (int)(e % S.n);
     const double p = S.P[(long long)i * S.ld + j];
@@ -148,6 +149,7 @@ __global__ void finalize_batch_kernel(const SpeciesSlot *__restrict__ slots, int
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
        x += (long long)gridDim.x * blockDim.x) {
     const SpeciesSlot &S = slots[find_slot(slots, nslots, x)];
+    if (S.active && __ldg(S.active) == 0) continue;   // switched-off system: outputs kept
     const long long e = x - S.off;
     const int i = (int)(e / S.n), j = (int)(e % S.n);
     const double nn = S.norma[i] * S.norma[j];

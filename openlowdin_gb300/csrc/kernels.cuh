@@ -234,6 +234,7 @@ struct SpeciesSlot {
   int n, nsh;
   int ld;                 // row stride of P, G and J (>= n; the arenas are n x n)
   long long off;          // prefix of n*n over the slots
+  const int *active;      // the slot's system is built while *active != 0 (null: always)
 };
 cudaError_t launch_prepare_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s);
 cudaError_t launch_finalize_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s);

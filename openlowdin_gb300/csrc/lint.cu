@@ -1342,6 +1342,7 @@ struct LowdinGB300_Batch {
       S.nsh = x.h->nshell();
       S.off = off[k];
       S.ld = x.ld > 0 ? x.ld : S.n;
+      S.active = active.p + x.sys;
       if (x.two_body) {
         // non-electron species are not screened: their norm pointers are never read
         SpeciesBufs b{S.Ds, S.Ds32, S.Dn ? S.Dn : Dn.p, S.Dn32 ? S.Dn32 : Dn32.p, S.Gacc, S.Gacc32};
