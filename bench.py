@@ -62,6 +62,8 @@ def parse():
                          "core-Hamiltonian-guess densities, then exit")
     ap.add_argument("--profile-precision", type=int, default=0,
                     help="precision bits of the profiled builds (0 FP64, 3 mixed split)")
+    ap.add_argument("--profile-split", type=float, default=1e-5,
+                    help="with --profile-fock: FP32/FP64 split bound of the mixed build")
     ap.add_argument("--profile-random", type=int, default=0,
                     help="with --profile-fock: this many random chain molecules (batched-RHF generator)")
     ap.add_argument("--profile-d-waters", type=int, default=0,
@@ -98,7 +100,7 @@ def profile_fock(args):
     b = torch.cuda.Event(enable_timing=True)
     a.record()
     for _ in range(args.profile_fock):
-        s.batch.fock(args.profile_precision, 1e-5, st)
+        s.batch.fock(args.profile_precision, args.profile_split, st)
     b.record()
     torch.cuda.synchronize()
     ms = a.elapsed_time(b) / max(1, args.profile_fock)
