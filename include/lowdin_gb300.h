@@ -197,6 +197,12 @@ int LowdinGB300_batch_set_active(LowdinGB300_Batch *b, const int *flags, void *s
    same split for coupling quartets (bound Q_ab Q_cd max(|D_A|, |D_B|)).
    0 = FP64 throughout. */
 int LowdinGB300_batch_fock(LowdinGB300_Batch *b, int precision, double split, void *stream);
+/* Mixed builds (precision != 0) also drop the quartets whose density-weighted
+   bound (the FP32 bound of the split) is below `skip`: with incremental
+   builds from a density change, late iterations then evaluate only the
+   quartets the change can move by more than `skip`.  Default 0 (only the
+   screening of the plain build). */
+int LowdinGB300_batch_set_skip(LowdinGB300_Batch *b, double skip);
 /* batch_fock replays a CUDA graph of its launch sequence (captured once per
    precision mode after a first eager build; default on); 0 launches eagerly. */
 int LowdinGB300_batch_use_graph(LowdinGB300_Batch *b, int on);

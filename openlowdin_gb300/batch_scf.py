@@ -37,6 +37,10 @@ from .scf import SCFResult, _one_body_device, _orthogonaliser, _orthogonaliser_n
 HOST_EIGH_MAX = 384   # matrices below this size are diagonalised on the host (single-threaded LAPACK beats the GPU solver up to ~350 functions)
 PAD = 1.0e4           # diagonal of H on padded rows (far above every occupied orbital energy)
 EXACT_GROUPS_MAX = 8  # bucket="auto": exact (n, occ, eta) groups up to this many, padded buckets beyond
+# mixed builds drop quartets whose density-weighted bound is below this (from
+# the density change, in incremental builds): the same size as the rounding
+# error of the FP32 quartets just below the split (1e-5 x 2^-24 ~ 6e-13)
+MIXED_SKIP = 1e-12
 
 
 def bucket_size(n: int) -> int:
@@ -44,6 +48,28 @@ def bucket_size(n: int) -> int:
     128, of 32 up to 256, of 64 above (at most ~25% padding past 64)."""
     step = 16 if n <= 128 else 32 if n <= 256 else 64
     return -(-n // step) * step
+
+
+@dataclass
+class _Full:
+    """Every member of a group (the view the final orbitals are computed on)."""
+    H: object
+    S: object
+    X: object
+    nsq: object
+    occ_mask: object
+    sys_index: object
+    sys_np: object
+    ns: object
+    occs: object
+    members: list
+    n: int
+    occ: int
+    eta: float
+    ragged: bool
+
+
+_COMPACT = ("H", "S", "X", "nsq", "occ_mask", "sys_index")   # device tensors sliced by _compact
 
 
 @dataclass
@@ -69,10 +95,12 @@ class BatchSCF:
     """SCF of many independent systems at once on one GPU."""
 
     def __init__(self, systems, device="cuda", precision="fp64", split=1e-5, diis_size=10, rebuild_every=1000,
-                 bucket="auto"):
+                 bucket="auto", skip=MIXED_SKIP):
         """bucket: False = one group per exact (n, occ, eta); True = padded
         size buckets (bucket_size) with per-member sizes and occupations;
-        "auto" = exact groups when they are at most EXACT_GROUPS_MAX."""
+        "auto" = exact groups when they are at most EXACT_GROUPS_MAX.
+        skip (mixed only): quartets whose density-weighted bound (from the
+        density change of an incremental build) is below skip are dropped."""
         import torch
         self.torch = torch
         self.rebuild_every = rebuild_every
@@ -133,18 +161,16 @@ class BatchSCF:
                 g.X = torch.stack([_orthogonaliser(x) for x in g.S])
             g.sys_np = np.array([s for s, _ in g.members])
             g.nsq = torch.tensor((g.ns.astype(np.float64)) ** 2, device=self.dev)
+            g.occ_mask = None
             if g.ragged:
                 occ_mask = (np.arange(g.occ)[None, :] < g.occs[:, None]).astype(np.float64)
                 g.occ_mask = torch.from_numpy(occ_mask).to(self.dev)[:, None, :]
             m = len(g.members)
-            g.P = torch.zeros((m, g.n, g.n), dtype=torch.float64, device=self.dev)
-            g.G = torch.zeros_like(g.P)
-            g.J = torch.zeros_like(g.P)
-            # library build buffers: input density (P or P - P_ref) and outputs
-            g.Pin = torch.zeros_like(g.P)
-            g.Gb = torch.zeros_like(g.P)
-            g.Jb = torch.zeros_like(g.P)
-            g.Pref = torch.zeros_like(g.P)
+            # library build buffers (fixed addresses, every member): input
+            # density (P or P - P_ref) and outputs
+            g.Pin = torch.zeros((m, g.n, g.n), dtype=torch.float64, device=self.dev)
+            g.Gb = torch.zeros_like(g.Pin)
+            g.Jb = torch.zeros_like(g.Pin)
         self.enuc = torch.tensor([nuclear_repulsion(s) for s in systems], dtype=torch.float64, device=self.dev)
         self.nsys = len(systems)
         # library batch: species buffers are slices of the stacked tensors
@@ -161,8 +187,14 @@ class BatchSCF:
                                   [sp["kappa"] / sp["eta"] for sp in sps],
                                   [1 if sp["n_particles"] > 1 else 0 for sp in sps], P, G, J, ld=ld)
         self.batch.finalize(torch.cuda.current_stream(self.dev).cuda_stream)
+        self.batch.set_skip(skip if precision == "mixed" else 0.0)
         for key, g in groups.items():
             g.sys_index = torch.tensor([s for s, _ in g.members], device=self.dev)
+            # the whole group; the iteration works on the members still running
+            # (_reset, _compact)
+            g.full = _Full(H=g.H, S=g.S, X=g.X, nsq=g.nsq, occ_mask=g.occ_mask, sys_index=g.sys_index,
+                           sys_np=g.sys_np, ns=g.ns, occs=g.occs, members=list(g.members), n=g.n, occ=g.occ,
+                           eta=g.eta, ragged=g.ragged)
 
     def _pad_members(self, g, mats):
         """Stacked H and S of a ragged group: member i in the top-left
@@ -322,6 +354,51 @@ class BatchSCF:
     class _State:
         pass
 
+    def _reset(self, g):
+        """Iterate over every member of g again (start of a solve)."""
+        torch = self.torch
+        f = g.full
+        for a in _COMPACT:
+            setattr(g, a, getattr(f, a))
+        g.sys_np, g.ns, g.occs, g.members = f.sys_np, f.ns, f.occs, list(f.members)
+        m = len(f.members)
+        g.alive_np = np.arange(m)
+        g.alive = torch.arange(m, device=self.dev)
+        g.compact = False
+        g.P = torch.zeros((m, g.n, g.n), dtype=torch.float64, device=self.dev)
+        g.G = torch.zeros_like(g.P)
+        g.J = torch.zeros_like(g.P)
+        g.Pref = torch.zeros_like(g.P)
+        g.Pfinal = torch.zeros_like(g.P)
+        g.Ffinal = torch.zeros_like(g.P)
+
+    def _compact(self, st, gi, g, keep):
+        """Drop the members of g whose systems converged (keep[i] False): their
+        final density and Fock matrix are stored, and every per-member tensor
+        of the iteration (matrices, DIIS history) shrinks to the members still
+        running, so converged molecules cost no batched GEMMs either."""
+        torch = self.torch
+        idx = np.flatnonzero(keep)
+        drop = np.flatnonzero(~keep)
+        dl = torch.from_numpy(drop).to(self.dev)
+        dpos = torch.from_numpy(g.alive_np[drop]).to(self.dev)
+        g.Pfinal.index_copy_(0, dpos, g.P.index_select(0, dl))
+        g.Ffinal.index_copy_(0, dpos, g.Flast.index_select(0, dl))
+        il = torch.from_numpy(idx).to(self.dev)
+        for a in _COMPACT + ("P", "G", "J", "Pref", "Flast"):
+            v = getattr(g, a)
+            if v is not None:
+                setattr(g, a, v.index_select(0, il))
+        for hist in (st.hist_F, st.hist_E):
+            for h in hist:
+                if h[gi] is not None:
+                    h[gi] = h[gi].index_select(0, il)
+        g.sys_np, g.ns, g.occs = g.sys_np[idx], g.ns[idx], g.occs[idx]
+        g.members = [g.members[i] for i in idx]
+        g.alive_np = g.alive_np[idx]
+        g.alive = torch.from_numpy(g.alive_np).to(self.dev)
+        g.compact = True
+
     def _state(self, tol_energy, tol_density, max_iter):
         torch = self.torch
         st = BatchSCF._State()
@@ -329,6 +406,7 @@ class BatchSCF:
         st.stream = torch.cuda.current_stream(self.dev).cuda_stream
         st.groups = list(self.groups.values())
         for g in st.groups:
+            self._reset(g)
             g.P.copy_(self._density(g, g.H))      # core-Hamiltonian guess
             g.Flast = g.H.clone()
         st.hist_F, st.hist_E, st.hist_B = [], [], []
@@ -336,7 +414,6 @@ class BatchSCF:
         st.final_e = np.zeros(self.nsys)
         st.conv = np.zeros(self.nsys, bool)
         st.iters = np.zeros(self.nsys, int)
-        st.frozen = torch.zeros(self.nsys, dtype=torch.bool, device=self.dev)
         self.batch.set_active(np.ones(self.nsys, np.int32), st.stream)
         st.it = 0
         st.done = False
@@ -369,29 +446,35 @@ class BatchSCF:
         # incremental couplings run in FP32 (their size scales with |dP|).
         full = (not mixed) or (it - 1) % self.rebuild_every == 0
         for g in groups:
-            if full:
-                g.Pin.copy_(g.P)
+            if not g.members:
+                continue
+            src = g.P if full else g.P - g.Pref
+            if g.compact:
+                g.Pin.index_copy_(0, g.alive, src)
             else:
-                torch.sub(g.P, g.Pref, out=g.Pin)
+                g.Pin.copy_(src)
         # precision bits: 1 = two-particle FP32/FP64 split, 2 = coupling split
         self.batch.fock(3 if mixed else 0, self.split, st.stream)
         self._tick(st, "fock")
         for g in groups:
+            if not g.members:
+                continue
+            Gb = g.Gb.index_select(0, g.alive) if g.compact else g.Gb
+            Jb = g.Jb.index_select(0, g.alive) if g.compact else g.Jb
             if full:
-                g.G.copy_(g.Gb)
-                g.J.copy_(g.Jb)
-            elif st.conv[g.sys_np].any():
-                # switched-off (converged) members: their Gb/Jb hold an old increment
-                keep = st.frozen[g.sys_index][:, None, None]
-                g.G.copy_(torch.where(keep, g.G, g.G + g.Gb))
-                g.J.copy_(torch.where(keep, g.J, g.J + g.Jb))
+                g.G.copy_(Gb)
+                g.J.copy_(Jb)
             else:
-                g.G += g.Gb
-                g.J += g.Jb
+                g.G += Gb
+                g.J += Jb
             g.Pref.copy_(g.P)
         energy = self.enuc.clone()
         Fs, Es = [], []
         for g in groups:
+            if not g.members:
+                Fs.append(None)
+                Es.append(None)
+                continue
             F = g.H + g.G + g.J
             e_sp = torch.sum(g.P * (g.H + 0.5 * g.G + 0.5 * g.J), dim=(1, 2))
             energy.index_add_(0, g.sys_index, e_sp)
@@ -409,6 +492,8 @@ class BatchSCF:
         h = len(st.hist_F)
         row = torch.zeros((self.nsys, h), dtype=torch.float64, device=self.dev)
         for gi, g in enumerate(groups):
+            if not g.members:
+                continue
             cur = Es[gi].reshape(len(g.members), -1)
             for j in range(h):
                 d = torch.sum(cur * st.hist_E[j][gi].reshape(len(g.members), -1), dim=1)
@@ -432,28 +517,30 @@ class BatchSCF:
         self._tick(st, "diis")
         st.pending = []
         for gi, g in enumerate(groups):
+            if not g.members:
+                st.pending.append(None)
+                continue
             if coef is None:
                 Fx = Fs[gi]
             else:
                 c = coef[g.sys_index]                               # [m, h]
                 Fx = sum(c[:, j, None, None] * st.hist_F[j][gi] for j in range(h))
-            skip = st.conv[g.sys_np]
-            st.pending.append(self._density_submit(g, Fx, skip if skip.any() else None))
+            st.pending.append(self._density_submit(g, Fx))
         st.Fs = Fs
         st.energy = energy
 
     def _finish(self, st):
         """Collect the eigensolves started by _start: new densities and the
-        convergence test; sets st.done."""
+        convergence test; sets st.done.  Converged systems leave the batch."""
         torch = self.torch
         dP = torch.zeros(self.nsys, dtype=torch.float64, device=self.dev)
         for gi, g in enumerate(st.groups):
+            if not g.members:
+                continue
             Pn = self._density_collect(g, st.pending[gi])
-            keep = st.frozen[g.sys_index]
             d = torch.sqrt(torch.sum((Pn - g.P) ** 2, dim=(1, 2)) / g.nsq)
             dP = torch.maximum(dP, torch.zeros_like(dP).scatter_reduce_(0, g.sys_index, d, reduce="amax"))
-            Pn = torch.where(keep[:, None, None], g.P, Pn)
-            g.Flast = torch.where(keep[:, None, None], g.Flast, st.Fs[gi])
+            g.Flast = st.Fs[gi]
             g.P.copy_(Pn)
         self._tick(st, "density")
         stats = torch.stack([st.energy, dP]).cpu().numpy()
@@ -465,17 +552,26 @@ class BatchSCF:
         newly = active & (np.abs(en - st.e_old) < st.tol_energy) & (dpn < st.tol_density)
         st.e_old[active] = en[active]
         st.conv |= newly
-        if newly.any():
-            # a converged system keeps its energy and density from here on and
-            # launches no more integral work
-            st.frozen |= torch.tensor(newly, device=self.dev)
-            self.batch.set_active(~st.conv, st.stream)
         st.done = bool(st.conv.all()) or st.it >= st.max_iter
+        if newly.any() and not st.done:
+            # a converged system keeps its energy, density and Fock matrix from
+            # here on: its integral work is switched off and its members leave
+            # the iteration's tensors
+            self.batch.set_active(~st.conv, st.stream)
+            for gi, g in enumerate(st.groups):
+                if g.members:
+                    keep = ~st.conv[g.sys_np]
+                    if not keep.all():
+                        self._compact(st, gi, g, keep)
 
     def _results(self, st):
+        torch = self.torch
         # Roothaan orbitals of the last Fock matrix of every species (one eigh)
         for g in st.groups:
-            g.eps, g.C, _ = self._diag(g, g.Flast)
+            if g.members:
+                g.Pfinal.index_copy_(0, g.alive, g.P)
+                g.Ffinal.index_copy_(0, g.alive, g.Flast)
+            g.eps, g.C, _ = self._diag(g.full, g.Ffinal)
         q = self.batch.quartets(st.stream)
         quartets = int(q.sum())
         self.last_class_quartets = q
@@ -484,10 +580,10 @@ class BatchSCF:
             eps, C, P = [], [], []
             for key, slot in self.where[si]:
                 g = self.groups[key]
-                k = int(g.ns[slot])
+                k = int(g.full.ns[slot])
                 eps.append(g.eps[slot, :k].cpu().numpy())
                 C.append(g.C[slot, :k, :k].cpu().numpy())
-                P.append(g.P[slot, :k, :k].cpu().numpy())
+                P.append(g.Pfinal[slot, :k, :k].cpu().numpy())
             out.append(SCFResult(float(st.final_e[si]), int(st.iters[si]), bool(st.conv[si]),
                                  time.perf_counter() - st.t0, eps, C, P, quartets))
         return out

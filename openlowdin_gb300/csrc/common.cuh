@@ -100,29 +100,52 @@ constexpr int kBoysPoints = 361;          // T_i = 0, 0.1, ..., 36.0
 constexpr int kBoysTaylor = 9;            // terms k = 0..8 (|dT| <= 0.05: error < 6e-18)
 constexpr int kBoysTaylorF32 = 6;
 constexpr int kBoysOrders = kMaxLQuartet + kBoysTaylor + 1;
+constexpr int kBoysStride = kBoysOrders + 1;  // row i: F_0..F_{kBoysOrders-1}(T_i), then e^{-T_i}
+
+// e^x for |x| <= h/2 = 0.05: Taylor polynomial of degree 9 (remainder below
+// 0.05^10 / 10! = 2.7e-20 relative), so e^{-T} = e^{-T_i} e^{T_i - T} costs
+// nine FMAs and one table read
+__host__ __device__ __forceinline__ double exp_small(double x) {
+  double s = 1.0 / 362880.0;  // 1/9!
+  s = fma(s, x, 1.0 / 40320.0);
+  s = fma(s, x, 1.0 / 5040.0);
+  s = fma(s, x, 1.0 / 720.0);
+  s = fma(s, x, 1.0 / 120.0);
+  s = fma(s, x, 1.0 / 24.0);
+  s = fma(s, x, 1.0 / 6.0);
+  s = fma(s, x, 0.5);
+  s = fma(s, x, 1.0);
+  return fma(s, x, 1.0);
+}
+
+__device__ __forceinline__ double rsqrt_r(double x) { return rsqrt(x); }
+__device__ __forceinline__ float rsqrt_r(float x) { return rsqrtf(x); }
 
 template <int L>
 __device__ __forceinline__ void boys_f64(double T, double (&F)[L + 1], const double *__restrict__ tab) {
   if (T < kBoysTMax) {
     const int i = __double2int_rn(T * (1.0 / kBoysH));
     const double mdT = i * kBoysH - T;  // -(T - T_i)
-    const double *t = tab + i * kBoysOrders + L;
+    const double *t = tab + i * kBoysStride + L;
     double s = __ldg(t + kBoysTaylor - 1);
 #pragma unroll
     for (int k = kBoysTaylor - 1; k >= 1; --k) s = fma(mdT * (1.0 / k), s, __ldg(t + k - 1));
     F[L] = s;
     if constexpr (L > 0) {
-      const double e = exp(-T);
+      const double e = __ldg(tab + i * kBoysStride + kBoysOrders) * exp_small(mdT);
       const double twoT = 2.0 * T;
 #pragma unroll
       for (int m = L - 1; m >= 0; --m) F[m] = fma(twoT, F[m + 1], e) * (1.0 / (2 * m + 1));
     }
   } else {
-    const double e = exp(-T);
-    F[0] = 0.88622692545275801365 / sqrt(T);  // sqrt(pi)/2
-    const double o2T = 0.5 / T;
+    const double r = rsqrt(T);
+    F[0] = 0.88622692545275801365 * r;  // sqrt(pi/T)/2
+    if constexpr (L > 0) {
+      const double e = exp(-T);
+      const double o2T = 0.5 * r * r;
 #pragma unroll
-    for (int m = 0; m < L; ++m) F[m + 1] = ((2 * m + 1) * F[m] - e) * o2T;
+      for (int m = 0; m < L; ++m) F[m + 1] = ((2 * m + 1) * F[m] - e) * o2T;
+    }
   }
 }
 
@@ -134,7 +157,7 @@ __device__ __forceinline__ void boys_f32(float T, float (&F)[L + 1], const float
   if (T < (float)kBoysTMax) {
     const int i = __float2int_rn(T * (float)(1.0 / kBoysH));
     const float mdT = i * (float)kBoysH - T;
-    const float *t = tab + i * kBoysOrders + L;
+    const float *t = tab + i * kBoysStride + L;
     float s = __ldg(t + kBoysTaylorF32 - 1);
 #pragma unroll
     for (int k = kBoysTaylorF32 - 1; k >= 1; --k) s = fmaf(mdT * (1.0f / k), s, __ldg(t + k - 1));

@@ -41,7 +41,8 @@ __device__ __forceinline__ void vrr_prim(R (&X)[QClass<LA, LB, LC, LD>::nE * QCl
   constexpr int L = QC_::L, L2 = QC_::L2, NE = QC_::NE, NF = QC_::NF, E0 = QC_::E0, F0 = QC_::F0,
                 nF = QC_::nF;
   const R p = pb.p, q = pk.p;
-  const R opq = R(1) / (p + q);
+  const R rs = rsqrt_r(p + q);    // 1 / sqrt(p + q)
+  const R opq = rs * rs;
   const R rp = q * opq;          // rho / p
   const R rq = p * opq;          // rho / q
   const R rho = p * rp;          // p q / (p + q)
@@ -58,7 +59,7 @@ __device__ __forceinline__ void vrr_prim(R (&X)[QClass<LA, LB, LC, LD>::nE * QCl
   R F[L + 1];
   BoysTab<R>::template eval<L>(rho * PQ2, F, boys64, boys32);
   // 2 pi^{5/2} K_ab K_cd / (p q sqrt(p + q)) with the constants folded into Kt
-  const R pref = pb.Kt * pk.Kt * sqrt(opq);
+  const R pref = pb.Kt * pk.Kt * rs;
   const R o2p = R(0.5) * pb.inv_p, o2q = R(0.5) * pk.inv_p, o2pq = R(0.5) * opq;
 
   // bra nodes Vb[e][m], m <= L - |e|
@@ -203,11 +204,12 @@ __device__ __forceinline__ void hrr_ket(const R *in, const R (&CD)[3], R *out) {
   }
 }
 
-// Full contracted quartet: out[NA*NB*NC*ND] row-major (a, b, c, d).  The bra
-// and ket primitive pairs may come from different species.
+// Full contracted quartet: out[NA*NB*NC*ND] row-major (a, b, c, d).  pbra and
+// pket point at the first primitive pair of the bra and of the ket pair (they
+// may come from different species, and from global or shared memory).
 template <typename R, int LA, int LB, int LC, int LD>
-__device__ __forceinline__ void eri_quartet(const PairT<R> &bra, const PrimT<R> *__restrict__ pbra,
-                                            const PairT<R> &ket, const PrimT<R> *__restrict__ pket,
+__device__ __forceinline__ void eri_quartet(const PairT<R> &bra, const PrimT<R> *pbra, const PairT<R> &ket,
+                                            const PrimT<R> *pket,
                                             const double *boys64, const float *boys32,
                                             R (&out)[QClass<LA, LB, LC, LD>::NINT]) {
   using QC_ = QClass<LA, LB, LC, LD>;
@@ -215,9 +217,9 @@ __device__ __forceinline__ void eri_quartet(const PairT<R> &bra, const PrimT<R> 
 #pragma unroll
   for (int i = 0; i < QC_::nE * QC_::nF; ++i) X[i] = R(0);
   for (int ib = 0; ib < bra.nprim; ++ib) {
-    const PrimT<R> pb = pbra[bra.prim0 + ib];
+    const PrimT<R> pb = pbra[ib];
     for (int ik = 0; ik < ket.nprim; ++ik) {
-      const PrimT<R> pk = pket[ket.prim0 + ik];
+      const PrimT<R> pk = pket[ik];
       vrr_prim<R, LA, LB, LC, LD>(X, pb, pk, boys64, boys32);
     }
   }

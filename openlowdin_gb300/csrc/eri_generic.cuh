@@ -89,16 +89,17 @@ __device__ inline void boys_f64_rt(int L, double T, double *F, const double *__r
   if (T < kBoysTMax) {
     const int i = __double2int_rn(T * (1.0 / kBoysH));
     const double mdT = i * kBoysH - T;
-    const double *t = tab + i * kBoysOrders + L;
+    const double *t = tab + i * kBoysStride + L;
     double s = __ldg(t + kBoysTaylor - 1);
     for (int k = kBoysTaylor - 1; k >= 1; --k) s = fma(mdT * (1.0 / k), s, __ldg(t + k - 1));
     F[L] = s;
-    const double e = exp(-T);
+    const double e = __ldg(tab + i * kBoysStride + kBoysOrders) * exp_small(mdT);
     for (int m = L - 1; m >= 0; --m) F[m] = fma(2.0 * T, F[m + 1], e) / (2 * m + 1);
   } else {
     const double e = exp(-T);
-    F[0] = 0.88622692545275801365 / sqrt(T);
-    const double o2T = 0.5 / T;
+    const double r = rsqrt(T);
+    F[0] = 0.88622692545275801365 * r;
+    const double o2T = 0.5 * r * r;
     for (int m = 0; m < L; ++m) F[m + 1] = ((2 * m + 1) * F[m] - e) * o2T;
   }
 }

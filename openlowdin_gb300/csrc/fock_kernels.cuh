@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(128) schwarz_kernel(SchwarzParams P) {
   const PairRec pr = P.pairs[P.p0 + t];
   constexpr int N = ncart(LA) * ncart(LB);
   double I[N * N];
-  eri_quartet<double, LA, LB, LA, LB>(pr, P.prims, pr, P.prims, P.boys.f64, P.boys.f32, I);
+  eri_quartet<double, LA, LB, LA, LB>(pr, P.prims + pr.prim0, pr, P.prims + pr.prim0, P.boys.f64, P.boys.f32, I);
   double m = 0;
 #pragma unroll
   for (int i = 0; i < N; ++i) m = fmax(m, fabs(I[i * N + i]));
@@ -82,12 +82,6 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
   const int local = blockIdx.x - T.blk0;
   const int tx = local % T.nbx, ty = local / T.nbx;
   if (T.triangle && tx * 32 > ty * kWarpsPerBlock + kWarpsPerBlock - 1) return;
-  const int kpos = tx * 32 + threadIdx.x;
-  const int bpos = ty * kWarpsPerBlock + threadIdx.y;
-  if (bpos >= T.nbra) return;  // warp-uniform
-  bool active = kpos < T.nket && (!T.triangle || kpos <= bpos);
-  const int bi = T.bra0 + bpos;
-  const int ki = T.ket0 + min(kpos, T.nket - 1);
   const PairT<R> *pairs;
   const PrimT<R> *prims;
   const R *D;
@@ -96,17 +90,51 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
   } else {
     pairs = T.pairs32; prims = T.prims32; D = T.Ds32;
   }
+  // The block's 32 ket pairs (shared by its bra warps) and the first primitive
+  // pair of each, staged once in shared memory by coalesced 16-byte copies.
+  // Strides 80 / 112 B (pairs) and 48 / 80 B (primitives) keep the per-lane
+  // 16-byte reads free of bank conflicts.
+  struct alignas(16) SPair {
+    PairT<R> p;
+    int4 pad;
+  };
+  __shared__ SPair sk[32];
+  __shared__ PrimT<R> skp[32];
+  {
+    constexpr int WP = sizeof(PairT<R>) / 16, WQ = sizeof(PrimT<R>) / 16;
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    for (int w = tid; w < 32 * WP; w += 32 * kWarpsPerBlock) {
+      const int r = w / WP, k = w % WP;
+      const int kr = T.ket0 + min(tx * 32 + r, T.nket - 1);
+      reinterpret_cast<int4 *>(&sk[r].p)[k] = __ldg(reinterpret_cast<const int4 *>(pairs + kr) + k);
+    }
+    __syncthreads();
+    for (int w = tid; w < 32 * WQ; w += 32 * kWarpsPerBlock) {
+      const int r = w / WQ, k = w % WQ;
+      reinterpret_cast<int4 *>(skp + r)[k] = __ldg(reinterpret_cast<const int4 *>(prims + sk[r].p.prim0) + k);
+    }
+    __syncthreads();
+  }
+  const int kpos = tx * 32 + threadIdx.x;
+  const int bpos = ty * kWarpsPerBlock + threadIdx.y;
+  if (bpos >= T.nbra) return;  // warp-uniform
+  bool active = kpos < T.nket && (!T.triangle || kpos <= bpos);
+  const int bi = T.bra0 + bpos;
+  const int ki = T.ket0 + min(kpos, T.nket - 1);
   const PairT<R> &bra = pairs[bi];
-  const PairT<R> ket = pairs[ki];
+  const PairT<R> &ket = sk[threadIdx.x].p;
   if (TL.split > 0.0) {
-    float b = T.pairs32[bi].Q * T.pairs32[ki].Q;
+    // FP32 bound from the FP32 Schwarz factors (the FP64 records hold the
+    // same values before rounding), identical in both launches
+    float b = T.pairs32[bi].Q * (float)ket.Q;
     if (T.screen) {
       b *= dnorm6(T.Dn32, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
-      if (b < (float)TL.eps) active = false;
+      if (b < fmaxf((float)TL.eps, TL.skip)) active = false;
     }
     if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) active = false;
   } else if (T.screen) {
-    const double b = T.pairs[bi].Q * T.pairs[ki].Q * dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
+    const double b = T.pairs[bi].Q * (F64 ? (double)ket.Q : T.pairs[ki].Q) *
+                     dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
     if (b < TL.eps) active = false;
   }
   if (__all_sync(0xffffffffu, !active)) return;
@@ -116,7 +144,8 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
   }
   R I[Q::NINT];
   if (active) {
-    eri_quartet<R, LA, LB, LC, LD>(bra, prims, ket, prims, TL.boys.f64, TL.boys.f32, I);
+    const PrimT<R> *kp = ket.nprim == 1 ? skp + threadIdx.x : prims + ket.prim0;
+    eri_quartet<R, LA, LB, LC, LD>(bra, prims + bra.prim0, ket, kp, TL.boys.f64, TL.boys.f32, I);
   } else {
 #pragma unroll
     for (int x = 0; x < Q::NINT; ++x) I[x] = R(0);
@@ -243,6 +272,7 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
     if (T.DnB32) dm = fmaxf(dm, __ldg(T.DnB32 + k32.sa * T.nshB + k32.sb));
     const float b = b32.Q * k32.Q * dm;
     if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) active = false;
+    if ((T.DnA32 || T.DnB32) && b < TL.skip) active = false;
   }
   if (__all_sync(0xffffffffu, !active)) return;
   if (T.count) {
@@ -261,7 +291,7 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
   const PairT<R> ket = pb[T.ket0 + min(kpos, T.nket - 1)];
   R I[Q::NINT];
   if (active) {
-    eri_quartet<R, LA, LB, LC, LD>(bra, pra, ket, prb, TL.boys.f64, TL.boys.f32, I);
+    eri_quartet<R, LA, LB, LC, LD>(bra, pra + bra.prim0, ket, prb + ket.prim0, TL.boys.f64, TL.boys.f32, I);
   } else {
 #pragma unroll
     for (int x = 0; x < Q::NINT; ++x) I[x] = R(0);
@@ -351,7 +381,7 @@ __global__ void __launch_bounds__(128) it_kernel(ITParams P) {
     if (b < P.eps) return;
   }
   double I[Q::NINT];
-  eri_quartet<double, LA, LB, LC, LD>(bra, P.pra, ket, P.prb, P.boys.f64, P.boys.f32, I);
+  eri_quartet<double, LA, LB, LC, LD>(bra, P.pra + bra.prim0, ket, P.prb + ket.prim0, P.boys.f64, P.boys.f32, I);
 #pragma unroll
   for (int x = 0; x < Q::NINT; ++x)
     if (!(fabs(I[x]) > P.cut)) I[x] = 0.0;
@@ -394,7 +424,8 @@ __global__ void __launch_bounds__(128) mp2x_kernel(MXParams P) {
   if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) return;
   if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) return;
   double I[Q::NINT];
-  eri_quartet<double, LA, LB, LC, LD>(bra, P.prims, ket, P.kprims, P.boys.f64, P.boys.f32, I);
+  eri_quartet<double, LA, LB, LC, LD>(bra, P.prims + bra.prim0, ket, P.kprims + ket.prim0, P.boys.f64, P.boys.f32,
+                                      I);
   const int col0 = __ldg(P.colbase + ki) - P.col_first;
   const bool two = bra.sa != bra.sb;
   const size_t n = P.n, ncol = P.ncol;

@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(128) jk_coop_kernel(const JKTask *__restrict__
         float b = T.pairs32[bi].Q * T.pairs32[ki].Q;
         if (T.screen) {
           b *= dnorm6(T.Dn32, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
-          if (b < (float)TL.eps) active = false;
+          if (b < fmaxf((float)TL.eps, TL.skip)) active = false;
         }
         if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) active = false;
       } else if (T.screen) {
@@ -176,6 +176,7 @@ __global__ void __launch_bounds__(128) cp_coop_kernel(const CPTask *__restrict__
         if (T.DnB32) dm = fmaxf(dm, __ldg(T.DnB32 + k32.sa * T.nshB + k32.sb));
         const float b = b32.Q * k32.Q * dm;
         if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) continue;
+        if ((T.DnA32 || T.DnB32) && b < TL.skip) continue;
       }
       if (T.count && lane == 0) atomicAdd(T.count, 1ull);
       const PairRec &bra = T.pa[bi];

@@ -89,6 +89,7 @@ struct TaskLaunch {
   double split;           // mixed precision: quartets with bound >= split run in FP64
   int lower;              // 1: this launch takes the quartets below split
   double cut;             // coupling: |raw| < cut is dropped
+  float skip;             // mixed launches: quartets whose density-weighted bound is below skip are dropped
   BoysTables boys;
 };
 

@@ -55,9 +55,11 @@ void set_error(const char *fmt, ...) {
 struct BoysHost {
   std::vector<double> f64;
   std::vector<float> f32;
-  BoysHost() : f64((size_t)kBoysPoints * kBoysOrders), f32((size_t)kBoysPoints * kBoysOrders) {
+  BoysHost() : f64((size_t)kBoysPoints * kBoysStride), f32((size_t)kBoysPoints * kBoysStride) {
     for (int i = 0; i < kBoysPoints; ++i) {
       const long double T = (long double)i * (long double)kBoysH;
+      f64[(size_t)i * kBoysStride + kBoysOrders] = (double)expl(-T);
+      f32[(size_t)i * kBoysStride + kBoysOrders] = (float)expl(-T);
       for (int n = 0; n < kBoysOrders; ++n) {
         long double term = 1.0L / (2 * n + 1), sum = term;
         for (int k = 1; k < 2000; ++k) {
@@ -66,8 +68,8 @@ struct BoysHost {
           if (term < 1e-24L * sum) break;
         }
         const double v = (double)(expl(-T) * sum);
-        f64[(size_t)i * kBoysOrders + n] = v;
-        f32[(size_t)i * kBoysOrders + n] = (float)v;
+        f64[(size_t)i * kBoysStride + n] = v;
+        f32[(size_t)i * kBoysStride + n] = (float)v;
       }
     }
   }
@@ -76,7 +78,7 @@ struct BoysHost {
     if (T < kBoysTMax) {
       const int i = (int)std::lround(T / kBoysH);
       const double mdT = i * kBoysH - T;
-      const double *t = &f64[(size_t)i * kBoysOrders + mmax];
+      const double *t = &f64[(size_t)i * kBoysStride + mmax];
       double s = t[kBoysTaylor - 1];
       for (int k = kBoysTaylor - 1; k >= 1; --k) s = std::fma(mdT / k, s, t[k - 1]);
       F[mmax] = s;
@@ -369,19 +371,22 @@ struct TaskSet {
     for (auto &g : group) g.clear();
   }
   void add(int cb, int ck, const T &t) { group[cb * kNumPairClasses + ck].push_back(t); }
-  // assigns blk0 / nbx and copies all groups to the device, ordered on stream s
-  bool upload(cudaStream_t s) {
+  // assigns blk0 / nbx and copies all groups to the device, ordered on stream s;
+  // with `on`, a task whose flag (t.active - flag_base) is off in `on` is left
+  // out, so the launches of switched-off systems carry no blocks at all
+  bool upload(cudaStream_t s, const int *flag_base = nullptr, const std::vector<int> *on = nullptr) {
     std::vector<T> flat;
     for (int c = 0; c < kNQC; ++c) {
       off[c] = (int)flat.size();
-      cnt[c] = (int)group[c].size();
       int b = 0;
       for (T t : group[c]) {
+        if (on && t.active && !(*on)[t.active - flag_base]) continue;
         t.nbx = task_nbx(t.nket);
         t.blk0 = b;
         b += t.nbx * task_nby(t.nbra);
         flat.push_back(t);
       }
+      cnt[c] = (int)flat.size() - off[c];
       nblk[c] = b;
     }
     if (flat.empty()) return true;
@@ -712,7 +717,7 @@ struct LibintInterface {
   }
 
   static bool launch_jk_groups(const TaskSet<JKTask> &ts, int precision, double split, BoysTables boys,
-                               cudaStream_t s) {
+                               cudaStream_t s, double skip = 0.0) {
     for (int c = 0; c < kNQC; ++c) {
       if (!ts.cnt[c]) continue;
       TaskLaunch tl{};
@@ -720,6 +725,7 @@ struct LibintInterface {
       tl.nblocks = ts.nblk[c];
       tl.eps = DBL_EPSILON;
       tl.cut = 1e-10;
+      tl.skip = (float)skip;
       tl.boys = boys;
       const int cb = c / kNumPairClasses, ck = c % kNumPairClasses;
       if (precision == 0) {
@@ -787,7 +793,8 @@ bool add_cp_tasks(TaskSet<CPTask> &ts, LibintInterface *A, LibintInterface *B, c
 }
 
 // mode 0: FP64, 1: FP32 throughout, 2: split at `split` (FP64 above, FP32 below)
-bool launch_cp_groups(const TaskSet<CPTask> &ts, int mode, double split, BoysTables boys, cudaStream_t s) {
+bool launch_cp_groups(const TaskSet<CPTask> &ts, int mode, double split, BoysTables boys, cudaStream_t s,
+                      double skip = 0.0) {
   for (int c = 0; c < kNQC; ++c) {
     if (!ts.cnt[c]) continue;
     TaskLaunch tl{};
@@ -795,6 +802,7 @@ bool launch_cp_groups(const TaskSet<CPTask> &ts, int mode, double split, BoysTab
     tl.nblocks = ts.nblk[c];
     tl.eps = DBL_EPSILON;
     tl.cut = 1e-10;
+    tl.skip = (float)skip;
     tl.boys = boys;
     const int cb = c / kNumPairClasses, ck = c % kNumPairClasses;
     if (mode == 2) {
@@ -1247,9 +1255,12 @@ struct LowdinGB300_Batch {
   // one-time kernel set-up that must not happen inside a capture.
   struct Graph {
     cudaGraphExec_t exec = nullptr;
-    double split = 0.0;
+    double split = 0.0, skip = 0.0;
     long long launches = 0;
   };
+  double skip = 0.0;   // mixed builds: density-weighted bound below which quartets are dropped
+  std::vector<int> on; // host copy of the per-system flags
+  bool tasks_dirty = false;
   Graph graphs[4];
   cudaStream_t capture = nullptr;
   bool use_graph = true;
@@ -1361,6 +1372,8 @@ struct LowdinGB300_Batch {
           return false;
         mark(cp, before, sp[a].sys);
       }
+    on.assign(std::max(1, nsys), 1);
+    tasks_dirty = false;
     nslots = (int)hs.size();
     if (!slots.ensure(hs.size())) return false;
     CK(cudaMemcpyAsync(slots.p, hs.data(), hs.size() * sizeof(SpeciesSlot), cudaMemcpyHostToDevice, s));
@@ -1375,9 +1388,15 @@ struct LowdinGB300_Batch {
       set_error("batch_fock: batch not finalised");
       return false;
     }
+    if (tasks_dirty) {
+      // systems were switched off or on: launch only the active systems' tasks
+      if (!jk.upload(s, active.p, &on) || !cp.upload(s, active.p, &on)) return false;
+      drop_graphs();
+      tasks_dirty = false;
+    }
     if (!use_graph || calls++ == 0) return fock_sequence(precision, split, s);
     Graph &g = graphs[precision & 3];
-    if (!g.exec || g.split != split) {
+    if (!g.exec || g.split != split || g.skip != skip) {
       if (g.exec) cudaGraphExecDestroy(g.exec);
       g = Graph{};
       if (!capture) CK(cudaStreamCreateWithFlags(&capture, cudaStreamNonBlocking));
@@ -1401,6 +1420,7 @@ struct LowdinGB300_Batch {
         return false;
       }
       g.split = split;
+      g.skip = skip;
       g.launches = captured;
     }
     CK(cudaGraphLaunch(g.exec, s));
@@ -1415,8 +1435,8 @@ struct LowdinGB300_Batch {
     CK(cudaMemsetAsync(cnt.p, 0, 2 * kNQC * sizeof(unsigned long long), s));
     CK(launch_prepare_batch(slots.p, nslots, total, s));
     const int jk_mixed = precision & 1;
-    if (!LibintInterface::launch_jk_groups(jk, jk_mixed, jk_mixed ? split : 0.0, boys, s)) return false;
-    if (!launch_cp_groups(cp, (precision & 2) ? 2 : 0, split, boys, s)) return false;
+    if (!LibintInterface::launch_jk_groups(jk, jk_mixed, jk_mixed ? split : 0.0, boys, s, skip)) return false;
+    if (!launch_cp_groups(cp, (precision & 2) ? 2 : 0, split, boys, s, skip)) return false;
     CK(launch_finalize_batch(slots.p, nslots, total, s));
     return true;
   }
@@ -1434,6 +1454,12 @@ int LowdinGB300_batch_add_system(LowdinGB300_Batch *b, LibintInterface **species
   return LowdinGB300_batch_add_system_ld(b, species, nspecies, charges, factors, two_body, dP, dG, dJ, nullptr);
 }
 
+int LowdinGB300_batch_set_skip(LowdinGB300_Batch *b, double skip) {
+  if (!b || !(skip >= 0.0)) return -1;
+  b->skip = skip;
+  return 0;
+}
+
 int LowdinGB300_batch_set_active(LowdinGB300_Batch *b, const int *flags, void *stream) {
   if (!b || !b->finalized || !flags) return -1;
   const size_t nsys = b->sys_first.size();
@@ -1441,6 +1467,11 @@ int LowdinGB300_batch_set_active(LowdinGB300_Batch *b, const int *flags, void *s
       cudaSuccess) {
     set_error("batch_set_active: copy failed");
     return -1;
+  }
+  for (size_t i = 0; i < nsys; ++i) {
+    const int f = flags[i] != 0;
+    if (b->on[i] != f) b->tasks_dirty = true;
+    b->on[i] = f;
   }
   return 0;
 }

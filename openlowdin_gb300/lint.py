@@ -101,6 +101,8 @@ def lib():
         L.LowdinGB300_batch_add_system_ld.argtypes = L.LowdinGB300_batch_add_system.argtypes + [
             np.ctypeslib.ndpointer(dtype=np.int32)]
         L.LowdinGB300_batch_add_system_ld.restype = ctypes.c_int
+        L.LowdinGB300_batch_set_skip.argtypes = [_vp, ctypes.c_double]
+        L.LowdinGB300_batch_set_skip.restype = ctypes.c_int
         L.LowdinGB300_batch_set_active.argtypes = [_vp, np.ctypeslib.ndpointer(dtype=np.int32), _vp]
         L.LowdinGB300_batch_set_active.restype = ctypes.c_int
         L.LowdinGB300_batch_finalize.argtypes = [_vp, _vp]
@@ -133,7 +135,7 @@ EXPORTED_SYMBOLS = [
     "LowdinGB300_last_quartets", "LowdinGB300_version", "LowdinGB300_last_class_quartets",
     "LowdinGB300_pair_class_counts", "LowdinGB300_measure_fma_tflops", "LowdinGB300_launch_count",
     "LowdinGB300_batch_new", "LowdinGB300_batch_del", "LowdinGB300_batch_add_system",
-    "LowdinGB300_batch_add_system_ld", "LowdinGB300_batch_set_active",
+    "LowdinGB300_batch_add_system_ld", "LowdinGB300_batch_set_active", "LowdinGB300_batch_set_skip",
     "LowdinGB300_batch_finalize", "LowdinGB300_batch_fock", "LowdinGB300_batch_use_graph",
     "LowdinGB300_batch_quartets",
     "LowdinGB300_batch_coupling_quartets", "LowdinGB300_noalloc_scratch_bytes",
@@ -174,6 +176,11 @@ class Batch:
             raise LowdinGB300Error("batch add_system failed")
         self.nsys = getattr(self, "nsys", 0) + 1
         return k
+
+    def set_skip(self, skip: float):
+        """Mixed builds drop quartets whose density-weighted bound is below skip."""
+        if lib().LowdinGB300_batch_set_skip(self.h, float(skip)) != 0:
+            raise LowdinGB300Error(f"batch set_skip({skip}) failed")
 
     def set_active(self, flags, stream: int = 0):
         """flags[s] != 0: system s (in add order) is built by the next fock calls."""

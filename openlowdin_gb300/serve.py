@@ -29,6 +29,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import lint
+from .batch_scf import MIXED_SKIP
 from .scf import _one_body_device, _orthogonaliser, n_occ, nuclear_repulsion
 from .systems import n_core
 
@@ -119,12 +120,13 @@ def footprint_bytes(sysd, kind: str, diis_size: int = 10, mp2_budget_gb: float =
 class ServingEngine:
     def __init__(self, device="cuda", precision="fp64", split=1e-5, hbm_budget_gb=150.0, max_active=256,
                  diis_size=10, tol_energy=1e-8, tol_density=1e-6, max_iter=100, mp2_precision=None,
-                 mp2_budget_gb=8.0):
+                 mp2_budget_gb=8.0, skip=None):
         import torch
         self.torch = torch
         self.dev = torch.device(device)
         self.precision = precision
         self.split = split
+        self.skip = (MIXED_SKIP if skip is None else skip) if precision == "mixed" else 0.0
         self.budget = hbm_budget_gb * 1e9
         self.max_active = max_active
         self.diis_size = diis_size
@@ -232,6 +234,7 @@ class ServingEngine:
                          [1 if sp["n_particles"] > 1 else 0 for sp in sps],
                          [s.Pin for s in job.sp], [s.Gb for s in job.sp], [s.Jb for s in job.sp])
         b.finalize(self.stream.cuda_stream)
+        b.set_skip(self.skip)
         return b
 
     # --------------------------------------------------------- SCF step --
