@@ -101,6 +101,13 @@ constexpr int kBoysTaylor = 9;            // terms k = 0..8 (|dT| <= 0.05: error
 constexpr int kBoysTaylorF32 = 6;
 constexpr int kBoysOrders = kMaxLQuartet + kBoysTaylor + 1;
 constexpr int kBoysStride = kBoysOrders + 1;  // row i: F_0..F_{kBoysOrders-1}(T_i), then e^{-T_i}
+// After that table, one table per order L = 0..kMaxLQuartet of the Taylor
+// coefficients of F_L about T_i, c_k = F_{L+k}(T_i) / k! (k < kBoysTaylor),
+// followed by e^{-T_i}: rows of kBoysSRow doubles, so the series is a plain
+// Horner chain of FMAs in (T_i - T).
+constexpr int kBoysSRow = kBoysTaylor + 1;
+constexpr int kBoysScaledOff = kBoysPoints * kBoysStride;
+constexpr int kBoysF64Size = kBoysScaledOff + (kMaxLQuartet + 1) * kBoysPoints * kBoysSRow;
 
 // e^x for |x| <= h/2 = 0.05: Taylor polynomial of degree 9 (remainder below
 // 0.05^10 / 10! = 2.7e-20 relative), so e^{-T} = e^{-T_i} e^{T_i - T} costs
@@ -126,13 +133,13 @@ __device__ __forceinline__ void boys_f64(double T, double (&F)[L + 1], const dou
   if (T < kBoysTMax) {
     const int i = __double2int_rn(T * (1.0 / kBoysH));
     const double mdT = i * kBoysH - T;  // -(T - T_i)
-    const double *t = tab + i * kBoysStride + L;
+    const double *t = tab + kBoysScaledOff + (L * kBoysPoints + i) * kBoysSRow;
     double s = __ldg(t + kBoysTaylor - 1);
 #pragma unroll
-    for (int k = kBoysTaylor - 1; k >= 1; --k) s = fma(mdT * (1.0 / k), s, __ldg(t + k - 1));
+    for (int k = kBoysTaylor - 1; k >= 1; --k) s = fma(s, mdT, __ldg(t + k - 1));
     F[L] = s;
     if constexpr (L > 0) {
-      const double e = __ldg(tab + i * kBoysStride + kBoysOrders) * exp_small(mdT);
+      const double e = __ldg(t + kBoysTaylor) * exp_small(mdT);
       const double twoT = 2.0 * T;
 #pragma unroll
       for (int m = L - 1; m >= 0; --m) F[m] = fma(twoT, F[m + 1], e) * (1.0 / (2 * m + 1));

@@ -89,11 +89,11 @@ __device__ inline void boys_f64_rt(int L, double T, double *F, const double *__r
   if (T < kBoysTMax) {
     const int i = __double2int_rn(T * (1.0 / kBoysH));
     const double mdT = i * kBoysH - T;
-    const double *t = tab + i * kBoysStride + L;
+    const double *t = tab + kBoysScaledOff + (L * kBoysPoints + i) * kBoysSRow;
     double s = __ldg(t + kBoysTaylor - 1);
-    for (int k = kBoysTaylor - 1; k >= 1; --k) s = fma(mdT * (1.0 / k), s, __ldg(t + k - 1));
+    for (int k = kBoysTaylor - 1; k >= 1; --k) s = fma(s, mdT, __ldg(t + k - 1));
     F[L] = s;
-    const double e = __ldg(tab + i * kBoysStride + kBoysOrders) * exp_small(mdT);
+    const double e = __ldg(t + kBoysTaylor) * exp_small(mdT);
     for (int m = L - 1; m >= 0; --m) F[m] = fma(2.0 * T, F[m + 1], e) / (2 * m + 1);
   } else {
     const double e = exp(-T);

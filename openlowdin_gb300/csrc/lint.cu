@@ -55,7 +55,7 @@ void set_error(const char *fmt, ...) {
 struct BoysHost {
   std::vector<double> f64;
   std::vector<float> f32;
-  BoysHost() : f64((size_t)kBoysPoints * kBoysStride), f32((size_t)kBoysPoints * kBoysStride) {
+  BoysHost() : f64((size_t)kBoysF64Size), f32((size_t)kBoysPoints * kBoysStride) {
     for (int i = 0; i < kBoysPoints; ++i) {
       const long double T = (long double)i * (long double)kBoysH;
       f64[(size_t)i * kBoysStride + kBoysOrders] = (double)expl(-T);
@@ -72,6 +72,17 @@ struct BoysHost {
         f32[(size_t)i * kBoysStride + n] = (float)v;
       }
     }
+    // per-order Taylor coefficients F_{L+k}(T_i) / k! and e^{-T_i}
+    for (int L = 0; L <= kMaxLQuartet; ++L)
+      for (int i = 0; i < kBoysPoints; ++i) {
+        double *row = &f64[kBoysScaledOff + ((size_t)L * kBoysPoints + i) * kBoysSRow];
+        double fact = 1.0;
+        for (int k = 0; k < kBoysTaylor; ++k) {
+          if (k > 0) fact *= k;
+          row[k] = f64[(size_t)i * kBoysStride + L + k] / fact;
+        }
+        row[kBoysTaylor] = f64[(size_t)i * kBoysStride + kBoysOrders];
+      }
   }
   // F_m(T), m = 0..mmax (host; Taylor + downward recursion like the device)
   void eval(int mmax, double T, double *F) const {
