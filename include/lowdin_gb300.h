@@ -263,6 +263,21 @@ int LowdinGB300_mp2_coupling(LibintInterface *a, LibintInterface *b, const doubl
                              void *stream);
 /* ket-component columns of the last LowdinGB300_mp2_direct / _mp2_coupling call */
 long long LowdinGB300_mp2_last_columns(void);
+/* LowdinGB300_mp2_direct in FP64 that also writes the transformed integrals
+   to `path` in the reference's moint.dat layout (replaces the DIRECT branch of
+   TransformIntegralsC_atomicToMolecularOfOneSpecie, TransformIntegralsC.f90:472-665,
+   with partialTransform = "MP2", :1489-1501): every (ia|jb) with i <= j
+   (b >= a when i == j), |value| > 1e-10, as Fortran sequential unformatted
+   records of `stack_size` (the reference's INTEGRAL_STACK_SIZE, 30000) int32
+   p, q, r, s (1-based orbital numbers) and FP64 values, the last record ending
+   with p = -1 (ReadTransformedIntegrals.f90:225-233 reads it).  *n_written =
+   integrals written.  Returns 0, or -1 with the error set. */
+int LowdinGB300_mp2_moint(LibintInterface *lint, const double *dD, const double *dC, const double *eps, int n_occ,
+                          int n_frozen, const char *path, int stack_size, double x_budget_gb, double *e2,
+                          long long *n_written, void *stream);
+/* The record writer alone (host only): `count` entries in the given order. */
+int LowdinGB300_moint_write(const char *path, int stack_size, const int *p, const int *q, const int *r,
+                            const int *s, const double *v, long long count);
 
 /* Split-BF16 GEMM on the tensor cores (no counterpart in the reference; the
    engine of the mixed-precision MP2 transform): C (M x N) = A (M x K) B^T with

@@ -1794,6 +1794,62 @@ bool mp2_batch_ints(const PairList &PA, const PairList &PB, MXParams q, int k0, 
   return true;
 }
 
+// Writer of the reference's transformed-integral file `<species>moint.dat`
+// (TransformIntegralsC.f90:531-654, read by ReadTransformedIntegrals.f90:225-233):
+// a Fortran sequential unformatted file whose records each hold four int32
+// index arrays p, q, r, s and one FP64 value array, all of the stack size
+// (30000 by default), framed by the record length in bytes (int32) before and
+// after, as gfortran writes them.  Entries fill a stack in the order they
+// come; a full stack is written as one record and cleared; the last record
+// marks the end with p = -1 after its last entry (zeros beyond).
+struct MointWriter {
+  FILE *f = nullptr;
+  int stack = 0, m = 0;
+  long long written = 0;
+  std::vector<int32_t> pp, qq, rr, ss;
+  std::vector<double> val;
+  bool open(const char *path, int stack_size) {
+    stack = stack_size;
+    pp.assign(stack, 0); qq.assign(stack, 0); rr.assign(stack, 0); ss.assign(stack, 0);
+    val.assign(stack, 0.0);
+    f = std::fopen(path, "wb");
+    if (!f) {
+      set_error("moint: cannot open %s for writing", path);
+      return false;
+    }
+    return true;
+  }
+  bool record() {
+    const int32_t len = (int32_t)((size_t)stack * (4 * sizeof(int32_t) + sizeof(double)));
+    bool ok = std::fwrite(&len, 4, 1, f) == 1;
+    for (auto *a : {&pp, &qq, &rr, &ss}) ok = ok && std::fwrite(a->data(), 4, stack, f) == (size_t)stack;
+    ok = ok && std::fwrite(val.data(), 8, stack, f) == (size_t)stack && std::fwrite(&len, 4, 1, f) == 1;
+    if (!ok) set_error("moint: write failed");
+    for (auto *a : {&pp, &qq, &rr, &ss}) std::fill(a->begin(), a->end(), 0);
+    std::fill(val.begin(), val.end(), 0.0);
+    return ok;
+  }
+  bool put(int p, int q, int r, int s_, double v) {
+    pp[m] = p; qq[m] = q; rr[m] = r; ss[m] = s_; val[m] = v;
+    ++written;
+    if (++m == stack) {
+      m = 0;
+      return record();
+    }
+    return true;
+  }
+  bool finish() {
+    pp[m] = -1;
+    const bool ok = record();
+    std::fclose(f);
+    f = nullptr;
+    return ok;
+  }
+  ~MointWriter() {
+    if (f) std::fclose(f);
+  }
+};
+
 // One MP2 term: intra-species (A == B, closed shell: (ia|jb)[2(ia|jb) -
 // (ib|ja)]/D) or inter-species (A != B: factor (ia|jb)^2 / D, factor = (q_A
 // q_B)^2 lambda_A lambda_B).  The bra index pairs (mu nu) belong to A, the ket
@@ -1806,7 +1862,27 @@ struct MP2Setup {
   int nA, nB, oA, vA, oB, vB, noccA, nfA, noccB, nfB;
   const double *dCA, *dCB, *epsA, *epsB;
   MXParams q;      // common integral parameters
+  MointWriter *moint = nullptr;   // FP64 intra-species path: also write every (ia|jb) to the file
 };
+
+// (ia|jb) of occupied i (M[j][b][a], device) into the file in the reference's
+// loop order: a, then j >= i, then b (b >= a when j == i), |v| > 1e-10
+// (TransformIntegralsC.f90:570-640 with the MP2 bounds of :1489-1501)
+bool moint_block(const MP2Setup &S, int i, const double *dM, std::vector<double> &h, cudaStream_t s) {
+  const int oB = S.oB, vB = S.vB, vA = S.vA;
+  h.resize((size_t)oB * vB * vA);
+  CK(cudaMemcpyAsync(h.data(), dM, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  const int p = S.nfA + i + 1;
+  for (int a = 0; a < vA; ++a)
+    for (int j = i; j < oB; ++j)
+      for (int b = (j == i ? a : 0); b < vB; ++b) {
+        const double v = h[((size_t)j * vB + b) * vA + a];
+        if (std::fabs(v) > 1e-10 && !S.moint->put(p, S.noccA + a + 1, S.nfB + j + 1, S.noccB + b + 1, v))
+          return false;
+      }
+  return true;
+}
 
 bool mp2_need(size_t bytes) {
   size_t freeb = 0, totb = 0;
@@ -1865,6 +1941,7 @@ bool mp2_fp64(MP2Setup &S, size_t budget, double *e2out, cudaStream_t s) {
   MXParams q = S.q;
   q.colbase = dcolbase.p;
   q.X = X.p;
+  std::vector<double> hM;
   const int nbatch = (int)mc.bfirst.size() - 1;
   for (int bt = 0; bt < nbatch; ++bt) {
     const int k0 = mc.bfirst[bt], k1 = mc.bfirst[bt + 1];
@@ -1895,6 +1972,7 @@ bool mp2_fp64(MP2Setup &S, size_t budget, double *e2out, cudaStream_t s) {
       CK(launch_mp2_energy_coupling<double>(M.p, oB, vB, vA, ei, EoB.p, EvA.p, EvB.p, 1e-10, S.factor, e2.p, s));
     else
       CK(launch_mp2_energy<double>(M.p, oB, vB, ei, EoB.p, EvB.p, 1e-10, e2.p, s));
+    if (S.moint && !moint_block(S, i, M.p, hM, s)) return false;
   }
   double e = 0;
   CK(cudaMemcpyAsync(&e, e2.p, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -2068,7 +2146,7 @@ bool mp2_run(MP2Setup &S, int precision, size_t budget, double *e2out, cudaStrea
 }
 
 bool mp2_direct(LibintInterface *L, const double *dD, const double *dC, const double *eps, int n_occ, int n_frozen,
-                int precision, size_t x_budget_bytes, double *e2out, cudaStream_t s) {
+                int precision, size_t x_budget_bytes, double *e2out, cudaStream_t s, MointWriter *moint = nullptr) {
   if (!L->is_electron) {
     set_error("mp2_direct: closed-shell MP2 is defined here for an electron species");
     return false;
@@ -2104,6 +2182,7 @@ bool mp2_direct(LibintInterface *L, const double *dD, const double *dC, const do
   q.cut = 1e-10;
   q.n = n;
   q.boys = L->boys;
+  S.moint = moint;
   return mp2_run(S, precision, x_budget_bytes, e2out, s);
 }
 
@@ -2188,6 +2267,36 @@ int LowdinGB300_mp2_coupling(LibintInterface *a, LibintInterface *b, const doubl
 }
 
 long long LowdinGB300_mp2_last_columns(void) { return g_mp2_last.ncols; }
+
+int LowdinGB300_mp2_moint(LibintInterface *lint, const double *dD, const double *dC, const double *eps, int n_occ,
+                          int n_frozen, const char *path, int stack_size, double x_budget_gb, double *e2,
+                          long long *n_written, void *stream) {
+  if (!check_handle(lint, __func__)) return -1;
+  if (!dD || !dC || !eps || !e2 || !path || stack_size < 1) {
+    set_error("%s: invalid argument", __func__);
+    return -1;
+  }
+  MointWriter w;
+  if (!w.open(path, stack_size)) return -1;
+  const size_t budget = x_budget_gb > 0 ? (size_t)(x_budget_gb * 1e9) : (size_t)8e9;
+  if (!mp2_direct(lint, dD, dC, eps, n_occ, n_frozen, 0, budget, e2, (cudaStream_t)stream, &w)) return -1;
+  if (!w.finish()) return -1;
+  if (n_written) *n_written = w.written;
+  return 0;
+}
+
+int LowdinGB300_moint_write(const char *path, int stack_size, const int *p, const int *q, const int *r,
+                            const int *s, const double *v, long long count) {
+  if (!path || stack_size < 1 || count < 0 || (count > 0 && (!p || !q || !r || !s || !v))) {
+    set_error("%s: invalid argument", __func__);
+    return -1;
+  }
+  MointWriter w;
+  if (!w.open(path, stack_size)) return -1;
+  for (long long k = 0; k < count; ++k)
+    if (!w.put(p[k], q[k], r[k], s[k], v[k])) return -1;
+  return w.finish() ? 0 : -1;
+}
 
 }  // extern "C"
 

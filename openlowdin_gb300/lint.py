@@ -80,6 +80,14 @@ def lib():
                                              ctypes.c_double, ctypes.POINTER(ctypes.c_double), _vp]
         L.LowdinGB300_mp2_direct.restype = ctypes.c_int
         L.LowdinGB300_mp2_last_columns.restype = ctypes.c_longlong
+        L.LowdinGB300_mp2_moint.argtypes = [_vp, _vp, _vp, _f64p, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
+                                            ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
+                                            ctypes.POINTER(ctypes.c_longlong), _vp]
+        L.LowdinGB300_mp2_moint.restype = ctypes.c_int
+        _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+        L.LowdinGB300_moint_write.argtypes = [ctypes.c_char_p, ctypes.c_int, _i32p, _i32p, _i32p, _i32p, _f64p,
+                                              ctypes.c_longlong]
+        L.LowdinGB300_moint_write.restype = ctypes.c_int
         L.LowdinGB300_mp2_coupling.argtypes = [_vp, _vp, _vp, _vp, _f64p, _f64p, ctypes.c_int, ctypes.c_int,
                                                ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                                ctypes.c_double, ctypes.POINTER(ctypes.c_double), _vp]
@@ -141,8 +149,18 @@ EXPORTED_SYMBOLS = [
     "LowdinGB300_batch_coupling_quartets", "LowdinGB300_noalloc_scratch_bytes",
     "LowdinGB300_twobody_device_noalloc", "LowdinGB300_mp2_direct", "LowdinGB300_mp2_last_columns", "LowdinGB300_mp2_coupling",
     "LowdinGB300_gemm_bf16_split", "LowdinGB300_gemm_bf16_precise",
-    "LowdinGB300_gemm_bench",
+    "LowdinGB300_gemm_bench", "LowdinGB300_mp2_moint", "LowdinGB300_moint_write",
 ]
+
+
+def moint_write(path: str, p, q, r, s, v, stack_size: int = 30000):
+    """Entries (1-based orbital numbers p, q, r, s and values v, in order) to a
+    moint.dat-layout file (LowdinGB300_moint_write; host only)."""
+    a = [np.ascontiguousarray(x, np.int32) for x in (p, q, r, s)]
+    vv = np.ascontiguousarray(v, np.float64)
+    if lib().LowdinGB300_moint_write(os.fsencode(path), int(stack_size), *a, vv, len(vv)) != 0:
+        _check()
+        raise LowdinGB300Error("moint_write failed")
 
 
 class Batch:
@@ -376,6 +394,20 @@ class Libint2Interface:
             _check()
             raise LowdinGB300Error("mp2_direct failed")
         return e2.value
+
+    def mp2_moint(self, d_ptr: int, c_ptr: int, eps, n_occ: int, n_frozen: int, path: str,
+                  stack_size: int = 30000, x_budget_gb: float = 0.0, stream: int = 0):
+        """FP64 E_MP2 as mp2_direct, also writing every (ia|jb) to `path` in the
+        reference's moint.dat layout; returns (E_MP2, integrals written)."""
+        e2 = ctypes.c_double(0.0)
+        nw = ctypes.c_longlong(0)
+        rc = lib().LowdinGB300_mp2_moint(self.h, d_ptr, c_ptr, np.ascontiguousarray(eps, np.float64), int(n_occ),
+                                         int(n_frozen), os.fsencode(path), int(stack_size), float(x_budget_gb),
+                                         ctypes.byref(e2), ctypes.byref(nw), stream)
+        if rc != 0:
+            _check()
+            raise LowdinGB300Error("mp2_moint failed")
+        return e2.value, nw.value
 
     def mp2_coupling(self, other: "Libint2Interface", ca_ptr: int, cb_ptr: int, eps_a, eps_b, n_occ_a: int,
                      n_frozen_a: int, n_occ_b: int, n_frozen_b: int, factor: float, precision: int = 0,

@@ -163,3 +163,43 @@ def test_mp2_coupling_d_shell_species(L, oracle):
                                            oracle.Basis.from_shells(p["shells"]), 2, Cp, ep, 1, 0, -1.0)
     assert abs(got - ref) < 1e-10 * max(1.0, abs(ref))
     he.close(); hp.close()
+
+
+def test_moint_file_matches_oracle(L, oracle, golden, tmp_path):
+    """LowdinGB300_mp2_moint on the golden water: the file holds the oracle's
+    (ia|jb) entries in the transform's order (same indices, values within
+    1e-10), and its MP2 energy is the device one and the golden one."""
+    torch = pytest.importorskip("torch")
+    from openlowdin_gb300 import moint as M
+    sysd = GS.h2o_boa(golden)
+    res = oracle.scf(oracle.from_plain(sysd))
+    sp = sysd["species"][0]
+    b = oracle.Basis.from_shells(sp["shells"])
+    C, eps = res.coefficients[0], res.orbital_energies[0]
+    nocc, n = 5, b.nbf
+    eri = oracle.eri_full(b)
+    iajb = np.einsum("pqrs,pi,qa,rj,sb->iajb", eri, C[:, :nocc], C[:, nocc:], C[:, :nocc], C[:, nocc:],
+                     optimize=True)
+    ref = M.mp2_entries(iajb, 0, nocc)
+    h = L.Libint2Interface(sp, 1)
+    dD = torch.tensor(res.densities[0], device="cuda")
+    dC = torch.tensor(np.ascontiguousarray(C.T), device="cuda")
+    path = str(tmp_path / "Emoint.dat")
+    e2, nw = h.mp2_moint(dD.data_ptr(), dC.data_ptr(), eps, nocc, 0, path, stack_size=1000,
+                         stream=torch.cuda.current_stream().cuda_stream)
+    h.close()
+    got = M.read_moint(path, 1000)
+    assert nw == len(got[4])
+    # entries within 1e-13 relative of the cut may fall on either side of it
+    near = lambda v: np.abs(np.abs(v) - 1e-10) < 1e-13
+    kg = {tuple(k): v for k, v in zip(np.stack(got[:4], 1).tolist(), got[4])}
+    kr = {tuple(k): v for k, v in zip(np.stack(ref[:4], 1).tolist(), ref[4])}
+    assert all(near(kr[k]) for k in set(kr) - set(kg))
+    assert all(near(kg[k]) for k in set(kg) - set(kr))
+    common = [k for k in kr if k in kg]
+    assert max(abs(kg[k] - kr[k]) for k in common) < 1e-10
+    order = np.lexsort(np.stack(got[:4], 1).astype(np.int64)[:, ::-1].T)
+    assert np.array_equal(order, np.arange(len(order)))
+    assert abs(M.mp2_energy(got, eps, nocc, 0, n) - e2) < 1e-10
+    g = golden["values"]["H2O.BOA.MP2.DIRECT"]["MP2 energy"]
+    assert abs(res.energy + e2 - g[0]) <= g[1]
