@@ -450,6 +450,9 @@ struct LibintInterface {
   DevBuf<double> dD, dDs, dDn, dGacc, dG, dA, dC, dDsC, dJacc;
   DevBuf<float> dDs32, dDn32, dGacc32, dDsC32, dJacc32;
   DevBuf<unsigned long long> dcount;
+  unsigned long long *hcount = nullptr;   // pinned copy of dcount, read once its stream is done
+  cudaStream_t count_stream = nullptr;
+  bool count_pending = false;
   long long last_quartets = -1;
   long long class_quartets[kNQC] = {0};
   TaskSet<JKTask> jk;        // cached J/K tasks of the handle's own buffers
@@ -476,6 +479,9 @@ struct LibintInterface {
     dDsC.release(); dJacc.release();
     dDs32.release(); dDn32.release(); dGacc32.release(); dDsC32.release(); dJacc32.release();
     dcount.release();
+    if (hcount) cudaFreeHost(hcount);
+    hcount = nullptr;
+    count_pending = false;
     jk.release();
     cp.release();
     jk_ready = false;
@@ -679,15 +685,26 @@ struct LibintInterface {
     CK(cudaMemsetAsync(dcount.p, 0, sizeof(unsigned long long) * kNQC, s));
     if (!launch_jk_groups(jk, precision, split, boys, s)) return false;
     CK(launch_symmetrize(dGacc.p, dGacc32.p, d_norma, n, 0.25, dGout, s));
-    unsigned long long cnt[kNQC];
-    CK(cudaMemcpyAsync(cnt, dcount.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    // the quartet counts travel with the result; they are summed when asked for
+    if (!hcount) CK(cudaHostAlloc((void **)&hcount, kNQC * sizeof(unsigned long long), cudaHostAllocDefault));
+    CK(cudaMemcpyAsync(hcount, dcount.p, kNQC * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    count_stream = s;
+    count_pending = true;
+    return true;
+  }
+
+  void collect_counts() {
+    if (!count_pending) return;
+    if (cudaStreamSynchronize(count_stream) != cudaSuccess) {
+      set_error("quartet counts: stream synchronisation failed");
+      return;
+    }
+    count_pending = false;
     last_quartets = 0;
     for (int c = 0; c < kNQC; ++c) {
-      class_quartets[c] = (long long)cnt[c];
-      last_quartets += (long long)cnt[c];
+      class_quartets[c] = (long long)hcount[c];
+      last_quartets += (long long)hcount[c];
     }
-    return true;
   }
 
   // J/K tasks of this species into ts: one task per (bra class >= ket class)
@@ -1197,12 +1214,17 @@ int LowdinGB300_coupling_device(LibintInterface *a, LibintInterface *b, const do
   return coupling(a, b, dDa, dDb, dJa, dJb, fp32 != 0, (cudaStream_t)stream) ? 0 : -1;
 }
 
-long long LowdinGB300_last_quartets(LibintInterface *lint) { return lint ? lint->last_quartets : -1; }
+long long LowdinGB300_last_quartets(LibintInterface *lint) {
+  if (!lint) return -1;
+  lint->collect_counts();
+  return lint->last_quartets;
+}
 
 long long LowdinGB300_launch_count(void) { return lgb::launch_count(); }
 
 int LowdinGB300_last_class_quartets(LibintInterface *lint, long long *out) {
   if (!check_handle(lint, __func__)) return -1;
+  lint->collect_counts();
   for (int c = 0; c < kNumPairClasses * kNumPairClasses; ++c) out[c] = lint->class_quartets[c];
   return kNumPairClasses * kNumPairClasses;
 }
