@@ -148,7 +148,9 @@ __device__ __forceinline__ void boys_f64(double T, double (&F)[L + 1], const dou
     const double r = rsqrt(T);
     F[0] = 0.88622692545275801365 * r;  // sqrt(pi/T)/2
     if constexpr (L > 0) {
-      const double e = exp(-T);
+      // e^{-T} < 1.1e-20 above T = 46: its share of every F_m (m <= 8) there is
+      // below 1e-11 relative and 1e-21 absolute, so it is left out
+      const double e = T < 46.0 ? exp(-T) : 0.0;
       const double o2T = 0.5 * r * r;
 #pragma unroll
       for (int m = 0; m < L; ++m) F[m + 1] = ((2 * m + 1) * F[m] - e) * o2T;

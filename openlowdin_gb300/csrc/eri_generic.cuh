@@ -96,7 +96,7 @@ __device__ inline void boys_f64_rt(int L, double T, double *F, const double *__r
     const double e = __ldg(t + kBoysTaylor) * exp_small(mdT);
     for (int m = L - 1; m >= 0; --m) F[m] = fma(2.0 * T, F[m + 1], e) / (2 * m + 1);
   } else {
-    const double e = exp(-T);
+    const double e = T < 46.0 ? exp(-T) : 0.0;   // below 1.1e-20 above T = 46
     const double r = rsqrt(T);
     F[0] = 0.88622692545275801365 * r;
     const double o2T = 0.5 * r * r;
