@@ -94,7 +94,11 @@ void LibintInterface_compute_coupling_direct(LibintInterface *lint, LibintInterf
 void LibintInterface_compute_coupling_directIT(LibintInterface *lint, LibintInterface *olint, double *dens,
                                                double *coeff, double *result, LGB_REF(int) p);
 
-/* Libint2Iface.h:399 -- UHF alpha/beta direct coupling: not provided. */
+/* Libint2Iface.h:399 (Libint2Iface.cpp:1626-1825, wrapper :3625-3658) -- UHF
+   alpha/beta Coulomb energy: result[0] = sum_{ij in lint, kl in olint}
+   dens(ij) (ij|kl) otherdens(kl) over the coupling integral set (raw
+   |v| < 1e-10 dropped, no screening); the two species share one basis in the
+   reference's use (E-ALPHA / E-BETA). */
 void LibintInterface_compute_alphabeta_direct(LibintInterface *lint, LibintInterface *olint, double *dens,
                                               double *otherdens, double *result);
 

@@ -571,8 +571,33 @@ void LibintInterface_compute_coupling_directIT(LibintInterface *lint, LibintInte
   first_quarter(lint, olint, nullptr, coeff, p, result);
 }
 
-void LibintInterface_compute_alphabeta_direct(LibintInterface *, LibintInterface *, double *, double *, double *) {
-  unsupported(__func__);
+void LibintInterface_compute_alphabeta_direct(LibintInterface *lint, LibintInterface *olint, double *dens,
+                                              double *otherdens, double *result) {
+  if (!check_handle(lint, __func__) || !check_handle(olint, __func__)) return;
+  if (!dens || !otherdens || !result) {
+    set_error("%s: null argument", __func__);
+    return;
+  }
+  if (!lint->ensure_all() || !olint->ensure_all()) return;
+  const int n = lint->nbasis, no = olint->nbasis;
+  cudaStream_t s = lint->stream;
+  if (!olint->dD.ensure((size_t)no * no) || !lint->dG.ensure((size_t)n * n)) return;
+  if (cudaMemcpyAsync(olint->dD.p, otherdens, sizeof(double) * no * no, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+    set_error("compute_alphabeta_direct: density upload failed");
+    return;
+  }
+  // sum_{ij kl} D(ij) (ij|kl) D_other(kl) over the coupling integral set (raw
+  // |v| < 1e-10 dropped, no screening) = sum_ij D(ij) J[D_other](ij)
+  if (!coupling(lint, olint, nullptr, olint->dD.p, lint->dG.p, nullptr, false, s)) return;
+  std::vector<double> J((size_t)n * n);
+  if (cudaMemcpyAsync(J.data(), lint->dG.p, sizeof(double) * n * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess) {
+    set_error("compute_alphabeta_direct: result download failed");
+    return;
+  }
+  double e = 0.0;
+  for (size_t k = 0; k < J.size(); ++k) e += dens[k] * J[k];
+  result[0] = e;
 }
 void LibintInterface_compute_coupling_disk(LibintInterface *, LibintInterface *, const char *) {
   unsupported(__func__);

@@ -52,6 +52,7 @@ def lib():
         L.LibintInterface_compute_2body_direct.argtypes = [_vp, _f64p, _f64p, ctypes.POINTER(ctypes.c_double)]
         L.LibintInterface_compute_2body_directIT.argtypes = [_vp, _f64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int)]
         L.LibintInterface_compute_coupling_direct.argtypes = [_vp, _vp, _f64p, _f64p]
+        L.LibintInterface_compute_alphabeta_direct.argtypes = [_vp, _vp, _f64p, _f64p, _f64p]
         L.LibintInterface_compute_coupling_directIT.argtypes = [_vp, _vp, _f64p, _f64p, _f64p,
                                                                 ctypes.POINTER(ctypes.c_int)]
         L.LowdinGB300_last_error.restype = ctypes.c_char_p
@@ -315,6 +316,14 @@ class Libint2Interface:
                                                       out)
         _check()
         return out
+
+    def compute_alphabeta_direct(self, other: "Libint2Interface", density, other_density) -> float:
+        """Libint2Interface_compute2BodyAlphaBeta_direct: sum D (ij|kl) D_other."""
+        out = np.zeros(1)
+        lib().LibintInterface_compute_alphabeta_direct(self.h, other.h, np.ascontiguousarray(density, np.float64),
+                                                       np.ascontiguousarray(other_density, np.float64), out)
+        _check()
+        return float(out[0])
 
     def compute_2body_directIT(self, density, coefficients, p: int) -> np.ndarray:
         n = self.nbasis

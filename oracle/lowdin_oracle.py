@@ -177,6 +177,16 @@ def coupling_direct(b: Basis, sid: int, ob: Basis, osid: int, Dother: np.ndarray
     return B.reshape(n, n)
 
 
+def alphabeta_direct(b: Basis, sid: int, ob: Basis, osid: int, D, Dother) -> float:
+    """LibintInterface_compute_alphabeta_direct (src/ints/Libint2Iface.cpp:1626-1825,
+    wrapper :3625-3658): sum_{ij kl} D(ij) (ij|kl) D_other(kl) over the
+    coupling integral set, i.e. D contracted with the full symmetric J[D_other]
+    of coupling_direct."""
+    B = coupling_direct(b, sid, ob, osid, Dother)
+    J = np.tril(B) + np.tril(B, -1).T
+    return float(np.sum(np.asarray(D, np.float64) * J))
+
+
 def two_body_directIT(b: Basis, is_electron: bool, D, C, p: int):
     n = b.nbf
     A = np.zeros(n ** 3)

@@ -102,6 +102,26 @@ def test_coupling_both_orders(L, oracle, ids):
     he.close(); hp.close()
 
 
+@pytest.mark.parametrize("ids", [(1, 2), (2, 1)])
+def test_alphabeta_energy(L, oracle, ids):
+    """LibintInterface_compute_alphabeta_direct: alpha and beta electrons of
+    the water basis (two species, one basis), random densities; both handle
+    orders give sum D_a (ij|kl) D_b."""
+    sp = S.water()["species"][0]
+    n = S.nbasis(sp)
+    rng = np.random.default_rng(12)
+    Da, Db = _sym(rng, n, 0.2), _sym(rng, n, 0.2)
+    ha = L.Libint2Interface(sp, ids[0])
+    hb = L.Libint2Interface(sp, ids[1])
+    b = oracle.Basis.from_shells(sp["shells"])
+    ref = oracle.alphabeta_direct(b, ids[0], b, ids[1], Da, Db)
+    e_ab = ha.compute_alphabeta_direct(hb, Da, Db)
+    e_ba = hb.compute_alphabeta_direct(ha, Db, Da)
+    assert abs(e_ab - ref) < 1e-10 * max(1.0, abs(ref))
+    assert abs(e_ba - ref) < 1e-10 * max(1.0, abs(ref))
+    ha.close(); hb.close()
+
+
 def test_first_quarter_intra(L, oracle):
     sysd = S.water()
     sp = sysd["species"][0]

@@ -169,3 +169,19 @@ def test_coupling_restatement(oracle, golden):
     B12 = oracle.coupling_direct(e, 1, p, 2, Dp)
     B21 = oracle.coupling_direct(e, 2, p, 1, Dp)
     assert np.max(np.abs(B12 - B21)) < 1e-10
+
+
+def test_alphabeta_restatement(oracle):
+    """alpha/beta Coulomb energy (Libint2Iface.cpp:1626-1825): symmetric in the
+    two species and equal to the full-tensor contraction up to the 1e-10 raw
+    integral cut."""
+    sp = S.water()["species"][0]
+    b = oracle.Basis.from_shells(sp["shells"])
+    rng = np.random.default_rng(8)
+    X, Y = rng.normal(size=(2, b.nbf, b.nbf)) * 0.1
+    Da, Db = X + X.T, Y + Y.T
+    e1 = oracle.alphabeta_direct(b, 1, b, 2, Da, Db)
+    e2 = oracle.alphabeta_direct(b, 2, b, 1, Db, Da)
+    full = float(np.einsum("ij,ijkl,kl->", Da, oracle.eri_full(b), Db))
+    assert abs(e1 - e2) < 1e-10 * abs(full)
+    assert abs(e1 - full) < 1e-7
