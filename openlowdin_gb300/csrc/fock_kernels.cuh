@@ -16,6 +16,27 @@ __device__ __forceinline__ R warp_sum(R v) {
   return v;
 }
 
+// The FP64 pipe of this GPU issues at 1/64 of the FP32 rate, so comparisons
+// and maxima of non-negative doubles are done on their bit patterns (IEEE
+// order of non-negative values = unsigned integer order of their bits):
+// integer instructions, identical decisions.
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ unsigned abs_bits(float v) { return __float_as_uint(v) & 0x7fffffffu; }
+// |v| < t and |v| > t for a non-negative threshold t
+template <typename R>
+__device__ __forceinline__ bool abs_below(R v, R t) { return abs_bits(v) < abs_bits(t); }
+template <typename R>
+__device__ __forceinline__ bool abs_above(R v, R t) { return abs_bits(v) > abs_bits(t); }
+// 2^k, k = 0..3 (quartet degeneracies), from the exponent field alone
+template <typename R>
+__device__ __forceinline__ R pow2(int k) {
+  if constexpr (std::is_same<R, double>::value) return __longlong_as_double((long long)(1023 + k) << 52);
+  else return __int_as_float((127 + k) << 23);
+}
+
+// largest shell-block maximum |D| over the six index pairs of a quartet
 template <typename T>
 __device__ __forceinline__ T dnorm6(const T *__restrict__ Dn, int nsh, int a, int b, int c, int d) {
   T m = __ldg(Dn + a * nsh + b);
@@ -25,6 +46,17 @@ __device__ __forceinline__ T dnorm6(const T *__restrict__ Dn, int nsh, int a, in
   m = max(m, __ldg(Dn + b * nsh + d));
   m = max(m, __ldg(Dn + c * nsh + d));
   return m;
+}
+template <>
+__device__ __forceinline__ double dnorm6(const double *__restrict__ Dn, int nsh, int a, int b, int c, int d) {
+  const unsigned long long *u = reinterpret_cast<const unsigned long long *>(Dn);   // entries are >= 0
+  unsigned long long m = __ldg(u + a * nsh + b);
+  m = max(m, __ldg(u + a * nsh + c));
+  m = max(m, __ldg(u + b * nsh + c));
+  m = max(m, __ldg(u + a * nsh + d));
+  m = max(m, __ldg(u + b * nsh + d));
+  m = max(m, __ldg(u + c * nsh + d));
+  return __longlong_as_double((long long)m);
 }
 
 // task owning flattened block b: last task with blk0 <= b (tasks sorted by blk0)
@@ -135,7 +167,7 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
   } else if (T.screen) {
     const double b = T.pairs[bi].Q * (F64 ? (double)ket.Q : T.pairs[ki].Q) *
                      dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
-    if (b < TL.eps) active = false;
+    if (abs_below(b, TL.eps)) active = false;
   }
   if (__all_sync(0xffffffffu, !active)) return;
   if (T.count) {
@@ -150,7 +182,7 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
 #pragma unroll
     for (int x = 0; x < Q::NINT; ++x) I[x] = R(0);
   }
-  const R deg = active ? R((bra.sa == bra.sb ? 1 : 2) * (ket.sa == ket.sb ? 1 : 2) * (bi == ki ? 1 : 2)) : R(0);
+  const R deg = active ? pow2<R>((bra.sa != bra.sb) + (ket.sa != ket.sb) + (bi != ki)) : R(0);
   const R hdeg = deg * R(T.hf);
   const int n = T.n;
   double *G = T.Gacc;
@@ -258,7 +290,7 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
     // test is done in FP32 in mixed launches so both launches agree
     const int bi = T.bra0 + bpos, ki = T.ket0 + min(kpos, T.nket - 1);
     const bool tiny = TL.split > 0.0 ? T.pa32[bi].Q * T.pb32[ki].Q * 0.999f < (float)TL.cut
-                                     : T.pa[bi].Q * T.pb[ki].Q * (1.0 - 1e-9) < TL.cut;
+                                     : abs_below(T.pa[bi].Q * T.pb[ki].Q * (1.0 - 1e-9), TL.cut);
     if (tiny) active = false;
   }
   if (TL.split > 0.0) {
@@ -299,7 +331,7 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
   const R cut = R(TL.cut);
 #pragma unroll
   for (int x = 0; x < Q::NINT; ++x)
-    if (!(fabs(I[x]) >= cut)) I[x] = R(0);
+    if (abs_below(I[x], cut)) I[x] = R(0);
   auto Iat = [&](int a, int b, int c, int d) -> R { return I[((a * NB + b) * NC + c) * ND + d]; };
   const int fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb;
   const bool abdiff = bra.sa != bra.sb, cddiff = ket.sa != ket.sb;
@@ -375,16 +407,16 @@ __global__ void __launch_bounds__(128) it_kernel(ITParams P) {
   const PairRec bra = P.pa[bi];
   const PairRec ket = P.pb[ki];
   // every raw integral is bounded by Q_ab Q_cd (Schwarz) and only |v| > cut is used
-  if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) return;
+  if (!abs_above(bra.Q * ket.Q * (1.0 - 1e-9), P.cut)) return;
   if (P.screen) {
     const double b = bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
-    if (b < P.eps) return;
+    if (abs_below(b, P.eps)) return;
   }
   double I[Q::NINT];
   eri_quartet<double, LA, LB, LC, LD>(bra, P.pra + bra.prim0, ket, P.prb + ket.prim0, P.boys.f64, P.boys.f32, I);
 #pragma unroll
   for (int x = 0; x < Q::NINT; ++x)
-    if (!(fabs(I[x]) > P.cut)) I[x] = 0.0;
+    if (!abs_above(I[x], P.cut)) I[x] = 0.0;
   auto I4 = [&](int a, int b, int c, int d) -> double { return I[((a * NB + b) * NC + c) * ND + d]; };
   const bool ab = bra.sa != bra.sb, cd = ket.sa != ket.sb;
   const int fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb, nB = P.nB;
@@ -421,8 +453,8 @@ __global__ void __launch_bounds__(128) mp2x_kernel(MXParams P) {
   const int bi = P.bra0 + bpos, ki = P.ket0 + kpos;
   const PairRec bra = P.pairs[bi];
   const PairRec ket = P.kpairs[ki];
-  if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) return;
-  if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) return;
+  if (!abs_above(bra.Q * ket.Q * (1.0 - 1e-9), P.cut)) return;
+  if (P.screen && abs_below(bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb), P.eps)) return;
   double I[Q::NINT];
   eri_quartet<double, LA, LB, LC, LD>(bra, P.prims + bra.prim0, ket, P.kprims + ket.prim0, P.boys.f64, P.boys.f32,
                                       I);
@@ -438,7 +470,7 @@ __global__ void __launch_bounds__(128) mp2x_kernel(MXParams P) {
 #pragma unroll
         for (int d = 0; d < ND; ++d) {
           const double v = I[((a * NB + b) * NC + c) * ND + d];
-          if (!(fabs(v) > P.cut)) continue;
+          if (!abs_above(v, P.cut)) continue;
           const size_t col = col0 + c * ND + d;
           const size_t i1 = ((bra.fa + a) * ncol + col) * n + bra.fb + b;
           const size_t i2 = ((bra.fb + b) * ncol + col) * n + bra.fa + a;

@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(128) jk_coop_kernel(const JKTask *__restrict__
         }
         if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) active = false;
       } else if (T.screen) {
-        if (bra.Q * ket.Q * dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < TL.eps) active = false;
+        if (abs_below(bra.Q * ket.Q * dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb), TL.eps)) active = false;
       }
       if (!active) continue;   // uniform across the warp
       if (T.count && lane == 0) atomicAdd(T.count, 1ull);
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(128) cp_coop_kernel(const CPTask *__restrict__
       eri_coop(g, ct, Lo, K.la, K.lb, K.lc, K.ld, bra, T.pra, ket, T.prb, TL.boys.f64, sm);
       auto Iat = [&](int a, int b, int c, int d) {
         const double v = I[((a * NB + b) * NC + c) * ND + d];
-        return fabs(v) >= TL.cut ? v : 0.0;
+        return abs_below(v, TL.cut) ? 0.0 : v;
       };
       const int fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb;
       const bool abdiff = bra.sa != bra.sb, cddiff = ket.sa != ket.sb;
@@ -236,8 +236,8 @@ __global__ void __launch_bounds__(128) it_coop_kernel(ITParams P, GenClass K) {
     const int bi = P.bra0 + bpos, ki = P.ket0 + kpos;
     const PairRec &bra = P.pa[bi];
     const PairRec &ket = P.pb[ki];
-    if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) continue;
-    if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) continue;
+    if (!abs_above(bra.Q * ket.Q * (1.0 - 1e-9), P.cut)) continue;
+    if (P.screen && abs_below(bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb), P.eps)) continue;
     eri_coop(g, ct, Lo, K.la, K.lb, K.lc, K.ld, bra, P.pra, ket, P.prb, P.boys.f64, sm);
     const bool ab = bra.sa != bra.sb, cd = ket.sa != ket.sb;
     const bool mirror = P.intra && bi != ki;
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(128) it_coop_kernel(ITParams P, GenClass K) {
           int a, b, c, d;
           it_map(r, mu, nu, l, s, &a, &b, &c, &d);
           const double v = I[((a * NB + b) * NC + c) * ND + d];
-          if (fabs(v) > P.cut) acc += __ldg(P.Cs + fmu + mu) * v;
+          if (abs_above(v, P.cut)) acc += __ldg(P.Cs + fmu + mu) * v;
         }
         atomicAdd(P.A + ((size_t)(fnu + nu) * P.nB + fl + l) * P.nB + fs + s, acc);
       }
@@ -282,8 +282,8 @@ __global__ void __launch_bounds__(128) mp2x_coop_kernel(MXParams P, GenClass K) 
     const int bi = P.bra0 + (int)(q / P.nket), ki = P.ket0 + (int)(q % P.nket);
     const PairRec &bra = P.pairs[bi];
     const PairRec &ket = P.kpairs[ki];
-    if (bra.Q * ket.Q * (1.0 - 1e-9) <= P.cut) continue;
-    if (P.screen && bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb) < P.eps) continue;
+    if (!abs_above(bra.Q * ket.Q * (1.0 - 1e-9), P.cut)) continue;
+    if (P.screen && abs_below(bra.Q * ket.Q * dnorm6(P.Dn, P.nsh, bra.sa, bra.sb, ket.sa, ket.sb), P.eps)) continue;
     eri_coop(g, ct, Lo, K.la, K.lb, K.lc, K.ld, bra, P.prims, ket, P.kprims, P.boys.f64, sm);
     const int col0 = __ldg(P.colbase + ki) - P.col_first;
     const bool two = bra.sa != bra.sb;
@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(128) mp2x_coop_kernel(MXParams P, GenClass K) 
     for (int t = lane; t < NA * NB * NC * ND; t += 32) {
       const int a = t / (NB * NC * ND), b = (t / (NC * ND)) % NB, c = (t / ND) % NC, d = t % ND;
       const double v = I[t];
-      if (!(fabs(v) > P.cut)) continue;
+      if (!abs_above(v, P.cut)) continue;
       const size_t col = col0 + c * ND + d;
       if (P.X) {
         P.X[((bra.fa + a) * ncol + col) * n + bra.fb + b] = v;
