@@ -155,15 +155,15 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
   const int ki = T.ket0 + min(kpos, T.nket - 1);
   const PairT<R> &bra = pairs[bi];
   const PairT<R> &ket = sk[threadIdx.x].p;
-  if (TL.split > 0.0) {
+  if (TL.mixed) {
     // FP32 bound from the FP32 Schwarz factors (the FP64 records hold the
     // same values before rounding), identical in both launches
     float b = T.pairs32[bi].Q * (float)ket.Q;
     if (T.screen) {
       b *= dnorm6(T.Dn32, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
-      if (b < fmaxf((float)TL.eps, TL.skip)) active = false;
+      if (b < fmaxf(TL.eps32, TL.skip)) active = false;
     }
-    if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) active = false;
+    if (TL.lower ? !(b < TL.split32) : (b < TL.split32)) active = false;
   } else if (T.screen) {
     const double b = T.pairs[bi].Q * (F64 ? (double)ket.Q : T.pairs[ki].Q) *
                      dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
@@ -183,7 +183,10 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
     for (int x = 0; x < Q::NINT; ++x) I[x] = R(0);
   }
   const R deg = active ? pow2<R>((bra.sa != bra.sb) + (ket.sa != ket.sb) + (bi != ki)) : R(0);
-  const R hdeg = deg * R(T.hf);
+  R hf;
+  if constexpr (F64) hf = T.hf;
+  else hf = T.hf32;
+  const R hdeg = deg * hf;
   const int n = T.n;
   double *G = T.Gacc;
   float *G32 = T.Gacc32;
@@ -289,11 +292,11 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
     // below the cut are dropped, so such a quartet contributes nothing; the
     // test is done in FP32 in mixed launches so both launches agree
     const int bi = T.bra0 + bpos, ki = T.ket0 + min(kpos, T.nket - 1);
-    const bool tiny = TL.split > 0.0 ? T.pa32[bi].Q * T.pb32[ki].Q * 0.999f < (float)TL.cut
+    const bool tiny = TL.mixed ? T.pa32[bi].Q * T.pb32[ki].Q * 0.999f < TL.cut32
                                      : abs_below(T.pa[bi].Q * T.pb[ki].Q * (1.0 - 1e-9), TL.cut);
     if (tiny) active = false;
   }
-  if (TL.split > 0.0) {
+  if (TL.mixed) {
     // mixed precision: FP32 for quartets whose Q_ab Q_cd max(|D_A|, |D_B|)
     // bound (FP32, identical in both launches) is below the split
     const int bi = T.bra0 + bpos, ki = T.ket0 + min(kpos, T.nket - 1);
@@ -303,7 +306,7 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
     if (T.DnA32) dm = __ldg(T.DnA32 + b32.sa * T.nshA + b32.sb);
     if (T.DnB32) dm = fmaxf(dm, __ldg(T.DnB32 + k32.sa * T.nshB + k32.sb));
     const float b = b32.Q * k32.Q * dm;
-    if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) active = false;
+    if (TL.lower ? !(b < TL.split32) : (b < TL.split32)) active = false;
     if ((T.DnA32 || T.DnB32) && b < TL.skip) active = false;
   }
   if (__all_sync(0xffffffffu, !active)) return;
@@ -328,14 +331,20 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
 #pragma unroll
     for (int x = 0; x < Q::NINT; ++x) I[x] = R(0);
   }
-  const R cut = R(TL.cut);
+  R cut, scale;
+  if constexpr (F64) {
+    cut = TL.cut;
+    scale = T.scale;
+  } else {
+    cut = TL.cut32;
+    scale = T.scale32;
+  }
 #pragma unroll
   for (int x = 0; x < Q::NINT; ++x)
     if (abs_below(I[x], cut)) I[x] = R(0);
   auto Iat = [&](int a, int b, int c, int d) -> R { return I[((a * NB + b) * NC + c) * ND + d]; };
   const int fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb;
   const bool abdiff = bra.sa != bra.sb, cddiff = ket.sa != ket.sb;
-  const R scale = R(T.scale);
   if (T.JA) {
     const R wk = active ? R(cddiff ? 2 : 1) * scale : R(0);
     const int nB = T.nB, nA = T.nA;

@@ -81,13 +81,13 @@ __global__ void __launch_bounds__(128) jk_coop_kernel(const JKTask *__restrict__
       const PairRec &bra = T.pairs[bi];
       const PairRec &ket = T.pairs[ki];
       bool active = true;
-      if (TL.split > 0.0) {
+      if (TL.mixed) {
         float b = T.pairs32[bi].Q * T.pairs32[ki].Q;
         if (T.screen) {
           b *= dnorm6(T.Dn32, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
-          if (b < fmaxf((float)TL.eps, TL.skip)) active = false;
+          if (b < fmaxf(TL.eps32, TL.skip)) active = false;
         }
-        if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) active = false;
+        if (TL.lower ? !(b < TL.split32) : (b < TL.split32)) active = false;
       } else if (T.screen) {
         if (abs_below(bra.Q * ket.Q * dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb), TL.eps)) active = false;
       }
@@ -165,17 +165,17 @@ __global__ void __launch_bounds__(128) cp_coop_kernel(const CPTask *__restrict__
     if (bpos >= T.nbra || (T.active && __ldg(T.active) == 0)) continue;
     for (int kpos = kpos0; kpos < kpos0 + 8 && kpos < T.nket; ++kpos) {
       const int bi = T.bra0 + bpos, ki = T.ket0 + kpos;
-      const bool tiny = TL.split > 0.0 ? T.pa32[bi].Q * T.pb32[ki].Q * 0.999f < (float)TL.cut
+      const bool tiny = TL.mixed ? T.pa32[bi].Q * T.pb32[ki].Q * 0.999f < TL.cut32
                                        : T.pa[bi].Q * T.pb[ki].Q * (1.0 - 1e-9) < TL.cut;
       if (tiny) continue;
-      if (TL.split > 0.0) {
+      if (TL.mixed) {
         const PairRec32 &b32 = T.pa32[bi];
         const PairRec32 &k32 = T.pb32[ki];
         float dm = 0.f;
         if (T.DnA32) dm = __ldg(T.DnA32 + b32.sa * T.nshA + b32.sb);
         if (T.DnB32) dm = fmaxf(dm, __ldg(T.DnB32 + k32.sa * T.nshB + k32.sb));
         const float b = b32.Q * k32.Q * dm;
-        if (TL.lower ? !(b < (float)TL.split) : (b < (float)TL.split)) continue;
+        if (TL.lower ? !(b < TL.split32) : (b < TL.split32)) continue;
         if ((T.DnA32 || T.DnB32) && b < TL.skip) continue;
       }
       if (T.count && lane == 0) atomicAdd(T.count, 1ull);

@@ -44,6 +44,7 @@ struct JKTask {
   unsigned long long *count;  // quartets evaluated (may be null)
   const int *active;      // the task's system is built while *active != 0 (null: always)
   double hf;              // 0.5 * exchange factor
+  float hf32;             // the same in FP32
   int bra0, nbra, ket0, nket;
   int n, nsh;
   int triangle;           // same pair class: only ket position <= bra position
@@ -77,6 +78,7 @@ struct CPTask {
   const int *active;      // the task's system is built while *active != 0 (null: always)
   int nshA, nshB;
   double scale;           // q_A q_B (1 for the reference-shaped calls)
+  float scale32;          // the same in FP32
   int bra0, nbra, ket0, nket;
   int nA, nB;
   int blk0, nbx;
@@ -90,8 +92,18 @@ struct TaskLaunch {
   int lower;              // 1: this launch takes the quartets below split
   double cut;             // coupling: |raw| < cut is dropped
   float skip;             // mixed launches: quartets whose density-weighted bound is below skip are dropped
+  // FP32 copies of the thresholds and the mixed flag (split > 0), so that the
+  // kernels issue no FP64 conversion or comparison for them
+  int mixed;
+  float eps32, split32, cut32;
   BoysTables boys;
 };
+inline void set_fp32_copies(TaskLaunch &tl) {
+  tl.mixed = tl.split > 0.0;
+  tl.eps32 = (float)tl.eps;
+  tl.split32 = (float)tl.split;
+  tl.cut32 = (float)tl.cut;
+}
 
 // Kernel entry types of the class-templated launch tables (class_tables.cuh);
 // null entries are served by the block-cooperative kernels (classes of total

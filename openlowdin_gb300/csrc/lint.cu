@@ -281,6 +281,7 @@ bool add_cp_tasks(TaskSet<CPTask> &ts, LibintInterface *A, LibintInterface *B, c
       t.nshA = A->nshell();
       t.nshB = B->nshell();
       t.scale = scale;
+      t.scale32 = (float)scale;
       t.bra0 = A->all.start[cb];
       t.nbra = A->all.count(cb);
       t.ket0 = B->all.start[ck];
@@ -307,11 +308,13 @@ bool launch_cp_groups(const TaskSet<CPTask> &ts, int mode, double split, BoysTab
     const int cb = c / kNumPairClasses, ck = c % kNumPairClasses;
     if (mode == 2) {
       tl.split = split;
+      set_fp32_copies(tl);
       tl.lower = 0;
       CK(launch_cp_tasks(cb, ck, false, ts.d + ts.off[c], tl, s));
       tl.lower = 1;
       CK(launch_cp_tasks(cb, ck, true, ts.d + ts.off[c], tl, s));
     } else {
+      set_fp32_copies(tl);
       CK(launch_cp_tasks(cb, ck, mode == 1, ts.d + ts.off[c], tl, s));
     }
   }

@@ -506,6 +506,7 @@ struct LibintInterface {
         t.Gacc32 = bf.G32;
         t.count = counters ? counters + cb * kNumPairClasses + ck : nullptr;
         t.hf = hf;
+        t.hf32 = (float)hf;
         t.bra0 = sig.start[cb];
         t.nbra = sig.count(cb);
         t.ket0 = sig.start[ck];
@@ -533,9 +534,11 @@ struct LibintInterface {
       const int cb = c / kNumPairClasses, ck = c % kNumPairClasses;
       if (precision == 0) {
         tl.split = 0.0;
+        set_fp32_copies(tl);
         CK(launch_jk_tasks(cb, ck, false, ts.d + ts.off[c], tl, s));
       } else {
         tl.split = split;
+        set_fp32_copies(tl);
         tl.lower = 0;
         CK(launch_jk_tasks(cb, ck, false, ts.d + ts.off[c], tl, s));
         tl.lower = 1;
