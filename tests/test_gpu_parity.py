@@ -122,6 +122,22 @@ def test_alphabeta_energy(L, oracle, ids):
     ha.close(); hb.close()
 
 
+def test_alphabeta_golden_apmo_water(L, oracle, golden):
+    """test/H2O.APMO.UHF.DIRECT.py: E-ALPHA/E-BETA Hartree energy from the
+    library (closed-shell solution: P_alpha = P_beta = P_e / 2)."""
+    sysd = GS.h2o_apmo(golden)
+    res = oracle.scf(oracle.from_plain(sysd))
+    sp = sysd["species"][0]
+    Ph = res.densities[0] / 2.0
+    ha, hb = L.Libint2Interface(sp, 1), L.Libint2Interface(sp, 2)
+    e = ha.compute_alphabeta_direct(hb, Ph, Ph)
+    ha.close(); hb.close()
+    b = oracle.Basis.from_shells(sp["shells"])
+    assert abs(e - oracle.alphabeta_direct(b, 1, b, 2, Ph, Ph)) < 1e-9
+    ref = golden["values"]["H2O.APMO.UHF.DIRECT"]["e-AlphaBetaRepulsion"]
+    assert abs(e - ref[0]) <= ref[1]
+
+
 def test_first_quarter_intra(L, oracle):
     sysd = S.water()
     sp = sysd["species"][0]

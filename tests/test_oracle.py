@@ -185,3 +185,17 @@ def test_alphabeta_restatement(oracle):
     full = float(np.einsum("ij,ijkl,kl->", Da, oracle.eri_full(b), Db))
     assert abs(e1 - e2) < 1e-10 * abs(full)
     assert abs(e1 - full) < 1e-7
+
+
+def test_golden_alphabeta_repulsion(oracle, golden):
+    """test/H2O.APMO.UHF.DIRECT.py: the E-ALPHA/E-BETA Hartree energy of the
+    APMO water.  Its UHF solution is closed shell (same total energy as RHF),
+    so P_alpha = P_beta = P_e / 2 of the RHF solution, and the energy is
+    sum P_alpha (ij|kl) P_beta over the coupling integral set."""
+    sysd = GS.h2o_apmo(golden)
+    res = oracle.scf(oracle.from_plain(sysd))
+    b = oracle.Basis.from_shells(sysd["species"][0]["shells"])
+    Ph = res.densities[0] / 2.0
+    e = oracle.alphabeta_direct(b, 1, b, 2, Ph, Ph)
+    ref = golden["values"]["H2O.APMO.UHF.DIRECT"]["e-AlphaBetaRepulsion"]
+    assert abs(e - ref[0]) <= ref[1], e
