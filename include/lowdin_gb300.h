@@ -279,6 +279,16 @@ long long LowdinGB300_mp2_last_columns(void);
 int LowdinGB300_mp2_moint(LibintInterface *lint, const double *dD, const double *dC, const double *eps, int n_occ,
                           int n_frozen, const char *path, int stack_size, double x_budget_gb, double *e2,
                           long long *n_written, void *stream);
+/* LowdinGB300_mp2_coupling in FP64 that also writes the inter-species
+   (ia|jb), i, a of species a and j, b of species b, to `path`
+   ("<species a>.<species b>moint.dat" in the reference; two-species DIRECT
+   branch of TransformIntegralsC.f90:1170-1374 with the MP2 bounds of
+   :1687-1697): every i, a, j, b in that loop order, |value| > 1e-10, same
+   record layout as LowdinGB300_mp2_moint. */
+int LowdinGB300_mp2_coupling_moint(LibintInterface *a, LibintInterface *b, const double *dCa, const double *dCb,
+                                   const double *eps_a, const double *eps_b, int n_occ_a, int n_frozen_a,
+                                   int n_occ_b, int n_frozen_b, double factor, const char *path, int stack_size,
+                                   double x_budget_gb, double *e2, long long *n_written, void *stream);
 /* The record writer alone (host only): `count` entries in the given order. */
 int LowdinGB300_moint_write(const char *path, int stack_size, const int *p, const int *q, const int *r,
                             const int *s, const double *v, long long count);

@@ -185,17 +185,20 @@ struct MP2Setup {
 };
 
 // (ia|jb) of occupied i (M[j][b][a], device) into the file in the reference's
-// loop order: a, then j >= i, then b (b >= a when j == i), |v| > 1e-10
-// (TransformIntegralsC.f90:570-640 with the MP2 bounds of :1489-1501)
+// loop order: a, then j, then b, |v| > 1e-10.  One species
+// (TransformIntegralsC.f90:570-640 with the MP2 bounds of :1489-1501): j >= i,
+// b >= a when j == i.  Two species (:1255-1350 with the bounds of :1687-1697):
+// every j and b of the other species.
 bool moint_block(const MP2Setup &S, int i, const double *dM, std::vector<double> &h, cudaStream_t s) {
   const int oB = S.oB, vB = S.vB, vA = S.vA;
   h.resize((size_t)oB * vB * vA);
   CK(cudaMemcpyAsync(h.data(), dM, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   const int p = S.nfA + i + 1;
+  const bool sym = !S.coupling;
   for (int a = 0; a < vA; ++a)
-    for (int j = i; j < oB; ++j)
-      for (int b = (j == i ? a : 0); b < vB; ++b) {
+    for (int j = sym ? i : 0; j < oB; ++j)
+      for (int b = (sym && j == i ? a : 0); b < vB; ++b) {
         const double v = h[((size_t)j * vB + b) * vA + a];
         if (std::fabs(v) > 1e-10 && !S.moint->put(p, S.noccA + a + 1, S.nfB + j + 1, S.noccB + b + 1, v))
           return false;
@@ -507,7 +510,7 @@ bool mp2_direct(LibintInterface *L, const double *dD, const double *dC, const do
 
 bool mp2_coupling(LibintInterface *A, LibintInterface *B, const double *dCA, const double *dCB, const double *epsA,
                   const double *epsB, int noccA, int nfA, int noccB, int nfB, double factor, int precision,
-                  size_t budget, double *e2out, cudaStream_t s) {
+                  size_t budget, double *e2out, cudaStream_t s, MointWriter *moint = nullptr) {
   if (A == B) {
     set_error("mp2_coupling: the two handles must be different species");
     return false;
@@ -551,6 +554,7 @@ bool mp2_coupling(LibintInterface *A, LibintInterface *B, const double *dCA, con
   q.cut = 1e-10;
   q.n = nA;
   q.boys = A->boys;
+  S.moint = moint;
   return mp2_run(S, precision, budget, e2out, s);
 }
 
@@ -599,6 +603,26 @@ int LowdinGB300_mp2_moint(LibintInterface *lint, const double *dD, const double 
   if (!w.open(path, stack_size)) return -1;
   const size_t budget = x_budget_gb > 0 ? (size_t)(x_budget_gb * 1e9) : (size_t)8e9;
   if (!mp2_direct(lint, dD, dC, eps, n_occ, n_frozen, 0, budget, e2, (cudaStream_t)stream, &w)) return -1;
+  if (!w.finish()) return -1;
+  if (n_written) *n_written = w.written;
+  return 0;
+}
+
+int LowdinGB300_mp2_coupling_moint(LibintInterface *a, LibintInterface *b, const double *dCa, const double *dCb,
+                                   const double *eps_a, const double *eps_b, int n_occ_a, int n_frozen_a,
+                                   int n_occ_b, int n_frozen_b, double factor, const char *path, int stack_size,
+                                   double x_budget_gb, double *e2, long long *n_written, void *stream) {
+  if (!check_handle(a, __func__) || !check_handle(b, __func__)) return -1;
+  if (!dCa || !dCb || !eps_a || !eps_b || !e2 || !path || stack_size < 1) {
+    set_error("%s: invalid argument", __func__);
+    return -1;
+  }
+  MointWriter w;
+  if (!w.open(path, stack_size)) return -1;
+  const size_t budget = x_budget_gb > 0 ? (size_t)(x_budget_gb * 1e9) : (size_t)8e9;
+  if (!mp2_coupling(a, b, dCa, dCb, eps_a, eps_b, n_occ_a, n_frozen_a, n_occ_b, n_frozen_b, factor, 0, budget, e2,
+                    (cudaStream_t)stream, &w))
+    return -1;
   if (!w.finish()) return -1;
   if (n_written) *n_written = w.written;
   return 0;

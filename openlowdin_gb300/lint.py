@@ -85,6 +85,11 @@ def lib():
                                             ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
                                             ctypes.POINTER(ctypes.c_longlong), _vp]
         L.LowdinGB300_mp2_moint.restype = ctypes.c_int
+        L.LowdinGB300_mp2_coupling_moint.argtypes = [_vp, _vp, _vp, _vp, _f64p, _f64p, ctypes.c_int, ctypes.c_int,
+                                                     ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_char_p,
+                                                     ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
+                                                     ctypes.POINTER(ctypes.c_longlong), _vp]
+        L.LowdinGB300_mp2_coupling_moint.restype = ctypes.c_int
         _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
         L.LowdinGB300_moint_write.argtypes = [ctypes.c_char_p, ctypes.c_int, _i32p, _i32p, _i32p, _i32p, _f64p,
                                               ctypes.c_longlong]
@@ -150,7 +155,7 @@ EXPORTED_SYMBOLS = [
     "LowdinGB300_batch_coupling_quartets", "LowdinGB300_noalloc_scratch_bytes",
     "LowdinGB300_twobody_device_noalloc", "LowdinGB300_mp2_direct", "LowdinGB300_mp2_last_columns", "LowdinGB300_mp2_coupling",
     "LowdinGB300_gemm_bf16_split", "LowdinGB300_gemm_bf16_precise",
-    "LowdinGB300_gemm_bench", "LowdinGB300_mp2_moint", "LowdinGB300_moint_write",
+    "LowdinGB300_gemm_bench", "LowdinGB300_mp2_moint", "LowdinGB300_mp2_coupling_moint", "LowdinGB300_moint_write",
 ]
 
 
@@ -416,6 +421,24 @@ class Libint2Interface:
         if rc != 0:
             _check()
             raise LowdinGB300Error("mp2_moint failed")
+        return e2.value, nw.value
+
+    def mp2_coupling_moint(self, other: "Libint2Interface", ca_ptr: int, cb_ptr: int, eps_a, eps_b, n_occ_a: int,
+                           n_frozen_a: int, n_occ_b: int, n_frozen_b: int, factor: float, path: str,
+                           stack_size: int = 30000, x_budget_gb: float = 0.0, stream: int = 0):
+        """FP64 inter-species MP2 term as mp2_coupling, also writing every
+        (ia|jb) to `path` in the moint.dat layout; returns (E, integrals written)."""
+        e2 = ctypes.c_double(0.0)
+        nw = ctypes.c_longlong(0)
+        rc = lib().LowdinGB300_mp2_coupling_moint(self.h, other.h, ca_ptr, cb_ptr,
+                                                  np.ascontiguousarray(eps_a, np.float64),
+                                                  np.ascontiguousarray(eps_b, np.float64), int(n_occ_a),
+                                                  int(n_frozen_a), int(n_occ_b), int(n_frozen_b), float(factor),
+                                                  os.fsencode(path), int(stack_size), float(x_budget_gb),
+                                                  ctypes.byref(e2), ctypes.byref(nw), stream)
+        if rc != 0:
+            _check()
+            raise LowdinGB300Error("mp2_coupling_moint failed")
         return e2.value, nw.value
 
     def mp2_coupling(self, other: "Libint2Interface", ca_ptr: int, cb_ptr: int, eps_a, eps_b, n_occ_a: int,

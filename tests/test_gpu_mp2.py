@@ -203,3 +203,45 @@ def test_moint_file_matches_oracle(L, oracle, golden, tmp_path):
     assert abs(M.mp2_energy(got, eps, nocc, 0, n) - e2) < 1e-10
     g = golden["values"]["H2O.BOA.MP2.DIRECT"]["MP2 energy"]
     assert abs(res.energy + e2 - g[0]) <= g[1]
+
+
+def test_coupling_moint_file_matches_oracle(L, oracle, golden, tmp_path):
+    """LowdinGB300_mp2_coupling_moint on the golden APMO water (electrons x
+    first proton species): the file holds the oracle's inter-species (ia|jb)
+    in the transform's order, and its energy is the device term."""
+    torch = pytest.importorskip("torch")
+    from openlowdin_gb300 import moint as M
+    sysd = GS.h2o_apmo(golden)
+    sysO = oracle.from_plain(sysd)
+    res = oracle.scf(sysO)
+    A, B = sysO.species[0], sysO.species[1]
+    CA, CB = res.coefficients[0], res.coefficients[1]
+    eA, eB = res.orbital_energies[0], res.orbital_energies[1]
+    oA, oB = A.n_occ, B.n_occ
+    ref = {}
+    for i in range(oA):
+        Ai = oracle.coupling_directIT(A.basis, 1, B.basis, 2, np.ascontiguousarray(CA.T), i)
+        Mi = np.einsum("nls,na,lj,sb->ajb", Ai, CA[:, oA:], CB[:, :oB], CB[:, oB:], optimize=True)
+        for a, j, b in zip(*np.nonzero(np.abs(Mi) > 1e-10)):
+            ref[(i + 1, oA + a + 1, j + 1, oB + b + 1)] = Mi[a, j, b]
+    factor = A.eta * B.eta * (A.charge * B.charge) ** 2
+    he = L.Libint2Interface(sysd["species"][0], 1)
+    hp = L.Libint2Interface(sysd["species"][1], 2)
+    dCA = torch.tensor(np.ascontiguousarray(CA.T), device="cuda")
+    dCB = torch.tensor(np.ascontiguousarray(CB.T), device="cuda")
+    path = str(tmp_path / "E-.H_1moint.dat")
+    e2, nw = he.mp2_coupling_moint(hp, dCA.data_ptr(), dCB.data_ptr(), eA, eB, oA, 0, oB, 0, factor, path,
+                                   stack_size=500, stream=torch.cuda.current_stream().cuda_stream)
+    he.close(); hp.close()
+    p, q, r, s, v = M.read_moint(path, 500)
+    assert nw == len(v)
+    key = np.stack([p, q, r, s], 1).astype(np.int64)
+    order = np.lexsort(key[:, ::-1].T)
+    assert np.array_equal(order, np.arange(len(order)))
+    got = {tuple(k): x for k, x in zip(key.tolist(), v)}
+    near = lambda x: abs(abs(x) - 1e-10) < 1e-13
+    assert all(near(ref[k]) for k in set(ref) - set(got))
+    assert all(near(got[k]) for k in set(got) - set(ref))
+    assert max(abs(got[k] - ref[k]) for k in got if k in ref) < 1e-10
+    den = eA[p - 1] + eB[r - 1] - eA[q - 1] - eB[s - 1]
+    assert abs(factor * float(np.sum(v ** 2 / den)) - e2) < 1e-10 * max(1.0, abs(e2))
