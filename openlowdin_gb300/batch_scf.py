@@ -20,9 +20,11 @@ block of its n x n slot (the library reads and writes it with row stride n),
 its padding has S = 1, X = 1 and H = PAD on the diagonal (so the padded
 orbitals sit far above every real one and are never occupied), and its own
 occupation count.  Host eigensolves run on the n_i x n_i block only.  A
-molecule that has converged is switched off in the library
-(LowdinGB300_batch_set_active) and skipped by the eigensolves, so it costs
-nothing while the rest of the batch iterates.
+molecule that has converged leaves the iteration: the library drops its tasks
+from the launches (LowdinGB300_batch_set_active), and its members leave the
+group tensors and the DIIS history (_compact) after their final density and
+Fock matrix are stored, so it costs nothing while the rest of the batch
+iterates.
 """
 from __future__ import annotations
 
