@@ -82,3 +82,12 @@ def test_mp2_entries_reproduce_golden_energy(oracle, golden):
     assert abs(e2 - oracle.rmp2(eri, C, eps, nocc)) < 1e-12
     g = golden["values"]["H2O.BOA.MP2.DIRECT"]["MP2 energy"]
     assert abs(res.energy + e2 - g[0]) <= g[1]
+
+
+def test_writer_reports_bad_arguments(built, tmp_path):
+    e = _entries(3)
+    with pytest.raises(lint.LowdinGB300Error):
+        lint.moint_write(str(tmp_path / "x.dat"), *e, stack_size=0)
+    with pytest.raises(lint.LowdinGB300Error):
+        lint.moint_write(str(tmp_path / "no_such_dir" / "x.dat"), *e, stack_size=7)
+    lint.lib().LowdinGB300_clear_error()
