@@ -1,6 +1,8 @@
-// Host side of liblowdin_gb300.so: the per-species handle behind the
-// LibintInterface_* C ABI, device data of a species (class-binned shell pairs
-// sorted by Schwarz factor), and the builds that queue the integral kernels.
+// Host side of liblowdin_gb300.so, part 1: error reporting, the Boys tables,
+// the host one-electron blocks, the coupling and first-quarter builds, the
+// LibintInterface_* C ABI with the device-resident entry points, and the
+// allocation-free two-particle build.  The per-species handle itself is in
+// lint_host.cuh, batched builds in batch.cu, MP2 in mp2.cu.
 #include "lint_host.cuh"
 
 namespace lgb {
