@@ -268,15 +268,19 @@ int LowdinGB300_batch_add_system_ld(LowdinGB300_Batch *b, LibintInterface **spec
     set_error("batch_add_system: invalid arguments");
     return -1;
   }
-  const int sys = (int)b->sys_first.size();
-  const int first = (int)b->sp.size();
-  b->sys_first.push_back(first);
+  // every species is checked before the batch changes: a rejected system
+  // leaves no trace
   for (int k = 0; k < nspecies; ++k) {
     if (!check_handle(species[k], __func__)) return -1;
     if (ld && ld[k] < species[k]->nbasis) {
       set_error("batch_add_system: row stride %d below the species' %d functions", ld[k], species[k]->nbasis);
       return -1;
     }
+  }
+  const int sys = (int)b->sys_first.size();
+  const int first = (int)b->sp.size();
+  b->sys_first.push_back(first);
+  for (int k = 0; k < nspecies; ++k) {
     LowdinGB300_Batch::Spec x{species[k], charges[k], factors[k], two_body[k], dP[k], dG ? dG[k] : nullptr,
                               dJ[k], sys, ld ? ld[k] : species[k]->nbasis};
     b->sp.push_back(x);

@@ -69,3 +69,53 @@ def test_flop_model_is_additive():
     # more angular momentum, more work
     assert FL.quartet_flops(0, 0, 0, 0) < FL.quartet_flops(1, 0, 0, 0) < FL.quartet_flops(1, 1, 1, 1) \
         < FL.quartet_flops(2, 2, 2, 2)
+
+
+def test_chain_generator_properties():
+    """Batched-RHF workload generator: seeded, closed shell, atoms at least
+    2 bohr apart, 3-30 atoms (one H more or less for the electron count)."""
+    for seed in range(40):
+        m = S.chain_molecule(20_000 + seed)
+        m2 = S.chain_molecule(20_000 + seed)
+        assert m["point_positions"] == m2["point_positions"]
+        Z = m["point_charges"]
+        assert int(sum(Z)) % 2 == 0
+        assert 3 <= len(Z) <= 31
+        R = np.array(m["point_positions"])
+        d = np.linalg.norm(R[:, None] - R[None], axis=-1) + np.eye(len(R)) * 1e9
+        assert d.min() >= 2.0 - 1e-12
+        assert m["species"][0]["n_particles"] == int(sum(Z))
+
+
+def test_canonical_orthogonaliser_drops_dependent_functions():
+    from openlowdin_gb300.scf import _orthogonaliser_np
+    rng = np.random.default_rng(5)
+    A = rng.normal(size=(6, 6))
+    S_full = A @ A.T + 6 * np.eye(6)
+    X = _orthogonaliser_np(S_full)
+    assert np.allclose(X.T @ S_full @ X, np.eye(6), atol=1e-12)
+    B = rng.normal(size=(6, 4))
+    S_def = B @ B.T                              # rank 4
+    X = _orthogonaliser_np(S_def)
+    assert X.shape == (6, 4)
+    assert np.allclose(X.T @ S_def @ X, np.eye(4), atol=1e-10)
+
+
+def test_batch_arguments_checked_on_the_host():
+    """Row strides below a species' size and flag arrays of the wrong length
+    are rejected before any device work."""
+    from openlowdin_gb300 import build, lint
+    build.build()
+    sp = S.water()["species"][0]
+    h = lint.Libint2Interface(sp, 1)
+    b = lint.Batch()
+    with pytest.raises(lint.LowdinGB300Error):
+        b.add_system([h], [-1.0], [-0.5], [1], [1], [1], [1], ld=[h.nbasis - 1])
+    lint.lib().LowdinGB300_clear_error()
+    b.add_system([h], [-1.0], [-0.5], [1], [1], [1], [1], ld=[h.nbasis + 8])
+    with pytest.raises(ValueError):
+        b.set_active([1, 1])
+    with pytest.raises(lint.LowdinGB300Error):
+        b.set_active([1])                        # not finalised yet
+    b.close()
+    h.close()
