@@ -337,9 +337,10 @@ def mp2_section(args):
     M, N, K = 128, 1 << 17, 640
     peak = None
     try:
-        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"]
-    except Exception:
-        pass
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = json.load(f)["bf16_tflops"]
+    except (OSError, KeyError, ValueError):
+        peak = None   # no measured peak on this machine: the fraction is left out
     gemms = {}
     for name, mode, products in (("split2_3products", 2, 3), ("split3_6products", 3, 6),
                                  ("precise_8products", 8, 8)):
@@ -577,8 +578,9 @@ def main():
         prof = os.path.join(ROOT, "profiles", "roofline_traffic.json")
         if os.path.exists(prof):
             try:
-                traffic = json.load(open(prof)).get("bytes_per_build")
-            except Exception:
+                with open(prof) as f:
+                    traffic = json.load(f).get("bytes_per_build")
+            except (OSError, ValueError):
                 traffic = None
         out["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
                            "frac": achieved / peak64 if peak64 > 0 else None, "traffic": traffic,
