@@ -79,3 +79,14 @@ def mp2_energy(entries, eps, n_occ: int, n_frozen: int, n_basis: int) -> float:
     eo, ev = e[n_frozen:n_occ], e[n_occ:n_basis]
     D = eo[:, None, None, None] - ev[None, :, None, None] + eo[None, None, :, None] - ev[None, None, None, :]
     return float(np.sum(T * (2.0 * T - T.transpose(0, 3, 2, 1)) / D))
+
+
+def mp2_coupling_energy(entries, eps_a, eps_b, factor: float) -> float:
+    """Inter-species MP2 term from a two-species file (every (ia|jb) with i, a
+    of species a and j, b of species b; absent entries are zero):
+    factor * sum (ia|jb)^2 / (e_i + e_j - e_a - e_b), factor = (q_a q_b)^2
+    lambda_a lambda_b (MPFunctions.f90:682-886)."""
+    p, q, r, s, v = entries
+    ea, eb = np.asarray(eps_a, np.float64), np.asarray(eps_b, np.float64)
+    den = ea[p - 1] + eb[r - 1] - ea[q - 1] - eb[s - 1]
+    return float(factor * np.sum(v * v / den))

@@ -91,3 +91,30 @@ def test_writer_reports_bad_arguments(built, tmp_path):
     with pytest.raises(lint.LowdinGB300Error):
         lint.moint_write(str(tmp_path / "no_such_dir" / "x.dat"), *e, stack_size=7)
     lint.lib().LowdinGB300_clear_error()
+
+
+def test_two_species_entries_reproduce_coupling_mp2(oracle, golden, built, tmp_path):
+    """Inter-species (ia|jb) of the golden APMO water (electrons x first proton
+    species) from the oracle's restated first quarter, written through the
+    library's record writer and read back, give the oracle's inter-species
+    MP2 term."""
+    sysd = GS.h2o_apmo(golden)
+    sysO = oracle.from_plain(sysd)
+    res = oracle.scf(sysO)
+    A, B = sysO.species[0], sysO.species[1]
+    CA, CB = res.coefficients[0], res.coefficients[1]
+    oA, oB = A.n_occ, B.n_occ
+    P, Q, R, S_, V = [], [], [], [], []
+    for i in range(oA):
+        Ai = oracle.coupling_directIT(A.basis, 1, B.basis, 2, np.ascontiguousarray(CA.T), i)
+        Mi = np.einsum("nls,na,lj,sb->ajb", Ai, CA[:, oA:], CB[:, :oB], CB[:, oB:], optimize=True)
+        for a, j, b in zip(*np.nonzero(np.abs(Mi) > 1e-10)):
+            P.append(i + 1); Q.append(oA + a + 1); R.append(j + 1); S_.append(oB + b + 1); V.append(Mi[a, j, b])
+    path = str(tmp_path / "E-.H_1moint.dat")
+    lint.moint_write(path, P, Q, R, S_, V, stack_size=300)
+    ent = M.read_moint(path, 300)
+    factor = A.eta * B.eta * (A.charge * B.charge) ** 2
+    e = M.mp2_coupling_energy(ent, res.orbital_energies[0], res.orbital_energies[1], factor)
+    ref = A.eta * B.eta * oracle.mp2_coupling_direct(A.basis, 1, CA, res.orbital_energies[0], oA, 0, B.basis, 2, CB,
+                                                     res.orbital_energies[1], oB, 0, A.charge * B.charge)
+    assert abs(e - ref) < 1e-12 * max(1.0, abs(ref))
