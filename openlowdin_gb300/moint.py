@@ -7,10 +7,12 @@ in bytes (int32) before and after, holding four int32 index arrays p, q, r, s
 (CONTROL's INTEGRAL_STACK_SIZE, 30000 by default).  The last record marks the
 end with p = -1 after its last entry.
 
-For the MP2 transform the entries are (ia|jb) in the order p = i, q = a,
-r = j >= i, s = b (b >= a when j == i), |value| > 1e-10; the library writes
-them with LowdinGB300_mp2_moint, this module reads them back and evaluates
-the closed-shell MP2 energy from them as MPFunctions.f90:514-662 does.
+For the MP2 transform of one species the entries are (ia|jb) in the order
+p = i, q = a, r = j >= i, s = b (b >= a when j == i), |value| > 1e-10
+(LowdinGB300_mp2_moint); for a species pair every i, a of the first and j, b
+of the second species in that order (LowdinGB300_mp2_coupling_moint).  This
+module reads them back and evaluates the MP2 terms from them as
+MPFunctions.f90:514-662 (closed shell) and :682-886 (inter-species) do.
 """
 from __future__ import annotations
 
