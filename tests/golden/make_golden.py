@@ -12,7 +12,8 @@ It extracts, as data:
     0.52917724924 bohr from ``src/core/Units.f90:37``),
   * the golden values asserted by the checkers ``test/H2O.BOA.DIRECT.py``,
     ``test/H2O.BOA.MP2.DIRECT.py``, ``test/H2O.APMO.MP2.py``,
-    ``test/H2O.APMO.UHF.DIRECT.py``.
+    ``test/H2O.APMO.UHF.DIRECT.py``, ``test/H2O.APMO.UMP2.DIRECT.py`` (the
+    last two use the geometry of ``test/H2O.APMO.MP2.lowdin``).
 The GPU machine has no reference tree, so the tests read only the JSON written here.
 """
 import json
@@ -98,6 +99,7 @@ def main():
             "H2O.BOA.MP2.DIRECT": read_checker("H2O.BOA.MP2.DIRECT.py"),
             "H2O.APMO.MP2": read_checker("H2O.APMO.MP2.py"),
             "H2O.APMO.UHF.DIRECT": read_checker("H2O.APMO.UHF.DIRECT.py"),
+            "H2O.APMO.UMP2.DIRECT": read_checker("H2O.APMO.UMP2.DIRECT.py"),
         },
     }
     with open(OUT, "w") as f:

@@ -105,12 +105,17 @@ def test_direct_mp2_restatement(oracle, golden):
 
 def test_golden_apmo_mp2(oracle, golden):
     """test/H2O.APMO.MP2.py: APMO-MP2 total energy (electron intra-species term
-    + electron-proton and proton-proton inter-species terms)."""
+    + electron-proton and proton-proton inter-species terms); and
+    test/H2O.APMO.UMP2.DIRECT.py on the same molecule, whose UHF solution is
+    closed shell, so its UMP2 total is the same sum."""
     sysO = oracle.from_plain(GS.h2o_apmo(golden))
     res = oracle.scf(sysO)
     r = oracle.apmo_mp2(sysO, res)
-    ref = golden["values"]["H2O.APMO.MP2"]["MP2 energy"]
-    assert abs(r["total"] - ref[0]) <= ref[1]
+    for name in ("H2O.APMO.MP2", "H2O.APMO.UMP2.DIRECT"):
+        ref = golden["values"][name]["MP2 energy"]
+        assert abs(r["total"] - ref[0]) <= ref[1], name
+    ref = golden["values"]["H2O.APMO.UMP2.DIRECT"]["HF energy"]
+    assert abs(res.energy - ref[0]) <= ref[1]
 
 
 def test_golden_h2o_apmo(oracle, golden):
