@@ -219,8 +219,8 @@ int LowdinGB300_batch_coupling_quartets(LowdinGB300_Batch *b, long long *out, vo
 /* Allocation-free two-particle build (no counterpart in the reference).
    Same result as LowdinGB300_twobody_device, for callers that cannot allocate
    device memory once running: a host program whose device memory is owned by
-   its own pool, a serving loop that forbids allocations after warm-up, or code
-   queuing into a captured stream.  Work buffers live in one static device
+   its own pool, or a serving loop that forbids allocations after warm-up.
+   Work buffers live in one static device
    array (LowdinGB300_noalloc_scratch_bytes() bytes, ~9.5 MB, held by every GPU
    that loads the library until the process exits); species are limited to 512
    Cartesian functions and 512 shells, larger ones are rejected with an error.

@@ -565,13 +565,12 @@ bool tensor_map(CUtensorMap *m, const void *base, long long rows, int Kp, int bo
 template <int NP>
 cudaError_t launch_gemm_np(const TmapSet &maps, const GemmArgs &g, unsigned nt, unsigned mt, unsigned batch,
                            cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    const cudaError_t e = cudaFuncSetAttribute(gemm_split_kernel<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               GemmCfg<NP>::kSmemBytes);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static PerDeviceLevel attr;
+  const cudaError_t e = attr.raise(1, [] {
+    return cudaFuncSetAttribute(gemm_split_kernel<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                GemmCfg<NP>::kSmemBytes);
+  });
+  if (e != cudaSuccess) return e;
   gemm_split_kernel<NP><<<dim3(nt, mt, batch), 128, GemmCfg<NP>::kSmemBytes, s>>>(maps, g);
   return cudaGetLastError();
 }
@@ -653,13 +652,11 @@ cudaError_t launch_gemm_precise(const Bf16Split &A, long long a_rows, const Bf16
   g.gcol_stride = out.gcol_stride;
   g.col0 = out.col0;
   g.err = derr;
-  static bool attr = false;
-  if (!attr) {
-    const cudaError_t e =
-        cudaFuncSetAttribute(gemm_precise_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static PerDeviceLevel attr;
+  const cudaError_t e = attr.raise(1, [] {
+    return cudaFuncSetAttribute(gemm_precise_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes);
+  });
+  if (e != cudaSuccess) return e;
   // persistent CTAs: one wave over the SMs (one CTA fits an SM), split over (M tiles x batches)
   long long per = (152LL + mt * batch - 1) / (mt * batch);
   const unsigned gx = (unsigned)std::max<long long>(1, std::min<long long>(nt, per));

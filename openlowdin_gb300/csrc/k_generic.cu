@@ -339,14 +339,15 @@ cudaError_t coop_attr(F *fn) {
 }
 
 bool coop_ready() {
-  static bool done = false;
-  if (done) return true;
-  if (coop_attr(jk_coop_kernel) != cudaSuccess || coop_attr(cp_coop_kernel) != cudaSuccess ||
-      coop_attr(it_coop_kernel) != cudaSuccess || coop_attr(mp2x_coop_kernel) != cudaSuccess ||
-      coop_attr(schwarz_coop_kernel) != cudaSuccess)
-    return false;
-  done = true;
-  return true;
+  static PerDeviceLevel done;
+  return done.raise(1, [] {
+           cudaError_t e = coop_attr(jk_coop_kernel);
+           if (e == cudaSuccess) e = coop_attr(cp_coop_kernel);
+           if (e == cudaSuccess) e = coop_attr(it_coop_kernel);
+           if (e == cudaSuccess) e = coop_attr(mp2x_coop_kernel);
+           if (e == cudaSuccess) e = coop_attr(schwarz_coop_kernel);
+           return e;
+         }) == cudaSuccess;
 }
 
 // launch shape of a cooperative kernel for class K: warps per CTA (each with

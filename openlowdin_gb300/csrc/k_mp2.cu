@@ -196,12 +196,12 @@ cudaError_t launch_mp2_unpack_csr(const float *Yp, long long ystride, const int 
                                   int Kp, int v, int np, __nv_bfloat16 *const *Z, cudaStream_t s) {
   if (Kp % 64 || v <= 0 || v > 65535 || np < 2 || np > kMaxPieces) return cudaErrorInvalidValue;
   const size_t smem = (size_t)kUnpackRows * Kp * sizeof(float);
-  static int attr_kp = 0;
-  if (smem > 48 * 1024 && Kp > attr_kp) {
-    const cudaError_t e =
-        cudaFuncSetAttribute(mp2_unpack_csr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static PerDeviceLevel attr;   // per device: the largest Kp set up so far
+  if (smem > 48 * 1024) {
+    const cudaError_t e = attr.raise(Kp, [smem] {
+      return cudaFuncSetAttribute(mp2_unpack_csr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    });
     if (e != cudaSuccess) return e;
-    attr_kp = Kp;
   }
   const dim3 grid((unsigned)((n + kUnpackRows - 1) / kUnpackRows), (unsigned)v);
   mp2_unpack_csr_kernel<<<grid, 256, smem, s>>>(Yp, ystride, rowptr, ent, n, Kp, np, Z[0], Z[1],

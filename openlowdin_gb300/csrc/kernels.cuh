@@ -9,9 +9,43 @@
 #pragma once
 #include <cuda_bf16.h>
 
+#include <mutex>
+#include <utility>
+#include <vector>
+
 #include "common.cuh"
 
 namespace lgb {
+
+// Per-device set-up (kernel attributes such as the dynamic shared-memory
+// limit are properties of a device): raise(level) runs f() on the current
+// device when that device has not yet been set up to at least `level`, under
+// a lock, so host threads calling the library at once and processes using
+// several devices are both served.
+class PerDeviceLevel {
+ public:
+  template <typename F>
+  cudaError_t raise(long long level, F &&f) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu_);
+    for (auto &d : done_)
+      if (d.first == dev) {
+        if (d.second >= level) return cudaSuccess;
+        e = f();
+        if (e == cudaSuccess) d.second = level;
+        return e;
+      }
+    e = f();
+    if (e == cudaSuccess) done_.push_back({dev, level});
+    return e;
+  }
+
+ private:
+  std::mutex mu_;
+  std::vector<std::pair<int, long long>> done_;
+};
 
 // pair class id of a canonical pair (la >= lb): (0,0)=0 (1,0)=1 (1,1)=2 (2,0)=3 (2,1)=4 (2,2)=5
 __host__ __device__ constexpr int pair_class(int la, int lb) { return la * (la + 1) / 2 + lb; }

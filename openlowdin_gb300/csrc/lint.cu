@@ -754,9 +754,8 @@ const char *LowdinGB300_version(void) { return "lowdin_gb300 0.1 (sm_103a, FP64/
 // ====================================================== allocation-free build
 // LowdinGB300_twobody_device_noalloc: the device two-particle build for
 // callers that must not allocate device memory once they are running -- a host
-// program that owns every device byte through its own pool, a serving loop that
-// forbids allocations after warm-up, or code queuing work into a captured
-// stream.  Its work buffers (scaled densities, shell-block norms, accumulators,
+// program that owns every device byte through its own pool, or a serving loop
+// that forbids allocations after warm-up.  Its work buffers (scaled densities, shell-block norms, accumulators,
 // task list, counters) live in one file-scope device array instead of
 // cudaMalloc'd memory; the handle's shell-pair data must already exist
 // (LibintInterface_init_2body_ints, which does allocate, is called at set-up).

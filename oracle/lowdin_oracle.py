@@ -40,6 +40,12 @@ _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 
 
+def reference_available() -> bool:
+    """Whether the openLOWDIN source tree the Makefile points at (environment
+    variable LOWDIN_REFERENCE, else the Makefile's default) is present."""
+    return subprocess.run(["make", "-s", "-C", _HERE, "have-reference"], capture_output=True).returncode == 0
+
+
 def build(ref: bool = False) -> None:
     """Compile liboracle.so (and the reference's Rys code when ``ref``)."""
     subprocess.check_call(["make", "-s", "-C", _HERE, "liboracle.so"])

@@ -1,8 +1,10 @@
 """Generate tests/golden/golden.json from an openLOWDIN source tree.
 
-Run once in a container that has the reference tree (default /root/reference):
+Run once in a container that has the reference tree:
 
     python tests/golden/make_golden.py [REFERENCE_ROOT]
+
+REFERENCE_ROOT defaults to $LOWDIN_REFERENCE, else /root/reference.
 
 It extracts, as data:
   * the basis-set entries the golden tests use from ``lib/basis`` (6-311G for
@@ -21,7 +23,7 @@ import os
 import re
 import sys
 
-ROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LOWDIN_REFERENCE", "/root/reference")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.json")
 BOHR = 0.52917724924  # src/core/Units.f90:37
 

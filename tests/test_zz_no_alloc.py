@@ -2,7 +2,7 @@
 
 Some callers cannot allocate device memory while they run (a host program that
 owns all device memory through its own pool, a serving loop that forbids
-allocations after warm-up, work queued into a captured stream).  For them
+allocations after warm-up).  For them
 LowdinGB300_twobody_device_noalloc keeps its work buffers in one static device
 array.  This file is collected last so that a failure here, in a run that stops
 at the first failure, comes after every other test has run.
