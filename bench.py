@@ -66,6 +66,9 @@ def parse():
                     help="with --profile-fock: FP32/FP64 split bound of the mixed build")
     ap.add_argument("--profile-random", type=int, default=0,
                     help="with --profile-fock: this many random chain molecules (batched-RHF generator)")
+    ap.add_argument("--profile-chain", type=int, default=0,
+                    help="with --profile-fock: one chain molecule of the serving generator with at least this "
+                         "many functions instead of the APMO batch")
     ap.add_argument("--profile-d-waters", type=int, default=0,
                     help="with --profile-fock: one cluster of this many waters with a d shell on O "
                          "instead of the APMO batch")
@@ -85,7 +88,9 @@ def profile_fock(args):
     torch.cuda.set_device(0)
     from openlowdin_gb300 import flops as FL
     from openlowdin_gb300 import systems as S
-    if args.profile_d_waters:
+    if args.profile_chain:
+        mols = [S.chain_for_basis(10_007, args.profile_chain)]
+    elif args.profile_d_waters:
         mols = [S.water_cluster(args.profile_d_waters, seed=0, o_d=True)]
     elif args.profile_random:
         mols = [S.chain_molecule(20_000 + i) for i in range(args.profile_random)]

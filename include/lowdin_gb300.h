@@ -193,8 +193,11 @@ int LowdinGB300_batch_add_system_ld(LowdinGB300_Batch *b, LibintInterface **spec
 int LowdinGB300_batch_finalize(LowdinGB300_Batch *b, void *stream);
 /* One flag per system (host array, in add order; copied on `stream`): the
    integral launches of a system whose flag is 0 return at once, leaving its
-   G and J unwritten (a converged molecule of the batch costs no quartets).
-   All systems are active after finalize. */
+   G and J unwritten (a converged molecule of the batch costs no quartets);
+   1 = built; 2 = built, and in mixed builds every quartet of the system is
+   evaluated in FP64 (a system whose mixed-precision solution failed its FP64
+   check continues in FP64 inside the same batch).  All systems are 1 after
+   finalize. */
 int LowdinGB300_batch_set_active(LowdinGB300_Batch *b, const int *flags, void *stream);
 /* precision bits: 1 = two-particle quartets whose Schwarz-density bound
    Q_ab Q_cd max|D block| is below `split` run in FP32 (the rest FP64); 2 = the
@@ -321,6 +324,15 @@ double LowdinGB300_gemm_bench(int M, int N, int K, int mode, int reps, void *str
    Queued on `stream`.  Returns 0, or -1 with the error set. */
 int LowdinGB300_one_body_device(LibintInterface *lint, int ncharge, const double *Z, const double *R, double *dS,
                                 double *dT, double *dV, void *stream);
+
+/* Pulay DIIS coefficients of nsys systems on the device (caller side of the
+   integral path; replaces the host solve of src/scf/Convergence.f90:543-633).
+   dE: [nsys][h][h] error products <e_i, e_j> (device, FP64), 1 <= h <= 20;
+   dcoef: [nsys][h] coefficients c minimising |sum_i c_i e_i| under
+   sum_i c_i = 1 (pseudo-inverse of the bordered Pulay matrix, eigenvalues
+   below 1e-12 of the largest dropped).  Queued on `stream`; returns 0, or -1
+   with the error set. */
+int LowdinGB300_diis_coefficients(const double *dE, int h, int nsys, double *dcoef, void *stream);
 
 /* Number of CUDA kernels this library has launched in the process. */
 long long LowdinGB300_launch_count(void);

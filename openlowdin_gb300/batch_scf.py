@@ -503,18 +503,14 @@ class BatchSCF:
                 row[:, j].index_add_(0, g.sys_index, d)
         st.hist_B.append(row)
         if h >= 2:
-            B = torch.zeros((self.nsys, h + 1, h + 1), dtype=torch.float64, device=self.dev)
+            # error products of every system, solved on the device
+            # (LowdinGB300_diis_coefficients): no host round trip
+            E = torch.empty((self.nsys, h, h), dtype=torch.float64, device=self.dev)
             for i in range(h):
-                B[:, i, :i + 1] = st.hist_B[i][:, :i + 1]
-                B[:, :i + 1, i] = st.hist_B[i][:, :i + 1]
-            B[:, h, :h] = -1.0
-            B[:, :h, h] = -1.0
-            # scale for conditioning, then solve every system at once
-            scale = torch.clamp(B[:, h - 1, h - 1].abs(), min=1e-300)
-            B[:, :h, :h] /= scale[:, None, None]
-            rhs = torch.zeros((self.nsys, h + 1, 1), dtype=torch.float64, device=self.dev)
-            rhs[:, h, 0] = -1.0
-            coef = torch.linalg.lstsq(B.cpu(), rhs.cpu()).solution[:, :h, 0].to(self.dev)
+                E[:, i, :i + 1] = st.hist_B[i][:, :i + 1]
+                E[:, :i + 1, i] = st.hist_B[i][:, :i + 1]
+            coef = torch.empty((self.nsys, h), dtype=torch.float64, device=self.dev)
+            lint.diis_coefficients(E.data_ptr(), h, self.nsys, coef.data_ptr(), st.stream)
         else:
             coef = None
         self._tick(st, "diis")

@@ -17,6 +17,11 @@ constexpr JKFn jk_entry() {
   if constexpr (templated_class<B, K>() && B >= K) return &jk_tasks_kernel<R, pc_la(B), pc_lb(B), pc_la(K), pc_lb(K)>;
   else return nullptr;
 }
+template <int B, int K>
+constexpr JKFn jkr_entry() {
+  if constexpr (templated_class<B, K>() && B >= K) return &jk32_row_kernel<pc_la(B), pc_lb(B), pc_la(K), pc_lb(K)>;
+  else return nullptr;
+}
 template <typename R, int B, int K>
 constexpr CPFn cp_entry() {
   if constexpr (templated_class<B, K>()) return &cp_tasks_kernel<R, pc_la(B), pc_lb(B), pc_la(K), pc_lb(K)>;
@@ -40,8 +45,10 @@ constexpr MXFn mx_entry() {
 #define LGB_JK_TABLES(B)                                   \
   extern const JKFn kJK64_##B[6];                          \
   extern const JKFn kJK32_##B[6];                          \
+  extern const JKFn kJKR_##B[6];                           \
   const JKFn kJK64_##B[6] = LGB_ROW6(jk_entry, double, B); \
-  const JKFn kJK32_##B[6] = LGB_ROW6(jk_entry, float, B);
+  const JKFn kJK32_##B[6] = LGB_ROW6(jk_entry, float, B);  \
+  const JKFn kJKR_##B[6] = LGB_ROW6(jkr_entry, B);
 
 #define LGB_CP_TABLES(B)                                   \
   extern const CPFn kCP64_##B[6];                          \

@@ -59,6 +59,12 @@ __device__ __forceinline__ double dnorm6(const double *__restrict__ Dn, int nsh,
   return __longlong_as_double((long long)m);
 }
 
+// Per-system build flag of a batch (LowdinGB300_batch_set_active): off
+// (converged, nothing built), on, or held in FP64 (mixed builds evaluate all
+// of the system's quartets in their FP64 launches).  Tasks without a flag are on.
+constexpr int kSysOff = 0, kSysOn = 1, kSysFP64 = 2;
+__device__ __forceinline__ int system_flag(const int *f) { return f ? __ldg(f) : kSysOn; }
+
 // task owning flattened block b: last task with blk0 <= b (tasks sorted by blk0)
 template <typename T>
 __device__ __forceinline__ int find_task(const T *__restrict__ tasks, int ntasks, int b) {
@@ -110,7 +116,9 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
   constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND;
   const int t = find_task(tasks, TL.ntasks, blockIdx.x);
   const JKTask &T = tasks[t];
-  if (T.active && __ldg(T.active) == 0) return;   // converged system: nothing to build
+  const int act = system_flag(T.active);
+  if (act == kSysOff) return;   // converged system: nothing to build
+  if (act == kSysFP64 && TL.mixed && TL.lower) return;   // system held in FP64: the FP64 launch takes it all
   const int local = blockIdx.x - T.blk0;
   const int tx = local % T.nbx, ty = local / T.nbx;
   if (T.triangle && tx * 32 > ty * kWarpsPerBlock + kWarpsPerBlock - 1) return;
@@ -163,7 +171,7 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
       b *= dnorm6(T.Dn32, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
       if (b < fmaxf(TL.eps32, TL.skip)) active = false;
     }
-    if (TL.lower ? !(b < TL.split32) : (b < TL.split32)) active = false;
+    if (act != kSysFP64 && (TL.lower ? !(b < TL.split32) : (b < TL.split32))) active = false;
   } else if (T.screen) {
     const double b = T.pairs[bi].Q * (F64 ? (double)ket.Q : T.pairs[ki].Q) *
                      dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
@@ -268,6 +276,190 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
     }
 }
 
+// ------------------------------------------------------- J/K, FP32 bra rows --
+// FP32 half of a mixed J/K build, one block per bra pair (a b| of a task; its
+// kRowWarps warps take the task's ket pairs 32 at a time).  The exchange
+// updates of a quartet touch only rows fa.. and fb.. of the output (K13, K14
+// on the rows of shell a, K23, K24 on those of shell b) and read only those
+// rows of D, so the block keeps both -- D rows and exchange accumulators,
+// NA + NB rows of n columns -- and the two shell-block-norm rows of shells a
+// and b in shared memory: per quartet the four exchange reads and updates and
+// four of the six screening norms are shared-memory accesses instead of
+// scattered global ones.  The bra Coulomb block (J12) is summed in registers
+// over every ket of the warp before one warp reduction; the ket Coulomb block
+// (J34) and the ket block of D stay global.  At the end the accumulated
+// exchange rows go to the global accumulator (non-zero entries only).
+// Quartet selection, bound and arithmetic are those of jk_tasks_kernel's FP32
+// launch (same FP32 bound, same screening and split), so the quartets taken
+// and the integrals are the same; only the order of the FP32 additions differs.
+template <typename T>
+__device__ __forceinline__ int find_task_rows(const T *__restrict__ tasks, int ntasks, int b) {
+  int lo = 0, hi = ntasks - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&tasks[mid].rblk0) <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <int LA, int LB, int LC, int LD>
+__global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *__restrict__ tasks, TaskLaunch TL) {
+  using Q = QClass<LA, LB, LC, LD>;
+  constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND, NR = NA + NB;
+  extern __shared__ float rsm[];
+  const int t = find_task_rows(tasks, TL.ntasks, blockIdx.x);
+  const JKTask &T = tasks[t];
+  if (system_flag(T.active) != kSysOn) return;   // converged, or held in FP64
+  const int bpos = blockIdx.x - T.rblk0;
+  if (bpos >= T.nbra) return;
+  const int bi = T.bra0 + bpos;
+  const int nk = T.triangle ? bpos + 1 : T.nket;  // ket positions [0, nk)
+  const int n = T.n, nsh = T.nsh;
+  const PairRec32 bra = T.pairs32[bi];
+  const PrimRec32 *__restrict__ prims = T.prims32;
+  float *Drow = rsm;              // [NR][n]: rows fa+a (a < NA), then fb+b
+  float *Krow = rsm + NR * n;     // [NR][n]: exchange accumulators of the same rows
+  float *Dnr = Krow + NR * n;     // [2][nsh]: shell-block norms of shells sa and sb
+  for (int i = threadIdx.x; i < NR * n; i += blockDim.x) {
+    const int r = i / n, c = i - r * n;
+    const int f = r < NA ? bra.fa + r : bra.fb + (r - NA);
+    Drow[i] = __ldg(T.Ds32 + (size_t)f * n + c);
+    Krow[i] = 0.f;
+  }
+  if (T.screen)
+    for (int i = threadIdx.x; i < 2 * nsh; i += blockDim.x)
+      Dnr[i] = __ldg(T.Dn32 + (size_t)(i < nsh ? bra.sa : bra.sb) * nsh + (i < nsh ? i : i - nsh));
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float hf = T.hf32;
+  const float *__restrict__ D = T.Ds32;
+  float *G32 = T.Gacc32;
+  const float cutoff = fmaxf(TL.eps32, TL.skip);
+  float j12[NA * NB];
+#pragma unroll
+  for (int x = 0; x < NA * NB; ++x) j12[x] = 0.f;
+  const float dn_ab = T.screen ? Dnr[bra.sb] : 0.f;
+  unsigned cnt = 0;
+  for (int k0 = warp * 32; k0 < nk; k0 += 32 * kRowWarps) {
+    const int kpos = k0 + lane;
+    bool active = kpos < nk;
+    const int ki = T.ket0 + min(kpos, nk - 1);
+    const PairRec32 ket = T.pairs32[ki];
+    float bound = bra.Q * ket.Q;
+    if (T.screen) {
+      float m = dn_ab;
+      m = fmaxf(m, Dnr[ket.sa]);
+      m = fmaxf(m, Dnr[nsh + ket.sa]);
+      m = fmaxf(m, Dnr[ket.sb]);
+      m = fmaxf(m, Dnr[nsh + ket.sb]);
+      m = fmaxf(m, __ldg(T.Dn32 + (size_t)ket.sa * nsh + ket.sb));
+      bound *= m;
+      if (bound < cutoff) active = false;
+    }
+    if (!(bound < TL.split32)) active = false;   // the FP64 launch takes these
+    const unsigned live = __ballot_sync(0xffffffffu, active);
+    if (!live) continue;
+    cnt += __popc(live);
+    float I[Q::NINT];
+    if (active) {
+      eri_quartet<float, LA, LB, LC, LD>(bra, prims + bra.prim0, ket, prims + ket.prim0, TL.boys.f64, TL.boys.f32,
+                                         I);
+    } else {
+#pragma unroll
+      for (int x = 0; x < Q::NINT; ++x) I[x] = 0.f;
+    }
+    const float deg = active ? pow2<float>((bra.sa != bra.sb) + (ket.sa != ket.sb) + (bi != ki)) : 0.f;
+    const float hdeg = deg * hf;
+    const int fc = ket.fa, fd = ket.fb;
+    auto Iat = [&](int a, int b, int c, int d) -> float { return I[((a * NB + b) * NC + c) * ND + d]; };
+    // J12 (bra block): D of the ket block, summed over this warp's kets
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+      for (int d = 0; d < ND; ++d) {
+        const float dcd = active ? __ldg(D + (size_t)(fc + c) * n + fd + d) * deg : 0.f;
+#pragma unroll
+        for (int a = 0; a < NA; ++a)
+#pragma unroll
+          for (int b = 0; b < NB; ++b) j12[a * NB + b] = fmaf(dcd, Iat(a, b, c, d), j12[a * NB + b]);
+      }
+    if (!active) continue;
+    // J34 (ket block)
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+      for (int d = 0; d < ND; ++d) {
+        float s = 0.f;
+#pragma unroll
+        for (int a = 0; a < NA; ++a)
+#pragma unroll
+          for (int b = 0; b < NB; ++b) s = fmaf(Drow[a * n + bra.fb + b], Iat(a, b, c, d), s);
+        atomicAdd(G32 + (size_t)(fc + c) * n + fd + d, s * deg);
+      }
+    // K13 (a,c) += D(b,d), K14 (a,d) += D(b,c): rows of shell a
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        float s = 0.f;
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
+#pragma unroll
+          for (int d = 0; d < ND; ++d) s = fmaf(Drow[(NA + b) * n + fd + d], Iat(a, b, c, d), s);
+        atomicAdd(Krow + a * n + fc + c, s * hdeg);
+      }
+#pragma unroll
+      for (int d = 0; d < ND; ++d) {
+        float s = 0.f;
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
+#pragma unroll
+          for (int c = 0; c < NC; ++c) s = fmaf(Drow[(NA + b) * n + fc + c], Iat(a, b, c, d), s);
+        atomicAdd(Krow + a * n + fd + d, s * hdeg);
+      }
+    }
+    // K24 (b,d) += D(a,c), K23 (b,c) += D(a,d): rows of shell b
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+#pragma unroll
+      for (int d = 0; d < ND; ++d) {
+        float s = 0.f;
+#pragma unroll
+        for (int a = 0; a < NA; ++a)
+#pragma unroll
+          for (int c = 0; c < NC; ++c) s = fmaf(Drow[a * n + fc + c], Iat(a, b, c, d), s);
+        atomicAdd(Krow + (NA + b) * n + fd + d, s * hdeg);
+      }
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        float s = 0.f;
+#pragma unroll
+        for (int a = 0; a < NA; ++a)
+#pragma unroll
+          for (int d = 0; d < ND; ++d) s = fmaf(Drow[a * n + fd + d], Iat(a, b, c, d), s);
+        atomicAdd(Krow + (NA + b) * n + fc + c, s * hdeg);
+      }
+    }
+  }
+  if (T.count && lane == 0 && cnt) atomicAdd(T.count, (unsigned long long)cnt);
+  // J12: one reduction per warp
+#pragma unroll
+  for (int x = 0; x < NA * NB; ++x) {
+    const float v = warp_sum(j12[x]);
+    if (lane == 0 && v != 0.f) atomicAdd(G32 + (size_t)(bra.fa + x / NB) * n + bra.fb + x % NB, v);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < NR * n; i += blockDim.x) {
+    const float v = Krow[i];
+    if (v != 0.f) {
+      const int r = i / n, c = i - r * n;
+      const int f = r < NA ? bra.fa + r : bra.fb + (r - NA);
+      atomicAdd(G32 + (size_t)f * n + c, v);
+    }
+  }
+}
+
 // ---------------------------------------------------------------- coupling --
 // Bra pairs of species A (every unordered shell pair), ket pairs of species B.
 // J_A[i][j] += scale sum_{kl} D_B[k][l] (ij|kl), J_B[k][l] += scale
@@ -280,7 +472,9 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
   constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND;
   const int t = find_task(tasks, TL.ntasks, blockIdx.x);
   const CPTask &T = tasks[t];
-  if (T.active && __ldg(T.active) == 0) return;   // converged system: nothing to build
+  const int act = system_flag(T.active);
+  if (act == kSysOff) return;   // converged system: nothing to build
+  if (act == kSysFP64 && TL.mixed && TL.lower) return;   // system held in FP64: the FP64 launch takes it all
   const int local = blockIdx.x - T.blk0;
   const int tx = local % T.nbx, ty = local / T.nbx;
   const int kpos = tx * 32 + threadIdx.x;
@@ -306,7 +500,7 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
     if (T.DnA32) dm = __ldg(T.DnA32 + b32.sa * T.nshA + b32.sb);
     if (T.DnB32) dm = fmaxf(dm, __ldg(T.DnB32 + k32.sa * T.nshB + k32.sb));
     const float b = b32.Q * k32.Q * dm;
-    if (TL.lower ? !(b < TL.split32) : (b < TL.split32)) active = false;
+    if (act != kSysFP64 && (TL.lower ? !(b < TL.split32) : (b < TL.split32))) active = false;
     if ((T.DnA32 || T.DnB32) && b < TL.skip) active = false;
   }
   if (__all_sync(0xffffffffu, !active)) return;

@@ -15,11 +15,13 @@
 #include "fock_kernels.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 
 namespace lgb {
 
 extern const JKFn kJK64_0[6], kJK64_1[6], kJK64_2[6], kJK64_3[6], kJK64_4[6], kJK64_5[6];
 extern const JKFn kJK32_0[6], kJK32_1[6], kJK32_2[6], kJK32_3[6], kJK32_4[6], kJK32_5[6];
+extern const JKFn kJKR_0[6], kJKR_1[6], kJKR_2[6], kJKR_3[6], kJKR_4[6], kJKR_5[6];
 extern const CPFn kCP64_0[6], kCP64_1[6], kCP64_2[6], kCP64_3[6], kCP64_4[6], kCP64_5[6];
 extern const CPFn kCP32_0[6], kCP32_1[6], kCP32_2[6], kCP32_3[6], kCP32_4[6], kCP32_5[6];
 extern const ITFn kIT_0[6], kIT_1[6], kIT_2[6], kIT_3[6], kIT_4[6], kIT_5[6];
@@ -29,12 +31,19 @@ namespace {
 
 const JKFn *const kJK64[6] = {kJK64_0, kJK64_1, kJK64_2, kJK64_3, kJK64_4, kJK64_5};
 const JKFn *const kJK32[6] = {kJK32_0, kJK32_1, kJK32_2, kJK32_3, kJK32_4, kJK32_5};
+const JKFn *const kJKR[6] = {kJKR_0, kJKR_1, kJKR_2, kJKR_3, kJKR_4, kJKR_5};
 const CPFn *const kCP64[6] = {kCP64_0, kCP64_1, kCP64_2, kCP64_3, kCP64_4, kCP64_5};
 const CPFn *const kCP32[6] = {kCP32_0, kCP32_1, kCP32_2, kCP32_3, kCP32_4, kCP32_5};
 const ITFn *const kIT[6] = {kIT_0, kIT_1, kIT_2, kIT_3, kIT_4, kIT_5};
 const MXFn *const kMX[6] = {kMX_0, kMX_1, kMX_2, kMX_3, kMX_4, kMX_5};
 
 const dim3 kBlock(32, kWarpsPerBlock);
+// LOWDIN_GB300_ROWS=0 keeps the FP32 half of mixed builds on jk_tasks_kernel
+// (read at every launch, so a process can compare both kernels)
+bool row_rows_off() {
+  const char *e = std::getenv("LOWDIN_GB300_ROWS");
+  return e && e[0] == '0';
+}
 constexpr int kCoUnitsPerTile = kWarpsPerBlock * 4;   // (bra row, group of 8 kets)
 constexpr int kCoMaxSmem = 200 * 1024;                 // dynamic shared memory of a cooperative CTA
 
@@ -74,7 +83,8 @@ __global__ void __launch_bounds__(128) jk_coop_kernel(const JKTask *__restrict__
   for (long long u = w0; u < (long long)TL.nblocks * kCoUnitsPerTile; u += wstep) {
     int bpos, kpos0;
     const JKTask &T = coop_unit(tasks, TL.ntasks, (int)u, &bpos, &kpos0);
-    if (bpos >= T.nbra || (T.active && __ldg(T.active) == 0)) continue;
+    const int act = system_flag(T.active);
+    if (bpos >= T.nbra || act == kSysOff || (act == kSysFP64 && TL.mixed && TL.lower)) continue;
     for (int kpos = kpos0; kpos < kpos0 + 8 && kpos < T.nket; ++kpos) {
       if (T.triangle && kpos > bpos) break;
       const int bi = T.bra0 + bpos, ki = T.ket0 + kpos;
@@ -87,7 +97,7 @@ __global__ void __launch_bounds__(128) jk_coop_kernel(const JKTask *__restrict__
           b *= dnorm6(T.Dn32, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
           if (b < fmaxf(TL.eps32, TL.skip)) active = false;
         }
-        if (TL.lower ? !(b < TL.split32) : (b < TL.split32)) active = false;
+        if (act != kSysFP64 && (TL.lower ? !(b < TL.split32) : (b < TL.split32))) active = false;
       } else if (T.screen) {
         if (abs_below(bra.Q * ket.Q * dnorm6(T.Dn, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb), TL.eps)) active = false;
       }
@@ -162,7 +172,8 @@ __global__ void __launch_bounds__(128) cp_coop_kernel(const CPTask *__restrict__
   for (long long u = w0; u < (long long)TL.nblocks * kCoUnitsPerTile; u += wstep) {
     int bpos, kpos0;
     const CPTask &T = coop_unit(tasks, TL.ntasks, (int)u, &bpos, &kpos0);
-    if (bpos >= T.nbra || (T.active && __ldg(T.active) == 0)) continue;
+    const int act = system_flag(T.active);
+    if (bpos >= T.nbra || act == kSysOff || (act == kSysFP64 && TL.mixed && TL.lower)) continue;
     for (int kpos = kpos0; kpos < kpos0 + 8 && kpos < T.nket; ++kpos) {
       const int bi = T.bra0 + bpos, ki = T.ket0 + kpos;
       const bool tiny = TL.mixed ? T.pa32[bi].Q * T.pb32[ki].Q * 0.999f < TL.cut32
@@ -175,7 +186,7 @@ __global__ void __launch_bounds__(128) cp_coop_kernel(const CPTask *__restrict__
         if (T.DnA32) dm = __ldg(T.DnA32 + b32.sa * T.nshA + b32.sb);
         if (T.DnB32) dm = fmaxf(dm, __ldg(T.DnB32 + k32.sa * T.nshB + k32.sb));
         const float b = b32.Q * k32.Q * dm;
-        if (TL.lower ? !(b < TL.split32) : (b < TL.split32)) continue;
+        if (act != kSysFP64 && (TL.lower ? !(b < TL.split32) : (b < TL.split32))) continue;
         if ((T.DnA32 || T.DnB32) && b < TL.skip) continue;
       }
       if (T.count && lane == 0) atomicAdd(T.count, 1ull);
@@ -370,10 +381,31 @@ bool class_supported(int pcb, int pck) {
   return pcb >= 0 && pck >= 0 && pcb < kNumPairClasses && pck < kNumPairClasses;
 }
 
+bool jk_rows_used(int pcb, int pck, int n, int nsh) {
+  if (!class_supported(pcb, pck) || !kJKR[pcb][pck]) return false;
+  if (row_rows_off()) return false;
+  return row_smem_bytes(ncart(pc_la(pcb)) + ncart(pc_lb(pcb)), n, nsh) <= (size_t)kRowMaxSmem;
+}
+
 cudaError_t launch_jk_tasks(int pcb, int pck, bool fp32, const JKTask *dtasks, const TaskLaunch &tl,
                             cudaStream_t s) {
   if (!class_supported(pcb, pck)) return cudaErrorNotSupported;
   if (tl.ntasks <= 0 || tl.nblocks <= 0) return cudaSuccess;
+  if (fp32 && tl.mixed && tl.lower && jk_rows_used(pcb, pck, tl.rows_n, tl.rows_nsh)) {
+    // the FP32 half of a mixed build: bra-row kernel
+    const JKFn r = kJKR[pcb][pck];
+    const size_t smem = row_smem_bytes(ncart(pc_la(pcb)) + ncart(pc_lb(pcb)), tl.rows_n, tl.rows_nsh);
+    static PerDeviceLevel attr[kNumPairClasses][kNumPairClasses];
+    if (smem > 48 * 1024) {
+      const cudaError_t e = attr[pcb][pck].raise((long long)smem, [r, smem] {
+        return cudaFuncSetAttribute(r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      });
+      if (e != cudaSuccess) return e;
+    }
+    if (tl.nrblocks > 0) r<<<tl.nrblocks, 32 * kRowWarps, smem, s>>>(dtasks, tl);
+    count_launches(1);
+    return cudaGetLastError();
+  }
   const JKFn f = fp32 ? kJK32[pcb][pck] : kJK64[pcb][pck];
   if (f) {
     f<<<tl.nblocks, kBlock, 0, s>>>(dtasks, tl);

@@ -1,0 +1,106 @@
+// Device-side pieces of the SCF driver (caller side of the integral path).
+//
+// Pulay DIIS coefficients (openLOWDIN src/scf/Convergence.f90:543-633): for
+// each system the error-product matrix E[i][j] = <e_i, e_j> of its last h
+// error vectors gives the bordered system
+//     [ E   -1 ] [c]   [ 0]
+//     [-1^T  0 ] [l] = [-1],
+// solved here by a pseudo-inverse.  The reference takes an SVD of the bordered
+// matrix and inverts the singular values above 1e-4; this kernel scales E by
+// its last diagonal element (conditioning), diagonalises the symmetric
+// bordered matrix by cyclic Jacobi rotations in FP64 (one thread per system;
+// h <= 20) and inverts the eigenvalues above 1e-12 of the largest in
+// magnitude, the rest are dropped -- the least-squares solution of the
+// extrapolation the host drivers computed with LAPACK, without a host round
+// trip.
+#include "lint_host.cuh"
+
+namespace lgb {
+namespace {
+
+constexpr int kDiisMax = 20;   // history length limit (h)
+
+__global__ void diis_solve_kernel(const double *__restrict__ E, int h, int nsys, double *__restrict__ coef,
+                                  int *__restrict__ status) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  constexpr int M = kDiisMax + 1;
+  double A[M][M], V[M][M];
+  const int m = h + 1;
+  const double *e = E + (size_t)s * h * h;
+  const double sc = fabs(e[(h - 1) * h + h - 1]) > 1e-300 ? 1.0 / fabs(e[(h - 1) * h + h - 1]) : 1.0;
+  for (int i = 0; i < m; ++i)
+    for (int j = 0; j < m; ++j) {
+      double v;
+      if (i < h && j < h) v = 0.5 * (e[i * h + j] + e[j * h + i]) * sc;
+      else if (i == h && j == h) v = 0.0;
+      else v = -1.0;
+      A[i][j] = v;
+      V[i][j] = i == j ? 1.0 : 0.0;
+    }
+  // cyclic Jacobi: rotate away every off-diagonal element, sweep until the
+  // off-diagonal norm is at FP64 rounding of the diagonal
+  int sweep = 0;
+  for (; sweep < 60; ++sweep) {
+    double off = 0.0, dia = 0.0;
+    for (int i = 0; i < m; ++i) {
+      dia += A[i][i] * A[i][i];
+      for (int j = i + 1; j < m; ++j) off += A[i][j] * A[i][j];
+    }
+    if (off <= 1e-30 * dia || off == 0.0) break;
+    for (int p = 0; p < m - 1; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        const double apq = A[p][q];
+        if (apq == 0.0) continue;
+        // tan of the rotation angle from cot(2 theta) = (a_qq - a_pp) / (2 a_pq)
+        const double th = (A[q][q] - A[p][p]) / (2.0 * apq);
+        const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < m; ++k) {
+          const double akp = A[k][p], akq = A[k][q];
+          A[k][p] = c * akp - sn * akq;
+          A[k][q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < m; ++k) {
+          const double apk = A[p][k], aqk = A[q][k];
+          A[p][k] = c * apk - sn * aqk;
+          A[q][k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < m; ++k) {
+          const double vkp = V[k][p], vkq = V[k][q];
+          V[k][p] = c * vkp - sn * vkq;
+          V[k][q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+  double amax = 0.0;
+  for (int i = 0; i < m; ++i) amax = fmax(amax, fabs(A[i][i]));
+  // x = V diag(1/lambda) V^T r with r = (0, ..., 0, -1)
+  for (int i = 0; i < h; ++i) {
+    double x = 0.0;
+    for (int k = 0; k < m; ++k) {
+      const double lam = A[k][k];
+      if (fabs(lam) > 1e-12 * amax) x += V[i][k] * (-V[h][k]) / lam;
+    }
+    coef[(size_t)s * h + i] = x;
+  }
+  if (status) status[s] = sweep;
+}
+
+}  // namespace
+}  // namespace lgb
+
+extern "C" int LowdinGB300_diis_coefficients(const double *dE, int h, int nsys, double *dcoef, void *stream) {
+  if (h < 1 || h > lgb::kDiisMax || nsys < 0 || (nsys > 0 && (!dE || !dcoef))) {
+    lgb::set_error("diis_coefficients: history length %d outside 1..%d or null arrays", h, lgb::kDiisMax);
+    return -1;
+  }
+  if (nsys == 0) return 0;
+  lgb::diis_solve_kernel<<<(nsys + 31) / 32, 32, 0, (cudaStream_t)stream>>>(dE, h, nsys, dcoef, nullptr);
+  lgb::count_launches(1);
+  if (cudaGetLastError() != cudaSuccess) {
+    lgb::set_error("diis_coefficients: launch failed");
+    return -1;
+  }
+  return 0;
+}

@@ -85,6 +85,7 @@ struct JKTask {
   int screen;             // Schwarz x density screening (electrons only)
   int blk0;               // first flattened block of the task
   int nbx;                // blocks along the ket axis
+  int rblk0;              // first block of the task in a bra-row launch (one block per bra pair)
 };
 
 // One coupling task: quartets (A pair | B pair) of two species; accumulates
@@ -121,6 +122,8 @@ struct CPTask {
 struct TaskLaunch {
   int ntasks;
   int nblocks;            // total flattened blocks
+  int nrblocks;           // bra-row launches: total bra pairs of the tasks
+  int rows_n, rows_nsh;   // bra-row launches: largest basis and shell count of the tasks
   double eps;             // screening threshold
   double split;           // mixed precision: quartets with bound >= split run in FP64
   int lower;              // 1: this launch takes the quartets below split
@@ -143,6 +146,13 @@ inline void set_fp32_copies(TaskLaunch &tl) {
 // null entries are served by the block-cooperative kernels (classes of total
 // angular momentum above kTemplatedMaxL).
 using JKFn = void (*)(const JKTask *, TaskLaunch);
+// FP32 J/K kernels that keep the bra pair's rows of D and of the exchange
+// output in shared memory (jk32_row_kernel), one block per bra pair
+constexpr int kRowWarps = 4;
+constexpr int kRowMaxSmem = 200 * 1024;
+__host__ __device__ constexpr size_t row_smem_bytes(int nrows, int n, int nsh) {
+  return (size_t)(2 * nrows * n + 2 * nsh) * sizeof(float);
+}
 using CPFn = void (*)(const CPTask *, TaskLaunch);
 struct ITParams;
 using ITFn = void (*)(ITParams);
@@ -216,6 +226,9 @@ inline int task_nby(int nbra) { return (nbra + kWarpsPerBlock - 1) / kWarpsPerBl
 // launchers (every class with l <= kMaxL)
 cudaError_t launch_jk_tasks(int pcb, int pck, bool fp32, const JKTask *dtasks, const TaskLaunch &tl,
                             cudaStream_t s);
+// whether the FP32 launch of class (pcb, pck) over species of up to n
+// functions / nsh shells runs on the bra-row kernel
+bool jk_rows_used(int pcb, int pck, int n, int nsh);
 cudaError_t launch_cp_tasks(int pcb, int pck, bool fp32, const CPTask *dtasks, const TaskLaunch &tl,
                             cudaStream_t s);
 cudaError_t launch_it(int pcb, int pck, const ITParams &p, cudaStream_t s);

@@ -843,9 +843,7 @@ int LowdinGB300_twobody_device_noalloc(LibintInterface *lint, const double *dD, 
     ts.cnt[c] = (int)ts.group[c].size();
     int b = 0;
     for (JKTask t : ts.group[c]) {
-      t.nbx = task_nbx(t.nket);
-      t.blk0 = b;
-      b += t.nbx * task_nby(t.nbra);
+      ts.place(c, t, b);
       flat.push_back(t);
     }
     ts.nblk[c] = b;

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include <cublas_v2.h>
@@ -151,6 +152,19 @@ struct TaskSet {
   T *d = nullptr;
   size_t cap = 0;
   int off[kNQC] = {0}, cnt[kNQC] = {0}, nblk[kNQC] = {0};
+  int nrblk[kNQC] = {0}, rn[kNQC] = {0}, rnsh[kNQC] = {0};   // bra-row launches (J/K tasks)
+  // block offsets of task t of group c (b: blocks so far in the group)
+  void place(int c, T &t, int &b) {
+    t.nbx = task_nbx(t.nket);
+    t.blk0 = b;
+    b += t.nbx * task_nby(t.nbra);
+    if constexpr (std::is_same<T, JKTask>::value) {
+      t.rblk0 = nrblk[c];
+      nrblk[c] += t.nbra;
+      rn[c] = std::max(rn[c], t.n);
+      rnsh[c] = std::max(rnsh[c], t.nsh);
+    }
+  }
   void clear() {
     for (auto &g : group) g.clear();
   }
@@ -163,11 +177,10 @@ struct TaskSet {
     for (int c = 0; c < kNQC; ++c) {
       off[c] = (int)flat.size();
       int b = 0;
+      nrblk[c] = rn[c] = rnsh[c] = 0;
       for (T t : group[c]) {
         if (on && t.active && !(*on)[t.active - flag_base]) continue;
-        t.nbx = task_nbx(t.nket);
-        t.blk0 = b;
-        b += t.nbx * task_nby(t.nbra);
+        place(c, t, b);
         flat.push_back(t);
       }
       cnt[c] = (int)flat.size() - off[c];
@@ -527,6 +540,9 @@ struct LibintInterface {
       TaskLaunch tl{};
       tl.ntasks = ts.cnt[c];
       tl.nblocks = ts.nblk[c];
+      tl.nrblocks = ts.nrblk[c];
+      tl.rows_n = ts.rn[c];
+      tl.rows_nsh = ts.rnsh[c];
       tl.eps = DBL_EPSILON;
       tl.cut = 1e-10;
       tl.skip = (float)skip;

@@ -98,6 +98,8 @@ def lib():
                                                ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                                ctypes.c_double, ctypes.POINTER(ctypes.c_double), _vp]
         L.LowdinGB300_mp2_coupling.restype = ctypes.c_int
+        L.LowdinGB300_diis_coefficients.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp]
+        L.LowdinGB300_diis_coefficients.restype = ctypes.c_int
         L.LowdinGB300_gemm_bf16_split.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                   ctypes.c_int, _vp]
         L.LowdinGB300_gemm_bf16_split.restype = ctypes.c_int
@@ -156,7 +158,15 @@ EXPORTED_SYMBOLS = [
     "LowdinGB300_twobody_device_noalloc", "LowdinGB300_mp2_direct", "LowdinGB300_mp2_last_columns", "LowdinGB300_mp2_coupling",
     "LowdinGB300_gemm_bf16_split", "LowdinGB300_gemm_bf16_precise",
     "LowdinGB300_gemm_bench", "LowdinGB300_mp2_moint", "LowdinGB300_mp2_coupling_moint", "LowdinGB300_moint_write",
+    "LowdinGB300_diis_coefficients",
 ]
+
+
+def diis_coefficients(e_ptr: int, h: int, nsys: int, coef_ptr: int, stream: int = 0):
+    """DIIS coefficients of nsys systems from their [h][h] error products
+    (device FP64 arrays), queued on `stream`."""
+    if lib().LowdinGB300_diis_coefficients(e_ptr, h, nsys, coef_ptr, stream) != 0:
+        _check()
 
 
 def moint_write(path: str, p, q, r, s, v, stack_size: int = 30000):

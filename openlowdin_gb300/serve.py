@@ -56,6 +56,10 @@ class Result:
     admitted: float
     finished: float
     nbasis: int
+    # mixed precision: |E_mixed - E_FP64| at the converged density (the FP64
+    # check's rebuild), and whether the check sent the job on in FP64
+    err_vs_fp64: float | None = None
+    guard_hit: bool = False
 
     @property
     def latency(self) -> float:
@@ -94,6 +98,15 @@ class _Job:
     hist_F: list = field(default_factory=list)
     hist_E: list = field(default_factory=list)
     hist_B: list = field(default_factory=list)
+    # FP64 check of a mixed-precision solution (ServingEngine.guard): flag is
+    # the job's batch flag (1 mixed, 2 every quartet in FP64), verify marks the
+    # iteration that rebuilds its matrices in FP64 at the converged density
+    flag: int = 1
+    verify: bool = False
+    e_mixed: float = float("nan")
+    err_vs_fp64: float | None = None
+    commutator: float | None = None
+    guard_hit: bool = False
 
 
 def footprint_bytes(sysd, kind: str, diis_size: int = 10, mp2_budget_gb: float = 8.0) -> float:
@@ -120,7 +133,13 @@ def footprint_bytes(sysd, kind: str, diis_size: int = 10, mp2_budget_gb: float =
 class ServingEngine:
     def __init__(self, device="cuda", precision="fp64", split=1e-5, hbm_budget_gb=150.0, max_active=256,
                  diis_size=10, tol_energy=1e-8, tol_density=1e-6, max_iter=100, mp2_precision=None,
-                 mp2_budget_gb=8.0, skip=None):
+                 mp2_budget_gb=8.0, skip=None, guard=True, guard_energy=1e-6, guard_commutator=1e-4):
+        """guard (mixed precision): when a job converges, its matrices are
+        rebuilt once in FP64 at the converged density; the FP64 energy is the
+        job's result and |E_mixed - E_FP64| its stated error.  If that error
+        exceeds guard_energy, or the largest element of the FP64 commutator
+        X^T (FPS - SPF) X exceeds guard_commutator, the job continues in FP64
+        (every quartet in the FP64 launches, full builds) until it converges."""
         import torch
         self.torch = torch
         self.dev = torch.device(device)
@@ -135,6 +154,9 @@ class ServingEngine:
         self.max_iter = max_iter
         self.mp2_precision = (2 if precision == "mixed" else 0) if mp2_precision is None else mp2_precision
         self.mp2_budget_gb = mp2_budget_gb
+        self.guard = guard and precision == "mixed"
+        self.guard_energy = guard_energy
+        self.guard_commutator = guard_commutator
         self.stream = torch.cuda.current_stream(self.dev)
         self.mp2_stream = torch.cuda.Stream(self.dev)
         self._pool = None
@@ -235,7 +257,15 @@ class ServingEngine:
                          [s.Pin for s in job.sp], [s.Gb for s in job.sp], [s.Jb for s in job.sp])
         b.finalize(self.stream.cuda_stream)
         b.set_skip(self.skip)
+        b.flags = [1] * len(jobs)
         return b
+
+    def _apply_flags(self, jobs, batch):
+        """Batch flags of the jobs (2: every quartet of the job in FP64)."""
+        flags = [job.flag for job in jobs]
+        if flags != batch.flags:
+            batch.set_active(flags, self.stream.cuda_stream)
+            batch.flags = flags
 
     # --------------------------------------------------------- SCF step --
     def _iterate(self, jobs, batch):
@@ -248,20 +278,23 @@ class ServingEngine:
         left running on the host pool."""
         torch = self.torch
         mixed = self.precision == "mixed"
-        for job in jobs:
-            full = (not mixed) or job.it == 0
+        # full builds: plain mode, a job's first iteration, and jobs in FP64
+        # (the guard's check and what follows a failed check)
+        fulls = [(not mixed) or job.it == 0 or job.flag == 2 for job in jobs]
+        for job, full in zip(jobs, fulls):
             for s in job.sp:
                 if full:
                     s.Pin.copy_(s.P)
                 else:
                     torch.sub(s.P, s.Pref, out=s.Pin)
+        if mixed:
+            self._apply_flags(jobs, batch)
         self._tick("other")
         batch.fock(3 if mixed else 0, self.split, self.stream.cuda_stream)
         self._tick("fock")
         stats = []
         dmats = []
-        for job in jobs:
-            full = (not mixed) or job.it == 0
+        for job, full in zip(jobs, fulls):
             Fs, Es = [], []
             energy = torch.tensor(job.enuc, dtype=torch.float64, device=self.dev)
             for s in job.sp:
@@ -287,29 +320,35 @@ class ServingEngine:
             h = len(job.hist_F)
             row = torch.stack([sum(torch.sum(e * f) for e, f in zip(Es, job.hist_E[j])) for j in range(h)])
             job.hist_B.append(row)
-            stats.append(energy)
+            if job.verify:
+                comm = torch.stack([e.abs().max() for e in Es]).max()
+                stats.append(torch.stack([energy, comm]))
+            else:
+                stats.append(torch.stack([energy, torch.zeros_like(energy)]))
         self._tick("assemble")
-        # DIIS coefficients of all jobs: their error-product rows in one
-        # transfer, the small Pulay systems solved on the host
-        flat = torch.cat([torch.cat(job.hist_B) for job in jobs]).cpu().numpy()
-        o = 0
-        coefs = []
-        for job in jobs:
-            h = len(job.hist_F)
-            B = np.zeros((h + 1, h + 1))
-            for i in range(h):
-                B[i, :i + 1] = flat[o:o + i + 1]
-                B[:i + 1, i] = flat[o:o + i + 1]
-                o += len(job.hist_B[i])
-            B[:h, :h] /= max(abs(B[h - 1, h - 1]), 1e-300)
-            B[h, :h] = B[:h, h] = -1.0
-            rhs = np.zeros(h + 1)
-            rhs[h] = -1.0
-            coefs.append(np.linalg.lstsq(B, rhs, rcond=None)[0][:h] if h >= 2 else None)
+        # DIIS coefficients of all jobs on the device (LowdinGB300_diis_coefficients,
+        # one launch per history length): no host round trip
+        byh = {}
+        for q, job in enumerate(jobs):
+            byh.setdefault(len(job.hist_F), []).append(q)
+        coefs = [None] * len(jobs)
+        for h, qs in byh.items():
+            if h < 2:
+                continue
+            E = torch.empty((len(qs), h, h), dtype=torch.float64, device=self.dev)
+            for r, q in enumerate(qs):
+                hb = jobs[q].hist_B
+                for i in range(h):
+                    E[r, i, :i + 1] = hb[i][:i + 1]
+                    E[r, :i + 1, i] = hb[i][:i + 1]
+            c = torch.empty((len(qs), h), dtype=torch.float64, device=self.dev)
+            lint.diis_coefficients(E.data_ptr(), h, len(qs), c.data_ptr(), self.stream.cuda_stream)
+            for r, q in enumerate(qs):
+                coefs[q] = c[r]
         for job, c in zip(jobs, coefs):
             h = len(job.hist_F)
             for k, s in enumerate(job.sp):
-                Fx = job.hist_F[-1][k] if c is None else sum(float(c[j]) * job.hist_F[j][k] for j in range(h))
+                Fx = job.hist_F[-1][k] if c is None else sum(c[j] * job.hist_F[j][k] for j in range(h))
                 dmats.append((s, Fx))
         self._tick("diis")
         return jobs, stats, self._density_submit(dmats)
@@ -332,7 +371,8 @@ class ServingEngine:
                 s.Flast = job.hist_F[-1][job.sp.index(s)]
                 s.P.copy_(Pn)
             dP.append(d)
-        vals = torch.stack([torch.stack(stats), torch.stack(dP)]).cpu().numpy()
+        st = torch.stack(stats)
+        vals = torch.stack([st[:, 0], torch.stack(dP), st[:, 1]]).cpu().numpy()
         self._tick("convergence")
         done = []
         for q, job in enumerate(jobs):
@@ -341,6 +381,26 @@ class ServingEngine:
             conv = abs(e - job.e_old) < self.tol_energy and d < self.tol_density
             job.e_old = e
             job.energy = e
+            if job.verify:
+                # the FP64 check: this iteration's matrices were rebuilt in FP64
+                # at the density the mixed iterations converged to
+                job.verify = False
+                job.err_vs_fp64 = abs(e - job.e_mixed)
+                job.commutator = float(vals[2, q])
+                if job.err_vs_fp64 <= self.guard_energy and job.commutator <= self.guard_commutator:
+                    job.converged = True
+                    done.append(job)
+                    continue
+                job.guard_hit = True      # continue in FP64 (flag stays 2)
+                job.e_old = float("nan")
+                continue
+            if conv and self.guard and job.flag == 1 and job.it < self.max_iter:
+                job.verify = True         # next iteration: FP64 rebuild at this density
+                job.flag = 2
+                job.e_mixed = e
+                continue
+            if conv and job.guard_hit:
+                job.err_vs_fp64 = 0.0     # finished in FP64 after a failed check
             job.converged = conv
             if conv or job.it >= self.max_iter:
                 done.append(job)
@@ -377,7 +437,7 @@ class ServingEngine:
         for h in job.handles:
             h.close()
         return Result(job.req.rid, job.req.kind, job.energy, e2, job.it, bool(getattr(job, "converged", False)),
-                      job.req.arrival, job.admitted, now, job.sp[0].n)
+                      job.req.arrival, job.admitted, now, job.sp[0].n, job.err_vs_fp64, job.guard_hit)
 
     # -------------------------------------------------------------- loop --
     def run(self, requests, realtime=True, on_iteration=None):

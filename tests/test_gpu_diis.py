@@ -1,0 +1,51 @@
+"""Device DIIS coefficients (LowdinGB300_diis_coefficients) against the
+least-squares solution of the bordered Pulay system on the host
+(src/scf/Convergence.f90:543-633 solves the same system through an SVD)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _host(E):
+    h = E.shape[0]
+    B = np.zeros((h + 1, h + 1))
+    B[:h, :h] = E / abs(E[h - 1, h - 1])
+    B[h, :h] = B[:h, h] = -1.0
+    rhs = np.zeros(h + 1)
+    rhs[h] = -1.0
+    return np.linalg.lstsq(B, rhs, rcond=None)[0][:h]
+
+
+@pytest.mark.parametrize("h", [2, 3, 7, 10, 20])
+def test_diis_coefficients_match_host_least_squares(h):
+    torch = pytest.importorskip("torch")
+    from openlowdin_gb300 import build, lint
+    build.build()
+    rng = np.random.default_rng(h)
+    nsys = 37
+    Es = []
+    for s in range(nsys):
+        # error vectors shrinking like an SCF history (condition grows with h)
+        V = rng.normal(size=(h, 200)) * (0.3 ** np.arange(h))[:, None]
+        Es.append(V @ V.T)
+    E = np.stack(Es)
+    dE = torch.tensor(E, device="cuda")
+    dc = torch.empty((nsys, h), dtype=torch.float64, device="cuda")
+    lint.diis_coefficients(dE.data_ptr(), h, nsys, dc.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    c = dc.cpu().numpy()
+    for s in range(nsys):
+        ref = _host(E[s])
+        assert abs(c[s].sum() - 1.0) < 1e-10
+        # the extrapolated error |sum c_i e_i|^2 = c^T E c is what DIIS minimises
+        assert c[s] @ E[s] @ c[s] <= ref @ E[s] @ ref * (1 + 1e-8) + 1e-300
+        assert np.max(np.abs(c[s] - ref)) < 1e-6 * max(1.0, np.max(np.abs(ref)))
+
+
+def test_diis_rejects_long_histories():
+    torch = pytest.importorskip("torch")
+    from openlowdin_gb300 import lint
+    dE = torch.zeros((1, 21, 21), dtype=torch.float64, device="cuda")
+    dc = torch.zeros((1, 21), dtype=torch.float64, device="cuda")
+    with pytest.raises(lint.LowdinGB300Error):
+        lint.diis_coefficients(dE.data_ptr(), 21, 1, dc.data_ptr())

@@ -62,3 +62,28 @@ def test_admission_respects_budget(serve):
     res = eng.run(reqs, realtime=False, on_iteration=seen.append)
     assert len(res) == 4 and all(r.converged for r in res)
     assert max(seen) == 1
+
+
+def test_mixed_jobs_state_their_fp64_error(serve):
+    """Every mixed job ends with an FP64 rebuild at its converged density:
+    its energy is the FP64 energy there and |E_mixed - E_FP64| is reported,
+    within the 1e-6 Eh bar; the plain run of the same job agrees to 1e-6."""
+    reqs = [serve.Request(S.chain_for_basis(400 + i, nbf), "scf", 0.0, i) for i, nbf in enumerate((60, 110))]
+    plain = {r.rid: r for r in serve.ServingEngine(precision="fp64").run(reqs, realtime=False)}
+    mixed = serve.ServingEngine(precision="mixed").run(reqs, realtime=False)
+    for r in mixed:
+        assert r.converged and not r.guard_hit
+        assert r.err_vs_fp64 is not None and r.err_vs_fp64 <= 1e-6
+        assert abs(r.energy - plain[r.rid].energy) < 1e-6
+
+
+def test_guard_sends_a_failed_job_on_in_fp64(serve):
+    """With every quartet forced into FP32 (split far above every bound) the
+    mixed solution misses the FP64 one by more than 1e-6 Eh: the check fires,
+    the job continues in FP64 and ends on the plain result."""
+    req = serve.Request(S.chain_for_basis(421, 90), "scf", 0.0, 0)
+    plain = serve.ServingEngine(precision="fp64").run([req], realtime=False)[0]
+    forced = serve.ServingEngine(precision="mixed", split=1e30).run([req], realtime=False)[0]
+    assert forced.converged and forced.guard_hit
+    assert forced.err_vs_fp64 == 0.0
+    assert abs(forced.energy - plain.energy) < 1e-8
