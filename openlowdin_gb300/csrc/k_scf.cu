@@ -6,13 +6,14 @@
 //     [ E   -1 ] [c]   [ 0]
 //     [-1^T  0 ] [l] = [-1],
 // solved here by a pseudo-inverse.  The reference takes an SVD of the bordered
-// matrix and inverts the singular values above 1e-4; this kernel scales E by
-// its last diagonal element (conditioning), diagonalises the symmetric
-// bordered matrix by cyclic Jacobi rotations in FP64 (one thread per system;
-// h <= 20) and inverts the eigenvalues above 1e-12 of the largest in
-// magnitude, the rest are dropped -- the least-squares solution of the
-// extrapolation the host drivers computed with LAPACK, without a host round
-// trip.
+// matrix and inverts the singular values above 1e-4.  An SCF history has
+// errors over many orders of magnitude, so this kernel first scales E to unit
+// diagonal (E' = D^-1 E D^-1, D = diag(sqrt(E_ii)), c = D^-1 c') with the
+// border w_i = 1/sqrt(E_ii) brought to at most 1 in magnitude, diagonalises
+// the symmetric bordered matrix by cyclic Jacobi rotations in FP64 (one
+// thread per system, h <= 20) and inverts the eigenvalues above 1e-12 of the
+// largest in magnitude (the rest are dropped): the minimum-norm least-squares
+// solution of the extrapolation, with no host round trip.
 #include "lint_host.cuh"
 
 namespace lgb {
@@ -28,13 +29,20 @@ __global__ void diis_solve_kernel(const double *__restrict__ E, int h, int nsys,
   double A[M][M], V[M][M];
   const int m = h + 1;
   const double *e = E + (size_t)s * h * h;
-  const double sc = fabs(e[(h - 1) * h + h - 1]) > 1e-300 ? 1.0 / fabs(e[(h - 1) * h + h - 1]) : 1.0;
+  // unit-diagonal scaling: dinv[i] = 1/sqrt(E_ii) (a zero error keeps a
+  // floor), border -alpha dinv[i] with alpha = 1 / max dinv
+  double dinv[kDiisMax], wmax = 0.0;
+  for (int i = 0; i < h; ++i) {
+    dinv[i] = 1.0 / sqrt(fmax(e[i * h + i], 1e-300));
+    wmax = fmax(wmax, dinv[i]);
+  }
+  const double alpha = 1.0 / wmax;
   for (int i = 0; i < m; ++i)
     for (int j = 0; j < m; ++j) {
       double v;
-      if (i < h && j < h) v = 0.5 * (e[i * h + j] + e[j * h + i]) * sc;
+      if (i < h && j < h) v = 0.5 * (e[i * h + j] + e[j * h + i]) * dinv[i] * dinv[j];
       else if (i == h && j == h) v = 0.0;
-      else v = -1.0;
+      else v = -alpha * dinv[i < h ? i : j];
       A[i][j] = v;
       V[i][j] = i == j ? 1.0 : 0.0;
     }
@@ -75,14 +83,14 @@ __global__ void diis_solve_kernel(const double *__restrict__ E, int h, int nsys,
   }
   double amax = 0.0;
   for (int i = 0; i < m; ++i) amax = fmax(amax, fabs(A[i][i]));
-  // x = V diag(1/lambda) V^T r with r = (0, ..., 0, -1)
+  // c' = V diag(1/lambda) V^T r with r = (0, ..., 0, -alpha); c = D^-1 c'
   for (int i = 0; i < h; ++i) {
     double x = 0.0;
     for (int k = 0; k < m; ++k) {
       const double lam = A[k][k];
-      if (fabs(lam) > 1e-12 * amax) x += V[i][k] * (-V[h][k]) / lam;
+      if (fabs(lam) > 1e-12 * amax) x += V[i][k] * (-alpha * V[h][k]) / lam;
     }
-    coef[(size_t)s * h + i] = x;
+    coef[(size_t)s * h + i] = x * dinv[i];
   }
   if (status) status[s] = sweep;
 }

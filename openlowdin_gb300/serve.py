@@ -391,8 +391,11 @@ class ServingEngine:
                     job.converged = True
                     done.append(job)
                     continue
-                job.guard_hit = True      # continue in FP64 (flag stays 2)
+                # continue in FP64 (flag stays 2): full FP64 builds and a
+                # fresh DIIS history (the mixed-precision Fock matrices leave it)
+                job.guard_hit = True
                 job.e_old = float("nan")
+                job.hist_F, job.hist_E, job.hist_B = [], [], []
                 continue
             if conv and self.guard and job.flag == 1 and job.it < self.max_iter:
                 job.verify = True         # next iteration: FP64 rebuild at this density

@@ -26,16 +26,23 @@ def L():
     return lint
 
 
-def _call_noalloc(L, h, D, G, factor, stream):
-    return L.lib().LowdinGB300_twobody_device_noalloc(h.h, D.data_ptr(), G.data_ptr(), float(factor), 0, 0.0,
-                                                      stream)
+def _call_noalloc(L, h, D, G, factor, stream, precision=0, split=0.0):
+    return L.lib().LowdinGB300_twobody_device_noalloc(h.h, D.data_ptr(), G.data_ptr(), float(factor), precision,
+                                                      float(split), stream)
 
 
+def _system(which):
+    return S.water() if which == "water" else S.water_cluster(4, seed=0, quantum_protons=True)
+
+
+# precision 1 splits at 1e-5: the FP32 work arrays of the scratch array are in
+# use; it is compared with the allocating entry point's mixed build, whose
+# FP32 additions may run in another order (1e-7 of the largest element)
+@pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("which", ["water", "apmo_electrons"])
-def test_noalloc_matches_allocating_entry_point_twice(L, which):
+def test_noalloc_matches_allocating_entry_point_twice(L, which, precision):
     torch = pytest.importorskip("torch")
-    sysd = S.water() if which == "water" else S.water_cluster(4, seed=0, quantum_protons=True)
-    sp = sysd["species"][0]
+    sp = _system(which)["species"][0]
     h = L.Libint2Interface(sp, 1)
     h.init_2body_ints()
     n = h.nbasis
@@ -43,16 +50,45 @@ def test_noalloc_matches_allocating_entry_point_twice(L, which):
     st = torch.cuda.current_stream().cuda_stream
     X = rng.normal(size=(n, n)) * 0.1
     D = torch.tensor(X + X.T, device="cuda")
+    split = 1e-5 if precision else 0.0
     Gref = torch.empty_like(D)
-    h.twobody_device(D.data_ptr(), Gref.data_ptr(), -0.5, 0, 0.0, st)
+    h.twobody_device(D.data_ptr(), Gref.data_ptr(), -0.5, precision, split, st)
     torch.cuda.synchronize()
+    tol = TOL if precision == 0 else 1e-7 * max(1.0, float(Gref.abs().max()))
     for call in range(2):
         G = torch.full_like(D, float("nan"))
-        assert _call_noalloc(L, h, D, G, -0.5, st) == 0, L.last_error()
+        assert _call_noalloc(L, h, D, G, -0.5, st, precision, split) == 0, L.last_error()
         torch.cuda.synchronize()
         err = float((G - Gref).abs().max())
-        assert err < TOL, (call, err)
+        assert err < tol, (call, err)
     h.close()
+
+
+def test_noalloc_alternating_species_share_the_array(L):
+    """Two species of different sizes take turns in the shared array on one
+    stream: what one call leaves behind must not leak into the next."""
+    torch = pytest.importorskip("torch")
+    st = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(32)
+    cases = []
+    for which in ("apmo_electrons", "water"):
+        h = L.Libint2Interface(_system(which)["species"][0], 1)
+        h.init_2body_ints()
+        n = h.nbasis
+        X = rng.normal(size=(n, n)) * 0.1
+        D = torch.tensor(X + X.T, device="cuda")
+        Gref = torch.empty_like(D)
+        h.twobody_device(D.data_ptr(), Gref.data_ptr(), -0.5, 0, 0.0, st)
+        cases.append((h, D, Gref))
+    torch.cuda.synchronize()
+    for rnd in range(2):
+        for h, D, Gref in cases:
+            G = torch.full_like(D, float("nan"))
+            assert _call_noalloc(L, h, D, G, -0.5, st) == 0, L.last_error()
+            torch.cuda.synchronize()
+            assert float((G - Gref).abs().max()) < TOL, rnd
+    for h, _, _ in cases:
+        h.close()
 
 
 def test_noalloc_rejects_species_above_the_limit(L):
