@@ -328,11 +328,20 @@ int LowdinGB300_one_body_device(LibintInterface *lint, int ncharge, const double
 /* Pulay DIIS coefficients of nsys systems on the device (caller side of the
    integral path; replaces the host solve of src/scf/Convergence.f90:543-633).
    dE: [nsys][h][h] error products <e_i, e_j> (device, FP64), 1 <= h <= 20;
-   dcoef: [nsys][h] coefficients c minimising |sum_i c_i e_i| under
-   sum_i c_i = 1 (pseudo-inverse of the bordered Pulay matrix, eigenvalues
-   below 1e-12 of the largest dropped).  Queued on `stream`; returns 0, or -1
-   with the error set. */
-int LowdinGB300_diis_coefficients(const double *dE, int h, int nsys, double *dcoef, void *stream);
+   dfirst: per system the first history entry to use (device ints, entries
+   before it get coefficient 0), or NULL for all; dcoef: [nsys][h]
+   coefficients c minimising |sum_i c_i e_i| under sum_i c_i = 1
+   (pseudo-inverse of the bordered Pulay matrix scaled to unit diagonal,
+   eigenvalues below 1e-12 of the largest dropped).  Queued on `stream`;
+   returns 0, or -1 with the error set. */
+int LowdinGB300_diis_coefficients(const double *dE, int h, int nsys, const int *dfirst, double *dcoef,
+                                  void *stream);
+
+/* The device Boys functions F_0..F_L(T) (L <= 4) at the n host arguments T,
+   into host out[n][L+1]: fp32 = 1 the arithmetic FP32 form of the FP32
+   kernels, 0 the tabulated FP64 form (a check of the integral kernels'
+   building block; no counterpart in the reference).  Returns 0 or -1. */
+int LowdinGB300_boys_eval(int fp32, int L, const double *T, int n, double *out);
 
 /* Number of CUDA kernels this library has launched in the process. */
 long long LowdinGB300_launch_count(void);

@@ -98,14 +98,22 @@ class BatchSCF:
     """SCF of many independent systems at once on one GPU."""
 
     def __init__(self, systems, device="cuda", precision="fp64", split=1e-5, diis_size=10, rebuild_every=1000,
-                 bucket="auto", skip=MIXED_SKIP):
+                 bucket="auto", skip=MIXED_SKIP, guard=True, guard_energy=1e-6, guard_commutator=1e-4):
         """bucket: False = one group per exact (n, occ, eta); True = padded
         size buckets (bucket_size) with per-member sizes and occupations;
         "auto" = exact groups when they are at most EXACT_GROUPS_MAX.
         skip (mixed only): quartets whose density-weighted bound (from the
-        density change of an incremental build) is below skip are dropped."""
+        density change of an incremental build) is below skip are dropped.
+        guard (mixed only): a system that converges is rebuilt once in FP64
+        at its converged density; that FP64 energy is its result and
+        |E_mixed - E_FP64| its stated error (SCFResult.err_vs_fp64).  Above
+        guard_energy, or with an FP64 commutator element above
+        guard_commutator, the system continues in FP64 until it converges."""
         import torch
         self.torch = torch
+        self.guard = guard and precision == "mixed"
+        self.guard_energy = guard_energy
+        self.guard_commutator = guard_commutator
         self.rebuild_every = rebuild_every
         self.trace = None
         self.dev = torch.device(device)
@@ -417,6 +425,16 @@ class BatchSCF:
         st.final_e = np.zeros(self.nsys)
         st.conv = np.zeros(self.nsys, bool)
         st.iters = np.zeros(self.nsys, int)
+        # FP64 check of mixed solutions: fp64[s] = the system's quartets all in
+        # FP64 (batch flag 2) and full builds; verify[s] = this iteration is
+        # the check; diis_first[s] = first DIIS entry used (set past the
+        # mixed entries when a check fails)
+        st.fp64 = np.zeros(self.nsys, bool)
+        st.verify = np.zeros(self.nsys, bool)
+        st.e_mixed = np.full(self.nsys, np.nan)
+        st.err_fp64 = np.full(self.nsys, np.nan)
+        st.guard_hit = np.zeros(self.nsys, bool)
+        st.diis_first = np.zeros(self.nsys, np.int32)
         self.batch.set_active(np.ones(self.nsys, np.int32), st.stream)
         st.it = 0
         st.done = False
@@ -448,10 +466,20 @@ class BatchSCF:
         # |dP| bound is below the split run in FP32, the rest in FP64, and
         # incremental couplings run in FP32 (their size scales with |dP|).
         full = (not mixed) or (it - 1) % self.rebuild_every == 0
-        for g in groups:
+        # systems in FP64 (an FP64 check, or after a failed one): full builds
+        fmask = {}
+        if not full and st.fp64.any():
+            for gi, g in enumerate(groups):
+                if g.members:
+                    m = st.fp64[g.sys_np]
+                    if m.any():
+                        fmask[gi] = torch.from_numpy(m).to(self.dev)[:, None, None]
+        for gi, g in enumerate(groups):
             if not g.members:
                 continue
             src = g.P if full else g.P - g.Pref
+            if gi in fmask:
+                src = torch.where(fmask[gi], g.P, src)
             if g.compact:
                 g.Pin.index_copy_(0, g.alive, src)
             else:
@@ -459,7 +487,7 @@ class BatchSCF:
         # precision bits: 1 = two-particle FP32/FP64 split, 2 = coupling split
         self.batch.fock(3 if mixed else 0, self.split, st.stream)
         self._tick(st, "fock")
-        for g in groups:
+        for gi, g in enumerate(groups):
             if not g.members:
                 continue
             Gb = g.Gb.index_select(0, g.alive) if g.compact else g.Gb
@@ -467,11 +495,15 @@ class BatchSCF:
             if full:
                 g.G.copy_(Gb)
                 g.J.copy_(Jb)
+            elif gi in fmask:
+                g.G.copy_(torch.where(fmask[gi], Gb, g.G + Gb))
+                g.J.copy_(torch.where(fmask[gi], Jb, g.J + Jb))
             else:
                 g.G += Gb
                 g.J += Jb
             g.Pref.copy_(g.P)
         energy = self.enuc.clone()
+        comm = torch.zeros(self.nsys, dtype=torch.float64, device=self.dev)
         Fs, Es = [], []
         for g in groups:
             if not g.members:
@@ -483,6 +515,8 @@ class BatchSCF:
             energy.index_add_(0, g.sys_index, e_sp)
             FPS = F @ g.P @ g.S
             err = g.X.transpose(1, 2) @ (FPS - FPS.transpose(1, 2)) @ g.X
+            if st.verify.any():
+                comm.scatter_reduce_(0, g.sys_index, err.abs().amax(dim=(1, 2)), reduce="amax")
             Fs.append(F)
             Es.append(err)
         self._tick(st, "assemble")
@@ -492,6 +526,7 @@ class BatchSCF:
         if len(st.hist_F) > self.diis_size:
             st.hist_F.pop(0); st.hist_E.pop(0); st.hist_B.pop(0)
             st.hist_B = [b[:, 1:] for b in st.hist_B]
+            st.diis_first = np.maximum(st.diis_first - 1, 0).astype(np.int32)
         h = len(st.hist_F)
         row = torch.zeros((self.nsys, h), dtype=torch.float64, device=self.dev)
         for gi, g in enumerate(groups):
@@ -510,7 +545,9 @@ class BatchSCF:
                 E[:, i, :i + 1] = st.hist_B[i][:, :i + 1]
                 E[:, :i + 1, i] = st.hist_B[i][:, :i + 1]
             coef = torch.empty((self.nsys, h), dtype=torch.float64, device=self.dev)
-            lint.diis_coefficients(E.data_ptr(), h, self.nsys, coef.data_ptr(), st.stream)
+            first = torch.from_numpy(st.diis_first).to(self.dev) if st.diis_first.any() else None
+            lint.diis_coefficients(E.data_ptr(), h, self.nsys, coef.data_ptr(), st.stream,
+                                   first.data_ptr() if first is not None else 0)
         else:
             coef = None
         self._tick(st, "diis")
@@ -527,6 +564,7 @@ class BatchSCF:
             st.pending.append(self._density_submit(g, Fx))
         st.Fs = Fs
         st.energy = energy
+        st.comm = comm
 
     def _finish(self, st):
         """Collect the eigensolves started by _start: new densities and the
@@ -542,21 +580,44 @@ class BatchSCF:
             g.Flast = st.Fs[gi]
             g.P.copy_(Pn)
         self._tick(st, "density")
-        stats = torch.stack([st.energy, dP]).cpu().numpy()
+        stats = torch.stack([st.energy, dP, st.comm]).cpu().numpy()
         self._tick(st, "convergence")
-        en, dpn = stats[0], stats[1]
+        en, dpn, cmm = stats[0], stats[1], stats[2]
         active = ~st.conv
         st.final_e[active] = en[active]
         st.iters[active] = st.it
         newly = active & (np.abs(en - st.e_old) < st.tol_energy) & (dpn < st.tol_density)
         st.e_old[active] = en[active]
+        flags_changed = False
+        if self.guard:
+            # systems whose FP64 check ran in this iteration
+            chk = active & st.verify
+            st.verify[:] = False
+            if chk.any():
+                err = np.abs(en - st.e_mixed)
+                ok = chk & (err <= self.guard_energy) & (cmm <= self.guard_commutator)
+                bad = chk & ~ok
+                st.err_fp64[chk] = err[chk]
+                newly = (newly & ~chk) | ok
+                st.guard_hit |= bad
+                st.e_old[bad] = np.nan
+                st.diis_first[bad] = len(st.hist_F)      # entries from here on only
+            # newly converged mixed systems: FP64 check next iteration
+            start = newly & ~st.fp64
+            if start.any() and st.it < st.max_iter:
+                st.verify |= start
+                st.fp64 |= start
+                st.e_mixed[start] = en[start]
+                newly &= ~start
+                flags_changed = True
+            st.err_fp64[newly & st.guard_hit] = 0.0
         st.conv |= newly
         st.done = bool(st.conv.all()) or st.it >= st.max_iter
-        if newly.any() and not st.done:
+        if (newly.any() or flags_changed) and not st.done:
             # a converged system keeps its energy, density and Fock matrix from
             # here on: its integral work is switched off and its members leave
-            # the iteration's tensors
-            self.batch.set_active(~st.conv, st.stream)
+            # the iteration's tensors; systems in FP64 get flag 2
+            self.batch.set_active(np.where(st.conv, 0, np.where(st.fp64, 2, 1)).astype(np.int32), st.stream)
             for gi, g in enumerate(st.groups):
                 if g.members:
                     keep = ~st.conv[g.sys_np]
@@ -583,8 +644,12 @@ class BatchSCF:
                 eps.append(g.eps[slot, :k].cpu().numpy())
                 C.append(g.C[slot, :k, :k].cpu().numpy())
                 P.append(g.Pfinal[slot, :k, :k].cpu().numpy())
-            out.append(SCFResult(float(st.final_e[si]), int(st.iters[si]), bool(st.conv[si]),
-                                 time.perf_counter() - st.t0, eps, C, P, quartets))
+            r = SCFResult(float(st.final_e[si]), int(st.iters[si]), bool(st.conv[si]),
+                          time.perf_counter() - st.t0, eps, C, P, quartets)
+            if self.guard:
+                r.err_vs_fp64 = None if np.isnan(st.err_fp64[si]) else float(st.err_fp64[si])
+                r.guard_hit = bool(st.guard_hit[si])
+            out.append(r)
         return out
 
     def solve(self, tol_energy=1e-8, tol_density=1e-6, max_iter=100):

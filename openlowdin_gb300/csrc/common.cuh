@@ -98,7 +98,6 @@ constexpr double kBoysH = 0.1;
 constexpr double kBoysTMax = 36.0;
 constexpr int kBoysPoints = 361;          // T_i = 0, 0.1, ..., 36.0
 constexpr int kBoysTaylor = 9;            // terms k = 0..8 (|dT| <= 0.05: error < 6e-18)
-constexpr int kBoysTaylorF32 = 6;
 constexpr int kBoysOrders = kMaxLQuartet + kBoysTaylor + 1;
 constexpr int kBoysStride = kBoysOrders + 1;  // row i: F_0..F_{kBoysOrders-1}(T_i), then e^{-T_i}
 // After that table, one table per order L = 0..kMaxLQuartet of the Taylor
@@ -158,31 +157,49 @@ __device__ __forceinline__ void boys_f64(double T, double (&F)[L + 1], const dou
   }
 }
 
-// FP32 Boys: Taylor about the float table; for T >= 36 the closed form
-// sqrt(pi/T)/2 (erfc(6) < 3e-17 relative) with the upward recursion, both exact
-// to FP32 rounding, so no FP64 instruction is issued.
+// FP32 Boys function by arithmetic alone (no table reads: a warp's 32
+// table rows are 32 scattered cache sectors, which bound the FP32 kernels on
+// the L1 pipe while their FMA pipe idled).
+//   L = 0: F_0(T) = sqrt(pi/T)/2 erf(sqrt(T)) (erff), F_0(0) = 1.
+//   L > 0, T < 4: F_L(T) = e^{-T} sum_k (2T)^k / ((2L+1)(2L+3)...(2L+2k+1))
+//     (a series of positive terms; kBoysSeries(L) terms leave < 1e-7 of the
+//     sum at T = 4), then the downward recursion
+//     F_m = (2T F_{m+1} + e^{-T}) / (2m+1).
+//   L > 0, T >= 4: F_0 as above, then the upward recursion
+//     F_{m+1} = ((2m+1) F_m - e^{-T}) / (2T) (stable there for m < 4).
+// Relative error below 8e-7 for every m <= L <= 4 and T >= 0 (checked against
+// the incomplete gamma function); FP32 evaluates only quartets whose
+// contribution is bounded by the mixed-precision split.
+__host__ __device__ constexpr int kBoysSeries(int L) { return L <= 1 ? 16 : (L == 2 ? 15 : 14); }
+constexpr float kBoysSplitT = 4.0f;
+
+__device__ __forceinline__ float boys0_f32(float T) {
+  return T < 1e-8f ? 1.0f - T * (1.0f / 3.0f) : 0.886226925f * erff(sqrtf(T)) * rsqrtf(T);
+}
+
 template <int L>
-__device__ __forceinline__ void boys_f32(float T, float (&F)[L + 1], const float *__restrict__ tab) {
-  if (T < (float)kBoysTMax) {
-    const int i = __float2int_rn(T * (float)(1.0 / kBoysH));
-    const float mdT = i * (float)kBoysH - T;
-    const float *t = tab + i * kBoysStride + L;
-    float s = __ldg(t + kBoysTaylorF32 - 1);
-#pragma unroll
-    for (int k = kBoysTaylorF32 - 1; k >= 1; --k) s = fmaf(mdT * (1.0f / k), s, __ldg(t + k - 1));
-    F[L] = s;
-    if constexpr (L > 0) {
-      const float e = __expf(-T);
-      const float twoT = 2.0f * T;
-#pragma unroll
-      for (int m = L - 1; m >= 0; --m) F[m] = fmaf(twoT, F[m + 1], e) * (1.0f / (2 * m + 1));
-    }
+__device__ __forceinline__ void boys_f32(float T, float (&F)[L + 1], const float *__restrict__) {
+  if constexpr (L == 0) {
+    F[0] = boys0_f32(T);
   } else {
     const float e = __expf(-T);
-    F[0] = 0.886226925f * rsqrtf(T);
-    const float o2T = 0.5f / T;
+    if (T < kBoysSplitT) {
+      const float twoT = 2.0f * T;
+      float term = 1.0f / (2 * L + 1), sum = term;
 #pragma unroll
-    for (int m = 0; m < L; ++m) F[m + 1] = fmaf((float)(2 * m + 1), F[m], -e) * o2T;
+      for (int k = 1; k <= kBoysSeries(L); ++k) {
+        term *= twoT * (1.0f / (2 * L + 2 * k + 1));
+        sum += term;
+      }
+      F[L] = e * sum;
+#pragma unroll
+      for (int m = L - 1; m >= 0; --m) F[m] = fmaf(twoT, F[m + 1], e) * (1.0f / (2 * m + 1));
+    } else {
+      F[0] = boys0_f32(T);
+      const float o2T = 0.5f / T;
+#pragma unroll
+      for (int m = 0; m < L; ++m) F[m + 1] = fmaf((float)(2 * m + 1), F[m], -e) * o2T;
+    }
   }
 }
 

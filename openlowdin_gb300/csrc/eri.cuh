@@ -230,4 +230,26 @@ __device__ __forceinline__ void eri_quartet(const PairT<R> &bra, const PrimT<R> 
   hrr_ket<R, LC, LD, QC_::NA * QC_::NB>(Y, CD, out);
 }
 
+// The same with a one-primitive ket pair whose primitive is passed by value
+// (the FP32 row kernels assemble it in registers from structure-of-arrays
+// fields).
+template <typename R, int LA, int LB, int LC, int LD>
+__device__ __forceinline__ void eri_quartet_k1(const PairT<R> &bra, const PrimT<R> *pbra, const PairT<R> &ket,
+                                               const PrimT<R> &pk, const double *boys64, const float *boys32,
+                                               R (&out)[QClass<LA, LB, LC, LD>::NINT]) {
+  using QC_ = QClass<LA, LB, LC, LD>;
+  R X[QC_::nE * QC_::nF];
+#pragma unroll
+  for (int i = 0; i < QC_::nE * QC_::nF; ++i) X[i] = R(0);
+  for (int ib = 0; ib < bra.nprim; ++ib) {
+    const PrimT<R> pb = pbra[ib];
+    vrr_prim<R, LA, LB, LC, LD>(X, pb, pk, boys64, boys32);
+  }
+  const R AB[3] = {bra.AB[0], bra.AB[1], bra.AB[2]};
+  const R CD[3] = {ket.AB[0], ket.AB[1], ket.AB[2]};
+  R Y[QC_::NA * QC_::NB * QC_::nF];
+  hrr<R, LA, LB, QC_::nF>(X, AB, Y);
+  hrr_ket<R, LC, LD, QC_::NA * QC_::NB>(Y, CD, out);
+}
+
 }  // namespace lgb

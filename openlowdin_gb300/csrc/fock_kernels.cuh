@@ -340,12 +340,46 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
 #pragma unroll
   for (int x = 0; x < NA * NB; ++x) j12[x] = 0.f;
   const float dn_ab = T.screen ? Dnr[bra.sb] : 0.f;
+  const float *__restrict__ soa = T.soa32;
+  const int np = T.npairs;
   unsigned cnt = 0;
   for (int k0 = warp * 32; k0 < nk; k0 += 32 * kRowWarps) {
     const int kpos = k0 + lane;
     bool active = kpos < nk;
     const int ki = T.ket0 + min(kpos, nk - 1);
-    const PairRec32 ket = T.pairs32[ki];
+    PairRec32 ket;
+    PrimRec32 kprim;
+    if (soa) {
+      // one coalesced 128-byte line per field and warp; only the fields the
+      // class reads are loaded
+      const float *f = soa + ki;
+      ket.Q = f[kSoaQ * np];
+      const int sh = __float_as_int(f[kSoaShells * np]), fn = __float_as_int(f[kSoaFuncs * np]);
+      ket.sa = sh & 0xffff;
+      ket.sb = sh >> 16;
+      ket.fa = fn & 0xffff;
+      ket.fb = fn >> 16;
+      ket.nprim = 1;
+      ket.prim0 = 0;
+      if constexpr (LD > 0) {
+        ket.AB[0] = f[kSoaABx * np];
+        ket.AB[1] = f[kSoaABy * np];
+        ket.AB[2] = f[kSoaABz * np];
+      }
+      kprim.p = f[kSoaP * np];
+      kprim.Kt = f[kSoaKt * np];
+      kprim.P[0] = f[kSoaPx * np];
+      kprim.P[1] = f[kSoaPy * np];
+      kprim.P[2] = f[kSoaPz * np];
+      if constexpr (LC + LD > 0) {
+        kprim.inv_p = f[kSoaInvP * np];
+        kprim.PA[0] = f[kSoaPAx * np];
+        kprim.PA[1] = f[kSoaPAy * np];
+        kprim.PA[2] = f[kSoaPAz * np];
+      }
+    } else {
+      ket = T.pairs32[ki];
+    }
     float bound = bra.Q * ket.Q;
     if (T.screen) {
       float m = dn_ab;
@@ -363,8 +397,11 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
     cnt += __popc(live);
     float I[Q::NINT];
     if (active) {
-      eri_quartet<float, LA, LB, LC, LD>(bra, prims + bra.prim0, ket, prims + ket.prim0, TL.boys.f64, TL.boys.f32,
-                                         I);
+      if (soa)
+        eri_quartet_k1<float, LA, LB, LC, LD>(bra, prims + bra.prim0, ket, kprim, TL.boys.f64, TL.boys.f32, I);
+      else
+        eri_quartet<float, LA, LB, LC, LD>(bra, prims + bra.prim0, ket, prims + ket.prim0, TL.boys.f64,
+                                           TL.boys.f32, I);
     } else {
 #pragma unroll
       for (int x = 0; x < Q::NINT; ++x) I[x] = 0.f;

@@ -9,6 +9,7 @@
 #pragma once
 #include <cuda_bf16.h>
 
+#include <cstring>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -60,6 +61,20 @@ struct BoysTables {
   const float *f32;
 };
 
+// Fields of the structure-of-arrays copy of a pair list's FP32 records
+// (one-primitive pairs): field k of pair i at soa[k * npairs + i].  Shell and
+// function indices are packed as a | b << 16 in the bits of a float.
+enum SoaField {
+  kSoaQ, kSoaShells, kSoaFuncs, kSoaP, kSoaInvP, kSoaKt, kSoaPx, kSoaPy, kSoaPz,
+  kSoaPAx, kSoaPAy, kSoaPAz, kSoaABx, kSoaABy, kSoaABz, kSoaFields
+};
+inline float __int_as_float_host(int v) {
+  float f;
+  static_assert(sizeof(f) == sizeof(v), "32-bit float");
+  memcpy(&f, &v, sizeof(f));
+  return f;
+}
+
 // One J/K task: quartets (bra in [bra0, bra0+nbra), ket in [ket0, ket0+nket))
 // of one species' significant pairs.
 // Every array exists in FP64 (used by the FP64 kernels) and FP32 (used by the
@@ -86,6 +101,8 @@ struct JKTask {
   int blk0;               // first flattened block of the task
   int nbx;                // blocks along the ket axis
   int rblk0;              // first block of the task in a bra-row launch (one block per bra pair)
+  const float *soa32;     // structure-of-arrays FP32 pair records (null: use pairs32 / prims32)
+  int npairs;             // pairs in the species' list (the field stride of soa32)
 };
 
 // One coupling task: quartets (A pair | B pair) of two species; accumulates

@@ -66,15 +66,21 @@ struct PairList {
   PrimRec *dp = nullptr;
   PairRec32 *d32 = nullptr;   // FP32 copies for the FP32 kernels
   PrimRec32 *dp32 = nullptr;
+  // the FP32 records of one-primitive pairs as structure of arrays
+  // (kSoaFields arrays of size(); null when a pair has several primitives),
+  // read by the FP32 row kernels one coalesced field at a time
+  float *soa32 = nullptr;
   void release() {
     if (d) cudaFree(d);
     if (dp) cudaFree(dp);
     if (d32) cudaFree(d32);
     if (dp32) cudaFree(dp32);
+    if (soa32) cudaFree(soa32);
     d = nullptr;
     dp = nullptr;
     d32 = nullptr;
     dp32 = nullptr;
+    soa32 = nullptr;
   }
   int count(int pc) const { return start[pc + 1] - start[pc]; }
   // uploads the FP64 records and their FP32 copies
@@ -103,7 +109,31 @@ struct PairList {
         b.PA[k] = (float)a.PA[k];
       }
     }
-    return dev_upload(d, h) && dev_upload(dp, hp) && dev_upload(d32, h32) && dev_upload(dp32, hp32);
+    if (!(dev_upload(d, h) && dev_upload(dp, hp) && dev_upload(d32, h32) && dev_upload(dp32, hp32))) return false;
+    bool one = !h.empty();
+    for (const auto &r : h) one = one && r.nprim == 1;
+    if (one) {
+      const size_t np = h.size();
+      std::vector<float> soa(kSoaFields * np);
+      for (size_t i = 0; i < np; ++i) {
+        const PairRec32 &r = h32[i];
+        const PrimRec32 &q = hp32[r.prim0];
+        float *c = soa.data() + i;
+        c[kSoaQ * np] = r.Q;
+        c[kSoaShells * np] = __int_as_float_host(r.sa | r.sb << 16);
+        c[kSoaFuncs * np] = __int_as_float_host(r.fa | r.fb << 16);
+        c[kSoaP * np] = q.p;
+        c[kSoaInvP * np] = q.inv_p;
+        c[kSoaKt * np] = q.Kt;
+        for (int k = 0; k < 3; ++k) {
+          c[(kSoaPx + k) * np] = q.P[k];
+          c[(kSoaPAx + k) * np] = q.PA[k];
+          c[(kSoaABx + k) * np] = r.AB[k];
+        }
+      }
+      if (!dev_upload(soa32, soa)) return false;
+    }
+    return true;
   }
 };
 
@@ -528,6 +558,8 @@ struct LibintInterface {
         t.nsh = nshell();
         t.triangle = cb == ck;
         t.screen = is_electron ? 1 : 0;
+        t.soa32 = sig.soa32;
+        t.npairs = (int)sig.h.size();
         ts.add(cb, ck, t);
       }
     return true;

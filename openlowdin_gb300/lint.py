@@ -98,8 +98,10 @@ def lib():
                                                ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                                ctypes.c_double, ctypes.POINTER(ctypes.c_double), _vp]
         L.LowdinGB300_mp2_coupling.restype = ctypes.c_int
-        L.LowdinGB300_diis_coefficients.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp]
+        L.LowdinGB300_diis_coefficients.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]
         L.LowdinGB300_diis_coefficients.restype = ctypes.c_int
+        L.LowdinGB300_boys_eval.argtypes = [ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int, _f64p]
+        L.LowdinGB300_boys_eval.restype = ctypes.c_int
         L.LowdinGB300_gemm_bf16_split.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                   ctypes.c_int, _vp]
         L.LowdinGB300_gemm_bf16_split.restype = ctypes.c_int
@@ -158,15 +160,26 @@ EXPORTED_SYMBOLS = [
     "LowdinGB300_twobody_device_noalloc", "LowdinGB300_mp2_direct", "LowdinGB300_mp2_last_columns", "LowdinGB300_mp2_coupling",
     "LowdinGB300_gemm_bf16_split", "LowdinGB300_gemm_bf16_precise",
     "LowdinGB300_gemm_bench", "LowdinGB300_mp2_moint", "LowdinGB300_mp2_coupling_moint", "LowdinGB300_moint_write",
-    "LowdinGB300_diis_coefficients",
+    "LowdinGB300_diis_coefficients", "LowdinGB300_boys_eval",
 ]
 
 
-def diis_coefficients(e_ptr: int, h: int, nsys: int, coef_ptr: int, stream: int = 0):
+def diis_coefficients(e_ptr: int, h: int, nsys: int, coef_ptr: int, stream: int = 0, first_ptr: int = 0):
     """DIIS coefficients of nsys systems from their [h][h] error products
-    (device FP64 arrays), queued on `stream`."""
-    if lib().LowdinGB300_diis_coefficients(e_ptr, h, nsys, coef_ptr, stream) != 0:
+    (device FP64 arrays), queued on `stream`; first_ptr: optional device int
+    array, per system the first history entry used."""
+    if lib().LowdinGB300_diis_coefficients(e_ptr, h, nsys, first_ptr or None, coef_ptr, stream) != 0:
         _check()
+
+
+def boys_eval(T, L: int, fp32: bool) -> np.ndarray:
+    """F_0..F_L at the arguments T from the device Boys function of the FP32
+    (fp32) or FP64 kernels; shape [len(T), L + 1]."""
+    T = np.ascontiguousarray(T, dtype=np.float64)
+    out = np.zeros((len(T), L + 1))
+    if lib().LowdinGB300_boys_eval(1 if fp32 else 0, L, T, len(T), out) != 0:
+        _check()
+    return out
 
 
 def moint_write(path: str, p, q, r, s, v, stack_size: int = 30000):

@@ -57,6 +57,10 @@ class SCFResult:
     coefficients: list = field(default_factory=list)
     densities: list = field(default_factory=list)
     quartets: int = 0
+    # mixed precision: |E_mixed - E_FP64| of the FP64 check at the converged
+    # density, and whether the check sent the system on in FP64
+    err_vs_fp64: float | None = None
+    guard_hit: bool = False
 
 
 def _one_body(handles, sysd):

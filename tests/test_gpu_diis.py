@@ -52,3 +52,22 @@ def test_diis_rejects_long_histories():
     dc = torch.zeros((1, 21), dtype=torch.float64, device="cuda")
     with pytest.raises(lint.LowdinGB300Error):
         lint.diis_coefficients(dE.data_ptr(), 21, 1, dc.data_ptr())
+
+
+@pytest.mark.parametrize("L", [0, 1, 2, 3, 4])
+def test_device_boys_functions_against_incomplete_gamma(L):
+    """The FP32 kernels' arithmetic Boys function within 1e-6 relative of the
+    incomplete-gamma definition for T in [0, 60]; the FP64 tabulated one within
+    1e-13 (every order m <= L)."""
+    from scipy.special import gamma, gammainc
+    from openlowdin_gb300 import build, lint
+    build.build()
+    T = np.concatenate([[0.0, 1e-10, 1e-6], np.linspace(1e-4, 1.0, 500), np.linspace(1.0, 60.0, 6000)])
+    for fp32, tol in ((True, 1e-6), (False, 1e-13)):
+        F = lint.boys_eval(T, L, fp32)
+        for m in range(L + 1):
+            ex = np.where(T < 1e-12, 1.0 / (2 * m + 1),
+                          gamma(m + 0.5) * gammainc(m + 0.5, np.maximum(T, 1e-300)) /
+                          (2 * np.maximum(T, 1e-300) ** (m + 0.5)))
+            rel = np.max(np.abs(F[:, m] - ex) / ex)
+            assert rel < tol, (fp32, m, rel)

@@ -244,3 +244,29 @@ def test_padded_buckets_match_exact_groups():
         for ea, eb in zip(a.orbital_energies, b.orbital_energies):
             assert ea.shape == eb.shape
             assert np.max(np.abs(ea - eb)) < 1e-6
+
+
+def test_batch_mixed_fp64_check_and_guard():
+    """BatchSCF in mixed precision: every converged system gets an FP64 check
+    (its stated error <= 1e-6 Eh, energy within 1e-6 of plain); with every
+    quartet forced into FP32 the check fails and the system finishes in FP64
+    on the plain energy."""
+    from openlowdin_gb300 import systems as S
+    from openlowdin_gb300.batch_scf import BatchSCF
+    mols = [S.chain_for_basis(500 + i, nbf) for i, nbf in enumerate((50, 80, 120))]
+    b = BatchSCF(mols, precision="fp64")
+    plain = b.solve()
+    b.close()
+    b = BatchSCF(mols, precision="mixed")
+    mixed = b.solve()
+    b.close()
+    for p, m in zip(plain, mixed):
+        assert p.converged and m.converged and not m.guard_hit
+        assert m.err_vs_fp64 is not None and m.err_vs_fp64 <= 1e-6
+        assert abs(m.energy - p.energy) < 1e-6
+    b = BatchSCF(mols, precision="mixed", split=1e30)
+    forced = b.solve()
+    b.close()
+    for p, f in zip(plain, forced):
+        assert f.converged and f.guard_hit and f.err_vs_fp64 == 0.0
+        assert abs(f.energy - p.energy) < 1e-8
