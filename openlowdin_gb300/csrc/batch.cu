@@ -27,6 +27,11 @@ struct LowdinGB300_Batch {
   DevBuf<float> Ds32, Dn32, Gacc32, Jacc32;
   DevBuf<unsigned long long> cnt;
   DevBuf<SpeciesSlot> slots;
+  // pair-indexed arrays of the FP32 row kernels, one PairSlot per two-body species
+  DevBuf<float> Dp32, Jp32, DnP32;
+  DevBuf<PairSlot> pslots;
+  int npslots = 0;
+  long long ptotal = 0;
   long long total = 0;
   int nslots = 0;
   TaskSet<JKTask> jk;
@@ -55,6 +60,7 @@ struct LowdinGB300_Batch {
     drop_graphs();
     if (capture) cudaStreamDestroy(capture);
     Ds.release(); Dn.release(); Gacc.release(); Jacc.release(); cnt.release(); slots.release();
+    Dp32.release(); Jp32.release(); DnP32.release(); pslots.release();
     Ds32.release(); Dn32.release(); Gacc32.release(); Jacc32.release();
     active.release();
     jk.release(); cp.release();
@@ -96,6 +102,21 @@ struct LowdinGB300_Batch {
     if (!Ds.ensure(tot) || !Gacc.ensure(tot) || !Jacc.ensure(tot) || !Dn.ensure(dsz) || !Ds32.ensure(tot) ||
         !Gacc32.ensure(tot) || !Jacc32.ensure(tot) || !Dn32.ensure(dsz) || !cnt.ensure(2 * kNQC))
       return false;
+    // pair-indexed arenas of the two-body species
+    std::vector<long long> peoff(sp.size(), -1), pairoff(sp.size(), -1);
+    long long petot = 0, pptot = 0;
+    for (size_t k = 0; k < sp.size(); ++k) {
+      if (!sp[k].two_body) continue;
+      long long pb[kNumPairClasses];
+      peoff[k] = petot;
+      pairoff[k] = pptot;
+      petot += pair_elements(sp[k].h->sig.start, pb);
+      pptot += (long long)sp[k].h->sig.h.size();
+    }
+    if (!Dp32.ensure(std::max(1LL, petot)) || !Jp32.ensure(std::max(1LL, petot)) ||
+        !DnP32.ensure(std::max(1LL, pptot)))
+      return false;
+    std::vector<PairSlot> hps;
     std::vector<SpeciesSlot> hs(sp.size());
     std::vector<SpeciesBufs> bf(sp.size());
     jk.clear();
@@ -141,10 +162,28 @@ struct LowdinGB300_Batch {
       S.active = active.p + x.sys;
       if (x.two_body) {
         // non-electron species are not screened: their norm pointers are never read
-        SpeciesBufs b{S.Ds, S.Ds32, S.Dn ? S.Dn : Dn.p, S.Dn32 ? S.Dn32 : Dn32.p, S.Gacc, S.Gacc32};
+        SpeciesBufs b{S.Ds, S.Ds32, S.Dn ? S.Dn : Dn.p, S.Dn32 ? S.Dn32 : Dn32.p, S.Gacc, S.Gacc32,
+                      Dp32.p + peoff[k], Jp32.p + peoff[k], DnP32.p + pairoff[k]};
         const auto before = sizes(jk);
         if (!x.h->add_jk_tasks(jk, b, 0.5 * x.factor, cnt.p)) return false;
         mark(jk, before, x.sys);
+        PairSlot ps{};
+        const PairList &L = x.h->sig;
+        ps.pairs = L.d32;
+        ps.npairs = (int)L.h.size();
+        ps.poff = pairoff[k];
+        for (int c = 0; c <= kNumPairClasses; ++c) ps.start[c] = L.start[c];
+        pair_elements(L.start, ps.pe_base);
+        ps.Ds32 = S.Ds32;
+        ps.Dn32 = x.h->is_electron ? S.Dn32 : nullptr;
+        ps.Gacc32 = S.Gacc32;
+        ps.n = S.n;
+        ps.nsh = S.nsh;
+        ps.Dp32 = Dp32.p + peoff[k];
+        ps.Jp32 = Jp32.p + peoff[k];
+        ps.DnP32 = DnP32.p + pairoff[k];
+        ps.active = S.active;
+        hps.push_back(ps);
       }
       bf[k] = SpeciesBufs{S.Ds, S.Ds32, S.Dn, S.Dn32, S.Jacc, S.Jacc32};
     }
@@ -162,6 +201,12 @@ struct LowdinGB300_Batch {
     nslots = (int)hs.size();
     if (!slots.ensure(hs.size())) return false;
     CK(cudaMemcpyAsync(slots.p, hs.data(), hs.size() * sizeof(SpeciesSlot), cudaMemcpyHostToDevice, s));
+    npslots = (int)hps.size();
+    ptotal = pptot;
+    if (npslots > 0) {
+      if (!pslots.ensure(hps.size())) return false;
+      CK(cudaMemcpyAsync(pslots.p, hps.data(), hps.size() * sizeof(PairSlot), cudaMemcpyHostToDevice, s));
+    }
     if (!jk.upload(s) || !cp.upload(s)) return false;
     CK(cudaStreamSynchronize(s));
     finalized = true;
@@ -220,7 +265,9 @@ struct LowdinGB300_Batch {
     CK(cudaMemsetAsync(cnt.p, 0, 2 * kNQC * sizeof(unsigned long long), s));
     CK(launch_prepare_batch(slots.p, nslots, total, s));
     const int jk_mixed = precision & 1;
+    if (jk_mixed && npslots) CK(launch_pair_gather(pslots.p, npslots, ptotal, s));
     if (!LibintInterface::launch_jk_groups(jk, jk_mixed, jk_mixed ? split : 0.0, boys, s, skip)) return false;
+    if (jk_mixed && npslots) CK(launch_pair_scatter(pslots.p, npslots, ptotal, s));
     if (!launch_cp_groups(cp, (precision & 2) ? 2 : 0, split, boys, s, skip)) return false;
     CK(launch_finalize_batch(slots.p, nslots, total, s));
     return true;

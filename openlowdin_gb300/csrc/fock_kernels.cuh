@@ -281,13 +281,17 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
 // kRowWarps warps take the task's ket pairs 32 at a time).  The exchange
 // updates of a quartet touch only rows fa.. and fb.. of the output (K13, K14
 // on the rows of shell a, K23, K24 on those of shell b) and read only those
-// rows of D, so the block keeps both -- D rows and exchange accumulators,
-// NA + NB rows of n columns -- and the two shell-block-norm rows of shells a
-// and b in shared memory: per quartet the four exchange reads and updates and
-// four of the six screening norms are shared-memory accesses instead of
-// scattered global ones.  The bra Coulomb block (J12) is summed in registers
-// over every ket of the warp before one warp reduction; the ket Coulomb block
-// (J34) and the ket block of D stay global.  At the end the accumulated
+// rows of D, so the block keeps both in shared memory, interleaved by column
+// (Drow[col][r], Krow[col][r], r < NA + NB, padded to an even count so a
+// column's D values are one vector load), together with the largest
+// shell-block norm of shells a and b against every shell (Dnab[s] =
+// max(|D|_{a s}, |D|_{b s})), which gives four of the six screening norms in
+// two reads.  The ket side is read from pair-indexed arrays when the build
+// provides them (JKTask::Dp32 / DnP32 / Jp32: per ket pair its D block, its
+// shell-block norm and its Coulomb accumulator, element-major inside the ket
+// class, so a warp's 32 kets are one coalesced line per element), else from
+// the n x n matrices.  The bra Coulomb block (J12) is summed in registers
+// over every ket of the warp before one warp reduction.  At the end the
 // exchange rows go to the global accumulator (non-zero entries only).
 // Quartet selection, bound and arithmetic are those of jk_tasks_kernel's FP32
 // launch (same FP32 bound, same screening and split), so the quartets taken
@@ -306,7 +310,7 @@ __device__ __forceinline__ int find_task_rows(const T *__restrict__ tasks, int n
 template <int LA, int LB, int LC, int LD>
 __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *__restrict__ tasks, TaskLaunch TL) {
   using Q = QClass<LA, LB, LC, LD>;
-  constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND, NR = NA + NB;
+  constexpr int NA = Q::NA, NB = Q::NB, NC = Q::NC, ND = Q::ND, NR = NA + NB, NRP = row_pitch(NA + NB);
   extern __shared__ float rsm[];
   const int t = find_task_rows(tasks, TL.ntasks, blockIdx.x);
   const JKTask &T = tasks[t];
@@ -318,18 +322,19 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
   const int n = T.n, nsh = T.nsh;
   const PairRec32 bra = T.pairs32[bi];
   const PrimRec32 *__restrict__ prims = T.prims32;
-  float *Drow = rsm;              // [NR][n]: rows fa+a (a < NA), then fb+b
-  float *Krow = rsm + NR * n;     // [NR][n]: exchange accumulators of the same rows
-  float *Dnr = Krow + NR * n;     // [2][nsh]: shell-block norms of shells sa and sb
-  for (int i = threadIdx.x; i < NR * n; i += blockDim.x) {
-    const int r = i / n, c = i - r * n;
-    const int f = r < NA ? bra.fa + r : bra.fb + (r - NA);
-    Drow[i] = __ldg(T.Ds32 + (size_t)f * n + c);
+  float *Drow = rsm;                 // [n][NRP]: D(fa + r, col) for r < NA, D(fb + r - NA, col) after
+  float *Krow = rsm + NRP * n;       // [n][NRP]: exchange accumulators of the same rows
+  float *Dnab = Krow + NRP * n;      // [nsh]
+  for (int i = threadIdx.x; i < NRP * n; i += blockDim.x) {
+    const int c = i / NRP, r = i - c * NRP;
+    float v = 0.f;
+    if (r < NR) v = __ldg(T.Ds32 + (size_t)(r < NA ? bra.fa + r : bra.fb + (r - NA)) * n + c);
+    Drow[i] = v;
     Krow[i] = 0.f;
   }
   if (T.screen)
-    for (int i = threadIdx.x; i < 2 * nsh; i += blockDim.x)
-      Dnr[i] = __ldg(T.Dn32 + (size_t)(i < nsh ? bra.sa : bra.sb) * nsh + (i < nsh ? i : i - nsh));
+    for (int i = threadIdx.x; i < nsh; i += blockDim.x)
+      Dnab[i] = fmaxf(__ldg(T.Dn32 + (size_t)bra.sa * nsh + i), __ldg(T.Dn32 + (size_t)bra.sb * nsh + i));
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float hf = T.hf32;
@@ -339,14 +344,19 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
   float j12[NA * NB];
 #pragma unroll
   for (int x = 0; x < NA * NB; ++x) j12[x] = 0.f;
-  const float dn_ab = T.screen ? Dnr[bra.sb] : 0.f;
+  const float dn_ab = T.screen ? __ldg(T.Dn32 + (size_t)bra.sa * nsh + bra.sb) : 0.f;
   const float *__restrict__ soa = T.soa32;
   const int np = T.npairs;
+  const float *__restrict__ Dp = T.Dp32;          // pair-indexed ket data (null: n x n matrices)
+  const float *__restrict__ DnP = T.DnP32;
+  float *Jp = T.Jp32;
+  const int kstride = T.nket;                     // element stride of the pair-indexed arrays
   unsigned cnt = 0;
   for (int k0 = warp * 32; k0 < nk; k0 += 32 * kRowWarps) {
     const int kpos = k0 + lane;
     bool active = kpos < nk;
-    const int ki = T.ket0 + min(kpos, nk - 1);
+    const int kq = min(kpos, nk - 1);
+    const int ki = T.ket0 + kq;
     PairRec32 ket;
     PrimRec32 kprim;
     if (soa) {
@@ -382,12 +392,8 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
     }
     float bound = bra.Q * ket.Q;
     if (T.screen) {
-      float m = dn_ab;
-      m = fmaxf(m, Dnr[ket.sa]);
-      m = fmaxf(m, Dnr[nsh + ket.sa]);
-      m = fmaxf(m, Dnr[ket.sb]);
-      m = fmaxf(m, Dnr[nsh + ket.sb]);
-      m = fmaxf(m, __ldg(T.Dn32 + (size_t)ket.sa * nsh + ket.sb));
+      float m = fmaxf(dn_ab, fmaxf(Dnab[ket.sa], Dnab[ket.sb]));
+      m = fmaxf(m, DnP ? DnP[ki] : __ldg(T.Dn32 + (size_t)ket.sa * nsh + ket.sb));
       bound *= m;
       if (bound < cutoff) active = false;
     }
@@ -415,14 +421,33 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
     for (int c = 0; c < NC; ++c)
 #pragma unroll
       for (int d = 0; d < ND; ++d) {
-        const float dcd = active ? __ldg(D + (size_t)(fc + c) * n + fd + d) * deg : 0.f;
+        float dcd = 0.f;
+        if (active) dcd = (Dp ? Dp[(size_t)(c * ND + d) * kstride + kq] : __ldg(D + (size_t)(fc + c) * n + fd + d)) * deg;
 #pragma unroll
         for (int a = 0; a < NA; ++a)
 #pragma unroll
           for (int b = 0; b < NB; ++b) j12[a * NB + b] = fmaf(dcd, Iat(a, b, c, d), j12[a * NB + b]);
       }
     if (!active) continue;
-    // J34 (ket block)
+    // the D rows of the bra shells at the ket's columns (one vector read per column)
+    float dc[NC][NRP], dd[ND][NRP];
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+      for (int r = 0; r < NRP; r += 2) {
+        const float2 v = *reinterpret_cast<const float2 *>(Drow + (fc + c) * NRP + r);
+        dc[c][r] = v.x;
+        dc[c][r + 1] = v.y;
+      }
+#pragma unroll
+    for (int d = 0; d < ND; ++d)
+#pragma unroll
+      for (int r = 0; r < NRP; r += 2) {
+        const float2 v = *reinterpret_cast<const float2 *>(Drow + (fd + d) * NRP + r);
+        dd[d][r] = v.x;
+        dd[d][r + 1] = v.y;
+      }
+    // J34 (ket block): D of the bra block
 #pragma unroll
     for (int c = 0; c < NC; ++c)
 #pragma unroll
@@ -431,8 +456,9 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
 #pragma unroll
         for (int a = 0; a < NA; ++a)
 #pragma unroll
-          for (int b = 0; b < NB; ++b) s = fmaf(Drow[a * n + bra.fb + b], Iat(a, b, c, d), s);
-        atomicAdd(G32 + (size_t)(fc + c) * n + fd + d, s * deg);
+          for (int b = 0; b < NB; ++b) s = fmaf(Drow[(bra.fb + b) * NRP + a], Iat(a, b, c, d), s);
+        if (Jp) atomicAdd(Jp + (size_t)(c * ND + d) * kstride + kq, s * deg);
+        else atomicAdd(G32 + (size_t)(fc + c) * n + fd + d, s * deg);
       }
     // K13 (a,c) += D(b,d), K14 (a,d) += D(b,c): rows of shell a
 #pragma unroll
@@ -443,8 +469,8 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
 #pragma unroll
         for (int b = 0; b < NB; ++b)
 #pragma unroll
-          for (int d = 0; d < ND; ++d) s = fmaf(Drow[(NA + b) * n + fd + d], Iat(a, b, c, d), s);
-        atomicAdd(Krow + a * n + fc + c, s * hdeg);
+          for (int d = 0; d < ND; ++d) s = fmaf(dd[d][NA + b], Iat(a, b, c, d), s);
+        atomicAdd(Krow + (fc + c) * NRP + a, s * hdeg);
       }
 #pragma unroll
       for (int d = 0; d < ND; ++d) {
@@ -452,8 +478,8 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
 #pragma unroll
         for (int b = 0; b < NB; ++b)
 #pragma unroll
-          for (int c = 0; c < NC; ++c) s = fmaf(Drow[(NA + b) * n + fc + c], Iat(a, b, c, d), s);
-        atomicAdd(Krow + a * n + fd + d, s * hdeg);
+          for (int c = 0; c < NC; ++c) s = fmaf(dc[c][NA + b], Iat(a, b, c, d), s);
+        atomicAdd(Krow + (fd + d) * NRP + a, s * hdeg);
       }
     }
     // K24 (b,d) += D(a,c), K23 (b,c) += D(a,d): rows of shell b
@@ -465,8 +491,8 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
 #pragma unroll
         for (int a = 0; a < NA; ++a)
 #pragma unroll
-          for (int c = 0; c < NC; ++c) s = fmaf(Drow[a * n + fc + c], Iat(a, b, c, d), s);
-        atomicAdd(Krow + (NA + b) * n + fd + d, s * hdeg);
+          for (int c = 0; c < NC; ++c) s = fmaf(dc[c][a], Iat(a, b, c, d), s);
+        atomicAdd(Krow + (fd + d) * NRP + NA + b, s * hdeg);
       }
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
@@ -474,8 +500,8 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
 #pragma unroll
         for (int a = 0; a < NA; ++a)
 #pragma unroll
-          for (int d = 0; d < ND; ++d) s = fmaf(Drow[a * n + fd + d], Iat(a, b, c, d), s);
-        atomicAdd(Krow + (NA + b) * n + fc + c, s * hdeg);
+          for (int d = 0; d < ND; ++d) s = fmaf(dd[d][a], Iat(a, b, c, d), s);
+        atomicAdd(Krow + (fc + c) * NRP + NA + b, s * hdeg);
       }
     }
   }
@@ -487,13 +513,10 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
     if (lane == 0 && v != 0.f) atomicAdd(G32 + (size_t)(bra.fa + x / NB) * n + bra.fb + x % NB, v);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < NR * n; i += blockDim.x) {
+  for (int i = threadIdx.x; i < NRP * n; i += blockDim.x) {
     const float v = Krow[i];
-    if (v != 0.f) {
-      const int r = i / n, c = i - r * n;
-      const int f = r < NA ? bra.fa + r : bra.fb + (r - NA);
-      atomicAdd(G32 + (size_t)f * n + c, v);
-    }
+    const int c = i / NRP, r = i - c * NRP;
+    if (v != 0.f && r < NR) atomicAdd(G32 + (size_t)(r < NA ? bra.fa + r : bra.fb + (r - NA)) * n + c, v);
   }
 }
 

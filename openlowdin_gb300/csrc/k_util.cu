@@ -167,7 +167,89 @@ __global__ void finalize_batch_kernel(const SpeciesSlot *__restrict__ slots, int
   }
 }
 
+__device__ __forceinline__ int find_pair_slot(const PairSlot *__restrict__ slots, int nslots, long long x) {
+  int lo = 0, hi = nslots - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (slots[mid].poff <= x) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// class of pair record `idx` of a slot and its position in the class
+__device__ __forceinline__ int pair_class_of(const PairSlot &S, int idx, int *pos) {
+  int c = 0;
+  while (c + 1 < kNumPairClasses && S.start[c + 1] <= idx) ++c;
+  *pos = idx - S.start[c];
+  return c;
+}
+
+// one thread per (slot, pair): its D block, norm, and a cleared accumulator
+__global__ void pair_gather_kernel(const PairSlot *__restrict__ slots, int nslots, long long total) {
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+       x += (long long)gridDim.x * blockDim.x) {
+    const PairSlot &S = slots[find_pair_slot(slots, nslots, x)];
+    if (S.active && __ldg(S.active) == 0) continue;
+    const int idx = (int)(x - S.poff);
+    int k;
+    const int c = pair_class_of(S, idx, &k);
+    const int cnt = S.start[c + 1] - S.start[c];
+    const PairRec32 r = S.pairs[idx];
+    const int nb = ncart(r.lb), ne = ncart(r.la) * nb;
+    const long long base = S.pe_base[c] + k;
+    for (int e = 0; e < ne; ++e) {
+      S.Dp32[base + (long long)e * cnt] = S.Ds32[(size_t)(r.fa + e / nb) * S.n + r.fb + e % nb];
+      S.Jp32[base + (long long)e * cnt] = 0.f;
+    }
+    if (S.Dn32) S.DnP32[idx] = S.Dn32[(size_t)r.sa * S.nsh + r.sb];
+  }
+}
+
+__global__ void pair_scatter_kernel(const PairSlot *__restrict__ slots, int nslots, long long total) {
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+       x += (long long)gridDim.x * blockDim.x) {
+    const PairSlot &S = slots[find_pair_slot(slots, nslots, x)];
+    if (S.active && __ldg(S.active) == 0) continue;
+    const int idx = (int)(x - S.poff);
+    int k;
+    const int c = pair_class_of(S, idx, &k);
+    const int cnt = S.start[c + 1] - S.start[c];
+    const PairRec32 r = S.pairs[idx];
+    const int nb = ncart(r.lb), ne = ncart(r.la) * nb;
+    const long long base = S.pe_base[c] + k;
+    // each pair owns its block of Gacc32 (distinct shell pairs, canonical order)
+    for (int e = 0; e < ne; ++e) {
+      const float v = S.Jp32[base + (long long)e * cnt];
+      if (v != 0.f) S.Gacc32[(size_t)(r.fa + e / nb) * S.n + r.fb + e % nb] += v;
+    }
+  }
+}
+
 }  // namespace
+
+long long pair_elements(const int *start, long long *pe_base) {
+  long long tot = 0;
+  for (int c = 0; c < kNumPairClasses; ++c) {
+    pe_base[c] = tot;
+    tot += (long long)(start[c + 1] - start[c]) * ncart(pc_la(c)) * ncart(pc_lb(c));
+  }
+  return tot;
+}
+
+cudaError_t launch_pair_gather(const PairSlot *slots, int nslots, long long total_pairs, cudaStream_t s) {
+  if (total_pairs <= 0) return cudaSuccess;
+  pair_gather_kernel<<<grid_for((size_t)total_pairs, 256), 256, 0, s>>>(slots, nslots, total_pairs);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pair_scatter(const PairSlot *slots, int nslots, long long total_pairs, cudaStream_t s) {
+  if (total_pairs <= 0) return cudaSuccess;
+  pair_scatter_kernel<<<grid_for((size_t)total_pairs, 256), 256, 0, s>>>(slots, nslots, total_pairs);
+  count_launches(1);
+  return cudaGetLastError();
+}
 
 void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }

@@ -103,6 +103,13 @@ struct JKTask {
   int rblk0;              // first block of the task in a bra-row launch (one block per bra pair)
   const float *soa32;     // structure-of-arrays FP32 pair records (null: use pairs32 / prims32)
   int npairs;             // pairs in the species' list (the field stride of soa32)
+  // pair-indexed ket data of the FP32 row kernels (null: read the n x n
+  // matrices), element e of the ket at class position k at [e * nket + k]:
+  // the ket's block of Ds32, its Coulomb (J34) accumulator, and (indexed by
+  // pair record) its shell-block norm
+  const float *Dp32;
+  float *Jp32;
+  const float *DnP32;
 };
 
 // One coupling task: quartets (A pair | B pair) of two species; accumulates
@@ -167,8 +174,10 @@ using JKFn = void (*)(const JKTask *, TaskLaunch);
 // output in shared memory (jk32_row_kernel), one block per bra pair
 constexpr int kRowWarps = 4;
 constexpr int kRowMaxSmem = 200 * 1024;
+// shared rows per column: the bra shells' NA + NB rows padded to an even count
+__host__ __device__ constexpr int row_pitch(int nrows) { return (nrows + 1) & ~1; }
 __host__ __device__ constexpr size_t row_smem_bytes(int nrows, int n, int nsh) {
-  return (size_t)(2 * nrows * n + 2 * nsh) * sizeof(float);
+  return (size_t)(2 * row_pitch(nrows) * n + nsh) * sizeof(float);
 }
 using CPFn = void (*)(const CPTask *, TaskLaunch);
 struct ITParams;
@@ -314,6 +323,29 @@ struct SpeciesSlot {
   const int *active;      // the slot's system is built while *active != 0 (null: always)
 };
 cudaError_t launch_prepare_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s);
+
+// pair-indexed copies of a species' FP32 density for the FP32 row kernels:
+// for every significant pair (class c, position k in its class) and element e
+// of its block, Dp32[pe_base[c] + e * count_c + k] = Ds32 at the block's
+// element, Jp32 there = 0, and DnP32[pair] = Dn32 of its shell block;
+// pair_scatter adds the Jp32 accumulators into Gacc32 after the build
+struct PairSlot {
+  const PairRec32 *pairs;
+  int npairs;
+  long long poff;         // prefix of npairs over the slots
+  int start[kNumPairClasses + 1];
+  long long pe_base[kNumPairClasses];
+  const float *Ds32, *Dn32;
+  float *Gacc32;
+  int n, nsh;
+  float *Dp32, *Jp32, *DnP32;
+  const int *active;      // slot's system flag (null: always built)
+};
+cudaError_t launch_pair_gather(const PairSlot *slots, int nslots, long long total_pairs, cudaStream_t s);
+cudaError_t launch_pair_scatter(const PairSlot *slots, int nslots, long long total_pairs, cudaStream_t s);
+// elements of the pair-indexed arrays of a pair list (class starts `start`),
+// and the per-class bases
+long long pair_elements(const int *start, long long *pe_base);
 cudaError_t launch_finalize_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s);
 
 // Split-BF16 operands: x ~= p[0] + p[1] (+ p[2]), each piece the BF16

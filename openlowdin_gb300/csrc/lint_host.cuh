@@ -172,6 +172,10 @@ struct SpeciesBufs {
   const float *Dn32;
   double *G;
   float *G32;
+  // pair-indexed arrays of the FP32 row kernels (PairSlot), or null
+  float *Dp32 = nullptr;
+  float *Jp32 = nullptr;
+  float *DnP32 = nullptr;
 };
 
 // Tasks grouped by quartet class (bra pair class * 6 + ket pair class); one
@@ -267,6 +271,8 @@ struct LibintInterface {
   DevBuf<double> dZR;          // point charges and positions of the last one-body call
   DevBuf<double> dD, dDs, dDn, dGacc, dG, dA, dC, dDsC, dJacc;
   DevBuf<float> dDs32, dDn32, dGacc32, dDsC32, dJacc32;
+  DevBuf<float> dDp32, dJp32, dDnP32;   // pair-indexed arrays of the FP32 row kernels
+  DevBuf<PairSlot> dpslot;
   DevBuf<unsigned long long> dcount;
   unsigned long long *hcount = nullptr;   // pinned copy of dcount, read once its stream is done
   cudaStream_t count_stream = nullptr;
@@ -296,6 +302,7 @@ struct LibintInterface {
     dD.release(); dDs.release(); dDn.release(); dGacc.release(); dG.release(); dA.release(); dC.release();
     dDsC.release(); dJacc.release();
     dDs32.release(); dDn32.release(); dGacc32.release(); dDsC32.release(); dJacc32.release();
+    dDp32.release(); dJp32.release(); dDnP32.release(); dpslot.release();
     dcount.release();
     if (hcount) cudaFreeHost(hcount);
     hcount = nullptr;
@@ -490,8 +497,31 @@ struct LibintInterface {
         !dcount.ensure(kNQC))
       return false;
     if (!jk_ready || jk_hf != 0.5 * factor) {
+      // pair-indexed arrays of the FP32 row kernels and their slot
+      long long pe_base[kNumPairClasses];
+      const long long pe = pair_elements(sig.start, pe_base);
+      const int npairs = (int)sig.h.size();
+      if (!dDp32.ensure(std::max(1LL, pe)) || !dJp32.ensure(std::max(1LL, pe)) ||
+          !dDnP32.ensure(std::max(1, npairs)) || !dpslot.ensure(1))
+        return false;
+      PairSlot ps{};
+      ps.pairs = sig.d32;
+      ps.npairs = npairs;
+      ps.poff = 0;
+      for (int c = 0; c <= kNumPairClasses; ++c) ps.start[c] = sig.start[c];
+      for (int c = 0; c < kNumPairClasses; ++c) ps.pe_base[c] = pe_base[c];
+      ps.Ds32 = dDs32.p;
+      ps.Dn32 = is_electron ? dDn32.p : nullptr;
+      ps.Gacc32 = dGacc32.p;
+      ps.n = n;
+      ps.nsh = nsh;
+      ps.Dp32 = dDp32.p;
+      ps.Jp32 = dJp32.p;
+      ps.DnP32 = dDnP32.p;
+      ps.active = nullptr;
+      CK(cudaMemcpyAsync(dpslot.p, &ps, sizeof(ps), cudaMemcpyHostToDevice, s));
       jk.clear();
-      SpeciesBufs b{dDs.p, dDs32.p, dDn.p, dDn32.p, dGacc.p, dGacc32.p};
+      SpeciesBufs b{dDs.p, dDs32.p, dDn.p, dDn32.p, dGacc.p, dGacc32.p, dDp32.p, dJp32.p, dDnP32.p};
       if (!add_jk_tasks(jk, b, 0.5 * factor, dcount.p)) return false;
       if (!jk.upload(s)) return false;
       jk_hf = 0.5 * factor;
@@ -501,7 +531,9 @@ struct LibintInterface {
     CK(cudaMemsetAsync(dGacc.p, 0, sizeof(double) * n * n, s));
     CK(cudaMemsetAsync(dGacc32.p, 0, sizeof(float) * n * n, s));
     CK(cudaMemsetAsync(dcount.p, 0, sizeof(unsigned long long) * kNQC, s));
+    if (precision != 0) CK(launch_pair_gather(dpslot.p, 1, (long long)sig.h.size(), s));
     if (!launch_jk_groups(jk, precision, split, boys, s)) return false;
+    if (precision != 0) CK(launch_pair_scatter(dpslot.p, 1, (long long)sig.h.size(), s));
     CK(launch_symmetrize(dGacc.p, dGacc32.p, d_norma, n, 0.25, dGout, s));
     // the quartet counts travel with the result; they are summed when asked for
     if (!hcount) CK(cudaHostAlloc((void **)&hcount, kNQC * sizeof(unsigned long long), cudaHostAllocDefault));
@@ -560,6 +592,13 @@ struct LibintInterface {
         t.screen = is_electron ? 1 : 0;
         t.soa32 = sig.soa32;
         t.npairs = (int)sig.h.size();
+        if (bf.Dp32) {
+          long long pe_base[kNumPairClasses];
+          pair_elements(sig.start, pe_base);
+          t.Dp32 = bf.Dp32 + pe_base[ck];
+          t.Jp32 = bf.Jp32 + pe_base[ck];
+          t.DnP32 = is_electron ? bf.DnP32 : nullptr;
+        }
         ts.add(cb, ck, t);
       }
     return true;

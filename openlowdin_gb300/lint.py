@@ -230,8 +230,9 @@ class Batch:
             raise LowdinGB300Error(f"batch set_skip({skip}) failed")
 
     def set_active(self, flags, stream: int = 0):
-        """flags[s] != 0: system s (in add order) is built by the next fock calls."""
-        f = np.ascontiguousarray(np.asarray(flags) != 0, np.int32)
+        """flags[s] (in add order): 0 = system s is not built by the next fock
+        calls, 1 = built, 2 = built with every quartet in FP64 in mixed builds."""
+        f = np.clip(np.ascontiguousarray(np.asarray(flags).astype(np.int64), np.int32), 0, 2).astype(np.int32)
         if f.size != getattr(self, "nsys", 0):
             raise ValueError(f"set_active wants {getattr(self, 'nsys', 0)} flags, got {f.size}")
         self._flags = f
