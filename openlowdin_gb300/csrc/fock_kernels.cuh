@@ -282,8 +282,8 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
 // updates of a quartet touch only rows fa.. and fb.. of the output (K13, K14
 // on the rows of shell a, K23, K24 on those of shell b) and read only those
 // rows of D, so the block keeps both in shared memory, interleaved by column
-// (Drow[col][r], Krow[col][r], r < NA + NB, padded to an even count so a
-// column's D values are one vector load), together with the largest
+// (Drow[col][r], Krow[col][r], r < NA + NB, padded to an odd pitch so that
+// random columns spread over the banks), together with the largest
 // shell-block norm of shells a and b against every shell (Dnab[s] =
 // max(|D|_{a s}, |D|_{b s})), which gives four of the six screening norms in
 // two reads.  The ket side is read from pair-indexed arrays when the build
@@ -429,24 +429,16 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
           for (int b = 0; b < NB; ++b) j12[a * NB + b] = fmaf(dcd, Iat(a, b, c, d), j12[a * NB + b]);
       }
     if (!active) continue;
-    // the D rows of the bra shells at the ket's columns (one vector read per column)
-    float dc[NC][NRP], dd[ND][NRP];
+    // the D rows of the bra shells at the ket's columns
+    float dc[NC][NR], dd[ND][NR];
 #pragma unroll
     for (int c = 0; c < NC; ++c)
 #pragma unroll
-      for (int r = 0; r < NRP; r += 2) {
-        const float2 v = *reinterpret_cast<const float2 *>(Drow + (fc + c) * NRP + r);
-        dc[c][r] = v.x;
-        dc[c][r + 1] = v.y;
-      }
+      for (int r = 0; r < NR; ++r) dc[c][r] = Drow[(fc + c) * NRP + r];
 #pragma unroll
     for (int d = 0; d < ND; ++d)
 #pragma unroll
-      for (int r = 0; r < NRP; r += 2) {
-        const float2 v = *reinterpret_cast<const float2 *>(Drow + (fd + d) * NRP + r);
-        dd[d][r] = v.x;
-        dd[d][r + 1] = v.y;
-      }
+      for (int r = 0; r < NR; ++r) dd[d][r] = Drow[(fd + d) * NRP + r];
     // J34 (ket block): D of the bra block
 #pragma unroll
     for (int c = 0; c < NC; ++c)

@@ -174,8 +174,9 @@ using JKFn = void (*)(const JKTask *, TaskLaunch);
 // output in shared memory (jk32_row_kernel), one block per bra pair
 constexpr int kRowWarps = 4;
 constexpr int kRowMaxSmem = 200 * 1024;
-// shared rows per column: the bra shells' NA + NB rows padded to an even count
-__host__ __device__ constexpr int row_pitch(int nrows) { return (nrows + 1) & ~1; }
+// shared rows per column: the bra shells' NA + NB rows padded to an odd count
+// (an odd column pitch spreads random columns over all 32 banks)
+__host__ __device__ constexpr int row_pitch(int nrows) { return nrows | 1; }
 __host__ __device__ constexpr size_t row_smem_bytes(int nrows, int n, int nsh) {
   return (size_t)(2 * row_pitch(nrows) * n + nsh) * sizeof(float);
 }
