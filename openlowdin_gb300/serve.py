@@ -133,13 +133,17 @@ def footprint_bytes(sysd, kind: str, diis_size: int = 10, mp2_budget_gb: float =
 class ServingEngine:
     def __init__(self, device="cuda", precision="fp64", split=1e-5, hbm_budget_gb=150.0, max_active=256,
                  diis_size=10, tol_energy=1e-8, tol_density=1e-6, max_iter=100, mp2_precision=None,
-                 mp2_budget_gb=8.0, skip=None, guard=True, guard_energy=1e-6, guard_commutator=1e-4):
+                 mp2_budget_gb=8.0, skip=None, guard=True, guard_energy=1e-6, guard_commutator=1e-4,
+                 tol_energy_mp2=1e-10, tol_density_mp2=1e-8):
         """guard (mixed precision): when a job converges, its matrices are
         rebuilt once in FP64 at the converged density; the FP64 energy is the
         job's result and |E_mixed - E_FP64| its stated error.  If that error
         exceeds guard_energy, or the largest element of the FP64 commutator
         X^T (FPS - SPF) X exceeds guard_commutator, the job continues in FP64
-        (every quartet in the FP64 launches, full builds) until it converges."""
+        (every quartet in the FP64 launches, full builds) until it converges.
+        SCF+MP2 jobs converge to tol_energy_mp2 / tol_density_mp2: the MP2
+        energy moves with the orbitals, and at rms(dP) < 1e-6 two converged
+        solutions of one molecule can differ by 1e-6 Eh in E2."""
         import torch
         self.torch = torch
         self.dev = torch.device(device)
@@ -151,6 +155,8 @@ class ServingEngine:
         self.diis_size = diis_size
         self.tol_energy = tol_energy
         self.tol_density = tol_density
+        self.tol_energy_mp2 = tol_energy_mp2
+        self.tol_density_mp2 = tol_density_mp2
         self.max_iter = max_iter
         self.mp2_precision = (2 if precision == "mixed" else 0) if mp2_precision is None else mp2_precision
         self.mp2_budget_gb = mp2_budget_gb
@@ -378,7 +384,10 @@ class ServingEngine:
         for q, job in enumerate(jobs):
             job.it += 1
             e, d = float(vals[0, q]), float(vals[1, q])
-            conv = abs(e - job.e_old) < self.tol_energy and d < self.tol_density
+            if job.req.kind == "scf+mp2":
+                conv = abs(e - job.e_old) < self.tol_energy_mp2 and d < self.tol_density_mp2
+            else:
+                conv = abs(e - job.e_old) < self.tol_energy and d < self.tol_density
             job.e_old = e
             job.energy = e
             if job.verify:
