@@ -166,6 +166,8 @@ class ServingEngine:
         self.stream = torch.cuda.current_stream(self.dev)
         self.mp2_stream = torch.cuda.Stream(self.dev)
         self._pool = None
+        self._gpool = None
+        self._tls = threading.local()
         # optional phase timing (set to {} before run): synchronises the device
         # at each phase boundary, so only for diagnostics
         self.trace = None
@@ -208,40 +210,81 @@ class ServingEngine:
         return self._density_collect(self._density_submit(items))
 
     def _density_submit(self, items):
-        """Start eta C_occ C_occ^T for a list of (species, F): small matrices are
-        diagonalised by LAPACK on the host pool (one transfer, futures returned
-        at once so the host work overlaps later GPU work), large ones by the
-        GPU solver."""
+        """Start eta C_occ C_occ^T for a list of (species, F) without waiting
+        for the GPU: X^T F X is queued on the engine's stream; matrices below
+        HOST_EIGH_MAX functions go to the host pool as one pinned copy (a pool
+        thread waits for the copy's event, then runs LAPACK), larger ones to a
+        GPU worker thread that runs the FP64 eigensolver and the density on its
+        own stream after an event of the engine's stream.  The caller can queue
+        the other cohort's Fock build at once: it overlaps these eigensolves."""
         torch = self.torch
+        main = self.stream
         out = [None] * len(items)
-        host_idx, host_mats = [], []
+        host_idx, host_mats, gpu_futs = [], [], {}
         for i, (s, F) in enumerate(items):
             Fp = s.X.T @ F @ s.X
             if s.n >= HOST_EIGH_MAX:
-                e, Cp = torch.linalg.eigh(Fp)
-                Co = s.X @ Cp[:, :s.occ]
-                out[i] = s.eta * Co @ Co.T
+                ev = torch.cuda.Event()
+                ev.record(main)
+                gpu_futs[i] = self._gpu_pool().submit(self._gpu_density, s, Fp, ev)
             else:
                 host_idx.append(i)
                 host_mats.append(Fp)
         futs = []
         if host_idx:
             sizes = [m.numel() for m in host_mats]
-            flat = torch.cat([m.reshape(-1) for m in host_mats]).cpu().numpy()
+            flat = torch.cat([m.reshape(-1) for m in host_mats])
+            pinned = torch.empty(flat.shape, dtype=flat.dtype, pin_memory=True)
+            pinned.copy_(flat, non_blocking=True)
+            ready = torch.cuda.Event()
+            ready.record(main)
             offs = np.cumsum([0] + sizes)
 
             def work(j):
+                ready.synchronize()
                 i = host_idx[j]
                 n = items[i][0].n
-                w, V = np.linalg.eigh(flat[offs[j]:offs[j + 1]].reshape(n, n))
+                w, V = np.linalg.eigh(pinned.numpy()[offs[j]:offs[j + 1]].reshape(n, n))
                 return np.ascontiguousarray(V[:, :items[i][0].occ])
 
             futs = [self._host_pool().submit(work, j) for j in range(len(host_idx))]
-        return items, out, host_idx, futs
+        return items, out, host_idx, futs, gpu_futs
+
+    def _gpu_density(self, s, Fp, ev):
+        """eta C_occ C_occ^T of one large species on a worker stream (FP64
+        eigensolver), after event ev of the engine's stream."""
+        torch = self.torch
+        side = self._side_stream()
+        with torch.cuda.stream(side):
+            side.wait_event(ev)
+            Fp.record_stream(side)
+            e, Cp = torch.linalg.eigh(Fp)
+            Co = s.X @ Cp[:, :s.occ]
+            P = s.eta * Co @ Co.T
+            done = torch.cuda.Event()
+            done.record(side)
+        return P, done
+
+    def _side_stream(self):
+        loc = self._tls
+        if not hasattr(loc, "stream"):
+            loc.stream = self.torch.cuda.Stream(self.dev)
+        return loc.stream
+
+    def _gpu_pool(self):
+        import concurrent.futures as cf
+        if self._gpool is None:
+            self._gpool = cf.ThreadPoolExecutor(max_workers=2)
+        return self._gpool
 
     def _density_collect(self, pending):
         torch = self.torch
-        items, out, host_idx, futs = pending
+        items, out, host_idx, futs, gpu_futs = pending
+        for i, f in gpu_futs.items():
+            P, done = f.result()
+            self.stream.wait_event(done)
+            P.record_stream(self.stream)
+            out[i] = P
         if host_idx:
             vecs = [f.result() for f in futs]
             allv = torch.from_numpy(np.concatenate([v.reshape(-1) for v in vecs])).to(self.dev, non_blocking=True)
