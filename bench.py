@@ -646,6 +646,8 @@ def main():
     reqs = serving_requests(args.steps, args.serve_rate, seed=args.seed + rank)
     warm = serving_requests(max(1, args.warmup), 1000.0, seed=9, hi=300)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    from openlowdin_gb300 import serve
+    serve.warm_up()                   # GPU eigensolver set-up in its worker threads
     for prec in ("mixed", "fp64"):
         serve_stream(warm, prec)      # untimed warm-up requests
 

@@ -109,6 +109,52 @@ class _Job:
     guard_hit: bool = False
 
 
+_POOLS = None
+_TLS = threading.local()
+_POOL_LOCK = threading.Lock()
+
+
+def _pools():
+    """(host LAPACK pool, GPU eigensolver pool), shared by every engine of the
+    process: one BLAS thread per host worker; the GPU workers each use their
+    own CUDA stream."""
+    global _POOLS
+    with _POOL_LOCK:
+        if _POOLS is None:
+            import concurrent.futures as cf
+            import os
+            _POOLS = (cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1))),
+                      cf.ThreadPoolExecutor(max_workers=2))
+    return _POOLS
+
+
+def _side_stream(dev):
+    if not hasattr(_TLS, "stream"):
+        import torch
+        _TLS.stream = torch.cuda.Stream(dev)
+    return _TLS.stream
+
+
+def warm_up(device="cuda"):
+    """Runs the GPU eigensolver once in every GPU worker thread (its library
+    set-up and first-use kernel loading happen here, not in a served job)."""
+    import torch
+    dev = torch.device(device)
+
+    def one():
+        s = _side_stream(dev)
+        with torch.cuda.stream(s):
+            a = torch.eye(400, dtype=torch.float64, device=dev) + 1e-3
+            torch.linalg.eigh(a)
+        s.synchronize()
+        return True
+
+    pool = _pools()[1]
+    futs = [pool.submit(one) for _ in range(4)]
+    for f in futs:
+        f.result()
+
+
 def footprint_bytes(sysd, kind: str, diis_size: int = 10, mp2_budget_gb: float = 8.0) -> float:
     """Device bytes a job holds while active: per species 11 n^2 matrices plus
     2 * diis_size history matrices (FP64), the handle's pair data, and for
@@ -165,9 +211,6 @@ class ServingEngine:
         self.guard_commutator = guard_commutator
         self.stream = torch.cuda.current_stream(self.dev)
         self.mp2_stream = torch.cuda.Stream(self.dev)
-        self._pool = None
-        self._gpool = None
-        self._tls = threading.local()
         # optional phase timing (set to {} before run): synchronises the device
         # at each phase boundary, so only for diagnostics
         self.trace = None
@@ -183,11 +226,7 @@ class ServingEngine:
 
     # ------------------------------------------------------------ helpers --
     def _host_pool(self):
-        import concurrent.futures as cf
-        import os
-        if self._pool is None:
-            self._pool = cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)))
-        return self._pool
+        return _pools()[0]
 
     def _new_job(self, req: Request, now: float, footprint: float) -> _Job:
         torch = self.torch
@@ -266,16 +305,10 @@ class ServingEngine:
         return P, done
 
     def _side_stream(self):
-        loc = self._tls
-        if not hasattr(loc, "stream"):
-            loc.stream = self.torch.cuda.Stream(self.dev)
-        return loc.stream
+        return _side_stream(self.dev)
 
     def _gpu_pool(self):
-        import concurrent.futures as cf
-        if self._gpool is None:
-            self._gpool = cf.ThreadPoolExecutor(max_workers=2)
-        return self._gpool
+        return _pools()[1]
 
     def _density_collect(self, pending):
         torch = self.torch
@@ -468,9 +501,12 @@ class ServingEngine:
             item = inbox.get()
             if item is None:
                 return
-            job, C, eps, P = item
+            job, Fp, Pd, ev = item
             try:
-                self._mp2_one(job, C, eps, P, results, start)
+                ev.synchronize()
+                eps, V = np.linalg.eigh(Fp.cpu().numpy())
+                C = job.sp[0].X.cpu().numpy() @ V
+                self._mp2_one(job, C, eps, Pd.cpu().numpy(), results, start)
             finally:
                 with self._lock:
                     self._used -= job.footprint
@@ -526,12 +562,13 @@ class ServingEngine:
                         cohorts[c].remove(job)
                         dirty[c] = True
                 if job.req.kind == "scf+mp2":
+                    # the final orbitals are computed by the MP2 worker: the
+                    # loop only queues the transformed Fock matrix and an event
                     sp0 = job.sp[0]
-                    Fp = (sp0.X.T @ sp0.Flast @ sp0.X).cpu().numpy()
-                    w, V = np.linalg.eigh(Fp)
-                    C = sp0.X.cpu().numpy() @ V
-                    torch.cuda.current_stream(self.dev).synchronize()
-                    inbox.put((job, C, w, sp0.P.cpu().numpy()))
+                    Fp = sp0.X.T @ sp0.Flast @ sp0.X
+                    ev = torch.cuda.Event()
+                    ev.record(self.stream)
+                    inbox.put((job, Fp, sp0.P.clone(), ev))
                 else:
                     results.append(self._finish(job, None, start))
                     with self._lock:
@@ -557,9 +594,14 @@ class ServingEngine:
                             break
                         self._used += fp
                     self._tick("other")
-                    cohorts[c].append(self._new_job(req, now, fp))
+                    job = self._new_job(req, now, fp)
+                    # the cohort with less work (sum of n^3) takes the job, so
+                    # both cohorts have GPU work to overlap the other's eigensolves
+                    work = [sum(sum(x.n ** 3 for x in j.sp) for j in cohorts[k]) for k in (0, 1)]
+                    k = 0 if work[0] <= work[1] else 1
+                    cohorts[k].append(job)
                     self._tick("admit")
-                    dirty[c] = True
+                    dirty[k] = True
                     nact += 1
                     pi += 1
                 if not cohorts[c]:
