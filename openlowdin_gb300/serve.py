@@ -135,11 +135,28 @@ def _side_stream(dev):
     return _TLS.stream
 
 
+_LINALG_READY = False
+
+
+def _load_linalg(dev):
+    """torch loads its CUDA linear-algebra library on the first eigensolve,
+    and that first call must not happen in two threads at once: make it
+    once, here, under a lock."""
+    global _LINALG_READY
+    with _POOL_LOCK:
+        if not _LINALG_READY:
+            import torch
+            torch.linalg.eigh(torch.eye(4, dtype=torch.float64, device=dev))
+            torch.cuda.synchronize(dev)
+            _LINALG_READY = True
+
+
 def warm_up(device="cuda"):
     """Runs the GPU eigensolver once in every GPU worker thread (its library
     set-up and first-use kernel loading happen here, not in a served job)."""
     import torch
     dev = torch.device(device)
+    _load_linalg(dev)
 
     def one():
         s = _side_stream(dev)
@@ -210,6 +227,7 @@ class ServingEngine:
         self.guard_energy = guard_energy
         self.guard_commutator = guard_commutator
         self.stream = torch.cuda.current_stream(self.dev)
+        _load_linalg(self.dev)
         self.mp2_stream = torch.cuda.Stream(self.dev)
         # optional phase timing (set to {} before run): synchronises the device
         # at each phase boundary, so only for diagnostics
