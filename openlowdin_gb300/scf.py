@@ -103,6 +103,38 @@ def _orthogonaliser(S, cut=1e-8, host_max=384):
     return U[:, keep] / torch.sqrt(w[keep])
 
 
+def occupied_subspace(Fp, occ, passes=2):
+    """Orthonormal basis of the occupied subspace (the occ lowest eigenvectors)
+    of a symmetric FP64 matrix Fp, from an FP32 eigensolve refined in FP64:
+    each pass re-orthonormalises the occupied and virtual blocks (Cholesky of
+    their overlaps), forms A_ov = C_o^T Fp C_v and the diagonals of the two
+    blocks in FP64, and rotates by the first-order occupied-virtual mixing
+    X_ia = A_ia / (d_a - d_i) (Rayleigh-Ritz / Jacobi correction of an
+    invariant subspace).  The error of the subspace falls quadratically: two
+    passes from FP32 vectors reach the FP64 eigensolver's occupied projector
+    to ~1e-14 for Fock matrices whose occupied-virtual gap is > ~1e-3 of
+    their spectral range.  Degeneracies inside the occupied or the virtual
+    block need no resolution (the projector does not depend on them).
+    Returns C_o (n x occ, FP64)."""
+    import torch
+    _, V32 = torch.linalg.eigh(Fp.to(torch.float32))
+    V = V32.to(torch.float64)
+    Vo, Vv = V[:, :occ], V[:, occ:]
+    for _ in range(passes):
+        Lo = torch.linalg.cholesky(Vo.T @ Vo)
+        Vo = torch.linalg.solve_triangular(Lo, Vo.T, upper=False).T
+        Vv = Vv - Vo @ (Vo.T @ Vv)
+        Lv = torch.linalg.cholesky(Vv.T @ Vv)
+        Vv = torch.linalg.solve_triangular(Lv, Vv.T, upper=False).T
+        FVo, FVv = Fp @ Vo, Fp @ Vv
+        do = torch.sum(Vo * FVo, dim=0)
+        dv = torch.sum(Vv * FVv, dim=0)
+        Xm = (Vo.T @ FVv) / (dv[None, :] - do[:, None])
+        Vo, Vv = Vo - Vv @ Xm.T, Vv + Vo @ Xm
+    Lo = torch.linalg.cholesky(Vo.T @ Vo)
+    return torch.linalg.solve_triangular(Lo, Vo.T, upper=False).T
+
+
 def _orthogonaliser_np(S, cut=1e-8):
     w, U = np.linalg.eigh(S)
     keep = w > cut

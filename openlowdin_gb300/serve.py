@@ -30,7 +30,7 @@ import numpy as np
 
 from . import lint
 from .batch_scf import MIXED_SKIP
-from .scf import _one_body_device, _orthogonaliser, n_occ, nuclear_repulsion
+from .scf import _one_body_device, _orthogonaliser, n_occ, nuclear_repulsion, occupied_subspace
 from .systems import n_core
 
 HOST_EIGH_MAX = 384
@@ -161,10 +161,14 @@ def warm_up(device="cuda"):
     def one():
         s = _side_stream(dev)
         with torch.cuda.stream(s):
-            a = torch.eye(400, dtype=torch.float64, device=dev) + 1e-3
-            torch.linalg.eigh(a)
+            for n in (400, 800, 1200):
+                a = torch.eye(n, dtype=torch.float64, device=dev) + 1e-3
+                torch.linalg.eigh(a)
+                torch.linalg.eigh(a.float())
         s.synchronize()
         return True
+
+    one()
 
     pool = _pools()[1]
     futs = [pool.submit(one) for _ in range(4)]
@@ -197,7 +201,7 @@ class ServingEngine:
     def __init__(self, device="cuda", precision="fp64", split=1e-5, hbm_budget_gb=150.0, max_active=256,
                  diis_size=10, tol_energy=1e-8, tol_density=1e-6, max_iter=100, mp2_precision=None,
                  mp2_budget_gb=8.0, skip=None, guard=True, guard_energy=1e-6, guard_commutator=1e-4,
-                 tol_energy_mp2=1e-10, tol_density_mp2=1e-8):
+                 tol_energy_mp2=1e-10, tol_density_mp2=1e-8, refine_eigh=None):
         """guard (mixed precision): when a job converges, its matrices are
         rebuilt once in FP64 at the converged density; the FP64 energy is the
         job's result and |E_mixed - E_FP64| its stated error.  If that error
@@ -206,7 +210,12 @@ class ServingEngine:
         (every quartet in the FP64 launches, full builds) until it converges.
         SCF+MP2 jobs converge to tol_energy_mp2 / tol_density_mp2: the MP2
         energy moves with the orbitals, and at rms(dP) < 1e-6 two converged
-        solutions of one molecule can differ by 1e-6 Eh in E2."""
+        solutions of one molecule can differ by 1e-6 Eh in E2.
+        refine_eigh (default: mixed precision): densities of species of at
+        least HOST_EIGH_MAX functions from an FP32 eigensolve whose occupied
+        subspace is refined in FP64 (scf.occupied_subspace) instead of the
+        FP64 eigensolver; the job's final orbitals always come from the FP64
+        eigensolver."""
         import torch
         self.torch = torch
         self.dev = torch.device(device)
@@ -224,6 +233,7 @@ class ServingEngine:
         self.mp2_precision = (2 if precision == "mixed" else 0) if mp2_precision is None else mp2_precision
         self.mp2_budget_gb = mp2_budget_gb
         self.guard = guard and precision == "mixed"
+        self.refine_eigh = (precision == "mixed") if refine_eigh is None else bool(refine_eigh)
         self.guard_energy = guard_energy
         self.guard_commutator = guard_commutator
         self.stream = torch.cuda.current_stream(self.dev)
@@ -315,8 +325,13 @@ class ServingEngine:
         with torch.cuda.stream(side):
             side.wait_event(ev)
             Fp.record_stream(side)
-            e, Cp = torch.linalg.eigh(Fp)
-            Co = s.X @ Cp[:, :s.occ]
+            if self.refine_eigh:
+                # mixed precision: FP32 eigensolve, FP64 refinement of the
+                # occupied subspace (scf.occupied_subspace)
+                Co = s.X @ occupied_subspace(Fp, s.occ)
+            else:
+                e, Cp = torch.linalg.eigh(Fp)
+                Co = s.X @ Cp[:, :s.occ]
             P = s.eta * Co @ Co.T
             done = torch.cuda.Event()
             done.record(side)

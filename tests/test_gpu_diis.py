@@ -70,3 +70,23 @@ def test_device_boys_functions_against_incomplete_gamma(L):
                           (2 * np.maximum(T, 1e-300) ** (m + 0.5)))
             rel = np.max(np.abs(F[:, m] - ex) / ex)
             assert rel < tol, (fp32, m, rel)
+
+
+@pytest.mark.parametrize("n,occ", [(200, 60), (600, 150)])
+def test_occupied_subspace_matches_fp64_eigensolver(n, occ):
+    """FP32 eigensolve + FP64 refinement of the occupied subspace gives the
+    FP64 eigensolver's density projector (a Fock-like spectrum: degenerate
+    core levels, a 0.05 Eh gap, virtuals up to 300 Eh)."""
+    torch = pytest.importorskip("torch")
+    from openlowdin_gb300.scf import occupied_subspace
+    rng = np.random.default_rng(n)
+    ev = np.concatenate([np.full(10, -20.0) + rng.normal(size=10) * 1e-3,
+                         -np.sort(rng.uniform(0.3, 1.5, occ - 10)),
+                         -0.25 + np.zeros(0), np.sort(rng.uniform(-0.2, 300, n - occ))])
+    Q, _ = np.linalg.qr(rng.normal(size=(n, n)))
+    F = torch.tensor((Q * ev) @ Q.T, device="cuda")
+    Co = occupied_subspace(F, occ)
+    w, V = torch.linalg.eigh(F)
+    P, Pe = Co @ Co.T, V[:, :occ] @ V[:, :occ].T
+    assert float((P - Pe).abs().max()) < 1e-11
+    assert float((Co.T @ Co - torch.eye(occ, dtype=Co.dtype, device="cuda")).abs().max()) < 1e-12
