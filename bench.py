@@ -240,12 +240,14 @@ def serving_requests(n, rate, seed=0, lo=STREAM_LO, hi=STREAM_HI, mp2_frac=MP2_F
     return reqs
 
 
-def serve_stream(reqs, precision, flush=None):
+def serve_stream(reqs, precision, flush=None, engines=None):
     """Serve `reqs` in real time with one engine; returns (results, seconds,
     CUDA-event milliseconds, kernels launched)."""
     import torch
     from openlowdin_gb300 import lint, serve
     eng = serve.ServingEngine(precision=precision)
+    if engines is not None:
+        engines.append(eng)
     if flush is not None:
         flush.fill_(1.0)              # L2 flush before the timed stream
     torch.cuda.synchronize()
@@ -271,6 +273,27 @@ def stream_summary(res, wall, reqs, rate):
             "p50_s": lat["p50_s"], "p99_s": lat["p99_s"], "offered_rate_req_s": rate,
             "arrival_span_s": span, "served_rate_req_s": len(conv) / wall,
             "iterations_mean": float(sum(x.iterations for x in res) / max(1, len(res)))}
+
+
+def tuning_summary(tuning):
+    """Per quartet class of the mixed builds: how often the autotuner kept the
+    bra-row FP32 kernel or the one-quartet-per-thread one, and the median
+    timings (ms) of both where they were timed."""
+    import numpy as np
+    names = ["ss", "ps", "pp", "ds", "dp", "dd"]
+    out = {}
+    for b in range(6):
+        for k in range(b + 1):
+            ch = [int(t[0][b, k]) for t in tuning if t[0][b, k] >= 0]
+            if not ch:
+                continue
+            ra = [float(t[1][b, k]) for t in tuning if t[1][b, k] > 0]
+            tl = [float(t[2][b, k]) for t in tuning if t[2][b, k] > 0]
+            out[f"({names[b]}|{names[k]})"] = {
+                "rows_kernel": ch.count(1), "tile_kernel": ch.count(0),
+                "median_ms_rows": float(np.median(ra)) if ra else None,
+                "median_ms_tiles": float(np.median(tl)) if tl else None}
+    return {"batches": len(tuning), "classes": out}
 
 
 def per_job_table(reqs, plain, mixed):
@@ -655,7 +678,8 @@ def main():
     barrier()
     clk = ClockSampler(local)
     clk.start()
-    res_m, wall_m, ms_m, launches = serve_stream(reqs, "mixed", flush)
+    engs = []
+    res_m, wall_m, ms_m, launches = serve_stream(reqs, "mixed", flush, engs)
     clocks = clk.stop()
     barrier()
     # the plain FP64 engine on the same requests
@@ -702,6 +726,7 @@ def main():
                        "max_err_vs_fp64_check_Eh": max(chk) if chk else None,
                        "max_abs_dE2_mixed_vs_plain_Eh": max(de2) if de2 else None,
                        "guard_hits": int(sum(bool(r.get("guard_hit")) for r in table)),
+                       "autotune": tuning_summary(engs[0].tuning),
                        "per_job": table},
            "clocks": clocks, "gpu_launches": int(launches)}
 

@@ -210,6 +210,17 @@ int LowdinGB300_batch_fock(LowdinGB300_Batch *b, int precision, double split, vo
    quartets the change can move by more than `skip`.  Default 0 (only the
    screening of the plain build). */
 int LowdinGB300_batch_set_skip(LowdinGB300_Batch *b, double skip);
+/* Autotuner of the mixed builds (no counterpart in the reference): for every
+   quartet class whose FP32 half can run on either FP32 kernel (one bra pair
+   per block with its exchange rows in shared memory, or one quartet per
+   thread), times both on the batch's current densities and keeps the faster
+   for the following batch_fock calls (split: the mixed build's split).
+   Choices are cached in the process by (class, size bucket); force = 1
+   re-times.  Both kernels take the same quartets.  Synchronises `stream`.
+   batch_tuning reports the 36 per-class choices (-1 not tuned, 0 one quartet
+   per thread, 1 bra rows) and the two timings (ms, -1 where not timed). */
+int LowdinGB300_batch_autotune(LowdinGB300_Batch *b, double split, int force, void *stream);
+int LowdinGB300_batch_tuning(LowdinGB300_Batch *b, int *choice, float *ms_rows, float *ms_tiles);
 /* batch_fock replays a CUDA graph of its launch sequence (captured once per
    precision mode after a first eager build; default on); 0 launches eagerly. */
 int LowdinGB300_batch_use_graph(LowdinGB300_Batch *b, int on);

@@ -484,6 +484,10 @@ class BatchSCF:
                 g.Pin.index_copy_(0, g.alive, src)
             else:
                 g.Pin.copy_(src)
+        if mixed and not getattr(self, "_tuned", False):
+            # FP32 kernel per quartet class, timed on these densities
+            self.batch.autotune(self.split, stream=st.stream)
+            self._tuned = True
         # precision bits: 1 = two-particle FP32/FP64 split, 2 = coupling split
         self.batch.fock(3 if mixed else 0, self.split, st.stream)
         self._tick(st, "fock")

@@ -2,6 +2,9 @@
 // matrices from one fixed sequence of launches, replayed from a CUDA graph.
 #include "lint_host.cuh"
 
+#include <map>
+#include <tuple>
+
 // ================================================================== batches
 // A batch holds many molecular systems (each a list of species handles) whose
 // two-particle and coupling builds run together: every species' density
@@ -55,6 +58,16 @@ struct LowdinGB300_Batch {
   cudaStream_t capture = nullptr;
   bool use_graph = true;
   long long calls = 0;
+  // FP32 kernel of the mixed launches per quartet class (autotune): -1 size
+  // rule, 0 jk_tasks_kernel, 1 bra-row kernel; the timings behind the choice
+  signed char rows_choice[kNQC];
+  float tune_ms[kNQC][2];
+  LowdinGB300_Batch() {
+    for (int c = 0; c < kNQC; ++c) {
+      rows_choice[c] = -1;
+      tune_ms[c][0] = tune_ms[c][1] = -1.f;
+    }
+  }
 
   ~LowdinGB300_Batch() {
     drop_graphs();
@@ -258,6 +271,82 @@ struct LowdinGB300_Batch {
     return true;
   }
 
+  // Autotuner: for every quartet class whose FP32 half can run on either
+  // FP32 kernel, time both on this batch's current densities (the FP32
+  // launch alone, after one untimed launch) and keep the faster.  Choices are
+  // cached process-wide by (class, log2 of the class's bra x ket pairs, log2
+  // of the largest species), so batches of similar molecules reuse them;
+  // `force` re-times.  Both kernels take the same quartets, so the choice
+  // changes only the order of FP32 additions.
+  bool autotune(double split, bool force, cudaStream_t s) {
+    if (!finalized) {
+      set_error("batch_autotune: batch not finalised");
+      return false;
+    }
+    if (tasks_dirty) {
+      if (!jk.upload(s, active.p, &on) || !cp.upload(s, active.p, &on)) return false;
+      drop_graphs();
+      tasks_dirty = false;
+    }
+    CK(cudaMemsetAsync(Dn.p, 0, Dn.n * sizeof(double), s));
+    CK(cudaMemsetAsync(Dn32.p, 0, Dn32.n * sizeof(float), s));
+    CK(launch_prepare_batch(slots.p, nslots, total, s));
+    if (npslots) CK(launch_pair_gather(pslots.p, npslots, ptotal, s));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    bool ok = true;
+    for (int c = 0; c < kNQC && ok; ++c) {
+      const int cb = c / kNumPairClasses, ck = c % kNumPairClasses;
+      if (!jk.cnt[c] || !jk_rows_used(cb, ck, jk.rn[c], jk.rnsh[c])) continue;
+      double work = 0;
+      for (const auto &t : jk.group[c]) work += (double)t.nbra * t.nket;
+      const auto key = std::make_tuple(c, (int)std::log2(std::max(1.0, work)), (int)std::log2(std::max(1, jk.rn[c])));
+      if (!force) {
+        std::lock_guard<std::mutex> lk(tune_mu());
+        auto it = tune_cache().find(key);
+        if (it != tune_cache().end()) {
+          rows_choice[c] = it->second;
+          continue;
+        }
+      }
+      float ms[2] = {0.f, 0.f};
+      for (int v = 1; v >= 0 && ok; --v) {
+        signed char pref[kNQC];
+        for (int k = 0; k < kNQC; ++k) pref[k] = (signed char)v;
+        ok = LibintInterface::launch_jk_groups(jk, 1, split, boys, s, skip, pref, c, true);
+        if (!ok) break;
+        if (cudaEventRecord(e0, s) != cudaSuccess) ok = false;
+        for (int r = 0; r < 2 && ok; ++r) ok = LibintInterface::launch_jk_groups(jk, 1, split, boys, s, skip, pref, c, true);
+        if (ok && (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                   cudaEventElapsedTime(&ms[v], e0, e1) != cudaSuccess))
+          ok = false;
+      }
+      if (!ok) break;
+      tune_ms[c][1] = ms[1] / 2;
+      tune_ms[c][0] = ms[0] / 2;
+      rows_choice[c] = ms[1] <= ms[0] ? 1 : 0;
+      std::lock_guard<std::mutex> lk(tune_mu());
+      tune_cache()[key] = rows_choice[c];
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!ok) {
+      set_error("batch_autotune: a timed launch failed");
+      return false;
+    }
+    drop_graphs();
+    return true;
+  }
+  static std::mutex &tune_mu() {
+    static std::mutex m;
+    return m;
+  }
+  static std::map<std::tuple<int, int, int>, signed char> &tune_cache() {
+    static std::map<std::tuple<int, int, int>, signed char> m;
+    return m;
+  }
+
   // every launch of one build, in stream order
   bool fock_sequence(int precision, double split, cudaStream_t s) {
     CK(cudaMemsetAsync(Dn.p, 0, Dn.n * sizeof(double), s));
@@ -266,7 +355,8 @@ struct LowdinGB300_Batch {
     CK(launch_prepare_batch(slots.p, nslots, total, s));
     const int jk_mixed = precision & 1;
     if (jk_mixed && npslots) CK(launch_pair_gather(pslots.p, npslots, ptotal, s));
-    if (!LibintInterface::launch_jk_groups(jk, jk_mixed, jk_mixed ? split : 0.0, boys, s, skip)) return false;
+    if (!LibintInterface::launch_jk_groups(jk, jk_mixed, jk_mixed ? split : 0.0, boys, s, skip, rows_choice))
+      return false;
     if (jk_mixed && npslots) CK(launch_pair_scatter(pslots.p, npslots, ptotal, s));
     if (!launch_cp_groups(cp, (precision & 2) ? 2 : 0, split, boys, s, skip)) return false;
     CK(launch_finalize_batch(slots.p, nslots, total, s));
@@ -344,6 +434,21 @@ int LowdinGB300_batch_finalize(LowdinGB300_Batch *b, void *stream) {
 int LowdinGB300_batch_fock(LowdinGB300_Batch *b, int precision, double split, void *stream) {
   if (!b) return -1;
   return b->fock(precision, split, (cudaStream_t)stream) ? 0 : -1;
+}
+
+int LowdinGB300_batch_autotune(LowdinGB300_Batch *b, double split, int force, void *stream) {
+  if (!b) return -1;
+  return b->autotune(split, force != 0, (cudaStream_t)stream) ? 0 : -1;
+}
+
+int LowdinGB300_batch_tuning(LowdinGB300_Batch *b, int *choice, float *ms_rows, float *ms_tiles) {
+  if (!b) return -1;
+  for (int c = 0; c < kNQC; ++c) {
+    if (choice) choice[c] = b->rows_choice[c];
+    if (ms_rows) ms_rows[c] = b->tune_ms[c][1];
+    if (ms_tiles) ms_tiles[c] = b->tune_ms[c][0];
+  }
+  return kNQC;
 }
 
 int LowdinGB300_batch_use_graph(LowdinGB300_Batch *b, int on) {

@@ -391,7 +391,7 @@ cudaError_t launch_jk_tasks(int pcb, int pck, bool fp32, const JKTask *dtasks, c
                             cudaStream_t s) {
   if (!class_supported(pcb, pck)) return cudaErrorNotSupported;
   if (tl.ntasks <= 0 || tl.nblocks <= 0) return cudaSuccess;
-  if (fp32 && tl.mixed && tl.lower && jk_rows_used(pcb, pck, tl.rows_n, tl.rows_nsh)) {
+  if (fp32 && tl.mixed && tl.lower && tl.rows_pref != 0 && jk_rows_used(pcb, pck, tl.rows_n, tl.rows_nsh)) {
     // the FP32 half of a mixed build: bra-row kernel
     const JKFn r = kJKR[pcb][pck];
     const size_t smem = row_smem_bytes(ncart(pc_la(pcb)) + ncart(pc_lb(pcb)), tl.rows_n, tl.rows_nsh);

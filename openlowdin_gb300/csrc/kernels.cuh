@@ -148,6 +148,7 @@ struct TaskLaunch {
   int nblocks;            // total flattened blocks
   int nrblocks;           // bra-row launches: total bra pairs of the tasks
   int rows_n, rows_nsh;   // bra-row launches: largest basis and shell count of the tasks
+  int rows_pref;          // FP32 half of a mixed launch: -1 size rule, 0 jk_tasks_kernel, 1 bra-row kernel
   double eps;             // screening threshold
   double split;           // mixed precision: quartets with bound >= split run in FP64
   int lower;              // 1: this launch takes the quartets below split

@@ -604,11 +604,16 @@ struct LibintInterface {
     return true;
   }
 
+  // rows: per quartet class the FP32 kernel of mixed launches (-1 size rule,
+  // 0 jk_tasks_kernel, 1 bra-row kernel; null: size rule); only: a single
+  // class (-1: all) and, with lower_only, only its FP32 launch (autotuning)
   static bool launch_jk_groups(const TaskSet<JKTask> &ts, int precision, double split, BoysTables boys,
-                               cudaStream_t s, double skip = 0.0) {
+                               cudaStream_t s, double skip = 0.0, const signed char *rows = nullptr,
+                               int only = -1, bool lower_only = false) {
     for (int c = 0; c < kNQC; ++c) {
-      if (!ts.cnt[c]) continue;
+      if (!ts.cnt[c] || (only >= 0 && c != only)) continue;
       TaskLaunch tl{};
+      tl.rows_pref = rows ? rows[c] : -1;
       tl.ntasks = ts.cnt[c];
       tl.nblocks = ts.nblk[c];
       tl.nrblocks = ts.nrblk[c];
@@ -627,7 +632,7 @@ struct LibintInterface {
         tl.split = split;
         set_fp32_copies(tl);
         tl.lower = 0;
-        CK(launch_jk_tasks(cb, ck, false, ts.d + ts.off[c], tl, s));
+        if (!lower_only) CK(launch_jk_tasks(cb, ck, false, ts.d + ts.off[c], tl, s));
         tl.lower = 1;
         CK(launch_jk_tasks(cb, ck, true, ts.d + ts.off[c], tl, s));
       }

@@ -100,6 +100,12 @@ def lib():
         L.LowdinGB300_mp2_coupling.restype = ctypes.c_int
         L.LowdinGB300_diis_coefficients.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]
         L.LowdinGB300_diis_coefficients.restype = ctypes.c_int
+        L.LowdinGB300_batch_autotune.argtypes = [_vp, ctypes.c_double, ctypes.c_int, _vp]
+        L.LowdinGB300_batch_autotune.restype = ctypes.c_int
+        L.LowdinGB300_batch_tuning.argtypes = [_vp, np.ctypeslib.ndpointer(dtype=np.int32),
+                                               np.ctypeslib.ndpointer(dtype=np.float32),
+                                               np.ctypeslib.ndpointer(dtype=np.float32)]
+        L.LowdinGB300_batch_tuning.restype = ctypes.c_int
         L.LowdinGB300_boys_eval.argtypes = [ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int, _f64p]
         L.LowdinGB300_boys_eval.restype = ctypes.c_int
         L.LowdinGB300_gemm_bf16_split.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -160,7 +166,8 @@ EXPORTED_SYMBOLS = [
     "LowdinGB300_twobody_device_noalloc", "LowdinGB300_mp2_direct", "LowdinGB300_mp2_last_columns", "LowdinGB300_mp2_coupling",
     "LowdinGB300_gemm_bf16_split", "LowdinGB300_gemm_bf16_precise",
     "LowdinGB300_gemm_bench", "LowdinGB300_mp2_moint", "LowdinGB300_mp2_coupling_moint", "LowdinGB300_moint_write",
-    "LowdinGB300_diis_coefficients", "LowdinGB300_boys_eval",
+    "LowdinGB300_diis_coefficients", "LowdinGB300_boys_eval", "LowdinGB300_batch_autotune",
+    "LowdinGB300_batch_tuning",
 ]
 
 
@@ -244,6 +251,22 @@ class Batch:
         if lib().LowdinGB300_batch_finalize(self.h, stream) != 0:
             _check()
             raise LowdinGB300Error("batch finalize failed")
+
+    def autotune(self, split: float = 1e-5, force: bool = False, stream: int = 0):
+        """Pick the faster FP32 kernel per quartet class for mixed builds
+        (LowdinGB300_batch_autotune)."""
+        if lib().LowdinGB300_batch_autotune(self.h, float(split), int(bool(force)), stream) != 0:
+            _check()
+            raise LowdinGB300Error("batch autotune failed")
+
+    def tuning(self):
+        """(choice [6, 6], ms bra-row kernel [6, 6], ms one-quartet-per-thread
+        kernel [6, 6]) of the last autotune."""
+        ch = np.zeros(36, np.int32)
+        a = np.zeros(36, np.float32)
+        b = np.zeros(36, np.float32)
+        lib().LowdinGB300_batch_tuning(self.h, ch, a, b)
+        return ch.reshape(6, 6), a.reshape(6, 6), b.reshape(6, 6)
 
     def use_graph(self, on: bool):
         lib().LowdinGB300_batch_use_graph(self.h, int(bool(on)))

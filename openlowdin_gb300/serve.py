@@ -201,7 +201,7 @@ class ServingEngine:
     def __init__(self, device="cuda", precision="fp64", split=1e-5, hbm_budget_gb=150.0, max_active=256,
                  diis_size=10, tol_energy=1e-8, tol_density=1e-6, max_iter=100, mp2_precision=None,
                  mp2_budget_gb=8.0, skip=None, guard=True, guard_energy=1e-6, guard_commutator=1e-4,
-                 tol_energy_mp2=1e-10, tol_density_mp2=1e-8, refine_eigh=None):
+                 tol_energy_mp2=1e-10, tol_density_mp2=1e-8, refine_eigh=None, autotune=True):
         """guard (mixed precision): when a job converges, its matrices are
         rebuilt once in FP64 at the converged density; the FP64 energy is the
         job's result and |E_mixed - E_FP64| its stated error.  If that error
@@ -215,7 +215,8 @@ class ServingEngine:
         least HOST_EIGH_MAX functions from an FP32 eigensolve whose occupied
         subspace is refined in FP64 (scf.occupied_subspace) instead of the
         FP64 eigensolver; the job's final orbitals always come from the FP64
-        eigensolver."""
+        eigensolver.  autotune (mixed): each new cohort batch picks its FP32
+        kernel per quartet class by timing (LowdinGB300_batch_autotune)."""
         import torch
         self.torch = torch
         self.dev = torch.device(device)
@@ -234,6 +235,8 @@ class ServingEngine:
         self.mp2_budget_gb = mp2_budget_gb
         self.guard = guard and precision == "mixed"
         self.refine_eigh = (precision == "mixed") if refine_eigh is None else bool(refine_eigh)
+        self.autotune = autotune
+        self.tuning = []     # (choice, ms rows, ms tiles) of every autotuned cohort batch
         self.guard_energy = guard_energy
         self.guard_commutator = guard_commutator
         self.stream = torch.cuda.current_stream(self.dev)
@@ -373,6 +376,7 @@ class ServingEngine:
         b.finalize(self.stream.cuda_stream)
         b.set_skip(self.skip)
         b.flags = [1] * len(jobs)
+        b.tuned = False
         return b
 
     def _apply_flags(self, jobs, batch):
@@ -404,6 +408,12 @@ class ServingEngine:
                     torch.sub(s.P, s.Pref, out=s.Pin)
         if mixed:
             self._apply_flags(jobs, batch)
+            if self.autotune and not batch.tuned:
+                # FP32 kernel per quartet class, timed on this cohort's densities
+                # (cached by class and size, so mostly a look-up)
+                batch.autotune(self.split, stream=self.stream.cuda_stream)
+                batch.tuned = True
+                self.tuning.append(batch.tuning())
         self._tick("other")
         batch.fock(3 if mixed else 0, self.split, self.stream.cuda_stream)
         self._tick("fock")

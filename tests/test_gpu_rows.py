@@ -67,3 +67,42 @@ def test_row_kernel_matches_tile_kernel(L, name, split, monkeypatch):
     tol = 1e-6 if split < 1e-3 else 2e-5
     assert float(np.max(np.abs(gr - go))) < tol * scale
     assert float(np.max(np.abs(gr - g64))) < 10 * tol * scale
+
+
+def test_autotune_keeps_the_quartets_and_the_matrices(L):
+    """The autotuner only chooses which FP32 kernel runs each class: a mixed
+    batch build before and after forced tuning evaluates the same quartets per
+    class and gives the same matrices up to the order of FP32 additions."""
+    torch = pytest.importorskip("torch")
+    mols = [S.chain_for_basis(10_021, 150), S.water_cluster(2, seed=3)]
+    st = torch.cuda.current_stream().cuda_stream
+    hs, bufs = [], []
+    b = L.Batch()
+    rng = np.random.default_rng(5)
+    for m in mols:
+        sp = m["species"][0]
+        h = L.Libint2Interface(sp, 1)
+        n = h.nbasis
+        X = rng.normal(size=(n, n)) * 0.03
+        P = torch.tensor(X + X.T, device="cuda")
+        G = torch.zeros_like(P)
+        J = torch.zeros_like(P)
+        b.add_system([h], [-1.0], [-0.5], [1], [P], [G], [J])
+        hs.append(h)
+        bufs.append((P, G, J))
+    b.finalize(st)
+    b.fock(3, 1e-5, st)
+    q0 = b.quartets(st).copy()
+    G0 = [g.clone() for _, g, _ in bufs]
+    b.autotune(1e-5, force=True, stream=st)
+    choice, ms_rows, ms_tiles = b.tuning()
+    assert (choice >= 0).any()
+    b.fock(3, 1e-5, st)
+    q1 = b.quartets(st)
+    assert np.array_equal(q0, q1)
+    for g0, (_, g1, _) in zip(G0, bufs):
+        scale = max(1.0, float(g0.abs().max()))
+        assert float((g1 - g0).abs().max()) < 1e-6 * scale
+    b.close()
+    for h in hs:
+        h.close()
