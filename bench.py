@@ -123,6 +123,7 @@ def profile_fock(args):
     else:
         mols = systems_for(0, args.batch)
     s = BatchSCF(mols)
+    s.batch.use_graph(False)          # profiling case: every launch eager
     st = torch.cuda.current_stream().cuda_stream
     for g in s.groups.values():
         g.Pin.copy_(s._density(g, g.H) if g.ragged else s._purify(g, g.H))
