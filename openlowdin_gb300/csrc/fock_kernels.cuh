@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
     float b = T.pairs32[bi].Q * (float)ket.Q;
     if (T.screen) {
       b *= dnorm6(T.Dn32, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
-      if (b < fmaxf(TL.eps32, TL.skip)) active = false;
+      if (b < fmaxf(TL.eps32, act == kSysFP64 ? 0.f : TL.skip)) active = false;   // no skip in an FP64 check
     }
     if (act != kSysFP64 && (TL.lower ? !(b < TL.split32) : (b < TL.split32))) active = false;
   } else if (T.screen) {
@@ -553,7 +553,7 @@ __global__ void __launch_bounds__(128) cp_tasks_kernel(const CPTask *__restrict_
     if (T.DnB32) dm = fmaxf(dm, __ldg(T.DnB32 + k32.sa * T.nshB + k32.sb));
     const float b = b32.Q * k32.Q * dm;
     if (act != kSysFP64 && (TL.lower ? !(b < TL.split32) : (b < TL.split32))) active = false;
-    if ((T.DnA32 || T.DnB32) && b < TL.skip) active = false;
+    if ((T.DnA32 || T.DnB32) && act != kSysFP64 && b < TL.skip) active = false;
   }
   if (__all_sync(0xffffffffu, !active)) return;
   if (T.count) {

@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(128) jk_coop_kernel(const JKTask *__restrict__
         float b = T.pairs32[bi].Q * T.pairs32[ki].Q;
         if (T.screen) {
           b *= dnorm6(T.Dn32, T.nsh, bra.sa, bra.sb, ket.sa, ket.sb);
-          if (b < fmaxf(TL.eps32, TL.skip)) active = false;
+          if (b < fmaxf(TL.eps32, act == kSysFP64 ? 0.f : TL.skip)) active = false;
         }
         if (act != kSysFP64 && (TL.lower ? !(b < TL.split32) : (b < TL.split32))) active = false;
       } else if (T.screen) {
@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(128) cp_coop_kernel(const CPTask *__restrict__
         if (T.DnB32) dm = fmaxf(dm, __ldg(T.DnB32 + k32.sa * T.nshB + k32.sb));
         const float b = b32.Q * k32.Q * dm;
         if (act != kSysFP64 && (TL.lower ? !(b < TL.split32) : (b < TL.split32))) continue;
-        if ((T.DnA32 || T.DnB32) && b < TL.skip) continue;
+        if ((T.DnA32 || T.DnB32) && act != kSysFP64 && b < TL.skip) continue;
       }
       if (T.count && lane == 0) atomicAdd(T.count, 1ull);
       const PairRec &bra = T.pa[bi];
