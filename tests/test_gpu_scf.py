@@ -250,7 +250,8 @@ def test_batch_mixed_fp64_check_and_guard():
     """BatchSCF in mixed precision: every converged system gets an FP64 check
     (its stated error <= 1e-6 Eh, energy within 1e-6 of plain); with every
     quartet forced into FP32 the check fails and the system finishes in FP64
-    on the plain energy."""
+    on the plain energy (the check bar is lowered to 1e-9 Eh so that it fails
+    for every molecule, whatever its size)."""
     from openlowdin_gb300 import systems as S
     from openlowdin_gb300.batch_scf import BatchSCF
     mols = [S.chain_for_basis(500 + i, nbf) for i, nbf in enumerate((50, 80, 120))]
@@ -264,7 +265,8 @@ def test_batch_mixed_fp64_check_and_guard():
         assert p.converged and m.converged and not m.guard_hit
         assert m.err_vs_fp64 is not None and m.err_vs_fp64 <= 1e-6
         assert abs(m.energy - p.energy) < 1e-6
-    b = BatchSCF(mols, precision="mixed", split=1e30)
+    # every quartet in FP32 and a check bar (1e-9 Eh) far below its error
+    b = BatchSCF(mols, precision="mixed", split=1e30, guard_energy=1e-9)
     forced = b.solve()
     b.close()
     for p, f in zip(plain, forced):

@@ -78,12 +78,12 @@ def test_mixed_jobs_state_their_fp64_error(serve):
 
 
 def test_guard_sends_a_failed_job_on_in_fp64(serve):
-    """With every quartet forced into FP32 (split far above every bound) the
-    mixed solution misses the FP64 one by more than 1e-6 Eh: the check fires,
-    the job continues in FP64 and ends on the plain result."""
+    """With every quartet forced into FP32 (split far above every bound) and
+    the check's bar at 1e-9 Eh the mixed solution fails its FP64 check: the
+    job continues in FP64 and ends on the plain result."""
     req = serve.Request(S.chain_for_basis(421, 90), "scf", 0.0, 0)
     plain = serve.ServingEngine(precision="fp64").run([req], realtime=False)[0]
-    forced = serve.ServingEngine(precision="mixed", split=1e30).run([req], realtime=False)[0]
+    forced = serve.ServingEngine(precision="mixed", split=1e30, guard_energy=1e-9).run([req], realtime=False)[0]
     assert forced.converged and forced.guard_hit
     assert forced.err_vs_fp64 == 0.0
     assert abs(forced.energy - plain.energy) < 1e-8
