@@ -280,15 +280,17 @@ __global__ void __launch_bounds__(128, 1) gemm_split_kernel(const __grid_constan
 // ------------------------------------------------------------ precise mode --
 // Three pieces per operand, eight products (p0q0 + p0q1 + p1q0 + p1q1 + p0q2
 // + p2q0 + p1q2 + p2q1), and no long FP32 running sum in the tensor cores:
-// the p0q0 product of every 16-wide K slab goes to a fresh tensor-memory
-// accumulator, the seven smaller products of a 64-wide K step to one more;
-// after every step the accumulator warps add the four slab sums in FP32 and
+// the p0q0 product of every 32-wide K slab (two MMAs) goes to a fresh
+// tensor-memory accumulator, the seven smaller products of a 64-wide K step
+// to one more; after every step the accumulator warps add the two slab sums in FP32 and
 // enter the step total into a compensated FP32 pair (hi + lo, Knuth's
 // error-free TwoSum), the corrections into the low part.  The tensor cores
-// then round each slab's main sum once (toward zero, to FP32) instead of
+// then round each slab's main sum twice (toward zero, to FP32) instead of
 // carrying a 640-term FP32 running sum, which is what limits a plain
 // FP32-accumulated product on inputs with strong cancellation; the FP32 pipe
-// (64x the FP64 rate on this part) keeps up with the tensor cores.
+// (64x the FP64 rate on this part) keeps up with the tensor cores.  (16-wide
+// slabs, one rounding each, cost the accumulator warps five tensor-memory
+// reads per element and step instead of three and bound the engine.)
 // Warps: 0 TMA producer, 1 MMA issuer, 2-9 accumulators / epilogue (warp w
 // reads tensor-memory lanes 32 (w % 4) .. + 31, columns 24 ((w - 2) / 4) ..
 // + 23 of each accumulator).  Tiles 128 x 48; persistent CTAs walk the N
@@ -296,7 +298,7 @@ __global__ void __launch_bounds__(128, 1) gemm_split_kernel(const __grid_constan
 constexpr int kPBN = 48, kPStages = 3, kPAccWarps = 8, kPColsPerWarp = kPBN / 2;
 constexpr int kPTileA = 128 * kBK * 2, kPTileB = kPBN * kBK * 2;
 constexpr int kPStageBytes = 3 * kPTileA + 3 * kPTileB;
-constexpr int kPBufCols = 5 * kPBN;                 // 4 slab accumulators + 1 correction accumulator
+constexpr int kPBufCols = 3 * kPBN;                 // 2 slab accumulators + 1 correction accumulator
 constexpr int kPTmemCols = 512;
 constexpr int kPThreads = 32 * (2 + kPAccWarps);
 constexpr int kPSmemBytes = kPStages * kPStageBytes + 1024 + 256;
@@ -424,12 +426,13 @@ __global__ void __launch_bounds__(kPThreads, 1) gemm_precise_kernel(const __grid
 #pragma unroll
           for (int kk = 0; kk < kBK / 16; ++kk) {
             const uint64_t off = (uint64_t)(kk * 16 * 2) >> 4;
-            umma_bf16(tb + (uint32_t)(kk * kPBN), da[0] + off, db[0] + off, idesc, 0u);   // fresh per slab
+            // main product: a fresh accumulator per 32-wide slab (two MMAs)
+            umma_bf16(tb + (uint32_t)((kk >> 1) * kPBN), da[0] + off, db[0] + off, idesc, (uint32_t)(kk & 1));
 #pragma unroll
             for (int p = 1; p < 8; ++p) {
               const int qa = p == 2 || p == 3 || p == 7 ? 1 : (p == 5 || p == 6 ? 2 : 0);
               const int qb = p == 1 || p == 3 || p == 6 ? 1 : (p == 4 || p == 7 ? 2 : 0);
-              umma_bf16(tb + (uint32_t)(4 * kPBN), da[qa] + off, db[qb] + off, idesc, (kk | (p - 1)) != 0);
+              umma_bf16(tb + (uint32_t)(2 * kPBN), da[qa] + off, db[qb] + off, idesc, (kk | (p - 1)) != 0);
             }
           }
           umma_commit(&empty[s]);
@@ -462,13 +465,13 @@ __global__ void __launch_bounds__(kPThreads, 1) gemm_precise_kernel(const __grid
         tc_fence_after();
         __syncwarp();
         const uint32_t ta = tmem + ((uint32_t)(wq * 32) << 16) + (uint32_t)(b * kPBufCols + c0);
-        // the step's four slab sums (each rounded once by the tensor cores)
+        // the step's two slab sums (each rounded twice by the tensor cores)
         // add in FP32, round to nearest; the step total enters the running
         // pair by TwoSum; the correction products go to the low part
         float stepsum[kPColsPerWarp];
         uint32_t r[kPColsPerWarp];
 #pragma unroll
-        for (int c = 0; c < 5; ++c) {
+        for (int c = 0; c < 3; ++c) {
           // loads at column offsets aligned to their width
           if (c0 == 0) {
             tmem_ld16(ta + (uint32_t)(c * kPBN), r);
@@ -481,7 +484,7 @@ __global__ void __launch_bounds__(kPThreads, 1) gemm_precise_kernel(const __grid
           if (c == 0) {
 #pragma unroll
             for (int j = 0; j < kPColsPerWarp; ++j) stepsum[j] = __uint_as_float(r[j]);
-          } else if (c < 4) {
+          } else if (c < 2) {
 #pragma unroll
             for (int j = 0; j < kPColsPerWarp; ++j) stepsum[j] += __uint_as_float(r[j]);
           } else {

@@ -1,5 +1,6 @@
 // MP2 transform helpers: coefficient preparation, unpacking of the packed
 // ket-pair columns into a full (lam, sig) square, and the pair-energy sum.
+#include <type_traits>
 #include <algorithm>
 
 #include "kernels.cuh"
@@ -62,14 +63,33 @@ __global__ void __launch_bounds__(256) mp2_energy_kernel(const T *__restrict__ M
   __syncthreads();
   const double eij = ei + eo[j];
   double acc = 0.0;
-  for (int y = threadIdx.y; y < 32; y += 8) {
-    const int b = b0 + y, a = a0 + threadIdx.x;
-    if (a < v && b < v) {
-      double x = (double)Mj[(size_t)b * v + a];      // (ia|jb)
-      double t = (double)tr[y][threadIdx.x];          // (ib|ja) = M[j][a][b]
-      if (!(fabs(x) > cut)) x = 0.0;
-      if (!(fabs(t) > cut)) t = 0.0;
-      acc += x * (2.0 * x - t) / (eij - ev[a] - ev[b]);
+  if constexpr (std::is_same<T, float>::value) {
+    // split-BF16 path: M is FP32, so each term is formed in FP32 (no FP64
+    // division per element, which dominated this kernel on the FP64 pipe);
+    // a thread's four terms are summed in FP32 and everything after in FP64
+    const float eijf = (float)eij, cutf = (float)cut;
+    float part = 0.f;
+    for (int y = threadIdx.y; y < 32; y += 8) {
+      const int b = b0 + y, a = a0 + threadIdx.x;
+      if (a < v && b < v) {
+        float x = Mj[(size_t)b * v + a];
+        float t = tr[y][threadIdx.x];
+        if (!(fabsf(x) > cutf)) x = 0.f;
+        if (!(fabsf(t) > cutf)) t = 0.f;
+        part += x * (2.f * x - t) / (eijf - (float)ev[a] - (float)ev[b]);
+      }
+    }
+    acc = part;
+  } else {
+    for (int y = threadIdx.y; y < 32; y += 8) {
+      const int b = b0 + y, a = a0 + threadIdx.x;
+      if (a < v && b < v) {
+        double x = (double)Mj[(size_t)b * v + a];      // (ia|jb)
+        double t = (double)tr[y][threadIdx.x];          // (ib|ja) = M[j][a][b]
+        if (!(fabs(x) > cut)) x = 0.0;
+        if (!(fabs(t) > cut)) t = 0.0;
+        acc += x * (2.0 * x - t) / (eij - ev[a] - ev[b]);
+      }
     }
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -147,11 +167,32 @@ __global__ void __launch_bounds__(256) mp2_energy_coupling_kernel(const T *__res
   const T *Mj = M + (size_t)j * vB * vA;
   const double eij = ei + eo[j];
   double acc = 0.0;
-  for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < (long long)vB * vA; t += (long long)gridDim.x * 256) {
-    const int b = (int)(t / vA), a = (int)(t % vA);
-    double x = (double)Mj[t];
-    if (!(fabs(x) > cut)) x = 0.0;
-    acc += x * x / (eij - evA[a] - evB[b]);
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32 terms (FP32 M), FP64 sums of each thread's short FP32 partials
+    const float eijf = (float)eij, cutf = (float)cut;
+    float part = 0.f;
+    int k = 0;
+    for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < (long long)vB * vA;
+         t += (long long)gridDim.x * 256) {
+      const int b = (int)(t / vA), a = (int)(t % vA);
+      float x = Mj[t];
+      if (!(fabsf(x) > cutf)) x = 0.f;
+      part += x * x / (eijf - (float)evA[a] - (float)evB[b]);
+      if (++k == 16) {
+        acc += part;
+        part = 0.f;
+        k = 0;
+      }
+    }
+    acc += part;
+  } else {
+    for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < (long long)vB * vA;
+         t += (long long)gridDim.x * 256) {
+      const int b = (int)(t / vA), a = (int)(t % vA);
+      double x = (double)Mj[t];
+      if (!(fabs(x) > cut)) x = 0.0;
+      acc += x * x / (eij - evA[a] - evB[b]);
+    }
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
