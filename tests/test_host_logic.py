@@ -119,3 +119,39 @@ def test_batch_arguments_checked_on_the_host():
         b.set_active([1])                        # not finalised yet
     b.close()
     h.close()
+
+
+def test_serving_stream_sizes_span_the_configured_range():
+    """The headline stream draws sizes log-uniformly from 30-1200 functions:
+    the generated chains reach at least the drawn size and stay within the
+    range plus one atom's functions."""
+    import bench
+    from openlowdin_gb300 import systems as S
+    reqs = bench.serving_requests(40, 50.0, seed=1)
+    n = np.array([S.nbasis(r.system["species"][0]) for r in reqs])
+    assert n.min() >= bench.STREAM_LO and n.max() <= bench.STREAM_HI + 20
+    # log-uniform: about half of the draws below the geometric mean (190)
+    assert 0.25 < np.mean(n < np.sqrt(bench.STREAM_LO * bench.STREAM_HI)) < 0.75
+
+
+def test_bench_per_job_table_and_tuning_summary():
+    """The per-job error table pairs mixed and plain results by request and
+    the autotuner summary counts the kernels kept per class."""
+    import bench
+    from types import SimpleNamespace as NS
+    reqs = [NS(rid=0, kind="scf"), NS(rid=1, kind="scf+mp2")]
+    plain = {0: NS(nbasis=40, iterations=20, converged=True, energy=-76.0, e2=None),
+             1: NS(nbasis=80, iterations=30, converged=True, energy=-150.0, e2=-0.5)}
+    mixed = {0: NS(nbasis=40, iterations=21, converged=True, energy=-76.0 + 3e-9, e2=None, err_vs_fp64=1e-9,
+                   guard_hit=False),
+             1: NS(nbasis=80, iterations=31, converged=False, energy=-150.1, e2=-0.6, err_vs_fp64=None,
+                   guard_hit=False)}
+    rows = bench.per_job_table(reqs, plain, mixed)
+    assert abs(rows[0]["abs_dE_mixed_vs_plain_Eh"] - 3e-9) < 1e-12
+    assert rows[1]["converged_mixed"] is False and abs(rows[1]["abs_dE2_mixed_vs_plain_Eh"] - 0.1) < 1e-12
+    ch = np.full((6, 6), -1)
+    ch[0, 0], ch[1, 0] = 1, 0
+    ms = np.where(ch >= 0, 1.0, -1.0).astype(np.float32)
+    s = bench.tuning_summary([(ch, ms, 2 * ms)])
+    assert s["batches"] == 1
+    assert s["classes"]["(ss|ss)"]["rows_kernel"] == 1 and s["classes"]["(ps|ss)"]["tile_kernel"] == 1
