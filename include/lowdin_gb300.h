@@ -105,14 +105,27 @@ void LibintInterface_compute_alphabeta_direct(LibintInterface *lint, LibintInter
 /* Libint2Iface.h:403 -- not provided. */
 void LibintInterface_compute_coupling_disk(LibintInterface *lint, LibintInterface *olint, const char *filename);
 
-/* Libint2Iface.h:407-437 -- G12 (inter-particle potential) integrals: not
-   provided (out of the direct Coulomb path). */
+/* Libint2Iface.h:407-415 -- G12 (inter-particle potential) integrals on disk:
+   not provided. */
 void libintinterface_compute_g12_disk(LibintInterface *lint, const char *filename, const double *coefficients,
                                       const double *exponents, const int pot_size);
 void libintinterface_compute_g12inter_disk(LibintInterface *lint, LibintInterface *olint, const char *filename,
                                            const double *coefficients, const double *exponents, const int pot_size);
+
+/* Libint2Iface.h:411 (Libint2Iface.cpp:2193-2365, wrapper :3687-3706) --
+   direct intra-species matrix of the inter-particle potential
+   V(r12) = sum_k coefficients[k] exp(-exponents[k] r12^2) (libint2's
+   contracted Gaussian geminal, pot_size terms, exponents >= 0): the loops,
+   degeneracies, six updates and 0.25 (G + G^T) of compute_2body_direct over
+   every quartet of the significant pairs (no screening); result n x n. */
 void libintinterface_compute_g12_direct(LibintInterface *lint, double *dens, double *result, LGB_REF(double) factor,
                                         const double *coefficients, const double *exponents, const int pot_size);
+
+/* Libint2Iface.h:418 (Libint2Iface.cpp:2367-2540, wrapper :3708-3734) --
+   inter-species matrix of the same potential: J of lint's species from
+   olint's density `dens` (n_o x n_o) over every pair of both species, raw
+   |v| < 1e-10 dropped; row >= col triangle of the n x n result, zero above,
+   as compute_coupling_direct. */
 void libintinterface_compute_g12inter_direct(LibintInterface *lint, LibintInterface *olint, double *dens,
                                              double *result, const double *coefficients, const double *exponents,
                                              const int pot_size);

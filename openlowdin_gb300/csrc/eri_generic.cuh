@@ -104,14 +104,38 @@ __device__ inline void boys_f64_rt(int L, double T, double *F, const double *__r
   }
 }
 
+// Auxiliary integrals of the contracted Gaussian geminal sum_k c_k exp(-g_k r12^2)
+// in the units of the Coulomb ones: with the Coulomb prefactor
+// 2 pi^{5/2} K_ab K_cd / (p q sqrt(p+q)) outside,
+//   F[m] = sqrt(pi)/2 sum_k c_k rho (rho+g_k)^{-3/2} (g_k/(rho+g_k))^m exp(-g_k T/(rho+g_k)),
+// the m-th (-d/dT) derivative of the Gaussian product integral at
+// T = rho |PQ|^2, which the Obara-Saika recursion consumes unchanged for any
+// operator of r12.  gem = {count, g_0..g_{n-1}, c_0..c_{n-1}}.
+__device__ inline void geminal_aux(int L, double rho, double T, const double *__restrict__ gem, double *F) {
+  const int n = (int)gem[0];
+  for (int m = 0; m <= L; ++m) F[m] = 0.0;
+  for (int k = 0; k < n; ++k) {
+    const double gk = gem[1 + k], ck = gem[1 + n + k];
+    const double t = 1.0 / (rho + gk);
+    const double r = gk * t;
+    double v = 0.88622692545275801365 * ck * rho * t * sqrt(t) * exp(-gk * t * T);
+    for (int m = 0; m <= L; ++m) {
+      F[m] += v;
+      v *= r;
+    }
+  }
+}
+
 // Raw contracted integrals of one quartet of runtime class (la lb|lc ld),
 // evaluated by the threads of group g together; result in sm[Lo.out ...],
 // row-major (a, b, c, d).  Every thread of the group must call it (it
 // synchronises the group); the result is valid after the call returns.
-template <typename G>
+// GEM: the operator is the geminal `gem` (geminal_aux) instead of 1/r12.
+template <typename G, bool GEM = false>
 __device__ inline void eri_coop(G g, const CartInfo *__restrict__ ct, const CoLayout &Lo, int la, int lb, int lc,
                                 int ld, const PairRec &bra, const PrimRec *__restrict__ pbra, const PairRec &ket,
-                                const PrimRec *__restrict__ pket, const double *boys64, double *sm) {
+                                const PrimRec *__restrict__ pket, const double *boys64, double *sm,
+                                const double *gem = nullptr) {
   const int tid = g.tid(), nt = g.nt();
   const int L1 = la + lb, L2 = lc + ld, L = L1 + L2, M = L + 1;
   const int NE = coff(L1 + 1), NF = coff(L2 + 1), E0 = coff(la), F0 = coff(lc);
@@ -153,7 +177,8 @@ __device__ inline void eri_coop(G g, const CartInfo *__restrict__ ct, const CoLa
         misc[15] = 0.5 * pk.inv_p;
         misc[16] = 0.5 * opq;
         double F[kGenMaxL + 1];
-        boys_f64_rt(L, rho * PQ2, F, boys64);
+        if constexpr (GEM) geminal_aux(L, rho, rho * PQ2, gem, F);
+        else boys_f64_rt(L, rho * PQ2, F, boys64);
         const double pref = pb.Kt * pk.Kt * sqrt(opq);
         for (int m = 0; m <= L; ++m) Vb[m] = pref * F[m];
       }

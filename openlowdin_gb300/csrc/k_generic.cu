@@ -222,6 +222,99 @@ __global__ void __launch_bounds__(128) cp_coop_kernel(const CPTask *__restrict__
   }
 }
 
+// ---------------------------------------------------------- geminal (G12) --
+// Every class runs here (the geminal matrices are not a hot path): one quartet
+// per warp, all quartets of the launch's bra x ket pair ranges, no screening.
+__global__ void __launch_bounds__(128) g12_coop_kernel(G12Params P, GenClass K) {
+  LGB_COOP_PROLOGUE(K)
+  const int NA = ncart(K.la), NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld);
+  const long long nq = (long long)P.nbra * P.nket;
+  for (long long q = w0; q < nq; q += wstep) {
+    const int bpos = (int)(q / P.nket), kpos = (int)(q % P.nket);
+    if (P.triangle && kpos > bpos) continue;
+    const int bi = P.bra0 + bpos, ki = P.ket0 + kpos;
+    const PairRec &bra = P.pa[bi];
+    const PairRec &ket = P.pb[ki];
+    eri_coop<WarpGroup, true>(g, ct, Lo, K.la, K.lb, K.lc, K.ld, bra, P.pra, ket, P.prb, nullptr, sm, P.gem);
+    auto Iat = [&](int a, int b, int c, int d) { return I[((a * NB + b) * NC + c) * ND + d]; };
+    const int fa = bra.fa, fb = bra.fb, fc = ket.fa, fd = ket.fb;
+    const double *__restrict__ D = P.Ds;
+    if (P.intra) {
+      const double deg = (bra.sa == bra.sb ? 1 : 2) * (ket.sa == ket.sb ? 1 : 2) * (bi == ki ? 1 : 2);
+      const double hdeg = deg * P.hf;
+      const int n = P.n;
+      const int n12 = NA * NB, n34 = NC * ND, n13 = NA * NC, n24 = NB * ND, n14 = NA * ND, n23 = NB * NC;
+      // the six updates, lanes over their output elements
+      for (int t = lane; t < n12 + n34 + n13 + n24 + n14 + n23; t += 32) {
+        int x = t;
+        double s = 0;
+        if (x < n12) {
+          const int a = x / NB, b = x % NB;
+          for (int c = 0; c < NC; ++c)
+            for (int d = 0; d < ND; ++d) s += D[(fc + c) * n + fd + d] * Iat(a, b, c, d);
+          atomicAdd(P.Gacc + (size_t)(fa + a) * n + fb + b, s * deg);
+          continue;
+        }
+        x -= n12;
+        if (x < n34) {
+          const int c = x / ND, d = x % ND;
+          for (int a = 0; a < NA; ++a)
+            for (int b = 0; b < NB; ++b) s += D[(fa + a) * n + fb + b] * Iat(a, b, c, d);
+          atomicAdd(P.Gacc + (size_t)(fc + c) * n + fd + d, s * deg);
+          continue;
+        }
+        x -= n34;
+        if (x < n13) {
+          const int a = x / NC, c = x % NC;
+          for (int b = 0; b < NB; ++b)
+            for (int d = 0; d < ND; ++d) s += D[(fb + b) * n + fd + d] * Iat(a, b, c, d);
+          atomicAdd(P.Gacc + (size_t)(fa + a) * n + fc + c, s * hdeg);
+          continue;
+        }
+        x -= n13;
+        if (x < n24) {
+          const int b = x / ND, d = x % ND;
+          for (int a = 0; a < NA; ++a)
+            for (int c = 0; c < NC; ++c) s += D[(fa + a) * n + fc + c] * Iat(a, b, c, d);
+          atomicAdd(P.Gacc + (size_t)(fb + b) * n + fd + d, s * hdeg);
+          continue;
+        }
+        x -= n24;
+        if (x < n14) {
+          const int a = x / ND, d = x % ND;
+          for (int b = 0; b < NB; ++b)
+            for (int c = 0; c < NC; ++c) s += D[(fb + b) * n + fc + c] * Iat(a, b, c, d);
+          atomicAdd(P.Gacc + (size_t)(fa + a) * n + fd + d, s * hdeg);
+          continue;
+        }
+        x -= n14;
+        {
+          const int b = x / NC, c = x % NC;
+          for (int a = 0; a < NA; ++a)
+            for (int d = 0; d < ND; ++d) s += D[(fa + a) * n + fd + d] * Iat(a, b, c, d);
+          atomicAdd(P.Gacc + (size_t)(fb + b) * n + fc + c, s * hdeg);
+        }
+      }
+    } else {
+      // J of the bra species: both orientations of a two-shell bra pair, the
+      // ket pair's density over its components (x2 for a two-shell ket pair)
+      const bool abdiff = bra.sa != bra.sb, cddiff = ket.sa != ket.sb;
+      for (int t = lane; t < NA * NB; t += 32) {
+        const int a = t / NB, b = t % NB;
+        double s = 0;
+        for (int c = 0; c < NC; ++c)
+          for (int d = 0; d < ND; ++d) {
+            const double v = Iat(a, b, c, d);
+            if (!abs_below(v, P.cut)) s += D[(size_t)(fc + c) * P.nB + fd + d] * v;
+          }
+        if (cddiff) s *= 2.0;
+        atomicAdd(P.Gacc + (size_t)(fa + a) * P.n + fb + b, s);
+        if (abdiff) atomicAdd(P.Gacc + (size_t)(fb + b) * P.n + fa + a, s);
+      }
+    }
+  }
+}
+
 // -------------------------------------------------------- first quarter --
 // role r of the permutational orbit: (mu, nu, l, s) -> quartet indices (a, b, c, d)
 __device__ __forceinline__ void it_map(int r, int mu, int nu, int l, int s, int *a, int *b, int *c, int *d) {
@@ -357,6 +450,7 @@ bool coop_ready() {
            if (e == cudaSuccess) e = coop_attr(it_coop_kernel);
            if (e == cudaSuccess) e = coop_attr(mp2x_coop_kernel);
            if (e == cudaSuccess) e = coop_attr(schwarz_coop_kernel);
+           if (e == cudaSuccess) e = coop_attr(g12_coop_kernel);
            return e;
          }) == cudaSuccess;
 }
@@ -466,6 +560,17 @@ cudaError_t launch_mp2x(int pcb, int pck, const MXParams &p, cudaStream_t s) {
     const CoopShape c = coop_shape(K, (long long)p.nbra * p.nket);
     mp2x_coop_kernel<<<c.grid, c.block, c.smem, s>>>(p, K);
   }
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_g12(int pcb, int pck, const G12Params &p, cudaStream_t s) {
+  if (!class_supported(pcb, pck) || !p.gem) return cudaErrorNotSupported;
+  if (p.nbra <= 0 || p.nket <= 0) return cudaSuccess;
+  if (!coop_ready()) return cudaErrorInvalidValue;
+  const GenClass K = gen_class(pcb, pck);
+  const CoopShape c = coop_shape(K, (long long)p.nbra * p.nket);
+  g12_coop_kernel<<<c.grid, c.block, c.smem, s>>>(p, K);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -210,6 +210,28 @@ struct ITParams {
   double cut;             // raw values with |v| <= cut are dropped (1e-10)
 };
 
+// Geminal (G12) two-particle matrices for the operator sum_k c_k exp(-g_k r12^2):
+// intra-species (six-update digestion of one species, every quartet of the
+// significant pairs, no screening) or inter-species (J of the bra species from
+// the ket species' density, raw |v| < cut dropped, no quartet skipped).
+struct G12Params {
+  const PairRec *pa;
+  const PrimRec *pra;
+  int bra0, nbra;
+  const PairRec *pb;
+  const PrimRec *prb;
+  int ket0, nket;
+  int intra;              // 1: one species, 0: coupling
+  int triangle;           // ket position <= bra position only
+  const double *Ds;       // norma-scaled density: intra n x n, coupling nB x nB (ket species)
+  double *Gacc;           // accumulator of the bra species (n x n)
+  int n, nB;
+  double hf;              // 0.5 * exchange factor (intra)
+  double cut;             // coupling: raw values with |v| < cut are dropped (1e-10)
+  const double *gem;      // {count, exponents..., coefficients...} in device memory
+};
+cudaError_t launch_g12(int pcb, int pck, const G12Params &p, cudaStream_t s);
+
 struct SchwarzParams {
   const PairRec *pairs;
   const PrimRec *prims;

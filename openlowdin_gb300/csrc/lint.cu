@@ -434,6 +434,89 @@ bool first_quarter(LibintInterface *A, LibintInterface *B, const double *hD, con
   return true;
 }
 
+// geminal parameters {count, exponents, coefficients} into A->dGem (stream of A)
+bool upload_geminal(LibintInterface *A, const double *coefficients, const double *exponents, int pot_size,
+                    const char *fn) {
+  if (pot_size <= 0 || !coefficients || !exponents) {
+    set_error("%s: the geminal needs pot_size > 0 coefficients and exponents (got %d)", fn, pot_size);
+    return false;
+  }
+  std::vector<double> h(1 + 2 * (size_t)pot_size);
+  h[0] = pot_size;
+  for (int k = 0; k < pot_size; ++k) {
+    if (!(exponents[k] >= 0.0) || !std::isfinite(exponents[k]) || !std::isfinite(coefficients[k])) {
+      set_error("%s: geminal term %d has exponent %g, coefficient %g (exponents must be finite and >= 0)", fn, k,
+                exponents[k], coefficients[k]);
+      return false;
+    }
+    h[1 + k] = exponents[k];
+    h[1 + pot_size + k] = coefficients[k];
+  }
+  if (!A->dGem.ensure(h.size())) return false;
+  // synchronous: the host vector is freed on return
+  CK(cudaMemcpyAsync(A->dGem.p, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, A->stream));
+  CK(cudaStreamSynchronize(A->stream));
+  return true;
+}
+
+// Geminal matrix on the device, ordered on s.  B == nullptr: intra-species
+// G = 0.25 (Gacc + Gacc^T) of A's significant pairs with exchange factor
+// `factor`, from A's density dD (n x n), into dOut.  Else: J of A's species from
+// B's density dD (nB x nB) over every pair of both species, lower triangle of
+// dOut (row >= col), zero above.  The geminal is A->dGem.
+bool g12_build(LibintInterface *A, LibintInterface *B, const double *dD, double factor, double *dOut,
+               cudaStream_t s) {
+  const int n = A->nbasis;
+  G12Params P{};
+  P.gem = A->dGem.p;
+  P.n = n;
+  if (!B) {
+    CK(launch_scale_density(dD, A->d_norma, n, A->dDs.p, A->dDs32.p, s));
+    CK(cudaMemsetAsync(A->dGacc.p, 0, sizeof(double) * n * n, s));
+    P.pa = P.pb = A->sig.d;
+    P.pra = P.prb = A->sig.dp;
+    P.intra = 1;
+    P.Ds = A->dDs.p;
+    P.Gacc = A->dGacc.p;
+    P.hf = 0.5 * factor;
+    for (int cb = 0; cb < kNumPairClasses; ++cb)
+      for (int ck = 0; ck <= cb; ++ck) {
+        if (!A->sig.count(cb) || !A->sig.count(ck)) continue;
+        P.bra0 = A->sig.start[cb];
+        P.nbra = A->sig.count(cb);
+        P.ket0 = A->sig.start[ck];
+        P.nket = A->sig.count(ck);
+        P.triangle = cb == ck;
+        CK(launch_g12(cb, ck, P, s));
+      }
+    CK(launch_symmetrize(A->dGacc.p, nullptr, A->d_norma, n, 0.25, dOut, s));
+    return true;
+  }
+  const int nB = B->nbasis;
+  CK(launch_scale_density(dD, B->d_norma, nB, B->dDsC.p, B->dDsC32.p, s));
+  CK(cudaMemsetAsync(A->dJacc.p, 0, sizeof(double) * n * n, s));
+  P.pa = A->all.d;
+  P.pra = A->all.dp;
+  P.pb = B->all.d;
+  P.prb = B->all.dp;
+  P.intra = 0;
+  P.Ds = B->dDsC.p;
+  P.Gacc = A->dJacc.p;
+  P.nB = nB;
+  P.cut = 1e-10;
+  for (int cb = 0; cb < kNumPairClasses; ++cb)
+    for (int ck = 0; ck < kNumPairClasses; ++ck) {
+      if (!A->all.count(cb) || !B->all.count(ck)) continue;
+      P.bra0 = A->all.start[cb];
+      P.nbra = A->all.count(cb);
+      P.ket0 = B->all.start[ck];
+      P.nket = B->all.count(ck);
+      CK(launch_g12(cb, ck, P, s));
+    }
+  CK(launch_coupling_extract(A->dJacc.p, nullptr, A->d_norma, n, 1.0, 1, dOut, s));
+  return true;
+}
+
 bool check_handle(LibintInterface *l, const char *fn) {
   if (!l) {
     set_error("%s: null handle", fn);
@@ -614,13 +697,53 @@ void libintinterface_compute_g12inter_disk(LibintInterface *, LibintInterface *,
                                            const double *, const int) {
   unsupported(__func__);
 }
-void libintinterface_compute_g12_direct(LibintInterface *, double *, double *, double &, const double *,
-                                        const double *, const int) {
-  unsupported(__func__);
+void libintinterface_compute_g12_direct(LibintInterface *lint, double *dens, double *result, double &factor,
+                                        const double *coefficients, const double *exponents, const int pot_size) {
+  if (!check_handle(lint, __func__)) return;
+  if (!dens || !result) {
+    set_error("%s: null argument", __func__);
+    return;
+  }
+  if (!lint->ensure_sig()) return;
+  const int n = lint->nbasis;
+  cudaStream_t s = lint->stream;
+  if (!upload_geminal(lint, coefficients, exponents, pot_size, __func__)) return;
+  if (!lint->dD.ensure((size_t)n * n) || !lint->dDs.ensure((size_t)n * n) || !lint->dDs32.ensure((size_t)n * n) ||
+      !lint->dGacc.ensure((size_t)n * n) || !lint->dG.ensure((size_t)n * n))
+    return;
+  if (cudaMemcpyAsync(lint->dD.p, dens, sizeof(double) * n * n, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+    set_error("%s: density upload failed", __func__);
+    return;
+  }
+  if (!g12_build(lint, nullptr, lint->dD.p, factor, lint->dG.p, s)) return;
+  if (cudaMemcpyAsync(result, lint->dG.p, sizeof(double) * n * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    set_error("%s: result download failed", __func__);
 }
-void libintinterface_compute_g12inter_direct(LibintInterface *, LibintInterface *, double *, double *,
-                                             const double *, const double *, const int) {
-  unsupported(__func__);
+
+void libintinterface_compute_g12inter_direct(LibintInterface *lint, LibintInterface *olint, double *dens,
+                                             double *result, const double *coefficients, const double *exponents,
+                                             const int pot_size) {
+  if (!check_handle(lint, __func__) || !check_handle(olint, __func__)) return;
+  if (!dens || !result) {
+    set_error("%s: null argument", __func__);
+    return;
+  }
+  if (!lint->ensure_all() || !olint->ensure_all()) return;
+  const int n = lint->nbasis, no = olint->nbasis;
+  cudaStream_t s = lint->stream;
+  if (!upload_geminal(lint, coefficients, exponents, pot_size, __func__)) return;
+  if (!olint->dD.ensure((size_t)no * no) || !olint->dDsC.ensure((size_t)no * no) ||
+      !olint->dDsC32.ensure((size_t)no * no) || !lint->dJacc.ensure((size_t)n * n) || !lint->dG.ensure((size_t)n * n))
+    return;
+  if (cudaMemcpyAsync(olint->dD.p, dens, sizeof(double) * no * no, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+    set_error("%s: density upload failed", __func__);
+    return;
+  }
+  if (!g12_build(lint, olint, olint->dD.p, 0.0, lint->dG.p, s)) return;
+  if (cudaMemcpyAsync(result, lint->dG.p, sizeof(double) * n * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    set_error("%s: result download failed", __func__);
 }
 void LibintInterface_compute_2body_directAll(LibintInterface *, double *, double *) { unsupported(__func__); }
 void LibintInterface_compute_coupling_directAll(LibintInterface *, LibintInterface *, double *, double *) {

@@ -269,6 +269,7 @@ struct LibintInterface {
   double *d_alpha = nullptr, *d_cn = nullptr;
   int *d_first = nullptr;
   DevBuf<double> dZR;          // point charges and positions of the last one-body call
+  DevBuf<double> dGem;         // geminal parameters of the last G12 call {count, exponents, coefficients}
   DevBuf<double> dD, dDs, dDn, dGacc, dG, dA, dC, dDsC, dJacc;
   DevBuf<float> dDs32, dDn32, dGacc32, dDsC32, dJacc32;
   DevBuf<float> dDp32, dJp32, dDnP32;   // pair-indexed arrays of the FP32 row kernels
@@ -299,6 +300,7 @@ struct LibintInterface {
     d_alpha = d_cn = nullptr;
     d_first = nullptr;
     dZR.release();
+    dGem.release();
     dD.release(); dDs.release(); dDn.release(); dGacc.release(); dG.release(); dA.release(); dC.release();
     dDsC.release(); dJacc.release();
     dDs32.release(); dDn32.release(); dGacc32.release(); dDsC32.release(); dJacc32.release();

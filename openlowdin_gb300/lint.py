@@ -53,6 +53,9 @@ def lib():
         L.LibintInterface_compute_2body_directIT.argtypes = [_vp, _f64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int)]
         L.LibintInterface_compute_coupling_direct.argtypes = [_vp, _vp, _f64p, _f64p]
         L.LibintInterface_compute_alphabeta_direct.argtypes = [_vp, _vp, _f64p, _f64p, _f64p]
+        L.libintinterface_compute_g12_direct.argtypes = [_vp, _f64p, _f64p, ctypes.POINTER(ctypes.c_double),
+                                                         _f64p, _f64p, ctypes.c_int]
+        L.libintinterface_compute_g12inter_direct.argtypes = [_vp, _vp, _f64p, _f64p, _f64p, _f64p, ctypes.c_int]
         L.LibintInterface_compute_coupling_directIT.argtypes = [_vp, _vp, _f64p, _f64p, _f64p,
                                                                 ctypes.POINTER(ctypes.c_int)]
         L.LowdinGB300_last_error.restype = ctypes.c_char_p
@@ -376,6 +379,35 @@ class Libint2Interface:
                                                        np.ascontiguousarray(other_density, np.float64), out)
         _check()
         return float(out[0])
+
+    def compute_g12_direct(self, density, factor: float, coefficients, exponents) -> np.ndarray:
+        """Libint2Interface_computeG12Intraspecies_direct: the two-particle matrix of
+        the potential sum_k c_k exp(-g_k r12^2) (coefficients c_k, exponents g_k)."""
+        n = self.nbasis
+        c = np.ascontiguousarray(coefficients, np.float64).ravel()
+        g = np.ascontiguousarray(exponents, np.float64).ravel()
+        if c.shape != g.shape:
+            raise ValueError("geminal coefficients and exponents differ in length")
+        out = np.empty((n, n))
+        f = ctypes.c_double(factor)
+        lib().libintinterface_compute_g12_direct(self.h, np.ascontiguousarray(density, np.float64), out,
+                                                 ctypes.byref(f), c, g, len(c))
+        _check()
+        return out
+
+    def compute_g12inter_direct(self, other: "Libint2Interface", other_density, coefficients,
+                                exponents) -> np.ndarray:
+        """Libint2Interface_computeG12Interspecies_direct: lower triangle (row >= col)."""
+        n = self.nbasis
+        c = np.ascontiguousarray(coefficients, np.float64).ravel()
+        g = np.ascontiguousarray(exponents, np.float64).ravel()
+        if c.shape != g.shape:
+            raise ValueError("geminal coefficients and exponents differ in length")
+        out = np.empty((n, n))
+        lib().libintinterface_compute_g12inter_direct(self.h, other.h, np.ascontiguousarray(other_density, np.float64),
+                                                      out, c, g, len(c))
+        _check()
+        return out
 
     def compute_2body_directIT(self, density, coefficients, p: int) -> np.ndarray:
         n = self.nbasis

@@ -76,6 +76,10 @@ def lib():
         L.or_potential.argtypes = B + [ctypes.c_int, _f64p, _f64p, _f64p]
         L.or_eri_full.argtypes = B + [_f64p, ctypes.c_int]
         L.or_boys.argtypes = [ctypes.c_int, ctypes.c_double, _f64p]
+        G = [ctypes.c_int, _f64p, _f64p]   # geminal: count, coefficients, exponents
+        L.or_g12_direct.argtypes = B + [_f64p, ctypes.c_double] + G + [_f64p, ctypes.c_int]
+        L.or_g12inter_direct.argtypes = B + [ctypes.c_int] + B + [ctypes.c_int, _f64p] + G + [_f64p, ctypes.c_int]
+        L.or_g12_primitive.argtypes = [_i32p, _f64p, _f64p] + G + [_f64p]
         L.or_last_quartet_count.restype = ctypes.c_longlong
         _LIB = L
     return _LIB
@@ -191,6 +195,44 @@ def alphabeta_direct(b: Basis, sid: int, ob: Basis, osid: int, D, Dother) -> flo
     B = coupling_direct(b, sid, ob, osid, Dother)
     J = np.tril(B) + np.tril(B, -1).T
     return float(np.sum(np.asarray(D, np.float64) * J))
+
+
+def _geminal(coefficients, exponents):
+    c = np.ascontiguousarray(coefficients, np.float64).ravel()
+    g = np.ascontiguousarray(exponents, np.float64).ravel()
+    if c.shape != g.shape:
+        raise ValueError("geminal coefficients and exponents differ in length")
+    return len(c), c, g
+
+
+def g12_direct(b: Basis, D: np.ndarray, factor: float, coefficients, exponents, nthreads=None):
+    """libintinterface_compute_g12_direct (row-major D -> G) for the operator
+    sum_k c_k exp(-g_k r12^2)."""
+    n = b.nbf
+    G = np.zeros(n * n)
+    lib().or_g12_direct(*b.args(), np.ascontiguousarray(D, np.float64).ravel(), float(factor),
+                        *_geminal(coefficients, exponents), G, nthreads or nthreads_default())
+    return G.reshape(n, n)
+
+
+def g12inter_direct(b: Basis, sid: int, ob: Basis, osid: int, Dother: np.ndarray, coefficients, exponents,
+                    nthreads=None):
+    """libintinterface_compute_g12inter_direct(lint=b, olint=ob, D_other)."""
+    n = b.nbf
+    B = np.zeros(n * n)
+    lib().or_g12inter_direct(*b.args(), sid, *ob.args(), osid, np.ascontiguousarray(Dother, np.float64).ravel(),
+                             *_geminal(coefficients, exponents), B, nthreads or nthreads_default())
+    return B.reshape(n, n)
+
+
+def g12_primitive(l4, alpha4, origins, coefficients, exponents) -> np.ndarray:
+    """Unnormalised primitive geminal integrals (la lb|g|lc ld), row-major."""
+    from math import prod
+    l4 = np.ascontiguousarray(l4, np.int32)
+    out = np.zeros(prod((l + 1) * (l + 2) // 2 for l in l4))
+    lib().or_g12_primitive(l4, np.ascontiguousarray(alpha4, np.float64),
+                           np.ascontiguousarray(origins, np.float64).ravel(), *_geminal(coefficients, exponents), out)
+    return out
 
 
 def two_body_directIT(b: Basis, is_electron: bool, D, C, p: int):

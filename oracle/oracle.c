@@ -17,6 +17,8 @@
  *                                        src/ints/Iterators.cpp:13-181
  *   - direct inter-species coupling      src/ints/Libint2Iface.cpp:1111-1294, 3566-3589
  *   - coupling first-quarter transform   src/ints/Libint2Iface.cpp:1296-1622, 3591-3620
+ *   - direct geminal (G12) matrices      src/ints/Libint2Iface.cpp:2193-2540, 3687-3734
+ *     (intra-species and inter-species, operator sum_k c_k exp(-g_k r12^2))
  * The ERI arithmetic itself lives in libint2 in the reference (third party, not
  * vendored; pinned at commit 668b10c4bdca5876984058742d4212675eb93f3f by the
  * reference's CI).  It is restated here from the published Obara-Saika recursion
@@ -222,10 +224,14 @@ typedef struct {
   double *Y;    /* after bra HRR */
   double *tmp;  /* HRR scratch */
   double *raw;  /* shell quartet buffer */
+  /* two-particle operator: Coulomb 1/r12 when gem_n == 0, else the contracted
+     Gaussian geminal sum_k gem_c[k] exp(-gem_g[k] r12^2) */
+  int gem_n;
+  const double *gem_c, *gem_g;
 } or_work;
 
 static or_work *work_new(void) {
-  or_work *w = (or_work *)malloc(sizeof(or_work));
+  or_work *w = (or_work *)calloc(1, sizeof(or_work));
   w->V = (double *)malloc(sizeof(double) * NCUM_MAX * NCUM_MAX * (OR_MAXLT + 1));
   w->X = (double *)malloc(sizeof(double) * NCUM_MAX * NCUM_MAX);
   w->Y = (double *)malloc(sizeof(double) * 225 * NCUM_MAX);
@@ -275,11 +281,30 @@ static void eri_shells(const or_shell *A, const or_shell *B, const or_shell *C, 
             PQ2 += (P[d] - Q[d]) * (P[d] - Q[d]);
           }
           double rho = p * q / (p + q);
-          double pref = 2.0 * pow(M_PI, 2.5) / (p * q * sqrt(p + q)) * Kab * Kcd;
           double wgt = A->cn[pa] * B->cn[pb] * C->cn[pc] * D->cn[pd];
-          or_boys(L, rho * PQ2, F);
-          /* [0|0]^(m) */
-          for (int m = 0; m <= L; ++m) V[m] = pref * F[m];
+          if (w->gem_n > 0) {
+            /* [0|0]^(m) of exp(-g r12^2): the Gaussian product integral
+               Kab Kcd (pi^2 / ((p+q)(rho+g)))^{3/2} exp(-rho g/(rho+g) |PQ|^2)
+               times (g/(rho+g))^m, the m-th (-d/dT) derivative at T = rho|PQ|^2,
+               which is what the Obara-Saika recursion below consumes for any
+               operator of r12 (Ahlrichs, Phys. Chem. Chem. Phys. 8, 3072 (2006)) */
+            for (int m = 0; m <= L; ++m) V[m] = 0.0;
+            for (int k = 0; k < w->gem_n; ++k) {
+              double g = w->gem_g[k], rg = rho + g;
+              double base = w->gem_c[k] * Kab * Kcd * pow(M_PI * M_PI / ((p + q) * rg), 1.5) *
+                            exp(-rho * g / rg * PQ2);
+              double r = g / rg, t = 1.0;
+              for (int m = 0; m <= L; ++m) {
+                V[m] += base * t;
+                t *= r;
+              }
+            }
+          } else {
+            double pref = 2.0 * pow(M_PI, 2.5) / (p * q * sqrt(p + q)) * Kab * Kcd;
+            or_boys(L, rho * PQ2, F);
+            /* [0|0]^(m) */
+            for (int m = 0; m <= L; ++m) V[m] = pref * F[m];
+          }
           double o2p = 0.5 / p, o2q = 0.5 / q, o2pq = 0.5 / (p + q), rp = rho / p, rq = rho / q;
           /* bra VRR: [e|0]^(m), m <= L-|e| */
           for (int e = 1; e < NE; ++e) {
@@ -411,6 +436,23 @@ void or_eri_primitive(const int *l4, const double *alpha4, const double *origin1
   work_free(w);
 }
 
+/* The same primitive set for the geminal operator sum_k coef[k] exp(-expo[k] r12^2). */
+void or_g12_primitive(const int *l4, const double *alpha4, const double *origin12, int npot, const double *coef,
+                      const double *expo, double *out) {
+  init_tables();
+  or_shell S[4];
+  for (int i = 0; i < 4; ++i) {
+    S[i].l = l4[i]; S[i].nprim = 1; S[i].alpha[0] = alpha4[i]; S[i].cn[0] = 1.0;
+    for (int d = 0; d < 3; ++d) S[i].O[d] = origin12[3 * i + d];
+  }
+  or_work *w = work_new();
+  w->gem_n = npot;
+  w->gem_c = coef;
+  w->gem_g = expo;
+  eri_shells(&S[0], &S[1], &S[2], &S[3], out, w);
+  work_free(w);
+}
+
 /* Significant-pair mask, Libint2Iface.cpp:3248-3342: mask[s1*nsh+s2] (s2<=s1)
    is 1 when both shells sit on the same centre or the Frobenius norm of the raw
    overlap block is >= 1e-12. */
@@ -496,16 +538,17 @@ long long or_last_quartet_count(void) { return g_last_quartets; }
    wrapper at :3510-3526 (Schwarz recomputed per call, shell pairs from
    init_2body_ints :54-67).  G = 0.25 (Gacc + Gacc^T); with factor f this is
    J[D] + f K[D].  D and G are row-major n x n. */
-void or_2body_direct(BASIS_ARGS, int is_electron, const double *D, double factor, double *Gout,
-                     int nthreads) {
+static void twobody_loops(BASIS_ARGS, int is_electron, const double *D, double factor, double *Gout,
+                          int nthreads, int gem_n, const double *gem_c, const double *gem_g) {
   or_basis *b = basis_new(BASIS_PASS);
   int n = b->nbf;
   unsigned char *mask = (unsigned char *)malloc((size_t)nsh * nsh);
   pair_mask(b, mask);
+  /* the geminal build screens nothing (Libint2Iface.cpp:2255-2330) */
+  int screen = is_electron && gem_n == 0;
   double *Q = (double *)malloc(sizeof(double) * nsh * nsh);
-  schwarz(b, Q, nthreads);
+  if (screen) schwarz(b, Q, nthreads);
   double *Dn = (double *)malloc(sizeof(double) * nsh * nsh);
-  int screen = is_electron;
   if (screen) shellblock_norm(b, D, Dn);
   const double eps = DBL_EPSILON;
   double *Gall = (double *)calloc((size_t)nthreads * n * n, sizeof(double));
@@ -518,6 +561,9 @@ void or_2body_direct(BASIS_ARGS, int is_electron, const double *D, double factor
 #endif
     double *g = Gall + (size_t)tid * n * n;
     or_work *w = work_new();
+    w->gem_n = gem_n;
+    w->gem_c = gem_c;
+    w->gem_g = gem_g;
     long long s1234 = 0;
     for (int s1 = 0; s1 < nsh; ++s1) {
       int bf1f = b->first[s1], n1 = ncart(b->sh[s1].l);
@@ -574,17 +620,32 @@ void or_2body_direct(BASIS_ARGS, int is_electron, const double *D, double factor
   basis_free(b);
 }
 
+void or_2body_direct(BASIS_ARGS, int is_electron, const double *D, double factor, double *Gout,
+                     int nthreads) {
+  twobody_loops(BASIS_PASS, is_electron, D, factor, Gout, nthreads, 0, NULL, NULL);
+}
+
+/* Direct intra-species geminal matrix, Libint2Iface.cpp:2193-2365 with the
+   wrapper at :3687-3706: the loops, degeneracies, six updates and 0.25 (G+G^T)
+   of the Coulomb build, the operator sum_k c_k exp(-g_k r12^2) (libint2's
+   contracted Gaussian geminal, parameters {g_k, c_k}), no screening of any kind. */
+void or_g12_direct(BASIS_ARGS, const double *D, double factor, int npot, const double *pot_coef,
+                   const double *pot_expo, double *Gout, int nthreads) {
+  twobody_loops(BASIS_PASS, 0, D, factor, Gout, nthreads, npot, pot_coef, pot_expo);
+}
+
 /* Direct inter-species coupling, Libint2Iface.cpp:1111-1294 and wrapper
    :3566-3589.  `this_` is the species whose matrix is built (lint), `other` the
    species whose density D (n_o x n_o) is contracted (olint).  When
    id_this > id_other the reference loops with the other species as the bra
    (permuted).  Only the lower triangle (row >= col) of the row-major result is
    written, the rest is zero; |raw| < 1e-10 integrals are skipped. */
-void or_coupling_direct(int nsh_a, const int *ls_a, const int *np_a, const double *or_a,
-                        const double *al_a, const double *co_a, int id_a,
-                        int nsh_b, const int *ls_b, const int *np_b, const double *or_b,
-                        const double *al_b, const double *co_b, int id_b,
-                        const double *D, double *Bout, int nthreads) {
+static void coupling_loops(int nsh_a, const int *ls_a, const int *np_a, const double *or_a,
+                           const double *al_a, const double *co_a, int id_a,
+                           int nsh_b, const int *ls_b, const int *np_b, const double *or_b,
+                           const double *al_b, const double *co_b, int id_b,
+                           const double *D, double *Bout, int nthreads,
+                           int gem_n, const double *gem_c, const double *gem_g) {
   or_basis *ba = basis_new(nsh_a, ls_a, np_a, or_a, al_a, co_a);
   or_basis *bo = basis_new(nsh_b, ls_b, np_b, or_b, al_b, co_b);
   int permuted = id_a > id_b;
@@ -599,6 +660,9 @@ void or_coupling_direct(int nsh_a, const int *ls_a, const int *np_a, const doubl
 #endif
     double *B = Ball + (size_t)tid * n * n;
     or_work *w = work_new();
+    w->gem_n = gem_n;
+    w->gem_c = gem_c;
+    w->gem_g = gem_g;
     long long s1234 = 0;
     for (int s1 = 0; s1 < self->nshell; ++s1)
       for (int s2 = s1; s2 < self->nshell; ++s2)
@@ -639,6 +703,29 @@ void or_coupling_direct(int nsh_a, const int *ls_a, const int *np_a, const doubl
   }
   free(Ball);
   basis_free(ba); basis_free(bo);
+}
+
+void or_coupling_direct(int nsh_a, const int *ls_a, const int *np_a, const double *or_a,
+                        const double *al_a, const double *co_a, int id_a,
+                        int nsh_b, const int *ls_b, const int *np_b, const double *or_b,
+                        const double *al_b, const double *co_b, int id_b,
+                        const double *D, double *Bout, int nthreads) {
+  coupling_loops(nsh_a, ls_a, np_a, or_a, al_a, co_a, id_a, nsh_b, ls_b, np_b, or_b, al_b, co_b, id_b, D, Bout,
+                 nthreads, 0, NULL, NULL);
+}
+
+/* Direct inter-species geminal matrix, Libint2Iface.cpp:2367-2540 with the
+   wrapper at :3708-3734: the loops, triangle rule, |raw| < 1e-10 cut and
+   lower-triangle result of the Coulomb coupling, with the operator
+   sum_k c_k exp(-g_k r12^2). */
+void or_g12inter_direct(int nsh_a, const int *ls_a, const int *np_a, const double *or_a,
+                        const double *al_a, const double *co_a, int id_a,
+                        int nsh_b, const int *ls_b, const int *np_b, const double *or_b,
+                        const double *al_b, const double *co_b, int id_b,
+                        const double *D, int npot, const double *coef, const double *expo, double *Bout,
+                        int nthreads) {
+  coupling_loops(nsh_a, ls_a, np_a, or_a, al_a, co_a, id_a, nsh_b, ls_b, np_b, or_b, al_b, co_b, id_b, D, Bout,
+                 nthreads, npot, coef, expo);
 }
 
 /* Enumeration of permutation-unique integrals inside one shell quartet, as
