@@ -74,6 +74,25 @@ def electron_species(shells, n_electrons):
             "shells": shells}
 
 
+def uhf_electron_species(shells, n_electrons, multiplicity=1):
+    """Open-shell (UHF) electrons as the reference runs them: two species,
+    E-ALPHA and E-BETA, over the same shells, each with kappa = -1, eta = 1
+    (one particle per orbital, exchange factor -1), coupled to each other by
+    the inter-species Coulomb matrix like any other species pair
+    (src/core/Species.f90, constantsOfCoupling.lib).  n_alpha - n_beta =
+    multiplicity - 1."""
+    n_beta = (int(n_electrons) - (int(multiplicity) - 1)) // 2
+    n_alpha = int(n_electrons) - n_beta
+    if n_beta < 0 or n_alpha - n_beta != int(multiplicity) - 1:
+        raise ValueError(f"{n_electrons} electrons cannot have multiplicity {multiplicity}")
+    out = []
+    for name, n in (("E-ALPHA", n_alpha), ("E-BETA", n_beta)):
+        sp = electron_species(shells, n)
+        sp.update(name=name, eta=1.0, particles_fraction=1.0)
+        out.append(sp)
+    return out
+
+
 def proton_species(shells, n_protons, name="H_1"):
     return {"name": name, "charge": 1.0, "mass": PROTON_MASS, "n_particles": int(n_protons),
             "kappa": -1.0, "eta": 1.0, "particles_fraction": 1.0, "is_electron": False,

@@ -15,7 +15,11 @@ It extracts, as data:
   * the golden values asserted by the checkers ``test/H2O.BOA.DIRECT.py``,
     ``test/H2O.BOA.MP2.DIRECT.py``, ``test/H2O.APMO.MP2.py``,
     ``test/H2O.APMO.UHF.DIRECT.py``, ``test/H2O.APMO.UMP2.DIRECT.py`` (the
-    last two use the geometry of ``test/H2O.APMO.MP2.lowdin``).
+    last two use the geometry of ``test/H2O.APMO.MP2.lowdin``),
+  * for open-shell UHF: the inputs and checkers ``test/HOO+.ROCI-HF`` (triplet
+    HOO+, cc-pVDZ electrons, DZSPNB proton), ``test/H3+.FCI`` (6-31G** electrons,
+    DZSPDN proton) and ``test/H.APMO.READCOEFF`` (one electron, cc-pVDZ, DZSNB
+    proton) with their bases (only the SCF energy of these checkers is used).
 The GPU machine has no reference tree, so the tests read only the JSON written here.
 """
 import json
@@ -63,9 +67,13 @@ def read_geometry(name):
         parts = ln.split()
         rec = {"particle": parts[0], "basis": parts[1],
                "position_bohr": [float(x) / BOHR for x in parts[2:5]]}
-        m = re.search(r"m\s*=\s*([0-9.Ee+-]+)", ln)
+        m = re.search(r"(?<![A-Za-z])m\s*=\s*([0-9.Ee+-]+)", ln)
         if m:
             rec["mass"] = float(m.group(1))
+        for key, name in (("addParticles", "add_particles"), ("multiplicity", "multiplicity")):
+            m = re.search(key + r"\s*=\s*([-0-9]+)", ln, re.IGNORECASE)
+            if m:
+                rec[name] = int(m.group(1))
         rows.append(rec)
     return rows
 
@@ -91,10 +99,19 @@ def main():
             "6-311G:H": read_basis("6-311G", "HYDROGEN", "H"),
             "6-311G:O": read_basis("6-311G", "OXYGEN", "O"),
             "NAKAI-5-SPD:H_1": read_basis("NAKAI-5-SPD", "HYDROGEN_1", "H_1"),
+            "CC-PVDZ:H": read_basis("CC-PVDZ", "HYDROGEN", "H"),
+            "CC-PVDZ:O": read_basis("CC-PVDZ", "OXYGEN", "O"),
+            "6-31G.D.P:H": read_basis("6-31G.D.P", "HYDROGEN", "H"),
+            "DZSNB:H_1": read_basis("DZSNB", "HYDROGEN", "H_1"),
+            "DZSPNB:H_1": read_basis("DZSPNB", "HYDROGEN", "H_1"),
+            "DZSPDN:H_1": read_basis("DZSPDN", "HYDROGEN", "H_1"),
         },
         "geometry": {
             "H2O.BOA.DIRECT": read_geometry("H2O.BOA.DIRECT.lowdin"),
             "H2O.APMO.MP2": read_geometry("H2O.APMO.MP2.lowdin"),
+            "HOO+.ROCI-HF": read_geometry("HOO+.ROCI-HF.lowdin"),
+            "H3+.FCI": read_geometry("H3+.FCI.lowdin"),
+            "H.APMO.READCOEFF": read_geometry("H.APMO.READCOEFF.lowdin"),
         },
         "values": {
             "H2O.BOA.DIRECT": read_checker("H2O.BOA.DIRECT.py"),
@@ -102,6 +119,9 @@ def main():
             "H2O.APMO.MP2": read_checker("H2O.APMO.MP2.py"),
             "H2O.APMO.UHF.DIRECT": read_checker("H2O.APMO.UHF.DIRECT.py"),
             "H2O.APMO.UMP2.DIRECT": read_checker("H2O.APMO.UMP2.DIRECT.py"),
+            "HOO+.ROCI-HF": read_checker("HOO+.ROCI-HF.py"),
+            "H3+.FCI": read_checker("H3+.FCI.py"),
+            "H.APMO.READCOEFF": read_checker("H.APMO.READCOEFF.py"),
         },
     }
     with open(OUT, "w") as f:

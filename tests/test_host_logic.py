@@ -155,3 +155,17 @@ def test_bench_per_job_table_and_tuning_summary():
     s = bench.tuning_summary([(ch, ms, 2 * ms)])
     assert s["batches"] == 1
     assert s["classes"]["(ss|ss)"]["rows_kernel"] == 1 and s["classes"]["(ps|ss)"]["tile_kernel"] == 1
+
+
+def test_uhf_electron_species_counts():
+    from openlowdin_gb300 import systems as S
+    shells = [(0, [1.0], [1.0], [0.0, 0.0, 0.0])]
+    a, b = S.uhf_electron_species(shells, 16, 3)
+    assert (a["name"], a["n_particles"], b["name"], b["n_particles"]) == ("E-ALPHA", 9, "E-BETA", 7)
+    for sp in (a, b):
+        assert sp["eta"] == 1.0 and sp["kappa"] / sp["eta"] == -1.0 and sp["particles_fraction"] == 1.0
+    a, b = S.uhf_electron_species(shells, 1, 2)
+    assert (a["n_particles"], b["n_particles"]) == (1, 0)
+    import pytest
+    with pytest.raises(ValueError):
+        S.uhf_electron_species(shells, 2, 2)
