@@ -79,6 +79,7 @@ def parse():
     ap.add_argument("--batch", type=int, default=8, help="molecules of the APMO batch section (0: off)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C ABI leg")
+    ap.add_argument("--e2e-plain", action="store_true", help="also run the host-buffer C ABI leg in plain FP64")
     ap.add_argument("--no-mp2", action="store_true", help="skip the d-shell MP2 transform section")
     ap.add_argument("--mp2-waters", type=int, default=16)
     ap.add_argument("--random-molecules", type=int, default=16,
@@ -318,20 +319,23 @@ def per_job_table(reqs, plain, mixed):
 
 
 # ------------------------------------------------ e2e: reference-facing ABI --
-def e2e_stream(reqs, workers=16):
+def e2e_stream(reqs, precision="mixed", workers=16):
     """The stream's requests through the reference-facing C ABI with host
     buffers: HostSCF calls LibintInterface_compute_2body_direct every
     iteration (host density in, host matrix out, the copies inside), host
     linear algebra as the Fortran caller does; MP2 requests then run
-    LowdinGB300_mp2_direct on orbitals copied in from the host.  Requests are
-    solved concurrently (one host thread each, up to `workers`)."""
+    LowdinGB300_mp2_direct on orbitals copied in from the host.  "mixed": the
+    handles' FP32/FP64 split (LowdinGB300_set_precision), density changes
+    passed in after the first build, an FP64 build at the converged density
+    for the stated error, split-BF16 MP2.  Requests are solved concurrently
+    (one host thread each, up to `workers`)."""
     import concurrent.futures as cf
     import numpy as np
     import torch
     from openlowdin_gb300 import lint, scf, systems as S
 
     def one(q):
-        hs = scf.HostSCF(q.system)
+        hs = scf.HostSCF(q.system, precision=precision)
         r = hs.solve(tol_energy=1e-10, tol_density=1e-8) if q.kind == "scf+mp2" else \
             hs.solve(tol_energy=1e-8, tol_density=1e-6)
         n = hs.handles[0].nbasis
@@ -345,8 +349,8 @@ def e2e_stream(reqs, workers=16):
                 dC = torch.from_numpy(np.ascontiguousarray(r.coefficients[0].T)).pin_memory().to(
                     "cuda", non_blocking=True)
                 e2 = hs.handles[0].mp2_direct(dD.data_ptr(), dC.data_ptr(), r.orbital_energies[0],
-                                              sp["n_particles"] // 2, S.n_core(q.system), 0, 8.0,
-                                              stream=st.cuda_stream)
+                                              sp["n_particles"] // 2, S.n_core(q.system),
+                                              2 if precision == "mixed" else 0, 8.0, stream=st.cuda_stream)
             up += 2 * 8 * n * n
             down += 8
         hs.close()
@@ -740,19 +744,28 @@ def main():
 
     if rank == 0:
         if not args.no_e2e:
-            e2e_res, e2e_wall = e2e_stream(reqs)
-            up = sum(x[2] for x in e2e_res)
-            down = sum(x[3] for x in e2e_res)
-            conv = sum(x[0].converged for x in e2e_res)
-            de_e2e = [abs(x[0].energy - plain[q.rid].energy) for x, q in zip(e2e_res, reqs)
-                      if x[0].converged and plain[q.rid].converged]
-            out["e2e"] = {"value": conv / e2e_wall, "unit": UNIT, "h2d_bytes_per_step": up // len(reqs),
-                          "d2h_bytes_per_step": down // len(reqs), "wall_s": e2e_wall, "converged": int(conv),
-                          "max_abs_dE_vs_plain_engine_Eh": max(de_e2e) if de_e2e else None,
-                          "path": "HostSCF: LibintInterface_compute_2body_direct with host buffers every "
-                                  "iteration (FP64, the reference program's calling pattern; host linear "
-                                  "algebra), MP2 via LowdinGB300_mp2_direct on orbitals copied from the "
-                                  "host; requests solved concurrently, one host thread each"}
+            for prec in (("mixed", "fp64") if args.e2e_plain else ("mixed",)):
+                e2e_res, e2e_wall = e2e_stream(reqs, prec)
+                up = sum(x[2] for x in e2e_res)
+                down = sum(x[3] for x in e2e_res)
+                conv = sum(x[0].converged for x in e2e_res)
+                de_e2e = [abs(x[0].energy - plain[q.rid].energy) for x, q in zip(e2e_res, reqs)
+                          if x[0].converged and plain[q.rid].converged]
+                chk = [x[0].err_vs_fp64 for x in e2e_res if x[0].err_vs_fp64 is not None]
+                line = {"value": conv / e2e_wall, "unit": UNIT, "h2d_bytes_per_step": up // len(reqs),
+                        "d2h_bytes_per_step": down // len(reqs), "wall_s": e2e_wall, "converged": int(conv),
+                        "precision": prec,
+                        "max_abs_dE_vs_plain_engine_Eh": max(de_e2e) if de_e2e else None,
+                        "max_err_vs_fp64_check_Eh": max(chk) if chk else None,
+                        "guard_hits": int(sum(bool(x[0].guard_hit) for x in e2e_res)),
+                        "path": "HostSCF: LibintInterface_compute_2body_direct with host buffers every "
+                                "iteration (the reference program's calling pattern; host linear algebra), "
+                                + ("the handles' FP32/FP64 split set once by LowdinGB300_set_precision, density "
+                                   "changes after the first build, an FP64 build at the converged density, "
+                                   if prec == "mixed" else "FP64, ")
+                                + "MP2 via LowdinGB300_mp2_direct on orbitals copied from the host; requests "
+                                  "solved concurrently, one host thread each"}
+                out["e2e" if prec == "mixed" else "e2e_plain_fp64"] = line
         big = reqs[int(np.argmax(sizes))].system
         out["roofline"] = roofline_section(big)
         if not args.no_cpu_baseline:

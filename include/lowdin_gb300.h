@@ -152,6 +152,15 @@ void LowdinGB300_clear_error(void);
    row-major n x n, host memory. */
 void LowdinGB300_potential(LibintInterface *lint, int ncharge, const double *Z, const double *R, double *result);
 
+/* Precision of this handle's LibintInterface_compute_2body_direct (host
+   buffers, the reference's own call): 0 = FP64 (default, the reference's
+   behaviour); 1 = quartets whose Schwarz bound times the density's shell-block
+   maximum is below `split` run in FP32, the rest in FP64 (a caller that passes
+   density changes gets the incremental mixed-precision build of the north
+   star's SCF).  The coupling and first-quarter calls stay FP64.  Returns 0, or
+   -1 for an unknown precision or a split outside (0, 1). */
+int LowdinGB300_set_precision(LibintInterface *lint, int precision, double split);
+
 /* Device-resident two-particle matrix: dG = J[dD] + factor K[dD] (n x n device
    buffers, full symmetric).  precision: 0 = FP64, 1 = mixed (quartets whose
    Schwarz-density bound is below `split` run in FP32, the rest in FP64).

@@ -615,7 +615,7 @@ void LibintInterface_compute_2body_direct(LibintInterface *lint, double *dens, d
     set_error("compute_2body_direct: density upload failed");
     return;
   }
-  if (!lint->twobody(lint->dD.p, lint->dG.p, factor, 0, 0.0, s)) return;
+  if (!lint->twobody(lint->dD.p, lint->dG.p, factor, lint->abi_precision, lint->abi_split, s)) return;
   if (cudaMemcpyAsync(result, lint->dG.p, sizeof(double) * n * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     set_error("compute_2body_direct: result download failed");
@@ -823,6 +823,21 @@ int LowdinGB300_one_body_device(LibintInterface *lint, int ncharge, const double
     set_error("%s: %s", __func__, cudaGetErrorString(e));
     return -1;
   }
+  return 0;
+}
+
+int LowdinGB300_set_precision(LibintInterface *lint, int precision, double split) {
+  if (!check_handle(lint, __func__)) return -1;
+  if (precision != 0 && precision != 1) {
+    set_error("%s: precision must be 0 (FP64) or 1 (FP32/FP64 split), got %d", __func__, precision);
+    return -1;
+  }
+  if (precision == 1 && !(split > 0.0 && split < 1.0)) {
+    set_error("%s: split bound %g outside (0, 1)", __func__, split);
+    return -1;
+  }
+  lint->abi_precision = precision;
+  lint->abi_split = precision ? split : 0.0;
   return 0;
 }
 

@@ -270,6 +270,10 @@ struct LibintInterface {
   int *d_first = nullptr;
   DevBuf<double> dZR;          // point charges and positions of the last one-body call
   DevBuf<double> dGem;         // geminal parameters of the last G12 call {count, exponents, coefficients}
+  // precision of LibintInterface_compute_2body_direct (LowdinGB300_set_precision):
+  // 0 = FP64 (the reference's behaviour), 1 = FP32/FP64 split at abi_split
+  int abi_precision = 0;
+  double abi_split = 1e-5;
   DevBuf<double> dD, dDs, dDn, dGacc, dG, dA, dC, dDsC, dJacc;
   DevBuf<float> dDs32, dDn32, dGacc32, dDsC32, dJacc32;
   DevBuf<float> dDp32, dJp32, dDnP32;   // pair-indexed arrays of the FP32 row kernels

@@ -53,6 +53,8 @@ def lib():
         L.LibintInterface_compute_2body_directIT.argtypes = [_vp, _f64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int)]
         L.LibintInterface_compute_coupling_direct.argtypes = [_vp, _vp, _f64p, _f64p]
         L.LibintInterface_compute_alphabeta_direct.argtypes = [_vp, _vp, _f64p, _f64p, _f64p]
+        L.LowdinGB300_set_precision.argtypes = [_vp, ctypes.c_int, ctypes.c_double]
+        L.LowdinGB300_set_precision.restype = ctypes.c_int
         L.libintinterface_compute_g12_direct.argtypes = [_vp, _f64p, _f64p, ctypes.POINTER(ctypes.c_double),
                                                          _f64p, _f64p, ctypes.c_int]
         L.libintinterface_compute_g12inter_direct.argtypes = [_vp, _vp, _f64p, _f64p, _f64p, _f64p, ctypes.c_int]
@@ -158,7 +160,7 @@ EXPORTED_SYMBOLS = [
     "libintinterface_compute_g12inter_direct", "LibintInterface_compute_2body_directAll",
     "LibintInterface_compute_coupling_directAll", "libintinterface_compute_g12_directAll",
     "libintinterface_compute_g12inter_directAll", "LowdinGB300_last_error", "LowdinGB300_clear_error",
-    "LowdinGB300_potential", "LowdinGB300_twobody_device", "LowdinGB300_one_body_device", "LowdinGB300_coupling_device",
+    "LowdinGB300_potential", "LowdinGB300_set_precision", "LowdinGB300_twobody_device", "LowdinGB300_one_body_device", "LowdinGB300_coupling_device",
     "LowdinGB300_last_quartets", "LowdinGB300_version", "LowdinGB300_last_class_quartets",
     "LowdinGB300_pair_class_counts", "LowdinGB300_measure_fma_tflops", "LowdinGB300_launch_count",
     "LowdinGB300_batch_new", "LowdinGB300_batch_del", "LowdinGB300_batch_add_system",
@@ -379,6 +381,11 @@ class Libint2Interface:
                                                        np.ascontiguousarray(other_density, np.float64), out)
         _check()
         return float(out[0])
+
+    def set_precision(self, precision: int, split: float = 1e-5):
+        """Precision of compute_2body_direct: 0 FP64, 1 FP32/FP64 split at `split`."""
+        if lib().LowdinGB300_set_precision(self.h, int(precision), float(split)) != 0:
+            _check()
 
     def compute_g12_direct(self, density, factor: float, coefficients, exponents) -> np.ndarray:
         """Libint2Interface_computeG12Intraspecies_direct: the two-particle matrix of

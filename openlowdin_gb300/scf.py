@@ -177,11 +177,24 @@ class _DIIS:
 
 class HostSCF:
     """SCF whose integral work goes through the host-buffer C ABI each
-    iteration (the reference program's calling pattern)."""
+    iteration (the reference program's calling pattern).
 
-    def __init__(self, sysd):
+    precision "mixed": the handles' compute_2body_direct runs the FP32/FP64
+    split (LowdinGB300_set_precision) and the caller passes density changes:
+    a full build on the first iteration, then G += G[P - P_ref]; when the
+    energy and density converge, one full FP64 build at the converged density
+    gives the result's energy and its stated error |E_mixed - E_FP64|; above
+    guard_energy, or with an FP64 commutator element above guard_commutator,
+    the solve continues in FP64 with a fresh DIIS history.  Couplings stay
+    FP64 full builds."""
+
+    def __init__(self, sysd, precision="fp64", split=1e-5, guard_energy=1e-6, guard_commutator=1e-4):
+        if precision not in ("fp64", "mixed"):
+            raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
         self.sysd = sysd
         self.species = sysd["species"]
+        self.precision, self.split = precision, split
+        self.guard_energy, self.guard_commutator = guard_energy, guard_commutator
         self.handles = [lint.Libint2Interface(sp, i + 1) for i, sp in enumerate(self.species)]
         for h in self.handles:
             h.init_2body_ints()
@@ -193,10 +206,19 @@ class HostSCF:
         for h in self.handles:
             h.close()
 
+    def _set_split(self, on: bool):
+        for h in self.handles:
+            h.set_precision(1 if on else 0, self.split)
+
     def solve(self, tol_energy=1e-8, tol_density=1e-6, max_iter=100) -> SCFResult:
         t0 = time.perf_counter()
         sp, H, S, X = self.species, self.H, self.S, self.X
         ns = len(sp)
+        mixed = self.precision == "mixed"
+        fp64 = not mixed          # builds in FP64 (plain, the FP64 check, after a failed check)
+        checking = False          # this iteration's build is the FP64 check
+        e_mixed, err_vs_fp64, guard_hit = None, None, False
+        self._set_split(mixed)
         P, C, eps = [], [], []
         for i in range(ns):
             e, Cp = np.linalg.eigh(X[i].T @ H[i] @ X[i])
@@ -204,15 +226,21 @@ class HostSCF:
             C.append(Ci); eps.append(e)
             o = n_occ(sp[i])
             P.append(sp[i]["eta"] * Ci[:, :o] @ Ci[:, :o].T)
+        Pref, Gprev = [None] * ns, [None] * ns
         diis = _DIIS(np)
         e_old, converged, it, quartets = None, False, 0, 0
         energy = 0.0
         for it in range(1, max_iter + 1):
+            full = fp64 or it == 1
             G, J = [], [[None] * ns for _ in range(ns)]
             for i in range(ns):
                 if sp[i]["n_particles"] > 1:
                     f = sp[i]["kappa"] / sp[i]["eta"]
-                    G.append(self.handles[i].compute_2body_direct(P[i], f) * sp[i]["charge"] ** 2)
+                    q2 = sp[i]["charge"] ** 2
+                    if full:
+                        G.append(self.handles[i].compute_2body_direct(P[i], f) * q2)
+                    else:
+                        G.append(Gprev[i] + self.handles[i].compute_2body_direct(P[i] - Pref[i], f) * q2)
                     quartets += max(0, self.handles[i].last_quartets())
                 else:
                     G.append(np.zeros_like(H[i]))
@@ -222,6 +250,7 @@ class HostSCF:
                     B = self.handles[i].compute_coupling_direct(self.handles[j], P[j])
                     B = (np.tril(B) + np.tril(B, -1).T) * sp[i]["charge"] * sp[j]["charge"]
                     J[i][j] = B
+            Pref, Gprev = [p.copy() for p in P], G
             F = [H[i] + G[i] + sum(J[i][j] for j in range(ns) if j != i) for i in range(ns)]
             energy = self.enuc
             for i in range(ns):
@@ -229,6 +258,19 @@ class HostSCF:
                 for j in range(i + 1, ns):
                     energy += float(np.sum(P[i] * J[i][j]))
             errs = [X[i].T @ (F[i] @ P[i] @ S[i] - S[i] @ P[i] @ F[i]) @ X[i] for i in range(ns)]
+            if checking:
+                checking = False
+                err_vs_fp64 = abs(e_mixed - energy)
+                comm = max(float(np.max(np.abs(e))) for e in errs)
+                if err_vs_fp64 <= self.guard_energy and comm <= self.guard_commutator:
+                    # the FP64 energy is the result; orbitals of the FP64 Fock matrix
+                    for i in range(ns):
+                        e, Cp = np.linalg.eigh(X[i].T @ F[i] @ X[i])
+                        C[i], eps[i] = X[i] @ Cp, e
+                    converged = True
+                    break
+                guard_hit = True                  # continue in FP64 from this build
+                diis, e_old = _DIIS(np), None
             Fx = diis(F, errs)
             dmax = 0.0
             newP = []
@@ -241,11 +283,18 @@ class HostSCF:
                 dmax = max(dmax, float(np.sqrt(np.mean((Pn - P[i]) ** 2))))
                 newP.append(Pn)
             if e_old is not None and abs(energy - e_old) < tol_energy and dmax < tol_density:
+                if not fp64:
+                    # FP64 check: a full FP64 build at this iteration's density
+                    fp64, checking, e_mixed = True, True, energy
+                    self._set_split(False)
+                    continue
                 converged = True
                 break
             e_old = energy
             P = newP
-        return SCFResult(energy, it, converged, time.perf_counter() - t0, eps, C, P, quartets)
+        self._set_split(False)
+        return SCFResult(energy, it, converged, time.perf_counter() - t0, eps, C, P, quartets,
+                         err_vs_fp64=err_vs_fp64, guard_hit=guard_hit)
 
 
 class DeviceSCF:

@@ -272,3 +272,44 @@ def test_batch_mixed_fp64_check_and_guard():
     for p, f in zip(plain, forced):
         assert f.converged and f.guard_hit and f.err_vs_fp64 == 0.0
         assert abs(f.energy - p.energy) < 1e-8
+
+
+def test_host_abi_mixed_precision_matches_plain(scf):
+    """The reference-shaped host-buffer calls with the handle's FP32/FP64 split
+    (LowdinGB300_set_precision) and incremental builds: within 1e-6 Eh of the
+    plain FP64 solve, with the FP64 check's stated error."""
+    sysd = S.chain_for_basis(10_003, 120)
+    s = scf.HostSCF(sysd)
+    rp = s.solve(tol_energy=1e-10, tol_density=1e-8)
+    s.close()
+    s = scf.HostSCF(sysd, precision="mixed")
+    rm = s.solve(tol_energy=1e-10, tol_density=1e-8)
+    s.close()
+    assert rp.converged and rm.converged
+    assert rm.err_vs_fp64 is not None and rm.err_vs_fp64 <= 1e-6
+    assert not rm.guard_hit
+    assert abs(rm.energy - rp.energy) <= 1e-6
+
+
+def test_host_abi_mixed_guard_continues_in_fp64(scf):
+    """A guard bar no mixed build meets: the check fires and the solve ends in
+    FP64 on the plain energy."""
+    sysd = S.water()
+    s = scf.HostSCF(sysd)
+    rp = s.solve(tol_energy=1e-10, tol_density=1e-8)
+    s.close()
+    s = scf.HostSCF(sysd, precision="mixed", split=0.5, guard_energy=1e-15)
+    rm = s.solve(tol_energy=1e-10, tol_density=1e-8)
+    s.close()
+    assert rm.converged and rm.guard_hit
+    assert abs(rm.energy - rp.energy) <= 1e-8
+
+
+def test_set_precision_rejects_bad_arguments(scf):
+    from openlowdin_gb300 import lint
+    h = lint.Libint2Interface(S.water()["species"][0], 1)
+    with pytest.raises(lint.LowdinGB300Error, match="precision"):
+        h.set_precision(3)
+    with pytest.raises(lint.LowdinGB300Error, match="split"):
+        h.set_precision(1, 2.0)
+    h.close()
