@@ -32,6 +32,7 @@ struct LowdinGB300_Batch {
   DevBuf<SpeciesSlot> slots;
   // pair-indexed arrays of the FP32 row kernels, one PairSlot per two-body species
   DevBuf<float> Dp32, Jp32, DnP32;
+  DevBuf<float> Dnmax32;   // per slot: largest shell-block norm of the build's input
   DevBuf<PairSlot> pslots;
   int npslots = 0;
   long long ptotal = 0;
@@ -127,7 +128,7 @@ struct LowdinGB300_Batch {
       pptot += (long long)sp[k].h->sig.h.size();
     }
     if (!Dp32.ensure(std::max(1LL, petot)) || !Jp32.ensure(std::max(1LL, petot)) ||
-        !DnP32.ensure(std::max(1LL, pptot)))
+        !DnP32.ensure(std::max(1LL, pptot)) || !Dnmax32.ensure(std::max<size_t>(1, sp.size())))
       return false;
     std::vector<PairSlot> hps;
     std::vector<SpeciesSlot> hs(sp.size());
@@ -173,10 +174,11 @@ struct LowdinGB300_Batch {
       S.off = off[k];
       S.ld = x.ld > 0 ? x.ld : S.n;
       S.active = active.p + x.sys;
+      S.Dnmax32 = S.Dn32 ? Dnmax32.p + k : nullptr;
       if (x.two_body) {
         // non-electron species are not screened: their norm pointers are never read
         SpeciesBufs b{S.Ds, S.Ds32, S.Dn ? S.Dn : Dn.p, S.Dn32 ? S.Dn32 : Dn32.p, S.Gacc, S.Gacc32,
-                      Dp32.p + peoff[k], Jp32.p + peoff[k], DnP32.p + pairoff[k]};
+                      Dp32.p + peoff[k], Jp32.p + peoff[k], DnP32.p + pairoff[k], S.Dnmax32};
         const auto before = sizes(jk);
         if (!x.h->add_jk_tasks(jk, b, 0.5 * x.factor, cnt.p)) return false;
         mark(jk, before, x.sys);
@@ -291,6 +293,7 @@ struct LowdinGB300_Batch {
     CK(cudaMemsetAsync(Dn.p, 0, Dn.n * sizeof(double), s));
     CK(cudaMemsetAsync(Dn32.p, 0, Dn32.n * sizeof(float), s));
     CK(launch_prepare_batch(slots.p, nslots, total, s));
+    CK(launch_dn_max_batch(slots.p, nslots, s));
     if (npslots) CK(launch_pair_gather(pslots.p, npslots, ptotal, s));
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -354,6 +357,7 @@ struct LowdinGB300_Batch {
     CK(cudaMemsetAsync(cnt.p, 0, 2 * kNQC * sizeof(unsigned long long), s));
     CK(launch_prepare_batch(slots.p, nslots, total, s));
     const int jk_mixed = precision & 1;
+    if (jk_mixed) CK(launch_dn_max_batch(slots.p, nslots, s));
     if (jk_mixed && npslots) CK(launch_pair_gather(pslots.p, npslots, ptotal, s));
     if (!LibintInterface::launch_jk_groups(jk, jk_mixed, jk_mixed ? split : 0.0, boys, s, skip, rows_choice))
       return false;

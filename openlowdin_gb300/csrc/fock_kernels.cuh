@@ -122,6 +122,15 @@ __global__ void __launch_bounds__(128) jk_tasks_kernel(const JKTask *__restrict_
   const int local = blockIdx.x - T.blk0;
   const int tx = local % T.nbx, ty = local / T.nbx;
   if (T.triangle && tx * 32 > ty * kWarpsPerBlock + kWarpsPerBlock - 1) return;
+  if (TL.mixed && act != kSysFP64 && ty * kWarpsPerBlock < T.nbra && (T.Dnmax32 || !T.screen)) {
+    // The tile's first bra and first ket carry its largest Schwarz factors and
+    // Dnmax32 bounds the six norms, so in FP32 (rounding is monotonic, same
+    // order of products) ub >= every quartet bound b of the tile: a tile the
+    // launch cannot take leaves before staging its records.
+    float ub = T.pairs32[T.bra0 + ty * kWarpsPerBlock].Q * T.pairs32[T.ket0 + tx * 32].Q;
+    if (T.screen) ub *= __ldg(T.Dnmax32);
+    if (TL.lower ? (T.screen && ub < fmaxf(TL.eps32, TL.skip)) : ub < TL.split32) return;
+  }
   const PairT<R> *pairs;
   const PrimT<R> *prims;
   const R *D;
@@ -322,6 +331,15 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
   const int n = T.n, nsh = T.nsh;
   const PairRec32 bra = T.pairs32[bi];
   const PrimRec32 *__restrict__ prims = T.prims32;
+  const float cutoff = fmaxf(TL.eps32, TL.skip);
+  // kets are sorted by decreasing Schwarz factor: bra.Q Q(ket k0) Dnmax32 bounds
+  // every quartet bound from ket position k0 on (same FP32 product order)
+  const float dmax = (T.screen && T.Dnmax32) ? __ldg(T.Dnmax32) : -1.f;
+  auto below_from = [&](int k0) {
+    const float qk = T.soa32 ? T.soa32[kSoaQ * T.npairs + T.ket0 + k0] : T.pairs32[T.ket0 + k0].Q;
+    return dmax >= 0.f && bra.Q * qk * dmax < cutoff;
+  };
+  if (below_from(0)) return;   // nothing of this bra row reaches the cutoff
   float *Drow = rsm;                 // [n][NRP]: D(fa + r, col) for r < NA, D(fb + r - NA, col) after
   float *Krow = rsm + NRP * n;       // [n][NRP]: exchange accumulators of the same rows
   float *Dnab = Krow + NRP * n;      // [nsh]
@@ -340,7 +358,6 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
   const float hf = T.hf32;
   const float *__restrict__ D = T.Ds32;
   float *G32 = T.Gacc32;
-  const float cutoff = fmaxf(TL.eps32, TL.skip);
   float j12[NA * NB];
 #pragma unroll
   for (int x = 0; x < NA * NB; ++x) j12[x] = 0.f;
@@ -353,6 +370,7 @@ __global__ void __launch_bounds__(32 * kRowWarps) jk32_row_kernel(const JKTask *
   const int kstride = T.nket;                     // element stride of the pair-indexed arrays
   unsigned cnt = 0;
   for (int k0 = warp * 32; k0 < nk; k0 += 32 * kRowWarps) {
+    if (below_from(k0)) break;   // warp-uniform; every later ket chunk is below too
     const int kpos = k0 + lane;
     bool active = kpos < nk;
     const int kq = min(kpos, nk - 1);

@@ -143,6 +143,37 @@ __global__ void prepare_batch_kernel(const SpeciesSlot *__restrict__ slots, int 
   }
 }
 
+// largest shell-block norm: one block per slot (or one block for one array)
+__device__ __forceinline__ float block_max(float m) {
+  __shared__ float part[32];
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  }
+  return m;   // valid in thread 0
+}
+
+__global__ void dn_max_batch_kernel(const SpeciesSlot *__restrict__ slots) {
+  const SpeciesSlot &S = slots[blockIdx.x];
+  if (!S.Dn32 || !S.Dnmax32) return;
+  if (S.active && __ldg(S.active) == 0) return;
+  const int cnt = S.nsh * S.nsh;
+  float m = 0.f;
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) m = fmaxf(m, S.Dn32[i]);
+  m = block_max(m);
+  if (threadIdx.x == 0) *S.Dnmax32 = m;
+}
+
+__global__ void dn_max_kernel(const float *__restrict__ Dn32, int cnt, float *__restrict__ out) {
+  float m = 0.f;
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) m = fmaxf(m, Dn32[i]);
+  m = block_max(m);
+  if (threadIdx.x == 0) *out = m;
+}
+
 // G = gscale N (Gacc + Gacc^T) N (0 when the species builds none), J = N Jacc N,
 // FP32 accumulators added in
 __global__ void finalize_batch_kernel(const SpeciesSlot *__restrict__ slots, int nslots, long long total) {
@@ -257,6 +288,19 @@ long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 cudaError_t launch_prepare_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s) {
   if (total <= 0) return cudaSuccess;
   prepare_batch_kernel<<<grid_for((size_t)total, 256), 256, 0, s>>>(slots, nslots, total);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dn_max_batch(const SpeciesSlot *slots, int nslots, cudaStream_t s) {
+  if (nslots <= 0) return cudaSuccess;
+  dn_max_batch_kernel<<<nslots, 256, 0, s>>>(slots);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dn_max(const float *Dn32, int count, float *out, cudaStream_t s) {
+  dn_max_kernel<<<1, 1024, 0, s>>>(Dn32, count, out);
   count_launches(1);
   return cudaGetLastError();
 }

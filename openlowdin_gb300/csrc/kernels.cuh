@@ -110,6 +110,11 @@ struct JKTask {
   const float *Dp32;
   float *Jp32;
   const float *DnP32;
+  // largest element of Dn32 (null: unknown).  Pair records are sorted by
+  // decreasing Schwarz factor inside a class, so Q(first bra) Q(first ket)
+  // Dnmax32 bounds every quartet bound of a tile or of a ket range after it:
+  // the mixed launches leave ranges that bound cannot reach at once
+  const float *Dnmax32;
 };
 
 // One coupling task: quartets (A pair | B pair) of two species; accumulates
@@ -345,8 +350,13 @@ struct SpeciesSlot {
   int ld;                 // row stride of P, G and J (>= n; the arenas are n x n)
   long long off;          // prefix of n*n over the slots
   const int *active;      // the slot's system is built while *active != 0 (null: always)
+  float *Dnmax32;         // largest element of Dn32 (null: not computed)
 };
 cudaError_t launch_prepare_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s);
+// Dnmax32 of every slot that has Dn32 (after launch_prepare_batch)
+cudaError_t launch_dn_max_batch(const SpeciesSlot *slots, int nslots, cudaStream_t s);
+// *out = max of Dn32[0 .. count)
+cudaError_t launch_dn_max(const float *Dn32, int count, float *out, cudaStream_t s);
 
 // pair-indexed copies of a species' FP32 density for the FP32 row kernels:
 // for every significant pair (class c, position k in its class) and element e

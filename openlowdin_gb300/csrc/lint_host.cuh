@@ -176,6 +176,7 @@ struct SpeciesBufs {
   float *Dp32 = nullptr;
   float *Jp32 = nullptr;
   float *DnP32 = nullptr;
+  const float *Dnmax32 = nullptr;   // largest element of Dn32, or null
 };
 
 // Tasks grouped by quartet class (bra pair class * 6 + ket pair class); one
@@ -277,6 +278,7 @@ struct LibintInterface {
   DevBuf<double> dD, dDs, dDn, dGacc, dG, dA, dC, dDsC, dJacc;
   DevBuf<float> dDs32, dDn32, dGacc32, dDsC32, dJacc32;
   DevBuf<float> dDp32, dJp32, dDnP32;   // pair-indexed arrays of the FP32 row kernels
+  DevBuf<float> dDnmax32;               // largest shell-block norm of the last density
   DevBuf<PairSlot> dpslot;
   DevBuf<unsigned long long> dcount;
   unsigned long long *hcount = nullptr;   // pinned copy of dcount, read once its stream is done
@@ -308,7 +310,7 @@ struct LibintInterface {
     dD.release(); dDs.release(); dDn.release(); dGacc.release(); dG.release(); dA.release(); dC.release();
     dDsC.release(); dJacc.release();
     dDs32.release(); dDn32.release(); dGacc32.release(); dDsC32.release(); dJacc32.release();
-    dDp32.release(); dJp32.release(); dDnP32.release(); dpslot.release();
+    dDp32.release(); dJp32.release(); dDnP32.release(); dpslot.release(); dDnmax32.release();
     dcount.release();
     if (hcount) cudaFreeHost(hcount);
     hcount = nullptr;
@@ -508,7 +510,7 @@ struct LibintInterface {
       const long long pe = pair_elements(sig.start, pe_base);
       const int npairs = (int)sig.h.size();
       if (!dDp32.ensure(std::max(1LL, pe)) || !dJp32.ensure(std::max(1LL, pe)) ||
-          !dDnP32.ensure(std::max(1, npairs)) || !dpslot.ensure(1))
+          !dDnP32.ensure(std::max(1, npairs)) || !dpslot.ensure(1) || !dDnmax32.ensure(1))
         return false;
       PairSlot ps{};
       ps.pairs = sig.d32;
@@ -527,13 +529,14 @@ struct LibintInterface {
       ps.active = nullptr;
       CK(cudaMemcpyAsync(dpslot.p, &ps, sizeof(ps), cudaMemcpyHostToDevice, s));
       jk.clear();
-      SpeciesBufs b{dDs.p, dDs32.p, dDn.p, dDn32.p, dGacc.p, dGacc32.p, dDp32.p, dJp32.p, dDnP32.p};
+      SpeciesBufs b{dDs.p, dDs32.p, dDn.p, dDn32.p, dGacc.p, dGacc32.p, dDp32.p, dJp32.p, dDnP32.p, dDnmax32.p};
       if (!add_jk_tasks(jk, b, 0.5 * factor, dcount.p)) return false;
       if (!jk.upload(s)) return false;
       jk_hf = 0.5 * factor;
       jk_ready = true;
     }
     CK(launch_prepare_density(dDin, d_norma, d_shell_of, n, nsh, dDs.p, dDs32.p, dDn.p, dDn32.p, s));
+    if (precision != 0 && is_electron) CK(launch_dn_max(dDn32.p, nsh * nsh, dDnmax32.p, s));
     CK(cudaMemsetAsync(dGacc.p, 0, sizeof(double) * n * n, s));
     CK(cudaMemsetAsync(dGacc32.p, 0, sizeof(float) * n * n, s));
     CK(cudaMemsetAsync(dcount.p, 0, sizeof(unsigned long long) * kNQC, s));
@@ -598,6 +601,7 @@ struct LibintInterface {
         t.screen = is_electron ? 1 : 0;
         t.soa32 = sig.soa32;
         t.npairs = (int)sig.h.size();
+        t.Dnmax32 = is_electron ? bf.Dnmax32 : nullptr;
         if (bf.Dp32) {
           long long pe_base[kNumPairClasses];
           pair_elements(sig.start, pe_base);
