@@ -282,9 +282,9 @@ def tuning_summary(tuning):
     bra-row FP32 kernel or the one-quartet-per-thread one, and the median
     timings (ms) of both where they were timed."""
     import numpy as np
-    names = ["ss", "ps", "pp", "ds", "dp", "dd"]
+    names = ["ss", "ps", "pp", "ds", "dp", "dd", "fs", "fp", "fd", "ff"]
     out = {}
-    for b in range(6):
+    for b in range(len(names)):
         for k in range(b + 1):
             ch = [int(t[0][b, k]) for t in tuning if t[0][b, k] >= 0]
             if not ch:

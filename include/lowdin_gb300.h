@@ -180,11 +180,12 @@ int LowdinGB300_coupling_device(LibintInterface *a, LibintInterface *b, const do
 long long LowdinGB300_last_quartets(LibintInterface *lint);
 
 /* Shell quartets per (bra pair class, ket pair class) of the last two-particle
-   build, 36 entries (pair classes ss, ps, pp, ds, dp, dd); returns 36 or -1. */
+   build, 100 entries (pair classes ss, ps, pp, ds, dp, dd, fs, fp, fd, ff;
+   class (la >= lb) at la (la + 1) / 2 + lb); returns 100 or -1. */
 int LowdinGB300_last_class_quartets(LibintInterface *lint, long long *out);
 
-/* Number of shell pairs per pair class (6 entries): significant pairs when
-   all_pairs = 0, every unordered pair when 1.  Returns 6 or -1. */
+/* Number of shell pairs per pair class (10 entries): significant pairs when
+   all_pairs = 0, every unordered pair when 1.  Returns 10 or -1. */
 int LowdinGB300_pair_class_counts(LibintInterface *lint, int all_pairs, int *out);
 
 /* Measured FMA throughput of the current GPU in TFLOP/s (fp64 = 1: FP64,
@@ -239,7 +240,7 @@ int LowdinGB300_batch_set_skip(LowdinGB300_Batch *b, double skip);
    for the following batch_fock calls (split: the mixed build's split).
    Choices are cached in the process by (class, size bucket); force = 1
    re-times.  Both kernels take the same quartets.  Synchronises `stream`.
-   batch_tuning reports the 36 per-class choices (-1 not tuned, 0 one quartet
+   batch_tuning reports the 100 per-class choices (-1 not tuned, 0 one quartet
    per thread, 1 bra rows) and the two timings (ms, -1 where not timed). */
 int LowdinGB300_batch_autotune(LowdinGB300_Batch *b, double split, int force, void *stream);
 int LowdinGB300_batch_tuning(LowdinGB300_Batch *b, int *choice, float *ms_rows, float *ms_tiles);
@@ -247,7 +248,7 @@ int LowdinGB300_batch_tuning(LowdinGB300_Batch *b, int *choice, float *ms_rows, 
    precision mode after a first eager build; default on); 0 launches eagerly. */
 int LowdinGB300_batch_use_graph(LowdinGB300_Batch *b, int on);
 /* quartets evaluated per (bra pair class, ket pair class) by the last J/K
-   build and by the last coupling build of the batch (36 entries each;
+   build and by the last coupling build of the batch (100 entries each;
    synchronise `stream`) */
 int LowdinGB300_batch_quartets(LowdinGB300_Batch *b, long long *out, void *stream);
 int LowdinGB300_batch_coupling_quartets(LowdinGB300_Batch *b, long long *out, void *stream);

@@ -9,8 +9,13 @@
 
 namespace lgb {
 
+// the pair classes of s, p and d shells with total angular momentum up to
+// kTemplatedMaxL; classes with an f shell run on the cooperative kernels
+constexpr int kTemplatedPairClasses = 6;
 template <int B, int K>
-constexpr bool templated_class() { return pc_L(B) + pc_L(K) <= kTemplatedMaxL; }
+constexpr bool templated_class() {
+  return B < kTemplatedPairClasses && K < kTemplatedPairClasses && pc_L(B) + pc_L(K) <= kTemplatedMaxL;
+}
 
 template <typename R, int B, int K>
 constexpr JKFn jk_entry() {
@@ -39,27 +44,29 @@ constexpr MXFn mx_entry() {
   else return nullptr;
 }
 
-#define LGB_ROW6(F, ...) \
-  { F<__VA_ARGS__, 0>(), F<__VA_ARGS__, 1>(), F<__VA_ARGS__, 2>(), F<__VA_ARGS__, 3>(), F<__VA_ARGS__, 4>(), F<__VA_ARGS__, 5>() }
+static_assert(kNumPairClasses == 10, "launch-table rows list every pair class");
+#define LGB_ROW(F, ...)                                                                                   \
+  { F<__VA_ARGS__, 0>(), F<__VA_ARGS__, 1>(), F<__VA_ARGS__, 2>(), F<__VA_ARGS__, 3>(), F<__VA_ARGS__, 4>(), \
+    F<__VA_ARGS__, 5>(), F<__VA_ARGS__, 6>(), F<__VA_ARGS__, 7>(), F<__VA_ARGS__, 8>(), F<__VA_ARGS__, 9>() }
 
 #define LGB_JK_TABLES(B)                                   \
-  extern const JKFn kJK64_##B[6];                          \
-  extern const JKFn kJK32_##B[6];                          \
-  extern const JKFn kJKR_##B[6];                           \
-  const JKFn kJK64_##B[6] = LGB_ROW6(jk_entry, double, B); \
-  const JKFn kJK32_##B[6] = LGB_ROW6(jk_entry, float, B);  \
-  const JKFn kJKR_##B[6] = LGB_ROW6(jkr_entry, B);
+  extern const JKFn kJK64_##B[kNumPairClasses];                          \
+  extern const JKFn kJK32_##B[kNumPairClasses];                          \
+  extern const JKFn kJKR_##B[kNumPairClasses];                           \
+  const JKFn kJK64_##B[kNumPairClasses] = LGB_ROW(jk_entry, double, B); \
+  const JKFn kJK32_##B[kNumPairClasses] = LGB_ROW(jk_entry, float, B);  \
+  const JKFn kJKR_##B[kNumPairClasses] = LGB_ROW(jkr_entry, B);
 
 #define LGB_CP_TABLES(B)                                   \
-  extern const CPFn kCP64_##B[6];                          \
-  extern const CPFn kCP32_##B[6];                          \
-  const CPFn kCP64_##B[6] = LGB_ROW6(cp_entry, double, B); \
-  const CPFn kCP32_##B[6] = LGB_ROW6(cp_entry, float, B);
+  extern const CPFn kCP64_##B[kNumPairClasses];                          \
+  extern const CPFn kCP32_##B[kNumPairClasses];                          \
+  const CPFn kCP64_##B[kNumPairClasses] = LGB_ROW(cp_entry, double, B); \
+  const CPFn kCP32_##B[kNumPairClasses] = LGB_ROW(cp_entry, float, B);
 
 #define LGB_IT_TABLE(B)                      \
-  extern const ITFn kIT_##B[6];              \
-  extern const MXFn kMX_##B[6];              \
-  const ITFn kIT_##B[6] = LGB_ROW6(it_entry, B); \
-  const MXFn kMX_##B[6] = LGB_ROW6(mx_entry, B);
+  extern const ITFn kIT_##B[kNumPairClasses];              \
+  extern const MXFn kMX_##B[kNumPairClasses];              \
+  const ITFn kIT_##B[kNumPairClasses] = LGB_ROW(it_entry, B); \
+  const MXFn kMX_##B[kNumPairClasses] = LGB_ROW(mx_entry, B);
 
 }  // namespace lgb

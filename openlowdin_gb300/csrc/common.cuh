@@ -7,7 +7,7 @@
 
 namespace lgb {
 
-constexpr int kMaxL = 2;               // per-shell angular momentum handled by the kernels (d)
+constexpr int kMaxL = 3;               // per-shell angular momentum handled by the kernels (f)
 constexpr int kMaxLQuartet = 4 * kMaxL;
 
 // ---- Cartesian components -------------------------------------------------

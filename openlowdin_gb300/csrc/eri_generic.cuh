@@ -11,13 +11,15 @@ namespace lgb {
 
 constexpr int kGenMaxL = 4 * kMaxL;   // largest total angular momentum of a quartet
 
-// Cartesian index table (cumulative index c through total 5): total,
-// exponents, recursion axis, c - 1_d and c + 1_d.  The cooperative kernels
-// copy it to shared memory; the runtime forms of clevel / cx / cminus ... loop.
+// Cartesian index table (cumulative index c through total 2 kMaxL, the largest
+// pair total): total, exponents, recursion axis, c - 1_d and c + 1_d (below
+// the top total).  The cooperative kernels copy it to shared memory; the
+// runtime forms of clevel / cx / cminus ... loop.
 struct CartInfo {
   unsigned char lev, xyz[3], dir, m[3], p[3], pad;
 };
-constexpr int kCartN = 56;
+constexpr int kCartTop = 2 * kMaxL;          // largest total of the table
+constexpr int kCartN = coff(kCartTop + 1);
 struct CartTable {
   CartInfo e[kCartN];
 };
@@ -32,7 +34,7 @@ __host__ __device__ constexpr CartTable make_cart_table() {
     q.dir = (unsigned char)cdir(c);
     for (int d = 0; d < 3; ++d) {
       q.m[d] = (unsigned char)(ccomp(c, d) > 0 ? cminus(c, d) : 0);
-      q.p[d] = (unsigned char)(clevel(c) < 5 ? cplus(c, d) : 0);
+      q.p[d] = (unsigned char)(clevel(c) < kCartTop ? cplus(c, d) : 0);
     }
     q.pad = 0;
   }
@@ -46,16 +48,17 @@ __device__ __forceinline__ const CartInfo *cart_shared(CartInfo *dst) {
   __syncthreads();
   return dst;
 }
-// Shared work arrays of one quartet evaluation, sized for its class (offsets
-// in doubles): bra nodes Vb[e][m], ket nodes Vk (blocks [f][e][m]), the
-// contracted X[e][f], the first horizontal-transfer level H, Y after the bra
-// transfer, the integrals, scalars of the primitive quartet, ket block
-// offsets (ints).
+// Work arrays of one quartet evaluation, sized for its class (offsets in
+// doubles): bra nodes Vb[e][m], ket nodes Vk (blocks [f][e][m]), the
+// contracted X[e][f], two buffers H0 / H1 for the intermediate
+// horizontal-transfer levels (level j writes H[(j - 1) & 1], reads
+// H[j & 1] of level j - 1), Y after the bra transfer, the integrals, scalars
+// of the primitive quartet, ket block offsets (ints).
 struct CoLayout {
-  int vb, vk, x, h, y, out, misc, kb, total;
+  int vb, vk, x, h0, h1, y, out, misc, kb, total;
 };
 constexpr int kCoMiscN = 32;
-constexpr int kCoKbN = 20;   // doubles holding 40 ints
+constexpr int kCoKbN = (kCartN + 2) / 2;   // doubles holding kCartN + 1 ints
 
 __host__ __device__ inline CoLayout co_layout(int la, int lb, int lc, int ld) {
   const int L1 = la + lb, L2 = lc + ld, L = L1 + L2;
@@ -63,14 +66,23 @@ __host__ __device__ inline CoLayout co_layout(int la, int lb, int lc, int ld) {
   const int NA = ncart(la), NB = ncart(lb), NC = ncart(lc), ND = ncart(ld);
   int nvk = 0;
   for (int f = 1; f < NF; ++f) nvk += NE * (L2 - clevel(f) + 1);
-  const int hb = lb == 2 ? (coff(la + 2) - coff(la)) * 3 * nF : 0;          // bra level 1 of 2
-  const int hk = ld == 2 ? NA * NB * (coff(lc + 2) - coff(lc)) * 3 : 0;     // ket level 1 of 2
+  // intermediate transfer levels j < lb (bra) and j < ld (ket)
+  int hmax = 0;
+  for (int j = 1; j < lb; ++j) {
+    const int s = (coff(la + lb - j + 1) - coff(la)) * ncart(j) * nF;
+    hmax = s > hmax ? s : hmax;
+  }
+  for (int j = 1; j < ld; ++j) {
+    const int s = NA * NB * (coff(lc + ld - j + 1) - coff(lc)) * ncart(j);
+    hmax = s > hmax ? s : hmax;
+  }
   CoLayout o;
   o.vb = 0;
   o.vk = o.vb + NE * (L + 1);
   o.x = o.vk + nvk;
-  o.h = o.x + nE * nF;
-  o.y = o.h + (hb > hk ? hb : hk);
+  o.h0 = o.x + nE * nF;
+  o.h1 = o.h0 + hmax;
+  o.y = o.h1 + hmax;
   o.out = o.y + NA * NB * nF;
   o.misc = o.out + NA * NB * NC * ND;
   o.kb = o.misc + kCoMiscN;
@@ -140,7 +152,8 @@ __device__ inline void eri_coop(G g, const CartInfo *__restrict__ ct, const CoLa
   const int L1 = la + lb, L2 = lc + ld, L = L1 + L2, M = L + 1;
   const int NE = coff(L1 + 1), NF = coff(L2 + 1), E0 = coff(la), F0 = coff(lc);
   const int nE = NE - E0, nF = NF - F0;
-  double *Vb = sm + Lo.vb, *Vk = sm + Lo.vk, *X = sm + Lo.x, *H = sm + Lo.h, *Y = sm + Lo.y, *out = sm + Lo.out;
+  double *Vb = sm + Lo.vb, *Vk = sm + Lo.vk, *X = sm + Lo.x, *Y = sm + Lo.y, *out = sm + Lo.out;
+  double *Hb[2] = {sm + Lo.h0, sm + Lo.h1};
   double *misc = sm + Lo.misc;
   int *kb = reinterpret_cast<int *>(sm + Lo.kb);
   g.sync();   // the previous quartet's readers of the work arrays are done
@@ -242,10 +255,9 @@ __device__ inline void eri_coop(G g, const CartInfo *__restrict__ ct, const CoLa
   } else {
     for (int j = 1; j <= lb; ++j) {
       const int na = (j == lb) ? NA : coff(la + lb - j + 1) - E0, nb = ncart(j), pnb = j == 1 ? 1 : ncart(j - 1);
-      const double *src = j == 1 ? X : H;
-      double *dst = j == lb ? Y : H;
-      // level j reads level j-1 (X or H) and writes H or Y: lb <= 2, so
-      // source and destination never coincide
+      // level j reads level j - 1 (X, or the other H buffer) and writes H or Y
+      const double *src = j == 1 ? X : Hb[j & 1];
+      double *dst = j == lb ? Y : Hb[(j - 1) & 1];
       for (int idx = tid; idx < na * nb * nF; idx += nt) {
         const int ar = idx / (nb * nF), rem = idx % (nb * nF), bi = rem / nF, k = rem % nF;
         const int b = coff(j) + bi, d = ct[b].dir, bm = ct[b].m[d] - coff(j - 1);
@@ -272,14 +284,15 @@ __device__ inline void eri_coop(G g, const CartInfo *__restrict__ ct, const CoLa
           v1 = Y[r * nF + cpr];
           v0 = Y[r * nF + cr];
         } else {
-          // level j - 1 = 1 lives in H as [r][c][d1] with c over totals lc..lc+ld-1
+          // level j - 1 lives in Hb[j & 1] as [r][c][d'] with c over totals lc..lc+ld-j+1
+          const double *Hp = Hb[j & 1];
           const int pnc = coff(lc + ld - (j - 1) + 1) - F0;
-          v1 = H[(r * pnc + cpr) * pnd + dm];
-          v0 = H[(r * pnc + cr) * pnd + dm];
+          v1 = Hp[(r * pnc + cpr) * pnd + dm];
+          v0 = Hp[(r * pnc + cr) * pnd + dm];
         }
         const double v = v1 + ket.AB[d] * v0;
         if (j == ld) out[(r * NC + cr) * ND + di] = v;
-        else H[(r * nc + cr) * nd + di] = v;
+        else Hb[(j - 1) & 1][(r * nc + cr) * nd + di] = v;
       }
       g.sync();
     }

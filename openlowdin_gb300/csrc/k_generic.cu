@@ -19,23 +19,31 @@
 
 namespace lgb {
 
-extern const JKFn kJK64_0[6], kJK64_1[6], kJK64_2[6], kJK64_3[6], kJK64_4[6], kJK64_5[6];
-extern const JKFn kJK32_0[6], kJK32_1[6], kJK32_2[6], kJK32_3[6], kJK32_4[6], kJK32_5[6];
-extern const JKFn kJKR_0[6], kJKR_1[6], kJKR_2[6], kJKR_3[6], kJKR_4[6], kJKR_5[6];
-extern const CPFn kCP64_0[6], kCP64_1[6], kCP64_2[6], kCP64_3[6], kCP64_4[6], kCP64_5[6];
-extern const CPFn kCP32_0[6], kCP32_1[6], kCP32_2[6], kCP32_3[6], kCP32_4[6], kCP32_5[6];
-extern const ITFn kIT_0[6], kIT_1[6], kIT_2[6], kIT_3[6], kIT_4[6], kIT_5[6];
-extern const MXFn kMX_0[6], kMX_1[6], kMX_2[6], kMX_3[6], kMX_4[6], kMX_5[6];
+constexpr int NPC = kNumPairClasses;
+extern const JKFn kJK64_0[NPC], kJK64_1[NPC], kJK64_2[NPC], kJK64_3[NPC], kJK64_4[NPC], kJK64_5[NPC];
+extern const JKFn kJK32_0[NPC], kJK32_1[NPC], kJK32_2[NPC], kJK32_3[NPC], kJK32_4[NPC], kJK32_5[NPC];
+extern const JKFn kJKR_0[NPC], kJKR_1[NPC], kJKR_2[NPC], kJKR_3[NPC], kJKR_4[NPC], kJKR_5[NPC];
+extern const CPFn kCP64_0[NPC], kCP64_1[NPC], kCP64_2[NPC], kCP64_3[NPC], kCP64_4[NPC], kCP64_5[NPC];
+extern const CPFn kCP32_0[NPC], kCP32_1[NPC], kCP32_2[NPC], kCP32_3[NPC], kCP32_4[NPC], kCP32_5[NPC];
+extern const ITFn kIT_0[NPC], kIT_1[NPC], kIT_2[NPC], kIT_3[NPC], kIT_4[NPC], kIT_5[NPC];
+extern const MXFn kMX_0[NPC], kMX_1[NPC], kMX_2[NPC], kMX_3[NPC], kMX_4[NPC], kMX_5[NPC];
 
 namespace {
 
-const JKFn *const kJK64[6] = {kJK64_0, kJK64_1, kJK64_2, kJK64_3, kJK64_4, kJK64_5};
-const JKFn *const kJK32[6] = {kJK32_0, kJK32_1, kJK32_2, kJK32_3, kJK32_4, kJK32_5};
-const JKFn *const kJKR[6] = {kJKR_0, kJKR_1, kJKR_2, kJKR_3, kJKR_4, kJKR_5};
-const CPFn *const kCP64[6] = {kCP64_0, kCP64_1, kCP64_2, kCP64_3, kCP64_4, kCP64_5};
-const CPFn *const kCP32[6] = {kCP32_0, kCP32_1, kCP32_2, kCP32_3, kCP32_4, kCP32_5};
-const ITFn *const kIT[6] = {kIT_0, kIT_1, kIT_2, kIT_3, kIT_4, kIT_5};
-const MXFn *const kMX[6] = {kMX_0, kMX_1, kMX_2, kMX_3, kMX_4, kMX_5};
+// bra pair classes with an f shell have no templated kernels: every entry null
+const JKFn kJKnone[NPC] = {};
+const CPFn kCPnone[NPC] = {};
+const ITFn kITnone[NPC] = {};
+const MXFn kMXnone[NPC] = {};
+#define LGB_F_ROWS(X) X, X, X, X
+const JKFn *const kJK64[NPC] = {kJK64_0, kJK64_1, kJK64_2, kJK64_3, kJK64_4, kJK64_5, LGB_F_ROWS(kJKnone)};
+const JKFn *const kJK32[NPC] = {kJK32_0, kJK32_1, kJK32_2, kJK32_3, kJK32_4, kJK32_5, LGB_F_ROWS(kJKnone)};
+const JKFn *const kJKR[NPC] = {kJKR_0, kJKR_1, kJKR_2, kJKR_3, kJKR_4, kJKR_5, LGB_F_ROWS(kJKnone)};
+const CPFn *const kCP64[NPC] = {kCP64_0, kCP64_1, kCP64_2, kCP64_3, kCP64_4, kCP64_5, LGB_F_ROWS(kCPnone)};
+const CPFn *const kCP32[NPC] = {kCP32_0, kCP32_1, kCP32_2, kCP32_3, kCP32_4, kCP32_5, LGB_F_ROWS(kCPnone)};
+const ITFn *const kIT[NPC] = {kIT_0, kIT_1, kIT_2, kIT_3, kIT_4, kIT_5, LGB_F_ROWS(kITnone)};
+const MXFn *const kMX[NPC] = {kMX_0, kMX_1, kMX_2, kMX_3, kMX_4, kMX_5, LGB_F_ROWS(kMXnone)};
+#undef LGB_F_ROWS
 
 const dim3 kBlock(32, kWarpsPerBlock);
 // LOWDIN_GB300_ROWS=0 keeps the FP32 half of mixed builds on jk_tasks_kernel
@@ -63,7 +71,10 @@ __device__ __forceinline__ const Task &coop_unit(const Task *tasks, int ntasks, 
   return T;
 }
 
-// every warp of a cooperative CTA is an independent worker with its own work arrays
+// every warp of a cooperative CTA is an independent worker with its own work
+// arrays: in shared memory, or, for classes whose arrays exceed a CTA's shared
+// memory (a pair of f shells against f or d), in the launch's global scratch
+// `gscr` (one slice per warp of the grid, cached by L2)
 #define LGB_COOP_PROLOGUE(K)                                              \
   extern __shared__ double smem[];                                        \
   __shared__ CartInfo cart_sm[kCartN];                                    \
@@ -71,13 +82,14 @@ __device__ __forceinline__ const Task &coop_unit(const Task *tasks, int ntasks, 
   const CoLayout Lo = co_layout(K.la, K.lb, K.lc, K.ld);                  \
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;             \
   const int nwarps = blockDim.x >> 5;                                     \
-  double *sm = smem + (size_t)warp * Lo.total;                            \
+  double *sm = gscr ? gscr + ((size_t)blockIdx.x * nwarps + warp) * Lo.total \
+                    : smem + (size_t)warp * Lo.total;                     \
   const double *I = sm + Lo.out;                                          \
   const WarpGroup g;                                                      \
   const long long w0 = (long long)blockIdx.x * nwarps + warp, wstep = (long long)gridDim.x * nwarps;
 
 // ------------------------------------------------------------------ J/K --
-__global__ void __launch_bounds__(128) jk_coop_kernel(const JKTask *__restrict__ tasks, TaskLaunch TL, GenClass K) {
+__global__ void __launch_bounds__(128) jk_coop_kernel(const JKTask *__restrict__ tasks, TaskLaunch TL, GenClass K, double *gscr) {
   LGB_COOP_PROLOGUE(K)
   const int NA = ncart(K.la), NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld);
   for (long long u = w0; u < (long long)TL.nblocks * kCoUnitsPerTile; u += wstep) {
@@ -166,7 +178,7 @@ __global__ void __launch_bounds__(128) jk_coop_kernel(const JKTask *__restrict__
 }
 
 // ------------------------------------------------------------- coupling --
-__global__ void __launch_bounds__(128) cp_coop_kernel(const CPTask *__restrict__ tasks, TaskLaunch TL, GenClass K) {
+__global__ void __launch_bounds__(128) cp_coop_kernel(const CPTask *__restrict__ tasks, TaskLaunch TL, GenClass K, double *gscr) {
   LGB_COOP_PROLOGUE(K)
   const int NA = ncart(K.la), NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld);
   for (long long u = w0; u < (long long)TL.nblocks * kCoUnitsPerTile; u += wstep) {
@@ -225,7 +237,7 @@ __global__ void __launch_bounds__(128) cp_coop_kernel(const CPTask *__restrict__
 // ---------------------------------------------------------- geminal (G12) --
 // Every class runs here (the geminal matrices are not a hot path): one quartet
 // per warp, all quartets of the launch's bra x ket pair ranges, no screening.
-__global__ void __launch_bounds__(128) g12_coop_kernel(G12Params P, GenClass K) {
+__global__ void __launch_bounds__(128) g12_coop_kernel(G12Params P, GenClass K, double *gscr) {
   LGB_COOP_PROLOGUE(K)
   const int NA = ncart(K.la), NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld);
   const long long nq = (long long)P.nbra * P.nket;
@@ -330,7 +342,7 @@ __device__ __forceinline__ void it_map(int r, int mu, int nu, int l, int s, int 
   }
 }
 
-__global__ void __launch_bounds__(128) it_coop_kernel(ITParams P, GenClass K) {
+__global__ void __launch_bounds__(128) it_coop_kernel(ITParams P, GenClass K, double *gscr) {
   LGB_COOP_PROLOGUE(K)
   const int NA = ncart(K.la), NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld);
   const long long nq = (long long)P.nbra * P.nket;
@@ -378,7 +390,7 @@ __global__ void __launch_bounds__(128) it_coop_kernel(ITParams P, GenClass K) {
 }
 
 // ------------------------------------------------------ MP2 transform input --
-__global__ void __launch_bounds__(128) mp2x_coop_kernel(MXParams P, GenClass K) {
+__global__ void __launch_bounds__(128) mp2x_coop_kernel(MXParams P, GenClass K, double *gscr) {
   LGB_COOP_PROLOGUE(K)
   const int NB = ncart(K.lb), NC = ncart(K.lc), ND = ncart(K.ld), NA = ncart(K.la);
   const long long nq = (long long)P.nbra * P.nket;
@@ -417,7 +429,7 @@ __global__ void __launch_bounds__(128) mp2x_coop_kernel(MXParams P, GenClass K) 
 }
 
 // ----------------------------------------------------------------- Schwarz --
-__global__ void __launch_bounds__(128) schwarz_coop_kernel(SchwarzParams P, GenClass K) {
+__global__ void __launch_bounds__(128) schwarz_coop_kernel(SchwarzParams P, GenClass K, double *gscr) {
   LGB_COOP_PROLOGUE(K)
   const int N = ncart(K.la) * ncart(K.lb);
   for (long long t = w0; t < P.np; t += wstep) {
@@ -456,17 +468,42 @@ bool coop_ready() {
 }
 
 // launch shape of a cooperative kernel for class K: warps per CTA (each with
-// its class-sized work arrays), dynamic shared memory, grid over `units`
+// its class-sized work arrays), dynamic shared memory, grid over `units`; a
+// class whose arrays exceed kCoMaxSmem runs one warp per CTA on global
+// scratch (`scratch` doubles, allocated on the stream for the launch)
 struct CoopShape {
   dim3 grid, block;
   size_t smem;
+  size_t scratch;
 };
 CoopShape coop_shape(const GenClass &K, long long units) {
   const size_t per = (size_t)co_layout(K.la, K.lb, K.lc, K.ld).total * sizeof(double);
+  if (per > (size_t)kCoMaxSmem) {
+    const long long ctas = std::max<long long>(1, std::min<long long>(units, 152LL * 4));
+    return CoopShape{dim3((unsigned)ctas), dim3(32u), 0, (size_t)ctas * per / sizeof(double)};
+  }
   int w = (int)std::min<size_t>(4, kCoMaxSmem / per);
   if (w < 1) w = 1;
   const long long ctas = std::max<long long>(1, std::min<long long>((units + w - 1) / w, 152LL * 16));
-  return CoopShape{dim3((unsigned)ctas), dim3((unsigned)(32 * w)), per * w};
+  return CoopShape{dim3((unsigned)ctas), dim3((unsigned)(32 * w)), per * w, 0};
+}
+
+// launches kernel `f` with shape c on stream s, with its global scratch when
+// the shape asks for one (stream-ordered allocation, freed after the launch)
+template <typename F, typename... Args>
+cudaError_t coop_launch(F f, const CoopShape &c, cudaStream_t s, Args... args) {
+  double *scr = nullptr;
+  if (c.scratch) {
+    const cudaError_t e = cudaMallocAsync((void **)&scr, c.scratch * sizeof(double), s);
+    if (e != cudaSuccess) return e;
+  }
+  f<<<c.grid, c.block, c.smem, s>>>(args..., scr);
+  cudaError_t e = cudaGetLastError();
+  if (scr) {
+    const cudaError_t e2 = cudaFreeAsync(scr, s);
+    if (e == cudaSuccess) e = e2;
+  }
+  return e;
 }
 
 }  // namespace
@@ -507,7 +544,8 @@ cudaError_t launch_jk_tasks(int pcb, int pck, bool fp32, const JKTask *dtasks, c
     if (!coop_ready()) return cudaErrorInvalidValue;
     const GenClass K = gen_class(pcb, pck);
     const CoopShape c = coop_shape(K, (long long)tl.nblocks * kCoUnitsPerTile);
-    jk_coop_kernel<<<c.grid, c.block, c.smem, s>>>(dtasks, tl, K);
+    const cudaError_t e = coop_launch(jk_coop_kernel, c, s, dtasks, tl, K);
+    if (e != cudaSuccess) return e;
   }
   count_launches(1);
   return cudaGetLastError();
@@ -524,7 +562,8 @@ cudaError_t launch_cp_tasks(int pcb, int pck, bool fp32, const CPTask *dtasks, c
     if (!coop_ready()) return cudaErrorInvalidValue;
     const GenClass K = gen_class(pcb, pck);
     const CoopShape c = coop_shape(K, (long long)tl.nblocks * kCoUnitsPerTile);
-    cp_coop_kernel<<<c.grid, c.block, c.smem, s>>>(dtasks, tl, K);
+    const cudaError_t e = coop_launch(cp_coop_kernel, c, s, dtasks, tl, K);
+    if (e != cudaSuccess) return e;
   }
   count_launches(1);
   return cudaGetLastError();
@@ -541,7 +580,8 @@ cudaError_t launch_it(int pcb, int pck, const ITParams &p, cudaStream_t s) {
     if (!coop_ready()) return cudaErrorInvalidValue;
     const GenClass K = gen_class(pcb, pck);
     const CoopShape c = coop_shape(K, (long long)p.nbra * p.nket);
-    it_coop_kernel<<<c.grid, c.block, c.smem, s>>>(p, K);
+    const cudaError_t e = coop_launch(it_coop_kernel, c, s, p, K);
+    if (e != cudaSuccess) return e;
   }
   count_launches(1);
   return cudaGetLastError();
@@ -558,7 +598,8 @@ cudaError_t launch_mp2x(int pcb, int pck, const MXParams &p, cudaStream_t s) {
     if (!coop_ready()) return cudaErrorInvalidValue;
     const GenClass K = gen_class(pcb, pck);
     const CoopShape c = coop_shape(K, (long long)p.nbra * p.nket);
-    mp2x_coop_kernel<<<c.grid, c.block, c.smem, s>>>(p, K);
+    const cudaError_t e = coop_launch(mp2x_coop_kernel, c, s, p, K);
+    if (e != cudaSuccess) return e;
   }
   count_launches(1);
   return cudaGetLastError();
@@ -570,7 +611,8 @@ cudaError_t launch_g12(int pcb, int pck, const G12Params &p, cudaStream_t s) {
   if (!coop_ready()) return cudaErrorInvalidValue;
   const GenClass K = gen_class(pcb, pck);
   const CoopShape c = coop_shape(K, (long long)p.nbra * p.nket);
-  g12_coop_kernel<<<c.grid, c.block, c.smem, s>>>(p, K);
+  const cudaError_t e = coop_launch(g12_coop_kernel, c, s, p, K);
+  if (e != cudaSuccess) return e;
   count_launches(1);
   return cudaGetLastError();
 }
@@ -584,7 +626,8 @@ cudaError_t launch_schwarz(int pc, const SchwarzParams &p, cudaStream_t s) {
     if (!coop_ready()) return cudaErrorInvalidValue;
     const GenClass K{pc_la(pc), pc_lb(pc), pc_la(pc), pc_lb(pc)};
     const CoopShape c = coop_shape(K, p.np);
-    schwarz_coop_kernel<<<c.grid, c.block, c.smem, s>>>(p, K);
+    const cudaError_t e = coop_launch(schwarz_coop_kernel, c, s, p, K);
+    if (e != cudaSuccess) return e;
   }
   count_launches(1);
   return cudaGetLastError();

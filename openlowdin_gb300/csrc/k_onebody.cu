@@ -44,7 +44,8 @@ __global__ void __launch_bounds__(128) one_body_kernel(OneBodyParams P) {
   const DevShell A = P.shells[s1], B = P.shells[s2];
   const CartInfo *ct = kCartTable.e;
   const int la = A.l, lb = B.l, n1 = ncart(la), n2 = ncart(lb);
-  double S[36], T[36], V[36];
+  constexpr int kNC2 = ncart(kMaxL) * ncart(kMaxL);
+  double S[kNC2], T[kNC2], V[kNC2];
   for (int k = 0; k < n1 * n2; ++k) S[k] = T[k] = V[k] = 0.0;
   double AB[3], AB2 = 0;
   for (int d = 0; d < 3; ++d) {
@@ -53,7 +54,7 @@ __global__ void __launch_bounds__(128) one_body_kernel(OneBodyParams P) {
   }
   // potential: vertical recursion on the bra up to la + lb, then transfer
   const int L = la + lb, NE = coff(L + 1), E0 = coff(la), M = L + 1;
-  double W[35 * 5], X[35];
+  double W[coff(2 * kMaxL + 1) * (2 * kMaxL + 1)], X[coff(2 * kMaxL + 1)];
   for (int e = 0; e < NE - E0; ++e) X[e] = 0.0;
   for (int pa = 0; pa < A.nprim; ++pa)
     for (int pb = 0; pb < B.nprim; ++pb) {
@@ -114,28 +115,23 @@ __global__ void __launch_bounds__(128) one_body_kernel(OneBodyParams P) {
       }
     }
   if (P.V) {
-    // horizontal transfer (a, b+1_i| = (a+1_i, b| + AB_i (a, b|, lb <= 2 levels
-    double H1[20 * 3];
+    // horizontal transfer (a, b+1_i| = (a+1_i, b| + AB_i (a, b| over lb
+    // levels: level j has rows over totals la .. la + lb - j (the last level
+    // only la) and ncart(j) columns; it reads level j - 1 (X for j = 1)
+    constexpr int kHRows = coff(2 * kMaxL), kHCols = ncart(kMaxL);
+    double Hb[2][kHRows * kHCols];
     if (lb == 0) {
       for (int f1 = 0; f1 < n1; ++f1) V[f1] = X[f1];
     } else {
-      const int na1 = coff(la + lb) - E0;   // level 1 rows: totals la .. la + lb - 1
-      for (int bi = 0; bi < 3; ++bi) {
-        const int bc = 1 + bi, d = ct[bc].dir;
-        for (int ar = 0; ar < na1; ++ar) {
-          const int apr = ct[E0 + ar].p[d] - E0;
-          H1[ar * 3 + bi] = X[apr] + AB[d] * X[ar];
-        }
-      }
-      if (lb == 1) {
-        for (int f1 = 0; f1 < n1; ++f1)
-          for (int bi = 0; bi < 3; ++bi) V[f1 * 3 + bi] = H1[f1 * 3 + bi];
-      } else {
-        for (int bi = 0; bi < 6; ++bi) {
-          const int bc = 4 + bi, d = ct[bc].dir, bm = ct[bc].m[d] - 1;
-          for (int ar = 0; ar < n1; ++ar) {
+      for (int j = 1; j <= lb; ++j) {
+        const int na = j == lb ? n1 : coff(la + lb - j + 1) - E0, nb = ncart(j), pnb = j == 1 ? 1 : ncart(j - 1);
+        const double *src = j == 1 ? X : Hb[j & 1];
+        double *dst = j == lb ? V : Hb[(j - 1) & 1];
+        for (int bi = 0; bi < nb; ++bi) {
+          const int bc = coff(j) + bi, d = ct[bc].dir, bm = ct[bc].m[d] - coff(j - 1);
+          for (int ar = 0; ar < na; ++ar) {
             const int apr = ct[E0 + ar].p[d] - E0;
-            V[ar * 6 + bi] = H1[apr * 3 + bm] + AB[d] * H1[ar * 3 + bm];
+            dst[ar * nb + bi] = src[apr * pnb + bm] + AB[d] * src[ar * pnb + bm];
           }
         }
       }

@@ -51,7 +51,7 @@ class PerDeviceLevel {
 // pair class id of a canonical pair (la >= lb): (0,0)=0 (1,0)=1 (1,1)=2 (2,0)=3 (2,1)=4 (2,2)=5
 __host__ __device__ constexpr int pair_class(int la, int lb) { return la * (la + 1) / 2 + lb; }
 constexpr int kNumPairClasses = (kMaxL + 1) * (kMaxL + 2) / 2;
-__host__ __device__ constexpr int pc_la(int pc) { return pc >= 3 ? 2 : (pc >= 1 ? 1 : 0); }
+__host__ __device__ constexpr int pc_la(int pc) { return pc >= 6 ? 3 : (pc >= 3 ? 2 : (pc >= 1 ? 1 : 0)); }
 __host__ __device__ constexpr int pc_lb(int pc) { return pc - pc_la(pc) * (pc_la(pc) + 1) / 2; }
 
 constexpr int kWarpsPerBlock = 4;  // bra pairs per block (one per warp); 32 kets per warp

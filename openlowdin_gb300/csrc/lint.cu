@@ -885,7 +885,7 @@ double LowdinGB300_measure_fma_tflops(int fp64) {
   return t;
 }
 
-const char *LowdinGB300_version(void) { return "lowdin_gb300 0.1 (sm_103a, FP64/FP32 Obara-Saika, s p d shells)"; }
+const char *LowdinGB300_version(void) { return "lowdin_gb300 0.1 (sm_103a, FP64/FP32 Obara-Saika, s p d f shells)"; }
 
 }  // extern "C"
 
@@ -963,6 +963,16 @@ int LowdinGB300_twobody_device_noalloc(LibintInterface *lint, const double *dD, 
               __func__, n, nsh, kNoAllocMaxBasis, kNoAllocMaxShells);
     return -1;
   }
+  for (const auto &sh : lint->shells)
+    if (sh.l > 2) {
+      // quartet classes of two f shells against f or d need work arrays in
+      // global memory beyond a CTA's shared memory, which only the allocating
+      // entry point provides
+      set_error("%s: shells above d (l=%d) are not supported by the allocation-free build; use "
+                "LowdinGB300_twobody_device",
+                __func__, sh.l);
+      return -1;
+    }
   unsigned char *base = nullptr;
   if (!noalloc_scratch(&base)) return -1;
   cudaStream_t s = (cudaStream_t)stream;

@@ -92,7 +92,7 @@ def quartet_flops(la, lb, lc, ld, kind="jk", nprim_quartets=1) -> int:
     return nprim_quartets * vrr_flops(la, lb, lc, ld) + hrr_flops(la, lb, lc, ld) + digest_flops(la, lb, lc, ld, kind)
 
 
-PAIR_CLASSES = [(0, 0), (1, 0), (1, 1), (2, 0), (2, 1), (2, 2)]
+PAIR_CLASSES = [(la, lb) for la in range(4) for lb in range(la + 1)]   # the library's ten pair classes
 
 
 def class_table_flops(counts, kind="jk") -> float:

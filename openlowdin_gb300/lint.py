@@ -27,6 +27,12 @@ _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _vp = ctypes.c_void_p
 
 
+# shell-pair classes of the library (s, p, d, f shells: ss ps pp ds dp dd fs fp fd ff),
+# the index of class (la >= lb) being la (la + 1) / 2 + lb
+NPC = 10
+PAIR_CLASSES = [(la, lb) for la in range(4) for lb in range(la + 1)]
+
+
 class LowdinGB300Error(RuntimeError):
     pass
 
@@ -267,11 +273,11 @@ class Batch:
     def tuning(self):
         """(choice [6, 6], ms bra-row kernel [6, 6], ms one-quartet-per-thread
         kernel [6, 6]) of the last autotune."""
-        ch = np.zeros(36, np.int32)
-        a = np.zeros(36, np.float32)
-        b = np.zeros(36, np.float32)
+        ch = np.zeros(NPC * NPC, np.int32)
+        a = np.zeros(NPC * NPC, np.float32)
+        b = np.zeros(NPC * NPC, np.float32)
         lib().LowdinGB300_batch_tuning(self.h, ch, a, b)
-        return ch.reshape(6, 6), a.reshape(6, 6), b.reshape(6, 6)
+        return ch.reshape(NPC, NPC), a.reshape(NPC, NPC), b.reshape(NPC, NPC)
 
     def use_graph(self, on: bool):
         lib().LowdinGB300_batch_use_graph(self.h, int(bool(on)))
@@ -282,16 +288,16 @@ class Batch:
             raise LowdinGB300Error("batch fock failed")
 
     def quartets(self, stream: int = 0) -> np.ndarray:
-        out = np.zeros(36, np.int64)
+        out = np.zeros(NPC * NPC, np.int64)
         if lib().LowdinGB300_batch_quartets(self.h, out, stream) < 0:
             _check()
-        return out.reshape(6, 6)
+        return out.reshape(NPC, NPC)
 
     def coupling_quartets(self, stream: int = 0) -> np.ndarray:
-        out = np.zeros(36, np.int64)
+        out = np.zeros(NPC * NPC, np.int64)
         if lib().LowdinGB300_batch_coupling_quartets(self.h, out, stream) < 0:
             _check()
-        return out.reshape(6, 6)
+        return out.reshape(NPC, NPC)
 
     def close(self):
         if getattr(self, "h", None):
@@ -477,10 +483,10 @@ class Libint2Interface:
         return int(lib().LowdinGB300_last_quartets(self.h))
 
     def last_class_quartets(self) -> np.ndarray:
-        """[6][6] quartets per (bra pair class, ket pair class) of the last build."""
-        out = np.zeros(36, np.int64)
+        """[NPC][NPC] quartets per (bra pair class, ket pair class) of the last build."""
+        out = np.zeros(NPC * NPC, np.int64)
         lib().LowdinGB300_last_class_quartets(self.h, out)
-        return out.reshape(6, 6)
+        return out.reshape(NPC, NPC)
 
     def mp2_direct(self, d_ptr: int, c_ptr: int, eps, n_occ: int, n_frozen: int = 0, precision: int = 0,
                    x_budget_gb: float = 0.0, stream: int = 0) -> float:
@@ -542,7 +548,7 @@ class Libint2Interface:
         return e2.value
 
     def pair_class_counts(self, all_pairs: bool) -> np.ndarray:
-        out = np.zeros(6, np.int32)
+        out = np.zeros(NPC, np.int32)
         if lib().LowdinGB300_pair_class_counts(self.h, int(all_pairs), out) < 0:
             _check()
         return out

@@ -19,7 +19,9 @@ It extracts, as data:
   * for open-shell UHF: the inputs and checkers ``test/HOO+.ROCI-HF`` (triplet
     HOO+, cc-pVDZ electrons, DZSPNB proton), ``test/H3+.FCI`` (6-31G** electrons,
     DZSPDN proton) and ``test/H.APMO.READCOEFF`` (one electron, cc-pVDZ, DZSNB
-    proton) with their bases (only the SCF energy of these checkers is used).
+    proton) with their bases (only the SCF energy of these checkers is used),
+  * ``test/HF.APMO`` (HF with cc-pVTZ electrons, f shell on F, and a DZSPDN
+    quantum proton): geometry, bases and the checker's HF and MP2 energies.
 The GPU machine has no reference tree, so the tests read only the JSON written here.
 """
 import json
@@ -105,6 +107,8 @@ def main():
             "DZSNB:H_1": read_basis("DZSNB", "HYDROGEN", "H_1"),
             "DZSPNB:H_1": read_basis("DZSPNB", "HYDROGEN", "H_1"),
             "DZSPDN:H_1": read_basis("DZSPDN", "HYDROGEN", "H_1"),
+            "CC-PVTZ:F": read_basis("CC-PVTZ", "FLUORINE", "F"),
+            "CC-PVTZ:H": read_basis("CC-PVTZ", "HYDROGEN", "H"),
         },
         "geometry": {
             "H2O.BOA.DIRECT": read_geometry("H2O.BOA.DIRECT.lowdin"),
@@ -112,6 +116,7 @@ def main():
             "HOO+.ROCI-HF": read_geometry("HOO+.ROCI-HF.lowdin"),
             "H3+.FCI": read_geometry("H3+.FCI.lowdin"),
             "H.APMO.READCOEFF": read_geometry("H.APMO.READCOEFF.lowdin"),
+            "HF.APMO": read_geometry("HF.APMO.lowdin"),
         },
         "values": {
             "H2O.BOA.DIRECT": read_checker("H2O.BOA.DIRECT.py"),
@@ -122,6 +127,7 @@ def main():
             "HOO+.ROCI-HF": read_checker("HOO+.ROCI-HF.py"),
             "H3+.FCI": read_checker("H3+.FCI.py"),
             "H.APMO.READCOEFF": read_checker("H.APMO.READCOEFF.py"),
+            "HF.APMO": read_checker("HF.APMO.py"),
         },
     }
     with open(OUT, "w") as f:

@@ -74,3 +74,20 @@ def h2o_apmo_uhf(golden):
     e = sysd["species"][0]
     sysd["species"] = S.uhf_electron_species(e["shells"], 10, 1) + sysd["species"][1:]
     return sysd
+
+
+def hf_apmo(golden):
+    """test/HF.APMO: HF with cc-pVTZ electrons (an f shell on F), classical F,
+    one quantum proton H_1 (DZSPDN)."""
+    geo = golden["geometry"]["HF.APMO"]
+    shells, Z, R, prot = [], [], [], []
+    for r in geo:
+        part = r["particle"]
+        if part.startswith("e-"):
+            shells += _shells(golden, "CC-PVTZ:" + part[3:-1], r["position_bohr"])
+        elif r["basis"] == "dirac":
+            Z.append(9.0); R.append(r["position_bohr"])
+        else:
+            prot.append(S.proton_species(_shells(golden, "DZSPDN:H_1", r["position_bohr"]), 1, name=part.upper()))
+    return {"species": [S.electron_species(shells, 10)] + prot, "point_charges": Z, "point_positions": R,
+            "name": "HF.APMO"}

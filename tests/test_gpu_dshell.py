@@ -50,7 +50,7 @@ def test_twobody_d_shells_random_density(L, oracle):
     ref = oracle.two_body_direct(oracle.Basis.from_shells(sp["shells"]), True, D, -0.5)
     assert np.max(np.abs(G - ref)) < TOL_FOCK
     assert h.last_quartets() == oracle.last_quartet_count()
-    cq = np.array(h.last_class_quartets()).reshape(6, 6)
+    cq = np.array(h.last_class_quartets()).reshape(L.NPC, L.NPC)
     assert cq[5, 5] > 0 and cq[5, 4] > 0       # cooperative classes evaluated
     h.close()
 

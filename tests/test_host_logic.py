@@ -60,7 +60,7 @@ def test_serving_stream_is_seeded_poisson():
 
 
 def test_flop_model_is_additive():
-    c = np.zeros((6, 6), np.int64)
+    c = np.zeros((10, 10), np.int64)
     c[0, 0], c[1, 0], c[1, 1] = 10, 7, 3
     tot = FL.class_table_flops(c, "jk")
     parts = 10 * FL.quartet_flops(0, 0, 0, 0, "jk") + 7 * FL.quartet_flops(1, 0, 0, 0, "jk") + \
@@ -149,7 +149,7 @@ def test_bench_per_job_table_and_tuning_summary():
     rows = bench.per_job_table(reqs, plain, mixed)
     assert abs(rows[0]["abs_dE_mixed_vs_plain_Eh"] - 3e-9) < 1e-12
     assert rows[1]["converged_mixed"] is False and abs(rows[1]["abs_dE2_mixed_vs_plain_Eh"] - 0.1) < 1e-12
-    ch = np.full((6, 6), -1)
+    ch = np.full((10, 10), -1)
     ch[0, 0], ch[1, 0] = 1, 0
     ms = np.where(ch >= 0, 1.0, -1.0).astype(np.float32)
     s = bench.tuning_summary([(ch, ms, 2 * ms)])
