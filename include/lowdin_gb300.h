@@ -341,8 +341,10 @@ int LowdinGB300_gemm_bf16_split(const float *dA, const float *dB, float *dC, int
                                 void *stream);
 /* Same product, three pieces per operand, eight products (adds p1q2 + p2q1)
    and no long FP32 running sums: every 16-wide K slab's main product is
-   rounded once and all partial results are added in FP64.  For contractions
-   with strong cancellation (the MP2 transform's first quarter). */
+   rounded once by the tensor cores, its mean rounding loss added back, and
+   the partial results enter a compensated FP32 sum (hi + lo).  For
+   contractions with strong cancellation and for squared results (every
+   quarter of the MP2 transform at precision 2). */
 int LowdinGB300_gemm_bf16_precise(const float *dA, const float *dB, float *dC, int M, int N, int K, void *stream);
 /* Benchmark of the tensor-core GEMM engines (no counterpart in the reference):
    operands of M x K and N x K pseudo-random values split once, then `reps`
