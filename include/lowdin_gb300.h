@@ -260,7 +260,8 @@ int LowdinGB300_batch_coupling_quartets(LowdinGB300_Batch *b, long long *out, vo
    Work buffers live in one static device
    array (LowdinGB300_noalloc_scratch_bytes() bytes, ~9.5 MB, held by every GPU
    that loads the library until the process exits); species are limited to 512
-   Cartesian functions and 512 shells, larger ones are rejected with an error.
+   Cartesian functions, 512 shells and shells up to d (f shells need global
+   work arrays for some classes); others are rejected with an error.
    The handle must have been set up with LibintInterface_init_2body_ints (which
    does allocate).  The first call on a device looks up the array's device
    address (cudaGetSymbolAddress): make that first call before any stream

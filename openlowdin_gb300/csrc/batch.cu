@@ -33,6 +33,7 @@ struct LowdinGB300_Batch {
   // pair-indexed arrays of the FP32 row kernels, one PairSlot per two-body species
   DevBuf<float> Dp32, Jp32, DnP32;
   DevBuf<float> Dnmax32;   // per slot: largest shell-block norm of the build's input
+  int max_nsh = 0;
   DevBuf<PairSlot> pslots;
   int npslots = 0;
   long long ptotal = 0;
@@ -128,8 +129,11 @@ struct LowdinGB300_Batch {
       pptot += (long long)sp[k].h->sig.h.size();
     }
     if (!Dp32.ensure(std::max(1LL, petot)) || !Jp32.ensure(std::max(1LL, petot)) ||
-        !DnP32.ensure(std::max(1LL, pptot)) || !Dnmax32.ensure(std::max<size_t>(1, sp.size())))
+        !DnP32.ensure(std::max(1LL, pptot)))
       return false;
+    max_nsh = 0;
+    for (size_t k = 0; k < sp.size(); ++k) max_nsh = std::max(max_nsh, sp[k].h->nshell());
+    if (!Dnmax32.ensure(std::max<size_t>(1, sp.size()))) return false;
     std::vector<PairSlot> hps;
     std::vector<SpeciesSlot> hs(sp.size());
     std::vector<SpeciesBufs> bf(sp.size());
@@ -293,7 +297,8 @@ struct LowdinGB300_Batch {
     CK(cudaMemsetAsync(Dn.p, 0, Dn.n * sizeof(double), s));
     CK(cudaMemsetAsync(Dn32.p, 0, Dn32.n * sizeof(float), s));
     CK(launch_prepare_batch(slots.p, nslots, total, s));
-    CK(launch_dn_max_batch(slots.p, nslots, s));
+    CK(cudaMemsetAsync(Dnmax32.p, 0, Dnmax32.n * sizeof(float), s));
+    CK(launch_dn_max_batch(slots.p, nslots, max_nsh, s));
     if (npslots) CK(launch_pair_gather(pslots.p, npslots, ptotal, s));
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -357,7 +362,10 @@ struct LowdinGB300_Batch {
     CK(cudaMemsetAsync(cnt.p, 0, 2 * kNQC * sizeof(unsigned long long), s));
     CK(launch_prepare_batch(slots.p, nslots, total, s));
     const int jk_mixed = precision & 1;
-    if (jk_mixed) CK(launch_dn_max_batch(slots.p, nslots, s));
+    if (jk_mixed) {
+      CK(cudaMemsetAsync(Dnmax32.p, 0, Dnmax32.n * sizeof(float), s));
+      CK(launch_dn_max_batch(slots.p, nslots, max_nsh, s));
+    }
     if (jk_mixed && npslots) CK(launch_pair_gather(pslots.p, npslots, ptotal, s));
     if (!LibintInterface::launch_jk_groups(jk, jk_mixed, jk_mixed ? split : 0.0, boys, s, skip, rows_choice))
       return false;

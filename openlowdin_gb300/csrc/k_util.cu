@@ -143,7 +143,7 @@ __global__ void prepare_batch_kernel(const SpeciesSlot *__restrict__ slots, int 
   }
 }
 
-// largest shell-block norm: one block per slot (or one block for one array)
+// maximum over the block (valid in thread 0)
 __device__ __forceinline__ float block_max(float m) {
   __shared__ float part[32];
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -156,22 +156,27 @@ __device__ __forceinline__ float block_max(float m) {
   return m;   // valid in thread 0
 }
 
-__global__ void dn_max_batch_kernel(const SpeciesSlot *__restrict__ slots) {
-  const SpeciesSlot &S = slots[blockIdx.x];
-  if (!S.Dn32 || !S.Dnmax32) return;
-  if (S.active && __ldg(S.active) == 0) return;
-  const int cnt = S.nsh * S.nsh;
+// largest of Dn32: block x takes columns [256 x, 256 x + 256) of the nsh x nsh
+// norms (a thread walks its column, coalesced across the block), its maximum
+// goes to *out (non-negative floats order as their bit patterns)
+__device__ __forceinline__ void dn_max_block(const float *__restrict__ Dn32, int nsh, float *__restrict__ out) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
   float m = 0.f;
-  for (int i = threadIdx.x; i < cnt; i += blockDim.x) m = fmaxf(m, S.Dn32[i]);
+  if (s < nsh)
+    for (int t = 0; t < nsh; ++t) m = fmaxf(m, Dn32[(size_t)t * nsh + s]);
   m = block_max(m);
-  if (threadIdx.x == 0) *S.Dnmax32 = m;
+  if (threadIdx.x == 0) atomicMax(reinterpret_cast<int *>(out), __float_as_int(m));
 }
 
-__global__ void dn_max_kernel(const float *__restrict__ Dn32, int cnt, float *__restrict__ out) {
-  float m = 0.f;
-  for (int i = threadIdx.x; i < cnt; i += blockDim.x) m = fmaxf(m, Dn32[i]);
-  m = block_max(m);
-  if (threadIdx.x == 0) *out = m;
+__global__ void dn_max_batch_kernel(const SpeciesSlot *__restrict__ slots) {
+  const SpeciesSlot &S = slots[blockIdx.y];
+  if (!S.Dn32 || !S.Dnmax32 || blockIdx.x * blockDim.x >= (unsigned)S.nsh) return;
+  if (S.active && __ldg(S.active) == 0) return;
+  dn_max_block(S.Dn32, S.nsh, S.Dnmax32);
+}
+
+__global__ void dn_max_kernel(const float *__restrict__ Dn32, int nsh, float *__restrict__ out) {
+  dn_max_block(Dn32, nsh, out);
 }
 
 // G = gscale N (Gacc + Gacc^T) N (0 when the species builds none), J = N Jacc N,
@@ -292,15 +297,17 @@ cudaError_t launch_prepare_batch(const SpeciesSlot *slots, int nslots, long long
   return cudaGetLastError();
 }
 
-cudaError_t launch_dn_max_batch(const SpeciesSlot *slots, int nslots, cudaStream_t s) {
-  if (nslots <= 0) return cudaSuccess;
-  dn_max_batch_kernel<<<nslots, 256, 0, s>>>(slots);
+cudaError_t launch_dn_max_batch(const SpeciesSlot *slots, int nslots, int max_nsh, cudaStream_t s) {
+  if (nslots <= 0 || max_nsh <= 0) return cudaSuccess;
+  dn_max_batch_kernel<<<dim3((unsigned)((max_nsh + 255) / 256), (unsigned)nslots), 256, 0, s>>>(slots);
   count_launches(1);
   return cudaGetLastError();
 }
 
-cudaError_t launch_dn_max(const float *Dn32, int count, float *out, cudaStream_t s) {
-  dn_max_kernel<<<1, 1024, 0, s>>>(Dn32, count, out);
+cudaError_t launch_dn_max(const float *Dn32, int nsh, float *out, cudaStream_t s) {
+  const cudaError_t e = cudaMemsetAsync(out, 0, sizeof(float), s);
+  if (e != cudaSuccess) return e;
+  dn_max_kernel<<<(nsh + 255) / 256, 256, 0, s>>>(Dn32, nsh, out);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -353,10 +353,11 @@ struct SpeciesSlot {
   float *Dnmax32;         // largest element of Dn32 (null: not computed)
 };
 cudaError_t launch_prepare_batch(const SpeciesSlot *slots, int nslots, long long total, cudaStream_t s);
-// Dnmax32 of every slot that has Dn32 (after launch_prepare_batch)
-cudaError_t launch_dn_max_batch(const SpeciesSlot *slots, int nslots, cudaStream_t s);
-// *out = max of Dn32[0 .. count)
-cudaError_t launch_dn_max(const float *Dn32, int count, float *out, cudaStream_t s);
+// Dnmax32 of every slot that has Dn32 (after launch_prepare_batch; the
+// Dnmax32 values must be zero beforehand); max_nsh: largest nsh of a slot
+cudaError_t launch_dn_max_batch(const SpeciesSlot *slots, int nslots, int max_nsh, cudaStream_t s);
+// *out = max of Dn32[0 .. nsh * nsh) (set to zero here first)
+cudaError_t launch_dn_max(const float *Dn32, int nsh, float *out, cudaStream_t s);
 
 // pair-indexed copies of a species' FP32 density for the FP32 row kernels:
 // for every significant pair (class c, position k in its class) and element e

@@ -536,7 +536,7 @@ struct LibintInterface {
       jk_ready = true;
     }
     CK(launch_prepare_density(dDin, d_norma, d_shell_of, n, nsh, dDs.p, dDs32.p, dDn.p, dDn32.p, s));
-    if (precision != 0 && is_electron) CK(launch_dn_max(dDn32.p, nsh * nsh, dDnmax32.p, s));
+    if (precision != 0 && is_electron) CK(launch_dn_max(dDn32.p, nsh, dDnmax32.p, s));
     CK(cudaMemsetAsync(dGacc.p, 0, sizeof(double) * n * n, s));
     CK(cudaMemsetAsync(dGacc32.p, 0, sizeof(float) * n * n, s));
     CK(cudaMemsetAsync(dcount.p, 0, sizeof(unsigned long long) * kNQC, s));

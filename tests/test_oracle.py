@@ -232,3 +232,34 @@ def test_golden_h2o_apmo_uhf(oracle, golden):
     res = oracle.scf(oracle.from_plain(GS.h2o_apmo_uhf(golden)), tol_energy=1e-11, tol_density=1e-9)
     ref = golden["values"]["H2O.APMO.UHF.DIRECT"]["HF energy"]
     assert res.converged and abs(res.energy - ref[0]) <= ref[1]
+
+
+def test_f_shell_loops_against_full_tensor(oracle):
+    """f shells (the classes the GPU runs on its cooperative kernels): the
+    screened direct loops equal J + fK contracted from the full integral
+    tensor, and the tensor keeps the 8-fold permutational symmetry."""
+    A, B = [0.0, 0.0, 0.0], [0.0, 0.9, 1.3]
+    sh = []
+    for c in (A, B):
+        sh += [(0, [3.0, 0.6], [0.4, 0.7], c), (1, [1.1], [1.0], c), (3, [1.3], [1.0], c)]
+    b = oracle.Basis.from_shells(sh)
+    eri = oracle.eri_full(b)
+    assert np.max(np.abs(eri - eri.transpose(1, 0, 2, 3))) < 1e-13
+    assert np.max(np.abs(eri - eri.transpose(2, 3, 0, 1))) < 1e-13
+    rng = np.random.default_rng(3)
+    X = rng.normal(size=(b.nbf, b.nbf)) * 0.1
+    D = X + X.T
+    G = oracle.two_body_direct(b, True, D, -0.5)
+    assert np.max(np.abs(G - _jk_full(eri, D, -0.5))) < 1e-10
+
+
+def test_golden_hf_apmo(oracle, golden):
+    """test/HF.APMO (cc-pVTZ with an f shell on F, DZSPDN proton): HF within
+    the checker's 1e-7 Eh, APMO-MP2 within 1e-5 Eh."""
+    sysd = GS.hf_apmo(golden)
+    sysO = oracle.from_plain(sysd)
+    res = oracle.scf(sysO, tol_energy=1e-11, tol_density=1e-9)
+    ref = golden["values"]["HF.APMO"]
+    assert res.converged and abs(res.energy - ref["HF energy"][0]) <= 1e-7
+    mp2 = oracle.apmo_mp2(sysO, res)
+    assert abs(mp2["total"] - ref["MP2 energy"][0]) <= ref["MP2 energy"][1]
