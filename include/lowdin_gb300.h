@@ -152,6 +152,16 @@ void LowdinGB300_clear_error(void);
    row-major n x n, host memory. */
 void LowdinGB300_potential(LibintInterface *lint, int ncharge, const double *Z, const double *R, double *result);
 
+/* External Gaussian-fit potential of a species (EXTERPOTENTIAL):
+   V_ij = sum_k c_k <i| exp(-g_k |r - C_k|^2) |j> (norma applied) for ncomp
+   s-type components with coefficients c, exponents g and origins C (3 ncomp,
+   bohr); row-major n x n, host memory, computed on the host.  Replaces
+   DirectIntegralManager_getExternalPotentialIntegrals
+   (src/ints/DirectIntegralManager.f90:848-949), which the reference computes
+   in Fortran outside the Libint interface. */
+void LowdinGB300_gaussian_potential(LibintInterface *lint, int ncomp, const double *coefficients,
+                                    const double *exponents, const double *origins, double *result);
+
 /* Precision of this handle's LibintInterface_compute_2body_direct (host
    buffers, the reference's own call): 0 = FP64 (default, the reference's
    behaviour); 1 = quartets whose Schwarz bound times the density's shell-block

@@ -34,7 +34,8 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import lint
-from .scf import SCFResult, _one_body_device, _orthogonaliser, _orthogonaliser_np, n_occ, nuclear_repulsion
+from .scf import (SCFResult, _one_body_device, _orthogonaliser, _orthogonaliser_np, coulomb_only, n_occ,
+                  nuclear_repulsion)
 
 HOST_EIGH_MAX = 384   # matrices below this size are diagonalised on the host (single-threaded LAPACK beats the GPU solver up to ~350 functions)
 PAD = 1.0e4           # diagonal of H on padded rows (far above every occupied orbital energy)
@@ -112,6 +113,8 @@ class BatchSCF:
         guard_energy, or with an FP64 commutator element above
         guard_commutator, the system continues in FP64 until it converges."""
         import torch
+        for sysd in systems:
+            coulomb_only(sysd, "BatchSCF")
         self.torch = torch
         self.guard = guard and precision == "mixed"
         self.guard_energy = guard_energy

@@ -182,6 +182,36 @@ void overlap_block(const HostShell &A, const HostShell &B, double *S, double *T)
     }
 }
 
+// raw external-potential block sum_k c_k <a| exp(-g_k |r - C_k|^2) |b>: the
+// three Gaussians multiply to exp(-p |r - P|^2) with p = a + b + g and
+// P = (a A + b B + g C) / p, times exp(-(a b AB^2 + a g AC^2 + b g BC^2) / p),
+// so each component is an ordinary overlap recursion about that P
+void gaussian_potential_block(const HostShell &A, const HostShell &B, int ncomp, const double *coef,
+                              const double *expo, const double *C, double *V) {
+  const int n1 = ncart(A.l), n2 = ncart(B.l);
+  std::fill(V, V + n1 * n2, 0.0);
+  for (int pa = 0; pa < A.nprim; ++pa)
+    for (int pb = 0; pb < B.nprim; ++pb)
+      for (int k = 0; k < ncomp; ++k) {
+        const double a = A.alpha[pa], b = B.alpha[pb], g = expo[k], p = a + b + g, o2p = 0.5 / p;
+        double e = 0, s[3][8][8];
+        for (int d = 0; d < 3; ++d) {
+          const double ab = A.O[d] - B.O[d], ac = A.O[d] - C[3 * k + d], bc = B.O[d] - C[3 * k + d];
+          e += a * b * ab * ab + a * g * ac * ac + b * g * bc * bc;
+          const double P = (a * A.O[d] + b * B.O[d] + g * C[3 * k + d]) / p;
+          ovl1d(A.l, B.l, P - A.O[d], P - B.O[d], o2p, s[d]);
+        }
+        const double pref = coef[k] * std::pow(M_PI / p, 1.5) * std::exp(-e / p) * A.cn[pa] * B.cn[pb];
+        for (int f1 = 0; f1 < n1; ++f1) {
+          const int c1 = coff(A.l) + f1;
+          for (int f2 = 0; f2 < n2; ++f2) {
+            const int c2 = coff(B.l) + f2;
+            V[f1 * n2 + f2] += pref * s[0][cx(c1)][cx(c2)] * s[1][cy(c1)][cy(c2)] * s[2][cz(c1)][cz(c2)];
+          }
+        }
+      }
+}
+
 // raw point-charge potential block sum_C Z_C <a|1/|r-C||b> via Obara-Saika on
 // the bra and horizontal transfer to b
 void potential_block(const HostShell &A, const HostShell &B, int nc, const double *Z, const double *R, double *V) {
@@ -778,6 +808,31 @@ void LowdinGB300_potential(LibintInterface *lint, int ncharge, const double *Z, 
     for (int s2 = 0; s2 < nsh; ++s2) {
       const HostShell &A = lint->shells[s1], &B = lint->shells[s2];
       potential_block(A, B, ncharge, Z, R, V);
+      const int n1 = ncart(A.l), n2 = ncart(B.l);
+      for (int f1 = 0; f1 < n1; ++f1)
+        for (int f2 = 0; f2 < n2; ++f2) {
+          const int i = lint->first[s1] + f1, j = lint->first[s2] + f2;
+          result[(size_t)i * n + j] = V[f1 * n2 + f2] * lint->norma[i] * lint->norma[j];
+        }
+    }
+}
+
+// the external Gaussian-fit potential of a species, the matrix the reference
+// builds in src/ints/DirectIntegralManager.f90:848-949 (each basis contraction
+// times each potential component, then an overlap with the other contraction)
+void LowdinGB300_gaussian_potential(LibintInterface *lint, int ncomp, const double *coefficients,
+                                    const double *exponents, const double *origins, double *result) {
+  if (!check_handle(lint, __func__)) return;
+  if (ncomp < 0 || (ncomp > 0 && (!coefficients || !exponents || !origins)) || !result) {
+    set_error("gaussian_potential: invalid components (ncomp=%d)", ncomp);
+    return;
+  }
+  const int n = lint->nbasis, nsh = lint->nshell();
+  double V[225];
+  for (int s1 = 0; s1 < nsh; ++s1)
+    for (int s2 = 0; s2 < nsh; ++s2) {
+      const HostShell &A = lint->shells[s1], &B = lint->shells[s2];
+      gaussian_potential_block(A, B, ncomp, coefficients, exponents, origins, V);
       const int n1 = ncart(A.l), n2 = ncart(B.l);
       for (int f1 = 0; f1 < n1; ++f1)
         for (int f2 = 0; f2 < n2; ++f2) {

@@ -68,6 +68,7 @@ def lib():
                                                                 ctypes.POINTER(ctypes.c_int)]
         L.LowdinGB300_last_error.restype = ctypes.c_char_p
         L.LowdinGB300_potential.argtypes = [_vp, ctypes.c_int, _f64p, _f64p, _f64p]
+        L.LowdinGB300_gaussian_potential.argtypes = [_vp, ctypes.c_int, _f64p, _f64p, _f64p, _f64p]
         L.LowdinGB300_twobody_device.argtypes = [_vp, _vp, _vp, ctypes.c_double, ctypes.c_int, ctypes.c_double, _vp]
         L.LowdinGB300_twobody_device.restype = ctypes.c_int
         L.LowdinGB300_one_body_device.argtypes = [_vp, ctypes.c_int, _f64p, _f64p, _vp, _vp, _vp, _vp]
@@ -166,7 +167,7 @@ EXPORTED_SYMBOLS = [
     "libintinterface_compute_g12inter_direct", "LibintInterface_compute_2body_directAll",
     "LibintInterface_compute_coupling_directAll", "libintinterface_compute_g12_directAll",
     "libintinterface_compute_g12inter_directAll", "LowdinGB300_last_error", "LowdinGB300_clear_error",
-    "LowdinGB300_potential", "LowdinGB300_set_precision", "LowdinGB300_twobody_device", "LowdinGB300_one_body_device", "LowdinGB300_coupling_device",
+    "LowdinGB300_potential", "LowdinGB300_gaussian_potential", "LowdinGB300_set_precision", "LowdinGB300_twobody_device", "LowdinGB300_one_body_device", "LowdinGB300_coupling_device",
     "LowdinGB300_last_quartets", "LowdinGB300_version", "LowdinGB300_last_class_quartets",
     "LowdinGB300_pair_class_counts", "LowdinGB300_measure_fma_tflops", "LowdinGB300_launch_count",
     "LowdinGB300_batch_new", "LowdinGB300_batch_del", "LowdinGB300_batch_add_system",
@@ -456,6 +457,21 @@ class Libint2Interface:
         Z = np.ascontiguousarray(charges, np.float64)
         R = np.ascontiguousarray(positions, np.float64).reshape(-1)
         lib().LowdinGB300_potential(self.h, len(Z), Z, R if len(R) else np.zeros(3), out)
+        _check()
+        return out
+
+    def gaussian_potential(self, coefficients, exponents, origins) -> np.ndarray:
+        """External Gaussian-fit potential sum_k c_k <i|exp(-g_k |r - C_k|^2)|j>
+        (host, LowdinGB300_gaussian_potential)."""
+        n = self.nbasis
+        out = np.empty((n, n))
+        c = np.ascontiguousarray(coefficients, np.float64)
+        g = np.ascontiguousarray(exponents, np.float64)
+        C = np.ascontiguousarray(origins, np.float64).reshape(-1)
+        if len(c) != len(g) or len(C) != 3 * len(c):
+            raise ValueError("gaussian_potential: coefficients, exponents and origins differ in length")
+        lib().LowdinGB300_gaussian_potential(self.h, len(c), c if len(c) else np.zeros(1),
+                                             g if len(g) else np.zeros(1), C if len(C) else np.zeros(3), out)
         _check()
         return out
 

@@ -12,6 +12,11 @@ src/scf (MultiSCF.f90:276-440 iteration scheme 3, WaveFunction.f90):
     J_i = sum_{j != i} q_i q_j J_i[P_j]              (WaveFunction.f90:1432-1505)
     F_i = H_i + G_i + J_i                            (WaveFunction.f90:1768-1826)
   E = E_nuc + sum_i tr P_i (H_i + G_i / 2) + sum_{i<j} tr P_i J_ij
+  Gaussian-fit potentials (HostSCF): an external potential of species i is
+  added to H_i (DirectIntegralManager.f90:848-949); with interpotentials
+  every G_i and J_ij is a G12 matrix of the pair's potential instead of
+  Coulomb, without charge factors, and pairs without one do not interact
+  (WaveFunction.f90:1097-1135, 1439-1477)
   Pulay DIIS over all species (one coefficient set), F' = X^T F X, C = X C',
   P_i = eta_i C_occ C_occ^T; converged when |dE| < tol and rms(dP) < tol_p.
 
@@ -88,6 +93,26 @@ def _one_body_device(handles, sysd, device, stream):
         H.append(T / sp["mass"] + sp["charge"] * V)
         S.append(Sm)
     return H, S
+
+
+def interpotentials(sysd) -> dict:
+    """{(i, j), i <= j: (coefficients, exponents)} of sysd["interpotentials"],
+    a list of {"species": [i, j], "coefficients": [...], "exponents": [...]}."""
+    out = {}
+    for e in sysd.get("interpotentials", []):
+        i, j = sorted(int(x) for x in e["species"])
+        if len(e["coefficients"]) != len(e["exponents"]):
+            raise ValueError(f"interpotential {i},{j}: coefficients and exponents differ in length")
+        out[(i, j)] = (list(e["coefficients"]), list(e["exponents"]))
+    return out
+
+
+def coulomb_only(sysd, who: str) -> None:
+    """Raise unless the system has only Coulomb interactions: drivers that keep
+    no Gaussian-fit potential path must not drop one silently."""
+    if sysd.get("interpotentials") or sysd.get("external_potentials"):
+        raise ValueError(f"{who}: Gaussian-fit potentials (interpotentials / external_potentials) "
+                         "are supported by HostSCF only")
 
 
 def _orthogonaliser(S, cut=1e-8, host_max=384):
@@ -186,7 +211,13 @@ class HostSCF:
     gives the result's energy and its stated error |E_mixed - E_FP64|; above
     guard_energy, or with an FP64 commutator element above guard_commutator,
     the solve continues in FP64 with a fresh DIIS history.  Couplings stay
-    FP64 full builds."""
+    FP64 full builds.
+
+    Gaussian-fit potentials: sysd["external_potentials"], a list of
+    {"species": i, "coefficients", "exponents", "origins"}, are added to H_i
+    (LowdinGB300_gaussian_potential); sysd["interpotentials"] switches every
+    species pair to G12 matrices (libintinterface_compute_g12_direct /
+    _g12inter_direct, FP64 full builds)."""
 
     def __init__(self, sysd, precision="fp64", split=1e-5, guard_energy=1e-6, guard_commutator=1e-4):
         if precision not in ("fp64", "mixed"):
@@ -199,6 +230,13 @@ class HostSCF:
         for h in self.handles:
             h.init_2body_ints()
         self.H, self.S = _one_body(self.handles, sysd)
+        for e in sysd.get("external_potentials", []):
+            i = int(e["species"])
+            self.H[i] = self.H[i] + self.handles[i].gaussian_potential(e["coefficients"], e["exponents"],
+                                                                       e["origins"])
+        self.g12 = interpotentials(sysd)
+        if self.g12 and precision != "fp64":
+            raise ValueError("mixed precision applies to Coulomb builds; G12 systems run in FP64")
         self.X = [_orthogonaliser_np(S) for S in self.S]
         self.enuc = nuclear_repulsion(sysd)
 
@@ -234,6 +272,22 @@ class HostSCF:
             full = fp64 or it == 1
             G, J = [], [[None] * ns for _ in range(ns)]
             for i in range(ns):
+                if self.g12:
+                    pot = self.g12.get((i, i))
+                    if sp[i]["n_particles"] > 1 and pot:
+                        G.append(self.handles[i].compute_g12_direct(P[i], sp[i]["kappa"] / sp[i]["eta"], *pot))
+                    else:
+                        G.append(np.zeros_like(H[i]))
+                    for j in range(ns):
+                        pot = self.g12.get((min(i, j), max(i, j)))
+                        if j == i:
+                            continue
+                        if pot:
+                            B = self.handles[i].compute_g12inter_direct(self.handles[j], P[j], *pot)
+                            J[i][j] = np.tril(B) + np.tril(B, -1).T
+                        else:
+                            J[i][j] = np.zeros_like(H[i])
+                    continue
                 if sp[i]["n_particles"] > 1:
                     f = sp[i]["kappa"] / sp[i]["eta"]
                     q2 = sp[i]["charge"] ** 2

@@ -30,7 +30,7 @@ import numpy as np
 
 from . import lint
 from .batch_scf import MIXED_SKIP
-from .scf import _one_body_device, _orthogonaliser, n_occ, nuclear_repulsion, occupied_subspace
+from .scf import _one_body_device, _orthogonaliser, coulomb_only, n_occ, nuclear_repulsion, occupied_subspace
 from .systems import n_core
 
 HOST_EIGH_MAX = 384
@@ -583,6 +583,8 @@ class ServingEngine:
         alternately: while one cohort's eigensolves run on the host pool, the
         other cohort's Fock build runs on the GPU."""
         torch = self.torch
+        for r in requests:
+            coulomb_only(r.system, "ServingEngine")
         pending = sorted(requests, key=lambda r: r.arrival)
         results = []
         cohorts = [[], []]

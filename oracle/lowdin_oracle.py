@@ -18,6 +18,10 @@ restated from the Fortran program:
   (``WaveFunction.f90:1768-1826``), P = eta C_occ C_occ^T (``:1830-1878``),
 * total energy E_nuc + sum_i tr P_i (H_i + G_i/2) + sum_{i<j} tr P_i J_ij
   (``WaveFunction.f90:1882-2003``),
+* Gaussian-fit potentials: INTERPOTENTIAL replaces every Coulomb term by G12
+  matrices without charge factors (``WaveFunction.f90:1097-1135, 1439-1477``),
+  EXTERPOTENTIAL adds sum_k c_k exp(-g_k |r - C_k|^2) to H
+  (``src/ints/DirectIntegralManager.f90:848-949``),
 * iteration scheme 3 -- every species once per global iteration
   (``src/scf/MultiSCF.f90:276-440``) with Pulay DIIS (``src/scf/Convergence.f90``),
 * closed-shell MP2 from (ia|jb) (``src/MBPT/MPFunctions.f90:514-662``).
@@ -268,6 +272,74 @@ def potential(b: Basis, charges, positions):
     return V.reshape(n, n)
 
 
+def _prim_norm(a: float, l: int) -> float:
+    """Norm of the x^l component of a primitive (src/ints/Libint2Iface.cpp:79-128)."""
+    df = 1.0
+    for k in range(2 * l - 1, 1, -2):
+        df *= k
+    return float(np.sqrt(2.0 ** l * (2.0 * a) ** (l + 1.5) / (np.pi ** 1.5 * df)))
+
+
+def _cart_exponents(l: int):
+    return [(l - i, i - j, j) for i in range(l + 1) for j in range(i + 1)]
+
+
+def gaussian_potential(b: Basis, coefficients, exponents, origins) -> np.ndarray:
+    """External Gaussian-fit potential V_ij = sum_k c_k <i|exp(-g_k |r - C_k|^2)|j>
+    (src/ints/DirectIntegralManager.f90:848-949: each contraction times each
+    potential component, then an overlap with the other contraction), each
+    Cartesian function normalised to one like ``norma``.
+
+    Computed by Gauss-Hermite quadrature in each direction after completing the
+    square of the three Gaussians (8 nodes: exact for the polynomial degree
+    <= 15 that shells up to l = 7 give), not by the recursion the library uses."""
+    xg, wg = np.polynomial.hermite.hermgauss(8)
+    cs = np.asarray(coefficients, float)
+    gs = np.asarray(exponents, float)
+    Cs = np.asarray(origins, float).reshape(-1, 3)
+    n = b.nbf
+    V, S = np.zeros((n, n)), np.zeros((n, n))
+    shells, off, first = [], 0, 0
+    for s in range(b.nshell):
+        l, k = int(b.l[s]), int(b.nprim[s])
+        al = b.alpha[off:off + k]
+        cn = np.array([b.coef[off + p] * _prim_norm(al[p], l) for p in range(k)])
+        shells.append((l, al, cn, b.origin[3 * s:3 * s + 3], first))
+        off += k
+        first += (l + 1) * (l + 2) // 2
+
+    def tables(a, A, la, bb, B, lb, g, C):
+        # T[k, d, i, j] = int (x-A_d)^i (x-B_d)^j exp(-(p (x-x0)^2)) dx, and the
+        # remaining factor exp(-c0_k) p_k^-1.5 of each component k
+        p = a + bb + g
+        x0 = (a * A[None, :] + bb * B[None, :] + g[:, None] * C) / p[:, None]
+        c0 = np.sum(a * A ** 2 + bb * B ** 2 + g[:, None] * C ** 2 - p[:, None] * x0 ** 2, axis=1)
+        x = x0[:, :, None] + xg[None, None, :] / np.sqrt(p)[:, None, None]
+        pa = (x - A[None, :, None])[..., None] ** np.arange(la + 1)
+        pb = (x - B[None, :, None])[..., None] ** np.arange(lb + 1)
+        T = np.einsum("q,kdqi,kdqj->kdij", wg, pa, pb)
+        return T, np.exp(-c0) / p ** 1.5
+
+    one, zero = np.ones(1), np.zeros((1, 3))
+    for la, aa, ca, A, fa in shells:
+        for lb, ab, cb, B, fb in shells:
+            ea, eb = _cart_exponents(la), _cart_exponents(lb)
+            for pa_ in range(len(aa)):
+                for pb_ in range(len(ab)):
+                    w = ca[pa_] * cb[pb_]
+                    for M, c, g, C in ((V, cs, gs, Cs), (S, one, np.zeros(1), zero)):
+                        if len(c) == 0:
+                            continue
+                        T, f = tables(aa[pa_], A, la, ab[pb_], B, lb, g, C)
+                        fk = w * c * f
+                        for i, (ix, iy, iz) in enumerate(ea):
+                            for j, (jx, jy, jz) in enumerate(eb):
+                                M[fa + i, fb + j] += float(np.sum(fk * T[:, 0, ix, jx] * T[:, 1, iy, jy]
+                                                                  * T[:, 2, iz, jz]))
+    nrm = 1.0 / np.sqrt(np.diag(S))
+    return V * np.outer(nrm, nrm)
+
+
 def boys(mmax: int, T: float) -> np.ndarray:
     F = np.zeros(mmax + 1)
     lib().or_boys(mmax, T, F)
@@ -301,9 +373,17 @@ class Species:
 
 @dataclass
 class System:
+    """Species, fixed point charges and, optionally, Gaussian-fit potentials:
+    ``interpotentials`` {(i, j), i <= j: (coefficients, exponents)} (INTERPOTENTIAL:
+    when present, every species pair interacts through G12 integrals instead of
+    Coulomb, without charge factors, and pairs without a potential not at all --
+    src/scf/WaveFunction.f90:1097-1135, 1439-1477) and ``external``
+    {i: (coefficients, exponents, origins)} (EXTERPOTENTIAL, added to H_i)."""
     species: list
     point_charges: np.ndarray = field(default_factory=lambda: np.zeros(0))
     point_positions: np.ndarray = field(default_factory=lambda: np.zeros((0, 3)))
+    interpotentials: dict = field(default_factory=dict)
+    external: dict = field(default_factory=dict)
 
     def nuclear_repulsion(self) -> float:
         Z, R = self.point_charges, self.point_positions
@@ -321,8 +401,14 @@ def from_plain(desc) -> System:
         sp.append(Species(s["name"], Basis.from_shells(s["shells"]), s["charge"], s["mass"],
                           s["n_particles"], s["kappa"], s["eta"], s["particles_fraction"],
                           s["is_electron"]))
+    inter = {}
+    for e in desc.get("interpotentials", []):
+        i, j = sorted(int(x) for x in e["species"])
+        inter[(i, j)] = (list(e["coefficients"]), list(e["exponents"]))
+    ext = {int(e["species"]): (list(e["coefficients"]), list(e["exponents"]), list(e["origins"]))
+           for e in desc.get("external_potentials", [])}
     return System(sp, np.array(desc["point_charges"], float),
-                  np.array(desc["point_positions"], float).reshape(-1, 3))
+                  np.array(desc["point_positions"], float).reshape(-1, 3), inter, ext)
 
 
 # ---------------------------------------------------------------------- SCF --
@@ -383,8 +469,11 @@ def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthrea
         V = potential(s.basis, system.point_charges, system.point_positions)
         # T / mass + (q) * V  -- puntual interaction scaled by the particle charge
         H.append(T / s.mass + s.charge * V)
+        if len(H) - 1 in system.external:
+            H[-1] = H[-1] + gaussian_potential(s.basis, *system.external[len(H) - 1])
         S.append(Sm)
         X.append(_orthogonaliser(Sm))
+    g12 = bool(system.interpotentials)
     # HCORE guess
     P, C, eps = [], [], []
     for i, s in enumerate(sp):
@@ -401,8 +490,10 @@ def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthrea
     for it in range(1, max_iter + 1):
         G, J = [], []
         for i, s in enumerate(sp):
-            if s.n_particles > 1:
+            if s.n_particles > 1 and not g12:
                 G.append(two_body_direct(s.basis, s.is_electron, P[i], s.exchange_factor, nthreads) * s.charge ** 2)
+            elif s.n_particles > 1 and (i, i) in system.interpotentials:
+                G.append(g12_direct(s.basis, P[i], s.exchange_factor, *system.interpotentials[(i, i)], nthreads))
             else:
                 G.append(np.zeros_like(H[i]))
             Ji = np.zeros_like(H[i])
@@ -410,7 +501,13 @@ def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthrea
             for j, o in enumerate(sp):
                 if j == i:
                     continue
-                B = coupling_direct(s.basis, i + 1, o.basis, j + 1, P[j], nthreads) * s.charge * o.charge
+                if not g12:
+                    B = coupling_direct(s.basis, i + 1, o.basis, j + 1, P[j], nthreads) * s.charge * o.charge
+                elif (min(i, j), max(i, j)) in system.interpotentials:
+                    B = g12inter_direct(s.basis, i + 1, o.basis, j + 1, P[j],
+                                        *system.interpotentials[(min(i, j), max(i, j))], nthreads)
+                else:
+                    B = np.zeros((s.basis.nbf, s.basis.nbf))
                 B = np.tril(B) + np.tril(B, -1).T  # row-major lower == Fortran upper
                 Jparts[j] = B
                 Ji += B

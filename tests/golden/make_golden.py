@@ -21,7 +21,13 @@ It extracts, as data:
     DZSPDN proton) and ``test/H.APMO.READCOEFF`` (one electron, cc-pVDZ, DZSNB
     proton) with their bases (only the SCF energy of these checkers is used),
   * ``test/HF.APMO`` (HF with cc-pVTZ electrons, f shell on F, and a DZSPDN
-    quantum proton): geometry, bases and the checker's HF and MP2 energies.
+    quantum proton): geometry, bases and the checker's HF and MP2 energies,
+  * the G12 tests ``test/TIP4P-dimer-{singlet,triplet}-direct`` (two quantum
+    protons of a TIP4P water dimer under fitted Gaussian potentials): the
+    geometry (bohr, ``units="BOHRS"``) with charges and masses, the charge of
+    the point particle N0 from ``lib/dataBases/elementalParticles.lib``, the
+    input's own BASIS block, its POTENTIAL blocks, the EXTERPOTENTIAL /
+    INTERPOTENTIAL assignments and the checkers' values.
 The GPU machine has no reference tree, so the tests read only the JSON written here.
 """
 import json
@@ -80,6 +86,86 @@ def read_geometry(name):
     return rows
 
 
+def particle_charge(symbol):
+    """CHARGE of a &PARTICLE entry of lib/dataBases/elementalParticles.lib."""
+    txt = open(os.path.join(ROOT, "lib", "dataBases", "elementalParticles.lib")).read()
+    for blk in txt.split("&PARTICLE")[1:]:
+        m = re.search(r'SYMBOL\s*=\s*"([^"]+)"', blk)
+        if m and m.group(1) == symbol:
+            return float(re.search(r"CHARGE\s*=\s*([-0-9.Ee+]+)", blk).group(1))
+    raise KeyError(symbol)
+
+
+def read_block(txt, head, tail):
+    return txt.split(head, 1)[1].split(tail, 1)[0]
+
+
+def read_g12_input(name):
+    """One TIP4P-style input: particles, inline basis, Gaussian potentials.
+
+    A POTENTIAL block holds, per 'O-<key>' entry, a component count, then per
+    component an 'id l' line, an 'exponent coefficient' line and an origin line
+    (the reader is src/core/GTFPotential.f90:155-307; it sets every
+    component to l = 0 and interpotential origins to zero)."""
+    txt = open(os.path.join(ROOT, "test", name + ".lowdin")).read()
+    units = re.search(r'units\s*=\s*"([A-Za-z]+)"', txt)
+    scale = 1.0 if units and units.group(1).upper().startswith("BOHR") else 1.0 / BOHR
+    particles = []
+    for ln in read_block(txt, "GEOMETRY", "END GEOMETRY").strip().splitlines():
+        t = ln.split()
+        if len(t) < 5:
+            continue
+        rec = {"particle": t[0], "basis": t[1], "position_bohr": [float(x) * scale for x in t[2:5]]}
+        m = re.search(r"(?<![A-Za-z])q\s*=\s*([-0-9.Ee+]+)", ln)
+        rec["charge"] = float(m.group(1)) if m else particle_charge(t[0])
+        m = re.search(r"(?<![A-Za-z])m\s*=\s*([0-9.Ee+-]+)", ln)
+        if m:
+            rec["mass"] = float(m.group(1))
+        particles.append(rec)
+    basis = {}
+    lines = read_block(txt, "\nBASIS ", "END BASIS").splitlines()
+    for i, ln in enumerate(lines):
+        m = re.match(r"^O-\S+\s+(\S+)\s+\(", ln.strip())
+        if not m:
+            continue
+        j = i + 1
+        nsh = int(lines[j].split()[0]); j += 1
+        shells = []
+        for _ in range(nsh):
+            _, l, npr = (int(x) for x in lines[j].split()[:3]); j += 1
+            ex, co = [], []
+            for _ in range(npr):
+                a, c = lines[j].split()[:2]; j += 1
+                ex.append(float(a)); co.append(float(c))
+            shells.append({"l": l, "exponents": ex, "coefficients": co})
+        basis[m.group(1)] = shells
+    potentials = {}
+    for blk in txt.split("\nPOTENTIAL ")[1:]:
+        lines = [x.strip() for x in blk.split("END POTENTIAL")[0].splitlines()]
+        entries, i = {}, 1
+        while i < len(lines):
+            if lines[i].startswith("O-"):
+                key, n = lines[i][2:], int(lines[i + 1].split()[0])
+                comps, j = [], i + 2
+                for _ in range(n):
+                    l = int(lines[j].split()[1])
+                    g, c = (float(x) for x in lines[j + 1].split()[:2])
+                    origin = [float(x) for x in lines[j + 2].split()[:3]]
+                    comps.append({"l": l, "exponent": g, "coefficient": c, "origin": origin})
+                    j += 3
+                entries[key] = comps
+                i = j
+            else:
+                i += 1
+        potentials[lines[0]] = entries
+    ext = [ln.split() for ln in read_block(txt, "EXTERPOTENTIAL", "END EXTERPOTENTIAL").strip().splitlines()]
+    inter = [ln.split() for ln in read_block(txt, "INTERPOTENTIAL", "END INTERPOTENTIAL").strip().splitlines()]
+    method = re.search(r'method\s*=\s*"([^"]+)"', txt).group(1)
+    return {"particles": particles, "basis": basis, "potentials": potentials, "method": method,
+            "external": [{"species": e[0], "potential": e[1]} for e in ext if len(e) == 2],
+            "inter": [{"species": [e[0], e[1]], "potential": e[2]} for e in inter if len(e) == 3]}
+
+
 def read_checker(name):
     txt = open(os.path.join(ROOT, "test", name)).read()
     vals = {}
@@ -128,6 +214,12 @@ def main():
             "H3+.FCI": read_checker("H3+.FCI.py"),
             "H.APMO.READCOEFF": read_checker("H.APMO.READCOEFF.py"),
             "HF.APMO": read_checker("HF.APMO.py"),
+            "TIP4P-dimer-singlet-direct": read_checker("TIP4P-dimer-singlet-direct.py"),
+            "TIP4P-dimer-triplet-direct": read_checker("TIP4P-dimer-triplet-direct.py"),
+        },
+        "g12_inputs": {
+            "TIP4P-dimer-singlet-direct": read_g12_input("TIP4P-dimer-singlet-direct"),
+            "TIP4P-dimer-triplet-direct": read_g12_input("TIP4P-dimer-triplet-direct"),
         },
     }
     with open(OUT, "w") as f:

@@ -1,4 +1,6 @@
 """Systems of the reference's golden tests, built from tests/golden/golden.json."""
+import numpy as np
+
 from openlowdin_gb300 import systems as S
 
 
@@ -91,3 +93,65 @@ def hf_apmo(golden):
             prot.append(S.proton_species(_shells(golden, "DZSPDN:H_1", r["position_bohr"]), 1, name=part.upper()))
     return {"species": [S.electron_species(shells, 10)] + prot, "point_charges": Z, "point_positions": R,
             "name": "HF.APMO"}
+
+
+def g12_system(golden, test):
+    """A TIP4P-style input of the reference (test/TIP4P-dimer-*-direct): one
+    quantum species per particle name with a basis (UHF: kappa = -1, eta = 1,
+    one particle per orbital), the 'dirac' rows as point charges, the
+    EXTERPOTENTIAL entries as external potentials and the INTERPOTENTIAL
+    entries as G12 pair potentials."""
+    inp = golden["g12_inputs"][test]
+    assert inp["method"] == "UHF"
+    names, rows, Z, R = [], {}, [], []
+    for r in inp["particles"]:
+        if r["basis"] == "dirac":
+            Z.append(r["charge"]); R.append(r["position_bohr"])
+            continue
+        if r["particle"] not in rows:
+            names.append(r["particle"]); rows[r["particle"]] = []
+        rows[r["particle"]].append(r)
+    species = []
+    for nm in names:
+        shells = []
+        for r in rows[nm]:
+            shells += [(s["l"], s["exponents"], s["coefficients"], list(r["position_bohr"])) for s in inp["basis"][nm]]
+        r0 = rows[nm][0]
+        species.append({"name": nm, "charge": r0["charge"], "mass": r0["mass"], "n_particles": len(rows[nm]),
+                        "kappa": -1.0, "eta": 1.0, "particles_fraction": 1.0, "is_electron": False,
+                        "shells": shells})
+
+    def comps(pot, key):
+        c = inp["potentials"][pot][key]
+        assert all(x["l"] == 0 for x in c)
+        return [x["coefficient"] for x in c], [x["exponent"] for x in c], [x["origin"] for x in c]
+
+    ext = []
+    for e in inp["external"]:
+        c, g, o = comps(e["potential"], e["species"])
+        ext.append({"species": names.index(e["species"]), "coefficients": c, "exponents": g, "origins": o})
+    inter = []
+    for e in inp["inter"]:
+        a, b = e["species"]
+        key = a + b if a + b in inp["potentials"][e["potential"]] else b + a
+        c, g, _ = comps(e["potential"], key)
+        inter.append({"species": [names.index(a), names.index(b)], "coefficients": c, "exponents": g})
+    return {"species": species, "point_charges": Z, "point_positions": R, "external_potentials": ext,
+            "interpotentials": inter, "name": test}
+
+
+def g12_components(P, names, sysd, Vext, Vfix, Ginter, Gintra_coulomb, Gintra):
+    """The energy components the TIP4P checkers read, from converged densities:
+    'X Ext Pot' tr P V_ext, 'X/Fixed interact.' tr P q V_fixed, 'X/Y Hartree'
+    tr P_X J_XY, and for a species with two particles 'X/X Hartree'
+    tr P J[P] / 2 and 'X Exchange' tr P (G - J[P]) / 2."""
+    out = {}
+    for i, nm in enumerate(names):
+        out[f"{nm} Ext Pot"] = float(np.sum(P[i] * Vext[i]))
+        out[f"{nm}/Fixed interact."] = float(np.sum(P[i] * Vfix[i]))
+        if Gintra[i] is not None:
+            out[f"{nm}/{nm} Hartree"] = 0.5 * float(np.sum(P[i] * Gintra_coulomb[i]))
+            out[f"{nm} Exchange"] = 0.5 * float(np.sum(P[i] * (Gintra[i] - Gintra_coulomb[i])))
+    for (i, j), B in Ginter.items():
+        out[f"{names[i]}/{names[j]} Hartree"] = float(np.sum(P[i] * B))
+    return out

@@ -102,3 +102,51 @@ def test_g12_rejects_bad_potentials(L):
     G = h.compute_g12_direct(D, -0.5, [1.0], [0.5])
     assert np.all(np.isfinite(G))
     h.close()
+
+
+@pytest.mark.parametrize("test", ["TIP4P-dimer-singlet-direct", "TIP4P-dimer-triplet-direct"])
+def test_tip4p_golden_through_host_scf(L, oracle, golden, test):
+    """test/TIP4P-dimer-*-direct end to end through the reference-shaped host
+    calls (HostSCF: external potential, G12 intra- and inter-species matrices
+    on the device each iteration): the checker's HF energy (1e-8) and energy
+    components (1e-4), the G12 matrices at the converged densities against the
+    oracle (1e-10), and the energy against the oracle SCF.  The triplet runs a
+    fixed 200 iterations (its energy is flat to 1e-10 long before its density
+    settles); the singlet converges."""
+    from openlowdin_gb300 import scf
+    from tests import golden_systems as GS
+    from tests.test_g12_golden import _components
+    sysd = GS.g12_system(golden, test)
+    singlet = "singlet" in test
+    s = scf.HostSCF(sysd)
+    r = s.solve(tol_energy=1e-12, tol_density=1e-9 if singlet else 0.0, max_iter=60 if singlet else 200)
+    sy = oracle.from_plain(sysd)
+    for i, (h, sp) in enumerate(zip(s.handles, sy.species)):
+        pot = sy.interpotentials.get((i, i))
+        if sp.n_particles > 1 and pot:
+            G = h.compute_g12_direct(r.densities[i], sp.exchange_factor, *pot)
+            assert np.max(np.abs(G - oracle.g12_direct(sp.basis, r.densities[i], sp.exchange_factor, *pot))) < TOL
+        for j, o in enumerate(sy.species):
+            pot = sy.interpotentials.get((min(i, j), max(i, j)))
+            if j != i and pot:
+                B = h.compute_g12inter_direct(s.handles[j], r.densities[j], *pot)
+                ref = oracle.g12inter_direct(sp.basis, i + 1, o.basis, j + 1, r.densities[j], *pot)
+                assert np.max(np.abs(np.tril(B) - np.tril(ref))) < TOL
+    s.close()
+    if singlet:
+        assert r.converged
+    ref = golden["values"][test]
+    assert abs(r.energy - ref["HF energy"][0]) <= ref["HF energy"][1], r.energy
+    res = oracle.scf(sy, tol_energy=1e-12, tol_density=1e-9 if singlet else 0.0, max_iter=60 if singlet else 200)
+    assert abs(r.energy - res.energy) < 1e-10
+    res.densities = r.densities
+    for j in range(len(sy.species)):
+        for k in list(res.coupling[j][1]):
+            b = sy.species[j].basis
+            pot = sy.interpotentials.get((min(j, k), max(j, k)))
+            B = oracle.g12inter_direct(b, j + 1, sy.species[k].basis, k + 1, r.densities[k], *pot)
+            res.coupling[j][1][k] = np.tril(B) + np.tril(B, -1).T
+    comps = _components(oracle, sysd, res)
+    for key, (val, tol) in ref.items():
+        if key != "HF energy":
+            assert abs(comps[key] - val) <= tol, (key, comps[key], val)
