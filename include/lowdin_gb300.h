@@ -273,9 +273,10 @@ int LowdinGB300_batch_coupling_quartets(LowdinGB300_Batch *b, long long *out, vo
    Cartesian functions, 512 shells and shells up to d (f shells need global
    work arrays for some classes); others are rejected with an error.
    The handle must have been set up with LibintInterface_init_2body_ints (which
-   does allocate).  The first call on a device looks up the array's device
-   address (cudaGetSymbolAddress): make that first call before any stream
-   capture.  Every call shares the array and clears what it accumulates; calls
+   does allocate).  The call uploads its task list from host memory that
+   lives only for the call, so it must not be recorded into a CUDA graph
+   (stream capture); it queues ordinary work on `stream`.  Every call shares
+   the array and clears what it accumulates; calls
    whose work overlaps on the GPU (other streams, other handles) race.
    Returns 0, or -1 with LowdinGB300_last_error() set. */
 size_t LowdinGB300_noalloc_scratch_bytes(void);
