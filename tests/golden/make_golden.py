@@ -22,6 +22,10 @@ It extracts, as data:
     proton) with their bases (only the SCF energy of these checkers is used),
   * ``test/HF.APMO`` (HF with cc-pVTZ electrons, f shell on F, and a DZSPDN
     quantum proton): geometry, bases and the checker's HF and MP2 energies,
+  * the UHF inputs ``test/H2.APMO.UEN`` (cc-pVTZ electrons, NAKAI-3-SPD
+    protons) and ``test/H2O.BOA.UEN`` (6-311++G** electrons): geometry, bases
+    and the checkers' HF and MP2 energies (their Epstein-Nesbet values are
+    not used),
   * the G12 tests ``test/TIP4P-dimer-{singlet,triplet}-direct`` (two quantum
     protons of a TIP4P water dimer under fitted Gaussian potentials): the
     geometry (bohr, ``units="BOHRS"``) with charges and masses, the charge of
@@ -195,6 +199,9 @@ def main():
             "DZSPDN:H_1": read_basis("DZSPDN", "HYDROGEN", "H_1"),
             "CC-PVTZ:F": read_basis("CC-PVTZ", "FLUORINE", "F"),
             "CC-PVTZ:H": read_basis("CC-PVTZ", "HYDROGEN", "H"),
+            "NAKAI-3-SPD:H_1": read_basis("NAKAI-3-SPD", "HYDROGEN_1", "H_1"),
+            "6-311++G.D.P:H": read_basis("6-311++G.D.P", "HYDROGEN", "H"),
+            "6-311++G.D.P:O": read_basis("6-311++G.D.P", "OXYGEN", "O"),
         },
         "geometry": {
             "H2O.BOA.DIRECT": read_geometry("H2O.BOA.DIRECT.lowdin"),
@@ -203,6 +210,8 @@ def main():
             "H3+.FCI": read_geometry("H3+.FCI.lowdin"),
             "H.APMO.READCOEFF": read_geometry("H.APMO.READCOEFF.lowdin"),
             "HF.APMO": read_geometry("HF.APMO.lowdin"),
+            "H2.APMO.UEN": read_geometry("H2.APMO.UEN.lowdin"),
+            "H2O.BOA.UEN": read_geometry("H2O.BOA.UEN.lowdin"),
         },
         "values": {
             "H2O.BOA.DIRECT": read_checker("H2O.BOA.DIRECT.py"),
@@ -214,6 +223,8 @@ def main():
             "H3+.FCI": read_checker("H3+.FCI.py"),
             "H.APMO.READCOEFF": read_checker("H.APMO.READCOEFF.py"),
             "HF.APMO": read_checker("HF.APMO.py"),
+            "H2.APMO.UEN": read_checker("H2.APMO.UEN.py"),
+            "H2O.BOA.UEN": read_checker("H2O.BOA.UEN.py"),
             "TIP4P-dimer-singlet-direct": read_checker("TIP4P-dimer-singlet-direct.py"),
             "TIP4P-dimer-triplet-direct": read_checker("TIP4P-dimer-triplet-direct.py"),
         },

@@ -4,7 +4,7 @@ against the reference's golden energies (tests/golden/golden.json)."""
 import pytest
 
 from tests import golden_systems as GS
-from tests.test_oracle import UHF_CASES
+from tests.test_oracle import UEN_CASES, UHF_CASES, closed_shell_twin
 
 pytestmark = pytest.mark.gpu
 
@@ -42,3 +42,24 @@ def test_h2o_apmo_uhf_golden_plain_and_mixed(scf, golden):
     rm = s.solve(tol_energy=1e-11, tol_density=1e-9)
     s.close()
     assert rm.converged and abs(rm.energy - r.energy) <= 1e-6
+
+
+@pytest.mark.parametrize("case", UEN_CASES, ids=[c[0] for c in UEN_CASES])
+def test_uen_mp2_golden(scf, oracle, golden, case):
+    """test/H2.APMO.UEN and test/H2O.BOA.UEN: closed-shell UHF solutions, so
+    the checkers' UMP2 energies are the closed-shell (APMO-)MP2 totals: the
+    device SCF of the merged electron species, then the device transform
+    (intra-species and every species pair) against the golden MP2 (1e-5)."""
+    from openlowdin_gb300 import lint
+    from tests.test_gpu_mp2 import _apmo_device_mp2
+    test, ebas, pbas = case
+    sysd = closed_shell_twin(GS.uhf_system(golden, test, ebas, pbas))
+    s = scf.DeviceSCF(sysd)
+    r = s.solve(tol_energy=1e-11, tol_density=1e-9)
+    s.close()
+    res = oracle.scf(oracle.from_plain(sysd), tol_energy=1e-11, tol_density=1e-9)
+    assert r.converged and abs(r.energy - res.energy) < 1e-9
+    assert abs(r.energy - golden["values"][test]["HF energy"][0]) <= 1e-8
+    total = res.energy + sum(_apmo_device_mp2(lint, sysd, res, 0).values())
+    ref = golden["values"][test]["MP2 energy"]
+    assert abs(total - ref[0]) <= ref[1], total

@@ -211,9 +211,14 @@ def test_golden_alphabeta_repulsion(oracle, golden):
 # default |dE| < 1e-8 (src/core/CONTROL.f90:1119) on a slowly converging
 # triplet; the fully converged energy lies 2.3e-8 Eh below its printed value
 # (lower, as the variational principle requires), hence 3e-8 there.
+# H2.APMO.UEN (closed-shell H2, cc-pVTZ electrons, NAKAI-3-SPD protons) lands
+# 9.9e-9 below the printed value, inside the checker's 1e-8; H2O.BOA.UEN
+# (6-311++G**) 5.2e-10 below it.
 UHF_CASES = [("H.APMO.READCOEFF", "CC-PVDZ", "DZSNB", 1e-8),
              ("H3+.FCI", "6-31G.D.P", "DZSPDN", 1e-8),
-             ("HOO+.ROCI-HF", "CC-PVDZ", "DZSPNB", 3e-8)]
+             ("HOO+.ROCI-HF", "CC-PVDZ", "DZSPNB", 3e-8),
+             ("H2.APMO.UEN", "CC-PVTZ", "NAKAI-3-SPD", 1e-8),
+             ("H2O.BOA.UEN", "6-311++G.D.P", None, 1e-8)]
 
 
 @pytest.mark.parametrize("case", UHF_CASES, ids=[c[0] for c in UHF_CASES])
@@ -225,6 +230,35 @@ def test_golden_uhf_energies(oracle, golden, case):
     res = oracle.scf(oracle.from_plain(sysd), tol_energy=1e-11, tol_density=1e-9, max_iter=300)
     assert res.converged
     assert abs(res.energy - golden["values"][test]["HF energy"][0]) <= tol
+
+
+UEN_CASES = [("H2.APMO.UEN", "CC-PVTZ", "NAKAI-3-SPD"), ("H2O.BOA.UEN", "6-311++G.D.P", None)]
+
+
+def closed_shell_twin(sysd):
+    """The RHF system of a closed-shell UHF system: E-ALPHA and E-BETA merged
+    back into one electron species."""
+    sp = sysd["species"]
+    assert sp[0]["name"] == "E-ALPHA" and sp[1]["name"] == "E-BETA"
+    assert sp[0]["n_particles"] == sp[1]["n_particles"]
+    return dict(sysd, species=[S.electron_species(sp[0]["shells"], 2 * sp[0]["n_particles"])] + sp[2:])
+
+
+@pytest.mark.parametrize("case", UEN_CASES, ids=[c[0] for c in UEN_CASES])
+def test_golden_uen_mp2(oracle, golden, case):
+    """test/H2.APMO.UEN and test/H2O.BOA.UEN: their UHF solutions are closed
+    shell (the UHF energy equals the RHF energy of the merged species), so the
+    UMP2 total is the closed-shell (APMO-)MP2 sum; against the checkers' MP2
+    energies (1e-5)."""
+    test, ebas, pbas = case
+    sysd = GS.uhf_system(golden, test, ebas, pbas)
+    ru = oracle.scf(oracle.from_plain(sysd), tol_energy=1e-11, tol_density=1e-9, max_iter=300)
+    sysO = oracle.from_plain(closed_shell_twin(sysd))
+    res = oracle.scf(sysO, tol_energy=1e-11, tol_density=1e-9)
+    assert ru.converged and res.converged and abs(ru.energy - res.energy) < 1e-10
+    total = oracle.apmo_mp2(sysO, res)["total"]
+    ref = golden["values"][test]["MP2 energy"]
+    assert abs(total - ref[0]) <= ref[1], total
 
 
 def test_golden_h2o_apmo_uhf(oracle, golden):
