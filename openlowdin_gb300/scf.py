@@ -107,6 +107,28 @@ def interpotentials(sysd) -> dict:
     return out
 
 
+DOUBLE_ZERO = 1e-12
+
+
+def damped_fock(F, P, kept):
+    """The reference's default convergence method (CONVERGENCE_METHOD 1,
+    src/scf/Convergence.f90:444-511) for one species: the kept pair
+    (F0, P0) starts as the first Fock matrix and density; with
+    dE = -tr(F0 (P - P0)) / 2 and dEF = tr((F - F0)(P - P0)), the step is
+    undamped (the pair becomes (F, P)) when dEF <= dE or |dEF| < 1e-12,
+    otherwise F0 and P0 move by dE / dEF towards F and P and F0 is the matrix
+    diagonalised.  Returns (matrix to diagonalise, new kept pair)."""
+    F0, P0 = kept
+    dP = P - P0
+    dE = -0.5 * float(np.vdot(F0, dP.T))
+    dEF = float(np.vdot(F - F0, dP.T))
+    if dEF <= dE or abs(dEF) < DOUBLE_ZERO:
+        return F, (F.copy(), P.copy())
+    w = dE / dEF
+    F0 = F0 + w * (F - F0)
+    return F0, (F0, P0 + w * (P - P0))
+
+
 def coulomb_only(sysd, who: str) -> None:
     """Raise unless the system has only Coulomb interactions: drivers that keep
     no Gaussian-fit potential path must not drop one silently."""
@@ -213,15 +235,24 @@ class HostSCF:
     the solve continues in FP64 with a fresh DIIS history.  Couplings stay
     FP64 full builds.
 
+    convergence: "diis" (Pulay over all species, the reference's method 2) or
+    "damping" (its default method 1, damped_fock); damping is slower but
+    follows the reference to its stationary point where DIIS can jump to
+    another one (species of several protons, for instance).
+
     Gaussian-fit potentials: sysd["external_potentials"], a list of
     {"species": i, "coefficients", "exponents", "origins"}, are added to H_i
     (LowdinGB300_gaussian_potential); sysd["interpotentials"] switches every
     species pair to G12 matrices (libintinterface_compute_g12_direct /
     _g12inter_direct, FP64 full builds)."""
 
-    def __init__(self, sysd, precision="fp64", split=1e-5, guard_energy=1e-6, guard_commutator=1e-4):
+    def __init__(self, sysd, precision="fp64", split=1e-5, guard_energy=1e-6, guard_commutator=1e-4,
+                 convergence="diis"):
         if precision not in ("fp64", "mixed"):
             raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
+        if convergence not in ("diis", "damping"):
+            raise ValueError(f"convergence must be 'diis' or 'damping', not {convergence!r}")
+        self.convergence = convergence
         self.sysd = sysd
         self.species = sysd["species"]
         self.precision, self.split = precision, split
@@ -266,6 +297,7 @@ class HostSCF:
             P.append(sp[i]["eta"] * Ci[:, :o] @ Ci[:, :o].T)
         Pref, Gprev = [None] * ns, [None] * ns
         diis = _DIIS(np)
+        kept = None
         e_old, converged, it, quartets = None, False, 0, 0
         energy = 0.0
         for it in range(1, max_iter + 1):
@@ -324,8 +356,16 @@ class HostSCF:
                     converged = True
                     break
                 guard_hit = True                  # continue in FP64 from this build
-                diis, e_old = _DIIS(np), None
-            Fx = diis(F, errs)
+                diis, e_old, kept = _DIIS(np), None, None
+            if self.convergence == "diis":
+                Fx = diis(F, errs)
+            else:
+                if kept is None:
+                    kept = [(F[i].copy(), P[i].copy()) for i in range(ns)]
+                Fx = []
+                for i in range(ns):
+                    Fd, kept[i] = damped_fock(F[i], P[i], kept[i])
+                    Fx.append(Fd)
             dmax = 0.0
             newP = []
             for i in range(ns):

@@ -23,7 +23,8 @@ restated from the Fortran program:
   EXTERPOTENTIAL adds sum_k c_k exp(-g_k |r - C_k|^2) to H
   (``src/ints/DirectIntegralManager.f90:848-949``),
 * iteration scheme 3 -- every species once per global iteration
-  (``src/scf/MultiSCF.f90:276-440``) with Pulay DIIS (``src/scf/Convergence.f90``),
+  (``src/scf/MultiSCF.f90:276-440``) with Pulay DIIS or the reference's
+  default damping (``src/scf/Convergence.f90:382-511``),
 * closed-shell MP2 from (ia|jb) (``src/MBPT/MPFunctions.f90:514-662``).
 """
 from __future__ import annotations
@@ -458,9 +459,36 @@ class DIIS:
         return [sum(c[i] * self.F[i][k] for i in range(m)) for k in range(len(Fs))]
 
 
+DOUBLE_ZERO_THRESHOLD = 1e-12   # src/core/CONTROL.f90:1592
+
+
+def damping_step(F, P, F0, P0):
+    """One species' step of the reference's default convergence method
+    (CONVERGENCE_METHOD 1, Convergence_dampingMethod,
+    src/scf/Convergence.f90:444-511): with the kept pair (F0, P0),
+    d = -tr(F0 (P - P0)) / 2 and f = tr((F - F0)(P - P0)); when f <= d or
+    |f| < 1e-12 the pair becomes (F, P) and F is used undamped, otherwise
+    lambda = d / f moves F0 and P0 by lambda towards F and P and the damped F0
+    is diagonalised.  Returns (Fock to diagonalise, F0, P0)."""
+    dP = P - P0
+    d = -0.5 * float(np.sum(F0 * dP.T))
+    f = float(np.sum((F - F0) * dP.T))
+    if f <= d or abs(f) < DOUBLE_ZERO_THRESHOLD:
+        return F, F.copy(), P.copy()
+    lam = d / f
+    F0 = F0 + lam * (F - F0)
+    return F0.copy(), F0, P0 + lam * (P - P0)
+
+
 def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthreads=None,
-        diis=True, verbose=False) -> SCFResult:
-    """Multi-species Hartree-Fock, iteration scheme 3, restated from src/scf."""
+        convergence="diis", verbose=False) -> SCFResult:
+    """Multi-species Hartree-Fock, iteration scheme 3, restated from src/scf.
+
+    convergence: "diis" (Pulay, CONVERGENCE_METHOD 2), "damping" (the
+    reference's default, CONVERGENCE_METHOD 1; the kept pair starts from the
+    first Fock build, src/scf/MultiSCF.f90:330-336) or "none"."""
+    if convergence not in ("diis", "damping", "none"):
+        raise ValueError(f"unknown convergence method {convergence!r}")
     sp = system.species
     ns = len(sp)
     H, X, S = [], [], []
@@ -484,6 +512,7 @@ def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthrea
         P.append(s.eta * Ci[:, :s.n_occ] @ Ci[:, :s.n_occ].T)
     enuc = system.nuclear_repulsion()
     diis_obj = DIIS()
+    kept = None
     e_old = None
     converged = False
     it = 0
@@ -522,9 +551,17 @@ def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthrea
         newP = []
         dmax = 0.0
         Fx = F
-        if diis:
+        if convergence == "diis":
             errs = [X[i].T @ (F[i] @ P[i] @ S[i] - S[i] @ P[i] @ F[i]) @ X[i] for i in range(ns)]
             Fx = diis_obj(F, errs)
+        elif convergence == "damping":
+            if kept is None:
+                kept = [(F[i].copy(), P[i].copy()) for i in range(ns)]
+            Fx = []
+            for i in range(ns):
+                Fd, F0, P0 = damping_step(F[i], P[i], *kept[i])
+                kept[i] = (F0, P0)
+                Fx.append(Fd)
         for i, s in enumerate(sp):
             Fi = Fx[i]
             e, Cp = np.linalg.eigh(X[i].T @ Fi @ X[i])

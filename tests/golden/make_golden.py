@@ -22,6 +22,12 @@ It extracts, as data:
     proton) with their bases (only the SCF energy of these checkers is used),
   * ``test/HF.APMO`` (HF with cc-pVTZ electrons, f shell on F, and a DZSPDN
     quantum proton): geometry, bases and the checker's HF and MP2 energies,
+  * ``test/H2O.APMO.iter0``-``iter3`` (6-31G electrons, one species of two
+    NAKAI-3-SP protons), ``test/PsH.P3`` (UHF electrons of H^- with cc-pVTZ, a
+    positron species) and ``test/He.POTENTIALS`` (UHF He electrons whose
+    nucleus is the fitted external potential HEE and whose electron-electron
+    interaction is the G12 potential EE, both from ``lib/potentials``):
+    geometries, bases, potentials and the checkers' HF energies,
   * the UHF inputs ``test/H2.APMO.UEN`` (cc-pVTZ electrons, NAKAI-3-SPD
     protons) and ``test/H2O.BOA.UEN`` (6-311++G** electrons): geometry, bases
     and the checkers' HF and MP2 energies (their Epstein-Nesbet values are
@@ -145,29 +151,51 @@ def read_g12_input(name):
         basis[m.group(1)] = shells
     potentials = {}
     for blk in txt.split("\nPOTENTIAL ")[1:]:
-        lines = [x.strip() for x in blk.split("END POTENTIAL")[0].splitlines()]
-        entries, i = {}, 1
-        while i < len(lines):
-            if lines[i].startswith("O-"):
-                key, n = lines[i][2:], int(lines[i + 1].split()[0])
-                comps, j = [], i + 2
-                for _ in range(n):
-                    l = int(lines[j].split()[1])
-                    g, c = (float(x) for x in lines[j + 1].split()[:2])
-                    origin = [float(x) for x in lines[j + 2].split()[:3]]
-                    comps.append({"l": l, "exponent": g, "coefficient": c, "origin": origin})
-                    j += 3
-                entries[key] = comps
-                i = j
-            else:
-                i += 1
-        potentials[lines[0]] = entries
+        lines = blk.split("END POTENTIAL")[0].splitlines()
+        potentials[lines[0].strip()] = potential_entries(lines[1:])
+    return dict(read_assignments(txt), particles=particles, basis=basis, potentials=potentials)
+
+
+def read_assignments(txt):
+    """method and the EXTERPOTENTIAL / INTERPOTENTIAL blocks of an input."""
     ext = [ln.split() for ln in read_block(txt, "EXTERPOTENTIAL", "END EXTERPOTENTIAL").strip().splitlines()]
     inter = [ln.split() for ln in read_block(txt, "INTERPOTENTIAL", "END INTERPOTENTIAL").strip().splitlines()]
     method = re.search(r'method\s*=\s*"([^"]+)"', txt).group(1)
-    return {"particles": particles, "basis": basis, "potentials": potentials, "method": method,
+    return {"method": method,
             "external": [{"species": e[0], "potential": e[1]} for e in ext if len(e) == 2],
             "inter": [{"species": [e[0], e[1]], "potential": e[2]} for e in inter if len(e) == 3]}
+
+
+def potential_entries(lines, keys=None):
+    """{key: components} of the 'O-<key>' entries in the lines of a potential
+    (an input's POTENTIAL block or a lib/potentials file); '#' lines after the
+    key are comments, as the reader skips them."""
+    lines = [x.strip() for x in lines]
+    entries, i = {}, 0
+    while i < len(lines):
+        if not lines[i].startswith("O-"):
+            i += 1
+            continue
+        key, j = lines[i][2:], i + 1
+        while lines[j].startswith("#"):
+            j += 1
+        n, j = int(lines[j].split()[0]), j + 1
+        comps = []
+        for _ in range(n):
+            l = int(lines[j].split()[1])
+            g, c = (float(x) for x in lines[j + 1].split()[:2])
+            origin = [float(x) for x in lines[j + 2].split()[:3]]
+            comps.append({"l": l, "exponent": g, "coefficient": c, "origin": origin})
+            j += 3
+        if keys is None or key in keys:
+            entries[key] = comps
+        i = j
+    return entries
+
+
+def read_potential_file(name, keys):
+    """The given entries of lib/potentials/<name>."""
+    return potential_entries(open(os.path.join(ROOT, "lib", "potentials", name)).read().splitlines(), keys)
 
 
 def read_checker(name):
@@ -200,6 +228,11 @@ def main():
             "CC-PVTZ:F": read_basis("CC-PVTZ", "FLUORINE", "F"),
             "CC-PVTZ:H": read_basis("CC-PVTZ", "HYDROGEN", "H"),
             "NAKAI-3-SPD:H_1": read_basis("NAKAI-3-SPD", "HYDROGEN_1", "H_1"),
+            "NAKAI-3-SP:H_1": read_basis("NAKAI-3-SP", "HYDROGEN_1", "H_1"),
+            "6-31G:H": read_basis("6-31G", "HYDROGEN", "H"),
+            "6-31G:O": read_basis("6-31G", "OXYGEN", "O"),
+            "6-31G:He": read_basis("6-31G", "HELIUM", "HE"),
+            "E+-H-7SP-AUG-CC-PVTZ:E+": read_basis("E+-H-7SP-AUG-CC-PVTZ", "POSITRON", "E+"),
             "6-311++G.D.P:H": read_basis("6-311++G.D.P", "HYDROGEN", "H"),
             "6-311++G.D.P:O": read_basis("6-311++G.D.P", "OXYGEN", "O"),
         },
@@ -212,6 +245,9 @@ def main():
             "HF.APMO": read_geometry("HF.APMO.lowdin"),
             "H2.APMO.UEN": read_geometry("H2.APMO.UEN.lowdin"),
             "H2O.BOA.UEN": read_geometry("H2O.BOA.UEN.lowdin"),
+            "H2O.APMO.iter0": read_geometry("H2O.APMO.iter0.lowdin"),
+            "PsH.P3": read_geometry("PsH.P3.lowdin"),
+            "He.POTENTIALS": read_geometry("He.POTENTIALS.lowdin"),
         },
         "values": {
             "H2O.BOA.DIRECT": read_checker("H2O.BOA.DIRECT.py"),
@@ -225,12 +261,22 @@ def main():
             "HF.APMO": read_checker("HF.APMO.py"),
             "H2.APMO.UEN": read_checker("H2.APMO.UEN.py"),
             "H2O.BOA.UEN": read_checker("H2O.BOA.UEN.py"),
+            "H2O.APMO.iter0": read_checker("H2O.APMO.iter0.py"),
+            "H2O.APMO.iter1": read_checker("H2O.APMO.iter1.py"),
+            "H2O.APMO.iter2": read_checker("H2O.APMO.iter2.py"),
+            "H2O.APMO.iter3": read_checker("H2O.APMO.iter3.py"),
+            "PsH.P3": read_checker("PsH.P3.py"),
+            "He.POTENTIALS": read_checker("He.POTENTIALS.py"),
             "TIP4P-dimer-singlet-direct": read_checker("TIP4P-dimer-singlet-direct.py"),
             "TIP4P-dimer-triplet-direct": read_checker("TIP4P-dimer-triplet-direct.py"),
         },
         "g12_inputs": {
             "TIP4P-dimer-singlet-direct": read_g12_input("TIP4P-dimer-singlet-direct"),
             "TIP4P-dimer-triplet-direct": read_g12_input("TIP4P-dimer-triplet-direct"),
+            "He.POTENTIALS": dict(read_assignments(open(os.path.join(ROOT, "test", "He.POTENTIALS.lowdin")).read()),
+                                  potentials={"HEE": read_potential_file("HEE", ("E-ALPHA", "E-BETA")),
+                                              "EE": read_potential_file("EE", ("E-ALPHAE-ALPHA", "E-ALPHAE-BETA",
+                                                                               "E-BETAE-BETA"))}),
         },
     }
     with open(OUT, "w") as f:

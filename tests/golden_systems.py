@@ -155,3 +155,64 @@ def g12_components(P, names, sysd, Vext, Vfix, Ginter, Gintra_coulomb, Gintra):
     for (i, j), B in Ginter.items():
         out[f"{names[i]}/{names[j]} Hartree"] = float(np.sum(P[i] * B))
     return out
+
+
+def h2o_apmo_two_protons(golden):
+    """test/H2O.APMO.iter0-iter3: 6-31G electrons, classical O, both protons in
+    one species H_1 (two particles, NAKAI-3-SP, kappa = -1, eta = 1)."""
+    geo = golden["geometry"]["H2O.APMO.iter0"]
+    shells, Z, R, pshells = [], [], [], []
+    for r in geo:
+        part = r["particle"]
+        if part.startswith("e-"):
+            shells += _shells(golden, "6-31G:" + part[3:-1], r["position_bohr"])
+        elif r["basis"] == "dirac":
+            Z.append(_Z[part]); R.append(r["position_bohr"])
+        else:
+            pshells += _shells(golden, "NAKAI-3-SP:H_1", r["position_bohr"])
+    return {"species": [S.electron_species(shells, 10), S.proton_species(pshells, 2)], "point_charges": Z,
+            "point_positions": R, "name": "H2O.APMO.iter"}
+
+
+def psh(golden):
+    """test/PsH.P3: the two electrons of H^- (e-(H) with addParticles=1, UHF,
+    cc-pVTZ), the H nucleus as a point charge and one positron species
+    (charge +1, mass 1, kappa = -1, eta = 1; e+-H-7SP-aug-cc-pVTZ)."""
+    geo = golden["geometry"]["PsH.P3"]
+    e, nuc, pos = geo
+    electrons = S.uhf_electron_species(_shells(golden, "CC-PVTZ:H", e["position_bohr"]), 1 + e["add_particles"], 1)
+    positron = {"name": "E+", "charge": 1.0, "mass": 1.0, "n_particles": 1, "kappa": -1.0, "eta": 1.0,
+                "particles_fraction": 1.0, "is_electron": False,
+                "shells": _shells(golden, "E+-H-7SP-AUG-CC-PVTZ:E+", pos["position_bohr"])}
+    return {"species": electrons + [positron], "point_charges": [_Z[nuc["particle"]]],
+            "point_positions": [nuc["position_bohr"]], "name": "PsH.P3"}
+
+
+def he_potentials(golden):
+    """test/He.POTENTIALS: the two electrons of He (e-(He), 6-31G, UHF) with no
+    nucleus; the fitted potential HEE acts on each electron species
+    (EXTERPOTENTIAL) and the fitted EE replaces their Coulomb interaction
+    (INTERPOTENTIAL: G12 pair potentials)."""
+    r = golden["geometry"]["He.POTENTIALS"][0]
+    species = S.uhf_electron_species(_shells(golden, "6-31G:He", r["position_bohr"]), 2, 1)
+    names = [s["name"] for s in species]
+    inp = golden["g12_inputs"]["He.POTENTIALS"]
+    assert inp["method"] == "UHF"
+    pots = inp["potentials"]
+
+    def comps(pot, key):
+        c = pots[pot.upper()][key]
+        assert all(x["l"] == 0 for x in c)
+        return [x["coefficient"] for x in c], [x["exponent"] for x in c], [x["origin"] for x in c]
+
+    ext = []
+    for e in inp["external"]:
+        c, g, o = comps(e["potential"], e["species"])
+        ext.append({"species": names.index(e["species"]), "coefficients": c, "exponents": g, "origins": o})
+    inter = []
+    for e in inp["inter"]:
+        a, b = e["species"]
+        c, g, _ = comps(e["potential"], a + b)
+        inter.append({"species": [names.index(a), names.index(b)], "coefficients": c, "exponents": g})
+    return {"species": species, "point_charges": [], "point_positions": [], "external_potentials": ext,
+            "interpotentials": inter, "name": "He.POTENTIALS"}

@@ -9,6 +9,9 @@ each, coupled by the inter-species G12 matrix.  Triplet: one species with both
 protons, UHF, G = G12 Coulomb - G12 exchange.  The checkers assert the HF
 energy to 1e-8 and the energy components to 1e-4.
 
+test/He.POTENTIALS does the same for the two electrons of He: the fitted
+potential HEE is their nucleus and the fitted EE their interaction.
+
 The external-potential matrix is checked twice: the oracle's quadrature against
 the identity exp(-0 r^2) = 1 (the overlap) and the library's host recursion
 (LowdinGB300_gaussian_potential, no GPU work) against the oracle.
@@ -124,3 +127,12 @@ def test_oracle_reproduces_tip4p_golden(oracle, golden, test):
         for key, (val, _) in ref.items():
             if key != "HF energy":
                 assert abs(comps[key] - val) < 2e-8, (key, comps[key], val)
+
+
+def test_oracle_reproduces_he_potentials(oracle, golden):
+    """test/He.POTENTIALS: the He electrons (UHF) with the fitted nucleus
+    potential HEE and the fitted electron-electron potential EE in place of
+    Coulomb (both from the reference's lib/potentials); HF energy 1e-8."""
+    res = oracle.scf(oracle.from_plain(GS.he_potentials(golden)), tol_energy=1e-11, tol_density=1e-9)
+    ref = golden["values"]["He.POTENTIALS"]["HF energy"]
+    assert res.converged and abs(res.energy - ref[0]) <= ref[1], res.energy

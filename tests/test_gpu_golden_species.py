@@ -1,0 +1,58 @@
+"""GPU runs of the reference's golden inputs with species beyond electrons and
+single protons: one species of two protons (test/H2O.APMO.iter0-3), a
+positron species (test/PsH.P3) and electrons interacting only through fitted
+Gaussian potentials (test/He.POTENTIALS), through the reference-shaped host
+calls (HostSCF) and, for PsH.P3, the device-resident driver too.  Energies
+against the checkers' HF values (1e-8 Eh) and against the oracle."""
+import pytest
+
+from tests import golden_systems as GS
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scf():
+    from openlowdin_gb300 import build, scf
+    build.build()
+    return scf
+
+
+def test_two_proton_species_with_the_reference_damping(scf, golden):
+    """Damping (the reference's default method) under test/H2O.APMO.iter3's
+    criteria: every iteration's two-particle matrices of the electrons and of
+    the two-proton species and both couplings come from the library."""
+    sysd = GS.h2o_apmo_two_protons(golden)
+    s = scf.HostSCF(sysd, convergence="damping")
+    r = s.solve(tol_energy=1e-10, tol_density=1e-6, max_iter=3000)
+    s.close()
+    assert r.converged
+    for k in ("H2O.APMO.iter0", "H2O.APMO.iter1", "H2O.APMO.iter2", "H2O.APMO.iter3"):
+        ref = golden["values"][k]["HF energy"]
+        assert abs(r.energy - ref[0]) <= ref[1], (k, r.energy)
+    it = golden["values"]["H2O.APMO.iter3"]["Iterations"]
+    assert abs(r.iterations - it[0]) <= it[1]
+
+
+def test_positron_species(scf, oracle, golden):
+    sysd = GS.psh(golden)
+    ref = golden["values"]["PsH.P3"]["HF energy"]
+    res = oracle.scf(oracle.from_plain(sysd), tol_energy=1e-11, tol_density=1e-9)
+    for cls in (scf.HostSCF, scf.DeviceSCF):
+        s = cls(sysd)
+        r = s.solve(tol_energy=1e-11, tol_density=1e-9)
+        s.close()
+        assert r.converged, cls.__name__
+        assert abs(r.energy - ref[0]) <= ref[1], (cls.__name__, r.energy)
+        assert abs(r.energy - res.energy) < 1e-10, cls.__name__
+
+
+def test_he_fitted_potentials(scf, oracle, golden):
+    sysd = GS.he_potentials(golden)
+    s = scf.HostSCF(sysd)
+    r = s.solve(tol_energy=1e-11, tol_density=1e-9)
+    s.close()
+    ref = golden["values"]["He.POTENTIALS"]["HF energy"]
+    assert r.converged and abs(r.energy - ref[0]) <= ref[1], r.energy
+    res = oracle.scf(oracle.from_plain(sysd), tol_energy=1e-11, tol_density=1e-9)
+    assert abs(r.energy - res.energy) < 1e-10

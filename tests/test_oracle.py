@@ -297,3 +297,33 @@ def test_golden_hf_apmo(oracle, golden):
     assert res.converged and abs(res.energy - ref["HF energy"][0]) <= 1e-7
     mp2 = oracle.apmo_mp2(sysO, res)
     assert abs(mp2["total"] - ref["MP2 energy"][0]) <= ref["MP2 energy"][1]
+
+
+def test_golden_two_proton_species_damping(oracle, golden):
+    """test/H2O.APMO.iter0-iter3: both protons in one species (kappa = -1,
+    eta = 1).  The reference's default convergence method (damping) under
+    iteration scheme 3 and test/H2O.APMO.iter3's criteria (|dE| < 1e-10, density
+    1e-6) stops after as many iterations as its checker records (1069) and
+    within 1e-8 of all four checkers' energies (1.2e-10 of iter3's).  Pulay
+    DIIS from the start ends on another stationary point 0.17 Eh higher,
+    which is why the drivers offer the reference's damping."""
+    sysd = GS.h2o_apmo_two_protons(golden)
+    res = oracle.scf(oracle.from_plain(sysd), convergence="damping", tol_energy=1e-10, tol_density=1e-6,
+                     max_iter=3000)
+    assert res.converged
+    for k in ("H2O.APMO.iter0", "H2O.APMO.iter1", "H2O.APMO.iter2", "H2O.APMO.iter3"):
+        ref = golden["values"][k]["HF energy"]
+        assert abs(res.energy - ref[0]) <= ref[1], (k, res.energy)
+    it = golden["values"]["H2O.APMO.iter3"]["Iterations"]
+    assert abs(res.iterations - it[0]) <= it[1]
+    assert abs(res.energy - golden["values"]["H2O.APMO.iter3"]["HF energy"][0]) < 5e-10
+    rd = oracle.scf(oracle.from_plain(sysd), convergence="diis", tol_energy=1e-10, tol_density=1e-7, max_iter=500)
+    assert rd.converged and rd.energy > res.energy + 0.1
+
+
+def test_golden_positron_species(oracle, golden):
+    """test/PsH.P3: UHF electrons of H^-, a positron species (+1 charge, unit
+    mass) and the H nucleus; the checker's HF energy within 1e-8."""
+    res = oracle.scf(oracle.from_plain(GS.psh(golden)), tol_energy=1e-11, tol_density=1e-9)
+    ref = golden["values"]["PsH.P3"]["HF energy"]
+    assert res.converged and abs(res.energy - ref[0]) <= ref[1], res.energy
