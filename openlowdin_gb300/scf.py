@@ -279,7 +279,11 @@ class HostSCF:
         for h in self.handles:
             h.set_precision(1 if on else 0, self.split)
 
-    def solve(self, tol_energy=1e-8, tol_density=1e-6, max_iter=100) -> SCFResult:
+    def solve(self, tol_energy=1e-8, tol_density=1e-6, max_iter=100, density_sum=False) -> SCFResult:
+        """Converged when |dE| < tol_energy and the density change is below
+        tol_density (either alone with the other tolerance set to inf): the
+        largest rms change over the species, or with density_sum their sum,
+        the reference's measure (MultiSCF.f90:350-425, 776-830)."""
         t0 = time.perf_counter()
         sp, H, S, X = self.species, self.H, self.S, self.X
         ns = len(sp)
@@ -374,7 +378,8 @@ class HostSCF:
                 C[i], eps[i] = Ci, e
                 o = n_occ(sp[i])
                 Pn = sp[i]["eta"] * Ci[:, :o] @ Ci[:, :o].T
-                dmax = max(dmax, float(np.sqrt(np.mean((Pn - P[i]) ** 2))))
+                rms = float(np.sqrt(np.mean((Pn - P[i]) ** 2)))
+                dmax = dmax + rms if density_sum else max(dmax, rms)
                 newP.append(Pn)
             if e_old is not None and abs(energy - e_old) < tol_energy and dmax < tol_density:
                 if not fp64:

@@ -481,12 +481,16 @@ def damping_step(F, P, F0, P0):
 
 
 def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthreads=None,
-        convergence="diis", verbose=False) -> SCFResult:
+        convergence="diis", density_sum=False, verbose=False) -> SCFResult:
     """Multi-species Hartree-Fock, iteration scheme 3, restated from src/scf.
 
     convergence: "diis" (Pulay, CONVERGENCE_METHOD 2), "damping" (the
     reference's default, CONVERGENCE_METHOD 1; the kept pair starts from the
-    first Fock build, src/scf/MultiSCF.f90:330-336) or "none"."""
+    first Fock build, src/scf/MultiSCF.f90:330-336) or "none".  Converged
+    when |dE| < tol_energy and the density change < tol_density (either
+    criterion alone with the other tolerance set to inf): the largest rms
+    change over the species, or with density_sum their sum, the reference's
+    measure (src/scf/MultiSCF.f90:350-425, 776-830)."""
     if convergence not in ("diis", "damping", "none"):
         raise ValueError(f"unknown convergence method {convergence!r}")
     sp = system.species
@@ -568,7 +572,8 @@ def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthrea
             Ci = X[i] @ Cp
             C[i] = Ci; eps[i] = e
             Pn = s.eta * Ci[:, :s.n_occ] @ Ci[:, :s.n_occ].T
-            dmax = max(dmax, float(np.sqrt(np.mean((Pn - P[i]) ** 2))))
+            rms = float(np.sqrt(np.mean((Pn - P[i]) ** 2)))
+            dmax = dmax + rms if density_sum else max(dmax, rms)
             newP.append(Pn)
         if verbose:
             print(f"iter {it:3d}  E = {energy:.12f}  dP = {dmax:.2e}")

@@ -23,7 +23,9 @@ It extracts, as data:
   * ``test/HF.APMO`` (HF with cc-pVTZ electrons, f shell on F, and a DZSPDN
     quantum proton): geometry, bases and the checker's HF and MP2 energies,
   * ``test/H2O.APMO.iter0``-``iter3`` (6-31G electrons, one species of two
-    NAKAI-3-SP protons), ``test/PsH.P3`` (UHF electrons of H^- with cc-pVTZ, a
+    NAKAI-3-SP protons), ``test/NH3.APMO.convBoth`` (6-31G* electrons, one
+    species of three DZSPNB protons; the values of its siblings convDens and
+    convEne too), ``test/PsH.P3`` (UHF electrons of H^- with cc-pVTZ, a
     positron species) and ``test/He.POTENTIALS`` (UHF He electrons whose
     nucleus is the fitted external potential HEE and whose electron-electron
     interaction is the G12 potential EE, both from ``lib/potentials``):
@@ -232,6 +234,8 @@ def main():
             "6-31G:H": read_basis("6-31G", "HYDROGEN", "H"),
             "6-31G:O": read_basis("6-31G", "OXYGEN", "O"),
             "6-31G:He": read_basis("6-31G", "HELIUM", "HE"),
+            "6-31G.D:N": read_basis("6-31G.D", "NITROGEN", "N"),
+            "6-31G.D:H": read_basis("6-31G.D", "HYDROGEN", "H"),
             "E+-H-7SP-AUG-CC-PVTZ:E+": read_basis("E+-H-7SP-AUG-CC-PVTZ", "POSITRON", "E+"),
             "6-311++G.D.P:H": read_basis("6-311++G.D.P", "HYDROGEN", "H"),
             "6-311++G.D.P:O": read_basis("6-311++G.D.P", "OXYGEN", "O"),
@@ -246,6 +250,7 @@ def main():
             "H2.APMO.UEN": read_geometry("H2.APMO.UEN.lowdin"),
             "H2O.BOA.UEN": read_geometry("H2O.BOA.UEN.lowdin"),
             "H2O.APMO.iter0": read_geometry("H2O.APMO.iter0.lowdin"),
+            "NH3.APMO.convBoth": read_geometry("NH3.APMO.convBoth.lowdin"),
             "PsH.P3": read_geometry("PsH.P3.lowdin"),
             "He.POTENTIALS": read_geometry("He.POTENTIALS.lowdin"),
         },
@@ -265,6 +270,9 @@ def main():
             "H2O.APMO.iter1": read_checker("H2O.APMO.iter1.py"),
             "H2O.APMO.iter2": read_checker("H2O.APMO.iter2.py"),
             "H2O.APMO.iter3": read_checker("H2O.APMO.iter3.py"),
+            "NH3.APMO.convBoth": read_checker("NH3.APMO.convBoth.py"),
+            "NH3.APMO.convDens": read_checker("NH3.APMO.convDens.py"),
+            "NH3.APMO.convEne": read_checker("NH3.APMO.convEne.py"),
             "PsH.P3": read_checker("PsH.P3.py"),
             "He.POTENTIALS": read_checker("He.POTENTIALS.py"),
             "TIP4P-dimer-singlet-direct": read_checker("TIP4P-dimer-singlet-direct.py"),

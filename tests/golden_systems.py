@@ -42,7 +42,7 @@ def h2o_apmo(golden):
             "name": "H2O.APMO"}
 
 
-_Z = {"H": 1.0, "H_1": 1.0, "O": 8.0}
+_Z = {"H": 1.0, "H_1": 1.0, "N": 7.0, "O": 8.0}
 
 
 def uhf_system(golden, test, electron_basis, proton_basis):
@@ -216,3 +216,20 @@ def he_potentials(golden):
         inter.append({"species": [names.index(a), names.index(b)], "coefficients": c, "exponents": g})
     return {"species": species, "point_charges": [], "point_positions": [], "external_potentials": ext,
             "interpotentials": inter, "name": "He.POTENTIALS"}
+
+
+def nh3_apmo_three_protons(golden):
+    """test/NH3.APMO.convBoth: 6-31G* electrons, classical N, the three protons
+    in one species H_1 (three particles, DZSPNB)."""
+    geo = golden["geometry"]["NH3.APMO.convBoth"]
+    shells, Z, R, pshells = [], [], [], []
+    for r in geo:
+        part = r["particle"]
+        if part.startswith("e-"):
+            shells += _shells(golden, "6-31G.D:" + part[3:-1], r["position_bohr"])
+        elif r["basis"] == "dirac":
+            Z.append(_Z[part]); R.append(r["position_bohr"])
+        else:
+            pshells += _shells(golden, "DZSPNB:H_1", r["position_bohr"])
+    return {"species": [S.electron_species(shells, 10), S.proton_species(pshells, 3)], "point_charges": Z,
+            "point_positions": R, "name": "NH3.APMO.convBoth"}

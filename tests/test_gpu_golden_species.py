@@ -1,5 +1,6 @@
 """GPU runs of the reference's golden inputs with species beyond electrons and
-single protons: one species of two protons (test/H2O.APMO.iter0-3), a
+single protons: one species of two or three protons (test/H2O.APMO.iter3,
+test/NH3.APMO.convBoth), a
 positron species (test/PsH.P3) and electrons interacting only through fitted
 Gaussian potentials (test/He.POTENTIALS), through the reference-shaped host
 calls (HostSCF) and, for PsH.P3, the device-resident driver too.  Energies
@@ -7,6 +8,7 @@ against the checkers' HF values (1e-8 Eh) and against the oracle."""
 import pytest
 
 from tests import golden_systems as GS
+from tests.test_oracle import DAMPING_CASES
 
 pytestmark = pytest.mark.gpu
 
@@ -18,20 +20,22 @@ def scf():
     return scf
 
 
-def test_two_proton_species_with_the_reference_damping(scf, golden):
-    """Damping (the reference's default method) under test/H2O.APMO.iter3's
+@pytest.mark.parametrize("case", DAMPING_CASES, ids=[c[1] for c in DAMPING_CASES])
+def test_multi_proton_species_with_the_reference_damping(scf, golden, case):
+    """Damping (the reference's default method) under each input's own
     criteria: every iteration's two-particle matrices of the electrons and of
-    the two-proton species and both couplings come from the library."""
-    sysd = GS.h2o_apmo_two_protons(golden)
+    the proton species and both couplings come from the library; the solve
+    stops where the reference's did (its recorded iteration count) at its
+    energy."""
+    build, test, te, td = case
+    sysd = getattr(GS, build)(golden)
     s = scf.HostSCF(sysd, convergence="damping")
-    r = s.solve(tol_energy=1e-10, tol_density=1e-6, max_iter=3000)
+    r = s.solve(tol_energy=te, tol_density=td, max_iter=3000, density_sum=True)
     s.close()
+    ref = golden["values"][test]
     assert r.converged
-    for k in ("H2O.APMO.iter0", "H2O.APMO.iter1", "H2O.APMO.iter2", "H2O.APMO.iter3"):
-        ref = golden["values"][k]["HF energy"]
-        assert abs(r.energy - ref[0]) <= ref[1], (k, r.energy)
-    it = golden["values"]["H2O.APMO.iter3"]["Iterations"]
-    assert abs(r.iterations - it[0]) <= it[1]
+    assert abs(r.energy - ref["HF energy"][0]) <= ref["HF energy"][1], r.energy
+    assert abs(r.iterations - ref["Iterations"][0]) <= ref["Iterations"][1], r.iterations
 
 
 def test_positron_species(scf, oracle, golden):

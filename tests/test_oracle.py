@@ -299,26 +299,45 @@ def test_golden_hf_apmo(oracle, golden):
     assert abs(mp2["total"] - ref["MP2 energy"][0]) <= ref["MP2 energy"][1]
 
 
-def test_golden_two_proton_species_damping(oracle, golden):
-    """test/H2O.APMO.iter0-iter3: both protons in one species (kappa = -1,
-    eta = 1).  The reference's default convergence method (damping) under
-    iteration scheme 3 and test/H2O.APMO.iter3's criteria (|dE| < 1e-10, density
-    1e-6) stops after as many iterations as its checker records (1069) and
-    within 1e-8 of all four checkers' energies (1.2e-10 of iter3's).  Pulay
-    DIIS from the start ends on another stationary point 0.17 Eh higher,
-    which is why the drivers offer the reference's damping."""
-    sysd = GS.h2o_apmo_two_protons(golden)
-    res = oracle.scf(oracle.from_plain(sysd), convergence="damping", tol_energy=1e-10, tol_density=1e-6,
-                     max_iter=3000)
+# the reference's own stopping rules of its scheme-3 inputs (scfConvergenceCriterium
+# ENERGY by default, BOTH in NH3.APMO.convBoth; the density change summed over
+# the species): (builder, test, tol_energy, tol_density)
+DAMPING_CASES = [("h2o_apmo_two_protons", "H2O.APMO.iter3", 1e-10, float("inf")),
+                 ("nh3_apmo_three_protons", "NH3.APMO.convBoth", 1e-8, 1e-6)]
+
+
+@pytest.mark.parametrize("case", DAMPING_CASES, ids=[c[1] for c in DAMPING_CASES])
+def test_golden_multi_proton_species_damping(oracle, golden, case):
+    """test/H2O.APMO.iter3 (both protons in one species, kappa = -1, eta = 1)
+    and test/NH3.APMO.convBoth (three protons in one species): the
+    reference's default convergence method (damping) under iteration scheme
+    3 and each input's own criteria stops after the number of iterations its
+    checker records (1069 and 1114; the checkers allow 800 and 200) and
+    within 1e-8 of its energy (1.2e-10 and 8.1e-10 off): the restated damping
+    follows the reference's trajectory.  The water's converged energy is
+    also within 1e-8 of iter0-iter2 (schemes 0-2)."""
+    build, test, te, td = case
+    sysd = getattr(GS, build)(golden)
+    res = oracle.scf(oracle.from_plain(sysd), convergence="damping", tol_energy=te, tol_density=td,
+                     density_sum=True, max_iter=3000)
     assert res.converged
-    for k in ("H2O.APMO.iter0", "H2O.APMO.iter1", "H2O.APMO.iter2", "H2O.APMO.iter3"):
-        ref = golden["values"][k]["HF energy"]
-        assert abs(res.energy - ref[0]) <= ref[1], (k, res.energy)
-    it = golden["values"]["H2O.APMO.iter3"]["Iterations"]
-    assert abs(res.iterations - it[0]) <= it[1]
-    assert abs(res.energy - golden["values"]["H2O.APMO.iter3"]["HF energy"][0]) < 5e-10
+    ref = golden["values"][test]
+    assert abs(res.energy - ref["HF energy"][0]) < 1e-9, res.energy
+    assert abs(res.iterations - ref["Iterations"][0]) <= 5, res.iterations
+    if test == "H2O.APMO.iter3":
+        for k in ("H2O.APMO.iter0", "H2O.APMO.iter1", "H2O.APMO.iter2"):
+            r = golden["values"][k]["HF energy"]
+            assert abs(res.energy - r[0]) <= r[1], (k, res.energy)
+
+
+def test_diis_ends_elsewhere_on_the_two_proton_species(oracle, golden):
+    """Pulay DIIS from the start ends on another stationary point 0.17 Eh
+    above the reference's solution, which is why the host driver offers the
+    reference's damping."""
+    sysd = GS.h2o_apmo_two_protons(golden)
     rd = oracle.scf(oracle.from_plain(sysd), convergence="diis", tol_energy=1e-10, tol_density=1e-7, max_iter=500)
-    assert rd.converged and rd.energy > res.energy + 0.1
+    ref = golden["values"]["H2O.APMO.iter3"]["HF energy"][0]
+    assert rd.converged and rd.energy > ref + 0.1
 
 
 def test_golden_positron_species(oracle, golden):
