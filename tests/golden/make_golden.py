@@ -30,6 +30,9 @@ It extracts, as data:
     nucleus is the fitted external potential HEE and whose electron-electron
     interaction is the G12 potential EE, both from ``lib/potentials``):
     geometries, bases, potentials and the checkers' HF energies,
+  * the HF energies of ``test/H2O.APMO.UP2``, ``test/H2O.APMO.FCI``,
+    ``test/CO.CISD-dipole``, ``test/Ne.CISD``, ``test/H2O.BOA`` and
+    ``test/H2O.BOA.UMP2`` (their post-HF values are not used),
   * the UHF inputs ``test/H2.APMO.UEN`` (cc-pVTZ electrons, NAKAI-3-SPD
     protons) and ``test/H2O.BOA.UEN`` (6-311++G** electrons): geometry, bases
     and the checkers' HF and MP2 energies (their Epstein-Nesbet values are
@@ -235,6 +238,11 @@ def main():
             "6-31G:O": read_basis("6-31G", "OXYGEN", "O"),
             "6-31G:He": read_basis("6-31G", "HELIUM", "HE"),
             "6-31G.D:N": read_basis("6-31G.D", "NITROGEN", "N"),
+            "6-31G.D:C": read_basis("6-31G.D", "CARBON", "C"),
+            "6-31G.D:O": read_basis("6-31G.D", "OXYGEN", "O"),
+            "6-311G.D.P:Ne": read_basis("6-311G.D.P", "NEON", "NE"),
+            "NAKAI-7-SP:H_1": read_basis("NAKAI-7-SP", "HYDROGEN_1", "H_1"),
+            "NAKAI-3-S:H_1": read_basis("NAKAI-3-S", "HYDROGEN_1", "H_1"),
             "6-31G.D:H": read_basis("6-31G.D", "HYDROGEN", "H"),
             "E+-H-7SP-AUG-CC-PVTZ:E+": read_basis("E+-H-7SP-AUG-CC-PVTZ", "POSITRON", "E+"),
             "6-311++G.D.P:H": read_basis("6-311++G.D.P", "HYDROGEN", "H"),
@@ -252,6 +260,12 @@ def main():
             "H2O.APMO.iter0": read_geometry("H2O.APMO.iter0.lowdin"),
             "NH3.APMO.convBoth": read_geometry("NH3.APMO.convBoth.lowdin"),
             "PsH.P3": read_geometry("PsH.P3.lowdin"),
+            "H2O.APMO.UP2": read_geometry("H2O.APMO.UP2.lowdin"),
+            "H2O.APMO.FCI": read_geometry("H2O.APMO.FCI.lowdin"),
+            "CO.CISD-dipole": read_geometry("CO.CISD-dipole.lowdin"),
+            "Ne.CISD": read_geometry("Ne.CISD.lowdin"),
+            "H2O.BOA": read_geometry("H2O.BOA.lowdin"),
+            "H2O.BOA.UMP2": read_geometry("H2O.BOA.UMP2.lowdin"),
             "He.POTENTIALS": read_geometry("He.POTENTIALS.lowdin"),
         },
         "values": {
@@ -274,6 +288,12 @@ def main():
             "NH3.APMO.convDens": read_checker("NH3.APMO.convDens.py"),
             "NH3.APMO.convEne": read_checker("NH3.APMO.convEne.py"),
             "PsH.P3": read_checker("PsH.P3.py"),
+            "H2O.APMO.UP2": read_checker("H2O.APMO.UP2.py"),
+            "H2O.APMO.FCI": read_checker("H2O.APMO.FCI.py"),
+            "CO.CISD-dipole": read_checker("CO.CISD-dipole.py"),
+            "Ne.CISD": read_checker("Ne.CISD.py"),
+            "H2O.BOA": read_checker("H2O.BOA.py"),
+            "H2O.BOA.UMP2": read_checker("H2O.BOA.UMP2.py"),
             "He.POTENTIALS": read_checker("He.POTENTIALS.py"),
             "TIP4P-dimer-singlet-direct": read_checker("TIP4P-dimer-singlet-direct.py"),
             "TIP4P-dimer-triplet-direct": read_checker("TIP4P-dimer-triplet-direct.py"),

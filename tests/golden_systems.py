@@ -42,7 +42,7 @@ def h2o_apmo(golden):
             "name": "H2O.APMO"}
 
 
-_Z = {"H": 1.0, "H_1": 1.0, "N": 7.0, "O": 8.0}
+_Z = {"H": 1.0, "H_1": 1.0, "C": 6.0, "N": 7.0, "O": 8.0, "Ne": 10.0}
 
 
 def uhf_system(golden, test, electron_basis, proton_basis):

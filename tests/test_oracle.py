@@ -261,6 +261,33 @@ def test_golden_uen_mp2(oracle, golden, case):
     assert abs(total - ref[0]) <= ref[1], total
 
 
+# HF energies of further inputs (electrons as E-ALPHA / E-BETA species, the
+# inputs' RHF or UHF solutions being closed shell), pinned in the oracle:
+# (test, electron basis, proton basis)
+HF_ONLY_CASES = [("H2O.APMO.UP2", "6-311G", "NAKAI-7-SP"), ("H2O.APMO.FCI", "6-31G", "NAKAI-3-S"),
+                 ("CO.CISD-dipole", "6-31G.D", None), ("Ne.CISD", "6-311G.D.P", None),
+                 ("H2O.BOA", "6-311G", None), ("H2O.BOA.UMP2", "6-311G", None)]
+
+
+@pytest.mark.parametrize("case", HF_ONLY_CASES, ids=[c[0] for c in HF_ONLY_CASES])
+def test_golden_hf_energies_more_inputs(oracle, golden, case):
+    test, ebas, pbas = case
+    sysd = GS.uhf_system(golden, test, ebas, pbas)
+    res = oracle.scf(oracle.from_plain(sysd), tol_energy=1e-11, tol_density=1e-9, max_iter=300)
+    ref = golden["values"][test]["HF energy"]
+    assert res.converged and abs(res.energy - ref[0]) <= ref[1], res.energy
+
+
+def test_golden_h2o_boa_ump2(oracle, golden):
+    """test/H2O.BOA.UMP2: closed-shell UHF water (6-311G), so its UMP2 total is
+    the closed-shell MP2 total (checker 1e-5)."""
+    sysd = closed_shell_twin(GS.uhf_system(golden, "H2O.BOA.UMP2", "6-311G", None))
+    sysO = oracle.from_plain(sysd)
+    res = oracle.scf(sysO, tol_energy=1e-11, tol_density=1e-9)
+    ref = golden["values"]["H2O.BOA.UMP2"]["MP2 energy"]
+    assert abs(oracle.apmo_mp2(sysO, res)["total"] - ref[0]) <= ref[1]
+
+
 def test_golden_h2o_apmo_uhf(oracle, golden):
     """test/H2O.APMO.UHF.DIRECT: -75.93125555356 within 1e-8 as a UHF solve."""
     res = oracle.scf(oracle.from_plain(GS.h2o_apmo_uhf(golden)), tol_energy=1e-11, tol_density=1e-9)
