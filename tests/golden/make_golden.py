@@ -30,6 +30,11 @@ It extracts, as data:
     nucleus is the fitted external potential HEE and whose electron-electron
     interaction is the G12 potential EE, both from ``lib/potentials``):
     geometries, bases, potentials and the checkers' HF energies,
+  * ``test/He2-C60potential-NOCI`` and ``He3-`` (helium atoms as quantum
+    particles in a C60 cage fitted as 25 Gaussian terms at each of the 60
+    carbon centres, lib/potentials HE2C60-IH-1P / -2P): geometry, basis,
+    potentials (stored as terms x centres, checked exact), particle constants
+    and the checkers' HF energies (their NOCI values are not used),
   * the HF energies of ``test/H2O.APMO.UP2``, ``test/H2O.APMO.FCI``,
     ``test/CO.CISD-dipole``, ``test/Ne.CISD``, ``test/H2O.BOA`` and
     ``test/H2O.BOA.UMP2`` (their post-HF values are not used),
@@ -109,6 +114,62 @@ def particle_charge(symbol):
         if m and m.group(1) == symbol:
             return float(re.search(r"CHARGE\s*=\s*([-0-9.Ee+]+)", blk).group(1))
     raise KeyError(symbol)
+
+
+def coupling_constants(symbol):
+    """KAPPA, ETA and PARTICLESFRACTION of a &SPECIE entry of
+    lib/dataBases/constantsOfCoupling.lib."""
+    txt = open(os.path.join(ROOT, "lib", "dataBases", "constantsOfCoupling.lib")).read()
+    for blk in txt.split("&SPECIE")[1:]:
+        m = re.search(r'SYMBOL\s*=\s*"([^"]+)"', blk)
+        if m and m.group(1) == symbol:
+            get = lambda k: float(re.search(k + r"\s*=\s*([-0-9.Ee+]+)", blk).group(1))
+            return {"kappa": get("KAPPA"), "eta": get("ETA"), "particles_fraction": get("PARTICLESFRACTION")}
+    raise KeyError(symbol)
+
+
+def factored(comps):
+    """A potential whose components are every (exponent, coefficient) term at
+    every centre, term-major as in the file, stored as the two lists; the
+    expansion is checked to give the file's components exactly."""
+    terms, centers = [], []
+    for c in comps:
+        assert c["l"] == 0
+        if [c["exponent"], c["coefficient"]] not in terms:
+            terms.append([c["exponent"], c["coefficient"]])
+        if c["origin"] not in centers:
+            centers.append(c["origin"])
+    assert [{"l": 0, "exponent": g, "coefficient": k, "origin": o} for g, k in terms for o in centers] == comps
+    return {"terms": terms, "centers": centers}
+
+
+def read_c60_input(name):
+    """test/He{2,3}-C60potential-NOCI: helium atoms as quantum particles
+    (HEA3 / HEB3, one s function each from lib/basis/HE2-1S) inside a C60
+    cage given as the external potential HE2C60-IH-1P (25 terms at each of
+    the 60 carbon centres) and interacting through HE2C60-IH-2P; charges and
+    masses of lib/dataBases, the input's m= overriding the mass."""
+    txt = open(os.path.join(ROOT, "test", name + ".lowdin")).read()
+    assert re.search(r'units\s*=\s*"BOHRS"', txt)
+    particles, names = [], []
+    for ln in read_block(txt, "GEOMETRY", "END GEOMETRY").strip().splitlines():
+        t = ln.split()
+        rec = {"particle": t[0], "basis": t[1], "position_bohr": [float(x) for x in t[2:5]],
+               "charge": particle_charge(t[0])}
+        m = re.search(r"(?<![A-Za-z])m\s*=\s*([0-9.Ee+-]+)", ln)
+        if m:
+            rec["mass"] = float(m.group(1))
+        if t[1] != "dirac" and t[0] not in names:
+            names.append(t[0])
+        particles.append(rec)
+    asg = read_assignments(txt)
+    ext = {e["potential"] for e in asg["external"]}
+    inter = {e["potential"] for e in asg["inter"]}
+    pots = {p: {k: factored(v) for k, v in read_potential_file(p.upper(), tuple(names)).items()} for p in ext}
+    pots.update({p: read_potential_file(p.upper(), tuple(a + b for a in names for b in names)) for p in inter})
+    basis = {n: read_basis(next(r["basis"] for r in particles if r["particle"] == n), "HELIUM", n) for n in names}
+    return dict(asg, particles=particles, basis=basis, potentials=pots,
+                constants={n: coupling_constants(n) for n in names})
 
 
 def read_block(txt, head, tail):
@@ -295,12 +356,16 @@ def main():
             "H2O.BOA": read_checker("H2O.BOA.py"),
             "H2O.BOA.UMP2": read_checker("H2O.BOA.UMP2.py"),
             "He.POTENTIALS": read_checker("He.POTENTIALS.py"),
+            "He2-C60potential-NOCI": read_checker("He2-C60potential-NOCI.py"),
+            "He3-C60potential-NOCI": read_checker("He3-C60potential-NOCI.py"),
             "TIP4P-dimer-singlet-direct": read_checker("TIP4P-dimer-singlet-direct.py"),
             "TIP4P-dimer-triplet-direct": read_checker("TIP4P-dimer-triplet-direct.py"),
         },
         "g12_inputs": {
             "TIP4P-dimer-singlet-direct": read_g12_input("TIP4P-dimer-singlet-direct"),
             "TIP4P-dimer-triplet-direct": read_g12_input("TIP4P-dimer-triplet-direct"),
+            "He2-C60potential-NOCI": read_c60_input("He2-C60potential-NOCI"),
+            "He3-C60potential-NOCI": read_c60_input("He3-C60potential-NOCI"),
             "He.POTENTIALS": dict(read_assignments(open(os.path.join(ROOT, "test", "He.POTENTIALS.lowdin")).read()),
                                   potentials={"HEE": read_potential_file("HEE", ("E-ALPHA", "E-BETA")),
                                               "EE": read_potential_file("EE", ("E-ALPHAE-ALPHA", "E-ALPHAE-BETA",

@@ -233,3 +233,43 @@ def nh3_apmo_three_protons(golden):
             pshells += _shells(golden, "DZSPNB:H_1", r["position_bohr"])
     return {"species": [S.electron_species(shells, 10), S.proton_species(pshells, 3)], "point_charges": Z,
             "point_positions": R, "name": "NH3.APMO.convBoth"}
+
+
+def c60_system(golden, test):
+    """test/He2-C60potential-NOCI / He3-: one species per particle name (HEA3,
+    HEB3; one s function per particle) with the particle database's charge and
+    coupling constants and the input's mass, the C60 cage as the external
+    potential of every species (expanded from terms x centres), the fitted
+    He-He potential as the G12 pair potentials, and the point particle N0."""
+    inp = golden["g12_inputs"][test]
+    assert inp["method"] == "UHF"
+    names, rows, Z, R = [], {}, [], []
+    for r in inp["particles"]:
+        if r["basis"] == "dirac":
+            Z.append(r["charge"]); R.append(r["position_bohr"])
+            continue
+        if r["particle"] not in rows:
+            names.append(r["particle"]); rows[r["particle"]] = []
+        rows[r["particle"]].append(r)
+    species = []
+    for nm in names:
+        shells = [(s["l"], s["exponents"], s["coefficients"], list(r["position_bohr"]))
+                  for r in rows[nm] for s in inp["basis"][nm]]
+        r0 = rows[nm][0]
+        species.append(dict(inp["constants"][nm], name=nm, charge=r0["charge"], mass=r0["mass"],
+                            n_particles=len(rows[nm]), is_electron=False, shells=shells))
+    ext = []
+    for e in inp["external"]:
+        f = inp["potentials"][e["potential"]][e["species"]]
+        terms = [(g, c, o) for g, c in f["terms"] for o in f["centers"]]
+        ext.append({"species": names.index(e["species"]), "coefficients": [t[1] for t in terms],
+                    "exponents": [t[0] for t in terms], "origins": [t[2] for t in terms]})
+    inter = []
+    for e in inp["inter"]:
+        a, b = e["species"]
+        c = inp["potentials"][e["potential"]][a + b]
+        assert all(x["l"] == 0 for x in c)
+        inter.append({"species": [names.index(a), names.index(b)], "coefficients": [x["coefficient"] for x in c],
+                      "exponents": [x["exponent"] for x in c]})
+    return {"species": species, "point_charges": Z, "point_positions": R, "external_potentials": ext,
+            "interpotentials": inter, "name": test}

@@ -10,7 +10,9 @@ protons, UHF, G = G12 Coulomb - G12 exchange.  The checkers assert the HF
 energy to 1e-8 and the energy components to 1e-4.
 
 test/He.POTENTIALS does the same for the two electrons of He: the fitted
-potential HEE is their nucleus and the fitted EE their interaction.
+potential HEE is their nucleus and the fitted EE their interaction; and
+test/He{2,3}-C60potential-NOCI for helium atoms in a C60 cage fitted as 1500
+off-centre Gaussian terms.
 
 The external-potential matrix is checked twice: the oracle's quadrature against
 the identity exp(-0 r^2) = 1 (the overlap) and the library's host recursion
@@ -136,3 +138,31 @@ def test_oracle_reproduces_he_potentials(oracle, golden):
     res = oracle.scf(oracle.from_plain(GS.he_potentials(golden)), tol_energy=1e-11, tol_density=1e-9)
     ref = golden["values"]["He.POTENTIALS"]["HF energy"]
     assert res.converged and abs(res.energy - ref[0]) <= ref[1], res.energy
+
+
+C60_TESTS = ("He2-C60potential-NOCI", "He3-C60potential-NOCI")
+
+
+@pytest.mark.parametrize("test", C60_TESTS)
+def test_oracle_reproduces_c60_cage(oracle, golden, test):
+    """test/He2-C60potential-NOCI and He3-: helium atoms (one s function each;
+    in He3 two of them form one species) in a C60 cage given as 1500 Gaussian
+    terms at the 60 carbon centres, interacting through a fitted He-He
+    potential; HF energy 1e-8 (the checkers' NOCI values are not used)."""
+    res = oracle.scf(oracle.from_plain(GS.c60_system(golden, test)), tol_energy=1e-12, tol_density=1e-10)
+    ref = golden["values"][test]["HF energy"]
+    assert res.converged and abs(res.energy - ref[0]) <= ref[1], res.energy
+
+
+def test_library_c60_cage_potential(built, oracle, golden):
+    """The library's host recursion on 1500 off-centre components against the
+    oracle's quadrature."""
+    sysd = GS.c60_system(golden, "He3-C60potential-NOCI")
+    for e in sysd["external_potentials"]:
+        sp = sysd["species"][e["species"]]
+        h = built.Libint2Interface(sp, 1)
+        ref = oracle.gaussian_potential(oracle.Basis.from_shells(sp["shells"]), e["coefficients"],
+                                        e["exponents"], e["origins"])
+        got = h.gaussian_potential(e["coefficients"], e["exponents"], e["origins"])
+        assert np.max(np.abs(got - ref)) < 1e-12 * max(1.0, np.max(np.abs(ref)))
+        h.close()

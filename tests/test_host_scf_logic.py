@@ -57,9 +57,14 @@ def test_damping_stops_where_the_reference_did(scf, golden, case):
     assert abs(r.iterations - ref["Iterations"][0]) <= 5
 
 
-@pytest.mark.parametrize("test", ["TIP4P-dimer-singlet-direct", "He.POTENTIALS"])
+@pytest.mark.parametrize("test", ["TIP4P-dimer-singlet-direct", "He.POTENTIALS", "He3-C60potential-NOCI"])
 def test_fitted_potentials(scf, golden, test):
-    sysd = GS.he_potentials(golden) if test == "He.POTENTIALS" else GS.g12_system(golden, test)
+    if test == "He.POTENTIALS":
+        sysd = GS.he_potentials(golden)
+    elif "C60" in test:
+        sysd = GS.c60_system(golden, test)
+    else:
+        sysd = GS.g12_system(golden, test)
     s = scf.HostSCF(sysd)
     r = s.solve(tol_energy=1e-11, tol_density=1e-9)
     s.close()
