@@ -2,7 +2,7 @@
 """Benchmark: served SCF(+MP2) solves/s of the mixed-precision engine on GB300.
 
 Headline workload (one "step" = one request of the stream): the serving
-stream of the batched/served spec form -- Poisson arrivals (default 50
+stream of the batched, served SCF -- Poisson arrivals (default 50
 req/s), H/C/N/O chain molecules of the batched-RHF generator grown to a size
 drawn log-uniformly from 30-1200 Cartesian functions, 70 % RHF and 30 % RHF +
 frozen-core MP2, admitted under a 150 GB HBM budget -- served by the

@@ -166,8 +166,8 @@ void LowdinGB300_gaussian_potential(LibintInterface *lint, int ncomp, const doub
    buffers, the reference's own call): 0 = FP64 (default, the reference's
    behaviour); 1 = quartets whose Schwarz bound times the density's shell-block
    maximum is below `split` run in FP32, the rest in FP64 (a caller that passes
-   density changes gets the incremental mixed-precision build of the north
-   star's SCF).  The coupling and first-quarter calls stay FP64.  Returns 0, or
+   density changes gets the incremental mixed-precision build of the
+   batched SCF).  The coupling and first-quarter calls stay FP64.  Returns 0, or
    -1 for an unknown precision or a split outside (0, 1). */
 int LowdinGB300_set_precision(LibintInterface *lint, int precision, double split);
 

@@ -335,7 +335,7 @@ struct LibintInterface {
     if (!device_boys(boys)) return false;
     for (const auto &s : shells)
       if (s.l > kMaxL) {
-        set_error("shell with l=%d: this build handles l <= %d", s.l, kMaxL);
+        set_error("shell with l=%d: the library handles l <= %d", s.l, kMaxL);
         return false;
       }
     std::vector<int> shell_of(nbasis);

@@ -359,7 +359,7 @@ class HostSCF:
                         C[i], eps[i] = X[i] @ Cp, e
                     converged = True
                     break
-                guard_hit = True                  # continue in FP64 from this build
+                guard_hit = True                  # continue in FP64 from this Fock build
                 diis, e_old, kept = _DIIS(np), None, None
             if self.convergence == "diis":
                 Fx = diis(F, errs)

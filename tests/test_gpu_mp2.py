@@ -1,7 +1,7 @@
 """Device MP2 (four-index transform + pair energies) against the oracle's
 restatement of the reference's DIRECT transform, on the same SCF inputs.
 
-Tolerance: 1e-10 Eh on E_MP2 for the FP64 path (the benchmark spec's MP2 bar is
+Tolerance: 1e-10 Eh on E_MP2 for the FP64 path (the plain path's MP2 bar is
 1e-8 Eh); the golden MP2 total energy within its test tolerance; the
 split-BF16 tensor-core path within 1e-6 Eh of the oracle (the per-job bar of
 the mixed-precision forms).
