@@ -54,3 +54,24 @@ def test_one_body_host_integrals_match_oracle(built, oracle):
     assert np.max(np.abs(h.one_body(2) - T0)) < 1e-11
     assert np.max(np.abs(h.potential(sysd["point_charges"], sysd["point_positions"]) - V0)) < 1e-11
     h.close()
+
+
+def test_one_body_host_integrals_f_shells_and_contractions(built, oracle):
+    """The host one-body matrices (overlap, kinetic, point-charge potential)
+    on contracted s, p, d and f shells over two centres, against the oracle."""
+    import numpy as np
+    from openlowdin_gb300 import systems
+    A, B = [0.0, 0.0, 0.0], [0.0, 0.9, 1.3]
+    sh = []
+    for c in (A, B):
+        sh += [(0, [3.0, 0.6], [0.4, 0.7], c), (1, [1.1, 0.3], [0.5, 0.6], c), (2, [0.9], [1.0], c),
+               (3, [1.3, 0.4], [0.3, 0.8], c)]
+    h = lint.Libint2Interface(systems.electron_species(sh, 6), 1)
+    b = oracle.Basis.from_shells(sh)
+    S0, T0 = oracle.overlap_kinetic(b)
+    Z, R = [3.0, 1.0], [[0.0, 0.0, 0.2], [0.5, 0.4, 1.0]]
+    V0 = oracle.potential(b, Z, R)
+    assert np.max(np.abs(h.one_body(1) - S0)) < 1e-13
+    assert np.max(np.abs(h.one_body(2) - T0)) < 1e-11
+    assert np.max(np.abs(h.potential(Z, R) - V0)) < 1e-11
+    h.close()
