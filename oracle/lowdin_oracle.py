@@ -480,9 +480,27 @@ def damping_step(F, P, F0, P0):
     return F0.copy(), F0, P0 + lam * (P - P0)
 
 
+def scheme_iterations(system: System, scheme: int, electronic_max=50, nonelectronic_max=50) -> list:
+    """Single-species sub-iterations per global iteration of the reference's
+    iteration schemes (src/scf/MultiSCF.f90:150-185): 0 = non-electronic
+    species iterate up to nonelectronic_max times, 1 = electrons up to
+    electronic_max, 2 = both, 3 = every species once (SCF_*_MAX_ITERATIONS
+    default to 50, src/core/CONTROL.f90:1474-1475)."""
+    out = []
+    for s in system.species:
+        el = s.is_electron
+        out.append({0: 1 if el else nonelectronic_max, 1: electronic_max if el else 1,
+                    2: electronic_max if el else nonelectronic_max, 3: 1}[scheme])
+    return out
+
+
 def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthreads=None,
-        convergence="diis", density_sum=False, verbose=False) -> SCFResult:
-    """Multi-species Hartree-Fock, iteration scheme 3, restated from src/scf.
+        convergence="diis", density_sum=False, sub_iterations=None, sub_tolerances=(1e-8, 1e-6),
+        sub_density_test=True, verbose=False) -> SCFResult:
+    """Multi-species Hartree-Fock restated from src/scf: every global
+    iteration builds every species' two-particle and coupling matrices, Fock
+    matrix and the total energy from the current densities, then updates the
+    species one after the other (src/scf/MultiSCF.f90:276-440).
 
     convergence: "diis" (Pulay, CONVERGENCE_METHOD 2), "damping" (the
     reference's default, CONVERGENCE_METHOD 1; the kept pair starts from the
@@ -490,9 +508,21 @@ def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthrea
     when |dE| < tol_energy and the density change < tol_density (either
     criterion alone with the other tolerance set to inf): the largest rms
     change over the species, or with density_sum their sum, the reference's
-    measure (src/scf/MultiSCF.f90:350-425, 776-830)."""
+    measure (src/scf/MultiSCF.f90:350-425, 776-830).
+
+    sub_iterations (scheme_iterations; default one per species, scheme 3):
+    a species with more than one iterates on its own inside the global
+    iteration -- diagonalise, new density, its energy tr P (H + G/2 + J) with
+    the matrices so far, rebuild its two-particle matrix (the couplings stay
+    those of the global build) -- while its energy change or its density
+    change exceeds sub_tolerances (1e-8 / 1e-6 by default, CONTROL.f90:
+    1461-1464), up to that many times (MultiSCF.f90:350-425).  Not with DIIS,
+    which the drivers here run over all species at once.  sub_density_test
+    False continues the sub-iterations on the energy change alone."""
     if convergence not in ("diis", "damping", "none"):
         raise ValueError(f"unknown convergence method {convergence!r}")
+    if sub_iterations is not None and max(sub_iterations) > 1 and convergence == "diis":
+        raise ValueError("single-species sub-iterations need damping or no convergence method")
     sp = system.species
     ns = len(sp)
     H, X, S = [], [], []
@@ -520,15 +550,26 @@ def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthrea
     e_old = None
     converged = False
     it = 0
+    sub = list(sub_iterations) if sub_iterations is not None else [1] * ns
+
+    def build_G(i, Pi):
+        s = sp[i]
+        if s.n_particles > 1 and not g12:
+            return two_body_direct(s.basis, s.is_electron, Pi, s.exchange_factor, nthreads) * s.charge ** 2
+        if s.n_particles > 1 and (i, i) in system.interpotentials:
+            return g12_direct(s.basis, Pi, s.exchange_factor, *system.interpotentials[(i, i)], nthreads)
+        return np.zeros_like(H[i])
+
+    def diagonalise(i, Fi):
+        e, Cp = np.linalg.eigh(X[i].T @ Fi @ X[i])
+        Ci = X[i] @ Cp
+        C[i] = Ci; eps[i] = e
+        return sp[i].eta * Ci[:, :sp[i].n_occ] @ Ci[:, :sp[i].n_occ].T
+
     for it in range(1, max_iter + 1):
         G, J = [], []
         for i, s in enumerate(sp):
-            if s.n_particles > 1 and not g12:
-                G.append(two_body_direct(s.basis, s.is_electron, P[i], s.exchange_factor, nthreads) * s.charge ** 2)
-            elif s.n_particles > 1 and (i, i) in system.interpotentials:
-                G.append(g12_direct(s.basis, P[i], s.exchange_factor, *system.interpotentials[(i, i)], nthreads))
-            else:
-                G.append(np.zeros_like(H[i]))
+            G.append(build_G(i, P[i]))
             Ji = np.zeros_like(H[i])
             Jparts = {}
             for j, o in enumerate(sp):
@@ -552,6 +593,39 @@ def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthrea
             for j, B in J[i][1].items():
                 if j > i:
                     energy += np.sum(P[i] * B)
+        if kept is None and convergence == "damping":
+            kept = [(F[i].copy(), P[i].copy()) for i in range(ns)]
+        if max(sub) > 1:
+            newP, dmax = [], 0.0
+            for i in range(ns):
+                Fi, Gi, Pi, Ji = F[i], G[i], P[i], J[i][0]
+                e_i = float(np.sum(Pi * (H[i] + 0.5 * Gi + Ji)))
+                d_e, rms, k = 1e16, np.inf, 0
+                while (abs(d_e) > sub_tolerances[0] or (sub_density_test and rms > sub_tolerances[1])) \
+                        and k < sub[i]:
+                    k += 1
+                    Fd = Fi
+                    if convergence == "damping":
+                        Fd, F0, P0 = damping_step(Fi, Pi, *kept[i])
+                        kept[i] = (F0, P0)
+                    Pn = diagonalise(i, Fd)
+                    rms = float(np.sqrt(np.mean((Pn - Pi) ** 2)))
+                    Pi = Pn
+                    e_new = float(np.sum(Pi * (H[i] + 0.5 * Gi + Ji)))
+                    if sub[i] > 1:
+                        Gi = build_G(i, Pi)
+                        Fi = H[i] + Gi + Ji
+                        d_e, e_i = e_i - e_new, e_new
+                newP.append(Pi)
+                dmax = dmax + rms if density_sum else max(dmax, rms)
+            if verbose:
+                print(f"iter {it:3d}  E = {energy:.12f}  dP = {dmax:.2e}")
+            if e_old is not None and abs(energy - e_old) < tol_energy and dmax < tol_density:
+                converged = True
+                break
+            e_old = energy
+            P = newP
+            continue
         newP = []
         dmax = 0.0
         Fx = F
@@ -559,19 +633,13 @@ def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthrea
             errs = [X[i].T @ (F[i] @ P[i] @ S[i] - S[i] @ P[i] @ F[i]) @ X[i] for i in range(ns)]
             Fx = diis_obj(F, errs)
         elif convergence == "damping":
-            if kept is None:
-                kept = [(F[i].copy(), P[i].copy()) for i in range(ns)]
             Fx = []
             for i in range(ns):
                 Fd, F0, P0 = damping_step(F[i], P[i], *kept[i])
                 kept[i] = (F0, P0)
                 Fx.append(Fd)
         for i, s in enumerate(sp):
-            Fi = Fx[i]
-            e, Cp = np.linalg.eigh(X[i].T @ Fi @ X[i])
-            Ci = X[i] @ Cp
-            C[i] = Ci; eps[i] = e
-            Pn = s.eta * Ci[:, :s.n_occ] @ Ci[:, :s.n_occ].T
+            Pn = diagonalise(i, Fx[i])
             rms = float(np.sqrt(np.mean((Pn - P[i]) ** 2)))
             dmax = dmax + rms if density_sum else max(dmax, rms)
             newP.append(Pn)
