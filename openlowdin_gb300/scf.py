@@ -279,14 +279,45 @@ class HostSCF:
         for h in self.handles:
             h.set_precision(1 if on else 0, self.split)
 
-    def solve(self, tol_energy=1e-8, tol_density=1e-6, max_iter=100, density_sum=False) -> SCFResult:
+    def _full_G(self, i, Pi):
+        """FP64 two-particle (or G12) matrix of species i from density Pi."""
+        sp = self.species[i]
+        if sp["n_particles"] <= 1:
+            return np.zeros_like(self.H[i])
+        f = sp["kappa"] / sp["eta"]
+        if self.g12:
+            pot = self.g12.get((i, i))
+            return self.handles[i].compute_g12_direct(Pi, f, *pot) if pot else np.zeros_like(self.H[i])
+        return self.handles[i].compute_2body_direct(Pi, f) * sp["charge"] ** 2
+
+    def solve(self, tol_energy=1e-8, tol_density=1e-6, max_iter=100, density_sum=False, scheme=3,
+              sub_max=(50, 50), sub_tolerances=(1e-8, 1e-6), sub_density_test=True) -> SCFResult:
         """Converged when |dE| < tol_energy and the density change is below
         tol_density (either alone with the other tolerance set to inf): the
         largest rms change over the species, or with density_sum their sum,
-        the reference's measure (MultiSCF.f90:350-425, 776-830)."""
+        the reference's measure (MultiSCF.f90:350-425, 776-830).
+
+        scheme: the reference's iteration scheme (MultiSCF.f90:150-185): 3 =
+        every species once per global iteration; 0 / 1 / 2 = the
+        non-electronic species / the electrons / every species iterate on
+        their own inside a global iteration, up to sub_max = (electronic,
+        non-electronic) times, while their energy tr P (H + G/2 + J) changes
+        by more than sub_tolerances[0] or (sub_density_test) their density by
+        more than sub_tolerances[1]; each such step rebuilds the species'
+        two-particle matrix, the couplings stay those of the global build.
+        Schemes 0-2 need convergence "damping" and FP64."""
+        if scheme not in (0, 1, 2, 3):
+            raise ValueError(f"iteration scheme must be 0-3, not {scheme!r}")
+        if scheme != 3 and (self.convergence != "damping" or self.precision != "fp64"):
+            raise ValueError("iteration schemes 0-2 run with convergence 'damping' in FP64")
         t0 = time.perf_counter()
         sp, H, S, X = self.species, self.H, self.S, self.X
         ns = len(sp)
+        sub = []
+        for s_ in sp:
+            el = s_["is_electron"]
+            sub.append({0: 1 if el else sub_max[1], 1: sub_max[0] if el else 1,
+                        2: sub_max[0] if el else sub_max[1], 3: 1}[scheme])
         mixed = self.precision == "mixed"
         fp64 = not mixed          # builds in FP64 (plain, the FP64 check, after a failed check)
         checking = False          # this iteration's build is the FP64 check
@@ -361,26 +392,51 @@ class HostSCF:
                     break
                 guard_hit = True                  # continue in FP64 from this Fock build
                 diis, e_old, kept = _DIIS(np), None, None
-            if self.convergence == "diis":
-                Fx = diis(F, errs)
-            else:
-                if kept is None:
-                    kept = [(F[i].copy(), P[i].copy()) for i in range(ns)]
-                Fx = []
-                for i in range(ns):
-                    Fd, kept[i] = damped_fock(F[i], P[i], kept[i])
-                    Fx.append(Fd)
-            dmax = 0.0
-            newP = []
-            for i in range(ns):
-                e, Cp = np.linalg.eigh(X[i].T @ Fx[i] @ X[i])
+            def density(i, Fi):
+                e, Cp = np.linalg.eigh(X[i].T @ Fi @ X[i])
                 Ci = X[i] @ Cp
                 C[i], eps[i] = Ci, e
                 o = n_occ(sp[i])
-                Pn = sp[i]["eta"] * Ci[:, :o] @ Ci[:, :o].T
-                rms = float(np.sqrt(np.mean((Pn - P[i]) ** 2)))
-                dmax = dmax + rms if density_sum else max(dmax, rms)
-                newP.append(Pn)
+                return sp[i]["eta"] * Ci[:, :o] @ Ci[:, :o].T
+
+            if self.convergence == "damping" and kept is None:
+                kept = [(F[i].copy(), P[i].copy()) for i in range(ns)]
+            dmax = 0.0
+            newP = []
+            if max(sub) > 1:
+                # nested scheme: each species in turn, on its own
+                for i in range(ns):
+                    Ji = sum(J[i][j] for j in range(ns) if j != i)
+                    Fi, Gi, Pi = F[i], G[i], P[i]
+                    e_i = float(np.sum(Pi * (H[i] + 0.5 * Gi + Ji)))
+                    d_e, rms, k = 1e16, math.inf, 0
+                    while (abs(d_e) > sub_tolerances[0] or (sub_density_test and rms > sub_tolerances[1])) \
+                            and k < sub[i]:
+                        k += 1
+                        Fd, kept[i] = damped_fock(Fi, Pi, kept[i])
+                        Pn = density(i, Fd)
+                        rms = float(np.sqrt(np.mean((Pn - Pi) ** 2)))
+                        Pi = Pn
+                        e_new = float(np.sum(Pi * (H[i] + 0.5 * Gi + Ji)))
+                        if sub[i] > 1:
+                            Gi = self._full_G(i, Pi)
+                            Fi = H[i] + Gi + Ji
+                            d_e, e_i = e_i - e_new, e_new
+                    newP.append(Pi)
+                    dmax = dmax + rms if density_sum else max(dmax, rms)
+            else:
+                if self.convergence == "diis":
+                    Fx = diis(F, errs)
+                else:
+                    Fx = []
+                    for i in range(ns):
+                        Fd, kept[i] = damped_fock(F[i], P[i], kept[i])
+                        Fx.append(Fd)
+                for i in range(ns):
+                    Pn = density(i, Fx[i])
+                    rms = float(np.sqrt(np.mean((Pn - P[i]) ** 2)))
+                    dmax = dmax + rms if density_sum else max(dmax, rms)
+                    newP.append(Pn)
             if e_old is not None and abs(energy - e_old) < tol_energy and dmax < tol_density:
                 if not fp64:
                     # FP64 check: a full FP64 build at this iteration's density

@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 from tests import golden_systems as GS
-from tests.test_oracle import DAMPING_CASES
+from tests.test_oracle import DAMPING_CASES, SCHEME_CASES
 
 
 @pytest.fixture
@@ -55,6 +55,18 @@ def test_damping_stops_where_the_reference_did(scf, golden, case):
     ref = golden["values"][test]
     assert r.converged and abs(r.energy - ref["HF energy"][0]) < 1e-9
     assert abs(r.iterations - ref["Iterations"][0]) <= 5
+
+
+@pytest.mark.parametrize("case", SCHEME_CASES[:3], ids=[c[1] for c in SCHEME_CASES[:3]])
+def test_nested_schemes_stop_where_the_reference_did(scf, golden, case):
+    build, test, scheme, emax, nmax, te, td = case
+    s = scf.HostSCF(getattr(GS, build)(golden), convergence="damping")
+    r = s.solve(tol_energy=te, tol_density=td, max_iter=3000, density_sum=True, scheme=scheme,
+                sub_max=(emax, nmax), sub_density_test=False)
+    s.close()
+    ref = golden["values"][test]
+    assert r.converged and abs(r.energy - ref["HF energy"][0]) <= ref["HF energy"][1]
+    assert abs(r.iterations - ref["Iterations"][0]) <= 2, r.iterations
 
 
 @pytest.mark.parametrize("test", ["TIP4P-dimer-singlet-direct", "He.POTENTIALS", "He3-C60potential-NOCI"])
@@ -111,6 +123,8 @@ def test_invalid_requests_raise(scf, golden):
         scf.HostSCF(tip4p, precision="mixed")
     with pytest.raises(ValueError, match="convergence"):
         scf.HostSCF(GS.h2o_boa(golden), convergence="levelshift")
+    with pytest.raises(ValueError, match="schemes 0-2"):
+        scf.HostSCF(GS.h2o_boa(golden)).solve(scheme=0)
     from openlowdin_gb300.batch_scf import BatchSCF
     with pytest.raises(ValueError, match="HostSCF only"):
         BatchSCF([tip4p])
