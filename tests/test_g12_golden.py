@@ -166,3 +166,25 @@ def test_library_c60_cage_potential(built, oracle, golden):
         got = h.gaussian_potential(e["coefficients"], e["exponents"], e["origins"])
         assert np.max(np.abs(got - ref)) < 1e-12 * max(1.0, np.max(np.abs(ref)))
         h.close()
+
+
+def test_library_gaussian_potential_random_cases(built, oracle):
+    """Random contracted shells up to f on random centres and random
+    off-centre components: the library's recursion against the oracle's
+    quadrature, relative 1e-11."""
+    rng = np.random.default_rng(11)
+    for case in range(6):
+        sh = []
+        for _ in range(int(rng.integers(2, 6))):
+            l = int(rng.integers(0, 4))
+            k = int(rng.integers(1, 4))
+            sh.append((l, list(rng.uniform(0.2, 6.0, k)), list(rng.uniform(0.1, 1.0, k)),
+                       list(rng.uniform(-1.5, 1.5, 3))))
+        m = int(rng.integers(1, 8))
+        coef, expo = rng.normal(size=m), rng.uniform(0.0, 4.0, m)
+        origins = rng.uniform(-2.0, 2.0, (m, 3))
+        h = built.Libint2Interface(S.electron_species(sh, 2), 1)
+        ref = oracle.gaussian_potential(oracle.Basis.from_shells(sh), coef, expo, origins)
+        got = h.gaussian_potential(coef, expo, origins)
+        assert np.max(np.abs(got - ref)) <= 1e-11 * max(1.0, np.max(np.abs(ref))), case
+        h.close()
