@@ -291,7 +291,7 @@ class HostSCF:
         return self.handles[i].compute_2body_direct(Pi, f) * sp["charge"] ** 2
 
     def solve(self, tol_energy=1e-8, tol_density=1e-6, max_iter=100, density_sum=False, scheme=3,
-              sub_max=(50, 50), sub_tolerances=(1e-8, 1e-6), sub_density_test=True) -> SCFResult:
+              sub_max=(50, 50), sub_tolerances=(1e-8, 1e-6)) -> SCFResult:
         """Converged when |dE| < tol_energy and the density change is below
         tol_density (either alone with the other tolerance set to inf): the
         largest rms change over the species, or with density_sum their sum,
@@ -302,10 +302,13 @@ class HostSCF:
         non-electronic species / the electrons / every species iterate on
         their own inside a global iteration, up to sub_max = (electronic,
         non-electronic) times, while their energy tr P (H + G/2 + J) changes
-        by more than sub_tolerances[0] or (sub_density_test) their density by
-        more than sub_tolerances[1]; each such step rebuilds the species'
-        two-particle matrix, the couplings stay those of the global build.
-        Schemes 0-2 need convergence "damping" and FP64."""
+        by more than sub_tolerances[0] or their density by more than
+        sub_tolerances[1]; each such step rebuilds the species' two-particle
+        matrix, the couplings stay those of the global build.  The
+        reference's criteria set the unused quantity's tolerances to 1.0
+        (CONTROL.f90:3174-3190): ENERGY gives (1e-8, 1.0), DENSITY (1.0,
+        1e-6), BOTH (1e-8, 1e-6).  Schemes 0-2 need convergence "damping"
+        and FP64."""
         if scheme not in (0, 1, 2, 3):
             raise ValueError(f"iteration scheme must be 0-3, not {scheme!r}")
         if scheme != 3 and (self.convergence != "damping" or self.precision != "fp64"):
@@ -410,8 +413,7 @@ class HostSCF:
                     Fi, Gi, Pi = F[i], G[i], P[i]
                     e_i = float(np.sum(Pi * (H[i] + 0.5 * Gi + Ji)))
                     d_e, rms, k = 1e16, math.inf, 0
-                    while (abs(d_e) > sub_tolerances[0] or (sub_density_test and rms > sub_tolerances[1])) \
-                            and k < sub[i]:
+                    while (abs(d_e) > sub_tolerances[0] or rms > sub_tolerances[1]) and k < sub[i]:
                         k += 1
                         Fd, kept[i] = damped_fock(Fi, Pi, kept[i])
                         Pn = density(i, Fd)

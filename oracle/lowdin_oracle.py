@@ -480,6 +480,24 @@ def damping_step(F, P, F0, P0):
     return F0.copy(), F0, P0 + lam * (P - P0)
 
 
+def reference_tolerances(criterion="ENERGY", total_energy=1e-8, total_density=1e-6, species_energy=1e-8,
+                         species_density=1e-6) -> dict:
+    """tol_energy, tol_density and sub_tolerances of scf() for the reference's
+    scfConvergenceCriterium: the global test uses the chosen quantities
+    (src/scf/MultiSCF.f90:813-830), and the reference switches the other
+    quantity's tolerances off by setting them, per species and total, to 1.0
+    (src/core/CONTROL.f90:3174-3190), which the single-species loops see."""
+    c = criterion.upper()
+    if c == "ENERGY":
+        return {"tol_energy": total_energy, "tol_density": float("inf"), "sub_tolerances": (species_energy, 1.0)}
+    if c == "DENSITY":
+        return {"tol_energy": float("inf"), "tol_density": total_density, "sub_tolerances": (1.0, species_density)}
+    if c == "BOTH":
+        return {"tol_energy": total_energy, "tol_density": total_density,
+                "sub_tolerances": (species_energy, species_density)}
+    raise ValueError(f"unknown convergence criterion {criterion!r}")
+
+
 def scheme_iterations(system: System, scheme: int, electronic_max=50, nonelectronic_max=50) -> list:
     """Single-species sub-iterations per global iteration of the reference's
     iteration schemes (src/scf/MultiSCF.f90:150-185): 0 = non-electronic
@@ -496,7 +514,7 @@ def scheme_iterations(system: System, scheme: int, electronic_max=50, nonelectro
 
 def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthreads=None,
         convergence="diis", density_sum=False, sub_iterations=None, sub_tolerances=(1e-8, 1e-6),
-        sub_density_test=True, verbose=False) -> SCFResult:
+        verbose=False) -> SCFResult:
     """Multi-species Hartree-Fock restated from src/scf: every global
     iteration builds every species' two-particle and coupling matrices, Fock
     matrix and the total energy from the current densities, then updates the
@@ -516,9 +534,9 @@ def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthrea
     the matrices so far, rebuild its two-particle matrix (the couplings stay
     those of the global build) -- while its energy change or its density
     change exceeds sub_tolerances (1e-8 / 1e-6 by default, CONTROL.f90:
-    1461-1464), up to that many times (MultiSCF.f90:350-425).  Not with DIIS,
-    which the drivers here run over all species at once.  sub_density_test
-    False continues the sub-iterations on the energy change alone."""
+    1461-1464; reference_tolerances gives the values the reference's
+    criteria leave), up to that many times (MultiSCF.f90:350-425).  Not
+    with DIIS, which the drivers here run over all species at once."""
     if convergence not in ("diis", "damping", "none"):
         raise ValueError(f"unknown convergence method {convergence!r}")
     if sub_iterations is not None and max(sub_iterations) > 1 and convergence == "diis":
@@ -601,8 +619,7 @@ def scf(system: System, tol_energy=1e-10, tol_density=1e-8, max_iter=200, nthrea
                 Fi, Gi, Pi, Ji = F[i], G[i], P[i], J[i][0]
                 e_i = float(np.sum(Pi * (H[i] + 0.5 * Gi + Ji)))
                 d_e, rms, k = 1e16, np.inf, 0
-                while (abs(d_e) > sub_tolerances[0] or (sub_density_test and rms > sub_tolerances[1])) \
-                        and k < sub[i]:
+                while (abs(d_e) > sub_tolerances[0] or rms > sub_tolerances[1]) and k < sub[i]:
                     k += 1
                     Fd = Fi
                     if convergence == "damping":

@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 from tests import golden_systems as GS
-from tests.test_oracle import DAMPING_CASES, SCHEME_CASES
+from tests.test_oracle import DAMPING_CASES, SCHEME_CASES, scheme_tolerances
 
 
 @pytest.fixture
@@ -57,12 +57,12 @@ def test_damping_stops_where_the_reference_did(scf, golden, case):
     assert abs(r.iterations - ref["Iterations"][0]) <= 5
 
 
-@pytest.mark.parametrize("case", SCHEME_CASES[:3], ids=[c[1] for c in SCHEME_CASES[:3]])
-def test_nested_schemes_stop_where_the_reference_did(scf, golden, case):
-    build, test, scheme, emax, nmax, te, td = case
+@pytest.mark.parametrize("case", SCHEME_CASES, ids=[c[1] for c in SCHEME_CASES])
+def test_nested_schemes_stop_where_the_reference_did(scf, oracle, golden, case):
+    build, test, scheme, emax, nmax, criterion, total = case
     s = scf.HostSCF(getattr(GS, build)(golden), convergence="damping")
-    r = s.solve(tol_energy=te, tol_density=td, max_iter=3000, density_sum=True, scheme=scheme,
-                sub_max=(emax, nmax), sub_density_test=False)
+    r = s.solve(max_iter=3000, density_sum=True, scheme=scheme, sub_max=(emax, nmax),
+                **scheme_tolerances(oracle, criterion, total))
     s.close()
     ref = golden["values"][test]
     assert r.converged and abs(r.energy - ref["HF energy"][0]) <= ref["HF energy"][1]

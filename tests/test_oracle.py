@@ -358,32 +358,36 @@ def test_golden_multi_proton_species_damping(oracle, golden, case):
 
 
 # the reference's nested schemes (0: non-electronic species iterate inside a
-# global iteration, 2: every species does): (builder, test, scheme, electronic
-# and non-electronic sub-iteration limits, tol_energy, tol_density)
-SCHEME_CASES = [("h2o_apmo_two_protons", "H2O.APMO.iter0", 0, 50, 25, 1e-10, float("inf")),
-                ("h2o_apmo_two_protons", "H2O.APMO.iter2", 2, 5, 15, 1e-10, float("inf")),
-                ("nh3_apmo_three_protons", "NH3.APMO.convEne", 0, 50, 50, 1e-9, float("inf")),
-                ("nh3_apmo_three_protons", "NH3.APMO.convDens", 2, 50, 50, float("inf"), 5e-7)]
+# global iteration, 2: every species does) with each input's own controls:
+# (builder, test, scheme, electronic and non-electronic sub-iteration limits,
+# scfConvergenceCriterium, its total tolerance)
+SCHEME_CASES = [("h2o_apmo_two_protons", "H2O.APMO.iter0", 0, 50, 25, "ENERGY", 1e-10),
+                ("h2o_apmo_two_protons", "H2O.APMO.iter2", 2, 5, 15, "ENERGY", 1e-10),
+                ("nh3_apmo_three_protons", "NH3.APMO.convEne", 0, 50, 50, "ENERGY", 1e-9),
+                ("nh3_apmo_three_protons", "NH3.APMO.convDens", 2, 50, 50, "DENSITY", 5e-7)]
+
+
+def scheme_tolerances(oracle, criterion, total):
+    if criterion == "ENERGY":
+        return oracle.reference_tolerances(criterion, total_energy=total)
+    return oracle.reference_tolerances(criterion, total_density=total)
 
 
 @pytest.mark.parametrize("case", SCHEME_CASES, ids=[c[1] for c in SCHEME_CASES])
 def test_golden_nested_iteration_schemes(oracle, golden, case):
     """Iteration schemes 0 and 2 with the reference's damping and each input's
-    own rules: the energy within the checker's 1e-8 and the global iteration
-    count within its tolerance.  With the single-species loop continuing on
-    its energy change alone, the counts of iter0, iter2 and convEne are the
-    recorded ones exactly (213, 230, 187); convDens gives 209 (recorded 178,
-    checker 40)."""
-    build, test, scheme, emax, nmax, te, td = case
+    own rules (its criterion switching the other quantity's tolerances off,
+    as the reference does): the energy within 1e-9 of the checker's and the
+    global iteration count the recorded one (213, 230, 187, 178)."""
+    build, test, scheme, emax, nmax, criterion, total = case
     sy = oracle.from_plain(getattr(GS, build)(golden))
-    res = oracle.scf(sy, convergence="damping", tol_energy=te, tol_density=td, density_sum=True, max_iter=3000,
-                     sub_iterations=oracle.scheme_iterations(sy, scheme, emax, nmax), sub_density_test=False)
+    res = oracle.scf(sy, convergence="damping", density_sum=True, max_iter=3000,
+                     sub_iterations=oracle.scheme_iterations(sy, scheme, emax, nmax),
+                     **scheme_tolerances(oracle, criterion, total))
     ref = golden["values"][test]
     assert res.converged
-    assert abs(res.energy - ref["HF energy"][0]) <= ref["HF energy"][1], res.energy
-    assert abs(res.iterations - ref["Iterations"][0]) <= ref["Iterations"][1], res.iterations
-    if test != "NH3.APMO.convDens":
-        assert abs(res.iterations - ref["Iterations"][0]) <= 2, res.iterations
+    assert abs(res.energy - ref["HF energy"][0]) < 1e-9, res.energy
+    assert abs(res.iterations - ref["Iterations"][0]) <= 2, res.iterations
 
 
 def test_diis_ends_elsewhere_on_the_two_proton_species(oracle, golden):
