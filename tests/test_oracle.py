@@ -288,6 +288,18 @@ def test_golden_h2o_boa_ump2(oracle, golden):
     assert abs(oracle.apmo_mp2(sysO, res)["total"] - ref[0]) <= ref[1]
 
 
+def test_golden_hoo_under_the_reference_default_rule(oracle, golden):
+    """test/HOO+.ROCI-HF sets no energy tolerance; under the reference's
+    defaults (damping, scheme 3, criterion ENERGY at 1e-8, CONTROL.f90) the
+    triplet stops within the checker's 1e-8 of the recorded energy, which the
+    fully converged solve undercuts by 2.3e-8."""
+    sysd = GS.uhf_system(golden, "HOO+.ROCI-HF", "CC-PVDZ", "DZSPNB")
+    res = oracle.scf(oracle.from_plain(sysd), convergence="damping", density_sum=True, max_iter=3000,
+                     **oracle.reference_tolerances("ENERGY"))
+    ref = golden["values"]["HOO+.ROCI-HF"]["HF energy"]
+    assert res.converged and abs(res.energy - ref[0]) <= ref[1], res.energy
+
+
 def test_golden_h2o_apmo_uhf(oracle, golden):
     """test/H2O.APMO.UHF.DIRECT: -75.93125555356 within 1e-8 as a UHF solve."""
     res = oracle.scf(oracle.from_plain(GS.h2o_apmo_uhf(golden)), tol_energy=1e-11, tol_density=1e-9)
