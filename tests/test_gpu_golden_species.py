@@ -8,7 +8,7 @@ against the checkers' HF values (1e-8 Eh) and against the oracle."""
 import pytest
 
 from tests import golden_systems as GS
-from tests.test_oracle import DAMPING_CASES
+from tests.test_oracle import DAMPING_CASES, SCHEME_CASES, scheme_tolerances
 
 pytestmark = pytest.mark.gpu
 
@@ -60,3 +60,20 @@ def test_he_fitted_potentials(scf, oracle, golden):
     assert r.converged and abs(r.energy - ref[0]) <= ref[1], r.energy
     res = oracle.scf(oracle.from_plain(sysd), tol_energy=1e-11, tol_density=1e-9)
     assert abs(r.energy - res.energy) < 1e-10
+
+
+@pytest.mark.parametrize("case", SCHEME_CASES, ids=[c[1] for c in SCHEME_CASES])
+def test_nested_iteration_schemes(scf, oracle, golden, case):
+    """The reference's iteration schemes 0 and 2 (species iterating on their
+    own inside a global iteration, damping, each input's criterion) through
+    the library: the checkers' energies (1e-8) and iteration counts (their
+    tolerances)."""
+    build, test, scheme, emax, nmax, criterion, total = case
+    s = scf.HostSCF(getattr(GS, build)(golden), convergence="damping")
+    r = s.solve(max_iter=3000, density_sum=True, scheme=scheme, sub_max=(emax, nmax),
+                **scheme_tolerances(oracle, criterion, total))
+    s.close()
+    ref = golden["values"][test]
+    assert r.converged
+    assert abs(r.energy - ref["HF energy"][0]) <= ref["HF energy"][1], r.energy
+    assert abs(r.iterations - ref["Iterations"][0]) <= ref["Iterations"][1], r.iterations
